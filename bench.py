@@ -1,0 +1,342 @@
+"""Benchmark: Hex8 continuity (pressure-Poisson) CVFEM assembly on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Workload (one "step"): zeroSystem + ContinuityAdvElemKernel assembly + sumInto
+of a 128^3 Hex8 mesh (2,097,152 elements, 2,146,689 nodes, 57,066,625 CRS
+non-zeros) with z-stretching ratio 1.05, density 1, pressure 0, dpdx 0 and a
+seeded 64-mode random-Fourier velocity (|k| in [1,16], amplitude ~ k^-5/3).
+The CRS values (456 MB) and node inputs exceed the 129 MB L2, so no flush
+is needed between steps.  Inputs are synthetic (no dataset exists for this
+path).  Printed metric: elements assembled per second (whole job).
+
+--impl reference times the reference's CPU algorithm (the oracle restatement
+of ContinuityAdvElemKernel + HexSCS + TpetraLinearSystem::sumInto, run on all
+host cores) on the same workload and prints the same JSON line.
+Multi-GPU: replicas only (one independent mesh per rank, no collective on
+the data path); value = elements of all ranks / max-over-ranks time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Hex8 elems assembled/s; P-Poisson solve ms to 1e-8 rel-res, learned vs plain"
+UNIT = "elements/s"
+N_EDGE = 128
+
+
+def workload_config():
+    return {"workload": "continuity_adv_hex8_%d^3_zstretch1.05_fourier64" % N_EDGE, "elements": N_EDGE ** 3,
+            "nodes": (N_EDGE + 1) ** 3, "nnz": (3 * N_EDGE + 1) ** 3, "kernel": "ContinuityAdvElemKernel",
+            "l2": "inputs and CRS values larger than L2 (no flush)"}
+
+
+def algorithmic_bytes(n_nodes, n_elems, nnz, n_rows):
+    # node inputs (x 24, u 24, rho 8, p 8, Gp 24) + conn 32/elem + CRS values + rhs, counted once
+    return 88 * n_nodes + 32 * n_elems + 8 * nnz + 8 * n_rows
+
+
+def make_inputs():
+    from nalu_gb300.meshgen import block_mesh, fourier_velocity
+    c, conn, gid = block_mesh(N_EDGE, z_ratio=1.05)
+    u = fourier_velocity(c, n_modes=64, kmin=1, kmax=16, seed=2024)
+    n = c.shape[0]
+    return c, conn, gid, u, np.ones(n), np.zeros(n), np.zeros((n, 3))
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self._p = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self._p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                        "--format=csv,noheader,nounits", "-lms", "100"],
+                                       stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except Exception:
+            self._p = None
+        return self
+
+    def _read(self):
+        for line in self._p.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+
+    def __exit__(self, *a):
+        if self._p:
+            time.sleep(0.25)
+            self._p.terminate()
+            try:
+                self._p.wait(timeout=5)
+            except Exception:
+                self._p.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4) if s[3 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per assembly launch from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "continuity_assembly_128.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("dram_bytes_per_launch"), d
+    return None, None
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        return ws, rank, local, dist
+    return 1, 0, 0, None
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def run_cpu_sample(O, c, conn, gid, u, rho, p, gp, n_elems_sample, n_threads):
+    """Oracle assembly of the first n_elems_sample elements (all nodes)."""
+    rp, ci, lid = O.graph(c.shape[0], conn, 1, gid)
+    sub = np.ascontiguousarray(conn[:n_elems_sample])
+    t0 = time.perf_counter()
+    O.assemble(O.KERNEL_CONTINUITY_ADV, c, sub, rp, ci, lid, scalar=p, coeff=rho, vec=u, vec2=gp,
+               n_threads=n_threads)
+    dt = time.perf_counter() - t0
+    return n_elems_sample / dt, dt
+
+
+def bench_reference(args):
+    ws, rank, local, dist = dist_init()
+    if rank != 0:
+        return 0
+    from oracle import oracle as O
+    if not os.path.exists(os.path.join(ROOT, "oracle", "liboracle.so")):
+        subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "liboracle.so"], check=True)
+    c, conn, gid, u, rho, p, gp = make_inputs()
+    nt = cpu_threads()
+    sample = 1 << 20  # half the mesh per step keeps the run within minutes
+    for _ in range(args.warmup):
+        run_cpu_sample(O, c, conn, gid, u, rho, p, gp, 1 << 16, nt)
+    rates = []
+    t_all = time.perf_counter()
+    for _ in range(args.steps):
+        r, _ = run_cpu_sample(O, c, conn, gid, u, rho, p, gp, sample, nt)
+        rates.append(r)
+    wall = time.perf_counter() - t_all
+    value = statistics.median(rates)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * wall / max(args.steps, 1), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": workload_config(),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": nt, "kind": "port",
+                             "sample": "first %d elements of the 128^3 mesh per step, colour-parallel oracle "
+                                       "(restated ContinuityAdvElemKernel + HexSCS + sumInto)" % sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def bench_gpu(args):
+    ws, rank, local, dist = dist_init()
+    import nalu_gb300 as ng
+    c, conn, gid, u, rho, p, gp = make_inputs()
+    n_nodes, n_elems = c.shape[0], conn.shape[0]
+    ctx = ng.Context(local)
+    ctx.mesh_create(c, conn, gid)
+    for nm, v in (("velocity", u), ("density", rho), ("pressure", p), ("dpdx", gp)):
+        ctx.field_set(nm, v)
+    ctx.build_elem_graph(1)
+    n_rows, nnz, _ = ctx.sizes()
+    opts = ng.default_assemble_opts(scatter=ng.SCATTER_AUTO)
+    # warm-up (includes the scatter autotune on the first call)
+    for _ in range(max(args.warmup, 3)):
+        ctx.zero()
+        ctx.assemble(ng.KERNEL_CONTINUITY_ADV, opts)
+    ctx.load_complete()
+    scatter = int(ctx_scatter_choice(ctx))
+    fp64_peak = ctx.probe_fp64_tflops()
+    # ---- device-timed region: inputs resident in HBM ----
+    launches0 = ctx.launches()
+    asm_ms = []
+    barrier(dist)
+    ctx.synchronize()
+    with ClockSampler(local) as clk:
+        ctx.event_record(0)
+        for s in range(args.steps):
+            ctx.zero()
+            ctx.event_record(2 + 2 * (s % 30))
+            ctx.assemble(ng.KERNEL_CONTINUITY_ADV, opts)
+            ctx.event_record(3 + 2 * (s % 30))
+            if s % 30 == 29:  # event slots are reused every 30 steps
+                asm_ms += [ctx.event_elapsed_ms(2 + 2 * k, 3 + 2 * k) for k in range(30)]
+        ctx.event_record(1)
+        ctx.synchronize()
+    total_ms = ctx.event_elapsed_ms(0, 1)
+    asm_ms += [ctx.event_elapsed_ms(2 + 2 * k, 3 + 2 * k) for k in range(args.steps % 30)]
+    launches = ctx.launches() - launches0
+    ctx.load_complete()
+    barrier(dist)
+    total_ms = max_over_ranks(dist, total_ms)
+    value = ws * n_elems * args.steps / (total_ms * 1e-3)
+    # ---- end-to-end through the C ABI with pinned host buffers ----
+    pin_in = {nm: ng.PinnedArray(v.shape) for nm, v in (("coordinates", c), ("velocity", u), ("density", rho),
+                                                         ("pressure", p), ("dpdx", gp))}
+    for nm, v in (("coordinates", c), ("velocity", u), ("density", rho), ("pressure", p), ("dpdx", gp)):
+        pin_in[nm].array[...] = v
+    out_v, out_r = ng.PinnedArray((nnz,)), ng.PinnedArray((n_rows,))
+    h2d = sum(a.array.nbytes for a in pin_in.values())
+    d2h = out_v.array.nbytes + out_r.array.nbytes
+
+    def e2e_step():
+        for nm, a in pin_in.items():
+            ctx.field_set_ptr(nm, a.ptr, a.array.size)
+        ctx.zero()
+        ctx.assemble(ng.KERNEL_CONTINUITY_ADV, opts)
+        ctx.system_to_ptr(out_v.ptr, out_r.ptr)
+
+    e2e_step()
+    barrier(dist)
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    ctx.synchronize()
+    e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
+    e2e_value = ws * n_elems * args.steps / e2e_s
+    # ---- plain PCG solve of the same continuity system (pressure pinned at node 0) ----
+    solve = None
+    if not args.no_solve:
+        ctx.zero()
+        ctx.assemble(ng.KERNEL_CONTINUITY_ADV, opts)
+        ctx.reset_rows([0])
+        ctx.sum_into_diag(0, 0, 1.0, 0.0)
+        ctx.load_complete()
+        info = ctx.solve(ng.default_solver_opts(tol=1e-8, max_iters=20000, check_every=50), raise_on_error=False)
+        solve = {"method": "Jacobi-PCG (FP64)", "ms": 1e3 * info.seconds, "iterations": info.iterations,
+                 "true_rel_res": info.true_rel_res, "status": info.status, "learned": "not built"}
+    # ---- CPU baseline on rank 0 (oracle, bounded sample) ----
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        from oracle import oracle as O
+        if not os.path.exists(os.path.join(ROOT, "oracle", "liboracle.so")):
+            subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "liboracle.so"], check=True)
+        sample = 1 << 18
+        r, dt = run_cpu_sample(O, c, conn, gid, u, rho, p, gp, sample, 1)
+        cpu = {"value": r, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": "first %d elements of the same 128^3 workload, serial element order (%.1f s)" % (sample, dt)}
+    # ---- roofline of the dominant kernel ----
+    peak, peak_kind = peaks()
+    alg = algorithmic_bytes(n_nodes, n_elems, nnz, n_rows)
+    avg_ms = statistics.mean(asm_ms)
+    achieved = alg / (avg_ms * 1e-3) / 1e9
+    traffic, prof = profile_traffic()
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": dict(workload_config(), scatter={1: "atomic", 2: "coloured"}.get(scatter, str(scatter)),
+                           parallelism="replicas" if ws > 1 else "single"),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": traffic, "peak_kind": peak_kind, "algorithmic_bytes_per_launch": alg,
+                         "kernel_ms": avg_ms, "fp64_probe_tflops": fp64_peak},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches, "clocks": clk.summary(), "cpu_baseline": cpu, "solve": solve}
+    for a in list(pin_in.values()) + [out_v, out_r]:
+        a.free()
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def ctx_scatter_choice(ctx):
+    """Which scatter the autotuner picked (times both once more to report it)."""
+    import nalu_gb300 as ng
+    best, pick = None, ng.SCATTER_ATOMIC
+    for s in (ng.SCATTER_ATOMIC, ng.SCATTER_COLOURED):
+        ctx.zero()
+        ctx.event_record(62)
+        ctx.assemble(ng.KERNEL_CONTINUITY_ADV, ng.default_assemble_opts(scatter=s))
+        ctx.event_record(63)
+        ms = ctx.event_elapsed_ms(62, 63)
+        if best is None or ms < best:
+            best, pick = ms, s
+    return pick
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-solve", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return bench_reference(args)
+    return bench_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

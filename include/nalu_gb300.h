@@ -1,0 +1,214 @@
+/*
+ * nalu_gb300.h -- C ABI of the GB300 (sm_103a) Hex8 CVFEM assembly and
+ * continuity-solve library.
+ *
+ * One opaque context = one CUDA device + one CUDA stream + one Hex8 mesh +
+ * its nodal/element fields + one linear system (CRS matrix, rhs, solution).
+ * Every function returns an int status (NALU_OK = 0, negative on error); no
+ * C++ exception crosses this boundary.  nalu_last_error() gives the message
+ * of the last failure on a context.  All pointers are plain host pointers
+ * unless a function says "device".  Node arrays are in the caller's node
+ * order; matrix rows/columns follow the reference's Tpetra numbering (nodes
+ * ordered by global id, numDof consecutive dofs per node).
+ *
+ * Each entry point names the reference interface it replaces
+ * (file:line within NaluCFD/Nalu).
+ */
+#ifndef NALU_GB300_H
+#define NALU_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NALU_OK 0
+#define NALU_ERR_ARG (-1)          /* bad argument (null pointer, size, enum) */
+#define NALU_ERR_CUDA (-2)         /* CUDA runtime failure */
+#define NALU_ERR_STATE (-3)        /* call out of order (e.g. assemble before graph) */
+#define NALU_ERR_NEG_JACOBIAN (-4) /* an element has det(J) <= 0 at an integration point */
+#define NALU_ERR_NONFINITE (-5)    /* NaN/Inf in assembled values or solver scalars */
+#define NALU_ERR_CAPACITY (-6)     /* a graph row exceeds the supported length */
+#define NALU_ERR_NOT_CONVERGED (-7)/* solver hit max iterations */
+#define NALU_ERR_GRAPH (-8)        /* element entry not present in the CRS graph */
+#define NALU_ERR_NO_DEVICE (-9)    /* no usable CUDA device */
+
+typedef struct nalu_ctx nalu_ctx;
+
+/* ---- context ----------------------------------------------------------- */
+int nalu_create(int device, nalu_ctx** out);
+int nalu_destroy(nalu_ctx* ctx);
+const char* nalu_last_error(const nalu_ctx* ctx);
+const char* nalu_status_string(int status);
+/* the context's CUDA stream (cudaStream_t), for callers that overlap work */
+int nalu_get_stream(nalu_ctx* ctx, void** stream);
+int nalu_synchronize(nalu_ctx* ctx);
+
+/* ---- mesh (STK bulk data for one Hex8 block) ---------------------------
+ * conn: [n_elems][8] 0-based node indices in the reference's Hex8 node order
+ * (include/master_element/Hex8CVFEM.h); gid: node global ids (NULL => i+1),
+ * which fix the row order exactly as TpetraLinearSystem::
+ * beginLinearSystemConstruction does (src/TpetraLinearSystem.C:189-327);
+ * coords: [n_nodes][3]. */
+int nalu_mesh_create(nalu_ctx* ctx, int64_t n_nodes, int64_t n_elems, const int32_t* conn,
+                     const int64_t* gid, const double* coords);
+
+/* ---- fields (stk::mesh::field_data gathers, src/ScratchViews.C:408-483) -- */
+enum nalu_field {
+  NALU_FIELD_COORDINATES = 0,  /* [n][3] */
+  NALU_FIELD_SCALAR_Q = 1,     /* [n]    ScalarDiffElemKernel scalarQ */
+  NALU_FIELD_DIFF_COEFF = 2,   /* [n]    ScalarDiffElemKernel diffFluxCoeff */
+  NALU_FIELD_VELOCITY = 3,     /* [n][3] */
+  NALU_FIELD_VELOCITY_RTM = 4, /* [n][3] */
+  NALU_FIELD_DENSITY = 5,      /* [n]    */
+  NALU_FIELD_PRESSURE = 6,     /* [n]    */
+  NALU_FIELD_DPDX = 7,         /* [n][3] Gpdx */
+  NALU_FIELD_VISCOSITY = 8,    /* [n]    */
+  NALU_FIELD_DUDX = 9,         /* [n][3][3] Gju */
+  NALU_FIELD_MDOT_SCS = 10,    /* element field [E][12] mass_flow_rate_scs */
+  NALU_FIELD_COUNT = 11
+};
+/* copy a field in (host or device source, caller node order) */
+int nalu_field_set(nalu_ctx* ctx, int field, const double* src, int64_t count, int src_is_device);
+int nalu_field_get(nalu_ctx* ctx, int field, double* dst, int64_t count, int dst_is_device);
+
+/* ---- linear system (LinearSystem, include/LinearSystem.h:39-167) -------- */
+/* buildElemToNodeGraph + finalizeLinearSystem (src/TpetraLinearSystem.C:430-435,
+ * 1256-1353): CRS graph with rows = numDof x nodes (Tpetra row order) */
+int nalu_linsys_build_elem_graph(nalu_ctx* ctx, int num_dof);
+int nalu_linsys_sizes(nalu_ctx* ctx, int64_t* n_rows, int64_t* nnz, int* num_dof);
+/* copy the CRS graph out (rowptr [n_rows+1] as size_t-compatible int64, colind int32) */
+int nalu_linsys_graph(nalu_ctx* ctx, int64_t* rowptr, int32_t* colind);
+/* device pointers of the system arrays (valid until the next graph build) */
+int nalu_linsys_device_arrays(nalu_ctx* ctx, const int64_t** rowptr, const int32_t** colind,
+                              double** values, double** rhs, double** solution);
+/* zeroSystem (src/TpetraLinearSystem.C:1355-1373) */
+int nalu_linsys_zero(nalu_ctx* ctx);
+/* sumInto of whole element matrices (src/TpetraLinearSystem.C:1458-1522):
+ * additive; lhs [n][(8 numDof)^2] row-major, rhs [n][8 numDof] */
+int nalu_linsys_sum_into(nalu_ctx* ctx, int64_t n, const int64_t* elem_ids, const double* lhs,
+                         const double* rhs);
+/* applyDirichletBCs (src/TpetraLinearSystem.C:1579-1653): for node rows
+ * dofs [begin,end): row -> unit diagonal, rhs = bc - solution
+ * (bc, solution: [n_nodes_bc][numDof] in the order of node_idx) */
+int nalu_linsys_apply_dirichlet(nalu_ctx* ctx, int64_t n, const int32_t* node_idx, int begin_dof,
+                                int end_dof, const double* bc, const double* solution);
+/* resetRows (src/TpetraLinearSystem.C:1707-1755): rows and rhs -> 0 */
+int nalu_linsys_reset_rows(nalu_ctx* ctx, int64_t n, const int32_t* node_idx, int begin_dof,
+                           int end_dof);
+/* 1x1 sumInto on a diagonal (FixPressureAtNodeAlgorithm, src/FixPressureAtNodeAlgorithm.C:53-80) */
+int nalu_linsys_sum_into_diag(nalu_ctx* ctx, int32_t node_idx, int dof, double diag, double rhs);
+/* loadComplete (src/TpetraLinearSystem.C:1757-1778): one rank, no export */
+int nalu_linsys_load_complete(nalu_ctx* ctx);
+/* copy values [nnz] and rhs [n_rows] out (either may be NULL) */
+int nalu_linsys_copy(nalu_ctx* ctx, double* values, double* rhs, int dst_is_device);
+
+/* ---- assembly (AssembleElemSolverAlgorithm::execute + Kernel::execute) --- */
+enum nalu_kernel {
+  NALU_KERNEL_SCALAR_DIFF = 0,        /* src/kernel/ScalarDiffElemKernel.C */
+  NALU_KERNEL_CONTINUITY_ADV = 1,     /* src/kernel/ContinuityAdvElemKernel.C */
+  NALU_KERNEL_MOMENTUM_ADV_DIFF = 2,  /* src/kernel/MomentumAdvDiffElemKernel.C */
+  NALU_KERNEL_MOMENTUM_UPW_ADV_DIFF = 3 /* src/kernel/MomentumUpwAdvDiffElemKernel.C */
+};
+enum nalu_scatter {
+  NALU_SCATTER_AUTO = 0,    /* autotuned choice, cached per context */
+  NALU_SCATTER_ATOMIC = 1,  /* FP64 atomics into the CRS values */
+  NALU_SCATTER_COLOURED = 2 /* element colouring, plain read-modify-write (deterministic) */
+};
+/* solution options that change the kernels (src/SolutionOptions.C) and the
+ * time-integrator scale (ContinuityAdvElemKernel::setup, :79-84) */
+typedef struct nalu_assemble_opts {
+  int shifted_grad_op;      /* get_shifted_grad_op(dof) */
+  int shift_mdot;           /* cvfemShiftMdot_ */
+  int shift_poisson;        /* get_shifted_grad_op("pressure") */
+  int reduced_sens;         /* cvfemReducedSensPoisson_ */
+  int skew_symmetric;       /* get_skew_symmetric(dof) */
+  int use_limiter;          /* primitive_uses_limiter(dof) */
+  double proj_time_scale;   /* dt / gamma1 */
+  double include_divu;      /* includeDivU_ */
+  double alpha;             /* get_alpha_factor */
+  double alpha_upw;         /* get_alpha_upw_factor */
+  double upw_factor;        /* get_upw_factor */
+  double hybrid_factor;     /* get_hybrid_factor (classic Peclet function, A = 5) */
+  int scatter;              /* enum nalu_scatter */
+  int reserved[7];
+} nalu_assemble_opts;
+void nalu_assemble_opts_default(nalu_assemble_opts* opts);
+/* run one element kernel over all elements and sum into the system */
+int nalu_assemble(nalu_ctx* ctx, int kernel, const nalu_assemble_opts* opts);
+/* mock capture (unit_tests/UnitTestLinearSystem.h:39-55): element matrix and
+ * rhs of element `elem`, without touching the system */
+int nalu_capture_element(nalu_ctx* ctx, int kernel, const nalu_assemble_opts* opts, int64_t elem,
+                         double* lhs, double* rhs);
+/* ComputeMdotElemAlgorithm (src/ComputeMdotElemAlgorithm.C:85-250):
+ * fills NALU_FIELD_MDOT_SCS from density, velocity_rtm, pressure, dpdx */
+int nalu_compute_mdot(nalu_ctx* ctx, const nalu_assemble_opts* opts);
+
+/* ---- linear solve (TpetraLinearSolver::solve, src/LinearSolver.C:183-232) */
+enum nalu_solver_method {
+  NALU_SOLVER_CG = 0,       /* preconditioned CG */
+  NALU_SOLVER_GMRES = 1     /* right-preconditioned restarted GMRES(m) */
+};
+enum nalu_precond {
+  NALU_PRECOND_NONE = 0,
+  NALU_PRECOND_JACOBI = 1,    /* Ifpack2 RELAXATION Jacobi, one sweep */
+  NALU_PRECOND_CHEBYSHEV = 2  /* Chebyshev polynomial in D^-1 A */
+};
+enum nalu_precision {
+  NALU_PRECISION_FP64 = 0,          /* everything FP64 */
+  NALU_PRECISION_FP32_INNER_IR = 1  /* FP32 inner solver, FP64 iterative refinement */
+};
+typedef struct nalu_solver_opts {
+  int method;        /* enum nalu_solver_method */
+  int precond;       /* enum nalu_precond */
+  int precision;     /* enum nalu_precision */
+  int max_iters;
+  int restart;       /* GMRES kspace */
+  int cheb_degree;
+  int check_every;   /* residual checks every N iterations (host sync) */
+  int x0_zero;       /* 1: start from 0 (else from the current solution) */
+  double tol;        /* stop on true ||b - A x|| / ||b|| <= tol */
+  double inner_tol;  /* inner tolerance for iterative refinement */
+  int reserved[6];
+} nalu_solver_opts;
+typedef struct nalu_solve_info {
+  int iterations;        /* inner iterations in total */
+  int outer_iterations;  /* refinement steps (1 for plain FP64) */
+  int status;
+  double true_rel_res;   /* FP64 ||b - A x|| / ||b|| */
+  double seconds;
+} nalu_solve_info;
+void nalu_solver_opts_default(nalu_solver_opts* opts);
+/* solve A x = rhs into the context's solution vector */
+int nalu_solve(nalu_ctx* ctx, const nalu_solver_opts* opts, nalu_solve_info* info);
+/* copy the solution [n_rows] out */
+int nalu_solution_get(nalu_ctx* ctx, double* x, int dst_is_device);
+int nalu_solution_set(nalu_ctx* ctx, const double* x, int src_is_device);
+/* y = A x with the context's matrix (FP64), host or device vectors */
+int nalu_spmv(nalu_ctx* ctx, const double* x, double* y, int is_device);
+
+/* ---- measurement helpers ------------------------------------------------ */
+/* number of this library's kernel launches since the context was created */
+int64_t nalu_kernel_launch_count(const nalu_ctx* ctx);
+/* device time (ms) of the last nalu_assemble's scatter+compute kernels,
+ * measured with CUDA events on the context stream */
+double nalu_last_assemble_ms(const nalu_ctx* ctx);
+/* FP64 multiply-add throughput of this device, measured by a short kernel
+ * (TFLOP/s, 2 flops per FMA) */
+int nalu_probe_fp64_tflops(nalu_ctx* ctx, double* tflops);
+/* CUDA events on the context stream: record into slot 0..63, and the device
+ * time between two recorded slots (waits for the later one) */
+int nalu_event_record(nalu_ctx* ctx, int slot);
+int nalu_event_elapsed_ms(nalu_ctx* ctx, int slot_a, int slot_b, double* ms);
+/* page-locked host memory for H2D/D2H staging */
+int nalu_host_alloc(size_t bytes, void** ptr);
+int nalu_host_free(void* ptr);
+/* write `bytes` zeros through a scratch buffer larger than L2 (cache flush) */
+int nalu_flush_l2(nalu_ctx* ctx, size_t bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,351 @@
+"""nalu_gb300 -- GB300 (sm_103a) Hex8 CVFEM assembly and continuity solve.
+
+Python front end of the C ABI declared in ``include/nalu_gb300.h``.  The
+compute runs in ``nalu_gb300/_lib/libnalu_gb300.so`` (built in tree by
+``python -m nalu_gb300.build``); there is no CPU fallback: if the library or a
+CUDA device is missing, every call raises.
+
+The classes mirror the reference's host interface for this path:
+
+* ``Context``            -- one device/stream/mesh/linear system (C ``nalu_ctx``)
+* ``LinearSystem``       -- TpetraLinearSystem's graph/zero/sumInto/BC/solve API
+* ``AssembleElemSolverAlgorithm`` -- runs the registered element kernels
+* ``ScalarDiffElemKernel``, ``ContinuityAdvElemKernel``,
+  ``MomentumAdvDiffElemKernel``, ``MomentumUpwAdvDiffElemKernel``
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libnalu_gb300.so")
+CHECK_LIB_PATH = os.path.join(_HERE, "_lib", "libnalu_elemcheck.so")
+
+NALU_OK = 0
+STATUS = {0: "ok", -1: "invalid argument", -2: "CUDA error", -3: "call out of order",
+          -4: "negative Jacobian", -5: "non-finite value", -6: "capacity exceeded",
+          -7: "not converged", -8: "entry missing from graph", -9: "no CUDA device"}
+
+FIELD = {"coordinates": 0, "scalar_q": 1, "diff_coeff": 2, "velocity": 3, "velocity_rtm": 4,
+         "density": 5, "pressure": 6, "dpdx": 7, "viscosity": 8, "dudx": 9, "mass_flow_rate_scs": 10}
+KERNEL_SCALAR_DIFF = 0
+KERNEL_CONTINUITY_ADV = 1
+KERNEL_MOMENTUM_ADV_DIFF = 2
+KERNEL_MOMENTUM_UPW_ADV_DIFF = 3
+SCATTER_AUTO, SCATTER_ATOMIC, SCATTER_COLOURED = 0, 1, 2
+SOLVER_CG, SOLVER_GMRES = 0, 1
+PRECOND_NONE, PRECOND_JACOBI, PRECOND_CHEBYSHEV = 0, 1, 2
+PRECISION_FP64, PRECISION_FP32_INNER_IR = 0, 1
+
+
+class NaluError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s (%d): %s" % (STATUS.get(status, "error"), status, msg))
+        self.status = status
+
+
+class AssembleOpts(ctypes.Structure):
+    _fields_ = [("shifted_grad_op", ctypes.c_int), ("shift_mdot", ctypes.c_int), ("shift_poisson", ctypes.c_int),
+                ("reduced_sens", ctypes.c_int), ("skew_symmetric", ctypes.c_int), ("use_limiter", ctypes.c_int),
+                ("proj_time_scale", ctypes.c_double), ("include_divu", ctypes.c_double),
+                ("alpha", ctypes.c_double), ("alpha_upw", ctypes.c_double), ("upw_factor", ctypes.c_double),
+                ("hybrid_factor", ctypes.c_double), ("scatter", ctypes.c_int), ("reserved", ctypes.c_int * 7)]
+
+
+class SolverOpts(ctypes.Structure):
+    _fields_ = [("method", ctypes.c_int), ("precond", ctypes.c_int), ("precision", ctypes.c_int),
+                ("max_iters", ctypes.c_int), ("restart", ctypes.c_int), ("cheb_degree", ctypes.c_int),
+                ("check_every", ctypes.c_int), ("x0_zero", ctypes.c_int), ("tol", ctypes.c_double),
+                ("inner_tol", ctypes.c_double), ("reserved", ctypes.c_int * 6)]
+
+
+class SolveInfo(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int), ("outer_iterations", ctypes.c_int), ("status", ctypes.c_int),
+                ("true_rel_res", ctypes.c_double), ("seconds", ctypes.c_double)]
+
+
+_lib = None
+
+
+def lib():
+    """Load the CUDA library (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("nalu_gb300 CUDA library missing: %s (run python -m nalu_gb300.build)" % LIB_PATH)
+        L = ctypes.CDLL(LIB_PATH)
+        P, I, I64, D = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_double
+        sig = {
+            "nalu_create": (I, [I, ctypes.POINTER(P)]),
+            "nalu_destroy": (I, [P]),
+            "nalu_last_error": (ctypes.c_char_p, [P]),
+            "nalu_status_string": (ctypes.c_char_p, [I]),
+            "nalu_get_stream": (I, [P, ctypes.POINTER(P)]),
+            "nalu_synchronize": (I, [P]),
+            "nalu_mesh_create": (I, [P, I64, I64, P, P, P]),
+            "nalu_field_set": (I, [P, I, P, I64, I]),
+            "nalu_field_get": (I, [P, I, P, I64, I]),
+            "nalu_linsys_build_elem_graph": (I, [P, I]),
+            "nalu_linsys_sizes": (I, [P, P, P, P]),
+            "nalu_linsys_graph": (I, [P, P, P]),
+            "nalu_linsys_device_arrays": (I, [P, P, P, P, P, P]),
+            "nalu_linsys_zero": (I, [P]),
+            "nalu_linsys_sum_into": (I, [P, I64, P, P, P]),
+            "nalu_linsys_apply_dirichlet": (I, [P, I64, P, I, I, P, P]),
+            "nalu_linsys_reset_rows": (I, [P, I64, P, I, I]),
+            "nalu_linsys_sum_into_diag": (I, [P, ctypes.c_int32, I, D, D]),
+            "nalu_linsys_load_complete": (I, [P]),
+            "nalu_linsys_copy": (I, [P, P, P, I]),
+            "nalu_assemble_opts_default": (None, [P]),
+            "nalu_assemble": (I, [P, I, P]),
+            "nalu_capture_element": (I, [P, I, P, I64, P, P]),
+            "nalu_compute_mdot": (I, [P, P]),
+            "nalu_solver_opts_default": (None, [P]),
+            "nalu_solve": (I, [P, P, P]),
+            "nalu_solution_get": (I, [P, P, I]),
+            "nalu_solution_set": (I, [P, P, I]),
+            "nalu_spmv": (I, [P, P, P, I]),
+            "nalu_kernel_launch_count": (I64, [P]),
+            "nalu_last_assemble_ms": (D, [P]),
+            "nalu_probe_fp64_tflops": (I, [P, ctypes.POINTER(D)]),
+            "nalu_event_record": (I, [P, I]),
+            "nalu_event_elapsed_ms": (I, [P, I, I, ctypes.POINTER(D)]),
+            "nalu_host_alloc": (I, [ctypes.c_size_t, ctypes.POINTER(P)]),
+            "nalu_host_free": (I, [P]),
+            "nalu_flush_l2": (I, [P, ctypes.c_size_t]),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return None if a is None else ctypes.c_void_p(a.ctypes.data)
+
+
+def default_assemble_opts(**kw):
+    o = AssembleOpts()
+    lib().nalu_assemble_opts_default(ctypes.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+def default_solver_opts(**kw):
+    o = SolverOpts()
+    lib().nalu_solver_opts_default(ctypes.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+class Context:
+    """One device, one stream, one Hex8 mesh and its linear system."""
+
+    def __init__(self, device=0):
+        self._h = ctypes.c_void_p()
+        rc = lib().nalu_create(device, ctypes.byref(self._h))
+        if rc:
+            raise NaluError(rc, "nalu_create(device=%d)" % device)
+
+    def _check(self, rc, what=""):
+        if rc:
+            msg = lib().nalu_last_error(self._h)
+            raise NaluError(rc, "%s: %s" % (what, msg.decode() if msg else ""))
+
+    def close(self):
+        if self._h:
+            lib().nalu_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    # mesh / fields
+    def mesh_create(self, coords, conn, gid=None):
+        coords = np.ascontiguousarray(coords, np.float64)
+        conn = np.ascontiguousarray(conn, np.int32)
+        gid = None if gid is None else np.ascontiguousarray(gid, np.int64)
+        self.n_nodes, self.n_elems = coords.shape[0], conn.shape[0]
+        self._check(lib().nalu_mesh_create(self._h, self.n_nodes, self.n_elems, _ptr(conn), _ptr(gid),
+                                           _ptr(coords)), "mesh_create")
+
+    def field_set(self, name, values):
+        a = np.ascontiguousarray(values, np.float64)
+        self._check(lib().nalu_field_set(self._h, FIELD[name], _ptr(a), a.size, 0), "field_set(%s)" % name)
+
+    def field_get(self, name, shape):
+        out = np.zeros(shape, np.float64)
+        self._check(lib().nalu_field_get(self._h, FIELD[name], _ptr(out), out.size, 0), "field_get(%s)" % name)
+        return out
+
+    # linear system
+    def build_elem_graph(self, num_dof):
+        self._check(lib().nalu_linsys_build_elem_graph(self._h, num_dof), "build_elem_graph")
+
+    def sizes(self):
+        nr, nnz, nd = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int()
+        self._check(lib().nalu_linsys_sizes(self._h, ctypes.byref(nr), ctypes.byref(nnz), ctypes.byref(nd)))
+        return nr.value, nnz.value, nd.value
+
+    def graph(self):
+        nr, nnz, _ = self.sizes()
+        rp = np.zeros(nr + 1, np.int64)
+        ci = np.zeros(nnz, np.int32)
+        self._check(lib().nalu_linsys_graph(self._h, _ptr(rp), _ptr(ci)), "graph")
+        return rp, ci
+
+    def zero(self):
+        self._check(lib().nalu_linsys_zero(self._h), "zero")
+
+    def sum_into(self, elem_ids, lhs, rhs):
+        e = np.ascontiguousarray(elem_ids, np.int64)
+        l_ = np.ascontiguousarray(lhs, np.float64)
+        r_ = np.ascontiguousarray(rhs, np.float64)
+        self._check(lib().nalu_linsys_sum_into(self._h, e.size, _ptr(e), _ptr(l_), _ptr(r_)), "sum_into")
+
+    def apply_dirichlet(self, nodes, bc, solution, begin_dof=0, end_dof=None):
+        nodes = np.ascontiguousarray(nodes, np.int32)
+        _, _, nd = self.sizes()
+        end_dof = nd if end_dof is None else end_dof
+        bc = np.ascontiguousarray(bc, np.float64)
+        solution = np.ascontiguousarray(solution, np.float64)
+        self._check(lib().nalu_linsys_apply_dirichlet(self._h, nodes.size, _ptr(nodes), begin_dof, end_dof,
+                                                      _ptr(bc), _ptr(solution)), "apply_dirichlet")
+
+    def reset_rows(self, nodes, begin_dof=0, end_dof=None):
+        nodes = np.ascontiguousarray(nodes, np.int32)
+        _, _, nd = self.sizes()
+        end_dof = nd if end_dof is None else end_dof
+        self._check(lib().nalu_linsys_reset_rows(self._h, nodes.size, _ptr(nodes), begin_dof, end_dof),
+                    "reset_rows")
+
+    def sum_into_diag(self, node, dof, diag, rhs):
+        self._check(lib().nalu_linsys_sum_into_diag(self._h, int(node), int(dof), float(diag), float(rhs)),
+                    "sum_into_diag")
+
+    def load_complete(self):
+        self._check(lib().nalu_linsys_load_complete(self._h), "load_complete")
+
+    def system(self):
+        nr, nnz, _ = self.sizes()
+        v = np.zeros(nnz)
+        r = np.zeros(nr)
+        self._check(lib().nalu_linsys_copy(self._h, _ptr(v), _ptr(r), 0), "copy")
+        return v, r
+
+    # assembly
+    def assemble(self, kernel, opts=None):
+        opts = default_assemble_opts() if opts is None else opts
+        self._check(lib().nalu_assemble(self._h, kernel, ctypes.byref(opts)), "assemble")
+
+    def capture_element(self, kernel, elem, opts=None):
+        opts = default_assemble_opts() if opts is None else opts
+        ne = 24 if kernel >= 2 else 8
+        lhs = np.zeros((ne, ne))
+        rhs = np.zeros(ne)
+        self._check(lib().nalu_capture_element(self._h, kernel, ctypes.byref(opts), int(elem), _ptr(lhs), _ptr(rhs)),
+                    "capture_element")
+        return lhs, rhs
+
+    def compute_mdot(self, opts=None):
+        opts = default_assemble_opts() if opts is None else opts
+        self._check(lib().nalu_compute_mdot(self._h, ctypes.byref(opts)), "compute_mdot")
+
+    # solve
+    def solve(self, opts=None, raise_on_error=True):
+        opts = default_solver_opts() if opts is None else opts
+        info = SolveInfo()
+        rc = lib().nalu_solve(self._h, ctypes.byref(opts), ctypes.byref(info))
+        if raise_on_error:
+            self._check(rc, "solve")
+        return info
+
+    def solution(self):
+        nr, _, _ = self.sizes()
+        x = np.zeros(nr)
+        self._check(lib().nalu_solution_get(self._h, _ptr(x), 0), "solution_get")
+        return x
+
+    def spmv(self, x):
+        x = np.ascontiguousarray(x, np.float64)
+        y = np.zeros_like(x)
+        self._check(lib().nalu_spmv(self._h, _ptr(x), _ptr(y), 0), "spmv")
+        return y
+
+    def synchronize(self):
+        self._check(lib().nalu_synchronize(self._h), "synchronize")
+
+    def launches(self):
+        return lib().nalu_kernel_launch_count(self._h)
+
+    def last_assemble_ms(self):
+        return lib().nalu_last_assemble_ms(self._h)
+
+    def probe_fp64_tflops(self):
+        t = ctypes.c_double()
+        self._check(lib().nalu_probe_fp64_tflops(self._h, ctypes.byref(t)), "probe")
+        return t.value
+
+    def event_record(self, slot):
+        self._check(lib().nalu_event_record(self._h, slot), "event_record")
+
+    def event_elapsed_ms(self, a, b):
+        t = ctypes.c_double()
+        self._check(lib().nalu_event_elapsed_ms(self._h, a, b, ctypes.byref(t)), "event_elapsed")
+        return t.value
+
+    def flush_l2(self, nbytes=512 << 20):
+        self._check(lib().nalu_flush_l2(self._h, nbytes), "flush_l2")
+
+    # raw pointer variants (pinned host buffers)
+    def field_set_ptr(self, name, ptr, count):
+        self._check(lib().nalu_field_set(self._h, FIELD[name], ptr, count, 0), "field_set(%s)" % name)
+
+    def system_to_ptr(self, values_ptr, rhs_ptr):
+        self._check(lib().nalu_linsys_copy(self._h, values_ptr, rhs_ptr, 0), "copy")
+
+
+class PinnedArray:
+    """numpy view of page-locked host memory from nalu_host_alloc."""
+
+    def __init__(self, shape, dtype=np.float64):
+        dt = np.dtype(dtype)
+        n = int(np.prod(shape))
+        self._p = ctypes.c_void_p()
+        rc = lib().nalu_host_alloc(max(n * dt.itemsize, 1), ctypes.byref(self._p))
+        if rc:
+            raise NaluError(rc, "nalu_host_alloc")
+        buf = (ctypes.c_char * (n * dt.itemsize)).from_address(self._p.value)
+        self.array = np.frombuffer(buf, dtype=dt, count=n).reshape(shape)
+
+    @property
+    def ptr(self):
+        return self._p
+
+    def free(self):
+        if self._p:
+            self.array = None
+            lib().nalu_host_free(self._p)
+            self._p = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+from .linear_system import (AssembleElemSolverAlgorithm, ContinuityAdvElemKernel, LinearSystem,  # noqa: E402
+                            MomentumAdvDiffElemKernel, MomentumUpwAdvDiffElemKernel, ScalarDiffElemKernel)

@@ -1,0 +1,67 @@
+"""Build the sm_103a library and the host-side element check, in tree.
+
+    python -m nalu_gb300.build            # library + host check
+Outputs:
+    nalu_gb300/_lib/libnalu_gb300.so      (CUDA kernels + C ABI)
+    nalu_gb300/_lib/libnalu_elemcheck.so  (element math compiled for the host)
+Each .cu file compiles in its own nvcc process, in parallel, for
+-gencode arch=compute_103a,code=sm_103a only.
+"""
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+OUT = os.path.join(HERE, "_lib")
+SOURCES = ["api.cu", "assemble.cu", "momentum.cu", "krylov.cu"]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def _nvcc():
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _run(cmd):
+    p = subprocess.run(cmd, capture_output=True, text=True)
+    if p.returncode != 0:
+        raise RuntimeError("command failed: %s\n%s%s" % (" ".join(cmd), p.stdout, p.stderr))
+    return p.stdout + p.stderr
+
+
+def build(verbose=False, ptxas_info=False):
+    os.makedirs(OUT, exist_ok=True)
+    nvcc = _nvcc()
+    objs = []
+    flags = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+                    "-I" + CSRC]
+    if ptxas_info:
+        flags += ["-Xptxas", "-v"]
+
+    def comp(src):
+        obj = os.path.join(OUT, src.replace(".cu", ".o"))
+        log = _run([nvcc] + flags + ["-c", os.path.join(CSRC, src), "-o", obj])
+        return obj, log
+
+    with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
+        for obj, log in ex.map(comp, SOURCES):
+            objs.append(obj)
+            if verbose and log.strip():
+                print(log)
+    lib = os.path.join(OUT, "libnalu_gb300.so")
+    _run([nvcc] + ARCH + ["-shared", "-o", lib] + objs + ["-lcudart"])
+    check = os.path.join(OUT, "libnalu_elemcheck.so")
+    cxx = shutil.which("g++") or "g++"
+    _run([cxx, "-std=c++17", "-O2", "-fPIC", "-shared", "-o", check, os.path.join(CSRC, "elem_hostcheck.cpp")])
+    for o in objs:
+        os.remove(o)
+    return lib
+
+
+if __name__ == "__main__":
+    print(build(verbose="-v" in sys.argv, ptxas_info="--ptxas" in sys.argv))

@@ -1,0 +1,83 @@
+// elem_hostcheck.cpp -- host build of the element math in hex8_elem.h.
+//
+// The sm_103a kernels and this file include the same header, so the CPU test
+// suite can check the restructured element math against the oracle on
+// thousands of random elements without a GPU.  Exposes plain C entry points.
+#include <cstdint>
+
+#include "hex8_elem.h"
+
+using namespace nalu_gb300;
+
+namespace {
+template <class F>
+void with_x(const double* xin, F f) {
+  double x[8][3];
+  for (int n = 0; n < 8; ++n)
+    for (int d = 0; d < 3; ++d) x[n][d] = xin[n * 3 + d];
+  f(x);
+}
+}  // namespace
+
+extern "C" {
+
+void hc_scalar_diff(const double* xin, const double* q, const double* k, int shift, double* lhs,
+                    double* rhs) {
+  with_x(xin, [&](double (&x)[8][3]) {
+    ArrayAcc acc{lhs};
+    if (shift) scalar_diff_lhs<true>(x, k, acc);
+    else scalar_diff_lhs<false>(x, k, acc);
+  });
+  for (int r = 0; r < 8; ++r) {
+    double s = 0.0;
+    for (int c = 0; c < 8; ++c) s += lhs[r * 8 + c] * q[c];
+    rhs[r] = -s;
+  }
+}
+
+void hc_continuity(const double* xin, const double* u, const double* rho, const double* p,
+                   const double* gp, double tau, int smdot, int spois, int reduced, double* lhs,
+                   double* rhs) {
+  double w[8][3];
+  for (int n = 0; n < 8; ++n)
+    for (int d = 0; d < 3; ++d) w[n][d] = rho[n] * u[n * 3 + d] + tau * gp[n * 3 + d];
+  const int mode = spois ? 2 : (reduced ? 1 : 0);
+  with_x(xin, [&](double (&x)[8][3]) {
+    ArrayAcc acc{lhs};
+    const double it = 1.0 / tau;
+    if (mode == 0) {
+      if (smdot) continuity_elem<0, true>(x, w, it, p, acc, rhs);
+      else continuity_elem<0, false>(x, w, it, p, acc, rhs);
+    } else if (mode == 1) {
+      if (smdot) continuity_elem<1, true>(x, w, it, p, acc, rhs);
+      else continuity_elem<1, false>(x, w, it, p, acc, rhs);
+    } else {
+      if (smdot) continuity_elem<2, true>(x, w, it, p, acc, rhs);
+      else continuity_elem<2, false>(x, w, it, p, acc, rhs);
+    }
+  });
+  if (mode != 1) {
+    for (int r = 0; r < 8; ++r) {
+      double s = 0.0;
+      for (int c = 0; c < 8; ++c) s += lhs[r * 8 + c] * p[c];
+      rhs[r] -= s;
+    }
+  }
+}
+
+void hc_mdot(const double* xin, const double* rho, const double* u, const double* p,
+             const double* gp, double tau, int smdot, int spois, double* mdot) {
+  double w[8][3];
+  for (int n = 0; n < 8; ++n)
+    for (int d = 0; d < 3; ++d) w[n][d] = rho[n] * u[n * 3 + d] + tau * gp[n * 3 + d];
+  with_x(xin, [&](double (&x)[8][3]) {
+    if (smdot) {
+      if (spois) mdot_elem<true, true>(x, w, p, tau, mdot);
+      else mdot_elem<true, false>(x, w, p, tau, mdot);
+    } else {
+      if (spois) mdot_elem<false, true>(x, w, p, tau, mdot);
+      else mdot_elem<false, false>(x, w, p, tau, mdot);
+    }
+  });
+}
+}

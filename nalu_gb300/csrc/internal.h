@@ -1,0 +1,130 @@
+// internal.h -- context layout and helpers shared by the library's
+// translation units (not part of the C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/nalu_gb300.h"
+
+namespace nalu_gb300 {
+
+// Device buffer owned by a context.
+template <class T>
+struct DBuf {
+  T* p = nullptr;
+  int64_t n = 0;
+  cudaError_t alloc(int64_t count) {
+    free();
+    if (count <= 0) return cudaSuccess;
+    cudaError_t e = cudaMalloc((void**)&p, sizeof(T) * (size_t)count);
+    if (e == cudaSuccess) n = count;
+    else p = nullptr;
+    return e;
+  }
+  void free() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+// Field storage: node fields in Tpetra row order (LID), element fields in
+// element order.
+struct Field {
+  DBuf<double> d;
+  int comps = 0;
+  bool set = false;
+};
+
+// Solver workspace (device vectors are allocated lazily per system size).
+struct SolverWork {
+  DBuf<double> r, z, p, q, ap, dinv, w, tmp;
+  DBuf<float> fvals, fr, fz, fp, fq, fdinv, fx;
+  DBuf<double> V, Hbuf;  // GMRES basis (restart+1 vectors)
+  DBuf<float> fV;
+  DBuf<double> scal;     // device scalars
+  DBuf<double> partial;  // block partial sums
+  int64_t n = 0;
+};
+
+}  // namespace nalu_gb300
+
+struct nalu_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string last_error;
+  int64_t launches = 0;
+  int sm_count = 0;
+
+  // mesh
+  int64_t n_nodes = 0, n_elems = 0;
+  bool identity_order = true;            // gid == index+1 for all nodes
+  std::vector<int32_t> h_lid;            // caller node index -> LID
+  std::vector<int32_t> h_conn_lid;       // [E][8] in LID space (host copy)
+  nalu_gb300::DBuf<int32_t> d_conn;      // [E][8] LIDs
+  nalu_gb300::DBuf<int32_t> d_lid;       // caller index -> LID (device)
+  nalu_gb300::Field fields[NALU_FIELD_COUNT];
+
+  // linear system
+  int num_dof = 0;
+  int64_t n_rows = 0, nnz = 0, node_nnz = 0;
+  nalu_gb300::DBuf<int64_t> d_nrowptr;   // node-level graph
+  nalu_gb300::DBuf<int32_t> d_ncolind;
+  nalu_gb300::DBuf<int64_t> d_rowptr;    // dof-level CRS (Tpetra layout)
+  nalu_gb300::DBuf<int32_t> d_colind;
+  nalu_gb300::DBuf<double> d_values, d_rhs, d_x;
+  nalu_gb300::DBuf<uint8_t> d_slots;     // [E][64] column offset in the node row
+  nalu_gb300::DBuf<uint8_t> d_bcmask;    // 1 where the row was made an identity row
+  nalu_gb300::DBuf<int32_t> d_colour_elems;  // element ids grouped by colour
+  std::vector<int64_t> colour_offsets;   // [n_colours+1]
+  int scatter_choice[4] = {0, 0, 0, 0};  // autotuned scatter per kernel (0 = not tuned)
+
+  // errors raised by kernels (negative Jacobian count, graph misses, ...)
+  nalu_gb300::DBuf<int32_t> d_flags;     // [4]
+
+  // timing
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t user_ev[64] = {};
+  double last_assemble_ms = 0.0;
+  nalu_gb300::DBuf<uint8_t> flush_buf;
+
+  nalu_gb300::SolverWork sw;
+};
+
+namespace nalu_gb300 {
+
+enum FlagSlot { FLAG_NEG_JAC = 0, FLAG_GRAPH_MISS = 1, FLAG_CAPACITY = 2, FLAG_NONFINITE = 3 };
+
+int set_error(nalu_ctx* ctx, int status, const std::string& msg);
+int cuda_check(nalu_ctx* ctx, cudaError_t e, const char* what);
+#define NALU_CUDA(ctx, call)                                      \
+  do {                                                            \
+    cudaError_t e_ = (call);                                      \
+    if (e_ != cudaSuccess) return nalu_gb300::cuda_check(ctx, e_, #call); \
+  } while (0)
+
+// launchers implemented in assemble.cu
+int launch_assemble(nalu_ctx* ctx, int kernel, const nalu_assemble_opts& o, int scatter);
+int launch_capture(nalu_ctx* ctx, int kernel, const nalu_assemble_opts& o, int64_t elem, double* d_lhs,
+                   double* d_rhs);
+int launch_mdot(nalu_ctx* ctx, const nalu_assemble_opts& o);
+int launch_slot_table(nalu_ctx* ctx);
+int launch_expand_graph(nalu_ctx* ctx);
+int launch_sum_into(nalu_ctx* ctx, int64_t n, const int64_t* d_elems, const double* d_lhs,
+                    const double* d_rhs);
+int launch_bc_rows(nalu_ctx* ctx, int64_t n, const int32_t* d_rows, const double* d_vals, int mode);
+int launch_permute_in(nalu_ctx* ctx, const double* src, double* dst, int comps, int64_t n);
+int launch_permute_out(nalu_ctx* ctx, const double* src, double* dst, int comps, int64_t n);
+int launch_fill(nalu_ctx* ctx, double* p, int64_t n, double v);
+int check_flags(nalu_ctx* ctx);
+int probe_fp64(nalu_ctx* ctx, double* tflops);
+
+// krylov.cu
+int solve(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* info);
+int spmv_fp64(nalu_ctx* ctx, const double* x, double* y);
+
+}  // namespace nalu_gb300

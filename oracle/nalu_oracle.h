@@ -1,0 +1,114 @@
+/*
+ * nalu_oracle.h -- CPU FP64 oracle for the Hex8 CVFEM assembly + continuity
+ * solve path of NaluCFD/Nalu.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker that the GPU path is
+ * compared against (tests, the smoke check, and the CPU-baseline leg of the
+ * benchmark).  Nothing in the product links or calls it.
+ *
+ * Every function restates the reference algorithm in plain C++ and keeps the
+ * reference's floating-point operation order (the library is compiled with
+ * -ffp-contract=off), so that on the same inputs it reproduces the reference's
+ * own compiled master-element code bit for bit (pinned by the oracle tests
+ * against the reference's Hex8CVFEM.C compiled in this container, and against
+ * the golden vectors of the reference's unit tests).
+ *
+ * Layouts: coords [8][3], nodal vectors [8][3], element matrices row-major
+ * [rows][cols], grad ops [ip][node][dim] -- the same as the reference's
+ * SharedMemView layouts (include/ScratchViews.h).
+ */
+#ifndef NALU_ORACLE_H
+#define NALU_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* --- master element (src/master_element/Hex8CVFEM.C) ------------------- */
+void orc_hex_scs_tables(int* lrscv24, double* intg_loc36, double* intg_loc_shift36);
+void orc_hex8_shape_fcn(int npts, const double* iso, double* shape /*[npts][8]*/);
+void orc_hex8_derivative(int npts, const double* iso, double* deriv /*[npts][8][3]*/);
+/* returns the number of integration points whose det(J) <= tiny */
+int  orc_generic_grad_op(int npts, const double* deriv, const double* coords,
+                         double* gradop /*[npts][8][3]*/, double* detj /*[npts] or NULL*/);
+int  orc_hex_scs_grad_op(const double* coords, int shifted, double* gradop, double* deriv);
+void orc_hex_scs_areav(const double* coords, double* areav /*[12][3]*/);
+void orc_hex_scv_volume(const double* coords, double* volume /*[8]*/);
+int  orc_hex_scv_grad_op(const double* coords, int shifted, double* gradop, double* deriv);
+
+/* --- element kernels (src/kernel/*.C) ----------------------------------- */
+void orc_scalar_diff_elem(const double* coords, const double* q, const double* diff_coeff,
+                          int shifted_grad_op, double* lhs /*[8][8]*/, double* rhs /*[8]*/);
+void orc_continuity_adv_elem(const double* coords, const double* velocity /*[8][3]*/,
+                             const double* density, const double* pressure,
+                             const double* gpdx /*[8][3]*/, double proj_time_scale,
+                             int shift_mdot, int shift_poisson, int reduced_sens,
+                             double* lhs, double* rhs);
+void orc_momentum_adv_diff_elem(const double* coords, const double* velocity,
+                                const double* viscosity, const double* mdot /*[12]*/,
+                                double include_divu, int shifted_grad_op, int skew_symmetric,
+                                double* lhs /*[24][24]*/, double* rhs /*[24]*/);
+void orc_momentum_upw_adv_diff_elem(const double* coords, const double* velocity,
+                                    const double* velocity_rtm, const double* density,
+                                    const double* viscosity, const double* gju /*[8][3][3]*/,
+                                    const double* mdot, double include_divu,
+                                    int shifted_grad_op, int skew_symmetric,
+                                    double alpha, double alpha_upw, double upw_factor,
+                                    double hybrid_factor, int use_limiter,
+                                    double* lhs, double* rhs);
+void orc_mdot_elem(const double* coords, const double* density, const double* velocity_rtm,
+                   const double* pressure, const double* gpdx, double proj_time_scale,
+                   int shift_mdot, int shift_poisson, double* mdot /*[12]*/);
+
+/* --- linear system (src/TpetraLinearSystem.C) --------------------------- */
+/* Restated buildElemToNodeGraph + finalizeLinearSystem on one rank.
+ * node_gid may be NULL (gid = index+1).  Call with colind == NULL to get
+ * n_rows and nnz; then call again with buffers of those sizes. */
+int orc_graph_build(int64_t n_nodes, int64_t n_elems, const int32_t* conn,
+                    const int64_t* node_gid, int num_dof,
+                    int64_t* n_rows, int64_t* nnz, int64_t* rowptr, int32_t* colind,
+                    int32_t* node_lid /*[n_nodes] out, may be NULL*/);
+
+/* Serial element-order assembly through the restated sumInto.  kernel:
+ * 0 ScalarDiff, 1 ContinuityAdv, 2 MomentumAdvDiff, 3 MomentumUpwAdvDiff.
+ * fields are in node-index order; opts is a double[16] option block:
+ *  [0] shifted_grad_op [1] shift_mdot [2] shift_poisson [3] reduced_sens
+ *  [4] proj_time_scale [5] include_divu [6] skew_symmetric [7] alpha
+ *  [8] alpha_upw [9] upw_factor [10] hybrid_factor [11] use_limiter */
+int orc_assemble(int kernel, int64_t n_nodes, int64_t n_elems, const int32_t* conn,
+                 const int32_t* node_lid, const double* coords,
+                 const double* f_scalar /*q or pressure*/, const double* f_coeff /*k, density or viscosity*/,
+                 const double* f_vec /*velocity*/, const double* f_vec2 /*Gpdx or velocity_rtm*/,
+                 const double* f_rho /*density for upwind*/, const double* f_gju /*[n][9]*/,
+                 const double* elem_mdot /*[E][12]*/, const double* opts,
+                 int num_dof, const int64_t* rowptr, const int32_t* colind,
+                 double* values, double* rhs, int n_threads);
+
+/* one element's sumInto (TpetraLinearSystem::sumInto :1458-1522);
+ * elem_nodes_lid[8] are node LIDs, lhs is (8*num_dof)^2 row-major */
+void orc_sum_into(int num_dof, const int32_t* elem_nodes_lid, const double* lhs, const double* rhs,
+                  const int64_t* rowptr, const int32_t* colind, double* values, double* sysrhs);
+void orc_apply_dirichlet(const int64_t* rowptr, const int32_t* colind, double* values,
+                         double* rhs, int64_t n_bc, const int32_t* rows,
+                         const double* bc_value, const double* current);
+void orc_reset_rows(const int64_t* rowptr, double* values, double* rhs,
+                    int64_t n_rows_reset, const int32_t* rows);
+void orc_sum_into_diag(const int64_t* rowptr, const int32_t* colind, double* values,
+                       double* rhs, int32_t row, double diag, double rhs_value);
+
+/* --- solvers (FP64, stand-in for Belos/Ifpack2, unpinned) -------------- */
+void orc_spmv(int64_t n, const int64_t* rowptr, const int32_t* colind, const double* v,
+              const double* x, double* y, int n_threads);
+/* Jacobi-PCG; returns iterations; res_out = true ||b-Ax||/||b|| */
+int orc_pcg_jacobi(int64_t n, const int64_t* rowptr, const int32_t* colind, const double* v,
+                   const double* b, double* x, double tol, int max_it, double* res_out,
+                   int n_threads);
+int orc_gmres_jacobi(int64_t n, const int64_t* rowptr, const int32_t* colind, const double* v,
+                     const double* b, double* x, int restart, double tol, int max_it,
+                     double* res_out, int n_threads);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

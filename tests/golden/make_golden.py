@@ -1,0 +1,111 @@
+"""Extract the reference's unit-test golden vectors into JSON fixtures.
+
+Run once where the NaluCFD/Nalu source tree is available:
+
+    python tests/golden/make_golden.py /root/reference
+
+It reads the test sources as text (no reference code is executed) and writes
+``tests/golden/nalu_unit_golds.json``.  The fixture records, per gold, the
+reference file and line the numbers come from, the tolerance the reference
+test uses, and the inputs needed to recompute it (mesh, fields, options).
+"""
+import json
+import os
+import re
+import sys
+
+
+def _strip_comments(text):
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return re.sub(r"//[^\n]*", "", text)
+
+
+def _find_array(src, name, start=0):
+    """Return (values, line) of the first `name[...] = { ... };` after start."""
+    m = re.compile(r"\b" + re.escape(name) + r"\s*(\[[^\]]*\])+\s*=\s*\{").search(src, start)
+    if not m:
+        raise KeyError(name)
+    depth, i = 0, m.end() - 1
+    while True:
+        c = src[i]
+        if c == "{":
+            depth += 1
+        elif c == "}":
+            depth -= 1
+            if depth == 0:
+                break
+        i += 1
+    body = _strip_comments(src[m.end() - 1:i + 1])
+    # expressions like 2.0*2 in the Tpetra table
+    exprs = re.findall(r"[-+]?[\d.]+(?:\s*\*\s*[\d.]+)?", body)
+    vals = [eval(e.replace(" ", "")) for e in exprs]
+    line = src.count("\n", 0, m.start()) + 1
+    return vals, line
+
+
+def _namespace_start(src, ns):
+    m = re.search(r"namespace\s+" + re.escape(ns) + r"\s*\{", src)
+    if not m:
+        raise KeyError(ns)
+    return m.end()
+
+
+def main(ref):
+    ut = os.path.join(ref, "unit_tests")
+    out = {"source": "NaluCFD/Nalu unit tests (text extraction)", "golds": {}}
+
+    def grab(relpath, name, ns=None):
+        src = open(os.path.join(ut, relpath)).read()
+        start = _namespace_start(src, ns) if ns else 0
+        vals, line = _find_array(src, name, start)
+        return vals, "unit_tests/%s:%d" % (relpath, line)
+
+    g = out["golds"]
+    lhs, at = grab("kernels/UnitTestScalarDiffElem.C", "lhs", "cvfem_diff")
+    g["scalar_diff"] = {"lhs": lhs, "rhs": [0.0] * 8, "at": at, "tol": 1.0e-15,
+                        "mesh": "unit_cube", "fields": "temperature=trig(aT=1,k=1), k=1"}
+    rhs, at_r = grab("kernels/UnitTestContinuityAdvElem.C", "rhs", "advection_default")
+    lhs, at_l = grab("kernels/UnitTestContinuityAdvElem.C", "lhs", "advection_default")
+    g["continuity_default"] = {"lhs": lhs, "rhs": rhs, "at": [at_r, at_l], "tol": 1.0e-15,
+                               "opts": {"shift_mdot": 0, "shift_poisson": 0, "reduced_sens": 0,
+                                        "proj_time_scale": 1.0}}
+    rhs, at_r = grab("kernels/UnitTestContinuityAdvElem.C", "rhs", "advection_reduced_sensitivities")
+    lhs, at_l = grab("kernels/UnitTestContinuityAdvElem.C", "lhs", "advection_reduced_sensitivities")
+    g["continuity_reduced_sens"] = {"lhs": lhs, "rhs": rhs, "at": [at_r, at_l], "tol": 1.0e-15,
+                                    "opts": {"shift_mdot": 0, "shift_poisson": 0, "reduced_sens": 1,
+                                             "proj_time_scale": 1.0}}
+    g["continuity_reduced_shift"] = dict(g["continuity_reduced_sens"])
+    g["continuity_reduced_shift"]["opts"] = {"shift_mdot": 0, "shift_poisson": 1, "reduced_sens": 1,
+                                             "proj_time_scale": 1.0}
+    rhs, at_r = grab("kernels/UnitTestMomentumAdvDiffElem.C", "rhs", "advection_diffusion")
+    lhs, at_l = grab("kernels/UnitTestMomentumAdvDiffElem.C", "lhs", "advection_diffusion")
+    assert len(rhs) == 24 and len(lhs) == 576, (len(rhs), len(lhs))
+    g["momentum_adv_diff"] = {"lhs": lhs, "rhs": rhs, "at": [at_r, at_l], "tol": 1.0e-15,
+                              "opts": {"include_divu": 0.0, "viscosity": 0.1}}
+    ev, at_e = grab("UnitTestTpetra.C", "elemVals")
+    lv, at_l = grab("UnitTestTpetra.C", "lhsVals")
+    src = open(os.path.join(ut, "UnitTestTpetra.C")).read()
+    m = re.search(r"goldRowLengths\s*=\s*\{([^}]*)\}", src)
+    rl = [int(x) for x in m.group(1).split(",")]
+    g["tpetra_2hex"] = {"elem_vals": ev, "lhs_vals": lv, "row_lengths": rl, "tol": 1.0e-9,
+                        "at": [at_e, at_l, "unit_tests/UnitTestTpetra.C:%d" % (src.count("\n", 0, m.start()) + 1)],
+                        "mesh": "generated:1x1x2"}
+    gs, at_g = grab("UnitTestKokkosMEGold.h", "hex8_scv_grad_op")
+    gss, at_s = grab("UnitTestKokkosMEGold.h", "hex8_scv_shifted_grad_op")
+    usrc = open(os.path.join(ut, "UnitTestUtils.C")).read()
+    k = usrc.index("case stk::topology::HEXAHEDRON_8:", usrc.index("create_one_perturbed_element(stk::mesh::BulkData"))
+    blk = usrc[k:usrc.index("break;", k)]
+    coords = [float(x) for x in re.findall(r"[-+]?\d*\.\d+", blk)]
+    assert len(coords) == 24
+    g["hex8_scv_grad_op"] = {"gradop": gs, "shifted_gradop": gss, "coords": coords, "tol": 1.0e-10,
+                             "at": [at_g, at_s, "unit_tests/UnitTestUtils.C:%d" % (usrc.count("\n", 0, k) + 1)]}
+    g["hex8_scv_volume_unit_cube"] = {"volume": [0.125] * 8, "tol": 2.220446049250313e-16,
+                                      "at": "unit_tests/UnitTestHexSCVDeterminant.C:60-75"}
+    dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "nalu_unit_golds.json")
+    with open(dst, "w") as f:
+        json.dump(out, f, indent=1)
+    print("wrote", dst, "with", len(g), "golds")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

@@ -1,0 +1,79 @@
+"""The restructured element math of the GPU kernels (nalu_gb300/csrc/hex8_elem.h),
+compiled for the host, against the oracle and the reference's golds (CPU)."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from helpers import TrigFields, block_mesh, check_dense
+
+P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+BASE = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0], [0, 0, 1], [1, 0, 1], [1, 1, 1], [0, 1, 1]], float)
+
+
+def _hc_scalar(L, c, q, k, sh):
+    lhs, rhs = np.zeros(64), np.zeros(8)
+    L.hc_scalar_diff(P(np.ascontiguousarray(c)), P(q), P(k), int(sh), P(lhs), P(rhs))
+    return lhs.reshape(8, 8), rhs
+
+
+def _hc_cont(L, c, u, rho, p, gp, tau, sm, sp, rd):
+    lhs, rhs = np.zeros(64), np.zeros(8)
+    L.hc_continuity(P(np.ascontiguousarray(c)), P(np.ascontiguousarray(u)), P(rho), P(p), P(np.ascontiguousarray(gp)),
+                    float(tau), sm, sp, rd, P(lhs), P(rhs))
+    return lhs.reshape(8, 8), rhs
+
+
+def test_golds_through_device_math(elemcheck, golds):
+    c, conn, gid = block_mesh(1, 1, 1)
+    e = conn[0]
+    lhs, rhs = _hc_scalar(elemcheck, c[e], TrigFields.temperature(c)[e], np.ones(8), 0)
+    assert np.max(np.abs(lhs.ravel() - golds["scalar_diff"]["lhs"])) <= 1e-15
+    assert np.max(np.abs(rhs)) <= 1e-15
+    for key, opts in [("continuity_default", (0, 0, 0)), ("continuity_reduced_sens", (0, 0, 1)),
+                      ("continuity_reduced_shift", (0, 1, 1))]:
+        lhs, rhs = _hc_cont(elemcheck, c[e], TrigFields.velocity(c)[e], np.ones(8), TrigFields.pressure(c)[e],
+                            TrigFields.dpdx(c)[e], 1.0, *opts)
+        assert np.max(np.abs(lhs.ravel() - golds[key]["lhs"])) <= 1e-15, key
+        assert np.max(np.abs(rhs - golds[key]["rhs"])) <= 1e-15, key
+
+
+@pytest.mark.parametrize("shift", [0, 1])
+def test_scalar_diff_random_elements(elemcheck, oracle, shift):
+    rng = np.random.default_rng(10 + shift)
+    for t in range(400):
+        h = rng.uniform(1 / 256, 1 / 8)
+        c = (BASE + 0.2 * rng.uniform(-1, 1, (8, 3))) * h + rng.uniform(0, 1, 3)
+        q, k = rng.uniform(0, 1, 8), rng.uniform(0.5, 2, 8)
+        l1, r1 = oracle.scalar_diff_elem(c, q, k, shift)
+        l2, r2 = _hc_scalar(elemcheck, c, q, k, shift)
+        check_dense(l2, l1, what="lhs")
+        check_dense(r2[None], r1[None], what="rhs")
+
+
+@pytest.mark.parametrize("opts", [(0, 0, 0), (0, 0, 1), (0, 1, 1), (1, 0, 0), (1, 1, 1)])
+def test_continuity_random_elements(elemcheck, oracle, opts):
+    rng = np.random.default_rng(20)
+    for t in range(300):
+        h = rng.uniform(1 / 256, 1 / 8)
+        c = (BASE + 0.2 * rng.uniform(-1, 1, (8, 3))) * h + rng.uniform(0, 1, 3)
+        u, gp = rng.normal(size=(8, 3)), rng.normal(size=(8, 3))
+        rho, p, tau = rng.uniform(0.5, 2, 8), rng.normal(size=8), rng.uniform(0.1, 2)
+        l1, r1 = oracle.continuity_adv_elem(c, u, rho, p, gp, tau, *opts)
+        l2, r2 = _hc_cont(elemcheck, c, u, rho, p, gp, tau, *opts)
+        check_dense(l2, l1, what="lhs")
+        check_dense(r2[None], r1[None], what="rhs")
+
+
+@pytest.mark.parametrize("sm,sp", [(0, 0), (1, 0), (0, 1), (1, 1)])
+def test_mdot_random_elements(elemcheck, oracle, sm, sp):
+    rng = np.random.default_rng(30)
+    for t in range(200):
+        h = rng.uniform(1 / 128, 1 / 8)
+        c = np.ascontiguousarray((BASE + 0.2 * rng.uniform(-1, 1, (8, 3))) * h + rng.uniform(0, 1, 3))
+        u, gp = np.ascontiguousarray(rng.normal(size=(8, 3))), np.ascontiguousarray(rng.normal(size=(8, 3)))
+        rho, p, tau = rng.uniform(0.5, 2, 8), rng.normal(size=8), rng.uniform(0.1, 2)
+        m1 = oracle.mdot_elem(c, rho, u, p, gp, tau, sm, sp)
+        m2 = np.zeros(12)
+        elemcheck.hc_mdot(P(c), P(rho), P(u), P(p), P(gp), float(tau), sm, sp, P(m2))
+        check_dense(m2[None], m1[None], what="mdot")

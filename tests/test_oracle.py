@@ -1,0 +1,157 @@
+"""The oracle pinned: against the reference's own compiled master element
+(where built here), the reference's unit-test golden vectors, and the Tpetra
+2-element graph/matrix test."""
+import numpy as np
+import pytest
+
+from helpers import TrigFields, block_mesh, check_dense
+
+BASE = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0], [0, 0, 1], [1, 0, 1], [1, 1, 1], [0, 1, 1]], float)
+
+
+def _unit_cube_element():
+    c, conn, gid = block_mesh(1, 1, 1)
+    return c, conn
+
+
+def test_oracle_bitwise_equals_reference_master_element(oracle):
+    """Restated HexSCS/HexSCV == the reference's Hex8CVFEM.C compiled from its
+    sources (oracle/_ref); only where that build exists."""
+    import ctypes
+    ref = oracle.ref()
+    if ref is None:
+        pytest.skip("reference master element not built here (oracle/_ref)")
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    rng = np.random.default_rng(42)
+    for t in range(300):
+        c = np.ascontiguousarray((BASE + 0.2 * rng.uniform(-1, 1, (8, 3))) * rng.uniform(0.01, 3) + rng.uniform(-2, 2, 3))
+        a1 = oracle.scs_areav(c)
+        a2 = np.zeros(36)
+        ref.ref_hex_scs_areav(P(c), P(a2))
+        assert np.array_equal(a1.ravel(), a2)
+        for sh in (0, 1):
+            g1, d1, _ = oracle.scs_grad_op(c, sh)
+            g2, d2 = np.zeros(288), np.zeros(288)
+            ref.ref_hex_scs_grad_op(P(c), sh, P(g2), P(d2))
+            assert np.array_equal(g1.ravel(), g2) and np.array_equal(d1.ravel(), d2)
+            g1, d1, _ = oracle.scv_grad_op(c, sh)
+            g2, d2 = np.zeros(192), np.zeros(192)
+            ref.ref_hex_scv_grad_op(P(c), sh, P(g2), P(d2))
+            assert np.array_equal(g1.ravel(), g2)
+        v2 = np.zeros(8)
+        ref.ref_hex_scv_volume(P(c), P(v2))
+        assert np.array_equal(oracle.scv_volume(c), v2)
+    lr, loc, locs = oracle.scs_tables()
+    for sh in (0, 1):
+        s2 = np.zeros(96)
+        ref.ref_hex_scs_shape_fcn(sh, P(s2))
+        assert np.array_equal(oracle.shape_fcn(locs if sh else loc).ravel(), s2)
+
+
+def test_golds_scalar_diff(oracle, golds):
+    c, conn = _unit_cube_element()
+    g = golds["scalar_diff"]
+    lhs, rhs = oracle.scalar_diff_elem(c[conn[0]], TrigFields.temperature(c)[conn[0]], np.ones(8))
+    assert np.max(np.abs(lhs.ravel() - g["lhs"])) <= g["tol"]
+    assert np.max(np.abs(rhs - np.array(g["rhs"]))) <= g["tol"]
+
+
+@pytest.mark.parametrize("key,opts", [("continuity_default", (0, 0, 0)), ("continuity_reduced_sens", (0, 0, 1)),
+                                      ("continuity_reduced_shift", (0, 1, 1))])
+def test_golds_continuity(oracle, golds, key, opts):
+    c, conn = _unit_cube_element()
+    e = conn[0]
+    g = golds[key]
+    lhs, rhs = oracle.continuity_adv_elem(c[e], TrigFields.velocity(c)[e], np.ones(8), TrigFields.pressure(c)[e],
+                                          TrigFields.dpdx(c)[e], 1.0, *opts)
+    assert np.max(np.abs(lhs.ravel() - g["lhs"])) <= g["tol"]
+    assert np.max(np.abs(rhs - g["rhs"])) <= g["tol"]
+
+
+def test_golds_momentum(oracle, golds):
+    c, conn = _unit_cube_element()
+    e = conn[0]
+    g = golds["momentum_adv_diff"]
+    u = TrigFields.velocity(c)[e]
+    mdot = oracle.mdot_elem(c[e], np.ones(8), u, np.zeros(8), np.zeros(24))
+    lhs, rhs = oracle.momentum_adv_diff_elem(c[e], u, 0.1 * np.ones(8), mdot, 0.0)
+    assert np.max(np.abs(lhs.ravel() - g["lhs"])) <= g["tol"]
+    assert np.max(np.abs(rhs - g["rhs"])) <= g["tol"]
+
+
+def test_golds_scv(oracle, golds):
+    g = golds["hex8_scv_grad_op"]
+    c = np.array(g["coords"]).reshape(8, 3)
+    assert np.max(np.abs(oracle.scv_grad_op(c)[0].ravel() - g["gradop"])) <= g["tol"]
+    assert np.max(np.abs(oracle.scv_grad_op(c, True)[0].ravel() - g["shifted_gradop"])) <= g["tol"]
+    cu, conn = _unit_cube_element()
+    assert np.max(np.abs(oracle.scv_volume(cu[conn[0]]) - 0.125)) <= golds["hex8_scv_volume_unit_cube"]["tol"]
+
+
+def test_tpetra_two_hex_graph_and_matrix(oracle, golds):
+    """unit_tests/UnitTestTpetra.C: generated:1x1x2, constant element matrix."""
+    g = golds["tpetra_2hex"]
+    c, conn, gid = block_mesh(1, 1, 2)
+    rp, ci, lid = oracle.graph(c.shape[0], conn, 1, gid)
+    assert np.diff(rp).tolist() == g["row_lengths"]
+    vals = np.zeros(ci.size)
+    rhs = np.zeros(rp.size - 1)
+    ev = np.array(g["elem_vals"])
+    for e in range(conn.shape[0]):
+        oracle.sum_into(1, lid[conn[e]], ev, np.zeros(8), rp, ci, vals, rhs)
+    dense = np.zeros((12, 12))
+    for i in range(12):
+        for k in range(rp[i], rp[i + 1]):
+            dense[i, ci[k]] = vals[k]
+    assert np.max(np.abs(dense.ravel() - g["lhs_vals"])) <= g["tol"]
+
+
+def test_graph_dof3_layout(oracle):
+    c, conn, gid = block_mesh(2, 1, 1)
+    rp1, ci1, _ = oracle.graph(c.shape[0], conn, 1)
+    rp3, ci3, _ = oracle.graph(c.shape[0], conn, 3)
+    assert rp3.size - 1 == 3 * (rp1.size - 1)
+    for a in range(rp1.size - 1):
+        nb = ci1[rp1[a]:rp1[a + 1]]
+        want = (3 * nb[:, None] + np.arange(3)[None, :]).ravel()
+        for d in range(3):
+            r = 3 * a + d
+            assert np.array_equal(ci3[rp3[r]:rp3[r + 1]], want)
+
+
+def test_graph_respects_global_ids(oracle):
+    """Rows follow ascending global id (beginLinearSystemConstruction)."""
+    c, conn, gid = block_mesh(3, 2, 2)
+    rng = np.random.default_rng(3)
+    perm_gid = rng.permutation(c.shape[0]).astype(np.int64) * 7 + 11
+    rp, ci, lid = oracle.graph(c.shape[0], conn, 1, perm_gid)
+    order = np.argsort(perm_gid, kind="stable")
+    assert np.array_equal(lid[order], np.arange(c.shape[0]))
+    for a in range(rp.size - 1):
+        row = ci[rp[a]:rp[a + 1]]
+        assert np.all(np.diff(row) > 0)
+
+
+def test_oracle_threaded_matches_serial(oracle):
+    c, conn, gid = block_mesh(6, 5, 4, jitter=0.1, seed=5)
+    rp, ci, lid = oracle.graph(c.shape[0], conn, 1)
+    rng = np.random.default_rng(0)
+    q, k = rng.uniform(size=c.shape[0]), rng.uniform(0.5, 2, c.shape[0])
+    v1, r1 = oracle.assemble(oracle.KERNEL_SCALAR_DIFF, c, conn, rp, ci, lid, scalar=q, coeff=k)
+    v2, r2 = oracle.assemble(oracle.KERNEL_SCALAR_DIFF, c, conn, rp, ci, lid, scalar=q, coeff=k, n_threads=4)
+    assert np.allclose(v1, v2, rtol=1e-13, atol=1e-15) and np.allclose(r1, r2, rtol=1e-13, atol=1e-15)
+
+
+def test_oracle_solvers(oracle):
+    c, conn, gid = block_mesh(6, 6, 6, jitter=0.1, seed=2)
+    rp, ci, lid = oracle.graph(c.shape[0], conn, 1)
+    v, r = oracle.assemble(oracle.KERNEL_SCALAR_DIFF, c, conn, rp, ci, lid, scalar=np.zeros(c.shape[0]),
+                           coeff=np.ones(c.shape[0]))
+    # Dirichlet on x = 0 and x = 1
+    nodes = np.where((c[:, 0] == 0.0) | (c[:, 0] == 1.0))[0]
+    b = np.random.default_rng(1).normal(size=rp.size - 1)
+    oracle.apply_dirichlet(rp, ci, v, b, nodes, c[nodes, 0], np.zeros(nodes.size))
+    x, it, res = oracle.pcg_jacobi(rp, ci, v, b, tol=1e-10)
+    assert res <= 1e-10
+    x2, it2, res2 = oracle.gmres_jacobi(rp, ci, v, b, restart=30, tol=1e-10)
+    assert res2 <= 1e-10 and np.allclose(x, x2, atol=1e-8)
