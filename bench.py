@@ -332,7 +332,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-solve", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--size", type=int, default=128, help="elements per edge (default: the 128^3 workload)")
     args = ap.parse_args()
+    global N_EDGE
+    N_EDGE = args.size
     if args.impl == "reference":
         return bench_reference(args)
     return bench_gpu(args)

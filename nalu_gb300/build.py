@@ -58,6 +58,10 @@ def build(verbose=False, ptxas_info=False):
     check = os.path.join(OUT, "libnalu_elemcheck.so")
     cxx = shutil.which("g++") or "g++"
     _run([cxx, "-std=c++17", "-O2", "-fPIC", "-shared", "-o", check, os.path.join(CSRC, "elem_hostcheck.cpp")])
+    # C++ caller of the host interface (include/nalu_gb300.hpp)
+    _run([cxx, "-std=c++17", "-O2", "-o", os.path.join(OUT, "heat_conduction"),
+          os.path.join(HERE, "examples", "heat_conduction.cpp"), "-L" + OUT, "-lnalu_gb300",
+          "-Wl,-rpath," + OUT])
     for o in objs:
         os.remove(o)
     return lib

@@ -58,14 +58,18 @@ __global__ void __launch_bounds__(256) k_spmv(int64_t n, const int64_t* __restri
   const int sub = threadIdx.x % TPR;
   const int64_t rows_per_block = blockDim.x / TPR;
   double dot = 0.0;
-  for (int64_t row = (int64_t)blockIdx.x * rows_per_block + threadIdx.x / TPR; row < n;
-       row += (int64_t)gridDim.x * rows_per_block) {
-    const int64_t b = __ldg(rp + row), e = __ldg(rp + row + 1);
+  // the loop bound is uniform across the warp (all lanes reach the shuffles)
+  for (int64_t base = (int64_t)blockIdx.x * rows_per_block; base < n; base += (int64_t)gridDim.x * rows_per_block) {
+    const int64_t row = base + threadIdx.x / TPR;
+    const bool valid = row < n;
     double s = 0.0;
-    for (int64_t j = b + sub; j < e; j += TPR) s += (double)__ldg(v + j) * (double)__ldg(x + __ldg(ci + j));
+    if (valid) {
+      const int64_t b = __ldg(rp + row), e = __ldg(rp + row + 1);
+      for (int64_t j = b + sub; j < e; j += TPR) s += (double)__ldg(v + j) * (double)__ldg(x + __ldg(ci + j));
+    }
 #pragma unroll
     for (int o = TPR / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, TPR);
-    if (sub == 0) {
+    if (valid && sub == 0) {
       y[row] = (XT)s;
       if (DOT) dot += s * (double)x[row];
     }
@@ -86,14 +90,17 @@ __global__ void __launch_bounds__(256) k_residual(int64_t n, const int64_t* __re
   const int sub = threadIdx.x % TPR;
   const int64_t rows_per_block = blockDim.x / TPR;
   double acc = 0.0;
-  for (int64_t row = (int64_t)blockIdx.x * rows_per_block + threadIdx.x / TPR; row < n;
-       row += (int64_t)gridDim.x * rows_per_block) {
-    const int64_t s0 = __ldg(rp + row), e = __ldg(rp + row + 1);
+  for (int64_t base = (int64_t)blockIdx.x * rows_per_block; base < n; base += (int64_t)gridDim.x * rows_per_block) {
+    const int64_t row = base + threadIdx.x / TPR;
+    const bool valid = row < n;
     double s = 0.0;
-    for (int64_t j = s0 + sub; j < e; j += TPR) s += __ldg(v + j) * __ldg(x + __ldg(ci + j));
+    if (valid) {
+      const int64_t s0 = __ldg(rp + row), e = __ldg(rp + row + 1);
+      for (int64_t j = s0 + sub; j < e; j += TPR) s += __ldg(v + j) * __ldg(x + __ldg(ci + j));
+    }
 #pragma unroll
     for (int o = TPR / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, TPR);
-    if (sub == 0) {
+    if (valid && sub == 0) {
       const double d = b[row] - s;
       r[row] = d;
       acc += d * d;
@@ -371,11 +378,11 @@ void cg_chunk(nalu_ctx* ctx, const Mat<VT>& A, Work<T>& w, double* scal, double*
     k_alpha<<<1, 1, 0, ctx->stream>>>(scal);
     const bool jac = precond != NALU_PRECOND_CHEBYSHEV;
     k_cg_update<T><<<g, kRedThreads, 0, ctx->stream>>>(n, scal, w.x, w.p, w.r, w.q, w.z, w.dinv, partial, jac ? 1 : 0);
-    ctx->launches += 3;
-    if (jac) {
-      k_finish<<<1, 256, 0, ctx->stream>>>(partial, g, 2, scal, S_RZNEW);
-    } else {
-      // z = cheb(r); rz via a dot kernel (multi_dot with k = 1)
+    // r.z (Jacobi) and r.r -> scal[S_RZNEW], scal[S_RR]
+    k_finish<<<1, 256, 0, ctx->stream>>>(partial, g, 2, scal, S_RZNEW);
+    ctx->launches += 4;
+    if (!jac) {
+      // z = cheb(r); r.z recomputed with the Chebyshev z
       cheb_apply<VT, T>(ctx, A, w.dinv, w.r, w.z, ctmp1, ctmp2, cheb);
       k_multi_dot<T><<<g, kRedThreads, 0, ctx->stream>>>(n, 1, w.r, w.z, partial);
       k_finish<<<1, 256, 0, ctx->stream>>>(partial, g, 1, scal, S_RZNEW);
@@ -400,7 +407,7 @@ double estimate_lmax(nalu_ctx* ctx, const Mat<VT>& A, const T* dinv, T* a, T* b,
     cudaStreamSynchronize(ctx->stream);
   }
   double lam = 1.0;
-  for (int it = 0; it < 12; ++it) {
+  for (int it = 0; it < 30; ++it) {
     spmv_launch<VT, T, false>(ctx, A, a, b, nullptr);
     k_copy_scale<T><<<g, 256, 0, ctx->stream>>>(n, b, b, nullptr, dinv);
     k_multi_dot<T><<<g, kRedThreads, 0, ctx->stream>>>(n, 1, b, b, partial);
@@ -630,7 +637,7 @@ int run_inner(nalu_ctx* ctx, const nalu_solver_opts& o, T* r, T* x, T* z, T* p, 
     Cheb<float, T> ch;
     if (o.precond == NALU_PRECOND_CHEBYSHEV) {
       ch.degree = o.cheb_degree > 1 ? o.cheb_degree : 4;
-      ch.lmax = 1.05 * estimate_lmax<float, T>(ctx, A, dinv, ct1, ct2, ctx->sw.partial.p, ctx->sw.scal.p);
+      ch.lmax = 1.1 * estimate_lmax<float, T>(ctx, A, dinv, ct1, ct2, ctx->sw.partial.p, ctx->sw.scal.p);
       ch.lmin = ch.lmax / 30.0;
     }
     cudaMemsetAsync(x, 0, sizeof(T) * ctx->n_rows, ctx->stream);
@@ -642,7 +649,7 @@ int run_inner(nalu_ctx* ctx, const nalu_solver_opts& o, T* r, T* x, T* z, T* p, 
   Cheb<double, T> ch;
   if (o.precond == NALU_PRECOND_CHEBYSHEV) {
     ch.degree = o.cheb_degree > 1 ? o.cheb_degree : 4;
-    ch.lmax = 1.05 * estimate_lmax<double, T>(ctx, A, dinv, ct1, ct2, ctx->sw.partial.p, ctx->sw.scal.p);
+    ch.lmax = 1.1 * estimate_lmax<double, T>(ctx, A, dinv, ct1, ct2, ctx->sw.partial.p, ctx->sw.scal.p);
     ch.lmin = ch.lmax / 30.0;
   }
   cudaMemsetAsync(x, 0, sizeof(T) * ctx->n_rows, ctx->stream);

@@ -278,7 +278,13 @@ def test_negative_jacobian_reported(gpu_ctx_factory):
     ctx.field_set("scalar_q", np.zeros(c.shape[0]))
     ctx.field_set("diff_coeff", np.ones(c.shape[0]))
     ctx.build_elem_graph(1)
-    ctx.assemble(ng.KERNEL_SCALAR_DIFF)
+    with pytest.raises(ng.NaluError) as ei:
+        # the status surfaces at the first host synchronisation point
+        ctx.assemble(ng.KERNEL_SCALAR_DIFF)
+        ctx.load_complete()
+    assert ei.value.status == -4
+    # the context stays usable: explicit scatter, then the status again at loadComplete
+    ctx.assemble(ng.KERNEL_SCALAR_DIFF, ng.default_assemble_opts(scatter=ng.SCATTER_ATOMIC))
     with pytest.raises(ng.NaluError) as ei:
         ctx.load_complete()
     assert ei.value.status == -4
