@@ -189,6 +189,27 @@ int nalu_solution_set(nalu_ctx* ctx, const double* x, int src_is_device);
 /* y = A x with the context's matrix (FP64), host or device vectors */
 int nalu_spmv(nalu_ctx* ctx, const double* x, double* y, int is_device);
 
+/* Jacobi-preconditioned CG on a caller-owned CRS system, allocating no device
+ * memory.  This entry point has no counterpart in the reference.  It is for
+ * callers that cannot let a library call cudaMalloc: codes that hand their
+ * whole device-memory budget to their own pool allocator, so an allocation
+ * outside the pool would fail or fragment it, and time-step loops that must
+ * not allocate because cudaMalloc/cudaFree can synchronise the device.
+ * rowptr [n+1], colind, values, rhs and x are device pointers; x is
+ * overwritten with the solution (the solve starts from zero, with rows that
+ * are identity rows taking x = rhs), and the stop rule is the true FP64
+ * residual ||rhs - A x|| / ||rhs|| <= tol, as nalu_solve.  The scratch
+ * vectors live in one static device array sized for at most 262,144 rows
+ * (about 10.8 MB, held by every GPU that loads the library until the
+ * process exits); larger n returns NALU_ERR_CAPACITY.  The first call on a
+ * device looks up that array's device address and must therefore come before
+ * any stream capture on that device.  All calls on a device share the array:
+ * calls that overlap on the GPU race on it.  stream may be NULL (the legacy
+ * default stream); the call returns after the solve has finished. */
+int nalu_pcg_jacobi_noalloc(int64_t n, const int64_t* rowptr, const int32_t* colind,
+                            const double* values, const double* rhs, double* x, double tol,
+                            int max_iters, int* iterations, double* true_rel_res, void* stream);
+
 /* ---- measurement helpers ------------------------------------------------ */
 /* number of this library's kernel launches since the context was created */
 int64_t nalu_kernel_launch_count(const nalu_ctx* ctx);

@@ -15,9 +15,11 @@
 // symmetric for the continuity and diffusion operators.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdint>
+#include <mutex>
 #include <vector>
 
 #include "internal.h"
@@ -750,3 +752,141 @@ int solve(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* info) {
 }
 
 }  // namespace nalu_gb300
+
+// ---------------------------------------------------------------------------
+// Jacobi-PCG that allocates no device memory: nalu_pcg_jacobi_noalloc.
+//
+// Its scratch (residual, preconditioned residual, search direction, A*p,
+// inverse diagonal, block partial sums, device scalars and the identity-row
+// mask) lives in one file-scope device array of fixed size, sized for
+// kNoAllocMaxRows rows.  Every GPU that loads this library holds the array
+// (about 10.8 MB) until the process exits.  Host code cannot use the array's
+// name as a device address, so the first call on each device, with that
+// device current, looks its address up with cudaGetSymbolAddress and caches
+// it.  All calls on a device share the array, so calls whose work overlaps on
+// the GPU (different streams, or different host threads) race on it.
+// ---------------------------------------------------------------------------
+namespace nalu_gb300 {
+namespace {
+constexpr int64_t kNoAllocMaxRows = 262144;
+constexpr int64_t kNoAllocScalars = 16;
+constexpr int64_t kNoAllocDoubles = 5 * kNoAllocMaxRows + 2 * kRedBlocks + kNoAllocScalars;
+constexpr int64_t kNoAllocMaskDoubles = kNoAllocMaxRows / 8;  // one byte per row
+constexpr int kNoAllocMaxDevices = 64;
+}  // namespace
+
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocDoubles + kNoAllocMaskDoubles];
+
+namespace {
+std::mutex g_noalloc_mutex;
+double* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+// device address of the scratch array on the current device (looked up once)
+cudaError_t noalloc_scratch(int device, double** out) {
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_ptr[device]) {
+    double* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress((void**)&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    g_noalloc_ptr[device] = p;
+  }
+  *out = g_noalloc_ptr[device];
+  return cudaSuccess;
+}
+
+double read_scalar_on(cudaStream_t s, const double* d, cudaError_t* err) {
+  double h = 0.0;
+  *err = cudaMemcpyAsync(&h, d, sizeof(double), cudaMemcpyDeviceToHost, s);
+  if (*err == cudaSuccess) *err = cudaStreamSynchronize(s);
+  return h;
+}
+
+template <int TPR>
+void noalloc_cg_chunk(cudaStream_t s, int64_t n, const int64_t* rp, const int32_t* ci, const double* v, double* x,
+                      double* r, double* z, double* p, double* q, const double* dinv, double* partial, double* scal,
+                      int iters) {
+  const unsigned g = grid_for(n, kRedThreads);
+  for (int it = 0; it < iters; ++it) {
+    k_spmv<double, double, TPR, true><<<kRedBlocks, 256, 0, s>>>(n, rp, ci, v, p, q, partial);
+    k_finish<<<1, 256, 0, s>>>(partial, kRedBlocks, 1, scal, S_PQ);
+    k_alpha<<<1, 1, 0, s>>>(scal);
+    k_cg_update<double><<<g, kRedThreads, 0, s>>>(n, scal, x, p, r, q, z, dinv, partial, 1);
+    k_finish<<<1, 256, 0, s>>>(partial, g, 2, scal, S_RZNEW);
+    k_beta<<<1, 1, 0, s>>>(scal);
+    k_p_update<double><<<g, kRedThreads, 0, s>>>(n, scal, z, p);
+  }
+}
+}  // namespace
+
+}  // namespace nalu_gb300
+
+extern "C" int nalu_pcg_jacobi_noalloc(int64_t n, const int64_t* rowptr, const int32_t* colind, const double* values,
+                                       const double* rhs, double* x, double tol, int max_iters, int* iterations,
+                                       double* true_rel_res, void* stream) {
+  using namespace nalu_gb300;
+  if (n <= 0 || !rowptr || !colind || !values || !rhs || !x || !(tol > 0.0) || max_iters <= 0) return NALU_ERR_ARG;
+  if (n > kNoAllocMaxRows) return NALU_ERR_CAPACITY;
+  int device = 0;
+  if (cudaGetDevice(&device) != cudaSuccess || device < 0 || device >= kNoAllocMaxDevices) return NALU_ERR_NO_DEVICE;
+  double* base = nullptr;
+  if (noalloc_scratch(device, &base) != cudaSuccess) return NALU_ERR_CUDA;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int64_t M = kNoAllocMaxRows;
+  double *r = base, *z = base + M, *p = base + 2 * M, *q = base + 3 * M, *dinv = base + 4 * M;
+  double* partial = base + 5 * M;
+  double* scal = partial + 2 * kRedBlocks;
+  uint8_t* mask = reinterpret_cast<uint8_t*>(base + kNoAllocDoubles);
+  cudaError_t err = cudaMemsetAsync(scal, 0, sizeof(double) * kNoAllocScalars, s);
+  if (err != cudaSuccess) return NALU_ERR_CUDA;
+  const unsigned g256 = (unsigned)((n + 255) / 256);
+  const unsigned g = grid_for(n, kRedThreads);
+  k_dinv<double, double><<<g256, 256, 0, s>>>(n, rowptr, colind, values, dinv, mask);
+  k_init_x<<<g256, 256, 0, s>>>(n, x, rhs, mask, 1);
+  k_multi_dot<double><<<g, kRedThreads, 0, s>>>(n, 1, rhs, rhs, partial);
+  k_finish<<<1, 256, 0, s>>>(partial, g, 1, scal, S_BB);
+  int64_t nnz = 0;
+  err = cudaMemcpyAsync(&nnz, rowptr + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
+  const double bnorm = std::sqrt(read_scalar_on(s, scal + S_BB, &err));
+  if (err != cudaSuccess) return NALU_ERR_CUDA;
+  const bool wide = nnz > 40 * n;  // 3-dof rows (81 entries) use 16 threads per row
+  const double bref = bnorm > 0 ? bnorm : 1.0;
+  int total = 0;
+  double res = 0.0;
+  int status = NALU_OK;
+  for (int outer = 0; outer < 8; ++outer) {
+    k_residual<<<kRedBlocks, 256, 0, s>>>(n, rowptr, colind, values, x, rhs, r, partial);
+    k_finish<<<1, 256, 0, s>>>(partial, kRedBlocks, 1, scal, S_TMP);
+    const double r0 = std::sqrt(read_scalar_on(s, scal + S_TMP, &err));
+    if (err != cudaSuccess) return NALU_ERR_CUDA;
+    res = r0 / bref;
+    if (res <= tol || total >= max_iters) break;
+    const double stop = std::max(tol * bref * 0.5, 1e-15 * r0);
+    k_copy_scale<double><<<g256, 256, 0, s>>>(n, r, z, nullptr, dinv);
+    cudaMemcpyAsync(p, z, sizeof(double) * n, cudaMemcpyDeviceToDevice, s);
+    k_multi_dot<double><<<g, kRedThreads, 0, s>>>(n, 1, r, z, partial);
+    k_finish<<<1, 256, 0, s>>>(partial, g, 1, scal, S_RZ);
+    while (total < max_iters) {
+      const int chunk = std::min(25, max_iters - total);
+      if (wide) noalloc_cg_chunk<16>(s, n, rowptr, colind, values, x, r, z, p, q, dinv, partial, scal, chunk);
+      else noalloc_cg_chunk<8>(s, n, rowptr, colind, values, x, r, z, p, q, dinv, partial, scal, chunk);
+      total += chunk;
+      const double rr = read_scalar_on(s, scal + S_RR, &err);
+      const double bad = read_scalar_on(s, scal + S_BAD, &err);
+      if (err != cudaSuccess) return NALU_ERR_CUDA;
+      if (bad != 0.0 || !std::isfinite(rr)) {
+        status = NALU_ERR_NONFINITE;
+        break;
+      }
+      if (std::sqrt(rr) <= stop) break;
+    }
+    if (status != NALU_OK) break;
+  }
+  k_residual<<<kRedBlocks, 256, 0, s>>>(n, rowptr, colind, values, x, rhs, r, partial);
+  k_finish<<<1, 256, 0, s>>>(partial, kRedBlocks, 1, scal, S_TMP);
+  res = std::sqrt(read_scalar_on(s, scal + S_TMP, &err)) / bref;
+  if (err != cudaSuccess) return NALU_ERR_CUDA;
+  if (iterations) *iterations = total;
+  if (true_rel_res) *true_rel_res = res;
+  if (status != NALU_OK) return status;
+  return res <= tol ? NALU_OK : NALU_ERR_NOT_CONVERGED;
+}
