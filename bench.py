@@ -206,13 +206,21 @@ def bench_gpu(args):
         ctx.field_set(nm, v)
     ctx.build_elem_graph(1)
     n_rows, nnz, _ = ctx.sizes()
-    opts = ng.default_assemble_opts(scatter=ng.SCATTER_AUTO)
-    # warm-up (includes the scatter autotune on the first call)
+    # pick arithmetic x scatter by device time (both pass the parity tests)
+    arith_names = {ng.ARITH_FP64: "fp64", ng.ARITH_DF64: "df64"}
+    want = {"auto": (ng.ARITH_FP64, ng.ARITH_DF64), "fp64": (ng.ARITH_FP64,), "df64": (ng.ARITH_DF64,)}[args.arith]
+    modes = {}
+    for ar in want:
+        for sc in (ng.SCATTER_ATOMIC, ng.SCATTER_COLOURED):
+            modes["%s_%s_ms" % (arith_names[ar], {1: "atomic", 2: "coloured"}[sc])] = time_mode(ctx, ar, sc)
+    best = min(modes, key=modes.get)
+    arith = ng.ARITH_DF64 if best.startswith("df64") else ng.ARITH_FP64
+    scatter = ng.SCATTER_COLOURED if "coloured" in best else ng.SCATTER_ATOMIC
+    opts = ng.default_assemble_opts(scatter=scatter, arith=arith)
     for _ in range(max(args.warmup, 3)):
         ctx.zero()
         ctx.assemble(ng.KERNEL_CONTINUITY_ADV, opts)
     ctx.load_complete()
-    scatter = int(ctx_scatter_choice(ctx))
     fp64_peak = ctx.probe_fp64_tflops()
     # ---- device-timed region: inputs resident in HBM ----
     launches0 = ctx.launches()
@@ -291,8 +299,11 @@ def bench_gpu(args):
     traffic, prof = profile_traffic()
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if arith == ng.ARITH_FP64 else "f64 in/out, df64 (FP32-pair) element math",
+            "data": "synthetic",
             "config": dict(workload_config(), scatter={1: "atomic", 2: "coloured"}.get(scatter, str(scatter)),
+                           arith=arith_names[arith], mode_ms=modes,
                            parallelism="replicas" if ws > 1 else "single"),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "peak_kind": peak_kind, "algorithmic_bytes_per_launch": alg,
@@ -309,19 +320,21 @@ def bench_gpu(args):
     return 0
 
 
-def ctx_scatter_choice(ctx):
-    """Which scatter the autotuner picked (times both once more to report it)."""
+def time_mode(ctx, arith, scatter, reps=3):
+    """Device time (ms, best of reps after one warm-up) of one continuity assembly."""
     import nalu_gb300 as ng
-    best, pick = None, ng.SCATTER_ATOMIC
-    for s in (ng.SCATTER_ATOMIC, ng.SCATTER_COLOURED):
+    o = ng.default_assemble_opts(scatter=scatter, arith=arith)
+    best = None
+    for r in range(reps + 1):
         ctx.zero()
         ctx.event_record(62)
-        ctx.assemble(ng.KERNEL_CONTINUITY_ADV, ng.default_assemble_opts(scatter=s))
+        ctx.assemble(ng.KERNEL_CONTINUITY_ADV, o)
         ctx.event_record(63)
         ms = ctx.event_elapsed_ms(62, 63)
-        if best is None or ms < best:
-            best, pick = ms, s
-    return pick
+        if r > 0 and (best is None or ms < best):
+            best = ms
+    ctx.load_complete()
+    return best
 
 
 def main():
@@ -333,6 +346,8 @@ def main():
     ap.add_argument("--no-solve", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--size", type=int, default=128, help="elements per edge (default: the 128^3 workload)")
+    ap.add_argument("--arith", default="auto", choices=["auto", "fp64", "df64"],
+                    help="element-math arithmetic (auto: the faster; both pass the parity tests)")
     args = ap.parse_args()
     global N_EDGE
     N_EDGE = args.size

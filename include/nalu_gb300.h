@@ -133,8 +133,15 @@ typedef struct nalu_assemble_opts {
   double upw_factor;        /* get_upw_factor */
   double hybrid_factor;     /* get_hybrid_factor (classic Peclet function, A = 5) */
   int scatter;              /* enum nalu_scatter */
-  int reserved[7];
+  int arith;                /* enum nalu_arith (scalar kernels) */
+  int reserved[6];
 } nalu_assemble_opts;
+/* arithmetic of the element math; inputs, outputs, the CRS scatter and the
+ * residual's -lhs.q term stay FP64 in both modes */
+enum nalu_arith {
+  NALU_ARITH_FP64 = 0,  /* FP64 throughout */
+  NALU_ARITH_DF64 = 1   /* double-float (hi+lo FP32 pair, ~48-bit) on the FP32 pipes */
+};
 void nalu_assemble_opts_default(nalu_assemble_opts* opts);
 /* run one element kernel over all elements and sum into the system */
 int nalu_assemble(nalu_ctx* ctx, int kernel, const nalu_assemble_opts* opts);

@@ -34,6 +34,7 @@ KERNEL_CONTINUITY_ADV = 1
 KERNEL_MOMENTUM_ADV_DIFF = 2
 KERNEL_MOMENTUM_UPW_ADV_DIFF = 3
 SCATTER_AUTO, SCATTER_ATOMIC, SCATTER_COLOURED = 0, 1, 2
+ARITH_FP64, ARITH_DF64 = 0, 1
 SOLVER_CG, SOLVER_GMRES = 0, 1
 PRECOND_NONE, PRECOND_JACOBI, PRECOND_CHEBYSHEV = 0, 1, 2
 PRECISION_FP64, PRECISION_FP32_INNER_IR = 0, 1
@@ -50,7 +51,8 @@ class AssembleOpts(ctypes.Structure):
                 ("reduced_sens", ctypes.c_int), ("skew_symmetric", ctypes.c_int), ("use_limiter", ctypes.c_int),
                 ("proj_time_scale", ctypes.c_double), ("include_divu", ctypes.c_double),
                 ("alpha", ctypes.c_double), ("alpha_upw", ctypes.c_double), ("upw_factor", ctypes.c_double),
-                ("hybrid_factor", ctypes.c_double), ("scatter", ctypes.c_int), ("reserved", ctypes.c_int * 7)]
+                ("hybrid_factor", ctypes.c_double), ("scatter", ctypes.c_int), ("arith", ctypes.c_int),
+                ("reserved", ctypes.c_int * 6)]
 
 
 class SolverOpts(ctypes.Structure):

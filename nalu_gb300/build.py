@@ -16,7 +16,8 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
-SOURCES = ["api.cu", "assemble.cu", "momentum.cu", "krylov.cu"]
+SOURCES = ["api.cu", "assemble.cu", "assemble_df.cu", "assemble_df_sd.cu", "assemble_df_c0.cu", "assemble_df_c1.cu",
+           "assemble_df_c2.cu", "momentum.cu", "krylov.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -57,7 +58,9 @@ def build(verbose=False, ptxas_info=False):
     _run([nvcc] + ARCH + ["-shared", "-o", lib] + objs + ["-lcudart"])
     check = os.path.join(OUT, "libnalu_elemcheck.so")
     cxx = shutil.which("g++") or "g++"
-    _run([cxx, "-std=c++17", "-O2", "-fPIC", "-shared", "-o", check, os.path.join(CSRC, "elem_hostcheck.cpp")])
+    # -ffp-contract=off: the double-float sequences must not be fused
+    _run([cxx, "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-shared", "-o", check,
+          os.path.join(CSRC, "elem_hostcheck.cpp")])
     # C++ caller of the host interface (include/nalu_gb300.hpp)
     _run([cxx, "-std=c++17", "-O2", "-o", os.path.join(OUT, "heat_conduction"),
           os.path.join(HERE, "examples", "heat_conduction.cpp"), "-L" + OUT, "-lnalu_gb300",

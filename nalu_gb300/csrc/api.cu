@@ -156,6 +156,7 @@ int nalu_destroy(nalu_ctx* ctx) {
   ctx->d_slots.free();
   ctx->d_bcmask.free();
   ctx->d_colour_elems.free();
+  ctx->d_node_df.free();
   ctx->d_flags.free();
   ctx->flush_buf.free();
   for (auto& ev : ctx->user_ev)

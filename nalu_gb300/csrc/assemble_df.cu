@@ -1,0 +1,121 @@
+// assemble_df.cu -- the scalar assembly kernels (ScalarDiffElemKernel,
+// ContinuityAdvElemKernel) with the element math in double-float (df64) on
+// the FP32 pipes (hex8_elem_df.h).  FP64 stays where precision is set by the
+// inputs and outputs: coordinate differences, the -lhs.p residual term, the
+// conversion of element-matrix entries back to FP64 and the CRS scatter.
+//
+// A per-node pre-pass splits the nodal inputs once (w = rho u + tau Gpdx for
+// continuity, the diffusion coefficient for ScalarDiff) into df64, so the
+// element kernel gathers 8-byte df64 values instead of converting 8x per node.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "assemble_df.cuh"
+
+namespace nalu_gb300 {
+
+NALU_DF_VARIANTS(NALU_DF_EXTERN)
+
+__global__ void k_prepass_k_df(const double* __restrict__ k, df64* __restrict__ out, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = df_from_double(__ldg(k + i));
+}
+
+__global__ void k_prepass_w_df(const double* __restrict__ u, const double* __restrict__ gp,
+                               const double* __restrict__ rho, double tau, df64* __restrict__ out, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double r = __ldg(rho + i);
+#pragma unroll
+  for (int d = 0; d < 3; ++d) out[3 * i + d] = df_from_double(r * __ldg(u + 3 * i + d) + tau * __ldg(gp + 3 * i + d));
+}
+
+namespace {
+
+void launch_df(nalu_ctx* ctx, int kernel, const nalu_assemble_opts& o, const AsmArgsDF& a, int out) {
+  if (kernel == NALU_KERNEL_SCALAR_DIFF) {
+    if (o.shifted_grad_op) launch_df_variant<0, 0, true, false>(ctx, a, out);
+    else launch_df_variant<0, 0, false, false>(ctx, a, out);
+    return;
+  }
+  const int mode = o.shift_poisson ? 2 : (o.reduced_sens ? 1 : 0);
+  if (o.shift_mdot) {
+    if (mode == 0) launch_df_variant<1, 0, false, true>(ctx, a, out);
+    else if (mode == 1) launch_df_variant<1, 1, false, true>(ctx, a, out);
+    else launch_df_variant<1, 2, false, true>(ctx, a, out);
+  } else {
+    if (mode == 0) launch_df_variant<1, 0, false, false>(ctx, a, out);
+    else if (mode == 1) launch_df_variant<1, 1, false, false>(ctx, a, out);
+    else launch_df_variant<1, 2, false, false>(ctx, a, out);
+  }
+}
+
+// split the nodal inputs into df64 (scratch owned by the context)
+int prepass(nalu_ctx* ctx, int kernel, const nalu_assemble_opts& o, AsmArgsDF& a) {
+  const int64_t n = ctx->n_nodes;
+  const int64_t need = kernel == NALU_KERNEL_SCALAR_DIFF ? n : 3 * n;
+  if (ctx->d_node_df.n < need) NALU_CUDA(ctx, ctx->d_node_df.alloc(need));
+  df64* out = reinterpret_cast<df64*>(ctx->d_node_df.p);
+  if (kernel == NALU_KERNEL_SCALAR_DIFF) {
+    k_prepass_k_df<<<nblk_df(n, 256), 256, 0, ctx->stream>>>(ctx->fields[NALU_FIELD_DIFF_COEFF].d.p, out, n);
+  } else {
+    k_prepass_w_df<<<nblk_df(n, 256), 256, 0, ctx->stream>>>(ctx->fields[NALU_FIELD_VELOCITY].d.p,
+                                                          ctx->fields[NALU_FIELD_DPDX].d.p,
+                                                          ctx->fields[NALU_FIELD_DENSITY].d.p, o.proj_time_scale,
+                                                          out, n);
+  }
+  ctx->launches++;
+  a.nodal = out;
+  return cuda_check(ctx, cudaGetLastError(), "df64 prepass");
+}
+
+AsmArgsDF base_args_df(nalu_ctx* ctx, int kernel, const nalu_assemble_opts& o) {
+  AsmArgsDF a{};
+  a.conn = ctx->d_conn.p;
+  a.x = ctx->fields[NALU_FIELD_COORDINATES].d.p;
+  a.f_a = kernel == NALU_KERNEL_SCALAR_DIFF ? ctx->fields[NALU_FIELD_SCALAR_Q].d.p : ctx->fields[NALU_FIELD_PRESSURE].d.p;
+  a.inv_tau = df_from_double(1.0 / o.proj_time_scale);
+  a.rowptr = ctx->d_rowptr.p;
+  a.slots = ctx->d_slots.p;
+  a.values = ctx->d_values.p;
+  a.rhs = ctx->d_rhs.p;
+  a.flags = ctx->d_flags.p;
+  return a;
+}
+
+}  // namespace
+
+int launch_assemble_df(nalu_ctx* ctx, int kernel, const nalu_assemble_opts& o, int scatter) {
+  AsmArgsDF a = base_args_df(ctx, kernel, o);
+  int rc = prepass(ctx, kernel, o, a);
+  if (rc) return rc;
+  if (scatter == NALU_SCATTER_COLOURED) {
+    const int nc = (int)ctx->colour_offsets.size() - 1;
+    for (int c = 0; c < nc; ++c) {
+      AsmArgsDF ac = a;
+      ac.elems = ctx->d_colour_elems.p + ctx->colour_offsets[c];
+      ac.count = ctx->colour_offsets[c + 1] - ctx->colour_offsets[c];
+      launch_df(ctx, kernel, o, ac, 1);
+    }
+  } else {
+    a.count = ctx->n_elems;
+    launch_df(ctx, kernel, o, a, 0);
+  }
+  return cuda_check(ctx, cudaGetLastError(), "df64 assemble launch");
+}
+
+int launch_capture_df(nalu_ctx* ctx, int kernel, const nalu_assemble_opts& o, int64_t elem, double* d_lhs,
+                      double* d_rhs) {
+  AsmArgsDF a = base_args_df(ctx, kernel, o);
+  int rc = prepass(ctx, kernel, o, a);
+  if (rc) return rc;
+  a.count = 1;
+  a.cap_elem = elem;
+  a.cap_lhs = d_lhs;
+  a.cap_rhs = d_rhs;
+  launch_df(ctx, kernel, o, a, 2);
+  return cuda_check(ctx, cudaGetLastError(), "df64 capture launch");
+}
+
+}  // namespace nalu_gb300

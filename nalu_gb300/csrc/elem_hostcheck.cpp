@@ -81,3 +81,56 @@ void hc_mdot(const double* xin, const double* rho, const double* u, const double
   });
 }
 }
+
+// ---- double-float (df64) element math, as the df64 kernels run it ----
+#include "hex8_elem_df.h"
+
+extern "C" {
+
+void hc_scalar_diff_df(const double* xin, const double* q, const double* k, int shift, double* lhs,
+                       double* rhs) {
+  df64 kd[8], m[64];
+  for (int n = 0; n < 8; ++n) kd[n] = df_from_double(k[n]);
+  with_x(xin, [&](double (&x)[8][3]) {
+    ArrayAccDF acc{m};
+    if (shift) scalar_diff_lhs_df<true>(x, kd, acc);
+    else scalar_diff_lhs_df<false>(x, kd, acc);
+  });
+  for (int i = 0; i < 64; ++i) lhs[i] = df_to_double(m[i]);
+  for (int r = 0; r < 8; ++r) {
+    double s = 0.0;
+    for (int c = 0; c < 8; ++c) s += lhs[r * 8 + c] * q[c];
+    rhs[r] = -s;
+  }
+}
+
+void hc_continuity_df(const double* xin, const double* u, const double* rho, const double* p,
+                      const double* gp, double tau, int smdot, int spois, int reduced, double* lhs,
+                      double* rhs) {
+  df64 w[8][3], m[64], r8[8];
+  for (int n = 0; n < 8; ++n)
+    for (int d = 0; d < 3; ++d) w[n][d] = df_from_double(rho[n] * u[n * 3 + d] + tau * gp[n * 3 + d]);
+  const int mode = spois ? 2 : (reduced ? 1 : 0);
+  const df64 it = df_from_double(1.0 / tau);
+  with_x(xin, [&](double (&x)[8][3]) {
+    ArrayAccDF acc{m};
+    if (mode == 0) {
+      if (smdot) continuity_elem_df<0, true>(x, w, it, p, acc, r8);
+      else continuity_elem_df<0, false>(x, w, it, p, acc, r8);
+    } else if (mode == 1) {
+      if (smdot) continuity_elem_df<1, true>(x, w, it, p, acc, r8);
+      else continuity_elem_df<1, false>(x, w, it, p, acc, r8);
+    } else {
+      if (smdot) continuity_elem_df<2, true>(x, w, it, p, acc, r8);
+      else continuity_elem_df<2, false>(x, w, it, p, acc, r8);
+    }
+  });
+  for (int i = 0; i < 64; ++i) lhs[i] = df_to_double(m[i]);
+  for (int r = 0; r < 8; ++r) {
+    double s = df_to_double(r8[r]);
+    if (mode != 1)
+      for (int c = 0; c < 8; ++c) s -= lhs[r * 8 + c] * p[c];
+    rhs[r] = s;
+  }
+}
+}

@@ -80,6 +80,7 @@ struct nalu_ctx {
   nalu_gb300::DBuf<uint8_t> d_slots;     // [E][64] column offset in the node row
   nalu_gb300::DBuf<uint8_t> d_bcmask;    // 1 where the row was made an identity row
   nalu_gb300::DBuf<int32_t> d_colour_elems;  // element ids grouped by colour
+  nalu_gb300::DBuf<double> d_node_df;    // df64 split of nodal kernel inputs (8 B each)
   std::vector<int64_t> colour_offsets;   // [n_colours+1]
   int scatter_choice[4] = {0, 0, 0, 0};  // autotuned scatter per kernel (0 = not tuned)
 
@@ -112,6 +113,10 @@ int launch_assemble(nalu_ctx* ctx, int kernel, const nalu_assemble_opts& o, int 
 int launch_capture(nalu_ctx* ctx, int kernel, const nalu_assemble_opts& o, int64_t elem, double* d_lhs,
                    double* d_rhs);
 int launch_mdot(nalu_ctx* ctx, const nalu_assemble_opts& o);
+// assemble_df.cu (double-float element math for the scalar kernels)
+int launch_assemble_df(nalu_ctx* ctx, int kernel, const nalu_assemble_opts& o, int scatter);
+int launch_capture_df(nalu_ctx* ctx, int kernel, const nalu_assemble_opts& o, int64_t elem, double* d_lhs,
+                      double* d_rhs);
 int launch_slot_table(nalu_ctx* ctx);
 int launch_expand_graph(nalu_ctx* ctx);
 int launch_sum_into(nalu_ctx* ctx, int64_t n, const int64_t* d_elems, const double* d_lhs,

@@ -43,11 +43,14 @@ def elemcheck():
     hdr = os.path.join(ROOT, "nalu_gb300", "csrc", "hex8_elem.h")
     if not os.path.exists(out) or os.path.getmtime(out) < max(os.path.getmtime(src), os.path.getmtime(hdr)):
         os.makedirs(os.path.dirname(out), exist_ok=True)
-        subprocess.run(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-o", out, src], check=True)
+        subprocess.run(["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-shared", "-o", out, src],
+                       check=True)
     L = ctypes.CDLL(out)
     P = ctypes.c_void_p
     L.hc_scalar_diff.argtypes = [P, P, P, ctypes.c_int, P, P]
     L.hc_continuity.argtypes = [P] * 5 + [ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P]
+    L.hc_scalar_diff_df.argtypes = [P, P, P, ctypes.c_int, P, P]
+    L.hc_continuity_df.argtypes = [P] * 5 + [ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P]
     L.hc_mdot.argtypes = [P] * 5 + [ctypes.c_double, ctypes.c_int, ctypes.c_int, P]
     return L
 

@@ -77,3 +77,54 @@ def test_mdot_random_elements(elemcheck, oracle, sm, sp):
         m2 = np.zeros(12)
         elemcheck.hc_mdot(P(c), P(rho), P(u), P(p), P(gp), float(tau), sm, sp, P(m2))
         check_dense(m2[None], m1[None], what="mdot")
+
+
+# ---- double-float (df64) element math of the ARITH_DF64 kernels -------------
+def _hc_scalar_df(L, c, q, k, sh):
+    lhs, rhs = np.zeros(64), np.zeros(8)
+    L.hc_scalar_diff_df(P(np.ascontiguousarray(c)), P(q), P(k), int(sh), P(lhs), P(rhs))
+    return lhs.reshape(8, 8), rhs
+
+
+def _hc_cont_df(L, c, u, rho, p, gp, tau, sm, sp, rd):
+    lhs, rhs = np.zeros(64), np.zeros(8)
+    L.hc_continuity_df(P(np.ascontiguousarray(c)), P(np.ascontiguousarray(u)), P(rho), P(p),
+                       P(np.ascontiguousarray(gp)), float(tau), sm, sp, rd, P(lhs), P(rhs))
+    return lhs.reshape(8, 8), rhs
+
+
+def test_golds_through_df64_math(elemcheck, golds):
+    c, conn, gid = block_mesh(1, 1, 1)
+    e = conn[0]
+    lhs, rhs = _hc_scalar_df(elemcheck, c[e], TrigFields.temperature(c)[e], np.ones(8), 0)
+    assert np.max(np.abs(lhs.ravel() - golds["scalar_diff"]["lhs"])) <= 1e-15
+    for key, opts in [("continuity_default", (0, 0, 0)), ("continuity_reduced_sens", (0, 0, 1)),
+                      ("continuity_reduced_shift", (0, 1, 1))]:
+        lhs, rhs = _hc_cont_df(elemcheck, c[e], TrigFields.velocity(c)[e], np.ones(8), TrigFields.pressure(c)[e],
+                               TrigFields.dpdx(c)[e], 1.0, *opts)
+        assert np.max(np.abs(lhs.ravel() - golds[key]["lhs"])) <= 1e-15, key
+        assert np.max(np.abs(rhs - golds[key]["rhs"])) <= 1e-15, key
+
+
+@pytest.mark.parametrize("translate", [0.0, 1.0, 5.0])
+def test_df64_random_elements(elemcheck, oracle, translate):
+    """Elements of size 1/256..1/16 placed up to `translate` from the origin
+    (coordinates much larger than the element: the hardest case for the
+    hi+lo split, handled by FP64 differences to node 0)."""
+    rng = np.random.default_rng(40 + int(translate))
+    for t in range(200):
+        h = rng.uniform(1 / 256, 1 / 16)
+        c = (BASE + 0.2 * rng.uniform(-1, 1, (8, 3))) * h + rng.uniform(0, translate, 3)
+        q, k = rng.uniform(0, 1, 8), rng.uniform(0.5, 2, 8)
+        for sh in (0, 1):
+            l1, r1 = oracle.scalar_diff_elem(c, q, k, sh)
+            l2, r2 = _hc_scalar_df(elemcheck, c, q, k, sh)
+            check_dense(l2, l1, what="df64 lhs")
+            check_dense(r2[None], r1[None], what="df64 rhs")
+        u, gp = rng.normal(size=(8, 3)), rng.normal(size=(8, 3))
+        rho, p, tau = rng.uniform(0.5, 2, 8), rng.normal(size=8), rng.uniform(0.1, 2)
+        for opts in [(0, 0, 0), (0, 0, 1), (0, 1, 1), (1, 0, 0)]:
+            l1, r1 = oracle.continuity_adv_elem(c, u, rho, p, gp, tau, *opts)
+            l2, r2 = _hc_cont_df(elemcheck, c, u, rho, p, gp, tau, *opts)
+            check_dense(l2, l1, what="df64 continuity lhs %s" % (opts,))
+            check_dense(r2[None], r1[None], what="df64 continuity rhs %s" % (opts,))

@@ -289,3 +289,74 @@ def test_negative_jacobian_reported(gpu_ctx_factory):
         ctx.load_complete()
     assert ei.value.status == -4
     ctx.close()
+
+
+# ---------------------------------------------------------------------------
+# double-float element math (ARITH_DF64) against the FP64 oracle
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("scatter", [ng.SCATTER_ATOMIC, ng.SCATTER_COLOURED])
+def test_df64_scalar_diff_32cube(gpu_ctx_factory, oracle, scatter):
+    c, conn, gid = block_mesh(32, jitter=0.1, seed=11)
+    rng = np.random.default_rng(12)
+    T, k = rng.uniform(0, 1, c.shape[0]), rng.uniform(0.5, 2.0, c.shape[0])
+    ctx = _ctx(gpu_ctx_factory, c, conn, gid)
+    ctx.field_set("scalar_q", T)
+    ctx.field_set("diff_coeff", k)
+    ctx.build_elem_graph(1)
+    rp, ci = ctx.graph()
+    _, _, lid = oracle.graph(c.shape[0], conn, 1, gid)
+    for shifted in (0, 1):
+        ctx.zero()
+        ctx.assemble(ng.KERNEL_SCALAR_DIFF, ng.default_assemble_opts(scatter=scatter, shifted_grad_op=shifted,
+                                                                     arith=ng.ARITH_DF64))
+        ctx.load_complete()
+        vals, rhs = ctx.system()
+        ov, orhs = oracle.assemble(oracle.KERNEL_SCALAR_DIFF, c, conn, rp, ci, lid, scalar=T, coeff=k,
+                                   opts=oracle.opts_block(shifted_grad_op=shifted), n_threads=8)
+        check_csr_values(vals, ov, rp, what="df64 values")
+        check_vec(rhs, orhs, what="df64 rhs")
+    ctx.close()
+
+
+@pytest.mark.parametrize("kw", [{}, {"reduced_sens": 1}, {"reduced_sens": 1, "shift_poisson": 1},
+                                {"shift_mdot": 1}, {"proj_time_scale": 0.37}])
+def test_df64_continuity(gpu_ctx_factory, oracle, kw):
+    c, conn, gid = block_mesh(12, 10, 9, jitter=0.1, seed=3, z_ratio=1.05)
+    u, rho, p, gp = continuity_fields(c, seed=4)
+    ctx = _ctx(gpu_ctx_factory, c, conn, gid)
+    for n, v in (("velocity", u), ("density", rho), ("pressure", p), ("dpdx", gp)):
+        ctx.field_set(n, v)
+    ctx.build_elem_graph(1)
+    ctx.zero()
+    ctx.assemble(ng.KERNEL_CONTINUITY_ADV, ng.default_assemble_opts(arith=ng.ARITH_DF64, **kw))
+    ctx.load_complete()
+    vals, rhs = ctx.system()
+    rp, ci = ctx.graph()
+    _, _, lid = oracle.graph(c.shape[0], conn, 1, gid)
+    o = oracle.opts_block(shift_mdot=kw.get("shift_mdot", 0), shift_poisson=kw.get("shift_poisson", 0),
+                          reduced_sens=kw.get("reduced_sens", 0), proj_time_scale=kw.get("proj_time_scale", 1.0))
+    ov, orhs = oracle.assemble(oracle.KERNEL_CONTINUITY_ADV, c, conn, rp, ci, lid, scalar=p, coeff=rho, vec=u,
+                               vec2=gp, opts=o, n_threads=8)
+    check_csr_values(vals, ov, rp, what="df64 values")
+    check_vec(rhs, orhs, what="df64 rhs")
+    ctx.close()
+
+
+def test_df64_golds_capture(gpu_ctx_factory, golds):
+    c, conn, gid = block_mesh(1, 1, 1)
+    ctx = _ctx(gpu_ctx_factory, c, conn)
+    ctx.field_set("scalar_q", TrigFields.temperature(c))
+    ctx.field_set("diff_coeff", np.ones(8))
+    lhs, rhs = ctx.capture_element(ng.KERNEL_SCALAR_DIFF, 0, ng.default_assemble_opts(arith=ng.ARITH_DF64))
+    assert np.max(np.abs(lhs.ravel() - golds["scalar_diff"]["lhs"])) <= 1e-15
+    ctx.field_set("velocity", TrigFields.velocity(c))
+    ctx.field_set("density", np.ones(8))
+    ctx.field_set("pressure", TrigFields.pressure(c))
+    ctx.field_set("dpdx", TrigFields.dpdx(c))
+    for key, kw in [("continuity_default", {}), ("continuity_reduced_sens", {"reduced_sens": 1}),
+                    ("continuity_reduced_shift", {"reduced_sens": 1, "shift_poisson": 1})]:
+        lhs, rhs = ctx.capture_element(ng.KERNEL_CONTINUITY_ADV, 0,
+                                       ng.default_assemble_opts(arith=ng.ARITH_DF64, **kw))
+        assert np.max(np.abs(lhs.ravel() - golds[key]["lhs"])) <= 1e-15, key
+        assert np.max(np.abs(rhs - golds[key]["rhs"])) <= 1e-15, key
+    ctx.close()
