@@ -164,6 +164,11 @@ int nalu_destroy(nalu_ctx* ctx) {
   auto& s = ctx->sw;
   for (auto* b : {&s.r, &s.z, &s.p, &s.q, &s.ap, &s.dinv, &s.w, &s.tmp, &s.V, &s.Hbuf, &s.scal, &s.partial}) b->free();
   for (auto* b : {&s.fvals, &s.fr, &s.fz, &s.fp, &s.fq, &s.fdinv, &s.fx, &s.fV}) b->free();
+  s.sell.ptr.free();
+  s.sell.len.free();
+  s.sell.col.free();
+  s.sell.vald.free();
+  s.sell.valf.free();
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);

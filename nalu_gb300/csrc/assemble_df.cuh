@@ -83,7 +83,10 @@ __global__ void __launch_bounds__(kAsmBlockDF) k_assemble_scalar_df(AsmArgsDF a)
     for (int n = 0; n < 8; ++n)
 #pragma unroll
       for (int d = 0; d < 3; ++d) w[n][d] = a.nodal[3 * (int64_t)nd[n] + d];
-    mindet = continuity_elem_df<MODE, SMDOT>(x, w, a.inv_tau, pv, acc, rhs_df);
+    df64 pd[8];
+#pragma unroll
+    for (int n = 0; n < 8; ++n) pd[n] = df_split_bits(pv[n]);
+    mindet = continuity_elem_df<MODE, SMDOT>(x, w, a.inv_tau, pd, acc, rhs_df);
   }
   if (!(mindet > 1.0e-50)) atomicAdd(a.flags + FLAG_NEG_JAC, 1);
   const bool rhs_from_lhs = (KIND == 0) || (MODE != 1);
@@ -91,10 +94,10 @@ __global__ void __launch_bounds__(kAsmBlockDF) k_assemble_scalar_df(AsmArgsDF a)
   if (OUT == 2) {
 #pragma unroll
     for (int r = 0; r < 8; ++r) {
-      double s = df_to_double(rhs_df[r]);
+      double s = df_to_double_bits(rhs_df[r]);
 #pragma unroll
       for (int c = 0; c < 8; ++c) {
-        const double v = df_to_double(acc.get(r, c));
+        const double v = df_to_double_bits(acc.get(r, c));
         a.cap_lhs[r * 8 + c] = v;
         if (rhs_from_lhs) s -= v * pv[c];
       }
@@ -107,12 +110,12 @@ __global__ void __launch_bounds__(kAsmBlockDF) k_assemble_scalar_df(AsmArgsDF a)
   for (int r = 0; r < 8; ++r) {
     const int64_t base = __ldg(a.rowptr + nd[r]);
     const uint2 o2 = __ldg(reinterpret_cast<const uint2*>(sl + 8 * r));
-    double s = df_to_double(rhs_df[r]);
+    double s = df_to_double_bits(rhs_df[r]);
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
       const uint32_t word = c < 4 ? o2.x : o2.y;
       const int off = (word >> (8 * (c & 3))) & 0xff;
-      const double v = df_to_double(acc.get(r, c));
+      const double v = df_to_double_bits(acc.get(r, c));
       if (rhs_from_lhs) s -= v * pv[c];
       double* dst = a.values + base + off;
       if (OUT == 0) atomicAdd(dst, v);

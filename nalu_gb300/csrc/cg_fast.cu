@@ -1,0 +1,312 @@
+// cg_fast.cu -- Jacobi-preconditioned CG with two kernels per iteration on a
+// sliced-ELL copy of the CRS matrix.
+//
+// Layout: SELL-32 (slices of 32 consecutive rows; entry k of every row of a
+// slice stored contiguously, so one thread per row reads coalesced; rows
+// shorter than the slice are padded with their own diagonal index and 0).
+// The copy is made once per solve from the assembled CRS values (FP64 or
+// FP32 for the mixed-precision inner solve).
+//
+// Iteration k (rz_k = r_k . z_k, z_k = D^-1 r_k):
+//   K1  beta = rz_k / rz_{k-1};  p_k = z_k + beta p_{k-1} (formed on the fly
+//       for every gathered column);  q = A p_k;  partial sums of p_k . q
+//   K2  alpha = rz_k / (p_k . q);  x += alpha p_k;  r -= alpha q;
+//       z = D^-1 r;  partial sums of r.z and r.r
+// Every block re-reduces the previous kernel's 1024 partials in the same
+// order, so all blocks use bit-identical alpha/beta and no scalar kernel or
+// host round trip sits between K1 and K2.  Buffers alternate between even and
+// odd iterations; a chunk of iterations is captured once into a CUDA graph.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+#include <vector>
+
+#include "internal.h"
+
+namespace nalu_gb300 {
+
+constexpr int kSlice = 32;
+constexpr int kCgBlocks = 1024;
+constexpr int kCgThreads = 256;
+
+namespace {
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// sum of `n` partials, identical in every block (fixed order), broadcast
+__device__ __forceinline__ double block_total(const double* __restrict__ part, int n, double* sh) {
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += part[i];
+  s = warp_sum_d(s);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) sh[w] = s;
+  __syncthreads();
+  if (w == 0) {
+    double t = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0.0;
+    t = warp_sum_d(t);
+    if (lane == 0) sh[32] = t;
+  }
+  __syncthreads();
+  const double total = sh[32];
+  __syncthreads();
+  return total;
+}
+
+__device__ __forceinline__ void block_store(double v, double* __restrict__ out, double* sh) {
+  v = warp_sum_d(v);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    double t = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0.0;
+    t = warp_sum_d(t);
+    if (lane == 0) *out = t;
+  }
+  __syncthreads();
+}
+
+// slice lengths (max row length in each slice of 32 rows)
+__global__ void k_sell_len(int64_t n, const int64_t* __restrict__ rp, int32_t* __restrict__ slen, int64_t nslices) {
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
+  const int lane = threadIdx.x & 31;
+  if (gw >= nslices) return;
+  const int64_t row = gw * kSlice + lane;
+  int len = row < n ? (int)(rp[row + 1] - rp[row]) : 0;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) len = max(len, __shfl_xor_sync(0xffffffffu, len, o));
+  if (lane == 0) slen[gw] = len;
+}
+
+template <class VT>
+__global__ void k_sell_fill(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                            const double* __restrict__ v, const int64_t* __restrict__ sptr,
+                            const int32_t* __restrict__ slen, int32_t* __restrict__ scol, VT* __restrict__ sval) {
+  const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t s = row / kSlice;
+  const int lane = (int)(row % kSlice);
+  if (row >= n) return;
+  const int64_t b = rp[row], len = rp[row + 1] - b;
+  const int sl = slen[s];
+  const int64_t base = sptr[s] + lane;
+  for (int k = 0; k < sl; ++k) {
+    const bool real = k < len;
+    scol[base + (int64_t)k * kSlice] = real ? ci[b + k] : (int32_t)row;
+    sval[base + (int64_t)k * kSlice] = real ? (VT)v[b + k] : (VT)0;
+  }
+}
+
+// z = D^-1 r ; partials of r.z and r.r
+template <class T>
+__global__ void __launch_bounds__(kCgThreads) k_cg_init(int64_t n, const T* __restrict__ r, const T* __restrict__ dinv,
+                                                        T* __restrict__ z, double* __restrict__ rz_part,
+                                                        double* __restrict__ rr_part) {
+  __shared__ double sh[33];
+  double rz = 0.0, rr = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double ri = (double)r[i];
+    const double zi = (double)dinv[i] * ri;
+    z[i] = (T)zi;
+    rz += ri * zi;
+    rr += ri * ri;
+  }
+  block_store(rz, rz_part + blockIdx.x, sh);
+  block_store(rr, rr_part + blockIdx.x, sh);
+}
+
+template <class T, class VT>
+__global__ void __launch_bounds__(kCgThreads) k_cg_spmv(int64_t n, int64_t nrows_padded, const int64_t* __restrict__ sptr,
+                                                        const int32_t* __restrict__ slen, const int32_t* __restrict__ scol,
+                                                        const VT* __restrict__ sval, const T* __restrict__ z,
+                                                        const T* __restrict__ p_old, T* __restrict__ p_new,
+                                                        T* __restrict__ q, const double* __restrict__ rz_cur,
+                                                        const double* __restrict__ rz_prev, int first,
+                                                        double* __restrict__ pq_part) {
+  __shared__ double sh[33];
+  double beta = 0.0;
+  if (!first) {
+    const double a = block_total(rz_cur, kCgBlocks, sh);
+    const double b = block_total(rz_prev, kCgBlocks, sh);
+    beta = a / b;
+  }
+  double dot = 0.0;
+  for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < nrows_padded;
+       row += (int64_t)gridDim.x * blockDim.x) {
+    if (row >= n) continue;
+    const int64_t s = row / kSlice;
+    const int len = __ldg(slen + s);
+    const int64_t base = __ldg(sptr + s) + (row % kSlice);
+    double acc = 0.0;
+    if (first) {
+      for (int k = 0; k < len; ++k) {
+        const int32_t c = __ldg(scol + base + (int64_t)k * kSlice);
+        acc += (double)__ldg(sval + base + (int64_t)k * kSlice) * (double)__ldg(z + c);
+      }
+    } else {
+      for (int k = 0; k < len; ++k) {
+        const int32_t c = __ldg(scol + base + (int64_t)k * kSlice);
+        const double pc = (double)__ldg(z + c) + beta * (double)__ldg(p_old + c);
+        acc += (double)__ldg(sval + base + (int64_t)k * kSlice) * pc;
+      }
+    }
+    const double pi = first ? (double)z[row] : (double)z[row] + beta * (double)p_old[row];
+    p_new[row] = (T)pi;
+    q[row] = (T)acc;
+    dot += pi * acc;
+  }
+  block_store(dot, pq_part + blockIdx.x, sh);
+}
+
+template <class T>
+__global__ void __launch_bounds__(kCgThreads) k_cg_axpy(int64_t n, T* __restrict__ x, const T* __restrict__ p,
+                                                        T* __restrict__ r, const T* __restrict__ q,
+                                                        T* __restrict__ z, const T* __restrict__ dinv,
+                                                        const double* __restrict__ rz_cur,
+                                                        const double* __restrict__ pq_part,
+                                                        double* __restrict__ rz_next, double* __restrict__ rr_part) {
+  __shared__ double sh[33];
+  const double rz = block_total(rz_cur, kCgBlocks, sh);
+  const double pq = block_total(pq_part, kCgBlocks, sh);
+  const double alpha = rz / pq;
+  double rzn = 0.0, rr = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    x[i] = (T)((double)x[i] + alpha * (double)p[i]);
+    const double ri = (double)r[i] - alpha * (double)q[i];
+    r[i] = (T)ri;
+    const double zi = (double)dinv[i] * ri;
+    z[i] = (T)zi;
+    rzn += ri * zi;
+    rr += ri * ri;
+  }
+  block_store(rzn, rz_next + blockIdx.x, sh);
+  block_store(rr, rr_part + blockIdx.x, sh);
+}
+
+template <class T, class VT>
+void cg_iteration(nalu_ctx* ctx, int k, int first, int64_t n, int64_t npad, const int64_t* sptr, const int32_t* slen,
+                  const int32_t* scol, const VT* sval, T* x, T* r, T* z, T* pbuf[2], T* q, const T* dinv,
+                  double* rzbuf[2], double* pq_part, double* rr_part) {
+  const int cur = k & 1, prev = cur ^ 1;
+  k_cg_spmv<T, VT><<<kCgBlocks, kCgThreads, 0, ctx->stream>>>(n, npad, sptr, slen, scol, sval, z, pbuf[prev],
+                                                              pbuf[cur], q, rzbuf[cur], rzbuf[prev], first, pq_part);
+  k_cg_axpy<T><<<kCgBlocks, kCgThreads, 0, ctx->stream>>>(n, x, pbuf[cur], r, q, z, dinv, rzbuf[cur], pq_part,
+                                                          rzbuf[prev], rr_part);
+  ctx->launches += 2;
+}
+
+}  // namespace
+
+// Build the SELL-32 copy of the context's matrix (values as VT).
+template <class VT>
+int sell_build(nalu_ctx* ctx, SellMatrix& S, const VT** vals_out) {
+  const int64_t n = ctx->n_rows;
+  const int64_t ns = (n + kSlice - 1) / kSlice;
+  if (S.len.n < ns) NALU_CUDA(ctx, S.len.alloc(ns));
+  if (S.ptr.n < ns + 1) NALU_CUDA(ctx, S.ptr.alloc(ns + 1));
+  k_sell_len<<<(unsigned)((ns * 32 + 255) / 256), 256, 0, ctx->stream>>>(n, ctx->d_rowptr.p, S.len.p, ns);
+  ctx->launches++;
+  std::vector<int32_t> hl(ns);
+  NALU_CUDA(ctx, cudaMemcpyAsync(hl.data(), S.len.p, sizeof(int32_t) * ns, cudaMemcpyDeviceToHost, ctx->stream));
+  NALU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  std::vector<int64_t> hp(ns + 1, 0);
+  for (int64_t s = 0; s < ns; ++s) hp[s + 1] = hp[s] + (int64_t)hl[s] * kSlice;
+  const int64_t total = hp[ns];
+  NALU_CUDA(ctx, cudaMemcpyAsync(S.ptr.p, hp.data(), sizeof(int64_t) * (ns + 1), cudaMemcpyHostToDevice, ctx->stream));
+  if (S.col.n < total) NALU_CUDA(ctx, S.col.alloc(total));
+  VT* vals = nullptr;
+  if constexpr (sizeof(VT) == 8) {
+    if (S.vald.n < total) NALU_CUDA(ctx, S.vald.alloc(total));
+    vals = reinterpret_cast<VT*>(S.vald.p);
+  } else {
+    if (S.valf.n < total) NALU_CUDA(ctx, S.valf.alloc(total));
+    vals = reinterpret_cast<VT*>(S.valf.p);
+  }
+  k_sell_fill<VT><<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(n, ctx->d_rowptr.p, ctx->d_colind.p,
+                                                                        ctx->d_values.p, S.ptr.p, S.len.p, S.col.p,
+                                                                        vals);
+  ctx->launches++;
+  S.nslices = ns;
+  S.stored = total;
+  *vals_out = vals;
+  NALU_CUDA(ctx, cudaMemcpyAsync(S.ptr.p, hp.data(), sizeof(int64_t) * (ns + 1), cudaMemcpyHostToDevice, ctx->stream));
+  NALU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return cuda_check(ctx, cudaGetLastError(), "sell build");
+}
+
+// Jacobi-CG on A x = r (x from 0), vectors of type T, matrix values VT.
+// r holds the initial residual; on return x holds the solution increment.
+template <class T, class VT>
+int pcg_fast(nalu_ctx* ctx, const VT* sval, const SellMatrix& S, T* x, T* r, T* z, T* p0, T* p1, T* q,
+             const T* dinv, double rtol, double r0norm, int max_it, int check_every, int* iters_out) {
+  const int64_t n = ctx->n_rows;
+  const int64_t npad = S.nslices * kSlice;
+  DBuf<double>& part = ctx->sw.partial;
+  if (part.n < 4 * kCgBlocks) NALU_CUDA(ctx, part.alloc(4 * kCgBlocks));
+  double* rzbuf[2] = {part.p, part.p + kCgBlocks};
+  double* pq_part = part.p + 2 * kCgBlocks;
+  double* rr_part = part.p + 3 * kCgBlocks;
+  T* pbuf[2] = {p0, p1};
+  NALU_CUDA(ctx, cudaMemsetAsync(x, 0, sizeof(T) * n, ctx->stream));
+  k_cg_init<T><<<kCgBlocks, kCgThreads, 0, ctx->stream>>>(n, r, dinv, z, rzbuf[0], rr_part);
+  ctx->launches++;
+  // iteration 0 (p_0 = z_0) outside the graph
+  cg_iteration<T, VT>(ctx, 0, 1, n, npad, S.ptr.p, S.len.p, S.col.p, sval, x, r, z, pbuf, q, dinv, rzbuf, pq_part,
+                      rr_part);
+  int chunk = check_every > 0 ? check_every : 50;
+  chunk += chunk & 1;  // even: the buffer pattern repeats every two iterations
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaError_t ce = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+  if (ce != cudaSuccess) return cuda_check(ctx, ce, "begin capture");
+  for (int k = 1; k <= chunk; ++k)
+    cg_iteration<T, VT>(ctx, k, 0, n, npad, S.ptr.p, S.len.p, S.col.p, sval, x, r, z, pbuf, q, dinv, rzbuf, pq_part,
+                        rr_part);
+  ce = cudaStreamEndCapture(ctx->stream, &graph);
+  if (ce != cudaSuccess) return cuda_check(ctx, ce, "end capture");
+  ce = cudaGraphInstantiate(&exec, graph, 0);
+  if (ce != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    return cuda_check(ctx, ce, "instantiate");
+  }
+  std::vector<double> hrr(kCgBlocks);
+  int it = 1, rc = NALU_OK;
+  const double stop = rtol * r0norm;
+  auto converged = [&](bool* bad) {
+    cudaMemcpyAsync(hrr.data(), rr_part, sizeof(double) * kCgBlocks, cudaMemcpyDeviceToHost, ctx->stream);
+    if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
+      *bad = true;
+      return false;
+    }
+    double s = 0.0;
+    for (double v : hrr) s += v;
+    *bad = !std::isfinite(s);
+    return std::sqrt(s) <= stop;
+  };
+  bool bad = false;
+  if (!converged(&bad) && !bad) {
+    while (it < max_it) {
+      cudaGraphLaunch(exec, ctx->stream);
+      it += chunk;
+      if (converged(&bad) || bad) break;
+    }
+  }
+  cudaGraphExecDestroy(exec);
+  cudaGraphDestroy(graph);
+  *iters_out = it;
+  if (bad) return set_error(ctx, NALU_ERR_NONFINITE, "CG breakdown (non-finite residual)");
+  if (it >= max_it) return NALU_ERR_NOT_CONVERGED;
+  return rc;
+}
+
+template int sell_build<double>(nalu_ctx*, SellMatrix&, const double**);
+template int sell_build<float>(nalu_ctx*, SellMatrix&, const float**);
+template int pcg_fast<double, double>(nalu_ctx*, const double*, const SellMatrix&, double*, double*, double*, double*,
+                                      double*, double*, const double*, double, double, int, int, int*);
+template int pcg_fast<float, float>(nalu_ctx*, const float*, const SellMatrix&, float*, float*, float*, float*,
+                                    float*, float*, const float*, double, double, int, int, int*);
+
+}  // namespace nalu_gb300

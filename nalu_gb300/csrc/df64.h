@@ -9,6 +9,8 @@
 #pragma once
 
 #include <cmath>
+#include <cstdint>
+#include <cstring>
 
 #ifdef __CUDACC__
 #define DF_HD __host__ __device__ __forceinline__
@@ -53,6 +55,71 @@ DF_HD df64 df_from_double(double x) {
   return {hi, lo};
 }
 DF_HD double df_to_double(df64 a) { return (double)a.hi + (double)a.lo; }
+
+// ---- conversions by integer bit manipulation (no FP64 instructions) ----
+#ifdef __CUDA_ARCH__
+DF_HD uint64_t d2u(double d) { return (uint64_t)__double_as_longlong(d); }
+DF_HD double u2d(uint64_t u) { return __longlong_as_double((long long)u); }
+DF_HD uint32_t f2u(float f) { return __float_as_uint(f); }
+DF_HD float u2f(uint32_t u) { return __uint_as_float(u); }
+DF_HD int clz32(uint32_t v) { return __clz(v); }
+#else
+DF_HD uint64_t d2u(double d) { uint64_t u; std::memcpy(&u, &d, 8); return u; }
+DF_HD double u2d(uint64_t u) { double d; std::memcpy(&d, &u, 8); return d; }
+DF_HD uint32_t f2u(float f) { uint32_t u; std::memcpy(&u, &f, 4); return u; }
+DF_HD float u2f(uint32_t u) { float f; std::memcpy(&f, &u, 4); return f; }
+DF_HD int clz32(uint32_t v) { return v ? __builtin_clz(v) : 32; }
+#endif
+
+// Exact widening of a float to a double (normal floats; zero and float
+// subnormals, |f| < 2^-126, map to zero).
+DF_HD double f2d_bits(float f) {
+  const uint32_t u = f2u(f);
+  const uint32_t e = (u >> 23) & 0xff;
+  if (e == 0) return 0.0;
+  const uint64_t sign = (uint64_t)(u >> 31) << 63;
+  const uint64_t exp = (uint64_t)(e - 127 + 1023) << 52;
+  return u2d(sign | exp | ((uint64_t)(u & 0x7fffff) << 29));
+}
+
+// hi + lo as a double: both widen exactly and their sum (<= 48 significant
+// bits) is exact in FP64, so one FP64 add is the only FP64 instruction.
+DF_HD double df_to_double_bits(df64 a) { return f2d_bits(a.hi) + f2d_bits(a.lo); }
+
+// Split a double into hi (nearest float) + lo (the remaining significand
+// bits, truncated to 24) with integer instructions only.  |d| must lie in
+// [2^-100, 2^127); smaller magnitudes return 0 (below anything the
+// element math sees relative to its inputs), which keeps lo a normal float.
+DF_HD df64 df_split_bits(double d) {
+  const uint64_t b = d2u(d);
+  const int e = (int)((b >> 52) & 0x7ff);
+  const int E = e - 1023;
+  if (e == 0 || E < -100) return {0.0f, 0.0f};
+  const uint32_t sgn = (uint32_t)(b >> 32) & 0x80000000u;
+  const uint64_t sig = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);  // 53 bits
+  uint32_t hs = (uint32_t)(sig >> 29);                              // top 24 bits
+  int32_t rem = (int32_t)(sig & ((1ull << 29) - 1));                // low 29 bits
+  if (rem >= (1 << 28)) {                                           // round hi to nearest
+    hs += 1;
+    rem -= (1 << 29);
+  }
+  int Eh = E;
+  if (hs == (1u << 24)) {
+    hs >>= 1;
+    Eh += 1;
+  }
+  const float hi = u2f(sgn | ((uint32_t)(Eh + 127) << 23) | (hs & 0x7fffffu));
+  float lo = 0.0f;
+  if (rem != 0) {
+    const uint32_t lsgn = rem < 0 ? (sgn ^ 0x80000000u) : sgn;
+    const uint32_t ar = (uint32_t)(rem < 0 ? -rem : rem);
+    const int msb = 31 - clz32(ar);
+    const uint32_t mant = msb > 23 ? (ar >> (msb - 23)) : (ar << (23 - msb));
+    const int el = msb + E - 52 + 127;
+    if (el > 0) lo = u2f(lsgn | ((uint32_t)el << 23) | (mant & 0x7fffffu));
+  }
+  return {hi, lo};
+}
 DF_HD df64 df_zero() { return {0.0f, 0.0f}; }
 
 DF_HD df64 df_neg(df64 a) { return {-a.hi, -a.lo}; }

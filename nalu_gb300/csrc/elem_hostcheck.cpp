@@ -96,7 +96,7 @@ void hc_scalar_diff_df(const double* xin, const double* q, const double* k, int 
     if (shift) scalar_diff_lhs_df<true>(x, kd, acc);
     else scalar_diff_lhs_df<false>(x, kd, acc);
   });
-  for (int i = 0; i < 64; ++i) lhs[i] = df_to_double(m[i]);
+  for (int i = 0; i < 64; ++i) lhs[i] = df_to_double_bits(m[i]);
   for (int r = 0; r < 8; ++r) {
     double s = 0.0;
     for (int c = 0; c < 8; ++c) s += lhs[r * 8 + c] * q[c];
@@ -107,27 +107,28 @@ void hc_scalar_diff_df(const double* xin, const double* q, const double* k, int 
 void hc_continuity_df(const double* xin, const double* u, const double* rho, const double* p,
                       const double* gp, double tau, int smdot, int spois, int reduced, double* lhs,
                       double* rhs) {
-  df64 w[8][3], m[64], r8[8];
+  df64 w[8][3], m[64], r8[8], pd[8];
   for (int n = 0; n < 8; ++n)
     for (int d = 0; d < 3; ++d) w[n][d] = df_from_double(rho[n] * u[n * 3 + d] + tau * gp[n * 3 + d]);
+  for (int n = 0; n < 8; ++n) pd[n] = df_split_bits(p[n]);
   const int mode = spois ? 2 : (reduced ? 1 : 0);
   const df64 it = df_from_double(1.0 / tau);
   with_x(xin, [&](double (&x)[8][3]) {
     ArrayAccDF acc{m};
     if (mode == 0) {
-      if (smdot) continuity_elem_df<0, true>(x, w, it, p, acc, r8);
-      else continuity_elem_df<0, false>(x, w, it, p, acc, r8);
+      if (smdot) continuity_elem_df<0, true>(x, w, it, pd, acc, r8);
+      else continuity_elem_df<0, false>(x, w, it, pd, acc, r8);
     } else if (mode == 1) {
-      if (smdot) continuity_elem_df<1, true>(x, w, it, p, acc, r8);
-      else continuity_elem_df<1, false>(x, w, it, p, acc, r8);
+      if (smdot) continuity_elem_df<1, true>(x, w, it, pd, acc, r8);
+      else continuity_elem_df<1, false>(x, w, it, pd, acc, r8);
     } else {
-      if (smdot) continuity_elem_df<2, true>(x, w, it, p, acc, r8);
-      else continuity_elem_df<2, false>(x, w, it, p, acc, r8);
+      if (smdot) continuity_elem_df<2, true>(x, w, it, pd, acc, r8);
+      else continuity_elem_df<2, false>(x, w, it, pd, acc, r8);
     }
   });
-  for (int i = 0; i < 64; ++i) lhs[i] = df_to_double(m[i]);
+  for (int i = 0; i < 64; ++i) lhs[i] = df_to_double_bits(m[i]);
   for (int r = 0; r < 8; ++r) {
-    double s = df_to_double(r8[r]);
+    double s = df_to_double_bits(r8[r]);
     if (mode != 1)
       for (int c = 0; c < 8; ++c) s -= lhs[r * 8 + c] * p[c];
     rhs[r] = s;

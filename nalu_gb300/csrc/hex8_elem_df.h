@@ -1,14 +1,19 @@
 // hex8_elem_df.h -- the Hex8 element math of hex8_elem.h in double-float
 // (df64) arithmetic on the FP32 pipes.
 //
-// Same formulation (edge-form Jacobian, areas from cofactor columns,
-// lhs factors from adj(J)^T A), same summation order of the element matrix.
+// Same formulation (edge-form Jacobian, areas from cofactor columns, lhs
+// factors from adj(J)^T A) and the same summation order of the element matrix
+// as hex8_elem.h.  Unlike the FP64 version the 12 integration points run as a
+// loop with their constants computed from the ip index: the unrolled df64 body
+// is too large for the instruction cache (measured: warps stalled on
+// instruction fetch).  All ip constants are dyadic rationals, exact in FP32.
+//
 // Precision: coordinates enter as FP64 differences to node 0 of the element
-// (so their full relative precision survives the split into hi + lo), nodal
+// (their full relative precision survives the split into hi + lo), nodal
 // fields enter pre-split per node; every operation is an error-free-transform
-// sequence with ~2^-48 relative rounding, i.e. about 32x the FP64 rounding
-// unit, well inside the 1e-12 parity tolerance (checked on the CPU against the
-// oracle by tests/test_elem_math.py and on the GPU by the parity tests).
+// sequence with ~2^-48 relative rounding, about 32x the FP64 unit, well inside
+// the 1e-12 parity tolerance (checked on the CPU against the oracle by
+// tests/test_elem_math.py and on the GPU by the parity tests).
 #pragma once
 
 #include "df64.h"
@@ -27,7 +32,7 @@ NALU_HD void rel_coords_df(const double x[8][3], df64 d[8][3]) {
 #pragma unroll
   for (int n = 1; n < 8; ++n)
 #pragma unroll
-    for (int i = 0; i < 3; ++i) d[n][i] = df_from_double(x[n][i] - x[0][i]);
+    for (int i = 0; i < 3; ++i) d[n][i] = df_split_bits(x[n][i] - x[0][i]);
 }
 
 NALU_HD void edge_form_df(const df64 d[8][3], EdgeFormDF& f) {
@@ -59,20 +64,35 @@ NALU_HD void edge_form_df(const df64 d[8][3], EdgeFormDF& f) {
   }
 }
 
-template <int IP, bool SHIFT>
-NALU_HD void jacobian_ip_df(const EdgeFormDF& f, df64 j[3][3]) {
-  constexpr double a = SHIFT ? 0.5 : 0.25;
+// ip location in FP32 arithmetic (a = 0.25 standard, 0.5 shifted); the same
+// table as ip_loc() in hex8_elem.h, evaluated without FP64 instructions
+NALU_HD float ip_loc_f(int ip, int k, float a) {
+  if (ip >= 8) return k == 2 ? 0.0f : (float)corner_sign(ip - 8, k) * a;
+  if (k == 2) return ip < 4 ? -a : a;
+  const int m = ip & 3;
+  if (m == 0) return k == 0 ? 0.0f : -a;
+  if (m == 1) return k == 0 ? a : 0.0f;
+  if (m == 2) return k == 0 ? 0.0f : a;
+  return k == 0 ? -a : 0.0f;
+}
+NALU_HD void ip_location(int ip, float a, float s[3]) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k) s[k] = ip_loc_f(ip, k, a);
+}
+
+// J at a runtime ip location s (all entries exact dyadic in FP32)
+NALU_HD void jacobian_df(const EdgeFormDF& f, const float s[3], df64 j[3][3]) {
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     const int u = (k == 0) ? 1 : 0;
     const int v = (k == 2) ? 1 : 2;
-    const double su = ip_loc(IP, u, a), sv = ip_loc(IP, v, a);
+    const float su = s[u], sv = s[v];
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
       df64 r = f.A[k][i];
-      if (su != 0.0) r = df_add(r, df_scale2(f.B[k][i], (float)su));
-      if (sv != 0.0) r = df_add(r, df_scale2(f.C[k][i], (float)sv));
-      if (su * sv != 0.0) r = df_add(r, df_scale2(f.D[k][i], (float)(su * sv)));
+      if (su != 0.0f) r = df_add(r, df_scale2(f.B[k][i], su));
+      if (sv != 0.0f) r = df_add(r, df_scale2(f.C[k][i], sv));
+      if (su != 0.0f && sv != 0.0f) r = df_add(r, df_scale2(f.D[k][i], su * sv));
       j[i][k] = r;
     }
   }
@@ -97,57 +117,55 @@ struct IpGeomDF {
   df64 det;
 };
 
-template <int IP>
-NALU_HD void ip_geometry_df(const EdgeFormDF& f, IpGeomDF& g) {
+NALU_HD void ip_geometry_df(const EdgeFormDF& f, int ip, IpGeomDF& g) {
+  float s[3];
+  ip_location(ip, 0.25f, s);
   df64 j[3][3], adj[3][3], det;
-  jacobian_ip_df<IP, false>(f, j);
+  jacobian_df(f, s, j);
   cofactor_df(j, adj, det);
-  constexpr int dd = ip_dir(IP);
-  constexpr float s = (float)(0.25 * ip_sign(IP));
+  const int dd = ip_dir(ip);
+  const float sc = (ip < 8 && (ip & 3) == 2) ? -0.25f : 0.25f;  // 1/4 ip_sign(ip)
 #pragma unroll
-  for (int i = 0; i < 3; ++i) g.area[i] = df_scale2(adj[i][dd], s);
+  for (int i = 0; i < 3; ++i) {
+    // adj[i][dd] with a runtime column index, without dynamic register indexing
+    const df64 col = dd == 0 ? adj[i][0] : (dd == 1 ? adj[i][1] : adj[i][2]);
+    g.area[i] = df_scale2(col, sc);
+  }
 #pragma unroll
   for (int jj = 0; jj < 3; ++jj)
     g.G[jj] = df_fma(adj[2][jj], g.area[2], df_fma(adj[1][jj], g.area[1], df_mul(adj[0][jj], g.area[0])));
   g.det = det;
 }
 
-template <int IP>
-NALU_HD void ip_shifted_G_df(const EdgeFormDF& f, const df64 area[3], df64 G[3], df64& det) {
+NALU_HD void ip_shifted_G_df(const EdgeFormDF& f, int ip, const df64 area[3], df64 G[3], df64& det) {
+  float s[3];
+  ip_location(ip, 0.5f, s);
   df64 j[3][3], adj[3][3];
-  jacobian_ip_df<IP, true>(f, j);
+  jacobian_df(f, s, j);
   cofactor_df(j, adj, det);
 #pragma unroll
   for (int jj = 0; jj < 3; ++jj)
     G[jj] = df_fma(adj[2][jj], area[2], df_fma(adj[1][jj], area[1], df_mul(adj[0][jj], area[0])));
 }
 
-// fac[c] = sum_j dN_c/ds_j(ip) * (G_j * scale)
-template <int IP, bool SHIFT>
-NALU_HD void lhs_factors_df(const df64 G[3], df64 scale, df64 fac[8]) {
-  constexpr double a = SHIFT ? 0.5 : 0.25;
+// fac[c] = sum_j dN_c/ds_j(s) * (G_j * scale)
+NALU_HD void lhs_factors_df(const df64 G[3], df64 scale, const float s[3], df64 fac[8]) {
   const df64 g0 = df_mul(G[0], scale), g1 = df_mul(G[1], scale), g2 = df_mul(G[2], scale);
 #pragma unroll
   for (int c = 0; c < 8; ++c) {
-    const double d0 = dshape_ip(IP, c, 0, a), d1 = dshape_ip(IP, c, 1, a), d2 = dshape_ip(IP, c, 2, a);
-    df64 r = df_zero();
-    bool first = true;
-    if (d0 != 0.0) { r = df_mul_f(g0, (float)d0); first = false; }
-    if (d1 != 0.0) { r = first ? df_mul_f(g1, (float)d1) : df_add(r, df_mul_f(g1, (float)d1)); first = false; }
-    if (d2 != 0.0) { r = first ? df_mul_f(g2, (float)d2) : df_add(r, df_mul_f(g2, (float)d2)); first = false; }
-    fac[c] = r;
+    const float c0 = (float)corner_sign(c, 0), c1 = (float)corner_sign(c, 1), c2 = (float)corner_sign(c, 2);
+    const float h0 = 0.5f + c0 * s[0], h1 = 0.5f + c1 * s[1], h2 = 0.5f + c2 * s[2];
+    const float d0 = c0 * h1 * h2, d1 = c1 * h0 * h2, d2 = c2 * h0 * h1;  // exact in FP32
+    fac[c] = df_add(df_add(df_mul_f(g0, d0), df_mul_f(g1, d1)), df_mul_f(g2, d2));
   }
 }
 
 // Trilinear coefficients of a nodal scalar: f(s) = sum_m c_m s^m over the 8
-// monomials {1, s1, s2, s1 s2, s3, s1 s3, s2 s3, s1 s2 s3} (index bit k set =
-// factor s_{k+1}); nodal values live at the corners s = +-1/2.
+// monomials (index bit k set = factor s_{k+1}); nodal values sit at s = +-1/2.
 NALU_HD void trilinear_coeffs_df(const df64 v[8], df64 c[8]) {
-  // reorder corners to bit order: bit0 = s1 sign, bit1 = s2 sign, bit2 = s3 sign
   df64 t[8];
 #pragma unroll
   for (int m = 0; m < 8; ++m) t[m] = v[node_of((m & 1) ? 1 : -1, (m & 2) ? 1 : -1, (m & 4) ? 1 : -1)];
-  // along each axis: f(-1/2) = a, f(+1/2) = b  ->  f(s) = (a+b)/2 + (b-a) s
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     const int bit = 1 << k;
@@ -163,29 +181,26 @@ NALU_HD void trilinear_coeffs_df(const df64 v[8], df64 c[8]) {
   for (int m = 0; m < 8; ++m) c[m] = t[m];
 }
 
-// evaluate trilinear coefficients at an ip (location a = 1/4 or 1/2)
-template <int IP, bool SHIFT>
-NALU_HD df64 trilinear_eval_df(const df64 c[8]) {
-  constexpr double a = SHIFT ? 0.5 : 0.25;
-  const double s[3] = {ip_loc(IP, 0, a), ip_loc(IP, 1, a), ip_loc(IP, 2, a)};
+// evaluate trilinear coefficients at s (every monomial weight is a power of two or 0)
+NALU_HD df64 trilinear_eval_df(const df64 c[8], const float s[3]) {
   df64 r = c[0];
 #pragma unroll
   for (int m = 1; m < 8; ++m) {
-    double w = 1.0;
+    float w = 1.0f;
 #pragma unroll
     for (int k = 0; k < 3; ++k)
       if (m & (1 << k)) w *= s[k];
-    if (w != 0.0) r = df_add(r, df_scale2(c[m], (float)w));
+    if (w != 0.0f) r = df_add(r, df_scale2(c[m], w));
   }
   return r;
 }
 
-// element matrix accumulator in df64 (first touch stores, later ips add)
-template <int IP, class Acc>
-NALU_HD void accumulate_ip_df(Acc& acc, const df64 fac[8]) {
-  constexpr int il = ip_left(IP), ir = ip_right(IP);
-  constexpr bool fl = first_ip_of_row(il) == IP;
-  constexpr bool fr = first_ip_of_row(ir) == IP;
+// element-matrix accumulation for one ip: first touch of a row stores
+template <class Acc>
+NALU_HD void accumulate_ip_df(Acc& acc, int ip, const df64 fac[8]) {
+  const int il = ip_left(ip), ir = ip_right(ip);
+  const bool fl = first_ip_of_row(il) == ip;
+  const bool fr = first_ip_of_row(ir) == ip;
 #pragma unroll
   for (int c = 0; c < 8; ++c) {
     if (fl) acc.set(il, c, fac[c]); else acc.add(il, c, fac[c]);
@@ -194,30 +209,8 @@ NALU_HD void accumulate_ip_df(Acc& acc, const df64 fac[8]) {
 }
 
 // ---------------------------------------------------------------------------
-// ScalarDiffElemKernel in df64: k given per node as df64
+// ScalarDiffElemKernel in df64 (k given per node as df64)
 // ---------------------------------------------------------------------------
-template <bool SHIFT, class Acc>
-struct ScalarDiffBodyDF {
-  const EdgeFormDF& f;
-  const df64* kc;  // trilinear coefficients of the diffusion coefficient
-  Acc& acc;
-  double mindet;
-  template <int IP>
-  NALU_HD void apply() {
-    IpGeomDF g;
-    ip_geometry_df<IP>(f, g);
-    df64 G[3] = {g.G[0], g.G[1], g.G[2]};
-    df64 det = g.det;
-    if (SHIFT) ip_shifted_G_df<IP>(f, g.area, G, det);
-    const double dd = df_to_double(det);
-    mindet = dd < mindet ? dd : mindet;
-    const df64 kIp = trilinear_eval_df<IP, false>(kc);
-    df64 fac[8];
-    lhs_factors_df<IP, SHIFT>(G, df_neg(df_mul(kIp, df_rcp(det))), fac);
-    accumulate_ip_df<IP>(acc, fac);
-  }
-};
-
 template <bool SHIFT, class Acc>
 NALU_HD double scalar_diff_lhs_df(const double x[8][3], const df64 k[8], Acc& acc) {
   EdgeFormDF f;
@@ -228,62 +221,33 @@ NALU_HD double scalar_diff_lhs_df(const double x[8][3], const df64 k[8], Acc& ac
   }
   df64 kc[8];
   trilinear_coeffs_df(k, kc);
-  ScalarDiffBodyDF<SHIFT, Acc> body{f, kc, acc, 1.0e300};
-  IpLoop<0, 12>::run(body);
-  return body.mindet;
+  float mindet = 3.0e38f;
+#pragma unroll 1
+  for (int ip = 0; ip < 12; ++ip) {
+    IpGeomDF g;
+    ip_geometry_df(f, ip, g);
+    df64 G[3] = {g.G[0], g.G[1], g.G[2]};
+    df64 det = g.det;
+    if (SHIFT) ip_shifted_G_df(f, ip, g.area, G, det);
+    mindet = fminf(mindet, det.hi);
+    float s[3];
+    ip_location(ip, 0.25f, s);
+    const df64 kIp = trilinear_eval_df(kc, s);
+    float sg[3];
+    ip_location(ip, SHIFT ? 0.5f : 0.25f, sg);
+    df64 fac[8];
+    lhs_factors_df(G, df_neg(df_mul(kIp, df_rcp(det))), sg, fac);
+    accumulate_ip_df(acc, ip, fac);
+  }
+  return f2d_bits(mindet);
 }
 
 // ---------------------------------------------------------------------------
-// ContinuityAdvElemKernel in df64 (MODE as in hex8_elem.h).  wc: trilinear
-// coefficients of w = rho u + tau Gpdx per component; the caller adds
+// ContinuityAdvElemKernel in df64 (MODE as in hex8_elem.h).  The caller adds
 // -lhs . p in FP64 for MODE 0/2.
 // ---------------------------------------------------------------------------
 template <int MODE, bool SMDOT, class Acc>
-struct ContinuityBodyDF {
-  const EdgeFormDF& f;
-  const df64 (*wc)[8];  // [3][8]
-  df64 inv_tau;
-  const double* p;
-  Acc& acc;
-  df64* rhs;
-  double mindet;
-  template <int IP>
-  NALU_HD void apply() {
-    IpGeomDF g;
-    ip_geometry_df<IP>(f, g);
-    constexpr int il = ip_left(IP), ir = ip_right(IP);
-    double dd = df_to_double(g.det);
-    mindet = dd < mindet ? dd : mindet;
-    df64 fac[8];
-    if (MODE == 0) {
-      lhs_factors_df<IP, false>(g.G, df_neg(df_rcp(g.det)), fac);
-    } else {
-      df64 Gs[3], dets;
-      ip_shifted_G_df<IP>(f, g.area, Gs, dets);
-      dd = df_to_double(dets);
-      mindet = dd < mindet ? dd : mindet;
-      lhs_factors_df<IP, true>(Gs, df_neg(df_rcp(dets)), fac);
-    }
-    accumulate_ip_df<IP>(acc, fac);
-    const df64 wx = trilinear_eval_df<IP, SMDOT>(wc[0]);
-    const df64 wy = trilinear_eval_df<IP, SMDOT>(wc[1]);
-    const df64 wz = trilinear_eval_df<IP, SMDOT>(wc[2]);
-    df64 m = df_mul(df_fma(wz, g.area[2], df_fma(wy, g.area[1], df_mul(wx, g.area[0]))), inv_tau);
-    if (MODE == 1) {
-      df64 fs[8];
-      lhs_factors_df<IP, false>(g.G, df_neg(df_rcp(g.det)), fs);
-      df64 dpa = df_zero();
-#pragma unroll
-      for (int c = 0; c < 8; ++c) dpa = df_add(dpa, df_mul(fs[c], df_from_double(p[c])));
-      m = df_add(m, dpa);
-    }
-    rhs[il] = df_sub(rhs[il], m);
-    rhs[ir] = df_add(rhs[ir], m);
-  }
-};
-
-template <int MODE, bool SMDOT, class Acc>
-NALU_HD double continuity_elem_df(const double x[8][3], const df64 w[8][3], df64 inv_tau, const double p[8],
+NALU_HD double continuity_elem_df(const double x[8][3], const df64 w[8][3], df64 inv_tau, const df64 p[8],
                                   Acc& acc, df64 rhs[8]) {
   EdgeFormDF f;
   {
@@ -301,9 +265,47 @@ NALU_HD double continuity_elem_df(const double x[8][3], const df64 w[8][3], df64
   }
 #pragma unroll
   for (int r = 0; r < 8; ++r) rhs[r] = df_zero();
-  ContinuityBodyDF<MODE, SMDOT, Acc> body{f, wc, inv_tau, p, acc, rhs, 1.0e300};
-  IpLoop<0, 12>::run(body);
-  return body.mindet;
+  float mindet = 3.0e38f;
+#pragma unroll 1
+  for (int ip = 0; ip < 12; ++ip) {
+    IpGeomDF g;
+    ip_geometry_df(f, ip, g);
+    mindet = fminf(mindet, g.det.hi);
+    df64 fac[8];
+    float s_std[3], s_sh[3];
+    ip_location(ip, 0.25f, s_std);
+    ip_location(ip, 0.5f, s_sh);
+    if (MODE == 0) {
+      lhs_factors_df(g.G, df_neg(df_rcp(g.det)), s_std, fac);
+    } else {
+      df64 Gs[3], dets;
+      ip_shifted_G_df(f, ip, g.area, Gs, dets);
+      mindet = fminf(mindet, dets.hi);
+      lhs_factors_df(Gs, df_neg(df_rcp(dets)), s_sh, fac);
+    }
+    accumulate_ip_df(acc, ip, fac);
+    const float* sm = SMDOT ? s_sh : s_std;
+    const df64 wx = trilinear_eval_df(wc[0], sm);
+    const df64 wy = trilinear_eval_df(wc[1], sm);
+    const df64 wz = trilinear_eval_df(wc[2], sm);
+    df64 m = df_mul(df_fma(wz, g.area[2], df_fma(wy, g.area[1], df_mul(wx, g.area[0]))), inv_tau);
+    if (MODE == 1) {
+      df64 fs[8];
+      lhs_factors_df(g.G, df_neg(df_rcp(g.det)), s_std, fs);
+      df64 dpa = df_zero();
+#pragma unroll
+      for (int c = 0; c < 8; ++c) dpa = df_fma(fs[c], p[c], dpa);
+      m = df_add(m, dpa);
+    }
+    const int il = ip_left(ip), ir = ip_right(ip);
+    // rhs[il] -= m ; rhs[ir] += m  (runtime row index without dynamic register indexing)
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      if (r == il) rhs[r] = df_sub(rhs[r], m);
+      if (r == ir) rhs[r] = df_add(rhs[r], m);
+    }
+  }
+  return f2d_bits(mindet);
 }
 
 // plain array accumulator (host check)

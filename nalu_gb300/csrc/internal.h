@@ -40,8 +40,19 @@ struct Field {
   bool set = false;
 };
 
+// SELL-32 copy of the CRS matrix for the fast CG (cg_fast.cu)
+struct SellMatrix {
+  DBuf<int64_t> ptr;   // [nslices+1] start of each slice
+  DBuf<int32_t> len;   // [nslices] entries per row in the slice
+  DBuf<int32_t> col;
+  DBuf<double> vald;
+  DBuf<float> valf;
+  int64_t nslices = 0, stored = 0;
+};
+
 // Solver workspace (device vectors are allocated lazily per system size).
 struct SolverWork {
+  SellMatrix sell;
   DBuf<double> r, z, p, q, ap, dinv, w, tmp;
   DBuf<float> fvals, fr, fz, fp, fq, fdinv, fx;
   DBuf<double> V, Hbuf;  // GMRES basis (restart+1 vectors)
@@ -131,5 +142,11 @@ int probe_fp64(nalu_ctx* ctx, double* tflops);
 // krylov.cu
 int solve(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* info);
 int spmv_fp64(nalu_ctx* ctx, const double* x, double* y);
+// cg_fast.cu
+template <class VT>
+int sell_build(nalu_ctx* ctx, SellMatrix& S, const VT** vals_out);
+template <class T, class VT>
+int pcg_fast(nalu_ctx* ctx, const VT* sval, const SellMatrix& S, T* x, T* r, T* z, T* p0, T* p1, T* q,
+             const T* dinv, double rtol, double r0norm, int max_it, int check_every, int* iters_out);
 
 }  // namespace nalu_gb300

@@ -705,8 +705,17 @@ int solve(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* info) {
         return rc;
       if (o.method == NALU_SOLVER_GMRES && (rc = ensure(ctx, s.V, (int64_t)(m + 1) * n))) return rc;
       cudaMemcpyAsync(s.r.p, s.tmp.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->stream);
-      rc = run_inner<double>(ctx, o, s.r.p, s.w.p, s.z.p, s.p.p, s.q.p, s.dinv.p, s.V.p, s.ap.p, s.tmp.p,
-                             ctx->d_values.p, false, rtol, r0, o.max_iters - total_it, &its);
+      if (o.method == NALU_SOLVER_CG && o.precond == NALU_PRECOND_JACOBI) {
+        // two-kernel Jacobi-CG on the SELL-32 copy (cg_fast.cu)
+        const double* sv = nullptr;
+        if (outer == 1 && (rc = sell_build<double>(ctx, s.sell, &sv))) return rc;
+        sv = s.sell.vald.p;
+        rc = pcg_fast<double, double>(ctx, sv, s.sell, s.w.p, s.r.p, s.z.p, s.p.p, s.ap.p, s.q.p, s.dinv.p, rtol, r0,
+                                      o.max_iters - total_it, o.check_every, &its);
+      } else {
+        rc = run_inner<double>(ctx, o, s.r.p, s.w.p, s.z.p, s.p.p, s.q.p, s.dinv.p, s.V.p, s.ap.p, s.tmp.p,
+                               ctx->d_values.p, false, rtol, r0, o.max_iters - total_it, &its);
+      }
       k_add_to<double><<<grid_for(n, 256), 256, 0, ctx->stream>>>(n, ctx->d_x.p, s.w.p);
     } else {
       if ((rc = ensuref(ctx, s.fvals, ctx->nnz)) || (rc = ensuref(ctx, s.fr, n)) || (rc = ensuref(ctx, s.fz, n)) ||
@@ -724,8 +733,16 @@ int solve(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* info) {
       }
       k_convert<double, float><<<kRedBlocks, 256, 0, ctx->stream>>>(n, s.tmp.p, s.fr.p);
       ctx->launches++;
-      rc = run_inner<float>(ctx, o, s.fr.p, s.fx.p, s.fz.p, s.fp.p, s.fq.p, s.fdinv.p, s.fV.p, ft1.p, ft2.p,
-                            s.fvals.p, true, rtol, r0, o.max_iters - total_it, &its);
+      if (o.method == NALU_SOLVER_CG && o.precond == NALU_PRECOND_JACOBI) {
+        const float* sv = nullptr;
+        if (outer == 1 && (rc = sell_build<float>(ctx, s.sell, &sv))) return rc;
+        sv = s.sell.valf.p;
+        rc = pcg_fast<float, float>(ctx, sv, s.sell, s.fx.p, s.fr.p, s.fz.p, s.fp.p, ft1.p, s.fq.p, s.fdinv.p, rtol,
+                                    r0, o.max_iters - total_it, o.check_every, &its);
+      } else {
+        rc = run_inner<float>(ctx, o, s.fr.p, s.fx.p, s.fz.p, s.fp.p, s.fq.p, s.fdinv.p, s.fV.p, ft1.p, ft2.p,
+                              s.fvals.p, true, rtol, r0, o.max_iters - total_it, &its);
+      }
       k_add_to<float><<<grid_for(n, 256), 256, 0, ctx->stream>>>(n, ctx->d_x.p, s.fx.p);
       cudaStreamSynchronize(ctx->stream);
       ft1.free();
