@@ -153,9 +153,9 @@ def cpu_threads():
         return os.cpu_count() or 1
 
 
-def run_cpu_sample(O, c, conn, gid, u, rho, p, gp, n_elems_sample, n_threads):
+def run_cpu_sample(O, c, conn, graph, u, rho, p, gp, n_elems_sample, n_threads):
     """Oracle assembly of the first n_elems_sample elements (all nodes)."""
-    rp, ci, lid = O.graph(c.shape[0], conn, 1, gid)
+    rp, ci, lid = graph
     sub = np.ascontiguousarray(conn[:n_elems_sample])
     t0 = time.perf_counter()
     O.assemble(O.KERNEL_CONTINUITY_ADV, c, sub, rp, ci, lid, scalar=p, coeff=rho, vec=u, vec2=gp,
@@ -173,13 +173,14 @@ def bench_reference(args):
         subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "liboracle.so"], check=True)
     c, conn, gid, u, rho, p, gp = make_inputs()
     nt = cpu_threads()
+    graph = O.graph(c.shape[0], conn, 1, gid)
     sample = 1 << 20  # half the mesh per step keeps the run within minutes
     for _ in range(args.warmup):
-        run_cpu_sample(O, c, conn, gid, u, rho, p, gp, 1 << 16, nt)
+        run_cpu_sample(O, c, conn, graph, u, rho, p, gp, 1 << 16, nt)
     rates = []
     t_all = time.perf_counter()
     for _ in range(args.steps):
-        r, _ = run_cpu_sample(O, c, conn, gid, u, rho, p, gp, sample, nt)
+        r, _ = run_cpu_sample(O, c, conn, graph, u, rho, p, gp, sample, nt)
         rates.append(r)
     wall = time.perf_counter() - t_all
     value = statistics.median(rates)
@@ -278,9 +279,14 @@ def bench_gpu(args):
         ctx.reset_rows([0])
         ctx.sum_into_diag(0, 0, 1.0, 0.0)
         ctx.load_complete()
-        info = ctx.solve(ng.default_solver_opts(tol=1e-8, max_iters=20000, check_every=50), raise_on_error=False)
-        solve = {"method": "Jacobi-PCG (FP64)", "ms": 1e3 * info.seconds, "iterations": info.iterations,
-                 "true_rel_res": info.true_rel_res, "status": info.status, "learned": "not built"}
+        solve = {}
+        for name, prec in (("jacobi_pcg_fp64", ng.PRECISION_FP64), ("jacobi_pcg_fp32_ir", ng.PRECISION_FP32_INNER_IR)):
+            info = ctx.solve(ng.default_solver_opts(tol=1e-8, max_iters=40000, check_every=50, precision=prec),
+                             raise_on_error=False)
+            solve[name] = {"ms": 1e3 * info.seconds, "iterations": info.iterations,
+                           "outer_iterations": info.outer_iterations, "true_rel_res": info.true_rel_res,
+                           "status": info.status}
+        solve["system"] = "continuity Laplacian of the same mesh, pressure pinned at node 0 (resetRows + diag 1)"
     # ---- CPU baseline on rank 0 (oracle, bounded sample) ----
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -288,7 +294,7 @@ def bench_gpu(args):
         if not os.path.exists(os.path.join(ROOT, "oracle", "liboracle.so")):
             subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "liboracle.so"], check=True)
         sample = 1 << 18
-        r, dt = run_cpu_sample(O, c, conn, gid, u, rho, p, gp, sample, 1)
+        r, dt = run_cpu_sample(O, c, conn, O.graph(c.shape[0], conn, 1, gid), u, rho, p, gp, sample, 1)
         cpu = {"value": r, "unit": UNIT, "cores": 1, "kind": "port",
                "sample": "first %d elements of the same 128^3 workload, serial element order (%.1f s)" % (sample, dt)}
     # ---- roofline of the dominant kernel ----

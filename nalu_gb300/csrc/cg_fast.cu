@@ -1,4 +1,4 @@
-// cg_fast.cu -- Jacobi-preconditioned CG with two kernels per iteration on a
+// cg_fast.cu -- Jacobi-preconditioned CG with three kernels per iteration on a
 // sliced-ELL copy of the CRS matrix.
 //
 // Layout: SELL-32 (slices of 32 consecutive rows; entry k of every row of a
@@ -8,14 +8,17 @@
 // FP32 for the mixed-precision inner solve).
 //
 // Iteration k (rz_k = r_k . z_k, z_k = D^-1 r_k):
-//   K1  beta = rz_k / rz_{k-1};  p_k = z_k + beta p_{k-1} (formed on the fly
-//       for every gathered column);  q = A p_k;  partial sums of p_k . q
-//   K2  alpha = rz_k / (p_k . q);  x += alpha p_k;  r -= alpha q;
+//   K0  beta = rz_k / rz_{k-1};  p = z + beta p
+//   K1  q = A p (one multiply-add per stored entry);  partial sums of p . q
+//   K2  alpha = rz_k / (p . q);  x += alpha p;  r -= alpha q;
 //       z = D^-1 r;  partial sums of r.z and r.r
 // Every block re-reduces the previous kernel's 1024 partials in the same
 // order, so all blocks use bit-identical alpha/beta and no scalar kernel or
-// host round trip sits between K1 and K2.  Buffers alternate between even and
-// odd iterations; a chunk of iterations is captured once into a CUDA graph.
+// host round trip sits between the kernels.  (Forming p inside the SpMV
+// gather instead would double its FP64 multiply-adds; on GB300 the SpMV is
+// then FP64-issue bound rather than HBM bound.)  The rz partial buffers
+// alternate between even and odd iterations; a chunk of iterations is
+// captured once into a CUDA graph.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -118,14 +121,11 @@ __global__ void __launch_bounds__(kCgThreads) k_cg_init(int64_t n, const T* __re
   block_store(rr, rr_part + blockIdx.x, sh);
 }
 
-template <class T, class VT>
-__global__ void __launch_bounds__(kCgThreads) k_cg_spmv(int64_t n, int64_t nrows_padded, const int64_t* __restrict__ sptr,
-                                                        const int32_t* __restrict__ slen, const int32_t* __restrict__ scol,
-                                                        const VT* __restrict__ sval, const T* __restrict__ z,
-                                                        const T* __restrict__ p_old, T* __restrict__ p_new,
-                                                        T* __restrict__ q, const double* __restrict__ rz_cur,
-                                                        const double* __restrict__ rz_prev, int first,
-                                                        double* __restrict__ pq_part) {
+// p = z + beta p with beta = rz_cur / rz_prev (beta = 0 on the first iteration)
+template <class T>
+__global__ void __launch_bounds__(kCgThreads) k_cg_pupdate(int64_t n, const T* __restrict__ z, T* __restrict__ p,
+                                                           const double* __restrict__ rz_cur,
+                                                           const double* __restrict__ rz_prev, int first) {
   __shared__ double sh[33];
   double beta = 0.0;
   if (!first) {
@@ -133,6 +133,17 @@ __global__ void __launch_bounds__(kCgThreads) k_cg_spmv(int64_t n, int64_t nrows
     const double b = block_total(rz_prev, kCgBlocks, sh);
     beta = a / b;
   }
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = first ? z[i] : (T)((double)z[i] + beta * (double)p[i]);
+}
+
+// q = A p on the SELL-32 copy (one multiply-add per stored entry); partials of p.q
+template <class T, class VT>
+__global__ void __launch_bounds__(kCgThreads) k_cg_spmv(int64_t n, int64_t nrows_padded, const int64_t* __restrict__ sptr,
+                                                        const int32_t* __restrict__ slen, const int32_t* __restrict__ scol,
+                                                        const VT* __restrict__ sval, const T* __restrict__ p,
+                                                        T* __restrict__ q, double* __restrict__ pq_part) {
+  __shared__ double sh[33];
   double dot = 0.0;
   for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < nrows_padded;
        row += (int64_t)gridDim.x * blockDim.x) {
@@ -140,23 +151,13 @@ __global__ void __launch_bounds__(kCgThreads) k_cg_spmv(int64_t n, int64_t nrows
     const int64_t s = row / kSlice;
     const int len = __ldg(slen + s);
     const int64_t base = __ldg(sptr + s) + (row % kSlice);
-    double acc = 0.0;
-    if (first) {
-      for (int k = 0; k < len; ++k) {
-        const int32_t c = __ldg(scol + base + (int64_t)k * kSlice);
-        acc += (double)__ldg(sval + base + (int64_t)k * kSlice) * (double)__ldg(z + c);
-      }
-    } else {
-      for (int k = 0; k < len; ++k) {
-        const int32_t c = __ldg(scol + base + (int64_t)k * kSlice);
-        const double pc = (double)__ldg(z + c) + beta * (double)__ldg(p_old + c);
-        acc += (double)__ldg(sval + base + (int64_t)k * kSlice) * pc;
-      }
+    T acc = 0;
+    for (int k = 0; k < len; ++k) {
+      const int32_t c = __ldg(scol + base + (int64_t)k * kSlice);
+      acc += (T)__ldg(sval + base + (int64_t)k * kSlice) * __ldg(p + c);
     }
-    const double pi = first ? (double)z[row] : (double)z[row] + beta * (double)p_old[row];
-    p_new[row] = (T)pi;
-    q[row] = (T)acc;
-    dot += pi * acc;
+    q[row] = acc;
+    dot += (double)p[row] * (double)acc;
   }
   block_store(dot, pq_part + blockIdx.x, sh);
 }
@@ -188,14 +189,14 @@ __global__ void __launch_bounds__(kCgThreads) k_cg_axpy(int64_t n, T* __restrict
 
 template <class T, class VT>
 void cg_iteration(nalu_ctx* ctx, int k, int first, int64_t n, int64_t npad, const int64_t* sptr, const int32_t* slen,
-                  const int32_t* scol, const VT* sval, T* x, T* r, T* z, T* pbuf[2], T* q, const T* dinv,
+                  const int32_t* scol, const VT* sval, T* x, T* r, T* z, T* p, T* q, const T* dinv,
                   double* rzbuf[2], double* pq_part, double* rr_part) {
   const int cur = k & 1, prev = cur ^ 1;
-  k_cg_spmv<T, VT><<<kCgBlocks, kCgThreads, 0, ctx->stream>>>(n, npad, sptr, slen, scol, sval, z, pbuf[prev],
-                                                              pbuf[cur], q, rzbuf[cur], rzbuf[prev], first, pq_part);
-  k_cg_axpy<T><<<kCgBlocks, kCgThreads, 0, ctx->stream>>>(n, x, pbuf[cur], r, q, z, dinv, rzbuf[cur], pq_part,
-                                                          rzbuf[prev], rr_part);
-  ctx->launches += 2;
+  k_cg_pupdate<T><<<kCgBlocks, kCgThreads, 0, ctx->stream>>>(n, z, p, rzbuf[cur], rzbuf[prev], first);
+  k_cg_spmv<T, VT><<<kCgBlocks, kCgThreads, 0, ctx->stream>>>(n, npad, sptr, slen, scol, sval, p, q, pq_part);
+  k_cg_axpy<T><<<kCgBlocks, kCgThreads, 0, ctx->stream>>>(n, x, p, r, q, z, dinv, rzbuf[cur], pq_part, rzbuf[prev],
+                                                          rr_part);
+  ctx->launches += 3;
 }
 
 }  // namespace
@@ -249,12 +250,11 @@ int pcg_fast(nalu_ctx* ctx, const VT* sval, const SellMatrix& S, T* x, T* r, T* 
   double* rzbuf[2] = {part.p, part.p + kCgBlocks};
   double* pq_part = part.p + 2 * kCgBlocks;
   double* rr_part = part.p + 3 * kCgBlocks;
-  T* pbuf[2] = {p0, p1};
   NALU_CUDA(ctx, cudaMemsetAsync(x, 0, sizeof(T) * n, ctx->stream));
   k_cg_init<T><<<kCgBlocks, kCgThreads, 0, ctx->stream>>>(n, r, dinv, z, rzbuf[0], rr_part);
   ctx->launches++;
   // iteration 0 (p_0 = z_0) outside the graph
-  cg_iteration<T, VT>(ctx, 0, 1, n, npad, S.ptr.p, S.len.p, S.col.p, sval, x, r, z, pbuf, q, dinv, rzbuf, pq_part,
+  cg_iteration<T, VT>(ctx, 0, 1, n, npad, S.ptr.p, S.len.p, S.col.p, sval, x, r, z, p0, q, dinv, rzbuf, pq_part,
                       rr_part);
   int chunk = check_every > 0 ? check_every : 50;
   chunk += chunk & 1;  // even: the buffer pattern repeats every two iterations
@@ -263,7 +263,7 @@ int pcg_fast(nalu_ctx* ctx, const VT* sval, const SellMatrix& S, T* x, T* r, T* 
   cudaError_t ce = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
   if (ce != cudaSuccess) return cuda_check(ctx, ce, "begin capture");
   for (int k = 1; k <= chunk; ++k)
-    cg_iteration<T, VT>(ctx, k, 0, n, npad, S.ptr.p, S.len.p, S.col.p, sval, x, r, z, pbuf, q, dinv, rzbuf, pq_part,
+    cg_iteration<T, VT>(ctx, k, 0, n, npad, S.ptr.p, S.len.p, S.col.p, sval, x, r, z, p0, q, dinv, rzbuf, pq_part,
                         rr_part);
   ce = cudaStreamEndCapture(ctx->stream, &graph);
   if (ce != cudaSuccess) return cuda_check(ctx, ce, "end capture");
