@@ -196,6 +196,19 @@ int nalu_solution_set(nalu_ctx* ctx, const double* x, int src_is_device);
 /* y = A x with the context's matrix (FP64), host or device vectors */
 int nalu_spmv(nalu_ctx* ctx, const double* x, double* y, int is_device);
 
+/* ---- batches of independent meshes ------------------------------------- */
+/* Declare that the context's mesh is a union of n independent problems:
+ * problem k owns the nodes [node_offsets[k], node_offsets[k+1]) in Tpetra row
+ * order (give the meshes ascending global ids problem by problem).  Assembly
+ * stays one launch over all elements (the graph is block diagonal); the
+ * batched solve below keeps separate scalars and a separate stop test per
+ * problem.  No reference counterpart: Nalu solves one system per rank. */
+int nalu_set_problems(nalu_ctx* ctx, int n, const int64_t* node_offsets);
+/* Jacobi-preconditioned CG on every problem at once in one persistent
+ * cooperative kernel (per-problem alpha/beta and convergence); infos[k]
+ * receives problem k's iterations and true FP64 relative residual. */
+int nalu_solve_batched(nalu_ctx* ctx, const nalu_solver_opts* opts, nalu_solve_info* infos);
+
 /* Jacobi-preconditioned CG on a caller-owned CRS system, allocating no device
  * memory.  This entry point has no counterpart in the reference.  It is for
  * callers that cannot let a library call cudaMalloc: codes that hand their

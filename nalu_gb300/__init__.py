@@ -108,6 +108,8 @@ def lib():
             "nalu_solution_get": (I, [P, P, I]),
             "nalu_solution_set": (I, [P, P, I]),
             "nalu_spmv": (I, [P, P, P, I]),
+            "nalu_set_problems": (I, [P, I, P]),
+            "nalu_solve_batched": (I, [P, P, P]),
             "nalu_kernel_launch_count": (I64, [P]),
             "nalu_last_assemble_ms": (D, [P]),
             "nalu_probe_fp64_tflops": (I, [P, ctypes.POINTER(D)]),
@@ -273,6 +275,21 @@ class Context:
         if raise_on_error:
             self._check(rc, "solve")
         return info
+
+    def set_problems(self, node_offsets):
+        """Declare the mesh a union of independent problems (node offsets in row order)."""
+        off = np.ascontiguousarray(node_offsets, np.int64)
+        self._check(lib().nalu_set_problems(self._h, len(off) - 1, _ptr(off)), "set_problems")
+        self._n_problems = len(off) - 1
+
+    def solve_batched(self, opts=None, raise_on_error=True):
+        """Jacobi-CG on every problem at once; a list of SolveInfo, one per problem."""
+        opts = default_solver_opts() if opts is None else opts
+        infos = (SolveInfo * self._n_problems)()
+        rc = lib().nalu_solve_batched(self._h, ctypes.byref(opts), infos)
+        if raise_on_error:
+            self._check(rc, "solve_batched")
+        return list(infos)
 
     def solution(self):
         nr, _, _ = self.sizes()

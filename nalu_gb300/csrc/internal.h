@@ -95,6 +95,9 @@ struct nalu_ctx {
   std::vector<int64_t> colour_offsets;   // [n_colours+1]
   int scatter_choice[4] = {0, 0, 0, 0};  // autotuned scatter per kernel (0 = not tuned)
 
+  // independent problems in one context (node offsets in LID order)
+  std::vector<int64_t> problem_offsets;
+
   // errors raised by kernels (negative Jacobian count, graph misses, ...)
   nalu_gb300::DBuf<int32_t> d_flags;     // [4]
 

@@ -127,3 +127,28 @@ class TrigFields:
         aT, k, pi = TrigFields.aT, TrigFields.k, np.pi
         x, y, z = c[:, 0], c[:, 1], c[:, 2]
         return (k / 4.0) * (np.cos(2.0 * aT * pi * x) + np.cos(2.0 * aT * pi * y) + np.cos(2.0 * aT * pi * z))
+
+
+def batch_block_meshes(n_problems, edge_range=(16, 96), jitter=0.1, seed=0):
+    """Union of independent Hex8 block meshes on the unit cube.
+
+    Each problem draws its three edge counts log-uniformly from edge_range
+    (rounded to integers) and its own interior jitter.  Problem k's nodes
+    follow problem k-1's, with global ids continuing across problems, so
+    every problem owns one contiguous range of rows.
+    Returns (coords, conn, gid, node_offsets int64 [P+1], edges int [P,3]).
+    """
+    rng = np.random.default_rng(seed)
+    lo, hi = np.log(edge_range[0]), np.log(edge_range[1])
+    edges = np.rint(np.exp(rng.uniform(lo, hi, size=(n_problems, 3)))).astype(np.int64)
+    coords, conns, offs = [], [], [0]
+    for k in range(n_problems):
+        nx, ny, nz = (int(e) for e in edges[k])
+        c, conn, _ = block_mesh(nx, ny, nz, jitter=jitter, seed=seed * 7919 + 1 + k)
+        coords.append(c)
+        conns.append(conn + offs[-1])
+        offs.append(offs[-1] + c.shape[0])
+    coords = np.ascontiguousarray(np.concatenate(coords))
+    conn = np.ascontiguousarray(np.concatenate(conns).astype(np.int32))
+    gid = np.arange(1, coords.shape[0] + 1, dtype=np.int64)
+    return coords, conn, gid, np.asarray(offs, dtype=np.int64), edges
