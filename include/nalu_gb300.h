@@ -161,7 +161,9 @@ enum nalu_solver_method {
 enum nalu_precond {
   NALU_PRECOND_NONE = 0,
   NALU_PRECOND_JACOBI = 1,    /* Ifpack2 RELAXATION Jacobi, one sweep */
-  NALU_PRECOND_CHEBYSHEV = 2  /* Chebyshev polynomial in D^-1 A */
+  NALU_PRECOND_CHEBYSHEV = 2, /* Chebyshev polynomial in D^-1 A */
+  NALU_PRECOND_LEARNED = 3    /* learned 27-point stencil (below) in flexible CG;
+                                 scalar systems, FP64, needs weights */
 };
 enum nalu_precision {
   NALU_PRECISION_FP64 = 0,          /* everything FP64 */
@@ -178,14 +180,21 @@ typedef struct nalu_solver_opts {
   int x0_zero;       /* 1: start from 0 (else from the current solution) */
   double tol;        /* stop on true ||b - A x|| / ||b|| <= tol */
   double inner_tol;  /* inner tolerance for iterative refinement */
-  int reserved[6];
+  int stall_window;  /* learned FCG stalls when the residual norm has no new
+                        minimum for max(stall_window, iterations taken to reach
+                        the current minimum); Chebyshev-Jacobi PCG then
+                        finishes (default 20) */
+  int reserved[5];
 } nalu_solver_opts;
 typedef struct nalu_solve_info {
   int iterations;        /* inner iterations in total */
   int outer_iterations;  /* refinement steps (1 for plain FP64) */
   int status;
   double true_rel_res;   /* FP64 ||b - A x|| / ||b|| */
-  double seconds;
+  double seconds;        /* wall time of the whole call, set-up included */
+  int fallback;          /* 1: the learned FCG stalled; Chebyshev-Jacobi PCG finished */
+  int learned_iterations;/* iterations spent in the learned FCG */
+  double setup_seconds;  /* learned preconditioner set-up (MLP stencil + SELL values) */
 } nalu_solve_info;
 void nalu_solver_opts_default(nalu_solver_opts* opts);
 /* solve A x = rhs into the context's solution vector */
@@ -208,6 +217,59 @@ int nalu_set_problems(nalu_ctx* ctx, int n, const int64_t* node_offsets);
  * cooperative kernel (per-problem alpha/beta and convergence); infos[k]
  * receives problem k's iterations and true FP64 relative residual. */
 int nalu_solve_batched(nalu_ctx* ctx, const nalu_solver_opts* opts, nalu_solve_info* infos);
+
+/* ---- learned preconditioner -------------------------------------------- */
+/* No reference counterpart: Nalu preconditions with Ifpack2/MueLu
+ * (src/LinearSolver.C:98-106).  A per-node MLP, 108 -> 64 -> 64 -> 64 -> 1
+ * with GELU (tanh form), reads 27 x 4 features of the node's 27-point
+ * neighbourhood (slot s = 9(dz+1) + 3(dy+1) + (dx+1) of the element-local
+ * offset): [0,27) residual / its RMS over the patch, [27,54) a_ij / a_ii,
+ * [54,81) neighbour mask, [81,108) a_jj / a_ii.  The correction is
+ * z_i = (r_i + rms_i * mlp_i) / a_ii.  At solve set-up the MLP is evaluated
+ * on the 27 unit-impulse residuals of every node (BF16 tensor-core kernel),
+ * which gives a 27-point stencil C; the preconditioner is the symmetric part
+ * of D^-1 (I + C), applied with the sparsity of A.
+ * Parameters (FP32, NALU_LEARNED_PARAMS): W1[64][108], b1[64], W2[64][64],
+ * b2[64], W3[64][64], b3[64], w4[64], b4. */
+#define NALU_LEARNED_PARAMS 15361
+/* deterministic initialisation: hidden layers U(-1/sqrt(fan_in), +), output 0
+ * (an untrained network is exactly Jacobi) */
+int nalu_learned_init(nalu_ctx* ctx, uint64_t seed);
+int nalu_learned_set_weights(nalu_ctx* ctx, const float* params, int64_t n);
+int nalu_learned_get_weights(nalu_ctx* ctx, float* params, int64_t n);
+/* Training pairs from plain Jacobi-PCG on the context's scalar system with
+ * n_rhs seeded N(0,1) right-hand sides: the first search direction
+ * p0 = D^-1 b and its image q0 = A p0 are an exact (residual, error) pair.
+ * n_samples random non-identity rows, spread over the right-hand sides:
+ * static_feats [n][81] (features 27..107), resid_feats [n][27] (q0 over the
+ * patch / its RMS), targets [n] (p0_i a_ii / RMS), rows [n] (the row of each
+ * sample; may be NULL).  *n_out <= n_samples
+ * (rows whose patch residual is 0 are skipped).  Host arrays. */
+int nalu_learned_harvest(nalu_ctx* ctx, int n_rhs, uint64_t seed, int64_t n_samples, float* static_feats,
+                         float* resid_feats, float* targets, int64_t* rows /* [n] or NULL */, int64_t* n_out);
+typedef struct nalu_train_opts {
+  int epochs;          /* default 40 */
+  int batch;           /* samples per Adam step, default 256, <= 1024 */
+  double lr;           /* Adam step size, default 1e-3 (beta 0.9/0.999, eps 1e-8) */
+  double val_fraction; /* held-out share of the samples, default 0.1 */
+  uint64_t seed;       /* sample order */
+  int reserved[4];
+} nalu_train_opts;
+void nalu_train_opts_default(nalu_train_opts* opts);
+/* Adam on the mean squared error of the stencil form
+ * pred = rf_13 + sum_s mask_s mlp(impulse_s, st) / sqrt(27) * rf_s against
+ * the targets, on the GPU (FP32).  history [epochs][2]: train and held-out
+ * MSE after each epoch (may be NULL). */
+int nalu_learned_train(nalu_ctx* ctx, const float* static_feats, const float* resid_feats, const float* targets,
+                       int64_t n, const nalu_train_opts* opts, float* history);
+/* loss and gradient of that loss at the current weights over n <= 1024
+ * samples (one batch); grad [NALU_LEARNED_PARAMS], host arrays */
+int nalu_learned_gradient(nalu_ctx* ctx, const float* static_feats, const float* resid_feats, const float* targets,
+                          int64_t n, float* grad, double* loss);
+/* the stencil of the current scalar system: stencil [n_rows][27] (host),
+ * mlp(impulse_s) / sqrt(27) per slot, 0 for missing neighbours and for
+ * identity rows */
+int nalu_learned_stencil(nalu_ctx* ctx, float* stencil);
 
 /* Jacobi-preconditioned CG on a caller-owned CRS system, allocating no device
  * memory.  This entry point has no counterpart in the reference.  It is for

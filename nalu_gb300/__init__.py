@@ -36,7 +36,8 @@ KERNEL_MOMENTUM_UPW_ADV_DIFF = 3
 SCATTER_AUTO, SCATTER_ATOMIC, SCATTER_COLOURED = 0, 1, 2
 ARITH_FP64, ARITH_DF64 = 0, 1
 SOLVER_CG, SOLVER_GMRES = 0, 1
-PRECOND_NONE, PRECOND_JACOBI, PRECOND_CHEBYSHEV = 0, 1, 2
+PRECOND_NONE, PRECOND_JACOBI, PRECOND_CHEBYSHEV, PRECOND_LEARNED = 0, 1, 2, 3
+LEARNED_PARAMS = 15361
 PRECISION_FP64, PRECISION_FP32_INNER_IR = 0, 1
 
 
@@ -59,12 +60,18 @@ class SolverOpts(ctypes.Structure):
     _fields_ = [("method", ctypes.c_int), ("precond", ctypes.c_int), ("precision", ctypes.c_int),
                 ("max_iters", ctypes.c_int), ("restart", ctypes.c_int), ("cheb_degree", ctypes.c_int),
                 ("check_every", ctypes.c_int), ("x0_zero", ctypes.c_int), ("tol", ctypes.c_double),
-                ("inner_tol", ctypes.c_double), ("reserved", ctypes.c_int * 6)]
+                ("inner_tol", ctypes.c_double), ("stall_window", ctypes.c_int), ("reserved", ctypes.c_int * 5)]
 
 
 class SolveInfo(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int), ("outer_iterations", ctypes.c_int), ("status", ctypes.c_int),
-                ("true_rel_res", ctypes.c_double), ("seconds", ctypes.c_double)]
+                ("true_rel_res", ctypes.c_double), ("seconds", ctypes.c_double), ("fallback", ctypes.c_int),
+                ("learned_iterations", ctypes.c_int), ("setup_seconds", ctypes.c_double)]
+
+
+class TrainOpts(ctypes.Structure):
+    _fields_ = [("epochs", ctypes.c_int), ("batch", ctypes.c_int), ("lr", ctypes.c_double),
+                ("val_fraction", ctypes.c_double), ("seed", ctypes.c_uint64), ("reserved", ctypes.c_int * 4)]
 
 
 _lib = None
@@ -109,6 +116,14 @@ def lib():
             "nalu_solution_set": (I, [P, P, I]),
             "nalu_spmv": (I, [P, P, P, I]),
             "nalu_set_problems": (I, [P, I, P]),
+            "nalu_learned_init": (I, [P, ctypes.c_uint64]),
+            "nalu_learned_set_weights": (I, [P, P, I64]),
+            "nalu_learned_get_weights": (I, [P, P, I64]),
+            "nalu_learned_harvest": (I, [P, I, ctypes.c_uint64, I64, P, P, P, P, ctypes.POINTER(I64)]),
+            "nalu_train_opts_default": (None, [P]),
+            "nalu_learned_train": (I, [P, P, P, P, I64, P, P]),
+            "nalu_learned_gradient": (I, [P, P, P, P, I64, P, ctypes.POINTER(D)]),
+            "nalu_learned_stencil": (I, [P, P]),
             "nalu_solve_batched": (I, [P, P, P]),
             "nalu_kernel_launch_count": (I64, [P]),
             "nalu_last_assemble_ms": (D, [P]),
@@ -290,6 +305,58 @@ class Context:
         if raise_on_error:
             self._check(rc, "solve_batched")
         return list(infos)
+
+    # learned preconditioner
+    def learned_init(self, seed=0):
+        self._check(lib().nalu_learned_init(self._h, int(seed)), "learned_init")
+
+    def learned_set_weights(self, params):
+        w = np.ascontiguousarray(params, np.float32)
+        self._check(lib().nalu_learned_set_weights(self._h, _ptr(w), w.size), "learned_set_weights")
+
+    def learned_weights(self):
+        w = np.zeros(LEARNED_PARAMS, np.float32)
+        self._check(lib().nalu_learned_get_weights(self._h, _ptr(w), w.size), "learned_get_weights")
+        return w
+
+    def learned_harvest(self, n_samples=20000, n_rhs=4, seed=0, with_rows=False):
+        """(static [n,81], residual [n,27], targets [n]) float32 training pairs (+ rows)."""
+        st = np.zeros((n_samples, 81), np.float32)
+        rf = np.zeros((n_samples, 27), np.float32)
+        tg = np.zeros(n_samples, np.float32)
+        rows = np.zeros(n_samples, np.int64)
+        got = ctypes.c_int64()
+        self._check(lib().nalu_learned_harvest(self._h, int(n_rhs), int(seed), int(n_samples), _ptr(st), _ptr(rf),
+                                               _ptr(tg), _ptr(rows), ctypes.byref(got)), "learned_harvest")
+        k = got.value
+        out = (st[:k].copy(), rf[:k].copy(), tg[:k].copy())
+        return out + (rows[:k].copy(),) if with_rows else out
+
+    def learned_train(self, st, rf, tg, **kw):
+        """Adam on the GPU; returns the [epochs, 2] train / held-out MSE history."""
+        o = TrainOpts()
+        lib().nalu_train_opts_default(ctypes.byref(o))
+        for k, v in kw.items():
+            setattr(o, k, v)
+        st, rf, tg = (np.ascontiguousarray(a, np.float32) for a in (st, rf, tg))
+        hist = np.zeros((o.epochs, 2), np.float32)
+        self._check(lib().nalu_learned_train(self._h, _ptr(st), _ptr(rf), _ptr(tg), tg.size, ctypes.byref(o),
+                                             _ptr(hist)), "learned_train")
+        return hist
+
+    def learned_gradient(self, st, rf, tg):
+        st, rf, tg = (np.ascontiguousarray(a, np.float32) for a in (st, rf, tg))
+        g = np.zeros(LEARNED_PARAMS, np.float32)
+        loss = ctypes.c_double()
+        self._check(lib().nalu_learned_gradient(self._h, _ptr(st), _ptr(rf), _ptr(tg), tg.size, _ptr(g),
+                                                ctypes.byref(loss)), "learned_gradient")
+        return loss.value, g
+
+    def learned_stencil(self):
+        nr, _, _ = self.sizes()
+        c = np.zeros((nr, 27), np.float32)
+        self._check(lib().nalu_learned_stencil(self._h, _ptr(c)), "learned_stencil")
+        return c
 
     def solution(self):
         nr, _, _ = self.sizes()

@@ -23,6 +23,7 @@ int set_error(nalu_ctx* ctx, int status, const std::string& msg) {
 
 int cuda_check(nalu_ctx* ctx, cudaError_t e, const char* what) {
   if (e == cudaSuccess) return NALU_OK;
+  cudaGetLastError();  // clear a pending launch error so that it does not resurface in a later call
   return set_error(ctx, NALU_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
@@ -255,6 +256,8 @@ int nalu_mesh_create(nalu_ctx* ctx, int64_t n_nodes, int64_t n_elems, const int3
   ctx->n_nodes = n_nodes;
   ctx->n_elems = n_elems;
   ctx->num_dof = 0;
+  ctx->learned.nbr_nodes = 0;  // the slot map belongs to the previous mesh
+  ctx->problem_offsets.clear();
   // LIDs: nodes sorted by global id (beginLinearSystemConstruction, :262-275)
   ctx->h_lid.assign(n_nodes, 0);
   ctx->identity_order = true;
@@ -760,6 +763,7 @@ void nalu_solver_opts_default(nalu_solver_opts* o) {
   o->x0_zero = 1;
   o->tol = 1e-8;
   o->inner_tol = 1e-4;
+  o->stall_window = 20;
 }
 
 int nalu_solve(nalu_ctx* ctx, const nalu_solver_opts* opts, nalu_solve_info* info) {

@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "internal.h"
+#include "reduce.cuh"
 
 namespace nalu_gb300 {
 
@@ -35,43 +36,9 @@ constexpr int kCgThreads = 256;
 
 namespace {
 
-__device__ __forceinline__ double warp_sum_d(double v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
-
-// sum of `n` partials, identical in every block (fixed order), broadcast
-__device__ __forceinline__ double block_total(const double* __restrict__ part, int n, double* sh) {
-  double s = 0.0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) s += part[i];
-  s = warp_sum_d(s);
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  if (lane == 0) sh[w] = s;
-  __syncthreads();
-  if (w == 0) {
-    double t = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0.0;
-    t = warp_sum_d(t);
-    if (lane == 0) sh[32] = t;
-  }
-  __syncthreads();
-  const double total = sh[32];
-  __syncthreads();
-  return total;
-}
-
-__device__ __forceinline__ void block_store(double v, double* __restrict__ out, double* sh) {
-  v = warp_sum_d(v);
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  if (lane == 0) sh[w] = v;
-  __syncthreads();
-  if (w == 0) {
-    double t = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0.0;
-    t = warp_sum_d(t);
-    if (lane == 0) *out = t;
-  }
-  __syncthreads();
-}
+using red::block_store;
+using red::block_total;
+using red::warp_sum_d;
 
 // slice lengths (max row length in each slice of 32 rows)
 __global__ void k_sell_len(int64_t n, const int64_t* __restrict__ rp, int32_t* __restrict__ slen, int64_t nslices) {

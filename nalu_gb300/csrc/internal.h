@@ -50,6 +50,18 @@ struct SellMatrix {
   int64_t nslices = 0, stored = 0;
 };
 
+// Learned preconditioner state (learned.cu).  The MLP parameters are FP32
+// master copies; the stencil and its SELL values are rebuilt per solve.
+struct LearnedState {
+  DBuf<float> params, adam_m, adam_v, grad;  // [kLearnedParams]
+  DBuf<uint16_t> wbf;                         // BF16 W2/W3 in the padded kernel layout
+  DBuf<int32_t> nbr;                          // [n][27] neighbour LID per topological slot, -1 if none
+  DBuf<float> stencil;                        // [n][27] MLP output per slot
+  DBuf<float> wsell;                          // preconditioner values on the SELL pattern of A
+  int64_t nbr_nodes = 0;                      // mesh size the slot map was built for
+  bool has_weights = false;
+};
+
 // Solver workspace (device vectors are allocated lazily per system size).
 struct SolverWork {
   SellMatrix sell;
@@ -108,6 +120,7 @@ struct nalu_ctx {
   nalu_gb300::DBuf<uint8_t> flush_buf;
 
   nalu_gb300::SolverWork sw;
+  nalu_gb300::LearnedState learned;
 };
 
 namespace nalu_gb300 {
@@ -145,9 +158,17 @@ int probe_fp64(nalu_ctx* ctx, double* tflops);
 // krylov.cu
 int solve(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* info);
 int spmv_fp64(nalu_ctx* ctx, const double* x, double* y);
+int compute_dinv(nalu_ctx* ctx);  // sw.dinv and d_bcmask for the current matrix
 // cg_fast.cu
 template <class VT>
 int sell_build(nalu_ctx* ctx, SellMatrix& S, const VT** vals_out);
+// learned.cu
+int learned_prepare(nalu_ctx* ctx);  // slot map, stencil and SELL preconditioner for the current matrix
+// flexible CG with the learned preconditioner on A x = r (x from 0); returns
+// NALU_ERR_NOT_CONVERGED with *stalled = 1 when the residual made no progress
+// for `stall_window` iterations
+int fcg_learned(nalu_ctx* ctx, double* x, double* r, double rtol, double r0norm, int max_it, int check_every,
+                int stall_window, int* iters_out, int* stalled);
 template <class T, class VT>
 int pcg_fast(nalu_ctx* ctx, const VT* sval, const SellMatrix& S, T* x, T* r, T* z, T* p0, T* p1, T* q,
              const T* dinv, double rtol, double r0norm, int max_it, int check_every, int* iters_out);

@@ -621,6 +621,18 @@ int gmres(nalu_ctx* ctx, const Mat<VT>& A, Work<T>& w, double rtol, int max_it, 
 
 }  // namespace
 
+// FP64 inverse diagonal into the solver workspace and the identity-row mask
+int compute_dinv(nalu_ctx* ctx) {
+  const int64_t n = ctx->n_rows;
+  int rc = ensure(ctx, ctx->sw.dinv, n);
+  if (rc) return rc;
+  if (ctx->d_bcmask.n < n) NALU_CUDA(ctx, ctx->d_bcmask.alloc(n));
+  k_dinv<double, double><<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(
+      n, ctx->d_rowptr.p, ctx->d_colind.p, ctx->d_values.p, ctx->sw.dinv.p, ctx->d_bcmask.p);
+  ctx->launches++;
+  return cuda_check(ctx, cudaGetLastError(), "dinv");
+}
+
 int spmv_fp64(nalu_ctx* ctx, const double* x, double* y) {
   Mat<double> A{ctx->n_rows, ctx->d_rowptr.p, ctx->d_colind.p, ctx->d_values.p, ctx->num_dof >= 3 ? 16 : 8};
   spmv_launch<double, double, false>(ctx, A, x, y, nullptr);
@@ -690,6 +702,14 @@ int solve(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* info) {
     return std::sqrt(read_scalar(ctx, s.scal.p + S_BB));
   }();
   const double bref = bnorm > 0 ? bnorm : 1.0;
+  const bool learned = o.precond == NALU_PRECOND_LEARNED;
+  if (learned && (o.method != NALU_SOLVER_CG || mixed))
+    return set_error(ctx, NALU_ERR_ARG, "the learned preconditioner runs in FP64 flexible CG only");
+  bool fallback = false;
+  int learned_its = 0;
+  double setup_s = 0.0;
+  nalu_solver_opts fb = o;  // Chebyshev-Jacobi PCG after a stall of the learned FCG
+  fb.precond = NALU_PRECOND_CHEBYSHEV;
   int total_it = 0, outer = 0;
   double res = true_residual(ctx, ctx->d_x.p, s.tmp.p) / bref;
   const int max_outer = mixed ? 60 : 8;
@@ -705,7 +725,22 @@ int solve(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* info) {
         return rc;
       if (o.method == NALU_SOLVER_GMRES && (rc = ensure(ctx, s.V, (int64_t)(m + 1) * n))) return rc;
       cudaMemcpyAsync(s.r.p, s.tmp.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->stream);
-      if (o.method == NALU_SOLVER_CG && o.precond == NALU_PRECOND_JACOBI) {
+      if (learned && !fallback) {
+        // flexible CG with the learned stencil (learned.cu)
+        const auto ts = std::chrono::steady_clock::now();
+        const double* sv = nullptr;
+        if (outer == 1 && ((rc = sell_build<double>(ctx, s.sell, &sv)) || (rc = learned_prepare(ctx)))) return rc;
+        NALU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        setup_s += std::chrono::duration<double>(std::chrono::steady_clock::now() - ts).count();
+        int stalled = 0;
+        rc = fcg_learned(ctx, s.w.p, s.r.p, rtol, r0, o.max_iters - total_it, o.check_every,
+                         o.stall_window > 0 ? o.stall_window : 20, &its, &stalled);
+        learned_its += its;
+        if (stalled) {
+          fallback = true;
+          rc = NALU_OK;
+        }
+      } else if (o.method == NALU_SOLVER_CG && o.precond == NALU_PRECOND_JACOBI) {
         // two-kernel Jacobi-CG on the SELL-32 copy (cg_fast.cu)
         const double* sv = nullptr;
         if (outer == 1 && (rc = sell_build<double>(ctx, s.sell, &sv))) return rc;
@@ -713,8 +748,8 @@ int solve(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* info) {
         rc = pcg_fast<double, double>(ctx, sv, s.sell, s.w.p, s.r.p, s.z.p, s.p.p, s.ap.p, s.q.p, s.dinv.p, rtol, r0,
                                       o.max_iters - total_it, o.check_every, &its);
       } else {
-        rc = run_inner<double>(ctx, o, s.r.p, s.w.p, s.z.p, s.p.p, s.q.p, s.dinv.p, s.V.p, s.ap.p, s.tmp.p,
-                               ctx->d_values.p, false, rtol, r0, o.max_iters - total_it, &its);
+        rc = run_inner<double>(ctx, learned ? fb : o, s.r.p, s.w.p, s.z.p, s.p.p, s.q.p, s.dinv.p, s.V.p, s.ap.p,
+                               s.tmp.p, ctx->d_values.p, false, rtol, r0, o.max_iters - total_it, &its);
       }
       k_add_to<double><<<grid_for(n, 256), 256, 0, ctx->stream>>>(n, ctx->d_x.p, s.w.p);
     } else {
@@ -760,6 +795,9 @@ int solve(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* info) {
   NALU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   info->iterations = total_it;
   info->outer_iterations = outer;
+  info->fallback = fallback ? 1 : 0;
+  info->learned_iterations = learned_its;
+  info->setup_seconds = setup_s;
   info->true_rel_res = res;
   info->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   if (rc == NALU_OK && res > o.tol) rc = set_error(ctx, NALU_ERR_NOT_CONVERGED, "tolerance not reached");

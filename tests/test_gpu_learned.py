@@ -1,0 +1,129 @@
+"""Learned preconditioner on the GPU: the training gradient and the BF16
+tensor-core stencil against the FP64 numpy reference model, the harvested
+features against host-computed ones, and flexible CG with the learned
+stencil (convergence, fewer iterations than Jacobi-PCG, and the
+Chebyshev-Jacobi fallback after a stall)."""
+import numpy as np
+import pytest
+
+import mlp_ref as M
+import nalu_gb300 as ng
+from helpers import block_mesh
+from nalu_gb300.meshgen import fourier_velocity
+
+pytestmark = pytest.mark.gpu
+
+
+def _continuity(gpu_ctx_factory, N, seed=1, jitter=0.0):
+    c, conn, gid = block_mesh(N, z_ratio=1.05, jitter=jitter, seed=seed)
+    n = c.shape[0]
+    ctx = gpu_ctx_factory()
+    ctx.mesh_create(c, conn, gid)
+    ctx.field_set("velocity", fourier_velocity(c, n_modes=64, seed=seed))
+    ctx.field_set("density", np.ones(n))
+    ctx.field_set("pressure", np.zeros(n))
+    ctx.field_set("dpdx", np.zeros((n, 3)))
+    ctx.build_elem_graph(1)
+    ctx.zero()
+    ctx.assemble(ng.KERNEL_CONTINUITY_ADV)
+    ctx.reset_rows([0])
+    ctx.sum_into_diag(0, 0, 1.0, 0.0)
+    ctx.load_complete()
+    return ctx, c, conn
+
+
+def test_learned_gradient_matches_reference(gpu_ctx_factory):
+    ctx = gpu_ctx_factory()
+    P = M.random_params(11).astype(np.float32)
+    ctx.learned_set_weights(P)
+    st, rf, tg = (a.astype(np.float32) for a in M.random_samples(96, 12))
+    loss, g = ctx.learned_gradient(st, rf, tg)
+    lref, gref = M.loss_and_grad(P.astype(np.float64), st, rf, tg)
+    assert abs(loss - lref) <= 1e-4 * lref
+    for k, (o, s) in M.SL.items():
+        sl = slice(o, o + int(np.prod(s)))
+        err = np.linalg.norm(g[sl] - gref[sl])
+        assert err <= 2e-4 * np.linalg.norm(gref[sl]) + 1e-7, (k, err, np.linalg.norm(gref[sl]))
+    ctx.close()
+
+
+def test_learned_stencil_matches_reference(gpu_ctx_factory):
+    ctx, c, conn = _continuity(gpu_ctx_factory, 10)
+    P = M.random_params(13).astype(np.float32)
+    ctx.learned_set_weights(P)
+    sten = ctx.learned_stencil()
+    rp, ci = ctx.graph()
+    v, _ = ctx.system()
+    nbr = M.slot_map(conn, c.shape[0])
+    st, _ = M.static_features(rp, ci, v, nbr)
+    ref = M.stencil(P.astype(np.float64), st)
+    ref[0] = 0.0  # the pinned row is an identity row
+    # BF16 weights and activations, FP32 accumulation
+    err = np.abs(sten - ref)
+    assert np.max(err) <= 2e-2 * np.max(np.abs(ref)), (np.max(err), np.max(np.abs(ref)))
+    assert np.all(sten[nbr < 0] == 0.0)
+    ctx.close()
+
+
+def test_learned_harvest_features(gpu_ctx_factory):
+    ctx, c, conn = _continuity(gpu_ctx_factory, 9)
+    ctx.learned_init(1)
+    st, rf, tg, rows = ctx.learned_harvest(n_samples=600, n_rhs=3, seed=5, with_rows=True)
+    assert 500 <= st.shape[0] <= 600 and np.all(rows > 0)  # row 0 is the identity row
+    rp, ci = ctx.graph()
+    v, _ = ctx.system()
+    nbr = M.slot_map(conn, c.shape[0])
+    sth, _ = M.static_features(rp, ci, v, nbr)
+    np.testing.assert_array_equal(st, sth[rows])
+    np.testing.assert_allclose((rf.astype(np.float64) ** 2).sum(1) / 27, 1.0, rtol=1e-5)
+    assert np.all(rf[nbr[rows] < 0] == 0.0)
+    assert np.all(np.isfinite(tg)) and np.std(tg) > 0
+    ctx.close()
+
+
+def test_learned_fcg_fewer_iterations_than_jacobi(gpu_ctx_factory, oracle):
+    ctx, _, _ = _continuity(gpu_ctx_factory, 24)
+    ctx.learned_init(1)
+    st, rf, tg = ctx.learned_harvest(n_samples=20000, n_rhs=4, seed=2)
+    hist = ctx.learned_train(st, rf, tg, epochs=30)
+    assert hist[-1, 1] < 0.5 * hist[0, 1] or hist[-1, 1] < 0.05, hist[[0, -1]]
+    plain = ctx.solve(ng.default_solver_opts(tol=1e-8, max_iters=20000))
+    xp = ctx.solution()
+    info = ctx.solve(ng.default_solver_opts(tol=1e-8, max_iters=20000, precond=ng.PRECOND_LEARNED))
+    x = ctx.solution()
+    rp, ci = ctx.graph()
+    v, b = ctx.system()
+    res = np.linalg.norm(b - oracle.spmv(rp, ci, v, x)) / np.linalg.norm(b)
+    assert info.status == 0 and info.fallback == 0 and res <= 1.05e-8, (info.status, info.fallback, res)
+    assert info.learned_iterations < 0.8 * plain.iterations, (info.learned_iterations, plain.iterations)
+    assert np.max(np.abs(x - xp)) <= 1e-4 * np.max(np.abs(xp))
+    ctx.close()
+
+
+@pytest.mark.parametrize("out_scale", [50.0, 1e37])
+def test_learned_breakdown_falls_back_to_chebyshev(gpu_ctx_factory, oracle, out_scale):
+    """An output layer far too large makes the stencil indefinite (a
+    non-positive FCG step), or overflows it to non-finite values; the FCG
+    stops and Chebyshev-Jacobi PCG finishes the solve."""
+    ctx, _, _ = _continuity(gpu_ctx_factory, 12)
+    P = M.random_params(17, out_scale=out_scale).astype(np.float32)
+    ctx.learned_set_weights(P)
+    info = ctx.solve(ng.default_solver_opts(tol=1e-8, max_iters=20000, precond=ng.PRECOND_LEARNED))
+    x = ctx.solution()
+    rp, ci = ctx.graph()
+    v, b = ctx.system()
+    res = np.linalg.norm(b - oracle.spmv(rp, ci, v, x)) / np.linalg.norm(b)
+    assert info.fallback == 1 and info.status == 0 and res <= 1.05e-8, (info.fallback, info.status, res)
+    ctx.close()
+
+
+def test_learned_errors(gpu_ctx_factory):
+    ctx, _, _ = _continuity(gpu_ctx_factory, 4)
+    with pytest.raises(ng.NaluError):  # no weights yet
+        ctx.solve(ng.default_solver_opts(precond=ng.PRECOND_LEARNED))
+    ctx.learned_init(0)
+    with pytest.raises(ng.NaluError):  # learned runs in FP64 CG only
+        ctx.solve(ng.default_solver_opts(precond=ng.PRECOND_LEARNED, method=ng.SOLVER_GMRES))
+    with pytest.raises(ng.NaluError):
+        ctx.learned_set_weights(np.zeros(10, np.float32))
+    ctx.close()
