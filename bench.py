@@ -277,6 +277,25 @@ def bench_gpu(args):
                            "outer_iterations": info.outer_iterations, "true_rel_res": info.true_rel_res,
                            "status": info.status}
         solve["system"] = "continuity Laplacian of the same mesh, pressure pinned at node 0 (resetRows + diag 1)"
+        # learned preconditioner: 20K pairs from PCG's first direction for 4 seeded random rhs of this
+        # 128^3 system, Adam on the GPU, then flexible CG with the learned stencil
+        t0 = time.perf_counter()
+        ctx.learned_init(7)
+        st, rf, tg = ctx.learned_harvest(n_samples=20000, n_rhs=4, seed=2024)
+        t1 = time.perf_counter()
+        hist = ctx.learned_train(st, rf, tg, epochs=40)
+        t2 = time.perf_counter()
+        learned_w = ctx.learned_weights()
+        info = ctx.solve(ng.default_solver_opts(tol=1e-8, max_iters=40000, precond=ng.PRECOND_LEARNED),
+                         raise_on_error=False)
+        solve["learned_fcg"] = {"ms": 1e3 * info.seconds, "setup_ms": 1e3 * info.setup_seconds,
+                                "iterations": info.iterations, "learned_iterations": info.learned_iterations,
+                                "fallback": info.fallback, "true_rel_res": info.true_rel_res, "status": info.status}
+        solve["learned_training"] = {"pairs": int(tg.size), "harvest_s": t1 - t0, "train_s": t2 - t1,
+                                     "epochs": 40, "val_mse_first_last": [float(hist[0, 1]), float(hist[-1, 1])]}
+        solve["learned_vs_plain_time"] = solve["jacobi_pcg_fp64"]["ms"] / solve["learned_fcg"]["ms"]
+        if not args.no_c4:
+            solve["c4_192"] = bench_c4(ng, learned_w)
     batch = None if args.no_batch else bench_batch(ng)
     # ---- CPU baseline on rank 0 (oracle, bounded sample) ----
     cpu = None
@@ -316,6 +335,40 @@ def bench_gpu(args):
     if dist is not None:
         dist.destroy_process_group()
     return 0
+
+
+def bench_c4(ng, weights, N=192):
+    """Continuity solve on 192^3 (z-stretch 1.05, Fourier64 velocity, pressure
+    pinned at node 0): plain Jacobi-PCG against flexible CG with the learned
+    preconditioner trained on the 128^3 system."""
+    from nalu_gb300.meshgen import block_mesh, fourier_velocity
+    c, conn, gid = block_mesh(N, z_ratio=1.05)
+    n = c.shape[0]
+    ctx = ng.Context(0)
+    ctx.mesh_create(c, conn, gid)
+    ctx.field_set("velocity", fourier_velocity(c, n_modes=64, kmin=1, kmax=16, seed=2024))
+    ctx.field_set("density", np.ones(n))
+    ctx.field_set("pressure", np.zeros(n))
+    ctx.field_set("dpdx", np.zeros((n, 3)))
+    ctx.build_elem_graph(1)
+    ctx.zero()
+    ctx.assemble(ng.KERNEL_CONTINUITY_ADV)
+    ctx.reset_rows([0])
+    ctx.sum_into_diag(0, 0, 1.0, 0.0)
+    ctx.load_complete()
+    ctx.learned_set_weights(weights)
+    out = {"workload": "continuity_adv_hex8_192^3_zstretch1.05_fourier64, pinned node 0", "nodes": int(n),
+           "nnz": int(ctx.sizes()[1])}
+    for name, kw in (("jacobi_pcg_fp64", {}), ("learned_fcg", {"precond": ng.PRECOND_LEARNED})):
+        info = ctx.solve(ng.default_solver_opts(tol=1e-8, max_iters=60000, check_every=50, **kw), raise_on_error=False)
+        out[name] = {"ms": 1e3 * info.seconds, "iterations": info.iterations, "true_rel_res": info.true_rel_res,
+                     "status": info.status}
+        if kw:
+            out[name].update(setup_ms=1e3 * info.setup_seconds, learned_iterations=info.learned_iterations,
+                             fallback=info.fallback)
+    out["learned_vs_plain_time"] = out["jacobi_pcg_fp64"]["ms"] / out["learned_fcg"]["ms"]
+    ctx.close()
+    return out
 
 
 def bench_batch(ng, n_problems=64, seed=2025, reps=2):
@@ -394,6 +447,7 @@ def main():
     ap.add_argument("--no-solve", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-problem batched workload")
+    ap.add_argument("--no-c4", action="store_true", help="skip the 192^3 learned-vs-plain continuity solve")
     ap.add_argument("--size", type=int, default=128, help="elements per edge (default: the 128^3 workload)")
     ap.add_argument("--arith", default="auto", choices=["auto", "fp64", "df64"],
                     help="element-math arithmetic (auto: the faster; both pass the parity tests)")

@@ -181,9 +181,9 @@ typedef struct nalu_solver_opts {
   double tol;        /* stop on true ||b - A x|| / ||b|| <= tol */
   double inner_tol;  /* inner tolerance for iterative refinement */
   int stall_window;  /* learned FCG stalls when the residual norm has no new
-                        minimum for max(stall_window, iterations taken to reach
-                        the current minimum); Chebyshev-Jacobi PCG then
-                        finishes (default 20) */
+                        minimum for max(stall_window, 4 x the iterations taken
+                        to reach the current minimum); Chebyshev-Jacobi PCG
+                        then finishes (default 20) */
   int reserved[5];
 } nalu_solver_opts;
 typedef struct nalu_solve_info {
@@ -228,7 +228,8 @@ int nalu_solve_batched(nalu_ctx* ctx, const nalu_solver_opts* opts, nalu_solve_i
  * z_i = (r_i + rms_i * mlp_i) / a_ii.  At solve set-up the MLP is evaluated
  * on the 27 unit-impulse residuals of every node (BF16 tensor-core kernel),
  * which gives a 27-point stencil C; the preconditioner is the symmetric part
- * of D^-1 (I + C), applied with the sparsity of A.
+ * of D^-1 (I + C) on the sparsity of A, its off-diagonals scaled symmetrically
+ * so that D^1/2 M D^1/2 is diagonally dominant (M is then positive definite).
  * Parameters (FP32, NALU_LEARNED_PARAMS): W1[64][108], b1[64], W2[64][64],
  * b2[64], W3[64][64], b3[64], w4[64], b4. */
 #define NALU_LEARNED_PARAMS 15361

@@ -23,10 +23,12 @@
 
 #include <cmath>
 #include <cstdint>
+#include <type_traits>
 #include <vector>
 
 #include "internal.h"
 #include "reduce.cuh"
+#include "spmv_df.cuh"
 
 namespace nalu_gb300 {
 
@@ -53,6 +55,15 @@ __global__ void k_sell_len(int64_t n, const int64_t* __restrict__ rp, int32_t* _
 }
 
 template <class VT>
+__device__ __forceinline__ VT sell_value(double v) {
+  return (VT)v;
+}
+template <>
+__device__ __forceinline__ float2 sell_value<float2>(double v) {
+  return split_df(v);
+}
+
+template <class VT>
 __global__ void k_sell_fill(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
                             const double* __restrict__ v, const int64_t* __restrict__ sptr,
                             const int32_t* __restrict__ slen, int32_t* __restrict__ scol, VT* __restrict__ sval) {
@@ -66,7 +77,7 @@ __global__ void k_sell_fill(int64_t n, const int64_t* __restrict__ rp, const int
   for (int k = 0; k < sl; ++k) {
     const bool real = k < len;
     scol[base + (int64_t)k * kSlice] = real ? ci[b + k] : (int32_t)row;
-    sval[base + (int64_t)k * kSlice] = real ? (VT)v[b + k] : (VT)0;
+    sval[base + (int64_t)k * kSlice] = sell_value<VT>(real ? v[b + k] : 0.0);
   }
 }
 
@@ -166,6 +177,102 @@ void cg_iteration(nalu_ctx* ctx, int k, int first, int64_t n, int64_t npad, cons
   ctx->launches += 3;
 }
 
+// ---- FP64 Jacobi-CG with the df64 SpMV and single-block scalar reductions ----
+__global__ void k_convert_f(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+
+// scalars: cs[CS_RZ] = r.z, cs[CS_ALPHA], cs[CS_BETA], cs[CS_RR] = r.r, cs[CS_PQ]
+enum { CS_RZ = 0, CS_ALPHA = 1, CS_BETA = 2, CS_RR = 3, CS_PQ = 4 };
+
+// Jacobi with the FP32-rounded inverse diagonal (the same one the iterations use)
+__global__ void __launch_bounds__(kCgThreads) k_cgd_init(int64_t n, const double* __restrict__ r,
+                                                         const float* __restrict__ dinvf,
+                                                         double* __restrict__ part, unsigned* __restrict__ cnt,
+                                                         double* __restrict__ cs) {
+  __shared__ double sh[33];
+  double rz = 0.0, rr = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double ri = r[i];
+    rz += ri * (widen_f(dinvf[i]) * ri);
+    rr += ri * ri;
+  }
+  const double v[2] = {rz, rr};
+  double t[2];
+  if (red::grid_reduce<2>(v, part, kCgBlocks, cnt, t, sh) && threadIdx.x == 0) {
+    cs[CS_RZ] = t[0];
+    cs[CS_RR] = t[1];
+  }
+}
+
+// p = D^-1 r + beta p (p held as FP32 pairs)
+__global__ void __launch_bounds__(kCgThreads) k_cgd_pupdate(int64_t n, const double* __restrict__ r,
+                                                            const float* __restrict__ dinvf,
+                                                            float2* __restrict__ p, const double* __restrict__ cs,
+                                                            int first) {
+  // all in FP32 pairs: z = D^-1 r (D^-1 an FP32 value), p = z + beta p
+  const float2 beta = split_df(first ? 0.0 : cs[CS_BETA]);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float2 z = fma_df(split_df(r[i]), make_float2(dinvf[i], 0.0f), make_float2(0.0f, 0.0f));
+    p[i] = first ? z : fma_df(beta, p[i], z);
+  }
+}
+
+// q = A p; alpha = r.z / p.q by the last block
+__global__ void __launch_bounds__(kCgThreads) k_cgd_spmv(int64_t n, int64_t npad, const int64_t* __restrict__ sptr,
+                                                         const int32_t* __restrict__ slen,
+                                                         const int32_t* __restrict__ scol,
+                                                         const float2* __restrict__ sval,
+                                                         const float2* __restrict__ p, double* __restrict__ q,
+                                                         double* __restrict__ part, unsigned* __restrict__ cnt,
+                                                         double* __restrict__ cs) {
+  __shared__ double sh[33];
+  double dot = 0.0;
+  for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < npad;
+       row += (int64_t)gridDim.x * blockDim.x) {
+    if (row >= n) continue;
+    const int64_t s = row / kSlice;
+    const double qi = sell_row_df(__ldg(sptr + s) + (row % kSlice), __ldg(slen + s), scol, sval, p);
+    q[row] = qi;
+    dot += join_df(p[row]) * qi;
+  }
+  const double v[1] = {dot};
+  double t[1];
+  if (red::grid_reduce<1>(v, part, kCgBlocks, cnt, t, sh) && threadIdx.x == 0) {
+    cs[CS_PQ] = t[0];
+    cs[CS_ALPHA] = cs[CS_RZ] / t[0];
+  }
+}
+
+// x += alpha p; r -= alpha q; r.D^-1 r and r.r as FP32 pairs (the FP64 pipe
+// keeps only the two updates); beta = rz_new / rz by the last block
+__global__ void __launch_bounds__(kCgThreads) k_cgd_axpy(int64_t n, double* __restrict__ x,
+                                                         const float2* __restrict__ p, double* __restrict__ r,
+                                                         const double* __restrict__ q,
+                                                         const float* __restrict__ dinvf,
+                                                         double* __restrict__ part, unsigned* __restrict__ cnt,
+                                                         double* __restrict__ cs) {
+  __shared__ double sh[33];
+  const double alpha = cs[CS_ALPHA];
+  float zh = 0.0f, zl = 0.0f, rh = 0.0f, rl = 0.0f;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    x[i] += alpha * join_df(p[i]);
+    const double ri = r[i] - alpha * q[i];
+    r[i] = ri;
+    const float2 rs = split_df(ri);
+    acc_sq_df(zh, zl, rs, dinvf[i]);
+    acc_sq_df(rh, rl, rs, 1.0f);
+  }
+  const double v[2] = {join_df(make_float2(zh, zl)), join_df(make_float2(rh, rl))};
+  double t[2];
+  if (red::grid_reduce<2>(v, part, kCgBlocks, cnt, t, sh) && threadIdx.x == 0) {
+    cs[CS_BETA] = t[0] / cs[CS_RZ];
+    cs[CS_RZ] = t[0];
+    cs[CS_RR] = t[1];
+  }
+}
+
 }  // namespace
 
 // Build the SELL-32 copy of the context's matrix (values as VT).
@@ -186,7 +293,10 @@ int sell_build(nalu_ctx* ctx, SellMatrix& S, const VT** vals_out) {
   NALU_CUDA(ctx, cudaMemcpyAsync(S.ptr.p, hp.data(), sizeof(int64_t) * (ns + 1), cudaMemcpyHostToDevice, ctx->stream));
   if (S.col.n < total) NALU_CUDA(ctx, S.col.alloc(total));
   VT* vals = nullptr;
-  if constexpr (sizeof(VT) == 8) {
+  if constexpr (std::is_same<VT, float2>::value) {
+    if (S.val2.n < total) NALU_CUDA(ctx, S.val2.alloc(total));
+    vals = reinterpret_cast<VT*>(S.val2.p);
+  } else if constexpr (sizeof(VT) == 8) {
     if (S.vald.n < total) NALU_CUDA(ctx, S.vald.alloc(total));
     vals = reinterpret_cast<VT*>(S.vald.p);
   } else {
@@ -269,7 +379,79 @@ int pcg_fast(nalu_ctx* ctx, const VT* sval, const SellMatrix& S, T* x, T* r, T* 
   return rc;
 }
 
+// FP64 Jacobi-CG on A x = r (x from 0) with the df64 SpMV on S.val2;
+// r holds the initial residual; on return x holds the solution increment.
+int pcg_df(nalu_ctx* ctx, const SellMatrix& S, double* x, double* r, double* z, double* q, const double* dinv,
+           double rtol, double r0norm, int max_it, int check_every, int* iters_out) {
+  const int64_t n = ctx->n_rows;
+  const int64_t npad = S.nslices * kSlice;
+  SolverWork& w = ctx->sw;
+  if (w.partial.n < 2 * kCgBlocks) NALU_CUDA(ctx, w.partial.alloc(2 * kCgBlocks));
+  if (w.p2.n < n) NALU_CUDA(ctx, w.p2.alloc(n));
+  if (w.cscal.n < 8) NALU_CUDA(ctx, w.cscal.alloc(8));
+  if (w.ccount.n < 1) NALU_CUDA(ctx, w.ccount.alloc(1));
+  double* part = w.partial.p;
+  unsigned* cnt = w.ccount.p;
+  double* cs = w.cscal.p;
+  float2* p = w.p2.p;
+  cudaStream_t st = ctx->stream;
+  NALU_CUDA(ctx, cudaMemsetAsync(cnt, 0, sizeof(unsigned), st));
+  NALU_CUDA(ctx, cudaMemsetAsync(cs, 0, sizeof(double) * 8, st));
+  NALU_CUDA(ctx, cudaMemsetAsync(x, 0, sizeof(double) * n, st));
+  if (w.fdinv.n < n) NALU_CUDA(ctx, w.fdinv.alloc(n));
+  float* dinvf = w.fdinv.p;
+  k_convert_f<<<kCgBlocks, kCgThreads, 0, st>>>(n, dinv, dinvf);
+  k_cgd_init<<<kCgBlocks, kCgThreads, 0, st>>>(n, r, dinvf, part, cnt, cs);
+  ctx->launches++;
+  auto iteration = [&](int first) {
+    k_cgd_pupdate<<<kCgBlocks, kCgThreads, 0, st>>>(n, r, dinvf, p, cs, first);
+    k_cgd_spmv<<<kCgBlocks, kCgThreads, 0, st>>>(n, npad, S.ptr.p, S.len.p, S.col.p, S.val2.p, p, q, part, cnt, cs);
+    k_cgd_axpy<<<kCgBlocks, kCgThreads, 0, st>>>(n, x, p, r, q, dinvf, part, cnt, cs);
+    ctx->launches += 3;
+  };
+  ctx->launches++;
+  iteration(1);
+  const int chunk = check_every > 0 ? check_every : 50;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaError_t ce = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+  if (ce != cudaSuccess) return cuda_check(ctx, ce, "begin capture");
+  for (int k = 0; k < chunk; ++k) iteration(0);
+  ce = cudaStreamEndCapture(st, &graph);
+  if (ce != cudaSuccess) return cuda_check(ctx, ce, "end capture");
+  ce = cudaGraphInstantiate(&exec, graph, 0);
+  if (ce != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    return cuda_check(ctx, ce, "instantiate");
+  }
+  const double stop = rtol * r0norm;
+  double rr = 0.0;
+  int it = 1;
+  bool bad = false, conv = false;
+  for (;;) {
+    NALU_CUDA(ctx, cudaMemcpyAsync(&rr, cs + CS_RR, sizeof(double), cudaMemcpyDeviceToHost, st));
+    NALU_CUDA(ctx, cudaStreamSynchronize(st));
+    if (!std::isfinite(rr)) {
+      bad = true;
+      break;
+    }
+    if (std::sqrt(rr) <= stop) {
+      conv = true;
+      break;
+    }
+    if (it >= max_it) break;
+    cudaGraphLaunch(exec, st);
+    it += chunk;
+  }
+  cudaGraphExecDestroy(exec);
+  cudaGraphDestroy(graph);
+  *iters_out = it;
+  if (bad) return set_error(ctx, NALU_ERR_NONFINITE, "CG breakdown (non-finite residual)");
+  return conv ? NALU_OK : NALU_ERR_NOT_CONVERGED;
+}
+
 template int sell_build<double>(nalu_ctx*, SellMatrix&, const double**);
+template int sell_build<float2>(nalu_ctx*, SellMatrix&, const float2**);
 template int sell_build<float>(nalu_ctx*, SellMatrix&, const float**);
 template int pcg_fast<double, double>(nalu_ctx*, const double*, const SellMatrix&, double*, double*, double*, double*,
                                       double*, double*, const double*, double, double, int, int, int*);

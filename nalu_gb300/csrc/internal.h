@@ -47,6 +47,7 @@ struct SellMatrix {
   DBuf<int32_t> col;
   DBuf<double> vald;
   DBuf<float> valf;
+  DBuf<float2> val2;   // FP32 pairs (hi, lo) for the df64 SpMV
   int64_t nslices = 0, stored = 0;
 };
 
@@ -71,6 +72,9 @@ struct SolverWork {
   DBuf<float> fV;
   DBuf<double> scal;     // device scalars
   DBuf<double> partial;  // block partial sums
+  DBuf<float2> p2;       // search direction as FP32 pairs (df64 SpMV)
+  DBuf<double> cscal;    // CG scalars written by the last block of each kernel
+  DBuf<unsigned> ccount; // arrival counter of the single-block reductions
   int64_t n = 0;
 };
 
@@ -169,6 +173,8 @@ int learned_prepare(nalu_ctx* ctx);  // slot map, stencil and SELL preconditione
 // for `stall_window` iterations
 int fcg_learned(nalu_ctx* ctx, double* x, double* r, double rtol, double r0norm, int max_it, int check_every,
                 int stall_window, int* iters_out, int* stalled);
+int pcg_df(nalu_ctx* ctx, const SellMatrix& S, double* x, double* r, double* z, double* q, const double* dinv,
+           double rtol, double r0norm, int max_it, int check_every, int* iters_out);
 template <class T, class VT>
 int pcg_fast(nalu_ctx* ctx, const VT* sval, const SellMatrix& S, T* x, T* r, T* z, T* p0, T* p1, T* q,
              const T* dinv, double rtol, double r0norm, int max_it, int check_every, int* iters_out);

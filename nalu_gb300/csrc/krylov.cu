@@ -728,8 +728,8 @@ int solve(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* info) {
       if (learned && !fallback) {
         // flexible CG with the learned stencil (learned.cu)
         const auto ts = std::chrono::steady_clock::now();
-        const double* sv = nullptr;
-        if (outer == 1 && ((rc = sell_build<double>(ctx, s.sell, &sv)) || (rc = learned_prepare(ctx)))) return rc;
+        const float2* sv2 = nullptr;
+        if (outer == 1 && ((rc = sell_build<float2>(ctx, s.sell, &sv2)) || (rc = learned_prepare(ctx)))) return rc;
         NALU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         setup_s += std::chrono::duration<double>(std::chrono::steady_clock::now() - ts).count();
         int stalled = 0;
@@ -743,10 +743,10 @@ int solve(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* info) {
       } else if (o.method == NALU_SOLVER_CG && o.precond == NALU_PRECOND_JACOBI) {
         // two-kernel Jacobi-CG on the SELL-32 copy (cg_fast.cu)
         const double* sv = nullptr;
-        if (outer == 1 && (rc = sell_build<double>(ctx, s.sell, &sv))) return rc;
-        sv = s.sell.vald.p;
-        rc = pcg_fast<double, double>(ctx, sv, s.sell, s.w.p, s.r.p, s.z.p, s.p.p, s.ap.p, s.q.p, s.dinv.p, rtol, r0,
-                                      o.max_iters - total_it, o.check_every, &its);
+        const float2* sv2 = nullptr;
+        if (outer == 1 && (rc = sell_build<float2>(ctx, s.sell, &sv2))) return rc;
+        rc = pcg_df(ctx, s.sell, s.w.p, s.r.p, s.z.p, s.q.p, s.dinv.p, rtol, r0, o.max_iters - total_it,
+                    o.check_every, &its);
       } else {
         rc = run_inner<double>(ctx, learned ? fb : o, s.r.p, s.w.p, s.z.p, s.p.p, s.q.p, s.dinv.p, s.V.p, s.ap.p,
                                s.tmp.p, ctx->d_values.p, false, rtol, r0, o.max_iters - total_it, &its);

@@ -14,7 +14,8 @@
 // uses its linear form: evaluated on the 27 unit-impulse residuals (r = e_s,
 // rms = 1/sqrt 27) it yields a stencil c_is = f(sqrt27 e_s, static_i)/sqrt27,
 // and the preconditioner is the symmetric part of D^-1 (I + C) on the
-// sparsity of A.  Training fits exactly that linear form.
+// sparsity of A, made positive definite by a symmetric Gershgorin scaling of
+// its off-diagonals.  Training fits exactly that linear form.
 //
 // Kernels.
 //   slot map        one thread per (element, local node pair), atomicMin
@@ -43,6 +44,7 @@
 #include "df64.h"
 #include "internal.h"
 #include "reduce.cuh"
+#include "spmv_df.cuh"
 
 namespace nalu_gb300 {
 
@@ -65,8 +67,6 @@ constexpr int kSlice = 32;
 
 namespace {
 
-using red::block_store;
-using red::block_total;
 
 // ---------------------------------------------------------------------------
 // slot map
@@ -372,6 +372,62 @@ __global__ void k_precond_sell(int64_t n, const int64_t* __restrict__ rp, const 
   }
 }
 
+// SPD safeguard (Gershgorin on D^1/2 M D^1/2): with d = a_ii, row i's
+// scaled diagonal is d_i M_ii and its scaled off-diagonal mass
+// sum_j |M_ij| sqrt(d_i d_j).  s_i = min(1, theta diag / offdiag); every
+// off-diagonal is then multiplied by min(s_i, s_j), which keeps M symmetric
+// and makes every scaled row diagonally dominant, hence M positive definite.
+// A row with a non-positive diagonal falls back to its Jacobi entry.
+constexpr float kSpdTheta = 0.95f;
+
+__global__ void k_precond_rowscale(int64_t n, const int64_t* __restrict__ sptr, const int32_t* __restrict__ slen,
+                                   const int32_t* __restrict__ scol, float* __restrict__ w,
+                                   const double* __restrict__ dinv, float* __restrict__ srow) {
+  const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= n) return;
+  const int64_t base = sptr[row / kSlice] + row % kSlice;
+  const int len = slen[row / kSlice];
+  const float di = (float)dinv[row];
+  float diag = 0.0f, off = 0.0f;
+  int64_t dpos = -1;
+  for (int k = 0; k < len; ++k) {
+    const int64_t e = base + (int64_t)k * kSlice;
+    const int32_t col = scol[e];
+    const float val = w[e];
+    if (col == row) {
+      if (dpos < 0) {  // padding repeats the diagonal index with value 0
+        diag = val / di;
+        dpos = e;
+      }
+    } else {
+      off += fabsf(val) * rsqrtf(di * (float)dinv[col]);
+    }
+  }
+  float sc = 1.0f;
+  if (!(diag > 0.0f)) {
+    sc = 0.0f;
+    if (dpos >= 0) w[dpos] = di;
+  } else if (off > kSpdTheta * diag) {
+    sc = kSpdTheta * diag / off;
+  }
+  srow[row] = sc;
+}
+
+__global__ void k_precond_apply_scale(int64_t n, const int64_t* __restrict__ sptr, const int32_t* __restrict__ slen,
+                                      const int32_t* __restrict__ scol, float* __restrict__ w,
+                                      const float* __restrict__ srow) {
+  const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= n) return;
+  const int64_t base = sptr[row / kSlice] + row % kSlice;
+  const int len = slen[row / kSlice];
+  const float si = srow[row];
+  for (int k = 0; k < len; ++k) {
+    const int64_t e = base + (int64_t)k * kSlice;
+    const int32_t col = scol[e];
+    if (col != row) w[e] *= fminf(si, srow[col]);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // flexible CG (Notay's FCG(1)) with the learned preconditioner
 //   z = M r;  beta = -(z . q_old) / (p_old . q_old);  p = z + beta p
@@ -384,16 +440,21 @@ __device__ __forceinline__ float d2f_trunc(double d) {
   const int e = (int)((b >> 52) & 0x7ff) - 1023;
   if (e < -126) return 0.0f;
   const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
-  if (e > 127) return __uint_as_float(sign | 0x7f800000u);
+  if (e > 127) return __uint_as_float(sign | 0x7f800000u | (e == 1024 && (b & 0xFFFFFFFFFFFFFull) ? 0x400000u : 0u));
   return __uint_as_float(sign | ((uint32_t)(e + 127) << 23) | (uint32_t)((b >> 29) & 0x7fffffu));
 }
 
+// scalars: fs[FS_BETA], fs[FS_ALPHA], fs[FS_PQ] (p . A p), fs[FS_RR] (r . r)
+enum { FS_BETA = 0, FS_ALPHA = 1, FS_PQ = 2, FS_RR = 3 };
+
+// z = M r (FP32 stencil values, FP32 residual); beta = -(z . q_old) / (p . q)_old by the last block
 __global__ void __launch_bounds__(kFcgThreads) k_fcg_prec(int64_t n, int64_t npad, const int64_t* __restrict__ sptr,
                                                           const int32_t* __restrict__ slen,
                                                           const int32_t* __restrict__ scol,
                                                           const float* __restrict__ w, const double* __restrict__ r,
                                                           const double* __restrict__ q, double* __restrict__ z,
-                                                          double* __restrict__ zq_part) {
+                                                          double* __restrict__ part, unsigned* __restrict__ cnt,
+                                                          double* __restrict__ fs, int first) {
   __shared__ double sh[33];
   double dot = 0.0;
   for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < npad;
@@ -403,76 +464,91 @@ __global__ void __launch_bounds__(kFcgThreads) k_fcg_prec(int64_t n, int64_t npa
     const int len = __ldg(slen + s);
     const int64_t base = __ldg(sptr + s) + (row % kSlice);
     float acc = 0.0f;
-    for (int k = 0; k < len; ++k) {
+    int k = 0;
+    for (; k + 4 <= len; k += 4) {  // loads of a group issued before the gathers
+      int32_t c[4];
+      float a[4];
+      double b[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        c[u] = __ldg(scol + base + (int64_t)(k + u) * kSlice);
+        a[u] = __ldg(w + base + (int64_t)(k + u) * kSlice);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) b[u] = __ldg(r + c[u]);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) acc = fmaf(a[u], d2f_trunc(b[u]), acc);
+    }
+    for (; k < len; ++k) {
       const int32_t c = __ldg(scol + base + (int64_t)k * kSlice);
       acc = fmaf(__ldg(w + base + (int64_t)k * kSlice), d2f_trunc(__ldg(r + c)), acc);
     }
-    const double zi = f2d_bits(acc);
+    const double zi = widen_f(acc);
     z[row] = zi;
     dot += zi * q[row];
   }
-  block_store(dot, zq_part + blockIdx.x, sh);
+  const double v[1] = {dot};
+  double t[1];
+  if (red::grid_reduce<1>(v, part, kFcgBlocks, cnt, t, sh) && threadIdx.x == 0)
+    fs[FS_BETA] = first ? 0.0 : -t[0] / fs[FS_PQ];
 }
 
 __global__ void __launch_bounds__(kFcgThreads) k_fcg_pupdate(int64_t n, const double* __restrict__ z,
-                                                             double* __restrict__ p,
-                                                             const double* __restrict__ zq_part,
-                                                             const double* __restrict__ pq_part, int first) {
-  __shared__ double sh[33];
-  double beta = 0.0;
-  if (!first) beta = -block_total(zq_part, kFcgBlocks, sh) / block_total(pq_part, kFcgBlocks, sh);
+                                                             float2* __restrict__ p, const double* __restrict__ fs,
+                                                             int first) {
+  const double beta = fs[FS_BETA];
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    p[i] = first ? z[i] : z[i] + beta * p[i];
+    p[i] = split_df(first ? z[i] : z[i] + beta * join_df(p[i]));
 }
 
+// q = A p (df64); alpha = (p . r) / (p . q) by the last block, which also
+// counts non-positive steps (the preconditioner is then not positive definite)
 __global__ void __launch_bounds__(kFcgThreads) k_fcg_spmv(int64_t n, int64_t npad, const int64_t* __restrict__ sptr,
                                                           const int32_t* __restrict__ slen,
                                                           const int32_t* __restrict__ scol,
-                                                          const double* __restrict__ sval,
-                                                          const double* __restrict__ p, const double* __restrict__ r,
-                                                          double* __restrict__ q, double* __restrict__ pq_part,
-                                                          double* __restrict__ pr_part) {
+                                                          const float2* __restrict__ sval,
+                                                          const float2* __restrict__ p, const double* __restrict__ r,
+                                                          double* __restrict__ q, double* __restrict__ part,
+                                                          unsigned* __restrict__ cnt, double* __restrict__ fs,
+                                                          int* __restrict__ nonpos) {
   __shared__ double sh[33];
   double pq = 0.0, pr = 0.0;
   for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < npad;
        row += (int64_t)gridDim.x * blockDim.x) {
     if (row >= n) continue;
     const int64_t s = row / kSlice;
-    const int len = __ldg(slen + s);
-    const int64_t base = __ldg(sptr + s) + (row % kSlice);
-    double acc = 0.0;
-    for (int k = 0; k < len; ++k) {
-      const int32_t c = __ldg(scol + base + (int64_t)k * kSlice);
-      acc += __ldg(sval + base + (int64_t)k * kSlice) * __ldg(p + c);
-    }
-    q[row] = acc;
-    const double pi = p[row];
-    pq += pi * acc;
+    const double qi = sell_row_df(__ldg(sptr + s) + (row % kSlice), __ldg(slen + s), scol, sval, p);
+    q[row] = qi;
+    const double pi = join_df(p[row]);
+    pq += pi * qi;
     pr += pi * r[row];
   }
-  block_store(pq, pq_part + blockIdx.x, sh);
-  block_store(pr, pr_part + blockIdx.x, sh);
+  const double v[2] = {pq, pr};
+  double t[2];
+  if (red::grid_reduce<2>(v, part, kFcgBlocks, cnt, t, sh) && threadIdx.x == 0) {
+    const double alpha = t[1] / t[0];
+    fs[FS_PQ] = t[0];
+    fs[FS_ALPHA] = alpha;
+    if (!(alpha > 0.0)) *nonpos += 1;
+  }
 }
 
 __global__ void __launch_bounds__(kFcgThreads) k_fcg_axpy(int64_t n, double* __restrict__ x,
-                                                          const double* __restrict__ p, double* __restrict__ r,
-                                                          const double* __restrict__ q,
-                                                          const double* __restrict__ pq_part,
-                                                          const double* __restrict__ pr_part,
-                                                          double* __restrict__ rr_part, int* __restrict__ nonpos) {
+                                                          const float2* __restrict__ p, double* __restrict__ r,
+                                                          const double* __restrict__ q, double* __restrict__ part,
+                                                          unsigned* __restrict__ cnt, double* __restrict__ fs) {
   __shared__ double sh[33];
-  const double alpha = block_total(pr_part, kFcgBlocks, sh) / block_total(pq_part, kFcgBlocks, sh);
-  // alpha = (z . r) / (p . A p): a non-positive step shows that the
-  // preconditioner is not positive definite on this residual
-  if (blockIdx.x == 0 && threadIdx.x == 0 && !(alpha > 0.0)) *nonpos += 1;
+  const double alpha = fs[FS_ALPHA];
   double rr = 0.0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    x[i] += alpha * p[i];
+    x[i] += alpha * join_df(p[i]);
     const double ri = r[i] - alpha * q[i];
     r[i] = ri;
     rr += ri * ri;
   }
-  block_store(rr, rr_part + blockIdx.x, sh);
+  const double v[1] = {rr};
+  double t[1];
+  if (red::grid_reduce<1>(v, part, kFcgBlocks, cnt, t, sh) && threadIdx.x == 0) fs[FS_RR] = t[0];
 }
 
 // ---------------------------------------------------------------------------
@@ -786,10 +862,15 @@ int learned_prepare(nalu_ctx* ctx) {
   const SellMatrix& S = ctx->sw.sell;
   const int64_t n = ctx->n_rows;
   if (L.wsell.n < S.stored) NALU_CUDA(ctx, L.wsell.alloc(S.stored));
-  k_precond_sell<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(n, ctx->d_rowptr.p, S.ptr.p, S.len.p, S.col.p,
-                                                                        L.nbr.p, L.stencil.p, ctx->sw.dinv.p,
-                                                                        ctx->d_bcmask.p, L.wsell.p);
-  ctx->launches++;
+  const unsigned g = (unsigned)((n + 255) / 256);
+  k_precond_sell<<<g, 256, 0, ctx->stream>>>(n, ctx->d_rowptr.p, S.ptr.p, S.len.p, S.col.p, L.nbr.p, L.stencil.p,
+                                             ctx->sw.dinv.p, ctx->d_bcmask.p, L.wsell.p);
+  DBuf<float> srow;
+  NALU_CUDA(ctx, srow.alloc(n));
+  k_precond_rowscale<<<g, 256, 0, ctx->stream>>>(n, S.ptr.p, S.len.p, S.col.p, L.wsell.p, ctx->sw.dinv.p, srow.p);
+  k_precond_apply_scale<<<g, 256, 0, ctx->stream>>>(n, S.ptr.p, S.len.p, S.col.p, L.wsell.p, srow.p);
+  ctx->launches += 3;
+  NALU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return cuda_check(ctx, cudaGetLastError(), "learned preconditioner values");
 }
 
@@ -800,58 +881,56 @@ int fcg_learned(nalu_ctx* ctx, double* x, double* r, double rtol, double r0norm,
   const SellMatrix& S = s.sell;
   const int64_t npad = S.nslices * kSlice;
   *stalled = 0;
-  if (s.partial.n < 4 * kFcgBlocks) NALU_CUDA(ctx, s.partial.alloc(4 * kFcgBlocks));
-  double* zq_part = s.partial.p;
-  double* pq_part = s.partial.p + kFcgBlocks;
-  double* pr_part = s.partial.p + 2 * kFcgBlocks;
-  double* rr_part = s.partial.p + 3 * kFcgBlocks;
-  double *z = s.z.p, *p = s.p.p, *q = s.q.p;
+  if (s.partial.n < 2 * kFcgBlocks) NALU_CUDA(ctx, s.partial.alloc(2 * kFcgBlocks));
+  if (s.p2.n < n) NALU_CUDA(ctx, s.p2.alloc(n));
+  if (s.cscal.n < 8) NALU_CUDA(ctx, s.cscal.alloc(8));
+  if (s.ccount.n < 1) NALU_CUDA(ctx, s.ccount.alloc(1));
+  double* part = s.partial.p;
+  unsigned* cnt = s.ccount.p;
+  double* fs = s.cscal.p;
+  double *z = s.z.p, *q = s.q.p;
+  float2* p = s.p2.p;
   DBuf<int> nonpos;
   NALU_CUDA(ctx, nonpos.alloc(1));
-  NALU_CUDA(ctx, cudaMemsetAsync(nonpos.p, 0, sizeof(int), ctx->stream));
-  NALU_CUDA(ctx, cudaMemsetAsync(x, 0, sizeof(double) * n, ctx->stream));
-  NALU_CUDA(ctx, cudaMemsetAsync(q, 0, sizeof(double) * n, ctx->stream));
+  cudaStream_t st = ctx->stream;
+  NALU_CUDA(ctx, cudaMemsetAsync(nonpos.p, 0, sizeof(int), st));
+  NALU_CUDA(ctx, cudaMemsetAsync(cnt, 0, sizeof(unsigned), st));
+  NALU_CUDA(ctx, cudaMemsetAsync(fs, 0, sizeof(double) * 8, st));
+  NALU_CUDA(ctx, cudaMemsetAsync(x, 0, sizeof(double) * n, st));
+  NALU_CUDA(ctx, cudaMemsetAsync(q, 0, sizeof(double) * n, st));
   const float* w = ctx->learned.wsell.p;
   auto iteration = [&](int first) {
-    k_fcg_prec<<<kFcgBlocks, kFcgThreads, 0, ctx->stream>>>(n, npad, S.ptr.p, S.len.p, S.col.p, w, r, q, z, zq_part);
-    k_fcg_pupdate<<<kFcgBlocks, kFcgThreads, 0, ctx->stream>>>(n, z, p, zq_part, pq_part, first);
-    k_fcg_spmv<<<kFcgBlocks, kFcgThreads, 0, ctx->stream>>>(n, npad, S.ptr.p, S.len.p, S.col.p, S.vald.p, p, r, q,
-                                                            pq_part, pr_part);
-    k_fcg_axpy<<<kFcgBlocks, kFcgThreads, 0, ctx->stream>>>(n, x, p, r, q, pq_part, pr_part, rr_part, nonpos.p);
+    k_fcg_prec<<<kFcgBlocks, kFcgThreads, 0, st>>>(n, npad, S.ptr.p, S.len.p, S.col.p, w, r, q, z, part, cnt, fs,
+                                                   first);
+    k_fcg_pupdate<<<kFcgBlocks, kFcgThreads, 0, st>>>(n, z, p, fs, first);
+    k_fcg_spmv<<<kFcgBlocks, kFcgThreads, 0, st>>>(n, npad, S.ptr.p, S.len.p, S.col.p, S.val2.p, p, r, q, part, cnt,
+                                                   fs, nonpos.p);
+    k_fcg_axpy<<<kFcgBlocks, kFcgThreads, 0, st>>>(n, x, p, r, q, part, cnt, fs);
     ctx->launches += 4;
   };
   iteration(1);
   const int chunk = std::max(1, check_every > 0 ? std::min(check_every, 10) : 10);
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
-  cudaError_t ce = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+  cudaError_t ce = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
   if (ce != cudaSuccess) return cuda_check(ctx, ce, "begin capture");
   for (int k = 0; k < chunk; ++k) iteration(0);
-  ce = cudaStreamEndCapture(ctx->stream, &graph);
+  ce = cudaStreamEndCapture(st, &graph);
   if (ce != cudaSuccess) return cuda_check(ctx, ce, "end capture");
   ce = cudaGraphInstantiate(&exec, graph, 0);
   if (ce != cudaSuccess) {
     cudaGraphDestroy(graph);
     return cuda_check(ctx, ce, "instantiate");
   }
-  std::vector<double> hrr(kFcgBlocks);
   const double stop = rtol * r0norm;
-  double last = INFINITY;
-  int it = 1;
+  double last = INFINITY, best = INFINITY;
+  int it = 1, best_it = 0, hnonpos = 0;
   bool bad = false, conv = false;
-  double best = INFINITY;
-  int best_it = 0;
-  int hnonpos = 0;
-  auto residual = [&]() {
-    cudaMemcpyAsync(hrr.data(), rr_part, sizeof(double) * kFcgBlocks, cudaMemcpyDeviceToHost, ctx->stream);
-    cudaMemcpyAsync(&hnonpos, nonpos.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
-    if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return (double)NAN;
-    double sum = 0.0;
-    for (double v : hrr) sum += v;
-    return std::sqrt(sum);
-  };
   for (;;) {
-    const double res = residual();
+    double rr = 0.0;
+    cudaMemcpyAsync(&rr, fs + FS_RR, sizeof(double), cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(&hnonpos, nonpos.p, sizeof(int), cudaMemcpyDeviceToHost, st);
+    const double res = cudaStreamSynchronize(st) == cudaSuccess ? std::sqrt(rr) : (double)NAN;
     last = res;
     if (!std::isfinite(res) || hnonpos > 0) {
       bad = true;  // breakdown: non-finite values or an indefinite preconditioner
@@ -864,15 +943,16 @@ int fcg_learned(nalu_ctx* ctx, double* x, double* r, double rtol, double r0norm,
     if (res < 0.999 * best) {
       best = res;
       best_it = it;
-    } else if (it - best_it > std::max(stall_window, best_it)) {
+    } else if (it - best_it > std::max(stall_window, 4 * best_it)) {
       // CG residual norms rise and fall in humps whose length grows with the
-      // iteration count, so the window is at least the number of iterations
-      // the current minimum took to reach
+      // iteration count (measured up to about the age of the current minimum),
+      // so the window is at least four times the iterations the current
+      // minimum took to reach
       *stalled = 1;
       break;
     }
     if (it >= max_it) break;
-    cudaGraphLaunch(exec, ctx->stream);
+    cudaGraphLaunch(exec, st);
     it += chunk;
   }
   cudaGraphExecDestroy(exec);
@@ -881,7 +961,7 @@ int fcg_learned(nalu_ctx* ctx, double* x, double* r, double rtol, double r0norm,
   if (bad) *stalled = 1;  // a breakdown is handed to the fallback like a stall
   if (*stalled && !(last < r0norm)) {
     // no progress at all: hand the fallback a zero increment, not a diverged one
-    NALU_CUDA(ctx, cudaMemsetAsync(x, 0, sizeof(double) * n, ctx->stream));
+    NALU_CUDA(ctx, cudaMemsetAsync(x, 0, sizeof(double) * n, st));
   }
   if (bad) return NALU_ERR_NOT_CONVERGED;
   return conv ? NALU_OK : NALU_ERR_NOT_CONVERGED;
