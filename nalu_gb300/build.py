@@ -43,6 +43,8 @@ def build(verbose=False, ptxas_info=False):
                     "-I" + CSRC]
     if ptxas_info:
         flags += ["-Xptxas", "-v"]
+    # extra compile definitions, e.g. NALU_NVCC_DEFINES="NALU_DF_MINB=6"
+    flags += ["-D" + d for d in os.environ.get("NALU_NVCC_DEFINES", "").split() if d]
 
     def comp(src):
         obj = os.path.join(OUT, src.replace(".cu", ".o"))

@@ -13,6 +13,10 @@
 namespace nalu_gb300 {
 
 constexpr int kAsmBlockDF = 64;
+// resident blocks per SM the register allocation must allow (occupancy vs spills)
+#ifndef NALU_DF_MINB
+#define NALU_DF_MINB 4
+#endif
 
 struct AsmArgsDF {
   const int32_t* __restrict__ conn;
@@ -42,7 +46,7 @@ struct SmemAccDF {
 };
 
 template <int KIND, int MODE, bool SHIFT, bool SMDOT>
-__global__ void __launch_bounds__(kAsmBlockDF) k_assemble_scalar_df(AsmArgsDF a) {
+__global__ void __launch_bounds__(kAsmBlockDF, NALU_DF_MINB) k_assemble_scalar_df(AsmArgsDF a) {
   const int OUT = a.out;
   __shared__ df64 s_lhs[64][kAsmBlockDF];
   const int t = threadIdx.x;

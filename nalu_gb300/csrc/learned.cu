@@ -464,24 +464,20 @@ __global__ void __launch_bounds__(kFcgThreads) k_fcg_prec(int64_t n, int64_t npa
     const int len = __ldg(slen + s);
     const int64_t base = __ldg(sptr + s) + (row % kSlice);
     float acc = 0.0f;
-    int k = 0;
-    for (; k + 4 <= len; k += 4) {  // loads of a group issued before the gathers
-      int32_t c[4];
-      float a[4];
-      double b[4];
+    for (int k = 0; k < len; k += 8) {  // loads of a group issued before the gathers
+      int32_t c[8];
+      float a[8];
+      double b[8];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        c[u] = __ldg(scol + base + (int64_t)(k + u) * kSlice);
-        a[u] = __ldg(w + base + (int64_t)(k + u) * kSlice);
+      for (int u = 0; u < 8; ++u) {
+        const bool in = k + u < len;
+        c[u] = in ? __ldg(scol + base + (int64_t)(k + u) * kSlice) : -1;
+        a[u] = in ? __ldg(w + base + (int64_t)(k + u) * kSlice) : 0.0f;
       }
 #pragma unroll
-      for (int u = 0; u < 4; ++u) b[u] = __ldg(r + c[u]);
+      for (int u = 0; u < 8; ++u) b[u] = c[u] >= 0 ? __ldg(r + c[u]) : 0.0;
 #pragma unroll
-      for (int u = 0; u < 4; ++u) acc = fmaf(a[u], d2f_trunc(b[u]), acc);
-    }
-    for (; k < len; ++k) {
-      const int32_t c = __ldg(scol + base + (int64_t)k * kSlice);
-      acc = fmaf(__ldg(w + base + (int64_t)k * kSlice), d2f_trunc(__ldg(r + c)), acc);
+      for (int u = 0; u < 8; ++u) acc = fmaf(a[u], d2f_trunc(b[u]), acc);
     }
     const double zi = widen_f(acc);
     z[row] = zi;
@@ -496,9 +492,11 @@ __global__ void __launch_bounds__(kFcgThreads) k_fcg_prec(int64_t n, int64_t npa
 __global__ void __launch_bounds__(kFcgThreads) k_fcg_pupdate(int64_t n, const double* __restrict__ z,
                                                              float2* __restrict__ p, const double* __restrict__ fs,
                                                              int first) {
-  const double beta = fs[FS_BETA];
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    p[i] = split_df(first ? z[i] : z[i] + beta * join_df(p[i]));
+  const float2 beta = split_df(first ? 0.0 : fs[FS_BETA]);  // FP32-pair update, no FP64 instruction
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float2 zi = split_df(z[i]);
+    p[i] = first ? zi : fma_df(beta, p[i], zi);
+  }
 }
 
 // q = A p (df64); alpha = (p . r) / (p . q) by the last block, which also
@@ -539,14 +537,14 @@ __global__ void __launch_bounds__(kFcgThreads) k_fcg_axpy(int64_t n, double* __r
                                                           unsigned* __restrict__ cnt, double* __restrict__ fs) {
   __shared__ double sh[33];
   const double alpha = fs[FS_ALPHA];
-  double rr = 0.0;
+  float rh = 0.0f, rl = 0.0f;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     x[i] += alpha * join_df(p[i]);
     const double ri = r[i] - alpha * q[i];
     r[i] = ri;
-    rr += ri * ri;
+    acc_sq_df(rh, rl, split_df(ri), 1.0f);
   }
-  const double v[1] = {rr};
+  const double v[1] = {join_df(make_float2(rh, rl))};
   double t[1];
   if (red::grid_reduce<1>(v, part, kFcgBlocks, cnt, t, sh) && threadIdx.x == 0) fs[FS_RR] = t[0];
 }
