@@ -10,9 +10,18 @@ The CRS values (456 MB) and node inputs exceed the 129 MB L2, so no flush
 is needed between steps.  Inputs are synthetic (no dataset exists for this
 path).  Printed metric: elements assembled per second (whole job).
 
+Beside the headline number the line carries the other configurations:
+"solve" (Jacobi-PCG, FP32-inner + FP64 refinement and the learned flexible CG
+on the pinned 128^3 continuity system, plus "c4_192": plain vs learned at
+192^3), "batch" (64 independent meshes, problems/s), "momentum_c3" (96^3
+momentum assembly and the mixed-precision GMRES solve) and "heat_c1" (32^3
+heat conduction assembly and solves).  --no-solve / --no-batch / --no-c1 /
+--no-c3 / --no-c4 skip them.
+
 --impl reference times the reference's CPU algorithm (the oracle restatement
 of ContinuityAdvElemKernel + HexSCS + TpetraLinearSystem::sumInto, run on all
-host cores) on the same workload and prints the same JSON line.
+host cores) on the same workload and prints the same JSON line, with the
+CPU Jacobi-PCG time per iteration on the full 128^3 system beside it.
 Multi-GPU: replicas only (one independent mesh per rank, no collective on
 the data path); value = elements of all ranks / max-over-ranks time.
 """
@@ -320,6 +329,8 @@ def bench_gpu(args):
         if not args.no_c4:
             solve["c4_192"] = bench_c4(ng, learned_w)
     batch = None if args.no_batch else bench_batch(ng)
+    momentum = None if args.no_c3 else bench_c3(ng)
+    heat = None if args.no_c1 else bench_c1(ng)
     # ---- CPU baseline on rank 0 (oracle, bounded sample) ----
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -349,7 +360,7 @@ def bench_gpu(args):
                          "kernel_ms": avg_ms, "fp64_probe_tflops": fp64_peak},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches, "clocks": clk.summary(), "cpu_baseline": cpu, "solve": solve,
-            "batch": batch}
+            "batch": batch, "momentum_c3": momentum, "heat_c1": heat}
     for a in list(pin_in.values()) + [out_v, out_r]:
         a.free()
     ctx.close()
@@ -358,6 +369,94 @@ def bench_gpu(args):
     if dist is not None:
         dist.destroy_process_group()
     return 0
+
+
+def bench_c1(ng, N=32, reps=5):
+    """Heat conduction (ScalarDiffElemKernel) on a 32^3 unit cube, interior
+    nodes jittered +-10%, k = 1, T ~ U[0,1]; Dirichlet T = 0 at x = 0 and
+    T = 1 at x = 1 (applyDirichletBCs semantics); Jacobi-PCG and
+    Jacobi-GMRES(50) to 1e-8.  The whole problem fits in L2."""
+    from nalu_gb300.meshgen import block_mesh
+    c, conn, gid = block_mesh(N, jitter=0.1, seed=21)
+    n = c.shape[0]
+    T = np.random.default_rng(22).uniform(0, 1, n)
+    ctx = ng.Context(0)
+    ctx.mesh_create(c, conn, gid)
+    ctx.field_set("scalar_q", T)
+    ctx.field_set("diff_coeff", np.ones(n))
+    ctx.build_elem_graph(1)
+    left, right = np.where(c[:, 0] == 0.0)[0], np.where(c[:, 0] == 1.0)[0]
+    nodes = np.concatenate([left, right])
+    bc = np.concatenate([np.zeros(left.size), np.ones(right.size)])
+    ms = []
+    for k in range(reps + 1):
+        ctx.zero()
+        ctx.event_record(0)
+        ctx.assemble(ng.KERNEL_SCALAR_DIFF)
+        ctx.event_record(1)
+        ctx.synchronize()
+        if k:
+            ms.append(ctx.event_elapsed_ms(0, 1))
+    ctx.apply_dirichlet(nodes, bc, T[nodes])
+    ctx.load_complete()
+    out = {"workload": "scalar_diff_hex8_32^3_jitter0.1_dirichlet_x", "elements": int(conn.shape[0]), "nodes": int(n),
+           "nnz": int(ctx.sizes()[1]), "assemble_ms": statistics.median(ms),
+           "elements_per_s": conn.shape[0] / (statistics.median(ms) * 1e-3)}
+    for name, kw in (("jacobi_pcg_fp64", {}), ("jacobi_gmres50_fp64", {"method": ng.SOLVER_GMRES, "restart": 50})):
+        info = ctx.solve(ng.default_solver_opts(tol=1e-8, max_iters=20000, **kw), raise_on_error=False)
+        out[name] = {"ms": 1e3 * info.seconds, "iterations": info.iterations, "true_rel_res": info.true_rel_res,
+                     "status": info.status}
+    ctx.close()
+    return out
+
+
+def bench_c3(ng, N=96, reps=5):
+    """Momentum (24x24 element matrices, 3 dofs/node) on a 96^3 unit cube with
+    the Fourier64 velocity, viscosity 1e-3, mdot from the velocity
+    (ComputeMdotElemAlgorithm): assembly time of the central
+    (MomentumAdvDiffElemKernel) and the upwind-blended (MomentumUpwAdvDiff,
+    alpha_upw 0.5) kernels, then the mixed-precision solve (FP32 Jacobi-GMRES(50)
+    inner, FP64 refinement to 1e-8) with no-slip Dirichlet walls."""
+    from nalu_gb300.meshgen import block_mesh, fourier_velocity
+    c, conn, gid = block_mesh(N)
+    n = c.shape[0]
+    u = fourier_velocity(c, n_modes=64, kmin=1, kmax=16, seed=2024)
+    ctx = ng.Context(0)
+    ctx.mesh_create(c, conn, gid)
+    for nm, val in (("velocity", u), ("velocity_rtm", u), ("density", np.ones(n)), ("viscosity", np.full(n, 1e-3)),
+                    ("pressure", np.zeros(n)), ("dpdx", np.zeros((n, 3))), ("dudx", np.zeros((n, 9)))):
+        ctx.field_set(nm, val)
+    ctx.compute_mdot()
+    ctx.build_elem_graph(3)
+    out = {"workload": "momentum_hex8_96^3_fourier64_mu1e-3", "elements": int(conn.shape[0]), "nodes": int(n),
+           "nnz": int(ctx.sizes()[1])}
+    for name, kern, o in (("central", ng.KERNEL_MOMENTUM_ADV_DIFF, ng.default_assemble_opts()),
+                          ("upwind_0.5", ng.KERNEL_MOMENTUM_UPW_ADV_DIFF,
+                           ng.default_assemble_opts(alpha_upw=0.5, hybrid_factor=1.0))):
+        ctx.zero()
+        ctx.assemble(kern, o)  # warm-up (and scatter autotune)
+        ms = []
+        for _ in range(reps):
+            ctx.zero()
+            ctx.event_record(0)
+            ctx.assemble(kern, o)
+            ctx.event_record(1)
+            ctx.synchronize()
+            ms.append(ctx.event_elapsed_ms(0, 1))
+        out[name] = {"assemble_ms": statistics.median(ms),
+                     "elements_per_s": conn.shape[0] / (statistics.median(ms) * 1e-3)}
+    # system of the upwind-blended kernel, no-slip walls
+    on_wall = np.any((c <= 1e-12) | (c >= 1.0 - 1e-12), axis=1)
+    walls = np.nonzero(on_wall)[0]
+    ctx.apply_dirichlet(walls, np.zeros((walls.size, 3)), u[walls])
+    ctx.load_complete()
+    info = ctx.solve(ng.default_solver_opts(method=ng.SOLVER_GMRES, precision=ng.PRECISION_FP32_INNER_IR, tol=1e-8,
+                                            restart=50, max_iters=20000), raise_on_error=False)
+    out["solve_gmres50_fp32_ir"] = {"ms": 1e3 * info.seconds, "iterations": info.iterations,
+                                    "outer_iterations": info.outer_iterations, "true_rel_res": info.true_rel_res,
+                                    "status": info.status}
+    ctx.close()
+    return out
 
 
 def bench_c4(ng, weights, N=192):
@@ -471,6 +570,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-problem batched workload")
     ap.add_argument("--no-c4", action="store_true", help="skip the 192^3 learned-vs-plain continuity solve")
+    ap.add_argument("--no-c3", action="store_true", help="skip the 96^3 momentum assembly and solve")
+    ap.add_argument("--no-c1", action="store_true", help="skip the 32^3 heat-conduction assembly and solve")
     ap.add_argument("--size", type=int, default=128, help="elements per edge (default: the 128^3 workload)")
     ap.add_argument("--arith", default="auto", choices=["auto", "fp64", "df64"],
                     help="element-math arithmetic (auto: the faster; both pass the parity tests)")
