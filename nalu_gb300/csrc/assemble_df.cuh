@@ -15,7 +15,7 @@ namespace nalu_gb300 {
 constexpr int kAsmBlockDF = 64;
 // resident blocks per SM the register allocation must allow (occupancy vs spills)
 #ifndef NALU_DF_MINB
-#define NALU_DF_MINB 4
+#define NALU_DF_MINB 5
 #endif
 
 struct AsmArgsDF {
@@ -38,17 +38,22 @@ struct AsmArgsDF {
 };
 
 struct SmemAccDF {
-  df64 (*s)[kAsmBlockDF];
+  df64 (*s)[kAsmBlockDF];   // [64 entries][threads]: element matrix
+  df64 (*rs)[kAsmBlockDF];  // [8 rows][threads]: element rhs
   int t;
   __device__ __forceinline__ void set(int r, int c, df64 v) { s[r * 8 + c][t] = v; }
   __device__ __forceinline__ void add(int r, int c, df64 v) { s[r * 8 + c][t] = df_add(s[r * 8 + c][t], v); }
   __device__ __forceinline__ df64 get(int r, int c) const { return s[r * 8 + c][t]; }
+  __device__ __forceinline__ void rset(int r, df64 v) { rs[r][t] = v; }
+  __device__ __forceinline__ void radd(int r, df64 v) { rs[r][t] = df_add(rs[r][t], v); }
+  __device__ __forceinline__ df64 rget(int r) const { return rs[r][t]; }
 };
 
 template <int KIND, int MODE, bool SHIFT, bool SMDOT>
 __global__ void __launch_bounds__(kAsmBlockDF, NALU_DF_MINB) k_assemble_scalar_df(AsmArgsDF a) {
   const int OUT = a.out;
   __shared__ df64 s_lhs[64][kAsmBlockDF];
+  __shared__ df64 s_rhs[8][kAsmBlockDF];
   const int t = threadIdx.x;
   const int64_t i = (int64_t)blockIdx.x * kAsmBlockDF + t;
   if (i >= a.count) return;
@@ -68,7 +73,7 @@ __global__ void __launch_bounds__(kAsmBlockDF, NALU_DF_MINB) k_assemble_scalar_d
     x[n][1] = __ldg(px + 1);
     x[n][2] = __ldg(px + 2);
   }
-  SmemAccDF acc{s_lhs, t};
+  SmemAccDF acc{s_lhs, s_rhs, t};
   double pv[8];
 #pragma unroll
   for (int n = 0; n < 8; ++n) pv[n] = __ldg(a.f_a + nd[n]);

@@ -159,8 +159,21 @@ DF_HD df64 df_fma(df64 a, df64 b, df64 c) {
   return quick_two_sum(s.hi, s.lo);
 }
 
-// a * b - c * d
-DF_HD df64 df_cross(df64 a, df64 b, df64 c, df64 d) { return df_sub(df_mul(a, b), df_mul(c, d)); }
+// a * b - c * d: both products with FMA error terms, one TwoSum of the
+// leading parts, one renormalisation (19 FP32 operations instead of 25)
+DF_HD df64 df_cross(df64 a, df64 b, df64 c, df64 d) {
+  const float p = f_mul(a.hi, b.hi);
+  float e = f_fma(a.hi, b.hi, -p);
+  e = f_fma(a.hi, b.lo, e);
+  e = f_fma(a.lo, b.hi, e);
+  const float q = f_mul(c.hi, d.hi);
+  float g = f_fma(c.hi, d.hi, -q);
+  g = f_fma(c.hi, d.lo, g);
+  g = f_fma(c.lo, d.hi, g);
+  df64 s = two_sum(p, -q);
+  s.lo = f_add(s.lo, f_sub(e, g));
+  return quick_two_sum(s.hi, s.lo);
+}
 
 // 1 / a: FP32 reciprocal refined by one Newton step in df64
 DF_HD df64 df_rcp(df64 a) {

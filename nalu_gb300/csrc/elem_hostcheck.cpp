@@ -92,7 +92,8 @@ void hc_scalar_diff_df(const double* xin, const double* q, const double* k, int 
   df64 kd[8], m[64];
   for (int n = 0; n < 8; ++n) kd[n] = df_from_double(k[n]);
   with_x(xin, [&](double (&x)[8][3]) {
-    ArrayAccDF acc{m};
+    df64 rr_acc[8];
+    ArrayAccDF acc{m, rr_acc};
     if (shift) scalar_diff_lhs_df<true>(x, kd, acc);
     else scalar_diff_lhs_df<false>(x, kd, acc);
   });
@@ -114,7 +115,8 @@ void hc_continuity_df(const double* xin, const double* u, const double* rho, con
   const int mode = spois ? 2 : (reduced ? 1 : 0);
   const df64 it = df_from_double(1.0 / tau);
   with_x(xin, [&](double (&x)[8][3]) {
-    ArrayAccDF acc{m};
+    df64 rr_acc[8];
+    ArrayAccDF acc{m, rr_acc};
     if (mode == 0) {
       if (smdot) continuity_elem_df<0, true>(x, w, it, pd, acc, r8);
       else continuity_elem_df<0, false>(x, w, it, pd, acc, r8);

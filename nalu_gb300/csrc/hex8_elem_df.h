@@ -149,14 +149,22 @@ NALU_HD void ip_shifted_G_df(const EdgeFormDF& f, int ip, const df64 area[3], df
 }
 
 // fac[c] = sum_j dN_c/ds_j(s) * (G_j * scale)
+//        = c0 h1 h2 g0 + h0 (c1 h2 g1 + c2 h1 g2),   h_k = 1/2 + c_k s_k;
+// the two corners of an x-edge share h1, h2 and the bracket, so each pair
+// costs one bracket and two short products.
 NALU_HD void lhs_factors_df(const df64 G[3], df64 scale, const float s[3], df64 fac[8]) {
   const df64 g0 = df_mul(G[0], scale), g1 = df_mul(G[1], scale), g2 = df_mul(G[2], scale);
+  const float hp = 0.5f + s[0], hm = 0.5f - s[0];  // h0 for c0 = +1, -1 (exact)
 #pragma unroll
-  for (int c = 0; c < 8; ++c) {
-    const float c0 = (float)corner_sign(c, 0), c1 = (float)corner_sign(c, 1), c2 = (float)corner_sign(c, 2);
-    const float h0 = 0.5f + c0 * s[0], h1 = 0.5f + c1 * s[1], h2 = 0.5f + c2 * s[2];
-    const float d0 = c0 * h1 * h2, d1 = c1 * h0 * h2, d2 = c2 * h0 * h1;  // exact in FP32
-    fac[c] = df_add(df_add(df_mul_f(g0, d0), df_mul_f(g1, d1)), df_mul_f(g2, d2));
+  for (int pr = 0; pr < 4; ++pr) {
+    const int cp = node_of(1, (pr & 1) ? 1 : -1, (pr & 2) ? 1 : -1);   // c0 = +1
+    const int cm = node_of(-1, (pr & 1) ? 1 : -1, (pr & 2) ? 1 : -1);  // c0 = -1
+    const float c1 = (float)corner_sign(cp, 1), c2 = (float)corner_sign(cp, 2);
+    const float h1 = 0.5f + c1 * s[1], h2 = 0.5f + c2 * s[2];
+    const df64 t = df_add(df_mul_f(g1, c1 * h2), df_mul_f(g2, c2 * h1));  // exact float factors
+    const df64 u = df_mul_f(g0, h1 * h2);
+    fac[cp] = df_add(u, df_mul_f(t, hp));
+    fac[cm] = df_add(df_neg(u), df_mul_f(t, hm));
   }
 }
 
@@ -264,7 +272,7 @@ NALU_HD double continuity_elem_df(const double x[8][3], const df64 w[8][3], df64
     trilinear_coeffs_df(v, wc[comp]);
   }
 #pragma unroll
-  for (int r = 0; r < 8; ++r) rhs[r] = df_zero();
+  for (int r = 0; r < 8; ++r) acc.rset(r, df_zero());
   float mindet = 3.0e38f;
 #pragma unroll 1
   for (int ip = 0; ip < 12; ++ip) {
@@ -297,22 +305,25 @@ NALU_HD double continuity_elem_df(const double x[8][3], const df64 w[8][3], df64
       for (int c = 0; c < 8; ++c) dpa = df_fma(fs[c], p[c], dpa);
       m = df_add(m, dpa);
     }
-    const int il = ip_left(ip), ir = ip_right(ip);
-    // rhs[il] -= m ; rhs[ir] += m  (runtime row index without dynamic register indexing)
-#pragma unroll
-    for (int r = 0; r < 8; ++r) {
-      if (r == il) rhs[r] = df_sub(rhs[r], m);
-      if (r == ir) rhs[r] = df_add(rhs[r], m);
-    }
+    // rhs[il] -= m ; rhs[ir] += m, accumulated beside the element matrix
+    // (runtime row index; registers cannot be indexed at run time)
+    acc.radd(ip_left(ip), df_neg(m));
+    acc.radd(ip_right(ip), m);
   }
+#pragma unroll
+  for (int r = 0; r < 8; ++r) rhs[r] = acc.rget(r);
   return f2d_bits(mindet);
 }
 
 // plain array accumulator (host check)
 struct ArrayAccDF {
   df64* m;
+  df64* rhs;  // [8], used by the continuity kernel
   NALU_HD void set(int r, int c, df64 v) { m[r * 8 + c] = v; }
   NALU_HD void add(int r, int c, df64 v) { m[r * 8 + c] = df_add(m[r * 8 + c], v); }
+  NALU_HD void rset(int r, df64 v) { rhs[r] = v; }
+  NALU_HD void radd(int r, df64 v) { rhs[r] = df_add(rhs[r], v); }
+  NALU_HD df64 rget(int r) const { return rhs[r]; }
 };
 
 }  // namespace nalu_gb300
