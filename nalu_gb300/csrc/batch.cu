@@ -2,14 +2,25 @@
 //
 // The meshes are one union mesh with disjoint node ranges, so the assembly is
 // a single launch over all elements and the CRS graph is block diagonal.  The
-// solve is Jacobi-preconditioned CG with separate alpha, beta and stop test
-// per problem, run as ONE persistent cooperative kernel: every iteration of
-// every problem happens inside that launch.  Rows are cut into tiles of at
-// most 256 rows that never cross a problem boundary; partial sums are kept per
-// tile and reduced per problem in a fixed order (deterministic).  Phases are
-// separated by a grid barrier whose waits are bounded: a barrier that does not
-// complete within its spin limit sets an error flag and the kernel returns,
-// so a fault can never turn into a hang.
+// solve is Jacobi-preconditioned CG with a separate alpha, beta and stop test
+// per problem, on the same arithmetic as the single-system CG (cg_fast.cu):
+// df64 SELL-32 SpMV, search direction as FP32 pairs, dot products as FP32
+// pairs, x and r in FP64.
+//
+// Rows are cut into tiles of at most 256 rows that never cross a problem
+// boundary; one block owns one tile and one thread one row.  An iteration is
+// three kernels over the tiles:
+//   pupdate  p = D^-1 r + beta_p p
+//   spmv     q = A p, tile sums of p.q; the last tile of a problem to finish
+//            (per-problem atomic ticket after a fence) sums that problem's
+//            tile partials in a fixed order and writes alpha_p
+//   axpy     x += alpha_p p, r -= alpha_p q, tile sums of r.D^-1 r and r.r;
+//            the last tile of a problem writes beta_p, and marks the problem
+//            done when its recursive residual is below its stop value
+// Tiles of finished problems return at once, so the work shrinks as problems
+// converge.  A chunk of iterations is captured into a CUDA graph; the host
+// reads the done flags between chunks and ends the solve with the true FP64
+// residual of every problem.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -18,287 +29,189 @@
 #include <vector>
 
 #include "internal.h"
+#include "reduce.cuh"
+#include "spmv_df.cuh"
 
 namespace nalu_gb300 {
 namespace {
 
-constexpr int kBT = 256;
-constexpr int kTileRows = 256;
-constexpr int kTPR = 8;
-constexpr long long kSpinLimit = 1ll << 25;
+constexpr int kBT = 256;  // threads per block = rows per tile
+constexpr int kTileRows = kBT;
+constexpr int kSliceB = 32;
 
-struct BatchArgs {
+struct TileArgs {
   int64_t n;
-  int P, ntiles, max_it;
-  const int64_t* __restrict__ rp;
-  const int32_t* __restrict__ ci;
-  const double* __restrict__ v;
-  const double* __restrict__ dinv;
-  const double* __restrict__ b;
-  double* x;
-  double* r;
-  double* z;
-  double* p;
-  double* q;
+  int P, ntiles;
   const int64_t* __restrict__ tile_row0;
   const int32_t* __restrict__ tile_rows;
   const int32_t* __restrict__ tile_prob;
   const int32_t* __restrict__ ptile0;
   const int32_t* __restrict__ ptile1;
-  double* tpart;  // [3][ntiles]
-  double* rz;     // [P]
-  double* alpha;
-  double* beta;
-  double* rr;
-  const double* stop2;
-  int* done;   // 0 active, 1 converged, 2 breakdown
-  int* iters;
-  unsigned* bar_count;
-  unsigned* bar_gen;
-  int* err;
+  // SELL-32 copy of the union matrix
+  const int64_t* __restrict__ sptr;
+  const int32_t* __restrict__ slen;
+  const int32_t* __restrict__ scol;
+  const float2* __restrict__ sval;
+  const float* __restrict__ dinvf;
+  double* x;
+  double* r;
+  double* q;
+  float2* p;
+  double* tpart;        // [2][ntiles]
+  unsigned* pcnt;       // [P] arrival tickets
+  double* alpha;        // [P]
+  double* beta;         // [P]
+  double* rz;           // [P]
+  double* rr;           // [P]
+  const double* stop2;  // [P]
+  int* done;            // [P] 0 active, 1 converged, 2 breakdown
+  int* iters;           // [P]
 };
 
-__device__ __forceinline__ double warp_sum(double v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
-
-// block sum broadcast to every thread (fixed order)
-__device__ double block_sum_bcast(double v, double* sh) {
-  v = warp_sum(v);
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  if (lane == 0) sh[w] = v;
-  __syncthreads();
-  if (w == 0) {
-    double t = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0.0;
-    t = warp_sum(t);
-    if (lane == 0) sh[32] = t;
+// The last tile of problem pr to arrive returns true (after a fence), with
+// the problem's tile partials summed in a fixed order into tot[].
+template <int K>
+__device__ bool problem_reduce(const TileArgs& a, int t, int pr, const double (&v)[K], double (&tot)[K],
+                               double* sh) {
+  __shared__ unsigned ticket;
+  for (int k = 0; k < K; ++k) {
+    const double s = red::block_sum(v[k], sh);
+    if (threadIdx.x == 0) a.tpart[k * a.ntiles + t] = s;
   }
-  __syncthreads();
-  const double total = sh[32];
-  __syncthreads();
-  return total;
-}
-
-// Grid barrier with a bounded wait (sense by generation counter).
-__device__ bool grid_barrier(const BatchArgs& a, int* sflag) {
-  __syncthreads();
+  const int t0 = a.ptile0[pr], t1 = a.ptile1[pr];
   if (threadIdx.x == 0) {
-    volatile unsigned* gen = a.bar_gen;
-    const unsigned g0 = *gen;
     __threadfence();
-    const unsigned arrived = atomicAdd(a.bar_count, 1u) + 1u;
-    int ok = 1;
-    if (arrived == gridDim.x) {
-      atomicExch(a.bar_count, 0u);
-      __threadfence();
-      atomicAdd(a.bar_gen, 1u);
-    } else {
-      long long spins = 0;
-      while (*gen == g0) {
-        if (++spins > kSpinLimit) {
-          atomicExch(a.err, 1);
-          ok = 0;
-          break;
-        }
-        __nanosleep(64);
-      }
-    }
-    __threadfence();
-    if (*(volatile int*)a.err) ok = 0;
-    *sflag = ok;
+    ticket = atomicAdd(a.pcnt + pr, 1u);
   }
   __syncthreads();
-  return *sflag != 0;
+  if (ticket != (unsigned)(t1 - t0 - 1)) return false;
+  __threadfence();
+  for (int k = 0; k < K; ++k) {
+    double s = 0.0;
+    for (int i = t0 + threadIdx.x; i < t1; i += blockDim.x) s += __ldcg(a.tpart + k * a.ntiles + i);
+    tot[k] = red::block_sum(s, sh);
+  }
+  if (threadIdx.x == 0) a.pcnt[pr] = 0u;
+  return true;
 }
 
-__global__ void __launch_bounds__(kBT) k_batched_cg(BatchArgs a) {
+__global__ void __launch_bounds__(kBT) k_bt_pupdate(TileArgs a) {
+  const int t = blockIdx.x;
+  const int pr = a.tile_prob[t];
+  if (a.done[pr]) return;
+  const int i = threadIdx.x;
+  if (i >= a.tile_rows[t]) return;
+  const int64_t row = a.tile_row0[t] + i;
+  const float2 beta = split_df(a.beta[pr]);
+  const float2 z = fma_df(split_df(a.r[row]), make_float2(a.dinvf[row], 0.0f), make_float2(0.0f, 0.0f));
+  a.p[row] = fma_df(beta, a.p[row], z);
+}
+
+__global__ void __launch_bounds__(kBT) k_bt_spmv(TileArgs a) {
   __shared__ double sh[33];
-  __shared__ int sflag;
-  const int G = gridDim.x;
-  for (int it = 0; it < a.max_it; ++it) {
-    // A: p = z + beta p
-    for (int t = blockIdx.x; t < a.ntiles; t += G) {
-      const int pr = a.tile_prob[t];
-      if (a.done[pr]) continue;
-      const double beta = it == 0 ? 0.0 : a.beta[pr];
-      const int64_t r0 = a.tile_row0[t];
-      const int nr = a.tile_rows[t];
-      for (int i = threadIdx.x; i < nr; i += blockDim.x) {
-        const int64_t row = r0 + i;
-        a.p[row] = it == 0 ? a.z[row] : a.z[row] + beta * a.p[row];
-      }
-    }
-    if (!grid_barrier(a, &sflag)) return;
-    // B: q = A p ; per-tile p.q
-    for (int t = blockIdx.x; t < a.ntiles; t += G) {
-      const int pr = a.tile_prob[t];
-      if (a.done[pr]) {
-        if (threadIdx.x == 0) a.tpart[t] = 0.0;
-        continue;
-      }
-      const int64_t r0 = a.tile_row0[t];
-      const int nr = a.tile_rows[t];
-      const int sub = threadIdx.x % kTPR;
-      double dot = 0.0;
-      for (int base = 0; base < nr; base += kBT / kTPR) {
-        const int i = base + threadIdx.x / kTPR;
-        const bool valid = i < nr;
-        double s = 0.0;
-        int64_t row = r0 + i;
-        if (valid) {
-          const int64_t jb = a.rp[row], je = a.rp[row + 1];
-          for (int64_t j = jb + sub; j < je; j += kTPR) s += a.v[j] * a.p[a.ci[j]];
-        }
-#pragma unroll
-        for (int o = kTPR / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, kTPR);
-        if (valid && sub == 0) {
-          a.q[row] = s;
-          dot += a.p[row] * s;
-        }
-      }
-      const double tot = block_sum_bcast(dot, sh);
-      if (threadIdx.x == 0) a.tpart[t] = tot;
-    }
-    if (!grid_barrier(a, &sflag)) return;
-    // C: alpha per problem
-    for (int pr = blockIdx.x; pr < a.P; pr += G) {
-      if (a.done[pr]) continue;
-      double s = 0.0;
-      for (int t = a.ptile0[pr] + threadIdx.x; t < a.ptile1[pr]; t += blockDim.x) s += a.tpart[t];
-      const double pq = block_sum_bcast(s, sh);
-      if (threadIdx.x == 0) {
-        const double al = a.rz[pr] / pq;
-        if (isfinite(al)) a.alpha[pr] = al;
-        else {
-          a.alpha[pr] = 0.0;
-          a.done[pr] = 2;
-        }
-      }
-    }
-    if (!grid_barrier(a, &sflag)) return;
-    // D: x += alpha p ; r -= alpha q ; z = D^-1 r ; per-tile r.z and r.r
-    for (int t = blockIdx.x; t < a.ntiles; t += G) {
-      const int pr = a.tile_prob[t];
-      double rz = 0.0, rr = 0.0;
-      if (!a.done[pr]) {
-        const double al = a.alpha[pr];
-        const int64_t r0 = a.tile_row0[t];
-        const int nr = a.tile_rows[t];
-        for (int i = threadIdx.x; i < nr; i += blockDim.x) {
-          const int64_t row = r0 + i;
-          a.x[row] += al * a.p[row];
-          const double ri = a.r[row] - al * a.q[row];
-          a.r[row] = ri;
-          const double zi = a.dinv[row] * ri;
-          a.z[row] = zi;
-          rz += ri * zi;
-          rr += ri * ri;
-        }
-      }
-      const double trz = block_sum_bcast(rz, sh);
-      const double trr = block_sum_bcast(rr, sh);
-      if (threadIdx.x == 0) {
-        a.tpart[a.ntiles + t] = trz;
-        a.tpart[2 * a.ntiles + t] = trr;
-      }
-    }
-    if (!grid_barrier(a, &sflag)) return;
-    // E: beta, residual and stop test per problem
-    for (int pr = blockIdx.x; pr < a.P; pr += G) {
-      if (a.done[pr]) continue;
-      double s1 = 0.0, s2 = 0.0;
-      for (int t = a.ptile0[pr] + threadIdx.x; t < a.ptile1[pr]; t += blockDim.x) {
-        s1 += a.tpart[a.ntiles + t];
-        s2 += a.tpart[2 * a.ntiles + t];
-      }
-      const double rzn = block_sum_bcast(s1, sh);
-      const double rrn = block_sum_bcast(s2, sh);
-      if (threadIdx.x == 0) {
-        const double be = rzn / a.rz[pr];
-        a.beta[pr] = isfinite(be) ? be : 0.0;
-        a.rz[pr] = rzn;
-        a.rr[pr] = rrn;
-        a.iters[pr] += 1;
-        if (!isfinite(rrn) || !isfinite(be)) a.done[pr] = 2;
-        else if (rrn <= a.stop2[pr]) a.done[pr] = 1;
-      }
-    }
-    if (!grid_barrier(a, &sflag)) return;
-    int active = 0;
-    for (int pr = threadIdx.x; pr < a.P; pr += blockDim.x) active |= (a.done[pr] == 0);
-    if (!__syncthreads_or(active)) break;
+  const int t = blockIdx.x;
+  const int pr = a.tile_prob[t];
+  if (a.done[pr]) return;
+  const int i = threadIdx.x;
+  double dot = 0.0;
+  if (i < a.tile_rows[t]) {
+    const int64_t row = a.tile_row0[t] + i;
+    const int64_t s = row / kSliceB;
+    const double qi = sell_row_df(__ldg(a.sptr + s) + (row % kSliceB), __ldg(a.slen + s), a.scol, a.sval, a.p);
+    a.q[row] = qi;
+    dot = join_df(a.p[row]) * qi;
+  }
+  const double v[1] = {dot};
+  double tot[1];
+  if (problem_reduce<1>(a, t, pr, v, tot, sh) && threadIdx.x == 0) a.alpha[pr] = a.rz[pr] / tot[0];
+}
+
+__global__ void __launch_bounds__(kBT) k_bt_axpy(TileArgs a) {
+  __shared__ double sh[33];
+  const int t = blockIdx.x;
+  const int pr = a.tile_prob[t];
+  if (a.done[pr]) return;
+  const int i = threadIdx.x;
+  float zh = 0.0f, zl = 0.0f, rh = 0.0f, rl = 0.0f;
+  if (i < a.tile_rows[t]) {
+    const int64_t row = a.tile_row0[t] + i;
+    const double al = a.alpha[pr];
+    a.x[row] += al * join_df(a.p[row]);
+    const double ri = a.r[row] - al * a.q[row];
+    a.r[row] = ri;
+    const float2 rs = split_df(ri);
+    acc_sq_df(zh, zl, rs, a.dinvf[row]);
+    acc_sq_df(rh, rl, rs, 1.0f);
+  }
+  const double v[2] = {join_df(make_float2(zh, zl)), join_df(make_float2(rh, rl))};
+  double tot[2];
+  if (problem_reduce<2>(a, t, pr, v, tot, sh) && threadIdx.x == 0) {
+    const double be = tot[0] / a.rz[pr];
+    a.beta[pr] = be;
+    a.rz[pr] = tot[0];
+    a.rr[pr] = tot[1];
+    a.iters[pr] += 1;
+    if (!isfinite(tot[1]) || !isfinite(be)) a.done[pr] = 2;
+    else if (tot[1] <= a.stop2[pr]) a.done[pr] = 1;
   }
 }
 
-// x = 0 except identity rows (x = b there); D^-1 and identity detection
-__global__ void k_batch_prep(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
-                             const double* __restrict__ v, const double* __restrict__ b, double* __restrict__ dinv,
+// x = 0 (or kept) except identity rows (x = b there)
+__global__ void k_batch_prep(int64_t n, const uint8_t* __restrict__ idmask, const double* __restrict__ b,
                              double* __restrict__ x, int zero) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  double d = 0.0;
-  bool off_zero = true;
-  for (int64_t j = rp[i]; j < rp[i + 1]; ++j) {
-    if (ci[j] == i) d = v[j];
-    else if (v[j] != 0.0) off_zero = false;
-  }
-  dinv[i] = d != 0.0 ? 1.0 / d : 1.0;
   double xi = zero ? 0.0 : x[i];
-  if (off_zero && d == 1.0) xi = b[i];
+  if (idmask[i]) xi = b[i];
   x[i] = xi;
 }
 
-// r = b - A x ; z = D^-1 r ; per-tile r.z, r.r, b.b
-__global__ void __launch_bounds__(kBT) k_batch_resid(BatchArgs a) {
+// r = b - A x (FP64 CRS), p = 0; per-tile r.D^-1 r, r.r, b.b
+__global__ void __launch_bounds__(kBT) k_batch_resid(TileArgs a, const int64_t* __restrict__ rp,
+                                                     const int32_t* __restrict__ ci, const double* __restrict__ v,
+                                                     const double* __restrict__ b, double* __restrict__ tb) {
   __shared__ double sh[33];
-  for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
-    const int64_t r0 = a.tile_row0[t];
-    const int nr = a.tile_rows[t];
-    const int sub = threadIdx.x % kTPR;
-    double rz = 0.0, rr = 0.0, bb = 0.0;
-    for (int base = 0; base < nr; base += kBT / kTPR) {
-      const int i = base + threadIdx.x / kTPR;
-      const bool valid = i < nr;
-      const int64_t row = r0 + i;
+  const int t = blockIdx.x;
+  const int i = threadIdx.x;
+  double rz = 0.0, rr = 0.0, bb = 0.0;
+  if (i < a.tile_rows[t]) {
+    const int64_t row = a.tile_row0[t] + i;
+    double s = 0.0;
+    for (int64_t j = rp[row]; j < rp[row + 1]; ++j) s += v[j] * a.x[ci[j]];
+    const double ri = b[row] - s;
+    a.r[row] = ri;
+    a.p[row] = make_float2(0.0f, 0.0f);
+    rz += ri * (widen_f(a.dinvf[row]) * ri);
+    rr += ri * ri;
+    bb += b[row] * b[row];
+  }
+  const double t1 = red::block_sum(rz, sh), t2 = red::block_sum(rr, sh), t3 = red::block_sum(bb, sh);
+  if (threadIdx.x == 0) {
+    a.tpart[t] = t1;
+    a.tpart[a.ntiles + t] = t2;
+    tb[t] = t3;
+  }
+}
+
+// per-problem sums of three tile arrays: out[3][P]
+__global__ void k_batch_sums(const double* __restrict__ t0p, const double* __restrict__ t1p,
+                             const double* __restrict__ t2p, const int32_t* __restrict__ ptile0,
+                             const int32_t* __restrict__ ptile1, int P, double* __restrict__ out) {
+  __shared__ double sh[33];
+  for (int pr = blockIdx.x; pr < P; pr += gridDim.x) {
+    const double* src[3] = {t0p, t1p, t2p};
+    for (int k = 0; k < 3; ++k) {
       double s = 0.0;
-      if (valid) {
-        for (int64_t j = a.rp[row] + sub; j < a.rp[row + 1]; j += kTPR) s += a.v[j] * a.x[a.ci[j]];
-      }
-#pragma unroll
-      for (int o = kTPR / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, kTPR);
-      if (valid && sub == 0) {
-        const double ri = a.b[row] - s;
-        a.r[row] = ri;
-        const double zi = a.dinv[row] * ri;
-        a.z[row] = zi;
-        rz += ri * zi;
-        rr += ri * ri;
-        bb += a.b[row] * a.b[row];
-      }
-    }
-    const double t1 = block_sum_bcast(rz, sh), t2 = block_sum_bcast(rr, sh), t3 = block_sum_bcast(bb, sh);
-    if (threadIdx.x == 0) {
-      a.tpart[t] = t1;
-      a.tpart[a.ntiles + t] = t2;
-      a.tpart[2 * a.ntiles + t] = t3;
+      for (int t = ptile0[pr] + threadIdx.x; t < ptile1[pr]; t += blockDim.x) s += src[k][t];
+      const double tot = red::block_sum(s, sh);
+      if (threadIdx.x == 0) out[k * P + pr] = tot;
     }
   }
 }
 
-// per-problem sums of the three tile partial arrays: out[3][P]
-__global__ void k_batch_sums(const double* __restrict__ tpart, int ntiles, const int32_t* __restrict__ ptile0,
-                             const int32_t* __restrict__ ptile1, int P, double* __restrict__ out) {
-  __shared__ double sh[33];
-  for (int pr = blockIdx.x; pr < P; pr += gridDim.x) {
-    for (int k = 0; k < 3; ++k) {
-      double s = 0.0;
-      for (int t = ptile0[pr] + threadIdx.x; t < ptile1[pr]; t += blockDim.x) s += tpart[k * ntiles + t];
-      const double tot = block_sum_bcast(s, sh);
-      if (threadIdx.x == 0) out[k * P + pr] = tot;
-    }
-  }
+__global__ void k_to_float(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
 }
 
 }  // namespace
@@ -324,15 +237,23 @@ int solve_batched(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* inf
   }
   const int ntiles = (int)trow0.size();
   SolverWork& s = ctx->sw;
+  int rc = compute_dinv(ctx);
+  if (rc) return rc;
+  const float2* sv2 = nullptr;
+  if ((rc = sell_build<float2>(ctx, s.sell, &sv2))) return rc;
   DBuf<int64_t> d_trow0;
-  DBuf<int32_t> d_ints;   // trows | tprob | pt0 | pt1 | done | iters | err
-  DBuf<double> d_dbl;     // tpart[3 ntiles] | rz alpha beta rr stop2 [P each] | sums [3P]
-  DBuf<unsigned> d_bar;
+  DBuf<int32_t> d_ints;  // trows | tprob | pt0 | pt1 | done | iters
+  DBuf<double> d_dbl;    // tpart[2 ntiles] | tb[ntiles] | alpha beta rz rr stop2 [P] | sums [3P]
+  DBuf<unsigned> d_cnt;
+  DBuf<float> dinvf;
+  DBuf<float2> p2;
   NALU_CUDA(ctx, d_trow0.alloc(ntiles));
-  NALU_CUDA(ctx, d_ints.alloc(2 * (int64_t)ntiles + 4 * (int64_t)P + 1));
+  NALU_CUDA(ctx, d_ints.alloc(2 * (int64_t)ntiles + 4 * (int64_t)P));
   NALU_CUDA(ctx, d_dbl.alloc(3 * (int64_t)ntiles + 8 * (int64_t)P));
-  NALU_CUDA(ctx, d_bar.alloc(2));
-  for (auto* b : {&s.r, &s.z, &s.p, &s.q, &s.dinv})
+  NALU_CUDA(ctx, d_cnt.alloc(P));
+  NALU_CUDA(ctx, dinvf.alloc(n));
+  NALU_CUDA(ctx, p2.alloc(n));
+  for (auto* b : {&s.r, &s.q})
     if (b->n < n) NALU_CUDA(ctx, b->alloc(n));
   int32_t* trows_d = d_ints.p;
   int32_t* tprob_d = trows_d + ntiles;
@@ -340,12 +261,12 @@ int solve_batched(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* inf
   int32_t* pt1_d = pt0_d + P;
   int32_t* done_d = pt1_d + P;
   int32_t* iters_d = done_d + P;
-  int32_t* err_d = iters_d + P;
   double* tpart = d_dbl.p;
-  double* rz_d = tpart + 3 * (int64_t)ntiles;
-  double* alpha_d = rz_d + P;
+  double* tb = tpart + 2 * (int64_t)ntiles;
+  double* alpha_d = tb + ntiles;
   double* beta_d = alpha_d + P;
-  double* rr_d = beta_d + P;
+  double* rz_d = beta_d + P;
+  double* rr_d = rz_d + P;
   double* stop2_d = rr_d + P;
   double* sums_d = stop2_d + P;  // [3][P]
   cudaStream_t st = ctx->stream;
@@ -354,61 +275,74 @@ int solve_batched(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* inf
   NALU_CUDA(ctx, cudaMemcpyAsync(tprob_d, tprob.data(), sizeof(int32_t) * ntiles, cudaMemcpyHostToDevice, st));
   NALU_CUDA(ctx, cudaMemcpyAsync(pt0_d, pt0.data(), sizeof(int32_t) * P, cudaMemcpyHostToDevice, st));
   NALU_CUDA(ctx, cudaMemcpyAsync(pt1_d, pt1.data(), sizeof(int32_t) * P, cudaMemcpyHostToDevice, st));
-  NALU_CUDA(ctx, cudaMemsetAsync(done_d, 0, sizeof(int32_t) * (2 * P + 1), st));
-  NALU_CUDA(ctx, cudaMemsetAsync(d_bar.p, 0, sizeof(unsigned) * 2, st));
+  NALU_CUDA(ctx, cudaMemsetAsync(iters_d, 0, sizeof(int32_t) * P, st));
+  NALU_CUDA(ctx, cudaMemsetAsync(d_cnt.p, 0, sizeof(unsigned) * P, st));
+  k_to_float<<<1024, 256, 0, st>>>(n, s.dinv.p, dinvf.p);
+  k_batch_prep<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, ctx->d_bcmask.p, ctx->d_rhs.p, ctx->d_x.p,
+                                                           o.x0_zero ? 1 : 0);
+  ctx->launches += 2;
 
-  BatchArgs a{};
+  TileArgs a{};
   a.n = n;
   a.P = P;
   a.ntiles = ntiles;
-  a.rp = ctx->d_rowptr.p;
-  a.ci = ctx->d_colind.p;
-  a.v = ctx->d_values.p;
-  a.dinv = s.dinv.p;
-  a.b = ctx->d_rhs.p;
-  a.x = ctx->d_x.p;
-  a.r = s.r.p;
-  a.z = s.z.p;
-  a.p = s.p.p;
-  a.q = s.q.p;
   a.tile_row0 = d_trow0.p;
   a.tile_rows = trows_d;
   a.tile_prob = tprob_d;
   a.ptile0 = pt0_d;
   a.ptile1 = pt1_d;
+  a.sptr = s.sell.ptr.p;
+  a.slen = s.sell.len.p;
+  a.scol = s.sell.col.p;
+  a.sval = s.sell.val2.p;
+  a.dinvf = dinvf.p;
+  a.x = ctx->d_x.p;
+  a.r = s.r.p;
+  a.q = s.q.p;
+  a.p = p2.p;
   a.tpart = tpart;
-  a.rz = rz_d;
+  a.pcnt = d_cnt.p;
   a.alpha = alpha_d;
   a.beta = beta_d;
+  a.rz = rz_d;
   a.rr = rr_d;
   a.stop2 = stop2_d;
   a.done = done_d;
   a.iters = iters_d;
-  a.bar_count = d_bar.p;
-  a.bar_gen = d_bar.p + 1;
-  a.err = err_d;
 
-  k_batch_prep<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, a.rp, a.ci, a.v, a.b, s.dinv.p, a.x, o.x0_zero ? 1 : 0);
-  ctx->launches++;
-  int blocks_per_sm = 0;
-  NALU_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_batched_cg, kBT, 0));
-  const int grid = std::max(1, std::min(ntiles, blocks_per_sm * ctx->sm_count));
+  const int chunk = o.check_every > 0 ? o.check_every : 25;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaError_t ce = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+  if (ce != cudaSuccess) return cuda_check(ctx, ce, "begin capture");
+  for (int k = 0; k < chunk; ++k) {
+    k_bt_pupdate<<<ntiles, kBT, 0, st>>>(a);
+    k_bt_spmv<<<ntiles, kBT, 0, st>>>(a);
+    k_bt_axpy<<<ntiles, kBT, 0, st>>>(a);
+  }
+  ce = cudaStreamEndCapture(st, &graph);
+  if (ce != cudaSuccess) return cuda_check(ctx, ce, "end capture");
+  ce = cudaGraphInstantiate(&exec, graph, 0);
+  if (ce != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    return cuda_check(ctx, ce, "instantiate");
+  }
+
   std::vector<double> sums(3 * P);
   std::vector<int32_t> done(P), iters(P);
-  std::vector<double> true_res(P, 0.0), bnorm(P, 0.0);
-  int rc = NALU_OK;
+  std::vector<double> true_res(P, 0.0);
   for (int outer = 0; outer < 6; ++outer) {
-    // true residual, z, r.z per problem; stop when every problem is within tol
-    k_batch_resid<<<std::min(ntiles, 4 * ctx->sm_count), kBT, 0, st>>>(a);
-    k_batch_sums<<<std::min(P, 1024), kBT, 0, st>>>(tpart, ntiles, pt0_d, pt1_d, P, sums_d);
+    // true residual r = b - A x (FP64), the Jacobi r.z and ||b|| per problem
+    k_batch_resid<<<ntiles, kBT, 0, st>>>(a, ctx->d_rowptr.p, ctx->d_colind.p, ctx->d_values.p, ctx->d_rhs.p, tb);
+    k_batch_sums<<<std::min(P, 1024), kBT, 0, st>>>(tpart, tpart + ntiles, tb, pt0_d, pt1_d, P, sums_d);
     ctx->launches += 2;
     NALU_CUDA(ctx, cudaMemcpyAsync(sums.data(), sums_d, sizeof(double) * 3 * P, cudaMemcpyDeviceToHost, st));
     NALU_CUDA(ctx, cudaStreamSynchronize(st));
     bool all = true;
     std::vector<double> stop2(P), rz0(P);
     for (int pr = 0; pr < P; ++pr) {
-      bnorm[pr] = std::sqrt(sums[2 * P + pr]);
-      const double bref = bnorm[pr] > 0 ? bnorm[pr] : 1.0;
+      const double bnorm = std::sqrt(sums[2 * P + pr]);
+      const double bref = bnorm > 0 ? bnorm : 1.0;
       true_res[pr] = std::sqrt(sums[P + pr]) / bref;
       done[pr] = true_res[pr] <= o.tol ? 1 : 0;
       all = all && done[pr];
@@ -419,20 +353,19 @@ int solve_batched(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* inf
     NALU_CUDA(ctx, cudaMemcpyAsync(stop2_d, stop2.data(), sizeof(double) * P, cudaMemcpyHostToDevice, st));
     NALU_CUDA(ctx, cudaMemcpyAsync(rz_d, rz0.data(), sizeof(double) * P, cudaMemcpyHostToDevice, st));
     NALU_CUDA(ctx, cudaMemcpyAsync(done_d, done.data(), sizeof(int32_t) * P, cudaMemcpyHostToDevice, st));
-    a.max_it = o.max_iters;
-    void* args[] = {&a};
-    cudaError_t ce = cudaLaunchCooperativeKernel((const void*)k_batched_cg, grid, kBT, args, 0, st);
-    if (ce != cudaSuccess) return cuda_check(ctx, ce, "cooperative batched CG launch");
-    ctx->launches++;
-    int32_t err = 0;
-    NALU_CUDA(ctx, cudaMemcpyAsync(&err, err_d, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-    NALU_CUDA(ctx, cudaMemcpyAsync(done.data(), done_d, sizeof(int32_t) * P, cudaMemcpyDeviceToHost, st));
-    NALU_CUDA(ctx, cudaStreamSynchronize(st));
-    if (err) {
-      rc = set_error(ctx, NALU_ERR_CUDA, "batched CG grid barrier timed out");
-      break;
+    NALU_CUDA(ctx, cudaMemsetAsync(beta_d, 0, sizeof(double) * P, st));
+    // CG on the current residual; x is updated in place
+    for (int it = 0; it < o.max_iters; it += chunk) {
+      cudaGraphLaunch(exec, st);
+      ctx->launches += 3 * chunk;
+      NALU_CUDA(ctx, cudaMemcpyAsync(done.data(), done_d, sizeof(int32_t) * P, cudaMemcpyDeviceToHost, st));
+      NALU_CUDA(ctx, cudaStreamSynchronize(st));
+      if (std::all_of(done.begin(), done.end(), [](int d) { return d != 0; })) break;
     }
+    if (std::any_of(done.begin(), done.end(), [](int d) { return d == 2; })) break;
   }
+  cudaGraphExecDestroy(exec);
+  cudaGraphDestroy(graph);
   NALU_CUDA(ctx, cudaMemcpyAsync(iters.data(), iters_d, sizeof(int32_t) * P, cudaMemcpyDeviceToHost, st));
   NALU_CUDA(ctx, cudaStreamSynchronize(st));
   const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -442,14 +375,12 @@ int solve_batched(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* inf
     infos[pr].outer_iterations = 1;
     infos[pr].true_rel_res = true_res[pr];
     infos[pr].seconds = secs;
-    infos[pr].status = true_res[pr] <= o.tol ? NALU_OK : NALU_ERR_NOT_CONVERGED;
+    infos[pr].fallback = 0;
+    infos[pr].learned_iterations = 0;
+    infos[pr].setup_seconds = 0.0;
+    infos[pr].status = true_res[pr] <= o.tol ? NALU_OK : (done[pr] == 2 ? NALU_ERR_NONFINITE : NALU_ERR_NOT_CONVERGED);
     all_ok = all_ok && infos[pr].status == NALU_OK;
   }
-  d_trow0.free();
-  d_ints.free();
-  d_dbl.free();
-  d_bar.free();
-  if (rc) return rc;
   return all_ok ? NALU_OK : set_error(ctx, NALU_ERR_NOT_CONVERGED, "some problems did not reach the tolerance");
 }
 
