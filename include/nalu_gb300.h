@@ -104,6 +104,16 @@ int nalu_linsys_sum_into_diag(nalu_ctx* ctx, int32_t node_idx, int dof, double d
 int nalu_linsys_load_complete(nalu_ctx* ctx);
 /* copy values [nnz] and rhs [n_rows] out (either may be NULL) */
 int nalu_linsys_copy(nalu_ctx* ctx, double* values, double* rhs, int dst_is_device);
+/* The same download without blocking the next assembly: the current values
+ * and rhs are snapshotted on the device (stream order) and sent to the host
+ * on a second stream, so the transfer overlaps whatever is queued next
+ * (field uploads, zeroSystem, assembly).  values / rhs are host buffers,
+ * pinned (nalu_host_alloc) for the transfer to be asynchronous; they hold the
+ * result after nalu_linsys_copy_wait or nalu_synchronize.  A second call
+ * waits on the device for the first download before reusing the snapshot.
+ * No reference counterpart (Tpetra's matrix lives on the host). */
+int nalu_linsys_copy_async(nalu_ctx* ctx, double* values, double* rhs);
+int nalu_linsys_copy_wait(nalu_ctx* ctx);
 
 /* ---- assembly (AssembleElemSolverAlgorithm::execute + Kernel::execute) --- */
 enum nalu_kernel {

@@ -106,6 +106,8 @@ def lib():
             "nalu_linsys_sum_into_diag": (I, [P, ctypes.c_int32, I, D, D]),
             "nalu_linsys_load_complete": (I, [P]),
             "nalu_linsys_copy": (I, [P, P, P, I]),
+            "nalu_linsys_copy_async": (I, [P, P, P]),
+            "nalu_linsys_copy_wait": (I, [P]),
             "nalu_assemble_opts_default": (None, [P]),
             "nalu_assemble": (I, [P, I, P]),
             "nalu_capture_element": (I, [P, I, P, I64, P, P]),
@@ -401,6 +403,13 @@ class Context:
 
     def system_to_ptr(self, values_ptr, rhs_ptr):
         self._check(lib().nalu_linsys_copy(self._h, values_ptr, rhs_ptr, 0), "copy")
+
+    def system_to_ptr_async(self, values_ptr, rhs_ptr):
+        """Start the download of values/rhs into pinned host memory; returns at once."""
+        self._check(lib().nalu_linsys_copy_async(self._h, values_ptr, rhs_ptr), "copy_async")
+
+    def copy_wait(self):
+        self._check(lib().nalu_linsys_copy_wait(self._h), "copy_wait")
 
 
 class PinnedArray:

@@ -170,6 +170,10 @@ int nalu_destroy(nalu_ctx* ctx) {
   s.sell.col.free();
   s.sell.vald.free();
   s.sell.valf.free();
+  if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
+  if (ctx->ev_snap) cudaEventDestroy(ctx->ev_snap);
+  if (ctx->ev_copied) cudaEventDestroy(ctx->ev_copied);
+  if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -188,6 +192,8 @@ int nalu_get_stream(nalu_ctx* ctx, void** stream) {
 int nalu_synchronize(nalu_ctx* ctx) {
   if (!ctx) return NALU_ERR_ARG;
   NALU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (ctx->copy_stream) NALU_CUDA(ctx, cudaStreamSynchronize(ctx->copy_stream));
+  ctx->copy_pending = false;
   return NALU_OK;
 }
 
@@ -597,6 +603,47 @@ int nalu_linsys_load_complete(nalu_ctx* ctx) {
   cudaSetDevice(ctx->device);
   NALU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return check_flags(ctx);
+}
+
+int nalu_linsys_copy_async(nalu_ctx* ctx, double* values, double* rhs) {
+  if (!ctx || (!values && !rhs)) return NALU_ERR_ARG;
+  if (ctx->num_dof == 0) return set_error(ctx, NALU_ERR_STATE, "no graph");
+  cudaSetDevice(ctx->device);
+  if (!ctx->copy_stream) {
+    NALU_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+    NALU_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_snap, cudaEventDisableTiming));
+    NALU_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_copied, cudaEventDisableTiming));
+  }
+  if (ctx->stage_values.n < ctx->nnz) NALU_CUDA(ctx, ctx->stage_values.alloc(ctx->nnz));
+  if (ctx->stage_rhs.n < ctx->n_rows) NALU_CUDA(ctx, ctx->stage_rhs.alloc(ctx->n_rows));
+  // the staging copy may be overwritten only after the previous download ended
+  if (ctx->copy_pending) NALU_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->ev_copied, 0));
+  if (values)
+    NALU_CUDA(ctx, cudaMemcpyAsync(ctx->stage_values.p, ctx->d_values.p, sizeof(double) * ctx->nnz,
+                                   cudaMemcpyDeviceToDevice, ctx->stream));
+  if (rhs)
+    NALU_CUDA(ctx, cudaMemcpyAsync(ctx->stage_rhs.p, ctx->d_rhs.p, sizeof(double) * ctx->n_rows,
+                                   cudaMemcpyDeviceToDevice, ctx->stream));
+  NALU_CUDA(ctx, cudaEventRecord(ctx->ev_snap, ctx->stream));
+  NALU_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_snap, 0));
+  if (values)
+    NALU_CUDA(ctx, cudaMemcpyAsync(values, ctx->stage_values.p, sizeof(double) * ctx->nnz, cudaMemcpyDeviceToHost,
+                                   ctx->copy_stream));
+  if (rhs)
+    NALU_CUDA(ctx, cudaMemcpyAsync(rhs, ctx->stage_rhs.p, sizeof(double) * ctx->n_rows, cudaMemcpyDeviceToHost,
+                                   ctx->copy_stream));
+  NALU_CUDA(ctx, cudaEventRecord(ctx->ev_copied, ctx->copy_stream));
+  ctx->copy_pending = true;
+  return NALU_OK;
+}
+
+int nalu_linsys_copy_wait(nalu_ctx* ctx) {
+  if (!ctx) return NALU_ERR_ARG;
+  if (!ctx->copy_pending) return NALU_OK;
+  cudaSetDevice(ctx->device);
+  NALU_CUDA(ctx, cudaEventSynchronize(ctx->ev_copied));
+  ctx->copy_pending = false;
+  return NALU_OK;
 }
 
 int nalu_linsys_copy(nalu_ctx* ctx, double* values, double* rhs, int dst_is_device) {

@@ -12,11 +12,29 @@
 
 namespace nalu_gb300 {
 
-// Device buffer owned by a context.
+// Device buffer (freed by its destructor; movable, not copyable).
 template <class T>
 struct DBuf {
   T* p = nullptr;
   int64_t n = 0;
+  DBuf() = default;
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  DBuf(DBuf&& o) noexcept : p(o.p), n(o.n) {
+    o.p = nullptr;
+    o.n = 0;
+  }
+  DBuf& operator=(DBuf&& o) noexcept {
+    if (this != &o) {
+      free();
+      p = o.p;
+      n = o.n;
+      o.p = nullptr;
+      o.n = 0;
+    }
+    return *this;
+  }
+  ~DBuf() { free(); }
   cudaError_t alloc(int64_t count) {
     free();
     if (count <= 0) return cudaSuccess;
@@ -116,6 +134,13 @@ struct nalu_ctx {
 
   // errors raised by kernels (negative Jacobian count, graph misses, ...)
   nalu_gb300::DBuf<int32_t> d_flags;     // [4]
+
+  // asynchronous result download (nalu_linsys_copy_async): staging copy of
+  // values/rhs, a second stream for the device-to-host transfer, events
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t ev_snap = nullptr, ev_copied = nullptr;
+  bool copy_pending = false;
+  nalu_gb300::DBuf<double> stage_values, stage_rhs;
 
   // timing
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;

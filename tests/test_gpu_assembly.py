@@ -360,3 +360,35 @@ def test_df64_golds_capture(gpu_ctx_factory, golds):
         assert np.max(np.abs(lhs.ravel() - golds[key]["lhs"])) <= 1e-15, key
         assert np.max(np.abs(rhs - golds[key]["rhs"])) <= 1e-15, key
     ctx.close()
+
+
+def test_async_download_matches_blocking_copy(gpu_ctx_factory):
+    """nalu_linsys_copy_async: the pinned host copy equals the blocking copy,
+    also for two downloads in a row with a different assembly in between
+    (the second snapshot waits for the first transfer)."""
+    c, conn, gid = block_mesh(20, jitter=0.1, seed=31)
+    n = c.shape[0]
+    u, rho, p, gp = continuity_fields(c, seed=32)
+    ctx = gpu_ctx_factory()
+    ctx.mesh_create(c, conn, gid)
+    for nm, val in (("velocity", u), ("density", rho), ("pressure", p), ("dpdx", gp)):
+        ctx.field_set(nm, val)
+    ctx.build_elem_graph(1)
+    nr, nnz, _ = ctx.sizes()
+    outs = [(ng.PinnedArray((nnz,)), ng.PinnedArray((nr,))) for _ in range(2)]
+    refs = []
+    for k, (ov, orr) in enumerate(outs):
+        ctx.field_set("density", rho * (1.0 + k))
+        ctx.zero()
+        ctx.assemble(ng.KERNEL_CONTINUITY_ADV)
+        refs.append(ctx.system())
+        ctx.system_to_ptr_async(ov.ptr, orr.ptr)
+    ctx.copy_wait()
+    for (ov, orr), (rv, rr) in zip(outs, refs):
+        np.testing.assert_array_equal(ov.array, rv)
+        np.testing.assert_array_equal(orr.array, rr)
+    assert not np.array_equal(outs[0][1].array, outs[1][1].array)
+    for ov, orr in outs:
+        ov.free()
+        orr.free()
+    ctx.close()
