@@ -299,7 +299,10 @@ def bench_gpu(args):
     e2e_value = ws * n_elems * args.steps / e2e_s
     # ---- plain PCG solve of the same continuity system (pressure pinned at node 0) ----
     solve = None
-    if not args.no_solve:
+    # the other configurations are reported by a single-GPU run only: with N > 1
+    # every rank runs the replicated headline measurement and nothing else
+    extras = ws == 1
+    if extras and not args.no_solve:
         ctx.zero()
         ctx.assemble(ng.KERNEL_CONTINUITY_ADV, opts)
         ctx.reset_rows([0])
@@ -331,13 +334,13 @@ def bench_gpu(args):
                                      "epochs": 40, "val_mse_first_last": [float(hist[0, 1]), float(hist[-1, 1])]}
         solve["learned_vs_plain_time"] = solve["jacobi_pcg_fp64"]["ms"] / solve["learned_fcg"]["ms"]
         if not args.no_c4:
-            solve["c4_192"] = bench_c4(ng, learned_w)
-    batch = None if args.no_batch else bench_batch(ng)
-    momentum = None if args.no_c3 else bench_c3(ng)
-    heat = None if args.no_c1 else bench_c1(ng)
+            solve["c4_192"] = bench_c4(ng, learned_w, local)
+    batch = bench_batch(ng, local) if extras and not args.no_batch else None
+    momentum = bench_c3(ng, local) if extras and not args.no_c3 else None
+    heat = bench_c1(ng, local) if extras and not args.no_c1 else None
     # ---- CPU baseline on rank 0 (oracle, bounded sample) ----
     cpu = None
-    if rank == 0 and not args.no_cpu:
+    if rank == 0 and ws == 1 and not args.no_cpu:
         from oracle import oracle as O
         if not os.path.exists(os.path.join(ROOT, "oracle", "liboracle.so")):
             subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "liboracle.so"], check=True)
@@ -375,7 +378,7 @@ def bench_gpu(args):
     return 0
 
 
-def bench_c1(ng, N=32, reps=5):
+def bench_c1(ng, dev=0, N=32, reps=5):
     """Heat conduction (ScalarDiffElemKernel) on a 32^3 unit cube, interior
     nodes jittered +-10%, k = 1, T ~ U[0,1]; Dirichlet T = 0 at x = 0 and
     T = 1 at x = 1 (applyDirichletBCs semantics); Jacobi-PCG and
@@ -384,7 +387,7 @@ def bench_c1(ng, N=32, reps=5):
     c, conn, gid = block_mesh(N, jitter=0.1, seed=21)
     n = c.shape[0]
     T = np.random.default_rng(22).uniform(0, 1, n)
-    ctx = ng.Context(0)
+    ctx = ng.Context(dev)
     ctx.mesh_create(c, conn, gid)
     ctx.field_set("scalar_q", T)
     ctx.field_set("diff_coeff", np.ones(n))
@@ -414,7 +417,7 @@ def bench_c1(ng, N=32, reps=5):
     return out
 
 
-def bench_c3(ng, N=96, reps=5):
+def bench_c3(ng, dev=0, N=96, reps=5):
     """Momentum (24x24 element matrices, 3 dofs/node) on a 96^3 unit cube with
     the Fourier64 velocity, viscosity 1e-3, mdot from the velocity
     (ComputeMdotElemAlgorithm): assembly time of the central
@@ -425,7 +428,7 @@ def bench_c3(ng, N=96, reps=5):
     c, conn, gid = block_mesh(N)
     n = c.shape[0]
     u = fourier_velocity(c, n_modes=64, kmin=1, kmax=16, seed=2024)
-    ctx = ng.Context(0)
+    ctx = ng.Context(dev)
     ctx.mesh_create(c, conn, gid)
     for nm, val in (("velocity", u), ("velocity_rtm", u), ("density", np.ones(n)), ("viscosity", np.full(n, 1e-3)),
                     ("pressure", np.zeros(n)), ("dpdx", np.zeros((n, 3))), ("dudx", np.zeros((n, 9)))):
@@ -463,14 +466,14 @@ def bench_c3(ng, N=96, reps=5):
     return out
 
 
-def bench_c4(ng, weights, N=192):
+def bench_c4(ng, weights, dev=0, N=192):
     """Continuity solve on 192^3 (z-stretch 1.05, Fourier64 velocity, pressure
     pinned at node 0): plain Jacobi-PCG against flexible CG with the learned
     preconditioner trained on the 128^3 system."""
     from nalu_gb300.meshgen import block_mesh, fourier_velocity
     c, conn, gid = block_mesh(N, z_ratio=1.05)
     n = c.shape[0]
-    ctx = ng.Context(0)
+    ctx = ng.Context(dev)
     ctx.mesh_create(c, conn, gid)
     ctx.field_set("velocity", fourier_velocity(c, n_modes=64, kmin=1, kmax=16, seed=2024))
     ctx.field_set("density", np.ones(n))
@@ -497,7 +500,7 @@ def bench_c4(ng, weights, N=192):
     return out
 
 
-def bench_batch(ng, n_problems=64, seed=2025, reps=2):
+def bench_batch(ng, dev=0, n_problems=64, seed=2025, reps=2):
     """64 independent continuity problems (edges per axis log-uniform in
     [16, 96], interior jitter 10%, own Fourier velocity each, pressure pinned
     at each problem's first node): one assembly launch over the union mesh,
@@ -507,7 +510,7 @@ def bench_batch(ng, n_problems=64, seed=2025, reps=2):
     n = c.shape[0]
     u = np.concatenate([fourier_velocity(c[off[k]:off[k + 1]], n_modes=64, seed=seed + 1 + k)
                         for k in range(n_problems)])
-    ctx = ng.Context(0)
+    ctx = ng.Context(dev)
     ctx.mesh_create(c, conn, gid)
     ctx.field_set("velocity", u)
     ctx.field_set("density", np.ones(n))
