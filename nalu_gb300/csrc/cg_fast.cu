@@ -21,6 +21,7 @@
 // captured once into a CUDA graph.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <type_traits>
@@ -379,6 +380,14 @@ int pcg_fast(nalu_ctx* ctx, const VT* sval, const SellMatrix& S, T* x, T* r, T* 
   return rc;
 }
 
+// grid of one full wave of `kernel`: SMs x resident blocks, capped at kCgBlocks
+unsigned wave_grid(nalu_ctx* ctx, const void* kernel, int threads) {
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0) != cudaSuccess || per_sm < 1)
+    per_sm = 1;
+  return (unsigned)std::min(kCgBlocks, per_sm * std::max(1, ctx->sm_count));
+}
+
 // FP64 Jacobi-CG on A x = r (x from 0) with the df64 SpMV on S.val2;
 // r holds the initial residual; on return x holds the solution increment.
 int pcg_df(nalu_ctx* ctx, const SellMatrix& S, double* x, double* r, double* z, double* q, const double* dinv,
@@ -403,10 +412,14 @@ int pcg_df(nalu_ctx* ctx, const SellMatrix& S, double* x, double* r, double* z, 
   k_convert_f<<<kCgBlocks, kCgThreads, 0, st>>>(n, dinv, dinvf);
   k_cgd_init<<<kCgBlocks, kCgThreads, 0, st>>>(n, r, dinvf, part, cnt, cs);
   ctx->launches++;
+  // one full wave per kernel: SMs x resident blocks (at most the partial-sum capacity)
+  const unsigned g_pu = wave_grid(ctx, (const void*)k_cgd_pupdate, kCgThreads);
+  const unsigned g_sp = wave_grid(ctx, (const void*)k_cgd_spmv, kCgThreads);
+  const unsigned g_ax = wave_grid(ctx, (const void*)k_cgd_axpy, kCgThreads);
   auto iteration = [&](int first) {
-    k_cgd_pupdate<<<kCgBlocks, kCgThreads, 0, st>>>(n, r, dinvf, p, cs, first);
-    k_cgd_spmv<<<kCgBlocks, kCgThreads, 0, st>>>(n, npad, S.ptr.p, S.len.p, S.col.p, S.val2.p, p, q, part, cnt, cs);
-    k_cgd_axpy<<<kCgBlocks, kCgThreads, 0, st>>>(n, x, p, r, q, dinvf, part, cnt, cs);
+    k_cgd_pupdate<<<g_pu, kCgThreads, 0, st>>>(n, r, dinvf, p, cs, first);
+    k_cgd_spmv<<<g_sp, kCgThreads, 0, st>>>(n, npad, S.ptr.p, S.len.p, S.col.p, S.val2.p, p, q, part, cnt, cs);
+    k_cgd_axpy<<<g_ax, kCgThreads, 0, st>>>(n, x, p, r, q, dinvf, part, cnt, cs);
     ctx->launches += 3;
   };
   ctx->launches++;

@@ -198,6 +198,7 @@ int learned_prepare(nalu_ctx* ctx);  // slot map, stencil and SELL preconditione
 // for `stall_window` iterations
 int fcg_learned(nalu_ctx* ctx, double* x, double* r, double rtol, double r0norm, int max_it, int check_every,
                 int stall_window, int* iters_out, int* stalled);
+unsigned wave_grid(nalu_ctx* ctx, const void* kernel, int threads);  // cg_fast.cu
 int pcg_df(nalu_ctx* ctx, const SellMatrix& S, double* x, double* r, double* z, double* q, const double* dinv,
            double rtol, double r0norm, int max_it, int check_every, int* iters_out);
 template <class T, class VT>

@@ -897,13 +897,16 @@ int fcg_learned(nalu_ctx* ctx, double* x, double* r, double rtol, double r0norm,
   NALU_CUDA(ctx, cudaMemsetAsync(x, 0, sizeof(double) * n, st));
   NALU_CUDA(ctx, cudaMemsetAsync(q, 0, sizeof(double) * n, st));
   const float* w = ctx->learned.wsell.p;
+  const unsigned g_pc = wave_grid(ctx, (const void*)k_fcg_prec, kFcgThreads);
+  const unsigned g_pu = wave_grid(ctx, (const void*)k_fcg_pupdate, kFcgThreads);
+  const unsigned g_sp = wave_grid(ctx, (const void*)k_fcg_spmv, kFcgThreads);
+  const unsigned g_ax = wave_grid(ctx, (const void*)k_fcg_axpy, kFcgThreads);
   auto iteration = [&](int first) {
-    k_fcg_prec<<<kFcgBlocks, kFcgThreads, 0, st>>>(n, npad, S.ptr.p, S.len.p, S.col.p, w, r, q, z, part, cnt, fs,
-                                                   first);
-    k_fcg_pupdate<<<kFcgBlocks, kFcgThreads, 0, st>>>(n, z, p, fs, first);
-    k_fcg_spmv<<<kFcgBlocks, kFcgThreads, 0, st>>>(n, npad, S.ptr.p, S.len.p, S.col.p, S.val2.p, p, r, q, part, cnt,
-                                                   fs, nonpos.p);
-    k_fcg_axpy<<<kFcgBlocks, kFcgThreads, 0, st>>>(n, x, p, r, q, part, cnt, fs);
+    k_fcg_prec<<<g_pc, kFcgThreads, 0, st>>>(n, npad, S.ptr.p, S.len.p, S.col.p, w, r, q, z, part, cnt, fs, first);
+    k_fcg_pupdate<<<g_pu, kFcgThreads, 0, st>>>(n, z, p, fs, first);
+    k_fcg_spmv<<<g_sp, kFcgThreads, 0, st>>>(n, npad, S.ptr.p, S.len.p, S.col.p, S.val2.p, p, r, q, part, cnt, fs,
+                                             nonpos.p);
+    k_fcg_axpy<<<g_ax, kFcgThreads, 0, st>>>(n, x, p, r, q, part, cnt, fs);
     ctx->launches += 4;
   };
   iteration(1);
