@@ -437,21 +437,23 @@ def bench_c3(ng, dev=0, N=96, reps=5):
     ctx.build_elem_graph(3)
     out = {"workload": "momentum_hex8_96^3_fourier64_mu1e-3", "elements": int(conn.shape[0]), "nodes": int(n),
            "nnz": int(ctx.sizes()[1])}
-    for name, kern, o in (("central", ng.KERNEL_MOMENTUM_ADV_DIFF, ng.default_assemble_opts()),
-                          ("upwind_0.5", ng.KERNEL_MOMENTUM_UPW_ADV_DIFF,
-                           ng.default_assemble_opts(alpha_upw=0.5, hybrid_factor=1.0))):
-        ctx.zero()
-        ctx.assemble(kern, o)  # warm-up (and scatter autotune)
-        ms = []
-        for _ in range(reps):
+    for name, kern, kw in (("central", ng.KERNEL_MOMENTUM_ADV_DIFF, {}),
+                           ("upwind_0.5", ng.KERNEL_MOMENTUM_UPW_ADV_DIFF, dict(alpha_upw=0.5, hybrid_factor=1.0))):
+        out[name] = {}
+        for an, ar in (("fp64", ng.ARITH_FP64), ("df64", ng.ARITH_DF64)):
+            o = ng.default_assemble_opts(arith=ar, **kw)
             ctx.zero()
-            ctx.event_record(0)
-            ctx.assemble(kern, o)
-            ctx.event_record(1)
-            ctx.synchronize()
-            ms.append(ctx.event_elapsed_ms(0, 1))
-        out[name] = {"assemble_ms": statistics.median(ms),
-                     "elements_per_s": conn.shape[0] / (statistics.median(ms) * 1e-3)}
+            ctx.assemble(kern, o)  # warm-up (and scatter autotune)
+            ms = []
+            for _ in range(reps):
+                ctx.zero()
+                ctx.event_record(0)
+                ctx.assemble(kern, o)
+                ctx.event_record(1)
+                ctx.synchronize()
+                ms.append(ctx.event_elapsed_ms(0, 1))
+            out[name][an] = {"assemble_ms": statistics.median(ms),
+                             "elements_per_s": conn.shape[0] / (statistics.median(ms) * 1e-3)}
     # system of the upwind-blended kernel, no-slip walls
     on_wall = np.any((c <= 1e-12) | (c >= 1.0 - 1e-12), axis=1)
     walls = np.nonzero(on_wall)[0]

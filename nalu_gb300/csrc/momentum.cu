@@ -18,53 +18,9 @@
 
 #include "hex8_elem.h"
 #include "internal.h"
+#include "momentum.cuh"
 
 namespace nalu_gb300 {
-
-constexpr int kMomElems = 16;
-constexpr int kMomThreads = kMomElems * 12;  // 192
-
-struct MomArgs {
-  const int32_t* __restrict__ conn;
-  const double* __restrict__ x;
-  const double* __restrict__ u;
-  const double* __restrict__ vrtm;
-  const double* __restrict__ rho;
-  const double* __restrict__ mu;
-  const double* __restrict__ gju;
-  const double* __restrict__ mdot;  // [E][12]
-  double include_divu, alpha, alpha_upw, upw, hf;
-  int use_limiter;
-  const int64_t* __restrict__ rowptr;
-  const uint8_t* __restrict__ slots;
-  double* __restrict__ values;
-  double* __restrict__ rhs;
-  const int32_t* __restrict__ elems;
-  int64_t count;
-  int32_t* flags;
-  double* cap_lhs;
-  double* cap_rhs;
-  int64_t cap_elem;
-};
-
-// shared-memory layout per element (doubles)
-struct MomLayout {
-  static constexpr int X = 0, U = 24, MU = 48, MD = 56, VR = 68, RHO = 92, GJU = 100;
-  static constexpr int NODE_END = 172;
-  static constexpr int DNDX = NODE_END;          // [12][8][3]
-  static constexpr int AA = DNDX + 288;          // [12][3]   -mu_ip * A_j
-  static constexpr int DIAG = AA + 36;           // [12][8]   same-dof factor
-  static constexpr int RIP = DIAG + 96;          // [12][3]   residual per ip
-  static constexpr int ALHS = RIP + 36;          // [12][2]   upwind L/R factors
-  static constexpr int SIZE = ALHS + 24;         // 676
-};
-
-// ips adjacent to node r, ascending
-__device__ __forceinline__ int node_ip(int r, int k) {
-  // node 0: 0 3 8 | 1: 0 1 9 | 2: 1 2 10 | 3: 2 3 11 | 4: 4 7 8 | 5: 4 5 9 | 6: 5 6 10 | 7: 6 7 11
-  const int tab[8][3] = {{0, 3, 8}, {0, 1, 9}, {1, 2, 10}, {2, 3, 11}, {4, 7, 8}, {4, 5, 9}, {5, 6, 10}, {6, 7, 11}};
-  return tab[r][k];
-}
 
 template <bool UPW, bool SHIFT, bool SKEW, int OUT>
 __global__ void __launch_bounds__(kMomThreads) k_assemble_momentum(MomArgs a) {
@@ -360,6 +316,12 @@ int launch_momentum(nalu_ctx* ctx, int kernel, const nalu_assemble_opts& o, int 
   a.rhs = ctx->d_rhs.p;
   a.flags = ctx->d_flags.p;
   const bool shift = o.shifted_grad_op != 0, skew = o.skew_symmetric != 0;
+  if (o.arith == NALU_ARITH_DF64) {
+    a.cap_elem = cap_elem;
+    a.cap_lhs = cap_lhs;
+    a.cap_rhs = cap_rhs;
+    return launch_momentum_df(ctx, kernel, a, scatter, cap_elem, shift, skew);
+  }
   if (cap_elem >= 0) {
     a.cap_elem = cap_elem;
     a.cap_lhs = cap_lhs;

@@ -1,0 +1,411 @@
+// momentum_df.cu -- the 24x24 momentum element kernels
+// (MomentumAdvDiffElemKernel, src/kernel/MomentumAdvDiffElemKernel.C:72-185;
+// MomentumUpwAdvDiffElemKernel, src/kernel/MomentumUpwAdvDiffElemKernel.C:90-320)
+// with the element math in double-float (FP32-pair) arithmetic.
+//
+// Same three phases and the same summation order as momentum.cu:
+//   0. gather: coordinates relative to node 0 of the element (FP64
+//      differences, then split), nodal fields split into FP32 pairs; nine
+//      threads per element form the edge-form Jacobian coefficients;
+//   1. one thread per (element, SCS ip): Jacobian from the edge form,
+//      cofactors, area vector, grad op, the per-ip sums; the upwind / Peclet
+//      scalar logic of the blended kernel stays in FP64 (a few dozen
+//      operations per ip);
+//   2. one thread per (element, matrix row): the 24 entries summed over the
+//      row node's three ips, converted to FP64 and scattered.
+// Shape-function values and derivatives at the ip locations are products of
+// 1/2 +- s with s in {0, +-1/4, +-1/2}: exact in FP32.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "hex8_elem_df.h"
+#include "internal.h"
+#include "momentum.cuh"
+
+namespace nalu_gb300 {
+namespace {
+
+// shared-memory layout per element in df64 words: MomLayout, then the edge form
+struct MomLayoutDF {
+  static constexpr int EF = MomLayout::SIZE;  // [k][i][A,B,C,D]
+  static constexpr int SIZE = EF + 36;
+};
+
+__device__ __forceinline__ float shape_f(int n, const float s[3]) {
+  return (0.5f + (float)corner_sign(n, 0) * s[0]) * (0.5f + (float)corner_sign(n, 1) * s[1]) *
+         (0.5f + (float)corner_sign(n, 2) * s[2]);
+}
+__device__ __forceinline__ float dshape_f(int n, int k, const float s[3]) {
+  float v = (float)corner_sign(n, k);
+#pragma unroll
+  for (int m = 0; m < 3; ++m)
+    if (m != k) v *= 0.5f + (float)corner_sign(n, m) * s[m];
+  return v;
+}
+__device__ __forceinline__ int node_of_rt(int s0, int s1, int s2) {
+  // STK Hex8 numbering from corner signs (runtime form of node_of)
+  const int lo = s1 < 0 ? (s0 < 0 ? 0 : 1) : (s0 < 0 ? 3 : 2);
+  return lo + (s2 < 0 ? 0 : 4);
+}
+
+// edge-form coefficients of column k, component i (the bilinear interpolation
+// of the four element edges along axis k): J[i][k](s) = A + B s_u + C s_v + D s_u s_v
+__device__ void edge_entry_df(const df64* X, int k, int i, df64* out) {
+  const int u = (k == 0) ? 1 : 0, v = (k == 2) ? 1 : 2;
+  df64 e[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    int sg[3];
+    sg[u] = (q & 1) ? 1 : -1;
+    sg[v] = (q & 2) ? 1 : -1;
+    sg[k] = -1;
+    const int a = node_of_rt(sg[0], sg[1], sg[2]);
+    sg[k] = 1;
+    const int b = node_of_rt(sg[0], sg[1], sg[2]);
+    e[q] = df_sub(X[3 * b + i], X[3 * a + i]);
+  }
+  const df64 p01 = df_add(e[0], e[1]), m01 = df_sub(e[1], e[0]);
+  const df64 p23 = df_add(e[2], e[3]), m23 = df_sub(e[3], e[2]);
+  out[0] = df_scale2(df_add(p01, p23), 0.25f);
+  out[1] = df_scale2(df_add(m01, m23), 0.5f);
+  out[2] = df_scale2(df_sub(p23, p01), 0.5f);
+  out[3] = df_sub(m23, m01);
+}
+
+// J at location s from the edge form in shared memory
+__device__ void jacobian_ef_df(const df64* EF, const float s[3], df64 j[3][3]) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const int u = (k == 0) ? 1 : 0, v = (k == 2) ? 1 : 2;
+    const float su = s[u], sv = s[v];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const df64* c = EF + 4 * (3 * k + i);
+      df64 r = c[0];
+      if (su != 0.0f) r = df_add(r, df_mul_f(c[1], su));
+      if (sv != 0.0f) r = df_add(r, df_mul_f(c[2], sv));
+      if (su != 0.0f && sv != 0.0f) r = df_add(r, df_mul_f(c[3], su * sv));
+      j[i][k] = r;
+    }
+  }
+}
+
+__device__ __forceinline__ double dbl(df64 v) { return df_to_double_bits(v); }
+__device__ __forceinline__ df64 spl(double v) { return df_split_bits(v); }
+
+template <bool UPW, bool SHIFT, bool SKEW, int OUT>
+__global__ void __launch_bounds__(kMomThreads) k_assemble_momentum_df(MomArgs a) {
+  extern __shared__ df64 smd[];
+  __shared__ int s_nodes[kMomElems][8];
+  __shared__ int64_t s_elem[kMomElems];
+  const int t = threadIdx.x;
+  const int el = t / 12, sub = t % 12;
+  const int64_t gi = (int64_t)blockIdx.x * kMomElems + el;
+  const bool valid = gi < a.count;
+  df64* S = smd + el * MomLayoutDF::SIZE;
+
+  // ---- phase 0: gather ----
+  if (valid) {
+    const int64_t e = (OUT == 2) ? a.cap_elem : (a.elems ? (int64_t)a.elems[gi] : gi);
+    if (sub == 0) s_elem[el] = e;
+    if (sub < 8) {
+      const int n = __ldg(a.conn + 8 * e + sub);
+      const int n0 = __ldg(a.conn + 8 * e);
+      s_nodes[el][sub] = n;
+      for (int d = 0; d < 3; ++d) {
+        S[MomLayout::X + 3 * sub + d] =
+            sub == 0 ? df_zero() : spl(__ldg(a.x + 3 * (int64_t)n + d) - __ldg(a.x + 3 * (int64_t)n0 + d));
+        S[MomLayout::U + 3 * sub + d] = spl(__ldg(a.u + 3 * (int64_t)n + d));
+      }
+      S[MomLayout::MU + sub] = spl(__ldg(a.mu + n));
+      if (UPW) {
+        for (int d = 0; d < 3; ++d) S[MomLayout::VR + 3 * sub + d] = spl(__ldg(a.vrtm + 3 * (int64_t)n + d));
+        S[MomLayout::RHO + sub] = spl(__ldg(a.rho + n));
+        for (int k = 0; k < 9; ++k) S[MomLayout::GJU + 9 * sub + k] = spl(__ldg(a.gju + 9 * (int64_t)n + k));
+      }
+    }
+    S[MomLayout::MD + sub] = spl(__ldg(a.mdot + 12 * e + sub));
+  }
+  __syncthreads();
+  if (valid && sub < 9) edge_entry_df(S + MomLayout::X, sub / 3, sub % 3, S + MomLayoutDF::EF + 4 * sub);
+  __syncthreads();
+
+  // ---- phase 1: per ip ----
+  if (valid) {
+    const int ip = sub;
+    float s[3], g[3], av[3];
+    ip_location(ip, 0.25f, s);
+    const df64* X = S + MomLayout::X;
+    const df64* EF = S + MomLayoutDF::EF;
+    df64 j[3][3], adj[3][3], det;
+    jacobian_ef_df(EF, s, j);
+    cofactor_df(j, adj, det);
+    const int dd = ip_dir(ip);
+    const float sg4 = (ip < 8 && (ip & 3) == 2) ? -0.25f : 0.25f;
+    df64 A[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) A[i] = df_scale2(dd == 0 ? adj[i][0] : (dd == 1 ? adj[i][1] : adj[i][2]), sg4);
+    float mindet = det.hi;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) g[k] = s[k];
+    if (SHIFT) {
+      ip_location(ip, 0.5f, g);
+      jacobian_ef_df(EF, g, j);
+      cofactor_df(j, adj, det);
+      mindet = fminf(mindet, det.hi);
+    }
+    if (!(mindet > 1.0e-37f)) atomicAdd(a.flags + FLAG_NEG_JAC, 1);  // det <= 0 (or below FP32 range)
+    const df64 inv = df_rcp(det);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) adj[i][k] = df_mul(adj[i][k], inv);
+    df64* DN = S + MomLayout::DNDX + 24 * ip;
+    const df64* Un = S + MomLayout::U;
+    const df64* MUn = S + MomLayout::MU;
+    const df64 tmdot = S[MomLayout::MD + ip];
+    ip_location(ip, SKEW ? 0.5f : 0.25f, av);
+    df64 muIp = df_zero(), uIp[3] = {df_zero(), df_zero(), df_zero()}, cIp[3] = {df_zero(), df_zero(), df_zero()};
+    df64 divU = df_zero(), dA[8], vr[3] = {df_zero(), df_zero(), df_zero()};
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      const float d0 = dshape_f(c, 0, g), d1 = dshape_f(c, 1, g), d2 = dshape_f(c, 2, g);
+      df64 dn[3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+        dn[i] = df_add(df_add(df_mul_f(adj[i][0], d0), df_mul_f(adj[i][1], d1)), df_mul_f(adj[i][2], d2));
+      DN[3 * c] = dn[0];
+      DN[3 * c + 1] = dn[1];
+      DN[3 * c + 2] = dn[2];
+      const float r = shape_f(c, s), rAdv = shape_f(c, av);
+      muIp = df_add(muIp, df_mul_f(MUn[c], r));
+      const df64 uc0 = Un[3 * c], uc1 = Un[3 * c + 1], uc2 = Un[3 * c + 2];
+      uIp[0] = df_add(uIp[0], df_mul_f(uc0, rAdv));
+      uIp[1] = df_add(uIp[1], df_mul_f(uc1, rAdv));
+      uIp[2] = df_add(uIp[2], df_mul_f(uc2, rAdv));
+      if (UPW) {
+        cIp[0] = df_add(cIp[0], df_mul_f(X[3 * c], rAdv));
+        cIp[1] = df_add(cIp[1], df_mul_f(X[3 * c + 1], rAdv));
+        cIp[2] = df_add(cIp[2], df_mul_f(X[3 * c + 2], rAdv));
+      }
+      divU = df_fma(uc2, dn[2], df_fma(uc1, dn[1], df_fma(uc0, dn[0], divU)));
+      dA[c] = df_fma(dn[2], A[2], df_fma(dn[1], A[1], df_mul(dn[0], A[0])));
+      const df64 Au = df_fma(A[2], uc2, df_fma(A[1], uc1, df_mul(A[0], uc0)));
+      vr[0] = df_fma(dA[c], uc0, df_fma(dn[0], Au, vr[0]));
+      vr[1] = df_fma(dA[c], uc1, df_fma(dn[1], Au, vr[1]));
+      vr[2] = df_fma(dA[c], uc2, df_fma(dn[2], Au, vr[2]));
+    }
+    const df64 nmu = df_neg(muIp);
+    df64* AA = S + MomLayout::AA + 3 * ip;
+    AA[0] = df_mul(nmu, A[0]);
+    AA[1] = df_mul(nmu, A[1]);
+    AA[2] = df_mul(nmu, A[2]);
+    double advscale = 1.0;
+    df64 aflux[3] = {df_mul(tmdot, uIp[0]), df_mul(tmdot, uIp[1]), df_mul(tmdot, uIp[2])};
+    double alhsL = 0.0, alhsR = 0.0;
+    if (UPW) {
+      // the blending scalars in FP64 (as in momentum.cu)
+      const int il = ip_left(ip), ir = ip_right(ip);
+      const double small_ = 1.0e-16;
+      const df64* VR = S + MomLayout::VR;
+      const df64* RHO = S + MomLayout::RHO;
+      const df64* GJ = S + MomLayout::GJU;
+      const double tm = dbl(tmdot);
+      double udotx = 0.0, duL[3], duR[3], uI[3], cI[3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        uI[i] = dbl(uIp[i]);
+        cI[i] = dbl(cIp[i]);
+      }
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        const double dxi = dbl(X[3 * ir + i]) - dbl(X[3 * il + i]);
+        const double ui = 0.5 * (dbl(VR[3 * il + i]) + dbl(VR[3 * ir + i]));
+        udotx += ui * dxi;
+        duL[i] = 0.0;
+        duR[i] = 0.0;
+#pragma unroll
+        for (int jj = 0; jj < 3; ++jj) {
+          duL[i] += (cI[jj] - dbl(X[3 * il + jj])) * dbl(GJ[9 * il + 3 * i + jj]);
+          duR[i] += (dbl(X[3 * ir + jj]) - cI[jj]) * dbl(GJ[9 * ir + 3 * i + jj]);
+        }
+      }
+      const double diffIp = 0.5 * (dbl(MUn[il]) / dbl(RHO[il]) + dbl(MUn[ir]) / dbl(RHO[ir]));
+      const double pe = fabs(udotx) / (diffIp + small_);
+      const double mpe = a.hf * pe;
+      const double pecfac = mpe * mpe / (5.0 + mpe * mpe);
+      const double om_pecfac = 1.0 - pecfac;
+      const double om_alpha = 1.0 - a.alpha, om_alphaUpw = 1.0 - a.alpha_upw;
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        double limL = 1.0, limR = 1.0;
+        const double uil = dbl(Un[3 * il + i]), uir = dbl(Un[3 * ir + i]);
+        if (a.use_limiter) {
+          const double dq = uir - uil;
+          const double dqMl = 2.0 * 2.0 * duL[i] - dq;
+          const double dqMr = 2.0 * 2.0 * duR[i] - dq;
+          limL = (2.0 * (dqMl * dq + fabs(dqMl * dq))) / ((dqMl + dq) * (dqMl + dq) + small_);
+          limR = (2.0 * (dqMr * dq + fabs(dqMr * dq))) / ((dqMr + dq) * (dqMr + dq) + small_);
+        }
+        const double uL = uil + duL[i] * a.upw * limL;
+        const double uR = uir - duR[i] * a.upw * limR;
+        const double uiUpw = tm > 0 ? a.alpha_upw * uL + om_alphaUpw * uI[i] : a.alpha_upw * uR + om_alphaUpw * uI[i];
+        const double hatL = a.alpha * uL + om_alpha * uI[i];
+        const double hatR = a.alpha * uR + om_alpha * uI[i];
+        const double uCds = 0.5 * (hatL + hatR);
+        aflux[i] = spl(tm * (pecfac * uiUpw + om_pecfac * uCds));
+      }
+      alhsL = 0.5 * (tm + fabs(tm)) * pecfac * a.alpha_upw + 0.5 * a.alpha * om_pecfac * tm;
+      alhsR = 0.5 * (tm - fabs(tm)) * pecfac * a.alpha_upw + 0.5 * a.alpha * om_pecfac * tm;
+      advscale = pecfac * om_alphaUpw + om_pecfac * om_alpha;
+    }
+    df64* DG = S + MomLayout::DIAG + 8 * ip;
+    const df64 tmsc = UPW ? df_mul(tmdot, spl(advscale)) : tmdot;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) DG[c] = df_fma(nmu, dA[c], df_mul_f(tmsc, shape_f(c, av)));
+    df64* RI = S + MomLayout::RIP + 3 * ip;
+    const df64 dstress = spl(2.0 / 3.0 * dbl(muIp) * dbl(divU) * a.include_divu);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) RI[i] = df_fma(nmu, vr[i], df_fma(dstress, A[i], aflux[i]));
+    S[MomLayout::ALHS + 2 * ip] = spl(alhsL);
+    S[MomLayout::ALHS + 2 * ip + 1] = spl(alhsR);
+  }
+  __syncthreads();
+
+  // ---- phase 2: rows; each thread owns rows sub and sub+12 of its element ----
+  if (!valid) return;
+  for (int h = 0; h < 2; ++h) {
+    const int row = sub + 12 * h;  // = 3 r + i
+    const int r = row / 3, i = row % 3;
+    df64 v[8][3];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) v[c][0] = v[c][1] = v[c][2] = df_zero();
+    df64 rs = df_zero();
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const int ip = node_ip(r, k);
+      const int il = ip_left(ip), ir = ip_right(ip);
+      const bool left = il == r;
+      const df64* DN = S + MomLayout::DNDX + 24 * ip;
+      const df64* AA = S + MomLayout::AA + 3 * ip;
+      const df64* DG = S + MomLayout::DIAG + 8 * ip;
+      const df64 aa0 = left ? AA[0] : df_neg(AA[0]), aa1 = left ? AA[1] : df_neg(AA[1]),
+                 aa2 = left ? AA[2] : df_neg(AA[2]);
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        const df64 di = DN[3 * c + i];
+        v[c][0] = df_fma(di, aa0, v[c][0]);
+        v[c][1] = df_fma(di, aa1, v[c][1]);
+        v[c][2] = df_fma(di, aa2, v[c][2]);
+        const df64 dg = left ? DG[c] : df_neg(DG[c]);
+        if (i == 0) v[c][0] = df_add(v[c][0], dg);
+        else if (i == 1) v[c][1] = df_add(v[c][1], dg);
+        else v[c][2] = df_add(v[c][2], dg);
+      }
+      if (UPW) {
+        const df64 aL = S[MomLayout::ALHS + 2 * ip], aR = S[MomLayout::ALHS + 2 * ip + 1];
+        const df64 sL = left ? aL : df_neg(aL), sR = left ? aR : df_neg(aR);
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+          if (c == il) {
+            if (i == 0) v[c][0] = df_add(v[c][0], sL);
+            else if (i == 1) v[c][1] = df_add(v[c][1], sL);
+            else v[c][2] = df_add(v[c][2], sL);
+          }
+          if (c == ir) {
+            if (i == 0) v[c][0] = df_add(v[c][0], sR);
+            else if (i == 1) v[c][1] = df_add(v[c][1], sR);
+            else v[c][2] = df_add(v[c][2], sR);
+          }
+        }
+      }
+      const df64 ri = S[MomLayout::RIP + 3 * ip + i];
+      rs = df_sub(rs, left ? ri : df_neg(ri));
+    }
+    if (OUT == 2) {
+#pragma unroll
+      for (int c = 0; c < 8; ++c)
+#pragma unroll
+        for (int jj = 0; jj < 3; ++jj) a.cap_lhs[row * 24 + 3 * c + jj] = dbl(v[c][jj]);
+      a.cap_rhs[row] = dbl(rs);
+      continue;
+    }
+    const int64_t e = s_elem[el];
+    const int64_t grow = 3 * (int64_t)s_nodes[el][r] + i;
+    const int64_t base = __ldg(a.rowptr + grow);
+    const uint2 o2 = __ldg(reinterpret_cast<const uint2*>(a.slots + 64 * e + 8 * r));
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      const uint32_t word = c < 4 ? o2.x : o2.y;
+      const int off = (word >> (8 * (c & 3))) & 0xff;
+      double* dst = a.values + base + 3 * off;
+#pragma unroll
+      for (int jj = 0; jj < 3; ++jj) {
+        if (OUT == 0) atomicAdd(dst + jj, dbl(v[c][jj]));
+        else dst[jj] += dbl(v[c][jj]);
+      }
+    }
+    if (OUT == 0) atomicAdd(a.rhs + grow, dbl(rs));
+    else a.rhs[grow] += dbl(rs);
+  }
+}
+
+template <bool UPW, bool SHIFT, bool SKEW, int OUT>
+void launch_mom_df_variant(nalu_ctx* ctx, const MomArgs& a, int64_t count) {
+  const size_t smem = sizeof(df64) * MomLayoutDF::SIZE * kMomElems;
+  cudaFuncSetAttribute(k_assemble_momentum_df<UPW, SHIFT, SKEW, OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)smem);
+  const unsigned grid = (unsigned)((count + kMomElems - 1) / kMomElems);
+  if (grid == 0) return;
+  k_assemble_momentum_df<UPW, SHIFT, SKEW, OUT><<<grid, kMomThreads, smem, ctx->stream>>>(a);
+  ctx->launches++;
+}
+
+template <int OUT>
+void launch_mom_df_out(nalu_ctx* ctx, bool upw, bool shift, bool skew, const MomArgs& a, int64_t count) {
+  if (upw) {
+    if (shift) {
+      if (skew) launch_mom_df_variant<true, true, true, OUT>(ctx, a, count);
+      else launch_mom_df_variant<true, true, false, OUT>(ctx, a, count);
+    } else {
+      if (skew) launch_mom_df_variant<true, false, true, OUT>(ctx, a, count);
+      else launch_mom_df_variant<true, false, false, OUT>(ctx, a, count);
+    }
+  } else {
+    if (shift) {
+      if (skew) launch_mom_df_variant<false, true, true, OUT>(ctx, a, count);
+      else launch_mom_df_variant<false, true, false, OUT>(ctx, a, count);
+    } else {
+      if (skew) launch_mom_df_variant<false, false, true, OUT>(ctx, a, count);
+      else launch_mom_df_variant<false, false, false, OUT>(ctx, a, count);
+    }
+  }
+}
+
+}  // namespace
+
+int launch_momentum_df(nalu_ctx* ctx, int kernel, const MomArgs& a, int scatter, int64_t cap_elem, bool shift,
+                       bool skew) {
+  const bool upw = kernel == NALU_KERNEL_MOMENTUM_UPW_ADV_DIFF;
+  if (cap_elem >= 0) {
+    MomArgs ac = a;
+    ac.count = 1;
+    launch_mom_df_out<2>(ctx, upw, shift, skew, ac, 1);
+  } else if (scatter == NALU_SCATTER_COLOURED) {
+    const int nc = (int)ctx->colour_offsets.size() - 1;
+    for (int c = 0; c < nc; ++c) {
+      MomArgs ac = a;
+      ac.elems = ctx->d_colour_elems.p + ctx->colour_offsets[c];
+      ac.count = ctx->colour_offsets[c + 1] - ctx->colour_offsets[c];
+      launch_mom_df_out<1>(ctx, upw, shift, skew, ac, ac.count);
+    }
+  } else {
+    MomArgs ac = a;
+    ac.count = ctx->n_elems;
+    launch_mom_df_out<0>(ctx, upw, shift, skew, ac, ac.count);
+  }
+  return cuda_check(ctx, cudaGetLastError(), "momentum (df64) launch");
+}
+
+}  // namespace nalu_gb300
