@@ -8,9 +8,8 @@
 //      differences, then split), nodal fields split into FP32 pairs; nine
 //      threads per element form the edge-form Jacobian coefficients;
 //   1. one thread per (element, SCS ip): Jacobian from the edge form,
-//      cofactors, area vector, grad op, the per-ip sums; the upwind / Peclet
-//      scalar logic of the blended kernel stays in FP64 (a few dozen
-//      operations per ip);
+//      cofactors, area vector, grad op, the per-ip sums and the upwind /
+//      Peclet blending of the blended kernel;
 //   2. one thread per (element, matrix row): the 24 entries summed over the
 //      row node's three ips, converted to FP64 and scattered.
 // Shape-function values and derivatives at the ip locations are products of
@@ -93,6 +92,8 @@ __device__ void jacobian_ef_df(const df64* EF, const float s[3], df64 j[3][3]) {
 
 __device__ __forceinline__ double dbl(df64 v) { return df_to_double_bits(v); }
 __device__ __forceinline__ df64 spl(double v) { return df_split_bits(v); }
+__device__ __forceinline__ df64 df_div(df64 a, df64 b) { return df_mul(a, df_rcp(b)); }
+__device__ __forceinline__ df64 df_abs(df64 a) { return a.hi < 0.0f ? df_neg(a) : a; }
 
 template <bool UPW, bool SHIFT, bool SKEW, int OUT>
 __global__ void __launch_bounds__(kMomThreads) k_assemble_momentum_df(MomArgs a) {
@@ -201,75 +202,78 @@ __global__ void __launch_bounds__(kMomThreads) k_assemble_momentum_df(MomArgs a)
     AA[0] = df_mul(nmu, A[0]);
     AA[1] = df_mul(nmu, A[1]);
     AA[2] = df_mul(nmu, A[2]);
-    double advscale = 1.0;
+    df64 advscale = df64{1.0f, 0.0f};
     df64 aflux[3] = {df_mul(tmdot, uIp[0]), df_mul(tmdot, uIp[1]), df_mul(tmdot, uIp[2])};
-    double alhsL = 0.0, alhsR = 0.0;
+    df64 alhsL = df_zero(), alhsR = df_zero();
     if (UPW) {
-      // the blending scalars in FP64 (as in momentum.cu)
+      // upwind / central blending (MomentumUpwAdvDiffElemKernel.C, classic Peclet
+      // function, optional van Leer limiter), in FP32 pairs like the rest
       const int il = ip_left(ip), ir = ip_right(ip);
-      const double small_ = 1.0e-16;
+      const df64 small_ = spl(1.0e-16);
       const df64* VR = S + MomLayout::VR;
       const df64* RHO = S + MomLayout::RHO;
       const df64* GJ = S + MomLayout::GJU;
-      const double tm = dbl(tmdot);
-      double udotx = 0.0, duL[3], duR[3], uI[3], cI[3];
+      df64 udotx = df_zero(), duL[3], duR[3];
 #pragma unroll
       for (int i = 0; i < 3; ++i) {
-        uI[i] = dbl(uIp[i]);
-        cI[i] = dbl(cIp[i]);
-      }
-#pragma unroll
-      for (int i = 0; i < 3; ++i) {
-        const double dxi = dbl(X[3 * ir + i]) - dbl(X[3 * il + i]);
-        const double ui = 0.5 * (dbl(VR[3 * il + i]) + dbl(VR[3 * ir + i]));
-        udotx += ui * dxi;
-        duL[i] = 0.0;
-        duR[i] = 0.0;
+        const df64 dxi = df_sub(X[3 * ir + i], X[3 * il + i]);
+        const df64 ui = df_scale2(df_add(VR[3 * il + i], VR[3 * ir + i]), 0.5f);
+        udotx = df_fma(ui, dxi, udotx);
+        duL[i] = df_zero();
+        duR[i] = df_zero();
 #pragma unroll
         for (int jj = 0; jj < 3; ++jj) {
-          duL[i] += (cI[jj] - dbl(X[3 * il + jj])) * dbl(GJ[9 * il + 3 * i + jj]);
-          duR[i] += (dbl(X[3 * ir + jj]) - cI[jj]) * dbl(GJ[9 * ir + 3 * i + jj]);
+          duL[i] = df_fma(df_sub(cIp[jj], X[3 * il + jj]), GJ[9 * il + 3 * i + jj], duL[i]);
+          duR[i] = df_fma(df_sub(X[3 * ir + jj], cIp[jj]), GJ[9 * ir + 3 * i + jj], duR[i]);
         }
       }
-      const double diffIp = 0.5 * (dbl(MUn[il]) / dbl(RHO[il]) + dbl(MUn[ir]) / dbl(RHO[ir]));
-      const double pe = fabs(udotx) / (diffIp + small_);
-      const double mpe = a.hf * pe;
-      const double pecfac = mpe * mpe / (5.0 + mpe * mpe);
-      const double om_pecfac = 1.0 - pecfac;
-      const double om_alpha = 1.0 - a.alpha, om_alphaUpw = 1.0 - a.alpha_upw;
+      const df64 diffIp = df_scale2(df_add(df_div(MUn[il], RHO[il]), df_div(MUn[ir], RHO[ir])), 0.5f);
+      const df64 pe = df_div(df_abs(udotx), df_add(diffIp, small_));
+      const df64 mpe = df_mul(spl(a.hf), pe);
+      const df64 mpe2 = df_mul(mpe, mpe);
+      const df64 pecfac = df_div(mpe2, df_add(df64{5.0f, 0.0f}, mpe2));
+      const df64 one = df64{1.0f, 0.0f};
+      const df64 om_pecfac = df_sub(one, pecfac);
+      const df64 alpha = spl(a.alpha), alpha_upw = spl(a.alpha_upw), upw = spl(a.upw);
+      const df64 om_alpha = df_sub(one, alpha), om_alphaUpw = df_sub(one, alpha_upw);
+      const bool pos = tmdot.hi > 0.0f;
 #pragma unroll
       for (int i = 0; i < 3; ++i) {
-        double limL = 1.0, limR = 1.0;
-        const double uil = dbl(Un[3 * il + i]), uir = dbl(Un[3 * ir + i]);
+        df64 limL = one, limR = one;
+        const df64 uil = Un[3 * il + i], uir = Un[3 * ir + i];
         if (a.use_limiter) {
-          const double dq = uir - uil;
-          const double dqMl = 2.0 * 2.0 * duL[i] - dq;
-          const double dqMr = 2.0 * 2.0 * duR[i] - dq;
-          limL = (2.0 * (dqMl * dq + fabs(dqMl * dq))) / ((dqMl + dq) * (dqMl + dq) + small_);
-          limR = (2.0 * (dqMr * dq + fabs(dqMr * dq))) / ((dqMr + dq) * (dqMr + dq) + small_);
+          const df64 dq = df_sub(uir, uil);
+          const df64 dqMl = df_sub(df_scale2(duL[i], 4.0f), dq);
+          const df64 dqMr = df_sub(df_scale2(duR[i], 4.0f), dq);
+          const df64 pl = df_mul(dqMl, dq), pr = df_mul(dqMr, dq);
+          const df64 sl = df_add(dqMl, dq), sr = df_add(dqMr, dq);
+          limL = df_div(df_scale2(df_add(pl, df_abs(pl)), 2.0f), df_add(df_mul(sl, sl), small_));
+          limR = df_div(df_scale2(df_add(pr, df_abs(pr)), 2.0f), df_add(df_mul(sr, sr), small_));
         }
-        const double uL = uil + duL[i] * a.upw * limL;
-        const double uR = uir - duR[i] * a.upw * limR;
-        const double uiUpw = tm > 0 ? a.alpha_upw * uL + om_alphaUpw * uI[i] : a.alpha_upw * uR + om_alphaUpw * uI[i];
-        const double hatL = a.alpha * uL + om_alpha * uI[i];
-        const double hatR = a.alpha * uR + om_alpha * uI[i];
-        const double uCds = 0.5 * (hatL + hatR);
-        aflux[i] = spl(tm * (pecfac * uiUpw + om_pecfac * uCds));
+        const df64 uL = df_fma(df_mul(duL[i], upw), limL, uil);
+        const df64 uR = df_sub(uir, df_mul(df_mul(duR[i], upw), limR));
+        const df64 uiUpw = df_fma(om_alphaUpw, uIp[i], df_mul(alpha_upw, pos ? uL : uR));
+        const df64 hatL = df_fma(om_alpha, uIp[i], df_mul(alpha, uL));
+        const df64 hatR = df_fma(om_alpha, uIp[i], df_mul(alpha, uR));
+        const df64 uCds = df_scale2(df_add(hatL, hatR), 0.5f);
+        aflux[i] = df_mul(tmdot, df_fma(om_pecfac, uCds, df_mul(pecfac, uiUpw)));
       }
-      alhsL = 0.5 * (tm + fabs(tm)) * pecfac * a.alpha_upw + 0.5 * a.alpha * om_pecfac * tm;
-      alhsR = 0.5 * (tm - fabs(tm)) * pecfac * a.alpha_upw + 0.5 * a.alpha * om_pecfac * tm;
-      advscale = pecfac * om_alphaUpw + om_pecfac * om_alpha;
+      const df64 atm = df_abs(tmdot);
+      const df64 cen = df_mul(df_scale2(df_mul(alpha, om_pecfac), 0.5f), tmdot);
+      alhsL = df_fma(df_scale2(df_add(tmdot, atm), 0.5f), df_mul(pecfac, alpha_upw), cen);
+      alhsR = df_fma(df_scale2(df_sub(tmdot, atm), 0.5f), df_mul(pecfac, alpha_upw), cen);
+      advscale = df_fma(om_pecfac, om_alpha, df_mul(pecfac, om_alphaUpw));
     }
     df64* DG = S + MomLayout::DIAG + 8 * ip;
-    const df64 tmsc = UPW ? df_mul(tmdot, spl(advscale)) : tmdot;
+    const df64 tmsc = UPW ? df_mul(tmdot, advscale) : tmdot;
 #pragma unroll
     for (int c = 0; c < 8; ++c) DG[c] = df_fma(nmu, dA[c], df_mul_f(tmsc, shape_f(c, av)));
     df64* RI = S + MomLayout::RIP + 3 * ip;
     const df64 dstress = spl(2.0 / 3.0 * dbl(muIp) * dbl(divU) * a.include_divu);
 #pragma unroll
     for (int i = 0; i < 3; ++i) RI[i] = df_fma(nmu, vr[i], df_fma(dstress, A[i], aflux[i]));
-    S[MomLayout::ALHS + 2 * ip] = spl(alhsL);
-    S[MomLayout::ALHS + 2 * ip + 1] = spl(alhsR);
+    S[MomLayout::ALHS + 2 * ip] = alhsL;
+    S[MomLayout::ALHS + 2 * ip + 1] = alhsR;
   }
   __syncthreads();
 
