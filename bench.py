@@ -325,14 +325,19 @@ def bench_gpu(args):
         hist = ctx.learned_train(st, rf, tg, epochs=40)
         t2 = time.perf_counter()
         learned_w = ctx.learned_weights()
-        info = ctx.solve(ng.default_solver_opts(tol=1e-8, max_iters=40000, precond=ng.PRECOND_LEARNED),
-                         raise_on_error=False)
-        solve["learned_fcg"] = {"ms": 1e3 * info.seconds, "setup_ms": 1e3 * info.setup_seconds,
-                                "iterations": info.iterations, "learned_iterations": info.learned_iterations,
-                                "fallback": info.fallback, "true_rel_res": info.true_rel_res, "status": info.status}
+        for key, probe in (("learned_fcg", 0), ("learned_fcg_probe", 1)):
+            info = ctx.solve(ng.default_solver_opts(tol=1e-8, max_iters=40000, precond=ng.PRECOND_LEARNED,
+                                                    learned_probe=probe), raise_on_error=False)
+            solve[key] = {"ms": 1e3 * info.seconds, "setup_ms": 1e3 * info.setup_seconds,
+                          "iterations": info.iterations, "learned_iterations": info.learned_iterations,
+                          "fallback": info.fallback, "true_rel_res": info.true_rel_res, "status": info.status}
+        solve["learned_fallback_codes"] = ("0 learned FCG finished, 1 it stalled -> Chebyshev-Jacobi PCG, "
+                                           "2 Jacobi-CG finished (opening probe or pace bound); learned_fcg runs "
+                                           "the flexible CG itself, learned_fcg_probe the default with the probe")
         solve["learned_training"] = {"pairs": int(tg.size), "harvest_s": t1 - t0, "train_s": t2 - t1,
                                      "epochs": 40, "val_mse_first_last": [float(hist[0, 1]), float(hist[-1, 1])]}
         solve["learned_vs_plain_time"] = solve["jacobi_pcg_fp64"]["ms"] / solve["learned_fcg"]["ms"]
+        solve["learned_probe_vs_plain_time"] = solve["jacobi_pcg_fp64"]["ms"] / solve["learned_fcg_probe"]["ms"]
         if not args.no_c4:
             solve["c4_192"] = bench_c4(ng, learned_w, local)
     batch = bench_batch(ng, local) if extras and not args.no_batch else None
@@ -490,7 +495,8 @@ def bench_c4(ng, weights, dev=0, N=192):
     ctx.learned_set_weights(weights)
     out = {"workload": "continuity_adv_hex8_192^3_zstretch1.05_fourier64, pinned node 0", "nodes": int(n),
            "nnz": int(ctx.sizes()[1])}
-    for name, kw in (("jacobi_pcg_fp64", {}), ("learned_fcg", {"precond": ng.PRECOND_LEARNED})):
+    for name, kw in (("jacobi_pcg_fp64", {}), ("learned_fcg", {"precond": ng.PRECOND_LEARNED, "learned_probe": 0}),
+                     ("learned_fcg_probe", {"precond": ng.PRECOND_LEARNED})):
         info = ctx.solve(ng.default_solver_opts(tol=1e-8, max_iters=60000, check_every=50, **kw), raise_on_error=False)
         out[name] = {"ms": 1e3 * info.seconds, "iterations": info.iterations, "true_rel_res": info.true_rel_res,
                      "status": info.status}
@@ -498,6 +504,7 @@ def bench_c4(ng, weights, dev=0, N=192):
             out[name].update(setup_ms=1e3 * info.setup_seconds, learned_iterations=info.learned_iterations,
                              fallback=info.fallback)
     out["learned_vs_plain_time"] = out["jacobi_pcg_fp64"]["ms"] / out["learned_fcg"]["ms"]
+    out["learned_probe_vs_plain_time"] = out["jacobi_pcg_fp64"]["ms"] / out["learned_fcg_probe"]["ms"]
     ctx.close()
     return out
 
@@ -542,14 +549,36 @@ def bench_batch(ng, dev=0, n_problems=64, seed=2025, reps=2):
     wall, asm_ms, infos = best
     its = sorted(i.iterations for i in infos)
     nnz = ctx.sizes()[1]
+    out = {"workload": "64 continuity problems, edges log-U[16,96] per axis, jitter 0.1, Fourier64 each",
+           "problems": n_problems, "elements": int(conn.shape[0]), "nodes": int(n), "nnz": int(nnz),
+           "problems_per_s": n_problems / wall, "per_problem_ms": 1e3 * wall / n_problems,
+           "wall_ms": 1e3 * wall, "assemble_bc_ms": asm_ms, "solve_ms": infos[0].seconds * 1e3,
+           "iterations_min_median_max": [its[0], its[len(its) // 2], its[-1]],
+           "max_true_rel_res": max(i.true_rel_res for i in infos),
+           "all_converged": all(i.status == 0 for i in infos), "preconditioner": "jacobi (plain PCG)"}
+    # learned flexible CG on the same batch: weights trained on this union system
+    # (20K PCG first-direction pairs, 4 seeded rhs, 40 epochs); the solve time
+    # includes the stencil set-up, the training is reported beside it
+    t0 = time.perf_counter()
+    ctx.learned_init(7)
+    st, rf, tg = ctx.learned_harvest(n_samples=20000, n_rhs=4, seed=2026)
+    ctx.learned_train(st, rf, tg, epochs=40)
+    train_s = time.perf_counter() - t0
+    linfos = ctx.solve_batched(ng.default_solver_opts(tol=1e-8, max_iters=40000, precond=ng.PRECOND_LEARNED),
+                               raise_on_error=False)
+    lits = sorted(i.iterations for i in linfos)
+    lsolve = linfos[0].seconds
+    out["learned_fcg"] = {"solve_ms": 1e3 * lsolve, "setup_ms": 1e3 * linfos[0].setup_seconds,
+                          "problems_per_s": n_problems / (asm_ms * 1e-3 + lsolve),
+                          "iterations_min_median_max": [lits[0], lits[len(lits) // 2], lits[-1]],
+                          "problems_on_learned": int(sum(i.fallback == 0 for i in linfos)),
+                          "problems_probe_chose_jacobi": int(sum(i.fallback == 2 for i in linfos)),
+                          "problems_fell_back_after_stall": int(sum(i.fallback == 1 for i in linfos)),
+                          "max_true_rel_res": max(i.true_rel_res for i in linfos),
+                          "all_converged": all(i.status == 0 for i in linfos), "training_s": train_s}
+    out["learned_vs_plain_time"] = infos[0].seconds / lsolve
     ctx.close()
-    return {"workload": "64 continuity problems, edges log-U[16,96] per axis, jitter 0.1, Fourier64 each",
-            "problems": n_problems, "elements": int(conn.shape[0]), "nodes": int(n), "nnz": int(nnz),
-            "problems_per_s": n_problems / wall, "per_problem_ms": 1e3 * wall / n_problems,
-            "wall_ms": 1e3 * wall, "assemble_bc_ms": asm_ms, "solve_ms": infos[0].seconds * 1e3,
-            "iterations_min_median_max": [its[0], its[len(its) // 2], its[-1]],
-            "max_true_rel_res": max(i.true_rel_res for i in infos),
-            "all_converged": all(i.status == 0 for i in infos), "preconditioner": "jacobi (plain PCG)"}
+    return out
 
 
 def time_mode(ctx, arith, scatter, reps=3):

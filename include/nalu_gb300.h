@@ -191,10 +191,15 @@ typedef struct nalu_solver_opts {
   double tol;        /* stop on true ||b - A x|| / ||b|| <= tol */
   double inner_tol;  /* inner tolerance for iterative refinement */
   int stall_window;  /* learned FCG stalls when the residual norm has no new
-                        minimum for max(stall_window, 4 x the iterations taken
+                        minimum for max(stall_window, 10 x the iterations taken
                         to reach the current minimum); Chebyshev-Jacobi PCG
                         then finishes (default 20) */
-  int reserved[5];
+  int learned_probe; /* learned FCG: 1 (default) opens with a short run of each
+                        of Jacobi-CG and the learned FCG and keeps the faster per
+                        unit of device time, and bounds the learned FCG by twice
+                        the iterations the probe predicts for Jacobi-CG; 0 runs
+                        the learned FCG with the stall fallback only */
+  int reserved[4];
 } nalu_solver_opts;
 typedef struct nalu_solve_info {
   int iterations;        /* inner iterations in total */
@@ -202,8 +207,14 @@ typedef struct nalu_solve_info {
   int status;
   double true_rel_res;   /* FP64 ||b - A x|| / ||b|| */
   double seconds;        /* wall time of the whole call, set-up included */
-  int fallback;          /* 1: the learned FCG stalled; Chebyshev-Jacobi PCG finished */
-  int learned_iterations;/* iterations spent in the learned FCG */
+  int fallback;          /* learned FCG: 0 it finished the solve; 1 it stalled or broke
+                            down and Chebyshev-Jacobi PCG finished; 2 Jacobi-CG
+                            finished, chosen by the opening probe (a short run of
+                            each method from the same start, compared per unit of
+                            device time) or because the learned FCG used twice the
+                            iterations the probe predicts for Jacobi-CG */
+  int learned_iterations;/* iterations spent in the learned FCG (probe included);
+                            iterations counts the probe runs too */
   double setup_seconds;  /* learned preconditioner set-up (MLP stencil + SELL values) */
 } nalu_solve_info;
 void nalu_solver_opts_default(nalu_solver_opts* opts);

@@ -60,7 +60,8 @@ class SolverOpts(ctypes.Structure):
     _fields_ = [("method", ctypes.c_int), ("precond", ctypes.c_int), ("precision", ctypes.c_int),
                 ("max_iters", ctypes.c_int), ("restart", ctypes.c_int), ("cheb_degree", ctypes.c_int),
                 ("check_every", ctypes.c_int), ("x0_zero", ctypes.c_int), ("tol", ctypes.c_double),
-                ("inner_tol", ctypes.c_double), ("stall_window", ctypes.c_int), ("reserved", ctypes.c_int * 5)]
+                ("inner_tol", ctypes.c_double), ("stall_window", ctypes.c_int), ("learned_probe", ctypes.c_int),
+                ("reserved", ctypes.c_int * 4)]
 
 
 class SolveInfo(ctypes.Structure):

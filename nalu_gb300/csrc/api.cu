@@ -811,6 +811,7 @@ void nalu_solver_opts_default(nalu_solver_opts* o) {
   o->tol = 1e-8;
   o->inner_tol = 1e-4;
   o->stall_window = 20;
+  o->learned_probe = 1;
 }
 
 int nalu_solve(nalu_ctx* ctx, const nalu_solver_opts* opts, nalu_solve_info* info) {

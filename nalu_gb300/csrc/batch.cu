@@ -18,9 +18,12 @@
 //            the last tile of a problem writes beta_p, and marks the problem
 //            done when its recursive residual is below its stop value
 // Tiles of finished problems return at once, so the work shrinks as problems
-// converge.  A chunk of iterations is captured into a CUDA graph; the host
-// reads the done flags between chunks and ends the solve with the true FP64
-// residual of every problem.
+// converge.  With the learned preconditioner every problem runs flexible CG
+// (a fourth kernel applies the learned stencil, z = M r, and the last tile
+// forms beta from z . q_old); a problem whose step turns non-positive
+// continues with Jacobi-CG after the next restart.  A chunk of iterations is
+// captured into a CUDA graph; the host reads the done flags between chunks and
+// ends the solve with the true FP64 residual of every problem.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -64,8 +67,15 @@ struct TileArgs {
   double* rz;           // [P]
   double* rr;           // [P]
   const double* stop2;  // [P]
-  int* done;            // [P] 0 active, 1 converged, 2 breakdown
-  int* iters;           // [P]
+  int* done;            // [P] 0 active, 1 converged, 2 breakdown, 3 learned step not positive
+  int* iters;           // [P] iterations in total
+  // learned flexible CG (mode 1): z = M r with the learned stencil values
+  const float* wsell;   // preconditioner values on the SELL pattern (or null)
+  double* z;            // [n]
+  const int* mode;      // [P] 0 Jacobi-CG, 1 learned FCG
+  double* pq;           // [P] p.Ap of the previous iteration
+  int* kiter;           // [P] iterations since the last restart
+  int* liters;          // [P] iterations in learned mode
 };
 
 // The last tile of problem pr to arrive returns true (after a fence), with
@@ -95,6 +105,34 @@ __device__ bool problem_reduce(const TileArgs& a, int t, int pr, const double (&
   return true;
 }
 
+// learned problems: z = M r (FP32 stencil values); beta = -(z . q_old) / (p . q)_old
+__global__ void __launch_bounds__(kBT) k_bt_prec(TileArgs a) {
+  __shared__ double sh[33];
+  const int t = blockIdx.x;
+  const int pr = a.tile_prob[t];
+  if (a.done[pr] || a.mode[pr] != 1) return;
+  const int i = threadIdx.x;
+  double dot = 0.0;
+  if (i < a.tile_rows[t]) {
+    const int64_t row = a.tile_row0[t] + i;
+    const int64_t sl = row / kSliceB;
+    const int64_t base = __ldg(a.sptr + sl) + (row % kSliceB);
+    const int len = __ldg(a.slen + sl);
+    float acc = 0.0f;
+    for (int k = 0; k < len; ++k) {
+      const int64_t e = base + (int64_t)k * kSliceB;
+      acc = fmaf(__ldg(a.wsell + e), narrow_f(__ldg(a.r + __ldg(a.scol + e))), acc);
+    }
+    const double zi = widen_f(acc);
+    a.z[row] = zi;
+    dot = zi * a.q[row];
+  }
+  const double v[1] = {dot};
+  double tot[1];
+  if (problem_reduce<1>(a, t, pr, v, tot, sh) && threadIdx.x == 0)
+    a.beta[pr] = a.kiter[pr] == 0 ? 0.0 : -tot[0] / a.pq[pr];
+}
+
 __global__ void __launch_bounds__(kBT) k_bt_pupdate(TileArgs a) {
   const int t = blockIdx.x;
   const int pr = a.tile_prob[t];
@@ -103,7 +141,9 @@ __global__ void __launch_bounds__(kBT) k_bt_pupdate(TileArgs a) {
   if (i >= a.tile_rows[t]) return;
   const int64_t row = a.tile_row0[t] + i;
   const float2 beta = split_df(a.beta[pr]);
-  const float2 z = fma_df(split_df(a.r[row]), make_float2(a.dinvf[row], 0.0f), make_float2(0.0f, 0.0f));
+  const float2 z = a.mode[pr] == 1 ? split_df(a.z[row])
+                                   : fma_df(split_df(a.r[row]), make_float2(a.dinvf[row], 0.0f),
+                                            make_float2(0.0f, 0.0f));
   a.p[row] = fma_df(beta, a.p[row], z);
 }
 
@@ -113,17 +153,31 @@ __global__ void __launch_bounds__(kBT) k_bt_spmv(TileArgs a) {
   const int pr = a.tile_prob[t];
   if (a.done[pr]) return;
   const int i = threadIdx.x;
-  double dot = 0.0;
+  double dot = 0.0, dpr = 0.0;
   if (i < a.tile_rows[t]) {
     const int64_t row = a.tile_row0[t] + i;
     const int64_t s = row / kSliceB;
     const double qi = sell_row_df(__ldg(a.sptr + s) + (row % kSliceB), __ldg(a.slen + s), a.scol, a.sval, a.p);
     a.q[row] = qi;
-    dot = join_df(a.p[row]) * qi;
+    const double pi = join_df(a.p[row]);
+    dot = pi * qi;
+    dpr = pi * a.r[row];
   }
-  const double v[1] = {dot};
-  double tot[1];
-  if (problem_reduce<1>(a, t, pr, v, tot, sh) && threadIdx.x == 0) a.alpha[pr] = a.rz[pr] / tot[0];
+  const double v[2] = {dot, dpr};
+  double tot[2];
+  if (problem_reduce<2>(a, t, pr, v, tot, sh) && threadIdx.x == 0) {
+    if (a.mode[pr] == 1) {  // flexible CG: alpha = (p . r) / (p . A p)
+      const double al = tot[1] / tot[0];
+      a.pq[pr] = tot[0];
+      a.alpha[pr] = al;
+      if (!(al > 0.0)) {  // the preconditioner is not positive on this residual
+        a.alpha[pr] = 0.0;
+        a.done[pr] = 3;
+      }
+    } else {
+      a.alpha[pr] = a.rz[pr] / tot[0];
+    }
+  }
 }
 
 __global__ void __launch_bounds__(kBT) k_bt_axpy(TileArgs a) {
@@ -146,11 +200,16 @@ __global__ void __launch_bounds__(kBT) k_bt_axpy(TileArgs a) {
   const double v[2] = {join_df(make_float2(zh, zl)), join_df(make_float2(rh, rl))};
   double tot[2];
   if (problem_reduce<2>(a, t, pr, v, tot, sh) && threadIdx.x == 0) {
-    const double be = tot[0] / a.rz[pr];
-    a.beta[pr] = be;
-    a.rz[pr] = tot[0];
+    const bool learned = a.mode[pr] == 1;
+    const double be = learned ? 0.0 : tot[0] / a.rz[pr];
+    if (!learned) {
+      a.beta[pr] = be;
+      a.rz[pr] = tot[0];
+    }
     a.rr[pr] = tot[1];
     a.iters[pr] += 1;
+    a.kiter[pr] += 1;
+    if (learned) a.liters[pr] += 1;
     if (!isfinite(tot[1]) || !isfinite(be)) a.done[pr] = 2;
     else if (tot[1] <= a.stop2[pr]) a.done[pr] = 1;
   }
@@ -181,6 +240,7 @@ __global__ void __launch_bounds__(kBT) k_batch_resid(TileArgs a, const int64_t* 
     const double ri = b[row] - s;
     a.r[row] = ri;
     a.p[row] = make_float2(0.0f, 0.0f);
+    a.q[row] = 0.0;
     rz += ri * (widen_f(a.dinvf[row]) * ri);
     rr += ri * ri;
     bb += b[row] * b[row];
@@ -242,14 +302,25 @@ int solve_batched(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* inf
   const float2* sv2 = nullptr;
   if ((rc = sell_build<float2>(ctx, s.sell, &sv2))) return rc;
   DBuf<int64_t> d_trow0;
-  DBuf<int32_t> d_ints;  // trows | tprob | pt0 | pt1 | done | iters
+  const bool learned = o.precond == NALU_PRECOND_LEARNED;
+  if (learned && (o.method != NALU_SOLVER_CG || o.precision != NALU_PRECISION_FP64))
+    return set_error(ctx, NALU_ERR_ARG, "the learned preconditioner runs in FP64 flexible CG only");
+  double setup_s = 0.0;
+  if (learned) {
+    const auto ts = std::chrono::steady_clock::now();
+    if ((rc = learned_prepare(ctx))) return rc;
+    setup_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - ts).count();
+  }
+  DBuf<int32_t> d_ints;  // trows | tprob | pt0 | pt1 | done | iters | mode | kiter | liters
   DBuf<double> d_dbl;    // tpart[2 ntiles] | tb[ntiles] | alpha beta rz rr stop2 [P] | sums [3P]
   DBuf<unsigned> d_cnt;
   DBuf<float> dinvf;
   DBuf<float2> p2;
   NALU_CUDA(ctx, d_trow0.alloc(ntiles));
-  NALU_CUDA(ctx, d_ints.alloc(2 * (int64_t)ntiles + 4 * (int64_t)P));
-  NALU_CUDA(ctx, d_dbl.alloc(3 * (int64_t)ntiles + 8 * (int64_t)P));
+  NALU_CUDA(ctx, d_ints.alloc(2 * (int64_t)ntiles + 7 * (int64_t)P));
+  NALU_CUDA(ctx, d_dbl.alloc(3 * (int64_t)ntiles + 9 * (int64_t)P));
+  DBuf<double> zbuf;
+  if (learned) NALU_CUDA(ctx, zbuf.alloc(n));
   NALU_CUDA(ctx, d_cnt.alloc(P));
   NALU_CUDA(ctx, dinvf.alloc(n));
   NALU_CUDA(ctx, p2.alloc(n));
@@ -261,6 +332,9 @@ int solve_batched(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* inf
   int32_t* pt1_d = pt0_d + P;
   int32_t* done_d = pt1_d + P;
   int32_t* iters_d = done_d + P;
+  int32_t* mode_d = iters_d + P;
+  int32_t* kiter_d = mode_d + P;
+  int32_t* liters_d = kiter_d + P;
   double* tpart = d_dbl.p;
   double* tb = tpart + 2 * (int64_t)ntiles;
   double* alpha_d = tb + ntiles;
@@ -269,6 +343,7 @@ int solve_batched(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* inf
   double* rr_d = rz_d + P;
   double* stop2_d = rr_d + P;
   double* sums_d = stop2_d + P;  // [3][P]
+  double* pq_d = sums_d + 3 * P;
   cudaStream_t st = ctx->stream;
   NALU_CUDA(ctx, cudaMemcpyAsync(d_trow0.p, trow0.data(), sizeof(int64_t) * ntiles, cudaMemcpyHostToDevice, st));
   NALU_CUDA(ctx, cudaMemcpyAsync(trows_d, trows.data(), sizeof(int32_t) * ntiles, cudaMemcpyHostToDevice, st));
@@ -276,6 +351,8 @@ int solve_batched(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* inf
   NALU_CUDA(ctx, cudaMemcpyAsync(pt0_d, pt0.data(), sizeof(int32_t) * P, cudaMemcpyHostToDevice, st));
   NALU_CUDA(ctx, cudaMemcpyAsync(pt1_d, pt1.data(), sizeof(int32_t) * P, cudaMemcpyHostToDevice, st));
   NALU_CUDA(ctx, cudaMemsetAsync(iters_d, 0, sizeof(int32_t) * P, st));
+  NALU_CUDA(ctx, cudaMemsetAsync(liters_d, 0, sizeof(int32_t) * P, st));
+  std::vector<int32_t> mode(P, learned ? 1 : 0), fallback(P, 0);
   NALU_CUDA(ctx, cudaMemsetAsync(d_cnt.p, 0, sizeof(unsigned) * P, st));
   k_to_float<<<1024, 256, 0, st>>>(n, s.dinv.p, dinvf.p);
   k_batch_prep<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, ctx->d_bcmask.p, ctx->d_rhs.p, ctx->d_x.p,
@@ -309,6 +386,12 @@ int solve_batched(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* inf
   a.stop2 = stop2_d;
   a.done = done_d;
   a.iters = iters_d;
+  a.wsell = learned ? ctx->learned.wsell.p : nullptr;
+  a.z = zbuf.p;
+  a.mode = mode_d;
+  a.pq = pq_d;
+  a.kiter = kiter_d;
+  a.liters = liters_d;
 
   const int chunk = o.check_every > 0 ? o.check_every : 25;
   cudaGraph_t graph = nullptr;
@@ -316,6 +399,7 @@ int solve_batched(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* inf
   cudaError_t ce = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
   if (ce != cudaSuccess) return cuda_check(ctx, ce, "begin capture");
   for (int k = 0; k < chunk; ++k) {
+    if (learned) k_bt_prec<<<ntiles, kBT, 0, st>>>(a);
     k_bt_pupdate<<<ntiles, kBT, 0, st>>>(a);
     k_bt_spmv<<<ntiles, kBT, 0, st>>>(a);
     k_bt_axpy<<<ntiles, kBT, 0, st>>>(a);
@@ -330,9 +414,12 @@ int solve_batched(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* inf
 
   std::vector<double> sums(3 * P);
   std::vector<int32_t> done(P), iters(P);
-  std::vector<double> true_res(P, 0.0);
-  for (int outer = 0; outer < 6; ++outer) {
-    // true residual r = b - A x (FP64), the Jacobi r.z and ||b|| per problem
+  std::vector<double> true_res(P, 0.0), r0(P, 0.0);
+  const int window = o.stall_window > 0 ? o.stall_window : 20;
+  // one round: true residual r = b - A x (FP64), Jacobi r.z and ||b|| per
+  // problem, then the per-problem start of CG; returns true when every
+  // problem already meets the tolerance
+  auto start_round = [&](bool apply_breakdowns) -> int {
     k_batch_resid<<<ntiles, kBT, 0, st>>>(a, ctx->d_rowptr.p, ctx->d_colind.p, ctx->d_values.p, ctx->d_rhs.p, tb);
     k_batch_sums<<<std::min(P, 1024), kBT, 0, st>>>(tpart, tpart + ntiles, tb, pt0_d, pt1_d, P, sums_d);
     ctx->launches += 2;
@@ -343,27 +430,114 @@ int solve_batched(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* inf
     for (int pr = 0; pr < P; ++pr) {
       const double bnorm = std::sqrt(sums[2 * P + pr]);
       const double bref = bnorm > 0 ? bnorm : 1.0;
-      true_res[pr] = std::sqrt(sums[P + pr]) / bref;
+      r0[pr] = std::sqrt(sums[P + pr]);
+      true_res[pr] = r0[pr] / bref;
+      if (apply_breakdowns && done[pr] == 3) {  // learned FCG stopped: Jacobi-CG from here
+        mode[pr] = 0;
+        fallback[pr] = 2;
+      }
       done[pr] = true_res[pr] <= o.tol ? 1 : 0;
       all = all && done[pr];
       stop2[pr] = std::pow(0.5 * o.tol * bref, 2);
       rz0[pr] = sums[pr];
     }
-    if (all) break;
+    if (all) return 1;
     NALU_CUDA(ctx, cudaMemcpyAsync(stop2_d, stop2.data(), sizeof(double) * P, cudaMemcpyHostToDevice, st));
     NALU_CUDA(ctx, cudaMemcpyAsync(rz_d, rz0.data(), sizeof(double) * P, cudaMemcpyHostToDevice, st));
     NALU_CUDA(ctx, cudaMemcpyAsync(done_d, done.data(), sizeof(int32_t) * P, cudaMemcpyHostToDevice, st));
     NALU_CUDA(ctx, cudaMemsetAsync(beta_d, 0, sizeof(double) * P, st));
-    // CG on the current residual; x is updated in place
-    for (int it = 0; it < o.max_iters; it += chunk) {
+    NALU_CUDA(ctx, cudaMemsetAsync(kiter_d, 0, sizeof(int32_t) * P, st));
+    NALU_CUDA(ctx, cudaMemcpyAsync(mode_d, mode.data(), sizeof(int32_t) * P, cudaMemcpyHostToDevice, st));
+    return 0;
+  };
+  // CG on the current residual for at most max_its iterations; x is updated in
+  // place.  A learned problem whose residual norm has no new minimum for
+  // max(stall_window, 4 x the age of its minimum) iterations stops and
+  // continues with Jacobi-CG after the restart (the single-system rule).
+  std::vector<double> rrh(P);
+  std::vector<int> pace(P, 0);  // learned problems: iteration budget from the Jacobi probe (0: none)
+  auto run_chunks = [&](int max_its, bool stall_test) -> int {
+    std::vector<double> best(P, INFINITY);
+    std::vector<int> best_it(P, 0);
+    for (int it = 0; it < max_its; it += chunk) {
       cudaGraphLaunch(exec, st);
-      ctx->launches += 3 * chunk;
+      ctx->launches += (learned ? 4 : 3) * chunk;
       NALU_CUDA(ctx, cudaMemcpyAsync(done.data(), done_d, sizeof(int32_t) * P, cudaMemcpyDeviceToHost, st));
+      NALU_CUDA(ctx, cudaMemcpyAsync(rrh.data(), rr_d, sizeof(double) * P, cudaMemcpyDeviceToHost, st));
+      NALU_CUDA(ctx, cudaStreamSynchronize(st));
+      const int now = it + chunk;
+      for (int pr = 0; pr < P && stall_test; ++pr) {
+        if (done[pr] != 0 || mode[pr] != 1) continue;
+        const double res = std::sqrt(rrh[pr]);
+        bool stop = pace[pr] > 0 && now > pace[pr];  // behind Jacobi-CG's pace
+        if (res < 0.999 * best[pr]) {
+          best[pr] = res;
+          best_it[pr] = now;
+        } else if (now - best_it[pr] > std::max(window, 10 * best_it[pr])) {
+          stop = true;
+        }
+        if (stop) {
+          done[pr] = 3;
+          NALU_CUDA(ctx, cudaMemcpyAsync(done_d + pr, &done[pr], sizeof(int32_t), cudaMemcpyHostToDevice, st));
+        }
+      }
       NALU_CUDA(ctx, cudaStreamSynchronize(st));
       if (std::all_of(done.begin(), done.end(), [](int d) { return d != 0; })) break;
     }
+    return NALU_OK;
+  };
+
+  if (learned && o.learned_probe) {
+    // probe: a short run of Jacobi-CG and of the learned FCG from the same
+    // start; each problem keeps the method that reduced its residual faster
+    // per unit of device time (the batch's time per iteration of each method)
+    DBuf<double> x0;
+    NALU_CUDA(ctx, x0.alloc(n));
+    NALU_CUDA(ctx, cudaMemcpyAsync(x0.p, ctx->d_x.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+    const int probe = chunk * std::max(1, (std::max(40, 2 * window) + chunk - 1) / chunk);
+    std::vector<double> res[2];
+    float ms[2] = {0.f, 0.f};
+    cudaEvent_t pe[2];
+    for (auto& e : pe) NALU_CUDA(ctx, cudaEventCreate(&e));
+    bool trivial = false;
+    for (int m = 0; m < 2 && !trivial; ++m) {
+      std::fill(mode.begin(), mode.end(), m);
+      NALU_CUDA(ctx, cudaMemcpyAsync(ctx->d_x.p, x0.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+      if (start_round(false)) {
+        trivial = true;
+        break;
+      }
+      NALU_CUDA(ctx, cudaEventRecord(pe[0], st));
+      int rcp = run_chunks(probe, false);
+      if (rcp) return rcp;
+      NALU_CUDA(ctx, cudaEventRecord(pe[1], st));
+      NALU_CUDA(ctx, cudaEventSynchronize(pe[1]));
+      cudaEventElapsedTime(&ms[m], pe[0], pe[1]);
+      res[m].resize(P);
+      for (int pr = 0; pr < P; ++pr)
+        res[m][pr] = done[pr] == 3 ? INFINITY : std::sqrt(std::max(rrh[pr], 0.0));
+    }
+    for (auto& e : pe) cudaEventDestroy(e);
+    for (int pr = 0; pr < P && !trivial; ++pr) {
+      const double lj = std::log(std::max(res[0][pr], 1e-300) / std::max(r0[pr], 1e-300));
+      const double rj = lj / std::max(ms[0], 1e-3f);
+      const double rl = std::log(std::max(res[1][pr], 1e-300) / std::max(r0[pr], 1e-300)) / std::max(ms[1], 1e-3f);
+      mode[pr] = rl < rj ? 1 : 0;
+      if (!mode[pr]) fallback[pr] = 2;
+      // iterations Jacobi-CG would need (probe rate extrapolated); the learned
+      // FCG gets at most twice as many before the problem changes to Jacobi-CG
+      if (lj < 0.0) pace[pr] = (int)std::min(2.0 * probe * std::log(0.5 * o.tol) / lj + probe, 2.0e9);
+    }
+    NALU_CUDA(ctx, cudaMemcpyAsync(ctx->d_x.p, x0.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+  }
+  for (int outer = 0; outer < 6; ++outer) {
+    if (start_round(outer > 0)) break;
+    int rcr = run_chunks(o.max_iters, learned);
+    if (rcr) return rcr;
     if (std::any_of(done.begin(), done.end(), [](int d) { return d == 2; })) break;
   }
+  std::vector<int32_t> liters(P, 0);
+  NALU_CUDA(ctx, cudaMemcpyAsync(liters.data(), liters_d, sizeof(int32_t) * P, cudaMemcpyDeviceToHost, st));
   cudaGraphExecDestroy(exec);
   cudaGraphDestroy(graph);
   NALU_CUDA(ctx, cudaMemcpyAsync(iters.data(), iters_d, sizeof(int32_t) * P, cudaMemcpyDeviceToHost, st));
@@ -375,9 +549,9 @@ int solve_batched(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* inf
     infos[pr].outer_iterations = 1;
     infos[pr].true_rel_res = true_res[pr];
     infos[pr].seconds = secs;
-    infos[pr].fallback = 0;
-    infos[pr].learned_iterations = 0;
-    infos[pr].setup_seconds = 0.0;
+    infos[pr].fallback = fallback[pr];
+    infos[pr].learned_iterations = liters[pr];
+    infos[pr].setup_seconds = setup_s;
     infos[pr].status = true_res[pr] <= o.tol ? NALU_OK : (done[pr] == 2 ? NALU_ERR_NONFINITE : NALU_ERR_NOT_CONVERGED);
     all_ok = all_ok && infos[pr].status == NALU_OK;
   }

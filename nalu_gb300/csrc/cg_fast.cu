@@ -391,7 +391,7 @@ unsigned wave_grid(nalu_ctx* ctx, const void* kernel, int threads) {
 // FP64 Jacobi-CG on A x = r (x from 0) with the df64 SpMV on S.val2;
 // r holds the initial residual; on return x holds the solution increment.
 int pcg_df(nalu_ctx* ctx, const SellMatrix& S, double* x, double* r, double* z, double* q, const double* dinv,
-           double rtol, double r0norm, int max_it, int check_every, int* iters_out) {
+           double rtol, double r0norm, int max_it, int check_every, int* iters_out, float* iter_ms) {
   const int64_t n = ctx->n_rows;
   const int64_t npad = S.nslices * kSlice;
   SolverWork& w = ctx->sw;
@@ -441,6 +441,12 @@ int pcg_df(nalu_ctx* ctx, const SellMatrix& S, double* x, double* r, double* z, 
   double rr = 0.0;
   int it = 1;
   bool bad = false, conv = false;
+  cudaEvent_t t_ev[2] = {nullptr, nullptr};
+  if (iter_ms) {
+    cudaEventCreate(&t_ev[0]);
+    cudaEventCreate(&t_ev[1]);
+    cudaEventRecord(t_ev[0], st);
+  }
   for (;;) {
     NALU_CUDA(ctx, cudaMemcpyAsync(&rr, cs + CS_RR, sizeof(double), cudaMemcpyDeviceToHost, st));
     NALU_CUDA(ctx, cudaStreamSynchronize(st));
@@ -455,6 +461,13 @@ int pcg_df(nalu_ctx* ctx, const SellMatrix& S, double* x, double* r, double* z, 
     if (it >= max_it) break;
     cudaGraphLaunch(exec, st);
     it += chunk;
+  }
+  if (iter_ms) {
+    cudaEventRecord(t_ev[1], st);
+    cudaEventSynchronize(t_ev[1]);
+    cudaEventElapsedTime(iter_ms, t_ev[0], t_ev[1]);
+    cudaEventDestroy(t_ev[0]);
+    cudaEventDestroy(t_ev[1]);
   }
   cudaGraphExecDestroy(exec);
   cudaGraphDestroy(graph);

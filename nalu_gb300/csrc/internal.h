@@ -197,10 +197,11 @@ int learned_prepare(nalu_ctx* ctx);  // slot map, stencil and SELL preconditione
 // NALU_ERR_NOT_CONVERGED with *stalled = 1 when the residual made no progress
 // for `stall_window` iterations
 int fcg_learned(nalu_ctx* ctx, double* x, double* r, double rtol, double r0norm, int max_it, int check_every,
-                int stall_window, int* iters_out, int* stalled);
+                int stall_window, int* iters_out, int* stalled, float* iter_ms = nullptr);
 unsigned wave_grid(nalu_ctx* ctx, const void* kernel, int threads);  // cg_fast.cu
+// *iter_ms (optional): device time of the iterations alone (set-up excluded)
 int pcg_df(nalu_ctx* ctx, const SellMatrix& S, double* x, double* r, double* z, double* q, const double* dinv,
-           double rtol, double r0norm, int max_it, int check_every, int* iters_out);
+           double rtol, double r0norm, int max_it, int check_every, int* iters_out, float* iter_ms = nullptr);
 template <class T, class VT>
 int pcg_fast(nalu_ctx* ctx, const VT* sval, const SellMatrix& S, T* x, T* r, T* z, T* p0, T* p1, T* q,
              const T* dinv, double rtol, double r0norm, int max_it, int check_every, int* iters_out);

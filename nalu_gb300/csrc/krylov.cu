@@ -432,6 +432,15 @@ double read_scalar(nalu_ctx* ctx, double* d) {
 }
 
 // true residual r = b - A x into sw.r, returns ||r||_2
+// ||v|| (FP64, fixed-order reduction)
+double vec_norm(nalu_ctx* ctx, const double* v) {
+  const int64_t n = ctx->n_rows;
+  k_multi_dot<double><<<grid_for(n, kRedThreads), kRedThreads, 0, ctx->stream>>>(n, 1, v, v, ctx->sw.partial.p);
+  k_finish<<<1, 256, 0, ctx->stream>>>(ctx->sw.partial.p, grid_for(n, kRedThreads), 1, ctx->sw.scal.p, S_TMP);
+  ctx->launches += 2;
+  return std::sqrt(read_scalar(ctx, ctx->sw.scal.p + S_TMP));
+}
+
 double true_residual(nalu_ctx* ctx, const double* x, double* r) {
   const int64_t n = ctx->n_rows;
   k_residual<<<kRedBlocks, 256, 0, ctx->stream>>>(n, ctx->d_rowptr.p, ctx->d_colind.p, ctx->d_values.p, x,
@@ -705,8 +714,8 @@ int solve(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* info) {
   const bool learned = o.precond == NALU_PRECOND_LEARNED;
   if (learned && (o.method != NALU_SOLVER_CG || mixed))
     return set_error(ctx, NALU_ERR_ARG, "the learned preconditioner runs in FP64 flexible CG only");
-  bool fallback = false;
-  int learned_its = 0;
+  bool fallback = false, probe_chose_jacobi = false;
+  int learned_its = 0, probe_its = 0, pace_its = 0;
   double setup_s = 0.0;
   nalu_solver_opts fb = o;  // Chebyshev-Jacobi PCG after a stall of the learned FCG
   fb.precond = NALU_PRECOND_CHEBYSHEV;
@@ -732,15 +741,59 @@ int solve(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* info) {
         if (outer == 1 && ((rc = sell_build<float2>(ctx, s.sell, &sv2)) || (rc = learned_prepare(ctx)))) return rc;
         NALU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         setup_s += std::chrono::duration<double>(std::chrono::steady_clock::now() - ts).count();
-        int stalled = 0;
-        rc = fcg_learned(ctx, s.w.p, s.r.p, rtol, r0, o.max_iters - total_it, o.check_every,
-                         o.stall_window > 0 ? o.stall_window : 20, &its, &stalled);
-        learned_its += its;
-        if (stalled) {
-          fallback = true;
+        const int window = o.stall_window > 0 ? o.stall_window : 20;
+        bool use_jacobi = false;
+        if (outer == 1 && o.learned_probe) {
+          // probe: a short run of each method from the same start; keep the one
+          // that reduces the residual faster per unit of device time
+          const int probe = std::max(40, 2 * window);
+          cudaEvent_t pe[1];
+          for (auto& e : pe) NALU_CUDA(ctx, cudaEventCreate(&e));
+          int itj = 0, itl = 0, stl = 0;
+          float msj = 0.f, msl = 0.f;  // device time of the iterations (set-up excluded)
+          rc = pcg_df(ctx, s.sell, s.w.p, s.r.p, s.z.p, s.q.p, s.dinv.p, rtol, r0, probe, 10, &itj, &msj);
+          const double resj = vec_norm(ctx, s.r.p);
+          cudaMemcpyAsync(s.r.p, s.tmp.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->stream);
+          const int rcl = fcg_learned(ctx, s.w.p, s.r.p, rtol, r0, probe, 10, 1 << 30, &itl, &stl, &msl);
+          const double resl = vec_norm(ctx, s.r.p);
+          for (auto& e : pe) cudaEventDestroy(e);
+          // residual reduction per millisecond of iterations
+          const double tj = itj * (double)msj / std::max(1, itj - 1), tl = itl * (double)msl / std::max(1, itl - 1);
+          const double ratej = std::log(std::max(resj, 1e-300) / r0) / std::max(tj, 1e-3);
+          const double ratel = std::log(std::max(resl, 1e-300) / r0) / std::max(tl, 1e-3);
+          use_jacobi = stl || (rcl != NALU_OK && rcl != NALU_ERR_NOT_CONVERGED) || !(ratel < ratej);
+          // pace: Jacobi-CG's probe rate, extrapolated, gives the iterations it
+          // would need; the learned FCG gets at most twice as many
+          if (resj < r0 && resj > 0.0) {
+            const double need = itj * std::log(std::max(rtol, 1e-300)) / std::log(resj / r0);
+            pace_its = (int)std::min(2.0 * need + probe, 2.0e9);
+          }
+          probe_its = itj + itl;
+          learned_its += itl;
           rc = NALU_OK;
+          cudaMemcpyAsync(s.r.p, s.tmp.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->stream);
         }
-      } else if (o.method == NALU_SOLVER_CG && o.precond == NALU_PRECOND_JACOBI) {
+        if (use_jacobi) {
+          probe_chose_jacobi = true;
+          fallback = true;  // the rest of the solve runs Jacobi-CG
+          rc = pcg_df(ctx, s.sell, s.w.p, s.r.p, s.z.p, s.q.p, s.dinv.p, rtol, r0, o.max_iters - total_it,
+                      o.check_every, &its);
+        } else {
+          int stalled = 0;
+          const int room = o.max_iters - total_it;
+          const int budget = pace_its > 0 ? std::min(room, pace_its) : room;
+          rc = fcg_learned(ctx, s.w.p, s.r.p, rtol, r0, budget, o.check_every, window, &its, &stalled);
+          learned_its += its;
+          if (stalled) {
+            fallback = true;  // Chebyshev-Jacobi PCG from here
+            rc = NALU_OK;
+          } else if (rc == NALU_ERR_NOT_CONVERGED && budget < room) {
+            probe_chose_jacobi = true;  // behind Jacobi-CG's pace: Jacobi-CG from the current iterate
+            fallback = true;
+            rc = NALU_OK;
+          }
+        }
+      } else if (o.method == NALU_SOLVER_CG && (o.precond == NALU_PRECOND_JACOBI || probe_chose_jacobi)) {
         // two-kernel Jacobi-CG on the SELL-32 copy (cg_fast.cu)
         const double* sv = nullptr;
         const float2* sv2 = nullptr;
@@ -793,9 +846,9 @@ int solve(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* info) {
     if (rc == NALU_ERR_NOT_CONVERGED) break;
   }
   NALU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  info->iterations = total_it;
+  info->iterations = total_it + probe_its;
   info->outer_iterations = outer;
-  info->fallback = fallback ? 1 : 0;
+  info->fallback = probe_chose_jacobi ? 2 : (fallback ? 1 : 0);
   info->learned_iterations = learned_its;
   info->setup_seconds = setup_s;
   info->true_rel_res = res;

@@ -373,12 +373,13 @@ __global__ void k_precond_sell(int64_t n, const int64_t* __restrict__ rp, const 
 }
 
 // SPD safeguard (Gershgorin on D^1/2 M D^1/2): with d = a_ii, row i's
-// scaled diagonal is d_i M_ii and its scaled off-diagonal mass
+// scaled diagonal is d_i M_ii (floored at 1/4) and its scaled off-diagonal mass
 // sum_j |M_ij| sqrt(d_i d_j).  s_i = min(1, theta diag / offdiag); every
 // off-diagonal is then multiplied by min(s_i, s_j), which keeps M symmetric
 // and makes every scaled row diagonally dominant, hence M positive definite.
 // A row with a non-positive diagonal falls back to its Jacobi entry.
 constexpr float kSpdTheta = 0.95f;
+constexpr float kSpdDiagFloor = 0.25f;
 
 __global__ void k_precond_rowscale(int64_t n, const int64_t* __restrict__ sptr, const int32_t* __restrict__ slen,
                                    const int32_t* __restrict__ scol, float* __restrict__ w,
@@ -403,12 +404,19 @@ __global__ void k_precond_rowscale(int64_t n, const int64_t* __restrict__ sptr, 
       off += fabsf(val) * rsqrtf(di * (float)dinv[col]);
     }
   }
+  // the scaled diagonal (M_ii a_ii, 1 for Jacobi) is kept at or above
+  // kSpdDiagFloor, so Gershgorin bounds the smallest eigenvalue of
+  // D^1/2 M D^1/2 below by (1 - theta) kSpdDiagFloor
   float sc = 1.0f;
   if (!(diag > 0.0f)) {
     sc = 0.0f;
     if (dpos >= 0) w[dpos] = di;
-  } else if (off > kSpdTheta * diag) {
-    sc = kSpdTheta * diag / off;
+  } else {
+    if (diag < kSpdDiagFloor) {
+      diag = kSpdDiagFloor;
+      if (dpos >= 0) w[dpos] = kSpdDiagFloor * di;
+    }
+    if (off > kSpdTheta * diag) sc = kSpdTheta * diag / off;
   }
   srow[row] = sc;
 }
@@ -433,21 +441,6 @@ __global__ void k_precond_apply_scale(int64_t n, const int64_t* __restrict__ spt
 //   z = M r;  beta = -(z . q_old) / (p_old . q_old);  p = z + beta p
 //   q = A p;  alpha = (p . r) / (p . q);  x += alpha p;  r -= alpha q
 // ---------------------------------------------------------------------------
-// double -> float by truncating the significand (integer instructions only;
-// the FP64 pipe is the scarce one on GB300).  |d| < 2^-126 gives 0.
-__device__ __forceinline__ float d2f_trunc(double d) {
-  const uint64_t b = (uint64_t)__double_as_longlong(d);
-  const int e = (int)((b >> 52) & 0x7ff) - 1023;
-  if (e < -126) return 0.0f;
-  const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
-  if (e > 127) return __uint_as_float(sign | 0x7f800000u | (e == 1024 && (b & 0xFFFFFFFFFFFFFull) ? 0x400000u : 0u));
-  return __uint_as_float(sign | ((uint32_t)(e + 127) << 23) | (uint32_t)((b >> 29) & 0x7fffffu));
-}
-
-// scalars: fs[FS_BETA], fs[FS_ALPHA], fs[FS_PQ] (p . A p), fs[FS_RR] (r . r)
-enum { FS_BETA = 0, FS_ALPHA = 1, FS_PQ = 2, FS_RR = 3 };
-
-// z = M r (FP32 stencil values, FP32 residual); beta = -(z . q_old) / (p . q)_old by the last block
 __global__ void __launch_bounds__(kFcgThreads) k_fcg_prec(int64_t n, int64_t npad, const int64_t* __restrict__ sptr,
                                                           const int32_t* __restrict__ slen,
                                                           const int32_t* __restrict__ scol,
@@ -477,7 +470,7 @@ __global__ void __launch_bounds__(kFcgThreads) k_fcg_prec(int64_t n, int64_t npa
 #pragma unroll
       for (int u = 0; u < 8; ++u) b[u] = c[u] >= 0 ? __ldg(r + c[u]) : 0.0;
 #pragma unroll
-      for (int u = 0; u < 8; ++u) acc = fmaf(a[u], d2f_trunc(b[u]), acc);
+      for (int u = 0; u < 8; ++u) acc = fmaf(a[u], narrow_f(b[u]), acc);
     }
     const double zi = widen_f(acc);
     z[row] = zi;
@@ -873,7 +866,7 @@ int learned_prepare(nalu_ctx* ctx) {
 }
 
 int fcg_learned(nalu_ctx* ctx, double* x, double* r, double rtol, double r0norm, int max_it, int check_every,
-                int stall_window, int* iters_out, int* stalled) {
+                int stall_window, int* iters_out, int* stalled, float* iter_ms) {
   const int64_t n = ctx->n_rows;
   SolverWork& s = ctx->sw;
   const SellMatrix& S = s.sell;
@@ -927,6 +920,12 @@ int fcg_learned(nalu_ctx* ctx, double* x, double* r, double rtol, double r0norm,
   double last = INFINITY, best = INFINITY;
   int it = 1, best_it = 0, hnonpos = 0;
   bool bad = false, conv = false;
+  cudaEvent_t t_ev[2] = {nullptr, nullptr};
+  if (iter_ms) {
+    cudaEventCreate(&t_ev[0]);
+    cudaEventCreate(&t_ev[1]);
+    cudaEventRecord(t_ev[0], st);
+  }
   for (;;) {
     double rr = 0.0;
     cudaMemcpyAsync(&rr, fs + FS_RR, sizeof(double), cudaMemcpyDeviceToHost, st);
@@ -944,17 +943,24 @@ int fcg_learned(nalu_ctx* ctx, double* x, double* r, double rtol, double r0norm,
     if (res < 0.999 * best) {
       best = res;
       best_it = it;
-    } else if (it - best_it > std::max(stall_window, 4 * best_it)) {
+    } else if (it - best_it > std::max(stall_window, 10 * best_it)) {
       // CG residual norms rise and fall in humps whose length grows with the
-      // iteration count (measured up to about the age of the current minimum),
-      // so the window is at least four times the iterations the current
-      // minimum took to reach
+      // iteration count (measured beyond the age of the current minimum), so
+      // the window is at least ten times the iterations the current minimum
+      // took to reach
       *stalled = 1;
       break;
     }
     if (it >= max_it) break;
     cudaGraphLaunch(exec, st);
     it += chunk;
+  }
+  if (iter_ms) {
+    cudaEventRecord(t_ev[1], st);
+    cudaEventSynchronize(t_ev[1]);
+    cudaEventElapsedTime(iter_ms, t_ev[0], t_ev[1]);
+    cudaEventDestroy(t_ev[0]);
+    cudaEventDestroy(t_ev[1]);
   }
   cudaGraphExecDestroy(exec);
   cudaGraphDestroy(graph);

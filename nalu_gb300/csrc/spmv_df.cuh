@@ -29,6 +29,22 @@ __device__ __forceinline__ float2 split_df(double d) {
   return make_float2(s.hi, s.lo);
 }
 
+// double -> float by truncating the significand (integer instructions only;
+// the FP64 pipe is the scarce one on GB300).  |d| < 2^-126 gives 0.
+__device__ __forceinline__ float narrow_f(double d) {
+  const uint64_t b = (uint64_t)__double_as_longlong(d);
+  const int e = (int)((b >> 52) & 0x7ff) - 1023;
+  if (e < -126) return 0.0f;
+  const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
+  if (e > 127) return __uint_as_float(sign | 0x7f800000u | (e == 1024 && (b & 0xFFFFFFFFFFFFFull) ? 0x400000u : 0u));
+  return __uint_as_float(sign | ((uint32_t)(e + 127) << 23) | (uint32_t)((b >> 29) & 0x7fffffu));
+}
+
+// scalars: fs[FS_BETA], fs[FS_ALPHA], fs[FS_PQ] (p . A p), fs[FS_RR] (r . r)
+enum { FS_BETA = 0, FS_ALPHA = 1, FS_PQ = 2, FS_RR = 3 };
+
+// z = M r (FP32 stencil values, FP32 residual); beta = -(z . q_old) / (p . q)_old by the last block
+
 // exact widening of a float with integer ops only (float subnormals -> 0,
 // infinities and NaN kept)
 __device__ __forceinline__ double widen_f(float f) {

@@ -112,3 +112,28 @@ def test_set_problems_rejects_coupled_split(gpu_ctx_factory):
         ctx.set_problems([0, int(off[-1]) + 1])  # does not span the nodes
     ctx.set_problems(off)
     ctx.close()
+
+
+def test_batched_learned_fcg(gpu_ctx_factory, oracle):
+    """The learned preconditioner on a batch (weights trained on the union
+    system): an opening probe runs both methods briefly and each problem
+    keeps the faster one; every problem reaches the tolerance on its own rows
+    and agrees with the oracle."""
+    ctx, off, _ = _batched_continuity(gpu_ctx_factory, 5, (10, 18), seed=21)
+    rp, ci = ctx.graph()
+    v, b = ctx.system()
+    plain = ctx.solve_batched(ng.default_solver_opts(tol=1e-9, max_iters=5000))
+    ctx.learned_init(3)
+    st, rf, tg = ctx.learned_harvest(n_samples=20000, n_rhs=4, seed=4)
+    ctx.learned_train(st, rf, tg, epochs=30)
+    infos = ctx.solve_batched(ng.default_solver_opts(tol=1e-9, max_iters=5000, precond=ng.PRECOND_LEARNED))
+    x = ctx.solution()
+    for k, info in enumerate(infos):
+        r0, r1 = int(off[k]), int(off[k + 1])
+        brp, bci, bv, bb = _block(rp, ci, v, b, r0, r1)
+        res = np.linalg.norm(bb - oracle.spmv(brp, bci, bv, x[r0:r1])) / np.linalg.norm(bb)
+        assert info.status == 0 and res <= 1.05e-9, (k, info.status, res)
+        assert info.learned_iterations > 0 and info.fallback in (0, 2), (k, info.fallback)
+        xo, _, _ = oracle.pcg_jacobi(brp, bci, bv, bb, tol=1e-12, max_it=20000, n_threads=4)
+        assert np.max(np.abs(x[r0:r1] - xo)) <= 1e-5 * np.max(np.abs(xo)), k
+    ctx.close()
