@@ -25,11 +25,14 @@
 namespace nalu_gb300 {
 namespace {
 
-// shared-memory layout per element in df64 words: MomLayout, then the edge form
+// shared-memory layout per element in df64 words: MomLayout, then the edge
+// form, padded so that the element stride (2 SIZE 32-bit words) is 2 mod 32:
+// equal offsets of the 16 elements of a block fall in different banks
 struct MomLayoutDF {
   static constexpr int EF = MomLayout::SIZE;  // [k][i][A,B,C,D]
-  static constexpr int SIZE = EF + 36;
+  static constexpr int SIZE = EF + 36 + 9;    // 721
 };
+static_assert((2 * MomLayoutDF::SIZE) % 32 == 2, "element stride");
 
 __device__ __forceinline__ float shape_f(int n, const float s[3]) {
   return (0.5f + (float)corner_sign(n, 0) * s[0]) * (0.5f + (float)corner_sign(n, 1) * s[1]) *
