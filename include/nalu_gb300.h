@@ -68,7 +68,8 @@ enum nalu_field {
   NALU_FIELD_VISCOSITY = 8,    /* [n]    */
   NALU_FIELD_DUDX = 9,         /* [n][3][3] Gju */
   NALU_FIELD_MDOT_SCS = 10,    /* element field [E][12] mass_flow_rate_scs */
-  NALU_FIELD_COUNT = 11
+  NALU_FIELD_DUAL_VOLUME = 11, /* [n]    dual_nodal_volume (nalu_compute_dual_volume) */
+  NALU_FIELD_COUNT = 12
 };
 /* copy a field in (host or device source, caller node order) */
 int nalu_field_set(nalu_ctx* ctx, int field, const double* src, int64_t count, int src_is_device);
@@ -162,6 +163,24 @@ int nalu_capture_element(nalu_ctx* ctx, int kernel, const nalu_assemble_opts* op
 /* ComputeMdotElemAlgorithm (src/ComputeMdotElemAlgorithm.C:85-250):
  * fills NALU_FIELD_MDOT_SCS from density, velocity_rtm, pressure, dpdx */
 int nalu_compute_mdot(nalu_ctx* ctx, const nalu_assemble_opts* opts);
+
+/* ---- nodal geometry and gradients --------------------------------------- */
+/* dual_nodal_volume: ComputeGeometryInteriorAlgorithm
+ * (src/ComputeGeometryInteriorAlgorithm.C) sums the eight sub-control volumes
+ * of HexSCV::determinant (src/master_element/Hex8CVFEM.C:149-180) into their
+ * nodes; fills NALU_FIELD_DUAL_VOLUME from the coordinates */
+int nalu_compute_dual_volume(nalu_ctx* ctx);
+/* HexSCV::determinant of one element: vol[8] (host) */
+int nalu_capture_scv_volumes(nalu_ctx* ctx, int64_t elem, double* vol);
+/* Element part of the projected nodal gradient (AssembleNodalGradElemAlgorithm,
+ * src/AssembleNodalGradElemAlgorithm.C; AssembleNodalGradUElemAlgorithm for a
+ * vector field): dst = sum over SCS of q_ip A / V, zeroed first.  src is a
+ * scalar field (dst 3 components, e.g. PRESSURE -> DPDX) or a 3-vector field
+ * (dst 9 components, d src_i / dx_j at 3 i + j, e.g. VELOCITY -> DUDX).
+ * Needs NALU_FIELD_DUAL_VOLUME.  The boundary-face closure
+ * (AssembleNodalGradBoundaryAlgorithm) is not part of this call.
+ * shifted: shifted_shape_fcn at the ips. */
+int nalu_compute_nodal_gradient(nalu_ctx* ctx, int src_field, int dst_field, int shifted);
 
 /* ---- linear solve (TpetraLinearSolver::solve, src/LinearSolver.C:183-232) */
 enum nalu_solver_method {

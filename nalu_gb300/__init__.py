@@ -28,7 +28,8 @@ STATUS = {0: "ok", -1: "invalid argument", -2: "CUDA error", -3: "call out of or
           -7: "not converged", -8: "entry missing from graph", -9: "no CUDA device"}
 
 FIELD = {"coordinates": 0, "scalar_q": 1, "diff_coeff": 2, "velocity": 3, "velocity_rtm": 4,
-         "density": 5, "pressure": 6, "dpdx": 7, "viscosity": 8, "dudx": 9, "mass_flow_rate_scs": 10}
+         "density": 5, "pressure": 6, "dpdx": 7, "viscosity": 8, "dudx": 9, "mass_flow_rate_scs": 10,
+         "dual_nodal_volume": 11}
 KERNEL_SCALAR_DIFF = 0
 KERNEL_CONTINUITY_ADV = 1
 KERNEL_MOMENTUM_ADV_DIFF = 2
@@ -113,6 +114,9 @@ def lib():
             "nalu_assemble": (I, [P, I, P]),
             "nalu_capture_element": (I, [P, I, P, I64, P, P]),
             "nalu_compute_mdot": (I, [P, P]),
+            "nalu_compute_dual_volume": (I, [P]),
+            "nalu_capture_scv_volumes": (I, [P, I64, P]),
+            "nalu_compute_nodal_gradient": (I, [P, I, I, I]),
             "nalu_solver_opts_default": (None, [P]),
             "nalu_solve": (I, [P, P, P]),
             "nalu_solution_get": (I, [P, P, I]),
@@ -284,6 +288,19 @@ class Context:
     def compute_mdot(self, opts=None):
         opts = default_assemble_opts() if opts is None else opts
         self._check(lib().nalu_compute_mdot(self._h, ctypes.byref(opts)), "compute_mdot")
+
+    # nodal geometry and gradients
+    def compute_dual_volume(self):
+        self._check(lib().nalu_compute_dual_volume(self._h), "compute_dual_volume")
+
+    def capture_scv_volumes(self, elem):
+        v = np.zeros(8)
+        self._check(lib().nalu_capture_scv_volumes(self._h, int(elem), _ptr(v)), "capture_scv_volumes")
+        return v
+
+    def compute_nodal_gradient(self, src, dst, shifted=False):
+        self._check(lib().nalu_compute_nodal_gradient(self._h, FIELD[src], FIELD[dst], int(bool(shifted))),
+                    "compute_nodal_gradient")
 
     # solve
     def solve(self, opts=None, raise_on_error=True):

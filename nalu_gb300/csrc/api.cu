@@ -60,6 +60,8 @@ int field_comps(int f) {
       return 9;
     case NALU_FIELD_MDOT_SCS:
       return 12;
+    case NALU_FIELD_DUAL_VOLUME:
+      return 1;
     default:
       return 1;
   }
@@ -793,6 +795,54 @@ int nalu_compute_mdot(nalu_ctx* ctx, const nalu_assemble_opts* opts) {
   int rc = launch_mdot(ctx, *opts);
   if (rc) return rc;
   m.set = true;
+  return NALU_OK;
+}
+
+// ---- nodal geometry and gradients -------------------------------------------------
+int nalu_compute_dual_volume(nalu_ctx* ctx) {
+  if (!ctx) return NALU_ERR_ARG;
+  if (!ctx->fields[NALU_FIELD_COORDINATES].set) return set_error(ctx, NALU_ERR_STATE, "no mesh");
+  cudaSetDevice(ctx->device);
+  Field& v = ctx->fields[NALU_FIELD_DUAL_VOLUME];
+  if (v.d.n != ctx->n_nodes) NALU_CUDA(ctx, v.d.alloc(ctx->n_nodes));
+  v.comps = 1;
+  int rc = launch_dual_volume(ctx, v.d.p, -1, nullptr);
+  if (rc) return rc;
+  v.set = true;
+  return NALU_OK;
+}
+
+int nalu_capture_scv_volumes(nalu_ctx* ctx, int64_t elem, double* vol) {
+  if (!ctx || !vol || elem < 0 || elem >= ctx->n_elems) return NALU_ERR_ARG;
+  if (!ctx->fields[NALU_FIELD_COORDINATES].set) return set_error(ctx, NALU_ERR_STATE, "no mesh");
+  cudaSetDevice(ctx->device);
+  DBuf<double> d;
+  NALU_CUDA(ctx, d.alloc(8));
+  int rc = launch_dual_volume(ctx, nullptr, elem, d.p);
+  if (rc) return rc;
+  NALU_CUDA(ctx, cudaMemcpyAsync(vol, d.p, sizeof(double) * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  NALU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return NALU_OK;
+}
+
+int nalu_compute_nodal_gradient(nalu_ctx* ctx, int src_field, int dst_field, int shifted) {
+  if (!ctx || src_field < 0 || src_field >= NALU_FIELD_COUNT || dst_field < 0 || dst_field >= NALU_FIELD_COUNT ||
+      src_field == NALU_FIELD_MDOT_SCS || dst_field == NALU_FIELD_MDOT_SCS || src_field == dst_field)
+    return set_error(ctx, NALU_ERR_ARG, "gradient fields");
+  const int sc = field_comps(src_field), dc = field_comps(dst_field);
+  if (!((sc == 1 && dc == 3) || (sc == 3 && dc == 9)))
+    return set_error(ctx, NALU_ERR_ARG, "gradient of a scalar needs a 3-vector field, of a vector a 9-component one");
+  if (!ctx->fields[src_field].set) return set_error(ctx, NALU_ERR_STATE, "gradient source field not set");
+  if (!ctx->fields[NALU_FIELD_DUAL_VOLUME].set)
+    return set_error(ctx, NALU_ERR_STATE, "dual_nodal_volume not computed (nalu_compute_dual_volume)");
+  cudaSetDevice(ctx->device);
+  Field& g = ctx->fields[dst_field];
+  if (g.d.n != ctx->n_nodes * dc) NALU_CUDA(ctx, g.d.alloc(ctx->n_nodes * dc));
+  g.comps = dc;
+  int rc = launch_nodal_grad(ctx, ctx->fields[src_field].d.p, sc, ctx->fields[NALU_FIELD_DUAL_VOLUME].d.p, g.d.p,
+                             shifted != 0);
+  if (rc) return rc;
+  g.set = true;
   return NALU_OK;
 }
 

@@ -174,6 +174,9 @@ int launch_assemble_df(nalu_ctx* ctx, int kernel, const nalu_assemble_opts& o, i
 int launch_capture_df(nalu_ctx* ctx, int kernel, const nalu_assemble_opts& o, int64_t elem, double* d_lhs,
                       double* d_rhs);
 int launch_slot_table(nalu_ctx* ctx);
+// geometry.cu
+int launch_dual_volume(nalu_ctx* ctx, double* vol, int64_t cap_elem, double* cap);
+int launch_nodal_grad(nalu_ctx* ctx, const double* q, int ncomp, const double* dvol, double* grad, bool shifted);
 int launch_expand_graph(nalu_ctx* ctx);
 int launch_sum_into(nalu_ctx* ctx, int64_t n, const int64_t* d_elems, const double* d_lhs,
                     const double* d_rhs);

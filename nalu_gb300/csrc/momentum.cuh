@@ -44,8 +44,11 @@ struct MomLayout {
   static constexpr int DIAG = AA + 36;           // [12][8]   same-dof factor
   static constexpr int RIP = DIAG + 96;          // [12][3]   residual per ip
   static constexpr int ALHS = RIP + 36;          // [12][2]   upwind L/R factors
-  static constexpr int SIZE = ALHS + 24;         // 676
+  // 652 used, padded to 657 so that the element stride (2 SIZE 32-bit words)
+  // is 2 mod 32: equal offsets of the 16 elements fall in different banks
+  static constexpr int SIZE = ALHS + 24 + 5;     // 657
 };
+static_assert((2 * MomLayout::SIZE) % 32 == 2, "element stride");
 
 // ips adjacent to node r, ascending
 __device__ __forceinline__ int node_ip(int r, int k) {

@@ -29,8 +29,8 @@ namespace {
 // form, padded so that the element stride (2 SIZE 32-bit words) is 2 mod 32:
 // equal offsets of the 16 elements of a block fall in different banks
 struct MomLayoutDF {
-  static constexpr int EF = MomLayout::SIZE;  // [k][i][A,B,C,D]
-  static constexpr int SIZE = EF + 36 + 9;    // 721
+  static constexpr int EF = MomLayout::ALHS + 24;  // [k][i][A,B,C,D]
+  static constexpr int SIZE = EF + 36 + 1;    // 689
 };
 static_assert((2 * MomLayoutDF::SIZE) % 32 == 2, "element stride");
 

@@ -319,6 +319,50 @@ void orc_hex_scv_volume(const double* coords, double* volume) {
   }
 }
 
+// ComputeGeometryInteriorAlgorithm (src/ComputeGeometryInteriorAlgorithm.C):
+// dualNodalVolume[ipNodeMap[ip]] += scv_volume[ip], element order
+void orc_dual_volume(int64_t n_nodes, int64_t n_elems, const int32_t* conn, const double* coords, double* vol) {
+  for (int64_t i = 0; i < n_nodes; ++i) vol[i] = 0.0;
+  for (int64_t e = 0; e < n_elems; ++e) {
+    double c[24], v[8];
+    for (int n = 0; n < 8; ++n)
+      for (int d = 0; d < 3; ++d) c[3 * n + d] = coords[3 * (int64_t)conn[8 * e + n] + d];
+    orc_hex_scv_volume(c, v);
+    for (int n = 0; n < 8; ++n) vol[conn[8 * e + n]] += v[n];
+  }
+}
+
+// AssembleNodalGradElemAlgorithm::execute (src/AssembleNodalGradElemAlgorithm.C:
+// the nodalGradientElem functor): qIp = sum N q; grad[il] += qIp A / V_il,
+// grad[ir] -= qIp A / V_ir; ncomp = 3 is the velocity form (dudx[i][j])
+void orc_nodal_grad_elem(int64_t n_nodes, int64_t n_elems, const int32_t* conn, const double* coords,
+                         const double* q, int ncomp, const double* dual_volume, int shifted, double* grad) {
+  const int64_t w = 3 * (int64_t)ncomp;
+  for (int64_t i = 0; i < n_nodes * w; ++i) grad[i] = 0.0;
+  double shp[96];
+  scs_shape(shifted != 0, shp);
+  for (int64_t e = 0; e < n_elems; ++e) {
+    const int32_t* nd = conn + 8 * e;
+    double c[24], areav[36];
+    for (int n = 0; n < 8; ++n)
+      for (int d = 0; d < 3; ++d) c[3 * n + d] = coords[3 * (int64_t)nd[n] + d];
+    orc_hex_scs_areav(c, areav);
+    for (int ip = 0; ip < 12; ++ip) {
+      const int il = kLrscv[2 * ip], ir = kLrscv[2 * ip + 1];
+      const double inv_l = 1.0 / dual_volume[nd[il]], inv_r = 1.0 / dual_volume[nd[ir]];
+      for (int k = 0; k < ncomp; ++k) {
+        double qip = 0.0;
+        for (int ic = 0; ic < 8; ++ic) qip += shp[ip * 8 + ic] * q[(int64_t)nd[ic] * ncomp + k];
+        for (int j = 0; j < 3; ++j) {
+          const double fac = qip * areav[ip * 3 + j];
+          grad[(int64_t)nd[il] * w + 3 * k + j] += fac * inv_l;
+          grad[(int64_t)nd[ir] * w + 3 * k + j] -= fac * inv_r;
+        }
+      }
+    }
+  }
+}
+
 // ScalarDiffElemKernel::execute: src/kernel/ScalarDiffElemKernel.C:66-110
 void orc_scalar_diff_elem(const double* coords, const double* q, const double* dk,
                           int shifted_grad_op, double* lhs, double* rhs) {

@@ -97,6 +97,20 @@ void orc_reset_rows(const int64_t* rowptr, double* values, double* rhs,
 void orc_sum_into_diag(const int64_t* rowptr, const int32_t* colind, double* values,
                        double* rhs, int32_t row, double diag, double rhs_value);
 
+/* --- nodal geometry and gradients -------------------------------------- */
+/* dual nodal volume: ComputeGeometryInteriorAlgorithm
+ * (src/ComputeGeometryInteriorAlgorithm.C) sums HexSCV::determinant's eight
+ * sub-control volumes into their nodes (ipNodeMap is the identity for Hex8);
+ * conn holds node indices [E][8], vol [n] is overwritten */
+void orc_dual_volume(int64_t n_nodes, int64_t n_elems, const int32_t* conn, const double* coords, double* vol);
+/* element part of the projected nodal gradient: AssembleNodalGradElemAlgorithm
+ * (src/AssembleNodalGradElemAlgorithm.C) for ncomp = 1 (dqdx [n][3]) and the
+ * vector form of AssembleNodalGradUElemAlgorithm for ncomp = 3 (dudx [n][3][3],
+ * du_i/dx_j at 3 i + j); q [n][ncomp]; grad is overwritten (zeroed first, as
+ * the algorithm driver does); shifted selects shifted_shape_fcn */
+void orc_nodal_grad_elem(int64_t n_nodes, int64_t n_elems, const int32_t* conn, const double* coords,
+                         const double* q, int ncomp, const double* dual_volume, int shifted, double* grad);
+
 /* --- solvers (FP64, stand-in for Belos/Ifpack2, unpinned) -------------- */
 void orc_spmv(int64_t n, const int64_t* rowptr, const int32_t* colind, const double* v,
               const double* x, double* y, int n_threads);

@@ -47,6 +47,9 @@ def lib():
                                                                                   ctypes.c_int, ctypes.c_void_p,
                                                                                   ctypes.c_int]
         L.orc_spmv.argtypes = [ctypes.c_int64] + [ctypes.c_void_p] * 5 + [ctypes.c_int]
+        L.orc_dual_volume.argtypes = [ctypes.c_int64, ctypes.c_int64] + [ctypes.c_void_p] * 3
+        L.orc_nodal_grad_elem.argtypes = [ctypes.c_int64, ctypes.c_int64] + [ctypes.c_void_p] * 3 + \
+            [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
         L.orc_continuity_adv_elem.argtypes = [ctypes.c_void_p] * 5 + [ctypes.c_double, ctypes.c_int, ctypes.c_int,
                                                                       ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
         L.orc_momentum_adv_diff_elem.argtypes = [ctypes.c_void_p] * 4 + [ctypes.c_double, ctypes.c_int,
@@ -246,3 +249,24 @@ def gmres_jacobi(rowptr, colind, values, b, restart=50, tol=1e-8, max_it=10000, 
     it = lib().orc_gmres_jacobi(n, _p(rowptr), _p(colind), _p(values), _p(_f64(b)), _p(x), int(restart),
                                 float(tol), int(max_it), ctypes.byref(res), int(n_threads))
     return x, it, res.value
+
+
+def dual_volume(coords, conn):
+    """Dual nodal volume (sum of HexSCV sub-control volumes per node)."""
+    coords = _f64(coords)
+    conn = np.ascontiguousarray(conn, np.int32)
+    vol = np.zeros(coords.shape[0])
+    lib().orc_dual_volume(coords.shape[0], conn.shape[0], _p(conn), _p(coords), _p(vol))
+    return vol
+
+
+def nodal_grad_elem(coords, conn, q, dual_volume, shifted=False):
+    """Element part of the projected nodal gradient; q [n] -> [n,3], q [n,3] -> [n,3,3]."""
+    coords = _f64(coords)
+    conn = np.ascontiguousarray(conn, np.int32)
+    q = _f64(q)
+    ncomp = 1 if q.ndim == 1 else q.shape[1]
+    grad = np.zeros((coords.shape[0], ncomp, 3))
+    lib().orc_nodal_grad_elem(coords.shape[0], conn.shape[0], _p(conn), _p(coords), _p(q), ncomp,
+                              _p(_f64(dual_volume)), int(bool(shifted)), _p(grad))
+    return grad[:, 0, :] if ncomp == 1 else grad

@@ -155,3 +155,85 @@ def test_oracle_solvers(oracle):
     assert res <= 1e-10
     x2, it2, res2 = oracle.gmres_jacobi(rp, ci, v, b, restart=30, tol=1e-10)
     assert res2 <= 1e-10 and np.allclose(x, x2, atol=1e-8)
+
+
+# ---------------------------------------------------------------------------
+# dual nodal volume and the element part of the projected nodal gradient
+# ---------------------------------------------------------------------------
+def _affine_block(n, seed=3):
+    """Block mesh under a random linear map of positive determinant (the
+    mapping of unit_tests/UnitTestMasterElements.C:185-228)."""
+    c, conn, gid = block_mesh(n, n, n)
+    rng = np.random.default_rng(seed)
+    q, _ = np.linalg.qr(rng.standard_normal((3, 3)))
+    m = q @ np.diag(rng.uniform(0.5, 1.5, 3))
+    if np.linalg.det(m) < 0:
+        m[:, 0] *= -1.0
+    return c @ m.T, conn, np.linalg.det(m)
+
+
+def _interior(n):
+    k, j, i = np.meshgrid(np.arange(n + 1), np.arange(n + 1), np.arange(n + 1), indexing="ij")
+    return ((i > 0) & (i < n) & (j > 0) & (j < n) & (k > 0) & (k < n)).ravel()
+
+
+def test_dual_volume(oracle):
+    n = 4
+    c0, conn, _ = block_mesh(n, n, n, jitter=0.3, seed=5)
+    v0 = oracle.dual_volume(c0, conn)
+    # scatter of HexSCV::determinant per element
+    ref = np.zeros(c0.shape[0])
+    for e in range(conn.shape[0]):
+        np.add.at(ref, conn[e], oracle.scv_volume(c0[conn[e]]))
+    assert np.max(np.abs(v0 - ref)) <= 1e-15
+    assert abs(v0.sum() - 1.0) <= 1e-13
+    # linear map: every volume scales by det(QR)
+    ca, conna, det = _affine_block(n)
+    cb, _, _ = block_mesh(n, n, n)
+    assert np.max(np.abs(oracle.dual_volume(ca, conna) - det * oracle.dual_volume(cb, conna))) <= 1e-15
+
+
+def _grad_restated(oracle, c, conn, q, vol, shifted):
+    """sum over the 12 SCS of q_ip A into the left (+) and right (-) node of each
+    face, divided by the dual volume (AssembleNodalGradElemAlgorithm.C:104-137;
+    shifted_shape_fcn at :197-201)."""
+    lr, loc, locs = oracle.scs_tables()
+    lr = lr.reshape(12, 2)
+    shp = oracle.shape_fcn((locs if shifted else loc).reshape(12, 3))
+    q2 = q.reshape(q.shape[0], -1)
+    g = np.zeros((c.shape[0], q2.shape[1], 3))
+    for e in range(conn.shape[0]):
+        a = oracle.scs_areav(c[conn[e]])
+        qip = shp @ q2[conn[e]]
+        for ip in range(12):
+            f = qip[ip][:, None] * a[ip][None, :]
+            g[conn[e][lr[ip, 0]]] += f
+            g[conn[e][lr[ip, 1]]] -= f
+    g /= vol[:, None, None]
+    return g[:, 0, :] if q.ndim == 1 else g
+
+
+@pytest.mark.parametrize("shifted", [False, True])
+def test_nodal_grad_elem_restated(oracle, shifted):
+    c, conn, _ = block_mesh(3, 3, 3, jitter=0.3, seed=2)
+    rng = np.random.default_rng(1)
+    vol = oracle.dual_volume(c, conn)
+    for q in (rng.standard_normal(c.shape[0]), rng.standard_normal((c.shape[0], 3))):
+        got = oracle.nodal_grad_elem(c, conn, q, vol, shifted)
+        ref = _grad_restated(oracle, c, conn, q, vol, shifted)
+        assert np.max(np.abs(got - ref)) <= 1e-12 * max(1.0, np.max(np.abs(ref)))
+
+
+def test_nodal_grad_elem_exact_for_linear_fields(oracle):
+    """Green-Gauss over a closed dual volume is exact for a linear field on an
+    affine mesh at interior nodes (boundary nodes lack the face closure)."""
+    n = 4
+    c, conn, _ = _affine_block(n)
+    vol = oracle.dual_volume(c, conn)
+    inner = _interior(n)
+    g = np.array([0.7, -1.3, 2.1])
+    got = oracle.nodal_grad_elem(c, conn, 0.4 + c @ g, vol)
+    assert np.max(np.abs(got[inner] - g)) <= 1e-12
+    m = np.array([[1.0, 2.0, -0.5], [0.3, -1.1, 0.8], [2.2, 0.1, -0.7]])
+    got = oracle.nodal_grad_elem(c, conn, c @ m.T, vol)
+    assert np.max(np.abs(got[inner] - m[None])) <= 1e-12
