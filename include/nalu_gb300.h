@@ -69,7 +69,14 @@ enum nalu_field {
   NALU_FIELD_DUDX = 9,         /* [n][3][3] Gju */
   NALU_FIELD_MDOT_SCS = 10,    /* element field [E][12] mass_flow_rate_scs */
   NALU_FIELD_DUAL_VOLUME = 11, /* [n]    dual_nodal_volume (nalu_compute_dual_volume) */
-  NALU_FIELD_COUNT = 12
+  /* older time levels of the two-/three-state fields (stk::mesh::StateN /
+   * StateNM1); DENSITY and VELOCITY above are state N+1.  The mass kernels
+   * read N-1 as N when N-1 is not set (a two-state field). */
+  NALU_FIELD_DENSITY_N = 12,    /* [n]    */
+  NALU_FIELD_DENSITY_NM1 = 13,  /* [n]    */
+  NALU_FIELD_VELOCITY_N = 14,   /* [n][3] */
+  NALU_FIELD_VELOCITY_NM1 = 15, /* [n][3] */
+  NALU_FIELD_COUNT = 16
 };
 /* copy a field in (host or device source, caller node order) */
 int nalu_field_set(nalu_ctx* ctx, int field, const double* src, int64_t count, int src_is_device);
@@ -121,7 +128,11 @@ enum nalu_kernel {
   NALU_KERNEL_SCALAR_DIFF = 0,        /* src/kernel/ScalarDiffElemKernel.C */
   NALU_KERNEL_CONTINUITY_ADV = 1,     /* src/kernel/ContinuityAdvElemKernel.C */
   NALU_KERNEL_MOMENTUM_ADV_DIFF = 2,  /* src/kernel/MomentumAdvDiffElemKernel.C */
-  NALU_KERNEL_MOMENTUM_UPW_ADV_DIFF = 3 /* src/kernel/MomentumUpwAdvDiffElemKernel.C */
+  NALU_KERNEL_MOMENTUM_UPW_ADV_DIFF = 3, /* src/kernel/MomentumUpwAdvDiffElemKernel.C */
+  /* time terms (gamma1 phi^{n+1} + gamma2 phi^n + gamma3 phi^{n-1}) / dt over
+   * the sub-control volumes; dt and the gammas come from the opts below */
+  NALU_KERNEL_CONTINUITY_MASS = 4,  /* src/kernel/ContinuityMassElemKernel.C (rhs only) */
+  NALU_KERNEL_MOMENTUM_MASS = 5     /* src/kernel/MomentumMassElemKernel.C (reads DPDX as Gjp) */
 };
 enum nalu_scatter {
   NALU_SCATTER_AUTO = 0,    /* autotuned choice, cached per context */
@@ -145,7 +156,13 @@ typedef struct nalu_assemble_opts {
   double hybrid_factor;     /* get_hybrid_factor (classic Peclet function, A = 5) */
   int scatter;              /* enum nalu_scatter */
   int arith;                /* enum nalu_arith (scalar kernels) */
-  int reserved[6];
+  int lumped_mass;          /* mass kernels: lumped (shifted_shape_fcn) */
+  int balanced_force;       /* MomentumMass: solnOpts.balancedForce_ (Gjp scaled by rho) */
+  double dt;                /* TimeIntegrator::get_time_step, > 0 for the mass kernels */
+  double gamma1;            /* TimeIntegrator::get_gamma1 (default 1, BDF1) */
+  double gamma2;            /* get_gamma2 (default -1) */
+  double gamma3;            /* get_gamma3 (default 0) */
+  int reserved[4];
 } nalu_assemble_opts;
 /* arithmetic of the element math; inputs, outputs, the CRS scatter and the
  * residual's -lhs.q term stay FP64 in both modes */

@@ -29,11 +29,13 @@ STATUS = {0: "ok", -1: "invalid argument", -2: "CUDA error", -3: "call out of or
 
 FIELD = {"coordinates": 0, "scalar_q": 1, "diff_coeff": 2, "velocity": 3, "velocity_rtm": 4,
          "density": 5, "pressure": 6, "dpdx": 7, "viscosity": 8, "dudx": 9, "mass_flow_rate_scs": 10,
-         "dual_nodal_volume": 11}
+         "dual_nodal_volume": 11, "density_n": 12, "density_nm1": 13, "velocity_n": 14, "velocity_nm1": 15}
 KERNEL_SCALAR_DIFF = 0
 KERNEL_CONTINUITY_ADV = 1
 KERNEL_MOMENTUM_ADV_DIFF = 2
 KERNEL_MOMENTUM_UPW_ADV_DIFF = 3
+KERNEL_CONTINUITY_MASS = 4
+KERNEL_MOMENTUM_MASS = 5
 SCATTER_AUTO, SCATTER_ATOMIC, SCATTER_COLOURED = 0, 1, 2
 ARITH_FP64, ARITH_DF64 = 0, 1
 SOLVER_CG, SOLVER_GMRES = 0, 1
@@ -54,7 +56,9 @@ class AssembleOpts(ctypes.Structure):
                 ("proj_time_scale", ctypes.c_double), ("include_divu", ctypes.c_double),
                 ("alpha", ctypes.c_double), ("alpha_upw", ctypes.c_double), ("upw_factor", ctypes.c_double),
                 ("hybrid_factor", ctypes.c_double), ("scatter", ctypes.c_int), ("arith", ctypes.c_int),
-                ("reserved", ctypes.c_int * 6)]
+                ("lumped_mass", ctypes.c_int), ("balanced_force", ctypes.c_int), ("dt", ctypes.c_double),
+                ("gamma1", ctypes.c_double), ("gamma2", ctypes.c_double), ("gamma3", ctypes.c_double),
+                ("reserved", ctypes.c_int * 4)]
 
 
 class SolverOpts(ctypes.Structure):
@@ -278,7 +282,7 @@ class Context:
 
     def capture_element(self, kernel, elem, opts=None):
         opts = default_assemble_opts() if opts is None else opts
-        ne = 24 if kernel >= 2 else 8
+        ne = 24 if kernel in (KERNEL_MOMENTUM_ADV_DIFF, KERNEL_MOMENTUM_UPW_ADV_DIFF, KERNEL_MOMENTUM_MASS) else 8
         lhs = np.zeros((ne, ne))
         rhs = np.zeros(ne)
         self._check(lib().nalu_capture_element(self._h, kernel, ctypes.byref(opts), int(elem), _ptr(lhs), _ptr(rhs)),

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <numeric>
@@ -55,6 +56,8 @@ int field_comps(int f) {
     case NALU_FIELD_VELOCITY:
     case NALU_FIELD_VELOCITY_RTM:
     case NALU_FIELD_DPDX:
+    case NALU_FIELD_VELOCITY_N:
+    case NALU_FIELD_VELOCITY_NM1:
       return 3;
     case NALU_FIELD_DUDX:
       return 9;
@@ -670,9 +673,25 @@ void nalu_assemble_opts_default(nalu_assemble_opts* o) {
   o->hybrid_factor = 0.0;
   o->include_divu = 0.0;
   o->scatter = NALU_SCATTER_AUTO;
+  o->gamma1 = 1.0;      // BDF1 (TimeIntegrator, src/TimeIntegrator.C)
+  o->gamma2 = -1.0;
+  o->gamma3 = 0.0;
 }
 
 namespace {
+int kernel_dof(int kernel) {
+  return (kernel == NALU_KERNEL_MOMENTUM_ADV_DIFF || kernel == NALU_KERNEL_MOMENTUM_UPW_ADV_DIFF ||
+          kernel == NALU_KERNEL_MOMENTUM_MASS) ? 3 : 1;
+}
+
+int check_time_opts(nalu_ctx* ctx, int kernel, const nalu_assemble_opts& o) {
+  if (kernel < NALU_KERNEL_CONTINUITY_MASS) return NALU_OK;
+  if (!(o.dt > 0.0) || !std::isfinite(o.dt)) return set_error(ctx, NALU_ERR_ARG, "mass kernels need dt > 0");
+  if (!(o.gamma1 != 0.0) || !std::isfinite(o.gamma1) || !std::isfinite(o.gamma2) || !std::isfinite(o.gamma3))
+    return set_error(ctx, NALU_ERR_ARG, "mass kernels need finite gammas, gamma1 != 0");
+  return NALU_OK;
+}
+
 int check_kernel_inputs(nalu_ctx* ctx, int kernel) {
   auto need = [&](int f, const char* name) -> int {
     if (!ctx->fields[f].set) return set_error(ctx, NALU_ERR_STATE, std::string("field not set: ") + name);
@@ -700,6 +719,15 @@ int check_kernel_inputs(nalu_ctx* ctx, int kernel) {
       if ((rc = need(NALU_FIELD_VISCOSITY, "viscosity"))) return rc;
       if ((rc = need(NALU_FIELD_DUDX, "dudx"))) return rc;
       return need(NALU_FIELD_MDOT_SCS, "mass_flow_rate_scs");
+    case NALU_KERNEL_CONTINUITY_MASS:
+      if ((rc = need(NALU_FIELD_DENSITY, "density"))) return rc;
+      return need(NALU_FIELD_DENSITY_N, "density (state N)");
+    case NALU_KERNEL_MOMENTUM_MASS:
+      if ((rc = need(NALU_FIELD_DENSITY, "density"))) return rc;
+      if ((rc = need(NALU_FIELD_DENSITY_N, "density (state N)"))) return rc;
+      if ((rc = need(NALU_FIELD_VELOCITY, "velocity"))) return rc;
+      if ((rc = need(NALU_FIELD_VELOCITY_N, "velocity (state N)"))) return rc;
+      return need(NALU_FIELD_DPDX, "dpdx");
     default:
       return set_error(ctx, NALU_ERR_ARG, "unknown kernel");
   }
@@ -717,15 +745,19 @@ double time_assemble(nalu_ctx* ctx, int kernel, const nalu_assemble_opts& o, int
 }  // namespace
 
 int nalu_assemble(nalu_ctx* ctx, int kernel, const nalu_assemble_opts* opts) {
-  if (!ctx || !opts || kernel < 0 || kernel > 3) return set_error(ctx, NALU_ERR_ARG, "assemble args");
+  if (!ctx || !opts || kernel < 0 || kernel > NALU_KERNEL_MOMENTUM_MASS)
+    return set_error(ctx, NALU_ERR_ARG, "assemble args");
   if (ctx->num_dof == 0) return set_error(ctx, NALU_ERR_STATE, "no graph");
-  const int want = kernel >= NALU_KERNEL_MOMENTUM_ADV_DIFF ? 3 : 1;
-  if (ctx->num_dof != want) return set_error(ctx, NALU_ERR_STATE, "graph numDof does not match the kernel");
+  if (ctx->num_dof != kernel_dof(kernel)) return set_error(ctx, NALU_ERR_STATE, "graph numDof does not match the kernel");
   if (!(opts->proj_time_scale != 0.0)) return set_error(ctx, NALU_ERR_ARG, "proj_time_scale must be non-zero");
-  int rc = check_kernel_inputs(ctx, kernel);
+  int rc = check_time_opts(ctx, kernel, *opts);
+  if (rc) return rc;
+  rc = check_kernel_inputs(ctx, kernel);
   if (rc) return rc;
   cudaSetDevice(ctx->device);
   int scatter = opts->scatter;
+  // the mass kernels scatter a few entries per row: atomics, no autotuning
+  if (scatter == NALU_SCATTER_AUTO && kernel >= NALU_KERNEL_CONTINUITY_MASS) scatter = NALU_SCATTER_ATOMIC;
   if (scatter == NALU_SCATTER_AUTO) {
     scatter = ctx->scatter_choice[kernel];
     if (scatter == 0) {
@@ -762,12 +794,15 @@ int nalu_assemble(nalu_ctx* ctx, int kernel, const nalu_assemble_opts* opts) {
 
 int nalu_capture_element(nalu_ctx* ctx, int kernel, const nalu_assemble_opts* opts, int64_t elem, double* lhs,
                          double* rhs) {
-  if (!ctx || !opts || !lhs || !rhs || kernel < 0 || kernel > 3) return set_error(ctx, NALU_ERR_ARG, "capture args");
+  if (!ctx || !opts || !lhs || !rhs || kernel < 0 || kernel > NALU_KERNEL_MOMENTUM_MASS)
+    return set_error(ctx, NALU_ERR_ARG, "capture args");
   if (elem < 0 || elem >= ctx->n_elems) return set_error(ctx, NALU_ERR_ARG, "element out of range");
-  int rc = check_kernel_inputs(ctx, kernel);
+  int rc = check_time_opts(ctx, kernel, *opts);
+  if (rc) return rc;
+  rc = check_kernel_inputs(ctx, kernel);
   if (rc) return rc;
   cudaSetDevice(ctx->device);
-  const int ne = kernel >= 2 ? 24 : 8;
+  const int ne = 8 * kernel_dof(kernel);
   DBuf<double> dl, dr;
   NALU_CUDA(ctx, dl.alloc(ne * ne));
   NALU_CUDA(ctx, dr.alloc(ne));

@@ -380,6 +380,7 @@ int launch_momentum(nalu_ctx* ctx, int kernel, const nalu_assemble_opts& o, int 
                     double* cap_lhs, double* cap_rhs);
 
 int launch_assemble(nalu_ctx* ctx, int kernel, const nalu_assemble_opts& o, int scatter) {
+  if (kernel >= NALU_KERNEL_CONTINUITY_MASS) return launch_mass(ctx, kernel, o, scatter, -1, nullptr, nullptr);
   if (kernel >= NALU_KERNEL_MOMENTUM_ADV_DIFF) return launch_momentum(ctx, kernel, o, scatter, -1, nullptr, nullptr);
   if (o.arith == NALU_ARITH_DF64) return launch_assemble_df(ctx, kernel, o, scatter);
   AsmArgs a = base_args(ctx, kernel, o);
@@ -400,6 +401,7 @@ int launch_assemble(nalu_ctx* ctx, int kernel, const nalu_assemble_opts& o, int 
 
 int launch_capture(nalu_ctx* ctx, int kernel, const nalu_assemble_opts& o, int64_t elem, double* d_lhs,
                    double* d_rhs) {
+  if (kernel >= NALU_KERNEL_CONTINUITY_MASS) return launch_mass(ctx, kernel, o, 0, elem, d_lhs, d_rhs);
   if (kernel >= NALU_KERNEL_MOMENTUM_ADV_DIFF) return launch_momentum(ctx, kernel, o, 0, elem, d_lhs, d_rhs);
   if (o.arith == NALU_ARITH_DF64) return launch_capture_df(ctx, kernel, o, elem, d_lhs, d_rhs);
   AsmArgs a = base_args(ctx, kernel, o);

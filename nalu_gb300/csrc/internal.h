@@ -127,7 +127,7 @@ struct nalu_ctx {
   nalu_gb300::DBuf<int32_t> d_colour_elems;  // element ids grouped by colour
   nalu_gb300::DBuf<double> d_node_df;    // df64 split of nodal kernel inputs (8 B each)
   std::vector<int64_t> colour_offsets;   // [n_colours+1]
-  int scatter_choice[4] = {0, 0, 0, 0};  // autotuned scatter per kernel (0 = not tuned)
+  int scatter_choice[6] = {0, 0, 0, 0, 0, 0};  // autotuned scatter per kernel (0 = not tuned)
 
   // independent problems in one context (node offsets in LID order)
   std::vector<int64_t> problem_offsets;
@@ -175,6 +175,8 @@ int launch_capture_df(nalu_ctx* ctx, int kernel, const nalu_assemble_opts& o, in
                       double* d_rhs);
 int launch_slot_table(nalu_ctx* ctx);
 // geometry.cu
+int launch_mass(nalu_ctx* ctx, int kernel, const nalu_assemble_opts& o, int scatter, int64_t cap_elem,
+                double* cap_lhs, double* cap_rhs);
 int launch_dual_volume(nalu_ctx* ctx, double* vol, int64_t cap_elem, double* cap);
 int launch_nodal_grad(nalu_ctx* ctx, const double* q, int ncomp, const double* dvol, double* grad, bool shifted);
 int launch_expand_graph(nalu_ctx* ctx);

@@ -319,6 +319,83 @@ void orc_hex_scv_volume(const double* coords, double* volume) {
   }
 }
 
+// SCV shape functions: HexSCV::shape_fcn / shifted_shape_fcn
+// (src/master_element/Hex8CVFEM.C:236-250, ips at :89-107), ip i in the
+// octant of node i
+static void scv_shape(int lumped, double* shp /*[8][8]*/) {
+  const double sx[8] = {-1, 1, 1, -1, -1, 1, 1, -1}, sy[8] = {-1, -1, 1, 1, -1, -1, 1, 1},
+               sz[8] = {-1, -1, -1, -1, 1, 1, 1, 1};
+  const double a = lumped ? 0.5 : 0.25;
+  double iso[24];
+  for (int ip = 0; ip < 8; ++ip) {
+    iso[3 * ip] = sx[ip] * a;
+    iso[3 * ip + 1] = sy[ip] * a;
+    iso[3 * ip + 2] = sz[ip] * a;
+  }
+  orc_hex8_shape_fcn(8, iso, shp);
+}
+
+// ContinuityMassElemKernel::execute (src/kernel/ContinuityMassElemKernel.C:84-120)
+void orc_continuity_mass_elem(const double* coords, const double* rho_nm1, const double* rho_n,
+                              const double* rho_np1, double dt, double gamma1, double gamma2, double gamma3,
+                              int lumped, double* lhs, double* rhs) {
+  double shp[64], scv[8];
+  scv_shape(lumped, shp);
+  orc_hex_scv_volume(coords, scv);
+  for (int i = 0; i < 64; ++i) lhs[i] = 0.0;
+  for (int i = 0; i < 8; ++i) rhs[i] = 0.0;
+  const double proj_time_scale = dt / gamma1;
+  for (int ip = 0; ip < 8; ++ip) {
+    double rNm1 = 0.0, rN = 0.0, rNp1 = 0.0;
+    for (int ic = 0; ic < 8; ++ic) {
+      const double r = shp[8 * ip + ic];
+      rNm1 += r * rho_nm1[ic];
+      rN += r * rho_n[ic];
+      rNp1 += r * rho_np1[ic];
+    }
+    rhs[ip] += -(gamma1 * rNp1 + gamma2 * rN + gamma3 * rNm1) * scv[ip] / dt / proj_time_scale;
+  }
+}
+
+// MomentumMassElemKernel::execute (src/kernel/MomentumMassElemKernel.C:100-171)
+void orc_momentum_mass_elem(const double* coords, const double* rho_nm1, const double* rho_n,
+                            const double* rho_np1, const double* u_nm1, const double* u_n,
+                            const double* u_np1, const double* gpdx, double dt, double gamma1,
+                            double gamma2, double gamma3, int lumped, int balanced_force, double* lhs,
+                            double* rhs) {
+  double shp[64], scv[8];
+  scv_shape(lumped, shp);
+  orc_hex_scv_volume(coords, scv);
+  for (int i = 0; i < 576; ++i) lhs[i] = 0.0;
+  for (int i = 0; i < 24; ++i) rhs[i] = 0.0;
+  const double dens_fac_on = balanced_force ? 1.0 : 0.0, om_dens_fac = balanced_force ? 0.0 : 1.0;
+  for (int ip = 0; ip < 8; ++ip) {
+    double rNm1 = 0.0, rN = 0.0, rNp1 = 0.0, uNm1[3] = {0, 0, 0}, uN[3] = {0, 0, 0}, uNp1[3] = {0, 0, 0},
+           g[3] = {0, 0, 0};
+    for (int ic = 0; ic < 8; ++ic) {
+      const double r = shp[8 * ip + ic];
+      rNm1 += r * rho_nm1[ic];
+      rN += r * rho_n[ic];
+      rNp1 += r * rho_np1[ic];
+      for (int j = 0; j < 3; ++j) {
+        uNm1[j] += r * u_nm1[3 * ic + j];
+        uN[j] += r * u_n[3 * ic + j];
+        uNp1[j] += r * u_np1[3 * ic + j];
+        g[j] += r * gpdx[3 * ic + j];
+      }
+    }
+    const double scV = scv[ip];
+    const double dens_fac = rNp1 * dens_fac_on + om_dens_fac;
+    for (int j = 0; j < 3; ++j)
+      rhs[3 * ip + j] += -(gamma1 * rNp1 * uNp1[j] + gamma2 * rN * uN[j] + gamma3 * rNm1 * uNm1[j]) * scV / dt -
+                         g[j] * scV * dens_fac;
+    for (int ic = 0; ic < 8; ++ic) {
+      const double lhsfac = shp[8 * ip + ic] * gamma1 * rNp1 * scV / dt;
+      for (int j = 0; j < 3; ++j) lhs[(3 * ip + j) * 24 + 3 * ic + j] += lhsfac;
+    }
+  }
+}
+
 // ComputeGeometryInteriorAlgorithm (src/ComputeGeometryInteriorAlgorithm.C):
 // dualNodalVolume[ipNodeMap[ip]] += scv_volume[ip], element order
 void orc_dual_volume(int64_t n_nodes, int64_t n_elems, const int32_t* conn, const double* coords, double* vol) {
@@ -924,6 +1001,44 @@ int orc_assemble(int kernel, int64_t n_nodes, int64_t n_elems, const int32_t* co
     parallel_for((int64_t)L.size(), n_threads, [&](int64_t b, int64_t en) {
       for (int64_t k = b; k < en; ++k) one(L[k]);
     });
+  }
+  return 0;
+}
+
+int orc_assemble_mass(int momentum, int64_t n_nodes, int64_t n_elems, const int32_t* conn,
+                      const int32_t* node_lid, const double* coords, const double* rho_nm1,
+                      const double* rho_n, const double* rho_np1, const double* u_nm1,
+                      const double* u_n, const double* u_np1, const double* gpdx, const double* tp,
+                      const int64_t* rowptr, const int32_t* colind, double* values, double* rhs) {
+  (void)n_nodes;
+  for (int64_t e = 0; e < n_elems; ++e) {
+    double c[24], a[8], b[8], d[8], u0[24], u1[24], u2[24], g[24], lhs[576], erhs[24];
+    int32_t elid[8];
+    const int32_t* en = conn + 8 * e;
+    for (int n = 0; n < 8; ++n) {
+      const int64_t i = en[n];
+      elid[n] = node_lid ? node_lid[i] : (int32_t)i;
+      a[n] = rho_nm1[i];
+      b[n] = rho_n[i];
+      d[n] = rho_np1[i];
+      for (int k = 0; k < 3; ++k) {
+        c[3 * n + k] = coords[3 * i + k];
+        if (momentum) {
+          u0[3 * n + k] = u_nm1[3 * i + k];
+          u1[3 * n + k] = u_n[3 * i + k];
+          u2[3 * n + k] = u_np1[3 * i + k];
+          g[3 * n + k] = gpdx[3 * i + k];
+        }
+      }
+    }
+    if (momentum) {
+      orc_momentum_mass_elem(c, a, b, d, u0, u1, u2, g, tp[0], tp[1], tp[2], tp[3], tp[4] != 0.0, tp[5] != 0.0,
+                             lhs, erhs);
+      sum_into(3, elid, lhs, erhs, rowptr, colind, values, rhs);
+    } else {
+      orc_continuity_mass_elem(c, a, b, d, tp[0], tp[1], tp[2], tp[3], tp[4] != 0.0, lhs, erhs);
+      sum_into(1, elid, lhs, erhs, rowptr, colind, values, rhs);
+    }
   }
   return 0;
 }

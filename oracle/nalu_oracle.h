@@ -61,6 +61,31 @@ void orc_mdot_elem(const double* coords, const double* density, const double* ve
                    const double* pressure, const double* gpdx, double proj_time_scale,
                    int shift_mdot, int shift_poisson, double* mdot /*[12]*/);
 
+/* time terms (BDF: gamma1 phi^{n+1} + gamma2 phi^n + gamma3 phi^{n-1}) at the
+ * eight sub-control volumes, ip i -> node i (HexSCV::ipNodeMap), shape
+ * functions at the SCV centroids or, lumped, at the nodes (shifted_shape_fcn).
+ * ContinuityMassElemKernel::execute (src/kernel/ContinuityMassElemKernel.C:84-120):
+ * rhs only, lhs [8][8] zero. */
+void orc_continuity_mass_elem(const double* coords, const double* rho_nm1, const double* rho_n,
+                              const double* rho_np1, double dt, double gamma1, double gamma2, double gamma3,
+                              int lumped, double* lhs /*[8][8]*/, double* rhs /*[8]*/);
+/* MomentumMassElemKernel::execute (src/kernel/MomentumMassElemKernel.C:100-171);
+ * gpdx [8][3] is Gjp, balanced_force selects densFac = rho^{n+1} */
+void orc_momentum_mass_elem(const double* coords, const double* rho_nm1, const double* rho_n,
+                            const double* rho_np1, const double* u_nm1, const double* u_n,
+                            const double* u_np1, const double* gpdx, double dt, double gamma1,
+                            double gamma2, double gamma3, int lumped, int balanced_force,
+                            double* lhs /*[24][24]*/, double* rhs /*[24]*/);
+/* serial element-order assembly of a mass kernel through the restated sumInto;
+ * momentum selects MomentumMass (num_dof 3) over ContinuityMass (num_dof 1);
+ * nodal fields in node-index order, u_* and gpdx [n][3] (NULL for continuity);
+ * tp = {dt, gamma1, gamma2, gamma3, lumped, balanced_force} */
+int orc_assemble_mass(int momentum, int64_t n_nodes, int64_t n_elems, const int32_t* conn,
+                      const int32_t* node_lid, const double* coords, const double* rho_nm1,
+                      const double* rho_n, const double* rho_np1, const double* u_nm1,
+                      const double* u_n, const double* u_np1, const double* gpdx, const double* tp,
+                      const int64_t* rowptr, const int32_t* colind, double* values, double* rhs);
+
 /* --- linear system (src/TpetraLinearSystem.C) --------------------------- */
 /* Restated buildElemToNodeGraph + finalizeLinearSystem on one rank.
  * node_gid may be NULL (gid = index+1).  Call with colind == NULL to get

@@ -18,6 +18,8 @@ KERNEL_SCALAR_DIFF = 0
 KERNEL_CONTINUITY_ADV = 1
 KERNEL_MOMENTUM_ADV_DIFF = 2
 KERNEL_MOMENTUM_UPW_ADV_DIFF = 3
+KERNEL_CONTINUITY_MASS = 4
+KERNEL_MOMENTUM_MASS = 5
 
 
 def _p(a):
@@ -60,6 +62,12 @@ def lib():
             [ctypes.c_double] * 4 + [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
         L.orc_mdot_elem.argtypes = [ctypes.c_void_p] * 5 + [ctypes.c_double, ctypes.c_int, ctypes.c_int,
                                                             ctypes.c_void_p]
+        L.orc_continuity_mass_elem.argtypes = [ctypes.c_void_p] * 4 + [ctypes.c_double] * 4 + \
+            [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+        L.orc_momentum_mass_elem.argtypes = [ctypes.c_void_p] * 8 + [ctypes.c_double] * 4 + \
+            [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+        L.orc_assemble_mass.restype = ctypes.c_int
+        L.orc_assemble_mass.argtypes = [ctypes.c_int, ctypes.c_int64, ctypes.c_int64] + [ctypes.c_void_p] * 15
         L.orc_apply_dirichlet.argtypes = [ctypes.c_void_p] * 4 + [ctypes.c_int64] + [ctypes.c_void_p] * 3
         L.orc_reset_rows.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_int64, ctypes.c_void_p]
         L.orc_sum_into.argtypes = [ctypes.c_int] + [ctypes.c_void_p] * 7
@@ -157,6 +165,42 @@ def mdot_elem(coords, rho, vrtm, p, gpdx, tau=1.0, shift_mdot=0, shift_poisson=0
     lib().orc_mdot_elem(_p(_f64(coords)), _p(_f64(rho)), _p(_f64(vrtm)), _p(_f64(p)), _p(_f64(gpdx)),
                         float(tau), int(shift_mdot), int(shift_poisson), _p(out))
     return out
+
+
+def continuity_mass_elem(coords, rho_nm1, rho_n, rho_np1, dt, gamma1=1.0, gamma2=-1.0, gamma3=0.0, lumped=False):
+    lhs, rhs = np.zeros(64), np.zeros(8)
+    lib().orc_continuity_mass_elem(_p(_f64(coords)), _p(_f64(rho_nm1)), _p(_f64(rho_n)), _p(_f64(rho_np1)),
+                                   float(dt), float(gamma1), float(gamma2), float(gamma3), int(bool(lumped)),
+                                   _p(lhs), _p(rhs))
+    return lhs.reshape(8, 8), rhs
+
+
+def momentum_mass_elem(coords, rho_nm1, rho_n, rho_np1, u_nm1, u_n, u_np1, gpdx, dt, gamma1=1.0, gamma2=-1.0,
+                       gamma3=0.0, lumped=False, balanced_force=False):
+    lhs, rhs = np.zeros(576), np.zeros(24)
+    lib().orc_momentum_mass_elem(_p(_f64(coords)), _p(_f64(rho_nm1)), _p(_f64(rho_n)), _p(_f64(rho_np1)),
+                                 _p(_f64(u_nm1)), _p(_f64(u_n)), _p(_f64(u_np1)), _p(_f64(gpdx)), float(dt),
+                                 float(gamma1), float(gamma2), float(gamma3), int(bool(lumped)),
+                                 int(bool(balanced_force)), _p(lhs), _p(rhs))
+    return lhs.reshape(24, 24), rhs
+
+
+def assemble_mass(momentum, coords, conn, rowptr, colind, lid, rho_nm1, rho_n, rho_np1, u_nm1=None, u_n=None,
+                  u_np1=None, gpdx=None, dt=1.0, gamma1=1.0, gamma2=-1.0, gamma3=0.0, lumped=False,
+                  balanced_force=False):
+    """Whole-mesh mass-term assembly (serial element order, restated sumInto)."""
+    values = np.zeros(colind.shape[0])
+    rhs = np.zeros(rowptr.shape[0] - 1)
+    conn = np.ascontiguousarray(conn, dtype=np.int32)
+    conv = lambda a: None if a is None else _f64(a)
+    tp = np.array([dt, gamma1, gamma2, gamma3, float(bool(lumped)), float(bool(balanced_force))])
+    rc = lib().orc_assemble_mass(int(bool(momentum)), coords.shape[0], conn.shape[0], _p(conn), _p(lid),
+                                 _p(_f64(coords)), _p(_f64(rho_nm1)), _p(_f64(rho_n)), _p(_f64(rho_np1)),
+                                 _p(conv(u_nm1)), _p(conv(u_n)), _p(conv(u_np1)), _p(conv(gpdx)), _p(tp),
+                                 _p(rowptr), _p(colind), _p(values), _p(rhs))
+    if rc:
+        raise RuntimeError("orc_assemble_mass: %d" % rc)
+    return values, rhs
 
 
 # ---- linear system ----------------------------------------------------------

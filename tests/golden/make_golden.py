@@ -101,6 +101,29 @@ def main(ref):
                              "at": [at_g, at_s, "unit_tests/UnitTestUtils.C:%d" % (usrc.count("\n", 0, k) + 1)]}
     g["hex8_scv_volume_unit_cube"] = {"volume": [0.125] * 8, "tol": 2.220446049250313e-16,
                                       "at": "unit_tests/UnitTestHexSCVDeterminant.C:60-75"}
+    # time terms: BDF1 with dt 0.1 (gamma 1, -1, 0); the fixtures fill state
+    # N+1 only (density 1, trig velocity / dpdx), state N stays 0
+    time = {"dt": 0.1, "gamma1": 1.0, "gamma2": -1.0, "gamma3": 0.0,
+            "fields": "density np1 = 1, n = nm1 = 0; velocity np1 = trig, n = nm1 = 0; dpdx = trig"}
+    csrc = open(os.path.join(ut, "kernels/UnitTestContinuityMassElem.C")).read()
+    for key, test in [("continuity_mass", "density_time_derivative)"),
+                      ("continuity_mass_lumped", "density_time_derivative_lumped)")]:
+        k = csrc.index(test)
+        m = re.compile(r"expect_all_near\(helperObjs\.linsys->rhs_,\s*([-+\d.eE]+)\)").search(csrc, k)
+        at = "unit_tests/kernels/UnitTestContinuityMassElem.C:%d" % (csrc.count("\n", 0, m.start()) + 1)
+        g[key] = dict(time, rhs=[float(m.group(1))] * 8, lhs=[0.0] * 64, at=at, tol=1.0e-15,
+                      lumped=key.endswith("lumped"))
+    rhs, at_r = grab("kernels/UnitTestMomentumMassElem.C", "rhs", "momentum_time_derivative")
+    lhs, at_l = grab("kernels/UnitTestMomentumMassElem.C", "lhs", "momentum_time_derivative")
+    assert len(rhs) == 24 and len(lhs) == 576
+    g["momentum_mass"] = dict(time, rhs=rhs, lhs=lhs, at=[at_r, at_l], tol=1.0e-15, lumped=False)
+    rhs, at_r = grab("kernels/UnitTestMomentumMassElem.C", "rhs", "momentum_time_derivative_lumped")
+    msrc = open(os.path.join(ut, "kernels/UnitTestMomentumMassElem.C")).read()
+    m = re.search(r"lhsExact\[i\*24\+i\]\s*=\s*([-+\d.eE]+)", msrc)
+    diag = float(m.group(1))
+    g["momentum_mass_lumped"] = dict(time, rhs=rhs, lhs=[diag if i % 25 == 0 else 0.0 for i in range(576)],
+                                     at=[at_r, "unit_tests/kernels/UnitTestMomentumMassElem.C:%d"
+                                         % (msrc.count("\n", 0, m.start()) + 1)], tol=1.0e-15, lumped=True)
     dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "nalu_unit_golds.json")
     with open(dst, "w") as f:
         json.dump(out, f, indent=1)

@@ -237,3 +237,55 @@ def test_nodal_grad_elem_exact_for_linear_fields(oracle):
     m = np.array([[1.0, 2.0, -0.5], [0.3, -1.1, 0.8], [2.2, 0.1, -0.7]])
     got = oracle.nodal_grad_elem(c, conn, c @ m.T, vol)
     assert np.max(np.abs(got[inner] - m[None])) <= 1e-12
+
+
+# ---------------------------------------------------------------------------
+# time terms (ContinuityMassElemKernel, MomentumMassElemKernel)
+# ---------------------------------------------------------------------------
+def mass_gold_inputs(c, conn):
+    """the kernel-test fixtures: state N+1 filled, states N and N-1 zero"""
+    e = conn[0]
+    z, one, z3 = np.zeros(8), np.ones(8), np.zeros((8, 3))
+    return dict(coords=c[e], rho=(z, z, one), u=(z3, z3, TrigFields.velocity(c)[e]), gpdx=TrigFields.dpdx(c)[e])
+
+
+@pytest.mark.parametrize("key", ["continuity_mass", "continuity_mass_lumped", "momentum_mass",
+                                 "momentum_mass_lumped"])
+def test_golds_mass(oracle, golds, key):
+    g = golds[key]
+    c, conn = _unit_cube_element()
+    f = mass_gold_inputs(c, conn)
+    t = (g["dt"], g["gamma1"], g["gamma2"], g["gamma3"])
+    if key.startswith("continuity"):
+        lhs, rhs = oracle.continuity_mass_elem(f["coords"], *f["rho"], *t, lumped=g["lumped"])
+    else:
+        lhs, rhs = oracle.momentum_mass_elem(f["coords"], *f["rho"], *f["u"], f["gpdx"], *t, lumped=g["lumped"])
+    assert np.max(np.abs(rhs - g["rhs"])) <= g["tol"], key
+    assert np.max(np.abs(lhs.ravel() - g["lhs"])) <= g["tol"], key
+
+
+def test_mass_assembly_matches_element_sum(oracle):
+    """orc_assemble_mass = per-element kernel + restated sumInto, BDF2 states"""
+    c, conn, gid = block_mesh(3, 2, 2, jitter=0.2, seed=6)
+    n = c.shape[0]
+    rng = np.random.default_rng(2)
+    rho = [1.0 + 0.1 * rng.random(n) for _ in range(3)]
+    u = [rng.standard_normal((n, 3)) for _ in range(3)]
+    gp = rng.standard_normal((n, 3))
+    t = dict(dt=0.05, gamma1=1.5, gamma2=-2.0, gamma3=0.5)
+    for mom, nd in ((False, 1), (True, 3)):
+        rp, ci, lid = oracle.graph(n, conn, nd, gid)
+        for lumped in (False, True):
+            v, r = oracle.assemble_mass(mom, c, conn, rp, ci, lid, *rho, *(u if mom else (None,) * 3),
+                                        gpdx=gp if mom else None, lumped=lumped, balanced_force=mom, **t)
+            v2, r2 = np.zeros_like(v), np.zeros_like(r)
+            for e in range(conn.shape[0]):
+                en = conn[e]
+                if mom:
+                    lhs, rhs = oracle.momentum_mass_elem(c[en], *[x[en] for x in rho], *[x[en] for x in u], gp[en],
+                                                         t["dt"], t["gamma1"], t["gamma2"], t["gamma3"], lumped, True)
+                else:
+                    lhs, rhs = oracle.continuity_mass_elem(c[en], *[x[en] for x in rho], t["dt"], t["gamma1"],
+                                                           t["gamma2"], t["gamma3"], lumped)
+                oracle.sum_into(nd, lid[en], lhs, rhs, rp, ci, v2, r2)
+            assert np.array_equal(v, v2) and np.array_equal(r, r2)
