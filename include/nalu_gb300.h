@@ -76,7 +76,10 @@ enum nalu_field {
   NALU_FIELD_DENSITY_NM1 = 13,  /* [n]    */
   NALU_FIELD_VELOCITY_N = 14,   /* [n][3] */
   NALU_FIELD_VELOCITY_NM1 = 15, /* [n][3] */
-  NALU_FIELD_COUNT = 16
+  /* boundary-condition fields of the face kernels */
+  NALU_FIELD_PRESSURE_BC = 16,  /* [n]    pressure_bc (open boundary) */
+  NALU_FIELD_VELOCITY_BC = 17,  /* [n][3] cont_velocity_bc (inflow boundary) */
+  NALU_FIELD_COUNT = 18
 };
 /* copy a field in (host or device source, caller node order) */
 int nalu_field_set(nalu_ctx* ctx, int field, const double* src, int64_t count, int src_is_device);
@@ -198,6 +201,52 @@ int nalu_capture_scv_volumes(nalu_ctx* ctx, int64_t elem, double* vol);
  * (AssembleNodalGradBoundaryAlgorithm) is not part of this call.
  * shifted: shifted_shape_fcn at the ips. */
 int nalu_compute_nodal_gradient(nalu_ctx* ctx, int src_field, int dst_field, int shifted);
+
+/* ---- boundary faces ------------------------------------------------------
+ * A side set is a list of element sides, as the mesh's boundary parts hold
+ * them: face k is side side[k] of element elem[k], with the Hex8 side
+ * numbering of HexSCS::sideNodeOrdinals_ (src/master_element/Hex8CVFEM.C:
+ * 415-422): 0 {0,1,5,4}, 1 {1,2,6,5}, 2 {2,3,7,6}, 3 {0,4,7,3}, 4 {0,3,2,1},
+ * 5 {4,5,6,7} (outward normals).  Face ip k sits at side node k
+ * (Quad3DSCS / HexSCS::ipNodeMap(side)). */
+#define NALU_MAX_FACE_SETS 16
+int nalu_faceset_define(nalu_ctx* ctx, int set, int64_t n, const int64_t* elem, const int32_t* side);
+/* the mesh's exposed sides (sides of exactly one element) as face set `set`,
+ * ordered by element then side; n_faces (may be NULL) receives the count */
+int nalu_faceset_skin(nalu_ctx* ctx, int set, int64_t* n_faces);
+int nalu_faceset_size(nalu_ctx* ctx, int set, int64_t* n_faces);
+int nalu_faceset_get(nalu_ctx* ctx, int set, int64_t* elem, int32_t* side);
+/* dynamic_pressure at the face ips, [n][4] host (ContinuityOpen's pbc offset);
+ * NULL clears it to zero */
+int nalu_faceset_dynamic_pressure(nalu_ctx* ctx, int set, const double* dynp);
+/* exposed_area_vector (ComputeGeometryBoundaryAlgorithm, Quad3DSCS::determinant
+ * = quad3d_scs_det, src/master_element/MasterElementWork.F:1467-1590) of the
+ * set's faces: area [n][4][3] (host), ip k at side node k */
+int nalu_faceset_exposed_area(nalu_ctx* ctx, int set, double* area);
+/* boundary closure of the projected nodal gradient over one side set
+ * (AssembleNodalGradBoundaryAlgorithm, src/AssembleNodalGradBoundaryAlgorithm.C:
+ * 75-153): dst[nn] += q_ip A_ip / V_nn, ADDED to a gradient made by
+ * nalu_compute_nodal_gradient with the same fields */
+int nalu_nodal_gradient_boundary(nalu_ctx* ctx, int set, int src_field, int dst_field, int shifted);
+enum nalu_face_kernel {
+  /* src/kernel/ContinuityInflowElemKernel.C: rhs -= rho u_bc . A / tau at
+   * the face nodes; reads DENSITY, VELOCITY_BC; shift_mdot selects the
+   * shifted face shape functions; tau = opts.proj_time_scale */
+  NALU_FACE_CONTINUITY_INFLOW = 0,
+  /* src/kernel/ContinuityOpenElemKernel.C: face-element kernel with the
+   * penalty 2 tau L^-1 (p - p_bc) |A| and the element pressure gradient at
+   * the exposed-face ips (HexSCS::face_grad_op); reads PRESSURE, PRESSURE_BC,
+   * DENSITY, VELOCITY, DPDX and the set's dynamic pressure; options
+   * shift_poisson, reduced_sens, shift_mdot as for ContinuityAdv */
+  NALU_FACE_CONTINUITY_OPEN = 1
+};
+/* run a face kernel over a side set and sum into the (numDof 1) system,
+ * rows of the face nodes, columns of the element's nodes */
+int nalu_assemble_faces(nalu_ctx* ctx, int set, int face_kernel, const nalu_assemble_opts* opts);
+/* face `face` of the set in mock-capture form: lhs [8][8], rhs [8] in the
+ * element's node order (rows of the side's four nodes filled) */
+int nalu_capture_face(nalu_ctx* ctx, int set, int face_kernel, const nalu_assemble_opts* opts, int64_t face,
+                      double* lhs, double* rhs);
 
 /* ---- linear solve (TpetraLinearSolver::solve, src/LinearSolver.C:183-232) */
 enum nalu_solver_method {

@@ -29,13 +29,16 @@ STATUS = {0: "ok", -1: "invalid argument", -2: "CUDA error", -3: "call out of or
 
 FIELD = {"coordinates": 0, "scalar_q": 1, "diff_coeff": 2, "velocity": 3, "velocity_rtm": 4,
          "density": 5, "pressure": 6, "dpdx": 7, "viscosity": 8, "dudx": 9, "mass_flow_rate_scs": 10,
-         "dual_nodal_volume": 11, "density_n": 12, "density_nm1": 13, "velocity_n": 14, "velocity_nm1": 15}
+         "dual_nodal_volume": 11, "density_n": 12, "density_nm1": 13, "velocity_n": 14, "velocity_nm1": 15,
+         "pressure_bc": 16, "cont_velocity_bc": 17}
 KERNEL_SCALAR_DIFF = 0
 KERNEL_CONTINUITY_ADV = 1
 KERNEL_MOMENTUM_ADV_DIFF = 2
 KERNEL_MOMENTUM_UPW_ADV_DIFF = 3
 KERNEL_CONTINUITY_MASS = 4
 KERNEL_MOMENTUM_MASS = 5
+FACE_CONTINUITY_INFLOW, FACE_CONTINUITY_OPEN = 0, 1
+MAX_FACE_SETS = 16
 SCATTER_AUTO, SCATTER_ATOMIC, SCATTER_COLOURED = 0, 1, 2
 ARITH_FP64, ARITH_DF64 = 0, 1
 SOLVER_CG, SOLVER_GMRES = 0, 1
@@ -121,6 +124,15 @@ def lib():
             "nalu_compute_dual_volume": (I, [P]),
             "nalu_capture_scv_volumes": (I, [P, I64, P]),
             "nalu_compute_nodal_gradient": (I, [P, I, I, I]),
+            "nalu_faceset_define": (I, [P, I, I64, P, P]),
+            "nalu_faceset_skin": (I, [P, I, ctypes.POINTER(I64)]),
+            "nalu_faceset_size": (I, [P, I, ctypes.POINTER(I64)]),
+            "nalu_faceset_get": (I, [P, I, P, P]),
+            "nalu_faceset_dynamic_pressure": (I, [P, I, P]),
+            "nalu_faceset_exposed_area": (I, [P, I, P]),
+            "nalu_nodal_gradient_boundary": (I, [P, I, I, I, I]),
+            "nalu_assemble_faces": (I, [P, I, I, P]),
+            "nalu_capture_face": (I, [P, I, I, P, I64, P, P]),
             "nalu_solver_opts_default": (None, [P]),
             "nalu_solve": (I, [P, P, P]),
             "nalu_solution_get": (I, [P, P, I]),
@@ -305,6 +317,56 @@ class Context:
     def compute_nodal_gradient(self, src, dst, shifted=False):
         self._check(lib().nalu_compute_nodal_gradient(self._h, FIELD[src], FIELD[dst], int(bool(shifted))),
                     "compute_nodal_gradient")
+
+    # boundary faces (side sets)
+    def faceset_define(self, set_id, elem, side):
+        e = np.ascontiguousarray(elem, np.int64)
+        sd = np.ascontiguousarray(side, np.int32)
+        if e.shape != sd.shape:
+            raise ValueError("elem and side differ in length")
+        self._check(lib().nalu_faceset_define(self._h, int(set_id), e.size, _ptr(e), _ptr(sd)), "faceset_define")
+
+    def faceset_skin(self, set_id):
+        n = ctypes.c_int64(0)
+        self._check(lib().nalu_faceset_skin(self._h, int(set_id), ctypes.byref(n)), "faceset_skin")
+        return n.value
+
+    def faceset_get(self, set_id):
+        n = ctypes.c_int64(0)
+        self._check(lib().nalu_faceset_size(self._h, int(set_id), ctypes.byref(n)), "faceset_size")
+        e = np.zeros(n.value, np.int64)
+        sd = np.zeros(n.value, np.int32)
+        self._check(lib().nalu_faceset_get(self._h, int(set_id), _ptr(e), _ptr(sd)), "faceset_get")
+        return e, sd
+
+    def faceset_dynamic_pressure(self, set_id, dynp=None):
+        d = None if dynp is None else np.ascontiguousarray(dynp, np.float64)
+        self._check(lib().nalu_faceset_dynamic_pressure(self._h, int(set_id), _ptr(d) if d is not None else None),
+                    "faceset_dynamic_pressure")
+
+    def faceset_exposed_area(self, set_id):
+        n = ctypes.c_int64(0)
+        self._check(lib().nalu_faceset_size(self._h, int(set_id), ctypes.byref(n)), "faceset_size")
+        a = np.zeros((n.value, 4, 3))
+        if n.value:
+            self._check(lib().nalu_faceset_exposed_area(self._h, int(set_id), _ptr(a)), "faceset_exposed_area")
+        return a
+
+    def nodal_gradient_boundary(self, set_id, src, dst, shifted=False):
+        self._check(lib().nalu_nodal_gradient_boundary(self._h, int(set_id), FIELD[src], FIELD[dst],
+                                                       int(bool(shifted))), "nodal_gradient_boundary")
+
+    def assemble_faces(self, set_id, kernel, opts=None):
+        opts = default_assemble_opts() if opts is None else opts
+        self._check(lib().nalu_assemble_faces(self._h, int(set_id), int(kernel), ctypes.byref(opts)),
+                    "assemble_faces")
+
+    def capture_face(self, set_id, kernel, face, opts=None):
+        opts = default_assemble_opts() if opts is None else opts
+        lhs, rhs = np.zeros((8, 8)), np.zeros(8)
+        self._check(lib().nalu_capture_face(self._h, int(set_id), int(kernel), ctypes.byref(opts), int(face),
+                                            _ptr(lhs), _ptr(rhs)), "capture_face")
+        return lhs, rhs
 
     # solve
     def solve(self, opts=None, raise_on_error=True):

@@ -46,10 +46,6 @@ int check_flags(nalu_ctx* ctx) {
   return NALU_OK;
 }
 
-}  // namespace nalu_gb300
-
-namespace {
-
 int field_comps(int f) {
   switch (f) {
     case NALU_FIELD_COORDINATES:
@@ -58,6 +54,7 @@ int field_comps(int f) {
     case NALU_FIELD_DPDX:
     case NALU_FIELD_VELOCITY_N:
     case NALU_FIELD_VELOCITY_NM1:
+    case NALU_FIELD_VELOCITY_BC:
       return 3;
     case NALU_FIELD_DUDX:
       return 9;
@@ -69,6 +66,11 @@ int field_comps(int f) {
       return 1;
   }
 }
+
+}  // namespace nalu_gb300
+
+namespace {
+
 
 template <class F>
 void parallel_ranges(int64_t n, F f) {
@@ -269,6 +271,7 @@ int nalu_mesh_create(nalu_ctx* ctx, int64_t n_nodes, int64_t n_elems, const int3
   ctx->num_dof = 0;
   ctx->learned.nbr_nodes = 0;  // the slot map belongs to the previous mesh
   ctx->problem_offsets.clear();
+  for (auto& fs : ctx->face_sets) fs.clear();  // side sets refer to the previous mesh's elements
   // LIDs: nodes sorted by global id (beginLinearSystemConstruction, :262-275)
   ctx->h_lid.assign(n_nodes, 0);
   ctx->identity_order = true;

@@ -96,6 +96,18 @@ struct SolverWork {
   int64_t n = 0;
 };
 
+// one side set: face k is side side[k] (0..5) of element elem[k]
+struct FaceSet {
+  DBuf<int32_t> elem;
+  DBuf<uint8_t> side;
+  DBuf<double> dynp;                  // [n][4] dynamic_pressure at the face ips, or empty (0)
+  std::vector<int32_t> h_elem;
+  std::vector<uint8_t> h_side;
+  int64_t n = 0;
+  bool defined = false;
+  void clear();
+};
+
 }  // namespace nalu_gb300
 
 struct nalu_ctx {
@@ -150,6 +162,9 @@ struct nalu_ctx {
 
   nalu_gb300::SolverWork sw;
   nalu_gb300::LearnedState learned;
+
+  // boundary side sets (nalu_faceset_define / nalu_faceset_skin)
+  nalu_gb300::FaceSet face_sets[NALU_MAX_FACE_SETS];
 };
 
 namespace nalu_gb300 {
@@ -157,6 +172,7 @@ namespace nalu_gb300 {
 enum FlagSlot { FLAG_NEG_JAC = 0, FLAG_GRAPH_MISS = 1, FLAG_CAPACITY = 2, FLAG_NONFINITE = 3 };
 
 int set_error(nalu_ctx* ctx, int status, const std::string& msg);
+int field_comps(int field);
 int cuda_check(nalu_ctx* ctx, cudaError_t e, const char* what);
 #define NALU_CUDA(ctx, call)                                      \
   do {                                                            \

@@ -18,6 +18,8 @@
 #include <limits>
 #include <thread>
 #include <vector>
+#include <map>
+#include <array>
 
 namespace {
 
@@ -1039,6 +1041,219 @@ int orc_assemble_mass(int momentum, int64_t n_nodes, int64_t n_elems, const int3
       orc_continuity_mass_elem(c, a, b, d, tp[0], tp[1], tp[2], tp[3], tp[4] != 0.0, lhs, erhs);
       sum_into(1, elid, lhs, erhs, rowptr, colind, values, rhs);
     }
+  }
+  return 0;
+}
+
+// ---- boundary faces -------------------------------------------------------
+static const int kSide[6][4] = {{0, 1, 5, 4}, {1, 2, 6, 5}, {2, 3, 7, 6}, {0, 4, 7, 3}, {0, 3, 2, 1}, {4, 5, 6, 7}};
+
+void orc_hex_side_nodes(int side, int* nodes4) {
+  for (int k = 0; k < 4; ++k) nodes4[k] = kSide[side][k];
+}
+
+// quad3d_scs_det (src/master_element/MasterElementWork.F:1467-1590)
+void orc_quad3d_scs_areav(const double* fc, double* areav) {
+  const double half = 0.5, one4th = 1.0 / 4.0;
+  double p[4][3], e[4][3], c[3];
+  for (int i = 0; i < 4; ++i)
+    for (int d = 0; d < 3; ++d) p[i][d] = fc[3 * i + d];
+  for (int d = 0; d < 3; ++d) {
+    e[0][d] = (p[0][d] + p[1][d]) * half;
+    e[1][d] = (p[1][d] + p[2][d]) * half;
+    e[2][d] = (p[2][d] + p[3][d]) * half;
+    e[3][d] = (p[3][d] + p[0][d]) * half;
+    c[d] = (p[0][d] + p[1][d] + p[2][d] + p[3][d]) * one4th;
+  }
+  for (int k = 0; k < 4; ++k) {
+    const int prev = (k + 3) % 4;  // sub-face k: corner p_k, edge midpoints e_{k-1}, e_k, centre c
+    const double dx13 = c[0] - p[k][0], dx24 = e[prev][0] - e[k][0];
+    const double dy13 = c[1] - p[k][1], dy24 = e[prev][1] - e[k][1];
+    const double dz13 = c[2] - p[k][2], dz24 = e[prev][2] - e[k][2];
+    areav[3 * k + 0] = half * (dz24 * dy13 - dz13 * dy24);
+    areav[3 * k + 1] = half * (dx24 * dz13 - dx13 * dz24);
+    areav[3 * k + 2] = half * (dy24 * dx13 - dy13 * dx24);
+  }
+}
+
+// HexSCS::face_grad_op (Hex8CVFEM.C:668-684); intgExpFace_ (:348-373): the
+// face node's parent location with the two in-plane coordinates halved;
+// intgExpFaceShift_ (:424-440): the face node itself
+int orc_hex_face_grad_op(int side, int shifted, const double* coords, double* gradop) {
+  static const double loc[8][3] = {{-0.5, -0.5, -0.5}, {0.5, -0.5, -0.5}, {0.5, 0.5, -0.5}, {-0.5, 0.5, -0.5},
+                                   {-0.5, -0.5, 0.5},  {0.5, -0.5, 0.5},  {0.5, 0.5, 0.5},  {-0.5, 0.5, 0.5}};
+  static const int normal_axis[6] = {1, 0, 1, 0, 2, 2};
+  double pts[12], deriv[96];
+  for (int k = 0; k < 4; ++k)
+    for (int d = 0; d < 3; ++d) {
+      const double x = loc[kSide[side][k]][d];
+      pts[3 * k + d] = (shifted || d == normal_axis[side]) ? x : 0.5 * x;
+    }
+  orc_hex8_derivative(4, pts, deriv);
+  return orc_generic_grad_op(4, deriv, coords, gradop, nullptr);
+}
+
+void orc_skin(int64_t n_elems, const int32_t* conn, uint8_t* flags) {
+  std::map<std::array<int32_t, 4>, int> count;
+  auto key = [&](int64_t e, int s) {
+    std::array<int32_t, 4> k;
+    for (int i = 0; i < 4; ++i) k[i] = conn[8 * e + kSide[s][i]];
+    std::sort(k.begin(), k.end());
+    return k;
+  };
+  for (int64_t e = 0; e < n_elems; ++e)
+    for (int s = 0; s < 6; ++s) ++count[key(e, s)];
+  for (int64_t e = 0; e < n_elems; ++e)
+    for (int s = 0; s < 6; ++s) flags[6 * e + s] = count[key(e, s)] == 1 ? 1 : 0;
+}
+
+// Quad3DSCS shape functions (quad3d_shape_fcn, MasterElementWork.F:3651-3700)
+// at intgLoc_ (Quad43DCVFEM.C:37-41) or intgLocShift_ (:44-48)
+static void quad_face_shape(int shifted, double shp[4][4]) {
+  const double a = shifted ? 0.5 : 0.25;
+  const double loc[4][2] = {{-a, -a}, {a, -a}, {a, a}, {-a, a}};
+  const double one4th = 1.0 / 4.0, half = 1.0 / 2.0;
+  for (int j = 0; j < 4; ++j) {
+    const double s1 = loc[j][0], s2 = loc[j][1];
+    shp[j][0] = one4th + half * (-s1 - s2) + s1 * s2;
+    shp[j][1] = one4th + half * (s1 - s2) - s1 * s2;
+    shp[j][2] = one4th + half * (s1 + s2) + s1 * s2;
+    shp[j][3] = one4th + half * (-s1 + s2) - s1 * s2;
+  }
+}
+
+static void face_area(int side, const double* coords, double* areav) {
+  double fc[12];
+  for (int k = 0; k < 4; ++k)
+    for (int d = 0; d < 3; ++d) fc[3 * k + d] = coords[3 * kSide[side][k] + d];
+  orc_quad3d_scs_areav(fc, areav);
+}
+
+void orc_nodal_grad_boundary(int64_t n_faces, const int32_t* face_elem, const int32_t* face_side,
+                             const int32_t* conn, const double* coords, const double* q, int ncomp,
+                             const double* dual_volume, int shifted, double* grad) {
+  double shp[4][4];
+  quad_face_shape(shifted, shp);
+  for (int64_t f = 0; f < n_faces; ++f) {
+    const int64_t e = face_elem[f];
+    const int s = face_side[f];
+    double c[24], a[12];
+    for (int n = 0; n < 8; ++n)
+      for (int d = 0; d < 3; ++d) c[3 * n + d] = coords[3 * (int64_t)conn[8 * e + n] + d];
+    face_area(s, c, a);
+    for (int ip = 0; ip < 4; ++ip) {
+      const int64_t nn = conn[8 * e + kSide[s][ip]];
+      const double inv_vol = 1.0 / dual_volume[nn];
+      for (int k = 0; k < ncomp; ++k) {
+        double qip = 0.0;
+        for (int ic = 0; ic < 4; ++ic) qip += shp[ip][ic] * q[(int64_t)conn[8 * e + kSide[s][ic]] * ncomp + k];
+        for (int j = 0; j < 3; ++j) grad[(nn * ncomp + k) * 3 + j] += qip * a[3 * ip + j] * inv_vol;
+      }
+    }
+  }
+}
+
+void orc_continuity_inflow_face(int side, const double* coords, const double* rho, const double* ubc,
+                                double proj_time_scale, int shifted, double* rhs) {
+  double shp[4][4], a[12];
+  quad_face_shape(shifted, shp);
+  face_area(side, coords, a);
+  for (int i = 0; i < 8; ++i) rhs[i] = 0.0;
+  for (int ip = 0; ip < 4; ++ip) {
+    const int nn = kSide[side][ip];
+    double w[3] = {0.0, 0.0, 0.0};
+    for (int ic = 0; ic < 4; ++ic) {
+      const double r = shp[ip][ic];
+      const double rhoIC = rho[kSide[side][ic]];
+      for (int j = 0; j < 3; ++j) w[j] += r * rhoIC * ubc[3 * kSide[side][ic] + j];
+    }
+    double mDot = 0.0;
+    for (int j = 0; j < 3; ++j) mDot += w[j] * a[3 * ip + j];
+    rhs[nn] -= mDot / proj_time_scale;
+  }
+}
+
+void orc_continuity_open_face(int side, const double* coords, const double* p, const double* pbc,
+                              const double* rho, const double* u, const double* gpdx, const double* dynp,
+                              double proj_time_scale, int shift_grad_op, int reduced_sens, int shift_mdot,
+                              double* lhs, double* rhs) {
+  const double penaltyFac = 2.0;
+  double shp[4][4], a[12], g_std[96], g_sh[96];
+  quad_face_shape(shift_mdot, shp);
+  face_area(side, coords, a);
+  orc_hex_face_grad_op(side, 0, coords, g_std);
+  orc_hex_face_grad_op(side, 1, coords, g_sh);
+  const double* dndx = shift_grad_op ? g_sh : g_std;
+  const double* dndx_lhs = (shift_grad_op || reduced_sens) ? g_sh : g_std;
+  for (int i = 0; i < 64; ++i) lhs[i] = 0.0;
+  for (int i = 0; i < 8; ++i) rhs[i] = 0.0;
+  const int* fn = kSide[side];
+  for (int ip = 0; ip < 4; ++ip) {
+    const int nn = fn[ip];
+    double w_rho_u[3] = {0, 0, 0}, w_gp[3] = {0, 0, 0}, w_dpdx[3] = {0, 0, 0};
+    double aMag = 0.0;
+    for (int j = 0; j < 3; ++j) aMag += a[3 * ip + j] * a[3 * ip + j];
+    aMag = std::sqrt(aMag);
+    double invL = 0.0;
+    for (int ic = 0; ic < 4; ++ic)
+      for (int j = 0; j < 3; ++j) invL += dndx[ip * 24 + fn[ic] * 3 + j] * a[3 * ip + j];
+    invL /= aMag;
+    double pBip = 0.0, pbcBip = -(dynp ? dynp[ip] : 0.0);
+    for (int ic = 0; ic < 4; ++ic) {
+      const double r = shp[ip][ic];
+      const double rhoIC = rho[fn[ic]];
+      pBip += r * p[fn[ic]];
+      pbcBip += r * pbc[fn[ic]];
+      for (int j = 0; j < 3; ++j) {
+        w_rho_u[j] += r * rhoIC * u[3 * fn[ic] + j];
+        w_gp[j] += r * gpdx[3 * fn[ic] + j];
+      }
+    }
+    for (int ic = 0; ic < 8; ++ic)
+      for (int j = 0; j < 3; ++j) w_dpdx[j] += dndx[ip * 24 + ic * 3 + j] * p[ic];
+    double mdot = penaltyFac * proj_time_scale * invL * (pBip - pbcBip) * aMag;
+    for (int j = 0; j < 3; ++j)
+      mdot += (w_rho_u[j] - proj_time_scale * (w_dpdx[j] - w_gp[j])) * a[3 * ip + j];
+    for (int ic = 0; ic < 4; ++ic) lhs[nn * 8 + fn[ic]] += shp[ip][ic] * penaltyFac * invL * aMag;
+    for (int ic = 0; ic < 8; ++ic) {
+      double lhsFac = 0.0;
+      for (int j = 0; j < 3; ++j) lhsFac += -dndx_lhs[ip * 24 + ic * 3 + j] * a[3 * ip + j];
+      lhs[nn * 8 + ic] += lhsFac;
+    }
+    rhs[nn] -= mdot / proj_time_scale;
+  }
+}
+
+int orc_assemble_faces(int kernel, int64_t n_faces, const int32_t* face_elem, const int32_t* face_side,
+                       const int32_t* conn, const int32_t* node_lid, const double* coords, const double* p,
+                       const double* pbc, const double* rho, const double* u, const double* gpdx,
+                       const double* dynp, const double* opts, const int64_t* rowptr, const int32_t* colind,
+                       double* values, double* rhs) {
+  for (int64_t f = 0; f < n_faces; ++f) {
+    const int64_t e = face_elem[f];
+    const int s = face_side[f];
+    double c[24], pe[8], pb[8], re[8], ue[24], ge[24], lhs[64], erhs[8];
+    int32_t elid[8];
+    for (int n = 0; n < 8; ++n) {
+      const int64_t i = conn[8 * e + n];
+      elid[n] = node_lid ? node_lid[i] : (int32_t)i;
+      pe[n] = p ? p[i] : 0.0;
+      pb[n] = pbc ? pbc[i] : 0.0;
+      re[n] = rho[i];
+      for (int d = 0; d < 3; ++d) {
+        c[3 * n + d] = coords[3 * i + d];
+        ue[3 * n + d] = u[3 * i + d];
+        ge[3 * n + d] = gpdx ? gpdx[3 * i + d] : 0.0;
+      }
+    }
+    if (kernel == 0) {
+      for (int i = 0; i < 64; ++i) lhs[i] = 0.0;
+      orc_continuity_inflow_face(s, c, re, ue, opts[0], opts[3] != 0.0, erhs);
+    } else {
+      orc_continuity_open_face(s, c, pe, pb, re, ue, ge, dynp ? dynp + 4 * f : nullptr, opts[0], opts[1] != 0.0,
+                               opts[2] != 0.0, opts[3] != 0.0, lhs, erhs);
+    }
+    sum_into(1, elid, lhs, erhs, rowptr, colind, values, rhs);
   }
   return 0;
 }

@@ -136,6 +136,51 @@ void orc_dual_volume(int64_t n_nodes, int64_t n_elems, const int32_t* conn, cons
 void orc_nodal_grad_elem(int64_t n_nodes, int64_t n_elems, const int32_t* conn, const double* coords,
                          const double* q, int ncomp, const double* dual_volume, int shifted, double* grad);
 
+/* --- boundary faces ---------------------------------------------------- */
+/* Hex8 side s (0..5) -> its four element-local nodes (HexSCS::sideNodeOrdinals_,
+ * src/master_element/Hex8CVFEM.C:415-422); the same table is the face ip ->
+ * node map HexSCS::ipNodeMap(face) (:380-392) */
+void orc_hex_side_nodes(int side, int* nodes4);
+/* Quad3DSCS::determinant = quad3d_scs_det (src/master_element/MasterElementWork.F:
+ * 1467-1590): the four sub-face area vectors of a quad, nodes in side order */
+void orc_quad3d_scs_areav(const double* fcoords /*[4][3]*/, double* areav /*[4][3]*/);
+/* HexSCS::face_grad_op / shifted_face_grad_op (Hex8CVFEM.C:668-684):
+ * hex8_derivative at the exposed-face ips of side `side` (intgExpFace_,
+ * :348-373; shifted: the face nodes) and generic_grad_op; returns the number of
+ * ips with det(J) <= tiny */
+int orc_hex_face_grad_op(int side, int shifted, const double* coords, double* gradop /*[4][8][3]*/);
+/* exposed faces: flags[6 e + s] = 1 when side s of element e is a face of no
+ * other element (conn holds node indices) */
+void orc_skin(int64_t n_elems, const int32_t* conn, uint8_t* flags);
+/* boundary closure of the projected nodal gradient
+ * (AssembleNodalGradBoundaryAlgorithm::execute, src/AssembleNodalGradBoundaryAlgorithm.C:
+ * 75-153): for every face ip, grad[nn] += q_ip A_ip / V_nn (nn the ip's node),
+ * ADDED to grad [n][ncomp][3]; faces in list order */
+void orc_nodal_grad_boundary(int64_t n_faces, const int32_t* face_elem, const int32_t* face_side,
+                             const int32_t* conn, const double* coords, const double* q, int ncomp,
+                             const double* dual_volume, int shifted, double* grad);
+/* ContinuityInflowElemKernel::execute (src/kernel/ContinuityInflowElemKernel.C:
+ * 73-108) on side `side` of one element, nodal inputs in element-node order;
+ * rows of the element: rhs[8] (no lhs) */
+void orc_continuity_inflow_face(int side, const double* coords, const double* rho,
+                                const double* velocity_bc /*[8][3]*/, double proj_time_scale,
+                                int shifted, double* rhs /*[8]*/);
+/* ContinuityOpenElemKernel::execute (src/kernel/ContinuityOpenElemKernel.C:
+ * 107-199), penaltyFac 2 (include/kernel/ContinuityOpenElemKernel.h:67); dynp
+ * the face's dynamic_pressure [4] (may be NULL = 0); lhs [8][8], rhs [8] */
+void orc_continuity_open_face(int side, const double* coords, const double* p, const double* pbc,
+                              const double* rho, const double* velocity, const double* gpdx,
+                              const double* dynp, double proj_time_scale, int shift_grad_op,
+                              int reduced_sens, int shift_mdot, double* lhs, double* rhs);
+/* face kernels over a face list, summed in list order through sumInto with
+ * the element's nodes (num_dof 1); kernel 0 inflow, 1 open; opts =
+ * {proj_time_scale, shift_grad_op, reduced_sens, shift_mdot}; dynp [nf][4] or NULL */
+int orc_assemble_faces(int kernel, int64_t n_faces, const int32_t* face_elem, const int32_t* face_side,
+                       const int32_t* conn, const int32_t* node_lid, const double* coords,
+                       const double* p, const double* pbc, const double* rho, const double* velocity,
+                       const double* gpdx, const double* dynp, const double* opts,
+                       const int64_t* rowptr, const int32_t* colind, double* values, double* rhs);
+
 /* --- solvers (FP64, stand-in for Belos/Ifpack2, unpinned) -------------- */
 void orc_spmv(int64_t n, const int64_t* rowptr, const int32_t* colind, const double* v,
               const double* x, double* y, int n_threads);

@@ -68,6 +68,19 @@ def lib():
             [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
         L.orc_assemble_mass.restype = ctypes.c_int
         L.orc_assemble_mass.argtypes = [ctypes.c_int, ctypes.c_int64, ctypes.c_int64] + [ctypes.c_void_p] * 15
+        L.orc_hex_side_nodes.argtypes = [ctypes.c_int, ctypes.c_void_p]
+        L.orc_quad3d_scs_areav.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.orc_hex_face_grad_op.restype = ctypes.c_int
+        L.orc_hex_face_grad_op.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+        L.orc_skin.argtypes = [ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p]
+        L.orc_nodal_grad_boundary.argtypes = [ctypes.c_int64] + [ctypes.c_void_p] * 5 + \
+            [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+        L.orc_continuity_inflow_face.argtypes = [ctypes.c_int] + [ctypes.c_void_p] * 3 + \
+            [ctypes.c_double, ctypes.c_int, ctypes.c_void_p]
+        L.orc_continuity_open_face.argtypes = [ctypes.c_int] + [ctypes.c_void_p] * 7 + \
+            [ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+        L.orc_assemble_faces.restype = ctypes.c_int
+        L.orc_assemble_faces.argtypes = [ctypes.c_int, ctypes.c_int64] + [ctypes.c_void_p] * 16
         L.orc_apply_dirichlet.argtypes = [ctypes.c_void_p] * 4 + [ctypes.c_int64] + [ctypes.c_void_p] * 3
         L.orc_reset_rows.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_int64, ctypes.c_void_p]
         L.orc_sum_into.argtypes = [ctypes.c_int] + [ctypes.c_void_p] * 7
@@ -200,6 +213,86 @@ def assemble_mass(momentum, coords, conn, rowptr, colind, lid, rho_nm1, rho_n, r
                                  _p(rowptr), _p(colind), _p(values), _p(rhs))
     if rc:
         raise RuntimeError("orc_assemble_mass: %d" % rc)
+    return values, rhs
+
+
+# ---- boundary faces ---------------------------------------------------------
+FACE_CONTINUITY_INFLOW = 0
+FACE_CONTINUITY_OPEN = 1
+
+
+def side_nodes(side):
+    out = np.zeros(4, np.int32)
+    lib().orc_hex_side_nodes(int(side), _p(out))
+    return out
+
+
+def quad_areav(fcoords):
+    out = np.zeros(12)
+    lib().orc_quad3d_scs_areav(_p(_f64(fcoords)), _p(out))
+    return out.reshape(4, 3)
+
+
+def face_grad_op(side, coords, shifted=False):
+    g = np.zeros(96)
+    nbad = lib().orc_hex_face_grad_op(int(side), int(bool(shifted)), _p(_f64(coords)), _p(g))
+    return g.reshape(4, 8, 3), nbad
+
+
+def skin(conn):
+    """(elem, side) pairs of the exposed faces, sorted by element then side"""
+    conn = np.ascontiguousarray(conn, np.int32)
+    flags = np.zeros(conn.shape[0] * 6, np.uint8)
+    lib().orc_skin(conn.shape[0], _p(conn), _p(flags))
+    idx = np.nonzero(flags)[0]
+    return (idx // 6).astype(np.int64), (idx % 6).astype(np.int32)
+
+
+def nodal_grad_boundary(coords, conn, face_elem, face_side, q, dual_volume, grad, shifted=False):
+    """adds the boundary closure into grad ([n,3] or [n,3,3]) in place"""
+    q = _f64(q)
+    ncomp = 1 if q.ndim == 1 else q.shape[1]
+    fe = np.ascontiguousarray(face_elem, np.int32)
+    fs = np.ascontiguousarray(face_side, np.int32)
+    assert grad.dtype == np.float64 and grad.flags.c_contiguous
+    lib().orc_nodal_grad_boundary(fe.shape[0], _p(fe), _p(fs), _p(np.ascontiguousarray(conn, np.int32)),
+                                  _p(_f64(coords)), _p(q), ncomp, _p(_f64(dual_volume)), int(bool(shifted)),
+                                  _p(grad))
+    return grad
+
+
+def continuity_inflow_face(side, coords, rho, ubc, proj_time_scale=1.0, shifted=False):
+    rhs = np.zeros(8)
+    lib().orc_continuity_inflow_face(int(side), _p(_f64(coords)), _p(_f64(rho)), _p(_f64(ubc)),
+                                     float(proj_time_scale), int(bool(shifted)), _p(rhs))
+    return np.zeros((8, 8)), rhs
+
+
+def continuity_open_face(side, coords, p, pbc, rho, u, gpdx, dynp=None, proj_time_scale=1.0, shift_grad_op=0,
+                         reduced_sens=0, shift_mdot=0):
+    lhs, rhs = np.zeros(64), np.zeros(8)
+    lib().orc_continuity_open_face(int(side), _p(_f64(coords)), _p(_f64(p)), _p(_f64(pbc)), _p(_f64(rho)),
+                                   _p(_f64(u)), _p(_f64(gpdx)), _p(None if dynp is None else _f64(dynp)),
+                                   float(proj_time_scale), int(shift_grad_op), int(reduced_sens), int(shift_mdot),
+                                   _p(lhs), _p(rhs))
+    return lhs.reshape(8, 8), rhs
+
+
+def assemble_faces(kernel, coords, conn, face_elem, face_side, rowptr, colind, lid, rho, velocity, p=None,
+                   pbc=None, gpdx=None, dynp=None, proj_time_scale=1.0, shift_grad_op=0, reduced_sens=0,
+                   shift_mdot=0):
+    values = np.zeros(colind.shape[0])
+    rhs = np.zeros(rowptr.shape[0] - 1)
+    fe = np.ascontiguousarray(face_elem, np.int32)
+    fs = np.ascontiguousarray(face_side, np.int32)
+    conv = lambda a: None if a is None else _f64(a)
+    o = np.array([proj_time_scale, shift_grad_op, reduced_sens, shift_mdot], np.float64)
+    rc = lib().orc_assemble_faces(int(kernel), fe.shape[0], _p(fe), _p(fs), _p(np.ascontiguousarray(conn, np.int32)),
+                                  _p(lid), _p(_f64(coords)), _p(conv(p)), _p(conv(pbc)), _p(_f64(rho)),
+                                  _p(_f64(velocity)), _p(conv(gpdx)), _p(conv(dynp)), _p(o), _p(rowptr), _p(colind),
+                                  _p(values), _p(rhs))
+    if rc:
+        raise RuntimeError("orc_assemble_faces: %d" % rc)
     return values, rhs
 
 

@@ -37,6 +37,18 @@ void ref_hex_scv_grad_op(const double* coords, int shifted, double* gradop, doub
   SharedMemView<DoubleType***> g(gradop, 8, 8, 3), d(deriv, 8, 8, 3);
   if (shifted) me.shifted_grad_op(c, g, d); else me.grad_op(c, g, d);
 }
+void ref_hex_face_grad_op(int side, int shifted, const double* coords, double* gradop) {
+  sierra::nalu::HexSCS me;
+  SharedMemView<DoubleType**> c(const_cast<double*>(coords), 8, 3);
+  SharedMemView<DoubleType***> g(gradop, 4, 8, 3);
+  if (shifted) me.shifted_face_grad_op(side, c, g); else me.face_grad_op(side, c, g);
+}
+void ref_hex_side_nodes(int side, int* nodes4) {
+  sierra::nalu::HexSCS me;
+  const int* o = me.side_node_ordinals(side);
+  const int* m = me.ipNodeMap(side);
+  for (int k = 0; k < 4; ++k) nodes4[k] = o[k], nodes4[4 + k] = m[k];
+}
 const int* ref_hex_scs_adjacent_nodes() {
   static sierra::nalu::HexSCS me;
   return me.adjacentNodes();

@@ -289,3 +289,103 @@ def test_mass_assembly_matches_element_sum(oracle):
                                                            t["gamma2"], t["gamma3"], lumped)
                 oracle.sum_into(nd, lid[en], lhs, rhs, rp, ci, v2, r2)
             assert np.array_equal(v, v2) and np.array_equal(r, r2)
+
+
+# ---------------------------------------------------------------------------
+# boundary faces
+# ---------------------------------------------------------------------------
+def test_face_tables_and_grad_op_equal_reference(oracle):
+    """side node ordinals, the face ip -> node map, and face_grad_op
+    (standard and shifted) bit for bit against the compiled reference"""
+    import ctypes
+    ref = oracle.ref()
+    if ref is None:
+        pytest.skip("reference master element not built here (oracle/_ref)")
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    for s in range(6):
+        t = np.zeros(8, np.int32)
+        ref.ref_hex_side_nodes(s, P(t))
+        assert np.array_equal(t[:4], oracle.side_nodes(s)) and np.array_equal(t[4:], oracle.side_nodes(s))
+    rng = np.random.default_rng(7)
+    for _ in range(100):
+        c = np.ascontiguousarray((BASE + 0.2 * rng.uniform(-1, 1, (8, 3))) * rng.uniform(0.01, 3) + rng.uniform(-2, 2, 3))
+        for s in range(6):
+            for sh in (0, 1):
+                g2 = np.zeros(96)
+                ref.ref_hex_face_grad_op(s, sh, P(c), P(g2))
+                assert np.array_equal(oracle.face_grad_op(s, c, sh)[0].ravel(), g2)
+
+
+def test_quad_areas(oracle):
+    rng = np.random.default_rng(3)
+    c, conn = _unit_cube_element()
+    e = conn[0]
+    outward = {0: [0, -1, 0], 1: [1, 0, 0], 2: [0, 1, 0], 3: [-1, 0, 0], 4: [0, 0, -1], 5: [0, 0, 1]}
+    for s in range(6):
+        a = oracle.quad_areav(c[e][oracle.side_nodes(s)])
+        assert np.allclose(a, 0.25 * np.array(outward[s])[None, :], atol=1e-16)
+    for _ in range(50):
+        p = rng.standard_normal((4, 3))
+        a = oracle.quad_areav(p)
+        # the four sub-faces tile the bilinear surface: sum = (p2 - p0) x (p3 - p1) / 2
+        assert np.allclose(a.sum(0), 0.5 * np.cross(p[2] - p[0], p[3] - p[1]), atol=1e-14)
+    # an element's six exposed faces close: their areas sum to zero
+    cj, connj, _ = block_mesh(1, 1, 1, jitter=0.0)
+    x = cj[connj[0]] + 0.15 * rng.uniform(-1, 1, (8, 3))
+    tot = sum(oracle.quad_areav(x[oracle.side_nodes(s)]).sum(0) for s in range(6))
+    assert np.max(np.abs(tot)) <= 1e-15
+
+
+def test_skin(oracle):
+    nx, ny, nz = 4, 3, 2
+    c, conn, _ = block_mesh(nx, ny, nz, jitter=0.2, seed=1)
+    fe, fs = oracle.skin(conn)
+    assert fe.shape[0] == 2 * (nx * ny + ny * nz + nz * nx)
+    lo, hi = c.min(0), c.max(0)
+    for e, s in zip(fe, fs):
+        x = c[conn[e][oracle.side_nodes(s)]]
+        assert np.any(np.all(np.isclose(x, lo[None, :]), axis=0) | np.all(np.isclose(x, hi[None, :]), axis=0))
+
+
+def test_nodal_gradient_with_closure_exact_everywhere(oracle):
+    """element part + boundary closure: Green-Gauss over every closed dual
+    volume, exact for a linear field on an affine mesh at all nodes"""
+    n = 3
+    c, conn, det = _affine_block(n)
+    vol = oracle.dual_volume(c, conn)
+    fe, fs = oracle.skin(conn)
+    g = np.array([0.7, -1.3, 2.1])
+    grad = oracle.nodal_grad_elem(c, conn, 0.4 + c @ g, vol)
+    oracle.nodal_grad_boundary(c, conn, fe, fs, 0.4 + c @ g, vol, grad)
+    assert np.max(np.abs(grad - g)) <= 1e-12
+    m = np.array([[1.0, 2.0, -0.5], [0.3, -1.1, 0.8], [2.2, 0.1, -0.7]])
+    grad = oracle.nodal_grad_elem(c, conn, c @ m.T, vol)
+    oracle.nodal_grad_boundary(c, conn, fe, fs, c @ m.T, vol, grad)
+    assert np.max(np.abs(grad - m[None])) <= 1e-12
+
+
+def test_continuity_face_kernels(oracle):
+    """inflow: sum of rhs = -rho U . (total face area) / tau; open with p = pbc
+    and the exact gradient on an affine mesh: mdot = rho u . A exactly, so the
+    open rhs equals the inflow rhs of the same velocity"""
+    n = 3
+    c, conn, _ = _affine_block(n, seed=9)
+    fe, fs = oracle.skin(conn)
+    U = np.array([0.3, -0.2, 0.5])
+    rho = np.full(c.shape[0], 1.2)
+    u = np.tile(U, (c.shape[0], 1))
+    gvec = np.array([0.4, 0.1, -0.3])
+    p = 1.0 + c @ gvec
+    gp = np.tile(gvec, (c.shape[0], 1))
+    tau = 0.25
+    for e, s in zip(fe[:12], fs[:12]):
+        x = c[conn[e]]
+        _, r_in = oracle.continuity_inflow_face(s, x, rho[conn[e]], u[conn[e]], tau)
+        a = oracle.quad_areav(x[oracle.side_nodes(s)])
+        assert abs(r_in.sum() + 1.2 * U @ a.sum(0) / tau) <= 1e-14
+        lhs, r_op = oracle.continuity_open_face(s, x, p[conn[e]], p[conn[e]], rho[conn[e]], u[conn[e]], gp[conn[e]],
+                                                proj_time_scale=tau)
+        assert np.max(np.abs(r_op - r_in)) <= 1e-13
+        # rows off the face stay empty; each face row: penalty part sums to 2 invL |A|, gradient part to 0
+        off = [k for k in range(8) if k not in oracle.side_nodes(s)]
+        assert np.all(lhs[off] == 0.0) and np.all(r_op[off] == 0.0)
