@@ -126,6 +126,14 @@ int nalu_linsys_copy(nalu_ctx* ctx, double* values, double* rhs, int dst_is_devi
 int nalu_linsys_copy_async(nalu_ctx* ctx, double* values, double* rhs);
 int nalu_linsys_copy_wait(nalu_ctx* ctx);
 
+/* MatrixMarket dumps (TpetraLinearSystem::writeToFile / writeSolutionToFile,
+ * src/TpetraLinearSystem.C:1967-2117): <base>-O-<count>.mm.1 (coordinate real
+ * general, 1-based global ids ndof (gid - 1) + idof + 1) and .rhs.1 (array);
+ * write_solution writes .sln.1 and advances count, as the reference's solve
+ * does after the solver returns (:1794-1817) */
+int nalu_linsys_write_system(nalu_ctx* ctx, const char* base);
+int nalu_linsys_write_solution(nalu_ctx* ctx, const char* base);
+
 /* ---- assembly (AssembleElemSolverAlgorithm::execute + Kernel::execute) --- */
 enum nalu_kernel {
   NALU_KERNEL_SCALAR_DIFF = 0,        /* src/kernel/ScalarDiffElemKernel.C */

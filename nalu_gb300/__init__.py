@@ -124,6 +124,8 @@ def lib():
             "nalu_compute_dual_volume": (I, [P]),
             "nalu_capture_scv_volumes": (I, [P, I64, P]),
             "nalu_compute_nodal_gradient": (I, [P, I, I, I]),
+            "nalu_linsys_write_system": (I, [P, ctypes.c_char_p]),
+            "nalu_linsys_write_solution": (I, [P, ctypes.c_char_p]),
             "nalu_faceset_define": (I, [P, I, I64, P, P]),
             "nalu_faceset_skin": (I, [P, I, ctypes.POINTER(I64)]),
             "nalu_faceset_size": (I, [P, I, ctypes.POINTER(I64)]),
@@ -317,6 +319,13 @@ class Context:
     def compute_nodal_gradient(self, src, dst, shifted=False):
         self._check(lib().nalu_compute_nodal_gradient(self._h, FIELD[src], FIELD[dst], int(bool(shifted))),
                     "compute_nodal_gradient")
+
+    # MatrixMarket dumps
+    def write_system(self, base):
+        self._check(lib().nalu_linsys_write_system(self._h, os.fsencode(base)), "write_system")
+
+    def write_solution(self, base):
+        self._check(lib().nalu_linsys_write_solution(self._h, os.fsencode(base)), "write_solution")
 
     # boundary faces (side sets)
     def faceset_define(self, set_id, elem, side):

@@ -274,6 +274,7 @@ int nalu_mesh_create(nalu_ctx* ctx, int64_t n_nodes, int64_t n_elems, const int3
   for (auto& fs : ctx->face_sets) fs.clear();  // side sets refer to the previous mesh's elements
   // LIDs: nodes sorted by global id (beginLinearSystemConstruction, :262-275)
   ctx->h_lid.assign(n_nodes, 0);
+  ctx->h_gid.resize(n_nodes);
   ctx->identity_order = true;
   if (gid) {
     std::vector<int64_t> order(n_nodes);
@@ -281,12 +282,14 @@ int nalu_mesh_create(nalu_ctx* ctx, int64_t n_nodes, int64_t n_elems, const int3
     std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return gid[a] < gid[b]; });
     for (int64_t k = 0; k < n_nodes; ++k) {
       ctx->h_lid[order[k]] = (int32_t)k;
+      ctx->h_gid[k] = gid[order[k]];
       if (order[k] != k) ctx->identity_order = false;
     }
     for (int64_t k = 1; k < n_nodes; ++k)
       if (gid[order[k]] == gid[order[k - 1]]) return set_error(ctx, NALU_ERR_ARG, "duplicate node global id");
   } else {
     std::iota(ctx->h_lid.begin(), ctx->h_lid.end(), 0);
+    std::iota(ctx->h_gid.begin(), ctx->h_gid.end(), (int64_t)1);
   }
   ctx->h_conn_lid.resize((size_t)n_elems * 8);
   for (int64_t i = 0; i < n_elems * 8; ++i) {

@@ -121,6 +121,8 @@ struct nalu_ctx {
   int64_t n_nodes = 0, n_elems = 0;
   bool identity_order = true;            // gid == index+1 for all nodes
   std::vector<int32_t> h_lid;            // caller node index -> LID
+  std::vector<int64_t> h_gid;            // LID -> node global id
+  int write_counter = 0;                 // TpetraLinearSystem::writeCounter_
   std::vector<int32_t> h_conn_lid;       // [E][8] in LID space (host copy)
   nalu_gb300::DBuf<int32_t> d_conn;      // [E][8] LIDs
   nalu_gb300::DBuf<int32_t> d_lid;       // caller index -> LID (device)
