@@ -14,9 +14,12 @@ Beside the headline number the line carries the other configurations:
 "solve" (Jacobi-PCG, FP32-inner + FP64 refinement and the learned flexible CG
 on the pinned 128^3 continuity system, plus "c4_192": plain vs learned at
 192^3), "batch" (64 independent meshes, problems/s), "momentum_c3" (96^3
-momentum assembly and the mixed-precision GMRES solve) and "heat_c1" (32^3
-heat conduction assembly and solves).  --no-solve / --no-batch / --no-c1 /
---no-c3 / --no-c4 skip them.
+momentum assembly, its time term and the mixed-precision GMRES solve),
+"heat_c1" (32^3 heat conduction assembly and solves) and
+"geometry_boundary_time" (dual volume, nodal gradients with the boundary
+closure, the continuity time term and the inflow/open face kernels on the
+headline mesh).  --no-solve / --no-batch / --no-c1 / --no-c3 / --no-c4 /
+--no-aux skip them.
 
 --impl reference times the reference's CPU algorithm (the oracle restatement
 of ContinuityAdvElemKernel + HexSCS + TpetraLinearSystem::sumInto, run on all
@@ -340,6 +343,7 @@ def bench_gpu(args):
         solve["learned_probe_vs_plain_time"] = solve["jacobi_pcg_fp64"]["ms"] / solve["learned_fcg_probe"]["ms"]
         if not args.no_c4:
             solve["c4_192"] = bench_c4(ng, learned_w, local)
+    aux = bench_aux(ng, ctx, c, conn, rho) if extras and not args.no_aux else None
     batch = bench_batch(ng, local) if extras and not args.no_batch else None
     momentum = bench_c3(ng, local) if extras and not args.no_c3 else None
     heat = bench_c1(ng, local) if extras and not args.no_c1 else None
@@ -372,7 +376,7 @@ def bench_gpu(args):
                          "kernel_ms": avg_ms, "fp64_probe_tflops": fp64_peak},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches, "clocks": clk.summary(), "cpu_baseline": cpu, "solve": solve,
-            "batch": batch, "momentum_c3": momentum, "heat_c1": heat}
+            "batch": batch, "momentum_c3": momentum, "heat_c1": heat, "geometry_boundary_time": aux}
     for a in list(pin_in.values()) + [out_v, out_r]:
         a.free()
     ctx.close()
@@ -381,6 +385,56 @@ def bench_gpu(args):
     if dist is not None:
         dist.destroy_process_group()
     return 0
+
+
+HEX_SIDES = ((0, 1, 5, 4), (1, 2, 6, 5), (2, 3, 7, 6), (0, 4, 7, 3), (0, 3, 2, 1), (4, 5, 6, 7))
+
+
+def timed_ms(ctx, fn, reps=5):
+    fn()  # warm-up
+    ms = []
+    for _ in range(reps):
+        ctx.event_record(0)
+        fn()
+        ctx.event_record(1)
+        ctx.synchronize()
+        ms.append(ctx.event_elapsed_ms(0, 1))
+    return statistics.median(ms)
+
+
+def bench_aux(ng, ctx, c, conn, rho):
+    """The rows on either side of the continuity assembly, on the same 128^3
+    mesh and context: dual nodal volume, the projected nodal gradient (element
+    part; boundary closure over the skin), the continuity time term, and the
+    inflow / open face kernels on the x = 0 / x = 1 sides."""
+    n = c.shape[0]
+    out = {"workload": "continuity_adv_hex8_128^3_zstretch1.05 mesh of the headline"}
+    out["dual_volume_ms"] = timed_ms(ctx, ctx.compute_dual_volume)
+    out["nodal_gradient_pressure_ms"] = timed_ms(ctx, lambda: ctx.compute_nodal_gradient("pressure", "dpdx"))
+    out["nodal_gradient_velocity_ms"] = timed_ms(ctx, lambda: ctx.compute_nodal_gradient("velocity", "dudx"))
+    t0 = time.perf_counter()
+    nf = ctx.faceset_skin(0)
+    out["skin_faces"] = nf
+    out["skin_extraction_s"] = time.perf_counter() - t0
+    out["gradient_closure_pressure_ms"] = timed_ms(ctx, lambda: ctx.nodal_gradient_boundary(0, "pressure", "dpdx"))
+    ctx.field_set("density_n", 0.99 * rho)
+    for lumped in (0, 1):
+        o = ng.default_assemble_opts(dt=1e-3, lumped_mass=lumped)
+        out["continuity_mass_%s_ms" % ("lumped" if lumped else "consistent")] = timed_ms(
+            ctx, lambda: ctx.assemble(ng.KERNEL_CONTINUITY_MASS, o))
+    fe, fs = ctx.faceset_get(0)
+    side_nodes = np.asarray(HEX_SIDES)[fs]                       # [nf, 4] element-local
+    xs = c[conn[fe[:, None], side_nodes], 0]                     # [nf, 4] x of the face nodes
+    for set_id, plane in ((1, 0.0), (2, 1.0)):
+        keep = np.all(np.abs(xs - plane) < 1e-12, axis=1)
+        ctx.faceset_define(set_id, fe[keep], fs[keep])
+        out["faces_x%d" % int(plane)] = int(keep.sum())
+    ctx.field_set("cont_velocity_bc", np.tile([1.0, 0.0, 0.0], (n, 1)))
+    ctx.field_set("pressure_bc", np.zeros(n))
+    o = ng.default_assemble_opts()
+    out["continuity_inflow_x0_ms"] = timed_ms(ctx, lambda: ctx.assemble_faces(1, ng.FACE_CONTINUITY_INFLOW, o))
+    out["continuity_open_x1_ms"] = timed_ms(ctx, lambda: ctx.assemble_faces(2, ng.FACE_CONTINUITY_OPEN, o))
+    return out
 
 
 def bench_c1(ng, dev=0, N=32, reps=5):
@@ -459,6 +513,18 @@ def bench_c3(ng, dev=0, N=96, reps=5):
                 ms.append(ctx.event_elapsed_ms(0, 1))
             out[name][an] = {"assemble_ms": statistics.median(ms),
                              "elements_per_s": conn.shape[0] / (statistics.median(ms) * 1e-3)}
+    # time term (MomentumMassElemKernel, BDF1)
+    ctx.field_set("density_n", np.ones(n))
+    ctx.field_set("velocity_n", 0.99 * u)
+    out["mass"] = {}
+    for lumped in (0, 1):
+        o = ng.default_assemble_opts(dt=1e-3, lumped_mass=lumped)
+        ms = timed_ms(ctx, lambda: ctx.assemble(ng.KERNEL_MOMENTUM_MASS, o), reps)
+        out["mass"]["lumped" if lumped else "consistent"] = {"assemble_ms": ms,
+                                                             "elements_per_s": conn.shape[0] / (ms * 1e-3)}
+    ctx.zero()
+    ctx.assemble(ng.KERNEL_MOMENTUM_UPW_ADV_DIFF,
+                 ng.default_assemble_opts(arith=ng.ARITH_DF64, alpha_upw=0.5, hybrid_factor=1.0))
     # system of the upwind-blended kernel, no-slip walls
     on_wall = np.any((c <= 1e-12) | (c >= 1.0 - 1e-12), axis=1)
     walls = np.nonzero(on_wall)[0]
@@ -610,6 +676,8 @@ def main():
     ap.add_argument("--no-c4", action="store_true", help="skip the 192^3 learned-vs-plain continuity solve")
     ap.add_argument("--no-c3", action="store_true", help="skip the 96^3 momentum assembly and solve")
     ap.add_argument("--no-c1", action="store_true", help="skip the 32^3 heat-conduction assembly and solve")
+    ap.add_argument("--no-aux", action="store_true",
+                    help="skip the geometry / gradient / time-term / face-kernel timings on the headline mesh")
     ap.add_argument("--size", type=int, default=128, help="elements per edge (default: the 128^3 workload)")
     ap.add_argument("--arith", default="auto", choices=["auto", "fp64", "df64"],
                     help="element-math arithmetic (auto: the faster; both pass the parity tests)")
