@@ -5,90 +5,66 @@
 // (subdivide_hex_8, Hex8GeometryFunctions.h:263-322), sub-hexahedron ip
 // holding node ip (ipNodeMap is the identity), and each volume is Grandy's
 // (hex_volume_grandy, Hex8GeometryFunctions.h:78-163): six face centroids and
-// 24 triangles whose signed contributions sum to 18 V.  Internal linkage: each
-// translation unit that includes it gets its own constant tables.
+// 24 triangles.  The same volume is evaluated here in a cheaper, equivalent
+// form (below); it differs from the reference's evaluation order only by
+// rounding, and is the closer of the two to the exact value (the reference's
+// corner-coordinate sums cancel by up to ~1e-14 relative on small elements
+// far from the origin).
 #pragma once
 #include <cstdint>
+
+#include "hex8_elem.h"
 
 namespace nalu_gb300 {
 namespace {
 
-// point k (0..26) of the 27-point subdivision, component d
-__device__ double subpoint(const double (*c)[3], int k, int d) {
-  auto m2 = [&](int a, int b) { return 0.5 * (c[a][d] + c[b][d]); };
-  auto m4 = [&](int a, int b, int e, int f) { return 0.25 * (c[a][d] + c[b][d] + c[e][d] + c[f][d]); };
-  switch (k) {
-    case 8: return m2(0, 1);
-    case 9: return m2(1, 2);
-    case 10: return m2(2, 3);
-    case 11: return m2(3, 0);
-    case 12: return m4(0, 1, 2, 3);
-    case 13: return m2(4, 5);
-    case 14: return m2(5, 6);
-    case 15: return m2(6, 7);
-    case 16: return m2(7, 4);
-    case 17: return m4(4, 5, 6, 7);
-    case 18: return m2(1, 5);
-    case 19: return m2(0, 4);
-    case 20: return m4(0, 1, 4, 5);
-    case 21: return m2(3, 7);
-    case 22: return m2(2, 6);
-    case 23: return m4(2, 3, 6, 7);
-    case 24: return m4(1, 2, 5, 6);
-    case 25: return m4(0, 3, 4, 7);
-    case 26: {
-      double s = 0.0;
-      for (int n = 0; n < 8; ++n) s += c[n][d];
-      return s * 0.125;
-    }
-    default: return c[k][d];
-  }
-}
-
-__constant__ int8_t c_sub[8][8] = {{0, 8, 12, 11, 19, 20, 26, 25},  {8, 1, 9, 12, 20, 18, 24, 26},
-                                   {12, 9, 2, 10, 26, 24, 22, 23},  {11, 12, 10, 3, 25, 26, 23, 21},
-                                   {19, 20, 26, 25, 4, 13, 17, 16}, {20, 18, 24, 26, 13, 5, 14, 17},
-                                   {26, 24, 22, 23, 17, 14, 6, 15}, {25, 26, 23, 21, 16, 17, 15, 7}};
-__constant__ int8_t c_gface[6][4] = {{0, 3, 2, 1}, {4, 5, 6, 7}, {0, 1, 5, 4}, {2, 3, 7, 6}, {1, 2, 6, 5}, {0, 4, 3, 7}};
-__constant__ int8_t c_gtri[24][3] = {{0, 8, 1},  {8, 2, 1},   {3, 2, 8},   {3, 8, 0},  {6, 9, 5},   {7, 9, 6},
-                                     {4, 9, 7},  {4, 5, 9},   {10, 0, 1},  {5, 10, 1}, {4, 10, 5},  {4, 0, 10},
-                                     {7, 6, 11}, {6, 2, 11},  {2, 3, 11},  {3, 7, 11}, {6, 12, 2},  {5, 12, 6},
-                                     {5, 1, 12}, {1, 2, 12},  {0, 4, 13},  {4, 7, 13}, {7, 3, 13},  {3, 0, 13}};
-
-// Grandy's hexahedron volume: six face centroids, 24 triangles
-__device__ double grandy_volume(const double (&h)[8][3]) {
-  double cv[14][3];
-#pragma unroll
-  for (int n = 0; n < 8; ++n)
-#pragma unroll
-    for (int d = 0; d < 3; ++d) cv[n][d] = h[n][d];
-#pragma unroll
-  for (int k = 0; k < 6; ++k)
-#pragma unroll
-    for (int d = 0; d < 3; ++d)
-      cv[k + 8][d] = 0.25 * (cv[c_gface[k][0]][d] + cv[c_gface[k][1]][d] + cv[c_gface[k][2]][d] + cv[c_gface[k][3]][d]);
-  double volume = 0.0;
-#pragma unroll
-  for (int k = 0; k < 24; ++k) {
-    const int p = c_gtri[k][0], q = c_gtri[k][1], r = c_gtri[k][2];
-    const double m0 = cv[p][0] + cv[q][0] + cv[r][0], m1 = cv[p][1] + cv[q][1] + cv[r][1],
-                 m2 = cv[p][2] + cv[q][2] + cv[r][2];
-    const double d0 = (cv[q][1] - cv[p][1]) * (cv[r][2] - cv[p][2]) - (cv[r][1] - cv[p][1]) * (cv[q][2] - cv[p][2]);
-    const double d1 = (cv[r][0] - cv[p][0]) * (cv[q][2] - cv[p][2]) - (cv[q][0] - cv[p][0]) * (cv[r][2] - cv[p][2]);
-    const double d2 = (cv[q][0] - cv[p][0]) * (cv[r][1] - cv[p][1]) - (cv[r][0] - cv[p][0]) * (cv[q][1] - cv[p][1]);
-    volume += m0 * d0 + m1 * d1 + m2 * d2;
-  }
-  return volume / 18.0;
-}
-
-// volume of sub-control volume ip of the element with corners c
+// Volume of sub-control volume ip: the sub-hexahedron between node ip's
+// corner and the parent centre, whose corners are node ip, the three edge
+// midpoints, the three face centroids at that node and the element centroid
+// (points of subdivide_hex_8).  Grandy's volume of a hexahedron (its faces
+// triangulated through their centroids) equals, summed face by face,
+//   V = sum_faces ((c - a) x (d - b)) . (a + b + c + d) / 24
+// (each face (a,b,c,d) contributes (a x b + b x c + c x d + d x a) . centroid / 6
+// and a x b + b x c + c x d + d x a = (c - a) x (d - b)), evaluated here about
+// the element centroid, which keeps the cancellation of the corner terms
+// small.  The sub-box is labelled in a frame mirrored so that node ip's side
+// is "high" on every axis; each mirrored axis flips the orientation, hence the
+// sign s0 s1 s2.  Corner k of that frame has the middle on the axes where
+// corner_sign(k, .) < 0.
 __device__ inline double scv_volume(const double (*c)[3], int ip) {
+  const int s0 = corner_sign(ip, 0), s1 = corner_sign(ip, 1), s2 = corner_sign(ip, 2);
+  const int nx = node_of(-s0, s1, s2), ny = node_of(s0, -s1, s2), nz = node_of(s0, s1, -s2);
+  const int nxy = node_of(-s0, -s1, s2), nxz = node_of(-s0, s1, -s2), nyz = node_of(s0, -s1, -s2);
   double h[8][3];
 #pragma unroll
-  for (int n = 0; n < 8; ++n)
+  for (int d = 0; d < 3; ++d) {
+    const double xb = ((c[0][d] + c[1][d]) + (c[2][d] + c[3][d]) + ((c[4][d] + c[5][d]) + (c[6][d] + c[7][d]))) * 0.125;
+    const double y0 = c[ip][d] - xb, yx = c[nx][d] - xb, yy = c[ny][d] - xb, yz = c[nz][d] - xb;
+    const double yxy = c[nxy][d] - xb, yxz = c[nxz][d] - xb, yyz = c[nyz][d] - xb;
+    h[0][d] = 0.0;                                   // centre
+    h[1][d] = ((y0 + yy) + (yz + yyz)) * 0.25;       // y, z middle: face centroid normal to x
+    h[2][d] = (y0 + yz) * 0.5;                       // z middle: edge midpoint
+    h[3][d] = ((y0 + yx) + (yz + yxz)) * 0.25;       // x, z middle
+    h[4][d] = ((y0 + yx) + (yy + yxy)) * 0.25;       // x, y middle
+    h[5][d] = (y0 + yy) * 0.5;                       // y middle
+    h[6][d] = y0;                                    // node ip
+    h[7][d] = (y0 + yx) * 0.5;                       // x middle
+  }
+  constexpr int kF[6][4] = {{0, 1, 5, 4}, {1, 2, 6, 5}, {2, 3, 7, 6}, {0, 4, 7, 3}, {0, 3, 2, 1}, {4, 5, 6, 7}};
+  double v = 0.0;
 #pragma unroll
-    for (int d = 0; d < 3; ++d) h[n][d] = subpoint(c, c_sub[ip][n], d);
-  return grandy_volume(h);
+  for (int f = 0; f < 6; ++f) {
+    const double* a = h[kF[f][0]];
+    const double* b = h[kF[f][1]];
+    const double* cc = h[kF[f][2]];
+    const double* dd = h[kF[f][3]];
+    const double p0 = cc[0] - a[0], p1 = cc[1] - a[1], p2 = cc[2] - a[2];
+    const double q0 = dd[0] - b[0], q1 = dd[1] - b[1], q2 = dd[2] - b[2];
+    const double m0 = (a[0] + b[0]) + (cc[0] + dd[0]), m1 = (a[1] + b[1]) + (cc[1] + dd[1]),
+                 m2 = (a[2] + b[2]) + (cc[2] + dd[2]);
+    v += (p1 * q2 - p2 * q1) * m0 + (p2 * q0 - p0 * q2) * m1 + (p0 * q1 - p1 * q0) * m2;
+  }
+  return (s0 * s1 * s2) * v * (1.0 / 24.0);
 }
 
 }  // namespace

@@ -3,7 +3,12 @@ dual_nodal_volume (HexSCV::determinant scattered to the nodes) and the element
 part of the projected nodal gradient (AssembleNodalGradElemAlgorithm and its
 velocity form).  The device sums element contributions with atomics, so the
 order of the (at most 8 per node) additions varies: tolerance
-|a - b| <= 1e-13 max|b| for the gradient, 1e-14 relative for volumes."""
+|a - b| <= 1e-13 max|b| for the gradient.  Volumes: 1e-13 relative.  The
+device evaluates Grandy's volume in its face form about the element centroid;
+the reference's corner-coordinate form (which the oracle reproduces bit for
+bit) carries up to ~1e-14 relative rounding of its own on small elements away
+from the origin, the face form ~5e-16 (checked against exact rational
+arithmetic)."""
 import numpy as np
 import pytest
 
@@ -31,7 +36,7 @@ def test_dual_volume(gpu_ctx_factory, oracle, case):
     ctx.compute_dual_volume()
     got = ctx.field_get("dual_nodal_volume", (c.shape[0],))
     ref = oracle.dual_volume(c, conn)
-    assert np.all(np.abs(got - ref) <= 1e-14 * np.abs(ref))
+    assert np.all(np.abs(got - ref) <= 1e-13 * np.abs(ref))
     for e in sorted({0, conn.shape[0] // 2, conn.shape[0] - 1}):
         v = ctx.capture_scv_volumes(e)
         assert np.max(np.abs(v - oracle.scv_volume(c[conn[e]]))) <= 1e-15 * max(1.0, np.max(np.abs(v)))
