@@ -76,7 +76,10 @@ __device__ void scs_area(const EdgeForm& f, int ip, double area[3]) {
   for (int i = 0; i < 3; ++i) area[i] = sc * (d == 0 ? adj[i][0] : (d == 1 ? adj[i][1] : adj[i][2]));
 }
 
-// projected nodal gradient, element part; q [n][NC], grad [n][NC][3]
+// projected nodal gradient, element part; q [n][NC], grad [n][NC][3].  The
+// twelve SCS area vectors are formed once; per component, the three SCS
+// contributions of each node are summed in registers (q_ip A, + to the left
+// node, - to the right) and leave as 8 x 3 atomics, scaled by 1/V of the node.
 template <int NC, bool SHIFT>
 __global__ void __launch_bounds__(128) k_nodal_grad(int64_t n_elems, const int32_t* __restrict__ conn,
                                                     const double* __restrict__ x, const double* __restrict__ q,
@@ -84,35 +87,50 @@ __global__ void __launch_bounds__(128) k_nodal_grad(int64_t n_elems, const int32
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= n_elems) return;
   int nd[8];
-  double xc[8][3], qn[8][NC], inv[8];
+  double xc[8][3];
 #pragma unroll
   for (int n = 0; n < 8; ++n) {
     nd[n] = __ldg(conn + 8 * e + n);
 #pragma unroll
     for (int d = 0; d < 3; ++d) xc[n][d] = __ldg(x + 3 * (int64_t)nd[n] + d);
-#pragma unroll
-    for (int k = 0; k < NC; ++k) qn[n][k] = __ldg(q + (int64_t)nd[n] * NC + k);
-    inv[n] = 1.0 / __ldg(dvol + nd[n]);
   }
-  EdgeForm f;
-  edge_form(xc, f);
-  const double a = SHIFT ? 0.5 : 0.25;
-#pragma unroll 1
-  for (int ip = 0; ip < 12; ++ip) {
-    double area[3];
-    scs_area(f, ip, area);
-    const int il = ip_left(ip), ir = ip_right(ip);
+  double area[12][3];
+  {
+    EdgeForm f;
+    edge_form(xc, f);
 #pragma unroll
-    for (int k = 0; k < NC; ++k) {
+    for (int ip = 0; ip < 12; ++ip) scs_area(f, ip, area[ip]);
+  }
+  constexpr double a = SHIFT ? 0.5 : 0.25;
+#pragma unroll 1
+  for (int k = 0; k < NC; ++k) {
+    double qn[8], acc[8][3];
+#pragma unroll
+    for (int n = 0; n < 8; ++n) {
+      qn[n] = __ldg(q + (int64_t)nd[n] * NC + k);
+      acc[n][0] = acc[n][1] = acc[n][2] = 0.0;
+    }
+#pragma unroll
+    for (int ip = 0; ip < 12; ++ip) {
       double qip = 0.0;
 #pragma unroll
-      for (int c = 0; c < 8; ++c) qip += shape(c, ip_loc(ip, 0, a), ip_loc(ip, 1, a), ip_loc(ip, 2, a)) * qn[c][k];
+      for (int c = 0; c < 8; ++c) {
+        const double w = shape_ip(ip, c, a);
+        if (w != 0.0) qip += w * qn[c];
+      }
+      const int il = ip_left(ip), ir = ip_right(ip);
 #pragma unroll
       for (int j = 0; j < 3; ++j) {
-        const double fac = qip * area[j];
-        atomicAdd(grad + ((int64_t)nd[il] * NC + k) * 3 + j, fac * inv[il]);
-        atomicAdd(grad + ((int64_t)nd[ir] * NC + k) * 3 + j, -fac * inv[ir]);
+        const double fac = qip * area[ip][j];
+        acc[il][j] += fac;
+        acc[ir][j] -= fac;
       }
+    }
+#pragma unroll
+    for (int n = 0; n < 8; ++n) {
+      const double inv = 1.0 / __ldg(dvol + nd[n]);
+#pragma unroll
+      for (int j = 0; j < 3; ++j) atomicAdd(grad + ((int64_t)nd[n] * NC + k) * 3 + j, acc[n][j] * inv);
     }
   }
 }
