@@ -272,6 +272,7 @@ int nalu_mesh_create(nalu_ctx* ctx, int64_t n_nodes, int64_t n_elems, const int3
   ctx->learned.nbr_nodes = 0;  // the slot map belongs to the previous mesh
   ctx->problem_offsets.clear();
   for (auto& fs : ctx->face_sets) fs.clear();  // side sets refer to the previous mesh's elements
+  ++ctx->coords_version;
   // LIDs: nodes sorted by global id (beginLinearSystemConstruction, :262-275)
   ctx->h_lid.assign(n_nodes, 0);
   ctx->h_gid.resize(n_nodes);
@@ -335,6 +336,7 @@ int nalu_field_set(nalu_ctx* ctx, int field, const double* src, int64_t count, i
     if (rc) return rc;
   }
   f.set = true;
+  if (field == NALU_FIELD_COORDINATES) ++ctx->coords_version;
   return NALU_OK;
 }
 

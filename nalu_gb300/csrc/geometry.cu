@@ -30,10 +30,11 @@ namespace {
 
 constexpr int kVolElems = 16;  // elements per block, 8 threads each
 
-// vol (node field) += sub-control volumes; cap (optional, one element) gets the eight volumes
+// vol (node field, optional) += sub-control volumes; scv (optional) [E][8]
+// gets them per element; cap (one element) gets its eight volumes
 __global__ void __launch_bounds__(kVolElems * 8) k_dual_volume(int64_t n_elems, const int32_t* __restrict__ conn,
                                                                const double* __restrict__ x, double* vol,
-                                                               int64_t cap_elem, double* cap) {
+                                                               double* scv_out, int64_t cap_elem, double* cap) {
   __shared__ double sc[kVolElems][8][3];
   const int el = threadIdx.x / 8, scv = threadIdx.x % 8;
   const int64_t e = cap_elem >= 0 ? cap_elem : (int64_t)blockIdx.x * kVolElems + el;
@@ -47,8 +48,12 @@ __global__ void __launch_bounds__(kVolElems * 8) k_dual_volume(int64_t n_elems, 
   __syncthreads();
   if (!valid) return;
   const double v = scv_volume(sc[el], scv);
-  if (cap) cap[scv] = v;
-  else atomicAdd(vol + node, v);
+  if (cap) {
+    cap[scv] = v;
+    return;
+  }
+  if (scv_out) scv_out[8 * e + scv] = v;
+  if (vol) atomicAdd(vol + node, v);
 }
 
 // SCS area vector of ip (runtime index): +-1/4 of a cofactor column of J at
@@ -145,15 +150,28 @@ __global__ void k_zero(int64_t n, double* p) {
 int launch_dual_volume(nalu_ctx* ctx, double* vol, int64_t cap_elem, double* cap) {
   const int64_t E = ctx->n_elems;
   if (E <= 0 || ctx->n_nodes <= 0) return NALU_OK;
+  double* scv_out = nullptr;
   if (cap_elem < 0) {
-    k_zero<<<(unsigned)((ctx->n_nodes + 255) / 256), 256, 0, ctx->stream>>>(ctx->n_nodes, vol);
-    ctx->launches++;
+    if (vol) {
+      k_zero<<<(unsigned)((ctx->n_nodes + 255) / 256), 256, 0, ctx->stream>>>(ctx->n_nodes, vol);
+      ctx->launches++;
+    }
+    // the per-element volumes refresh the cache on the way
+    if (ctx->d_scv.n != 8 * E) NALU_CUDA(ctx, ctx->d_scv.alloc(8 * E));
+    scv_out = ctx->d_scv.p;
   }
   const unsigned grid = cap_elem >= 0 ? 1u : (unsigned)((E + kVolElems - 1) / kVolElems);
   k_dual_volume<<<grid, kVolElems * 8, 0, ctx->stream>>>(E, ctx->d_conn.p, ctx->fields[NALU_FIELD_COORDINATES].d.p,
-                                                          vol, cap_elem, cap);
+                                                          vol, scv_out, cap_elem, cap);
   ctx->launches++;
-  return cuda_check(ctx, cudaGetLastError(), "dual volume");
+  const int rc = cuda_check(ctx, cudaGetLastError(), "dual volume");
+  if (rc == NALU_OK && scv_out) ctx->scv_version = ctx->coords_version;
+  return rc;
+}
+
+int ensure_scv_cache(nalu_ctx* ctx) {
+  if (ctx->scv_version == ctx->coords_version && ctx->d_scv.n == 8 * ctx->n_elems) return NALU_OK;
+  return launch_dual_volume(ctx, nullptr, -1, nullptr);
 }
 
 int launch_nodal_grad(nalu_ctx* ctx, const double* q, int ncomp, const double* dvol, double* grad, bool shifted) {

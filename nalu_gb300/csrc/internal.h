@@ -167,6 +167,11 @@ struct nalu_ctx {
 
   // boundary side sets (nalu_faceset_define / nalu_faceset_skin)
   nalu_gb300::FaceSet face_sets[NALU_MAX_FACE_SETS];
+
+  // HexSCV volumes [E][8], kept while the coordinates do not change
+  // (coords_version counts coordinate uploads)
+  nalu_gb300::DBuf<double> d_scv;
+  int64_t coords_version = 0, scv_version = -1;
 };
 
 namespace nalu_gb300 {
@@ -196,6 +201,8 @@ int launch_slot_table(nalu_ctx* ctx);
 int launch_mass(nalu_ctx* ctx, int kernel, const nalu_assemble_opts& o, int scatter, int64_t cap_elem,
                 double* cap_lhs, double* cap_rhs);
 int launch_dual_volume(nalu_ctx* ctx, double* vol, int64_t cap_elem, double* cap);
+// make d_scv hold the current coordinates' SCV volumes
+int ensure_scv_cache(nalu_ctx* ctx);
 int launch_nodal_grad(nalu_ctx* ctx, const double* q, int ncomp, const double* dvol, double* grad, bool shifted);
 int launch_expand_graph(nalu_ctx* ctx);
 int launch_sum_into(nalu_ctx* ctx, int64_t n, const int64_t* d_elems, const double* d_lhs,

@@ -15,8 +15,10 @@
 // is formed from separately interpolated factors, as the reference does.
 //
 // Layout: 16 elements per 128-thread block, thread = (element, ip).  The
-// element's corners and nodal states go to shared memory, the thread computes
-// its SCV volume (Grandy), interpolates, and scatters its row: for continuity
+// element's nodal states go to shared memory; the SCV volume comes from the
+// context's per-element volume cache (HexSCV::determinant of the current
+// coordinates, refreshed when they change); the thread interpolates and
+// scatters its row: for continuity
 // only the rhs entry, for momentum 3 rows x 8 (lumped: 1) diagonal-block
 // entries through the per-element slot table, FP64 atomics or, per colour,
 // plain adds.
@@ -25,7 +27,6 @@
 #include <cstdint>
 
 #include "internal.h"
-#include "scv.cuh"
 
 namespace nalu_gb300 {
 namespace {
@@ -34,9 +35,9 @@ constexpr int kMassElems = 16;
 
 struct MassArgs {
   const int32_t* conn;
+  const double* scv;     // [E][8] HexSCV volumes
   const int32_t* elems;  // element list of one colour, or null (all elements)
   int64_t count;
-  const double* x;
   const double* rho[3];  // states N-1, N, N+1
   const double* u[3];
   const double* gjp;
@@ -64,7 +65,6 @@ __device__ __forceinline__ double scv_weight(int ip, int c) {
 
 template <bool MOM, bool LUMPED, int OUT>
 __global__ void __launch_bounds__(kMassElems * 8) k_assemble_mass(MassArgs a) {
-  __shared__ double s_x[kMassElems][8][3];
   __shared__ double s_rho[kMassElems][3][8];
   __shared__ double s_u[MOM ? kMassElems : 1][3][8][3];
   __shared__ double s_g[MOM ? kMassElems : 1][8][3];
@@ -76,8 +76,6 @@ __global__ void __launch_bounds__(kMassElems * 8) k_assemble_mass(MassArgs a) {
   if (valid) {
     e = OUT == 2 ? a.cap_elem : (a.elems ? __ldg(a.elems + k) : k);
     node = __ldg(a.conn + 8 * e + ip);
-#pragma unroll
-    for (int d = 0; d < 3; ++d) s_x[el][ip][d] = __ldg(a.x + 3 * (int64_t)node + d);
 #pragma unroll
     for (int t = 0; t < 3; ++t) s_rho[el][t][ip] = __ldg(a.rho[t] + node);
     if (MOM) {
@@ -91,7 +89,7 @@ __global__ void __launch_bounds__(kMassElems * 8) k_assemble_mass(MassArgs a) {
   }
   __syncthreads();
   if (!valid) return;
-  const double scV = scv_volume(s_x[el], ip);
+  const double scV = __ldg(a.scv + 8 * e + ip);
   double r[3] = {0.0, 0.0, 0.0}, uu[3][3] = {}, g[3] = {0.0, 0.0, 0.0};
   if (LUMPED) {
 #pragma unroll
@@ -188,9 +186,11 @@ void launch_out(nalu_ctx* ctx, bool mom, bool lumped, const MassArgs& a, int64_t
 int launch_mass(nalu_ctx* ctx, int kernel, const nalu_assemble_opts& o, int scatter, int64_t cap_elem,
                 double* cap_lhs, double* cap_rhs) {
   const bool mom = kernel == NALU_KERNEL_MOMENTUM_MASS;
+  int rc = ensure_scv_cache(ctx);
+  if (rc) return rc;
   MassArgs a{};
   a.conn = ctx->d_conn.p;
-  a.x = ctx->fields[NALU_FIELD_COORDINATES].d.p;
+  a.scv = ctx->d_scv.p;
   const Field& rn = ctx->fields[NALU_FIELD_DENSITY_N];
   const Field& rnm1 = ctx->fields[NALU_FIELD_DENSITY_NM1];
   a.rho[0] = rnm1.set ? rnm1.d.p : rn.d.p;

@@ -142,3 +142,29 @@ def test_mass_errors(gpu_ctx_factory):
     _, rhs = ctx.system()
     assert np.max(np.abs(rhs)) == 0.0             # rho^{n+1} = rho^n: no time term
     ctx.close()
+
+
+def test_mass_follows_moved_coordinates(gpu_ctx_factory, oracle):
+    """the SCV volumes are kept per element between calls; new coordinates
+    (mesh motion) must reach the next time term"""
+    c, conn, gid = block_mesh(5, 4, 3, jitter=0.2, seed=3)
+    n = c.shape[0]
+    rho, _, _ = _states(n, 1)
+    ctx = _ctx(gpu_ctx_factory, c, conn, gid)
+    ctx.field_set("density_n", rho[1])
+    ctx.field_set("density", rho[2])
+    ctx.build_elem_graph(1)
+    rp, ci = ctx.graph()
+    _, _, lid = oracle.graph(n, conn, 1, gid)
+    o = ng.default_assemble_opts(dt=0.1, scatter=ng.SCATTER_ATOMIC)
+    for scale in (1.0, 1.7, 0.6):
+        moved = c * np.array([scale, 1.0, 1.0 / scale ** 0.5])
+        ctx.field_set("coordinates", moved)
+        ctx.zero()
+        ctx.assemble(ng.KERNEL_CONTINUITY_MASS, o)
+        _, rhs = ctx.system()
+        _, orhs = oracle.assemble_mass(False, moved, conn, rp, ci, lid, rho[1], rho[1], rho[2], dt=0.1)
+        check_vec(rhs, orhs)
+    ctx.compute_dual_volume()
+    assert np.allclose(ctx.field_get("dual_nodal_volume", (n,)), oracle.dual_volume(moved, conn), rtol=1e-13)
+    ctx.close()
