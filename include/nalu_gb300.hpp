@@ -51,6 +51,17 @@ class Context {
   void field(nalu_field f, const double* v, int64_t count) {
     check(nalu_field_set(ctx_, f, v, count, 0), "nalu_field_set");
   }
+  // a boundary part as a side set: face k is side ordinal[k] of element elem[k]
+  void sideSet(int set, const std::vector<int64_t>& elem, const std::vector<int32_t>& ordinal) {
+    if (elem.size() != ordinal.size()) throw Error(NALU_ERR_ARG, "sideSet: elem and ordinal differ in length");
+    check(nalu_faceset_define(ctx_, set, (int64_t)elem.size(), elem.data(), ordinal.data()), "nalu_faceset_define");
+  }
+  // all exposed sides of the mesh as side set `set`; returns their number
+  int64_t skin(int set) {
+    int64_t n = 0;
+    check(nalu_faceset_skin(ctx_, set, &n), "nalu_faceset_skin");
+    return n;
+  }
   int64_t n_nodes() const { return n_nodes_; }
 
  private:
@@ -58,13 +69,18 @@ class Context {
   int64_t n_nodes_ = 0;
 };
 
+// The TimeIntegrator values the kernels' setup() reads (BDF coefficients
+// gamma1 phi^{n+1} + gamma2 phi^n + gamma3 phi^{n-1}; BDF1 by default).
+struct TimeIntegrator {
+  double dt = 1.0, gamma1 = 1.0, gamma2 = -1.0, gamma3 = 0.0;
+};
+
 // Kernel: the reference's Kernel interface, reduced to what selects a device
-// kernel (its id) and its solution options; setup() takes the time-integrator
-// values that ContinuityAdvElemKernel::setup reads.
+// kernel (its id) and its solution options; setup() takes the time integrator.
 class Kernel {
  public:
   virtual ~Kernel() = default;
-  virtual void setup(double /*dt*/, double /*gamma1*/) {}
+  virtual void setup(const TimeIntegrator& /*ti*/) {}
   virtual int numDof() const { return 1; }
   int id() const { return id_; }
   nalu_assemble_opts opts;
@@ -91,7 +107,29 @@ class ContinuityAdvElemKernel : public Kernel {
     opts.shift_poisson = shiftPoisson;
     opts.reduced_sens = reducedSens || shiftPoisson;  // SolutionOptions.C:719-724
   }
-  void setup(double dt, double gamma1) override { opts.proj_time_scale = dt / gamma1; }
+  void setup(const TimeIntegrator& ti) override { opts.proj_time_scale = ti.dt / ti.gamma1; }
+};
+
+// time terms (src/kernel/ContinuityMassElemKernel.C, MomentumMassElemKernel.C)
+class ContinuityMassElemKernel : public Kernel {
+ public:
+  explicit ContinuityMassElemKernel(bool lumpedMass = false) : ContinuityMassElemKernel(lumpedMass, NALU_KERNEL_CONTINUITY_MASS) {}
+  ContinuityMassElemKernel(bool lumpedMass, int id) : Kernel(id) { opts.lumped_mass = lumpedMass; }
+  void setup(const TimeIntegrator& ti) override {
+    opts.dt = ti.dt;
+    opts.gamma1 = ti.gamma1;
+    opts.gamma2 = ti.gamma2;
+    opts.gamma3 = ti.gamma3;
+  }
+};
+
+class MomentumMassElemKernel : public ContinuityMassElemKernel {
+ public:
+  explicit MomentumMassElemKernel(bool lumpedMass = false, bool balancedForce = false)
+      : ContinuityMassElemKernel(lumpedMass, NALU_KERNEL_MOMENTUM_MASS) {
+    opts.balanced_force = balancedForce;
+  }
+  int numDof() const override { return 3; }
 };
 
 class MomentumAdvDiffElemKernel : public Kernel {
@@ -179,10 +217,10 @@ class AssembleElemSolverAlgorithm {
  public:
   explicit AssembleElemSolverAlgorithm(LinearSystem& ls) : linsys_(ls) {}
   void initialize_connectivity() { linsys_.buildElemToNodeGraph(); }
-  void execute(double dt = 1.0, double gamma1 = 1.0) {
+  void execute(const TimeIntegrator& ti = TimeIntegrator()) {
     for (Kernel* k : activeKernels_) {
       if (k->numDof() != linsys_.numDof()) throw Error(NALU_ERR_STATE, "kernel numDof != linear system numDof");
-      k->setup(dt, gamma1);
+      k->setup(ti);
       linsys_.context().check(nalu_assemble(linsys_.context().get(), k->id(), &k->opts), "execute");
     }
   }
@@ -190,6 +228,55 @@ class AssembleElemSolverAlgorithm {
 
  private:
   LinearSystem& linsys_;
+};
+
+// Face (and face-element) kernels of one boundary part
+// (src/kernel/ContinuityInflowElemKernel.C, ContinuityOpenElemKernel.C)
+class FaceKernel {
+ public:
+  explicit FaceKernel(int id) : id_(id) { nalu_assemble_opts_default(&opts); }
+  virtual ~FaceKernel() = default;
+  virtual void setup(const TimeIntegrator& ti) { opts.proj_time_scale = ti.dt / ti.gamma1; }
+  int id() const { return id_; }
+  nalu_assemble_opts opts;
+
+ private:
+  int id_;
+};
+
+class ContinuityInflowElemKernel : public FaceKernel {
+ public:
+  explicit ContinuityInflowElemKernel(bool useShifted = false) : FaceKernel(NALU_FACE_CONTINUITY_INFLOW) {
+    opts.shift_mdot = useShifted;
+  }
+};
+
+class ContinuityOpenElemKernel : public FaceKernel {
+ public:
+  ContinuityOpenElemKernel(bool shiftMdot = false, bool shiftPoisson = false, bool reducedSens = false)
+      : FaceKernel(NALU_FACE_CONTINUITY_OPEN) {
+    opts.shift_mdot = shiftMdot;
+    opts.shift_poisson = shiftPoisson;
+    opts.reduced_sens = reducedSens || shiftPoisson;
+  }
+};
+
+// AssembleFaceElemSolverAlgorithm over one side set
+class AssembleFaceElemSolverAlgorithm {
+ public:
+  AssembleFaceElemSolverAlgorithm(LinearSystem& ls, int sideSet) : linsys_(ls), set_(sideSet) {}
+  void execute(const TimeIntegrator& ti = TimeIntegrator()) {
+    if (linsys_.numDof() != 1) throw Error(NALU_ERR_STATE, "face kernels need a numDof 1 system");
+    for (FaceKernel* k : activeKernels_) {
+      k->setup(ti);
+      linsys_.context().check(nalu_assemble_faces(linsys_.context().get(), set_, k->id(), &k->opts), "execute");
+    }
+  }
+  std::vector<FaceKernel*> activeKernels_;
+
+ private:
+  LinearSystem& linsys_;
+  int set_;
 };
 
 }  // namespace nalu_gb300

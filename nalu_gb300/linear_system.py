@@ -9,14 +9,33 @@ surface; every call goes through the C ABI (``include/nalu_gb300.h``).
 * ``AssembleElemSolverAlgorithm``  -- include/AssembleElemSolverAlgorithm.h:38-112
 * ``*ElemKernel``                  -- include/kernel/Kernel.h:95-125 and the
                                       kernel sources named on each class
+* ``AssembleFaceElemSolverAlgorithm`` -- src/AssembleFaceElemSolverAlgorithm.C,
+                                      with the continuity inflow / open kernels
 
 Kernels run as one fused device pass each (gather, master element, element
 matrix, sumInto).  Several active kernels therefore add into the system one
 after the other instead of into one shared element matrix; the sums are the
 same up to floating-point summation order.
 """
-from . import (KERNEL_CONTINUITY_ADV, KERNEL_MOMENTUM_ADV_DIFF, KERNEL_MOMENTUM_UPW_ADV_DIFF,
-               KERNEL_SCALAR_DIFF, default_assemble_opts, default_solver_opts)
+from . import (FACE_CONTINUITY_INFLOW, FACE_CONTINUITY_OPEN, KERNEL_CONTINUITY_ADV, KERNEL_CONTINUITY_MASS,
+               KERNEL_MOMENTUM_ADV_DIFF, KERNEL_MOMENTUM_MASS, KERNEL_MOMENTUM_UPW_ADV_DIFF, KERNEL_SCALAR_DIFF,
+               default_assemble_opts, default_solver_opts)
+
+
+class TimeIntegrator:
+    """The TimeIntegrator values the kernels' setup() reads: time step and
+    the BDF coefficients gamma1 phi^{n+1} + gamma2 phi^n + gamma3 phi^{n-1}
+    (BDF1 by default)."""
+
+    def __init__(self, dt=1.0, gamma1=1.0, gamma2=-1.0, gamma3=0.0):
+        self.dt, self.gamma1, self.gamma2, self.gamma3 = dt, gamma1, gamma2, gamma3
+
+    @staticmethod
+    def of(ti):
+        """accepts a TimeIntegrator, a (dt, gamma1[, gamma2, gamma3]) tuple or None"""
+        if ti is None or isinstance(ti, TimeIntegrator):
+            return ti
+        return TimeIntegrator(*ti)
 
 
 class Kernel:
@@ -57,9 +76,34 @@ class ContinuityAdvElemKernel(Kernel):
 
     def setup(self, time_integrator=None):
         """projTimeScale = dt / gamma1 (ContinuityAdvElemKernel.C:79-84)."""
-        if time_integrator is not None:
-            dt, gamma1 = time_integrator
-            self.opts.proj_time_scale = dt / gamma1
+        ti = TimeIntegrator.of(time_integrator)
+        if ti is not None:
+            self.opts.proj_time_scale = ti.dt / ti.gamma1
+
+
+class ContinuityMassElemKernel(Kernel):
+    """src/kernel/ContinuityMassElemKernel.C: density time derivative at the
+    sub-control volumes (fields density, density_n, density_nm1)."""
+
+    kernel_id = KERNEL_CONTINUITY_MASS
+
+    def __init__(self, lumped_mass=False):
+        super().__init__(lumped_mass=int(lumped_mass))
+
+    def setup(self, time_integrator=None):
+        ti = TimeIntegrator.of(time_integrator) or TimeIntegrator()
+        self.opts.dt, self.opts.gamma1, self.opts.gamma2, self.opts.gamma3 = ti.dt, ti.gamma1, ti.gamma2, ti.gamma3
+
+
+class MomentumMassElemKernel(ContinuityMassElemKernel):
+    """src/kernel/MomentumMassElemKernel.C: (rho u) time derivative and the
+    Gjp source (fields density*, velocity, velocity_n, velocity_nm1, dpdx)."""
+
+    kernel_id = KERNEL_MOMENTUM_MASS
+    num_dof = 3
+
+    def __init__(self, lumped_mass=False, balanced_force=False):
+        Kernel.__init__(self, lumped_mass=int(lumped_mass), balanced_force=int(balanced_force))
 
 
 class MomentumAdvDiffElemKernel(Kernel):
@@ -151,3 +195,44 @@ class AssembleElemSolverAlgorithm:
                 raise ValueError("kernel numDof does not match the linear system")
             k.setup(time_integrator)
             self.linsys.ctx.assemble(k.kernel_id, k.opts)
+
+
+class ContinuityInflowElemKernel(Kernel):
+    """src/kernel/ContinuityInflowElemKernel.C (field cont_velocity_bc)."""
+
+    kernel_id = FACE_CONTINUITY_INFLOW
+
+    def __init__(self, use_shifted=False):
+        super().__init__(shift_mdot=int(use_shifted))
+
+    def setup(self, time_integrator=None):
+        ti = TimeIntegrator.of(time_integrator)
+        if ti is not None:
+            self.opts.proj_time_scale = ti.dt / ti.gamma1
+
+
+class ContinuityOpenElemKernel(ContinuityInflowElemKernel):
+    """src/kernel/ContinuityOpenElemKernel.C (fields pressure, pressure_bc,
+    density, velocity, dpdx; the side set's dynamic pressure)."""
+
+    kernel_id = FACE_CONTINUITY_OPEN
+
+    def __init__(self, shift_mdot=False, shift_poisson=False, reduced_sens=False):
+        Kernel.__init__(self, shift_mdot=int(shift_mdot), shift_poisson=int(shift_poisson),
+                        reduced_sens=int(reduced_sens or shift_poisson))
+
+
+class AssembleFaceElemSolverAlgorithm:
+    """Face / face-element loop driver (src/AssembleFaceElemSolverAlgorithm.C)
+    over one side set of the context (``Context.faceset_define`` or
+    ``faceset_skin``)."""
+
+    def __init__(self, linsys, side_set):
+        self.linsys = linsys
+        self.side_set = side_set
+        self.activeKernels_ = []
+
+    def execute(self, time_integrator=None):
+        for k in self.activeKernels_:
+            k.setup(time_integrator)
+            self.linsys.ctx.assemble_faces(self.side_set, k.kernel_id, k.opts)

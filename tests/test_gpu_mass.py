@@ -168,3 +168,40 @@ def test_mass_follows_moved_coordinates(gpu_ctx_factory, oracle):
     ctx.compute_dual_volume()
     assert np.allclose(ctx.field_get("dual_nodal_volume", (n,)), oracle.dual_volume(moved, conn), rtol=1e-13)
     ctx.close()
+
+
+def test_mirror_algorithms(gpu_ctx_factory):
+    """the reference-shaped drivers: element kernels with a BDF2 TimeIntegrator
+    and a face algorithm over a side set sum to the direct calls"""
+    from nalu_gb300.linear_system import (AssembleElemSolverAlgorithm, AssembleFaceElemSolverAlgorithm,
+                                          ContinuityAdvElemKernel, ContinuityMassElemKernel,
+                                          ContinuityInflowElemKernel, LinearSystem, TimeIntegrator)
+    c, conn, gid = block_mesh(5, 4, 4, jitter=0.2, seed=9)
+    n = c.shape[0]
+    rho, u, gp = _states(n, 4)
+    ctx = _ctx(gpu_ctx_factory, c, conn, gid)
+    for name, v in (("density", rho[2]), ("density_n", rho[1]), ("density_nm1", rho[0]), ("velocity", u[2]),
+                    ("pressure", np.zeros(n)), ("dpdx", gp), ("cont_velocity_bc", u[1])):
+        ctx.field_set(name, v)
+    ctx.faceset_skin(0)
+    ls = LinearSystem(ctx, 1)
+    alg = AssembleElemSolverAlgorithm(ls)
+    alg.activeKernels_ = [ContinuityAdvElemKernel(), ContinuityMassElemKernel()]
+    alg.initialize_connectivity()
+    face = AssembleFaceElemSolverAlgorithm(ls, 0)
+    face.activeKernels_ = [ContinuityInflowElemKernel()]
+    ti = TimeIntegrator(0.05, 1.5, -2.0, 0.5)
+    ls.zeroSystem()
+    alg.execute(ti)
+    face.execute(ti)
+    v1, r1 = ctx.system()
+    ctx.zero()
+    tau = 0.05 / 1.5
+    ctx.assemble(ng.KERNEL_CONTINUITY_ADV, ng.default_assemble_opts(proj_time_scale=tau))
+    ctx.assemble(ng.KERNEL_CONTINUITY_MASS, ng.default_assemble_opts(dt=0.05, gamma1=1.5, gamma2=-2.0, gamma3=0.5))
+    ctx.assemble_faces(0, ng.FACE_CONTINUITY_INFLOW, ng.default_assemble_opts(proj_time_scale=tau))
+    v2, r2 = ctx.system()
+    rp, _ = ctx.graph()
+    check_csr_values(v1, v2, rp)
+    check_vec(r1, r2)
+    ctx.close()
