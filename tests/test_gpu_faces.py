@@ -191,3 +191,33 @@ def test_face_errors(gpu_ctx_factory):
         ctx.nodal_gradient_boundary(0, "pressure", "dpdx")
     assert e.value.status == -3
     ctx.close()
+
+
+def test_face_set_edge_cases(gpu_ctx_factory, oracle):
+    c, conn, gid = block_mesh(1, 1, 1)
+    n = c.shape[0]
+    ctx = _mesh(gpu_ctx_factory, c, conn, gid)
+    # one element: all six sides exposed, in side order
+    assert ctx.faceset_skin(0) == 6
+    e, s = ctx.faceset_get(0)
+    assert np.array_equal(e, np.zeros(6)) and np.array_equal(s, np.arange(6))
+    a = ctx.faceset_exposed_area(0)
+    assert np.max(np.abs(a.sum(axis=(0, 1)))) <= 1e-16 and np.allclose(np.abs(a).sum(axis=(1, 2)), 1.0)
+    # an empty set is valid and does nothing
+    ctx.faceset_define(1, [], [])
+    assert ctx.faceset_get(1)[0].size == 0 and ctx.faceset_exposed_area(1).shape == (0, 4, 3)
+    ctx.field_set("density", np.ones(n))
+    ctx.field_set("cont_velocity_bc", np.ones((n, 3)))
+    ctx.build_elem_graph(1)
+    ctx.zero()
+    ctx.assemble_faces(1, ng.FACE_CONTINUITY_INFLOW)
+    vals, rhs = ctx.system()
+    assert not vals.any() and not rhs.any()
+    # redefining replaces; a new mesh clears every set
+    ctx.faceset_define(1, [0], [5])
+    assert ctx.faceset_get(1)[1].tolist() == [5]
+    ctx.mesh_create(c, conn, gid)
+    with pytest.raises(ng.NaluError) as err:
+        ctx.faceset_get(1)
+    assert err.value.status == -3
+    ctx.close()
