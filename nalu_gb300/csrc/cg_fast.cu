@@ -189,17 +189,19 @@ enum { CS_RZ = 0, CS_ALPHA = 1, CS_BETA = 2, CS_RR = 3, CS_PQ = 4 };
 
 // Jacobi with the FP32-rounded inverse diagonal (the same one the iterations use)
 __global__ void __launch_bounds__(kCgThreads) k_cgd_init(int64_t n, const double* __restrict__ r,
-                                                         const float* __restrict__ dinvf,
-                                                         double* __restrict__ part, unsigned* __restrict__ cnt,
-                                                         double* __restrict__ cs) {
+                                                         const float* __restrict__ dinvf, float2* __restrict__ r2,
+                                                         float2* __restrict__ x2, double* __restrict__ part,
+                                                         unsigned* __restrict__ cnt, double* __restrict__ cs) {
   __shared__ double sh[33];
-  double rz = 0.0, rr = 0.0;
+  float zh = 0.0f, zl = 0.0f, rh = 0.0f, rl = 0.0f;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const double ri = r[i];
-    rz += ri * (widen_f(dinvf[i]) * ri);
-    rr += ri * ri;
+    const float2 rs = split_df(r[i]);
+    r2[i] = rs;
+    x2[i] = make_float2(0.0f, 0.0f);
+    acc_sq_df(zh, zl, rs, dinvf[i]);
+    acc_sq_df(rh, rl, rs, 1.0f);
   }
-  const double v[2] = {rz, rr};
+  const double v[2] = {join_df(make_float2(zh, zl)), join_df(make_float2(rh, rl))};
   double t[2];
   if (red::grid_reduce<2>(v, part, kCgBlocks, cnt, t, sh) && threadIdx.x == 0) {
     cs[CS_RZ] = t[0];
@@ -207,38 +209,37 @@ __global__ void __launch_bounds__(kCgThreads) k_cgd_init(int64_t n, const double
   }
 }
 
-// p = D^-1 r + beta p (p held as FP32 pairs)
-__global__ void __launch_bounds__(kCgThreads) k_cgd_pupdate(int64_t n, const double* __restrict__ r,
+// p = D^-1 r + beta p (FP32 pairs)
+__global__ void __launch_bounds__(kCgThreads) k_cgd_pupdate(int64_t n, const float2* __restrict__ r2,
                                                             const float* __restrict__ dinvf,
                                                             float2* __restrict__ p, const double* __restrict__ cs,
                                                             int first) {
-  // all in FP32 pairs: z = D^-1 r (D^-1 an FP32 value), p = z + beta p
   const float2 beta = split_df(first ? 0.0 : cs[CS_BETA]);
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const float2 z = fma_df(split_df(r[i]), make_float2(dinvf[i], 0.0f), make_float2(0.0f, 0.0f));
+    const float2 z = fma_df(r2[i], make_float2(dinvf[i], 0.0f), make_float2(0.0f, 0.0f));
     p[i] = first ? z : fma_df(beta, p[i], z);
   }
 }
 
-// q = A p; alpha = r.z / p.q by the last block
+// q = A p (FP32 pairs); alpha = r.z / p.q by the last block
 __global__ void __launch_bounds__(kCgThreads) k_cgd_spmv(int64_t n, int64_t npad, const int64_t* __restrict__ sptr,
                                                          const int32_t* __restrict__ slen,
                                                          const int32_t* __restrict__ scol,
                                                          const float2* __restrict__ sval,
-                                                         const float2* __restrict__ p, double* __restrict__ q,
+                                                         const float2* __restrict__ p, float2* __restrict__ q2,
                                                          double* __restrict__ part, unsigned* __restrict__ cnt,
                                                          double* __restrict__ cs) {
   __shared__ double sh[33];
-  double dot = 0.0;
+  float dh = 0.0f, dl = 0.0f;
   for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < npad;
        row += (int64_t)gridDim.x * blockDim.x) {
     if (row >= n) continue;
     const int64_t s = row / kSlice;
-    const double qi = sell_row_df(__ldg(sptr + s) + (row % kSlice), __ldg(slen + s), scol, sval, p);
-    q[row] = qi;
-    dot += join_df(p[row]) * qi;
+    const float2 qi = sell_row_df2(__ldg(sptr + s) + (row % kSlice), __ldg(slen + s), scol, sval, p);
+    q2[row] = qi;
+    acc_mul_df(dh, dl, p[row], qi);
   }
-  const double v[1] = {dot};
+  const double v[1] = {join_df(make_float2(dh, dl))};
   double t[1];
   if (red::grid_reduce<1>(v, part, kCgBlocks, cnt, t, sh) && threadIdx.x == 0) {
     cs[CS_PQ] = t[0];
@@ -246,22 +247,22 @@ __global__ void __launch_bounds__(kCgThreads) k_cgd_spmv(int64_t n, int64_t npad
   }
 }
 
-// x += alpha p; r -= alpha q; r.D^-1 r and r.r as FP32 pairs (the FP64 pipe
-// keeps only the two updates); beta = rz_new / rz by the last block
-__global__ void __launch_bounds__(kCgThreads) k_cgd_axpy(int64_t n, double* __restrict__ x,
-                                                         const float2* __restrict__ p, double* __restrict__ r,
-                                                         const double* __restrict__ q,
+// x += alpha p; r -= alpha q; r.D^-1 r and r.r, all as FP32 pairs (no FP64
+// instruction per row); beta = rz_new / rz by the last block
+__global__ void __launch_bounds__(kCgThreads) k_cgd_axpy(int64_t n, float2* __restrict__ x2,
+                                                         const float2* __restrict__ p, float2* __restrict__ r2,
+                                                         const float2* __restrict__ q2,
                                                          const float* __restrict__ dinvf,
                                                          double* __restrict__ part, unsigned* __restrict__ cnt,
                                                          double* __restrict__ cs) {
   __shared__ double sh[33];
-  const double alpha = cs[CS_ALPHA];
+  const float2 alpha = split_df(cs[CS_ALPHA]);
+  const float2 nalpha = make_float2(-alpha.x, -alpha.y);
   float zh = 0.0f, zl = 0.0f, rh = 0.0f, rl = 0.0f;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    x[i] += alpha * join_df(p[i]);
-    const double ri = r[i] - alpha * q[i];
-    r[i] = ri;
-    const float2 rs = split_df(ri);
+    x2[i] = fma_df(alpha, p[i], x2[i]);
+    const float2 rs = fma_df(nalpha, q2[i], r2[i]);
+    r2[i] = rs;
     acc_sq_df(zh, zl, rs, dinvf[i]);
     acc_sq_df(rh, rl, rs, 1.0f);
   }
@@ -271,6 +272,15 @@ __global__ void __launch_bounds__(kCgThreads) k_cgd_axpy(int64_t n, double* __re
     cs[CS_BETA] = t[0] / cs[CS_RZ];
     cs[CS_RZ] = t[0];
     cs[CS_RR] = t[1];
+  }
+}
+
+// iterate and residual back to FP64
+__global__ void k_cgd_finish(int64_t n, const float2* __restrict__ x2, const float2* __restrict__ r2,
+                             double* __restrict__ x, double* __restrict__ r) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    x[i] = join_df(x2[i]);
+    r[i] = join_df(r2[i]);
   }
 }
 
@@ -399,27 +409,32 @@ int pcg_df(nalu_ctx* ctx, const SellMatrix& S, double* x, double* r, double* z, 
   if (w.p2.n < n) NALU_CUDA(ctx, w.p2.alloc(n));
   if (w.cscal.n < 8) NALU_CUDA(ctx, w.cscal.alloc(8));
   if (w.ccount.n < 1) NALU_CUDA(ctx, w.ccount.alloc(1));
+  if (w.x2.n < n) NALU_CUDA(ctx, w.x2.alloc(n));
+  if (w.r2.n < n) NALU_CUDA(ctx, w.r2.alloc(n));
+  if (w.q2.n < n) NALU_CUDA(ctx, w.q2.alloc(n));
   double* part = w.partial.p;
   unsigned* cnt = w.ccount.p;
   double* cs = w.cscal.p;
   float2* p = w.p2.p;
+  float2* x2 = w.x2.p;
+  float2* r2 = w.r2.p;
+  float2* q2 = w.q2.p;
   cudaStream_t st = ctx->stream;
   NALU_CUDA(ctx, cudaMemsetAsync(cnt, 0, sizeof(unsigned), st));
   NALU_CUDA(ctx, cudaMemsetAsync(cs, 0, sizeof(double) * 8, st));
-  NALU_CUDA(ctx, cudaMemsetAsync(x, 0, sizeof(double) * n, st));
   if (w.fdinv.n < n) NALU_CUDA(ctx, w.fdinv.alloc(n));
   float* dinvf = w.fdinv.p;
   k_convert_f<<<kCgBlocks, kCgThreads, 0, st>>>(n, dinv, dinvf);
-  k_cgd_init<<<kCgBlocks, kCgThreads, 0, st>>>(n, r, dinvf, part, cnt, cs);
+  k_cgd_init<<<kCgBlocks, kCgThreads, 0, st>>>(n, r, dinvf, r2, x2, part, cnt, cs);
   ctx->launches++;
   // one full wave per kernel: SMs x resident blocks (at most the partial-sum capacity)
   const unsigned g_pu = wave_grid(ctx, (const void*)k_cgd_pupdate, kCgThreads);
   const unsigned g_sp = wave_grid(ctx, (const void*)k_cgd_spmv, kCgThreads);
   const unsigned g_ax = wave_grid(ctx, (const void*)k_cgd_axpy, kCgThreads);
   auto iteration = [&](int first) {
-    k_cgd_pupdate<<<g_pu, kCgThreads, 0, st>>>(n, r, dinvf, p, cs, first);
-    k_cgd_spmv<<<g_sp, kCgThreads, 0, st>>>(n, npad, S.ptr.p, S.len.p, S.col.p, S.val2.p, p, q, part, cnt, cs);
-    k_cgd_axpy<<<g_ax, kCgThreads, 0, st>>>(n, x, p, r, q, dinvf, part, cnt, cs);
+    k_cgd_pupdate<<<g_pu, kCgThreads, 0, st>>>(n, r2, dinvf, p, cs, first);
+    k_cgd_spmv<<<g_sp, kCgThreads, 0, st>>>(n, npad, S.ptr.p, S.len.p, S.col.p, S.val2.p, p, q2, part, cnt, cs);
+    k_cgd_axpy<<<g_ax, kCgThreads, 0, st>>>(n, x2, p, r2, q2, dinvf, part, cnt, cs);
     ctx->launches += 3;
   };
   ctx->launches++;
@@ -471,6 +486,9 @@ int pcg_df(nalu_ctx* ctx, const SellMatrix& S, double* x, double* r, double* z, 
   }
   cudaGraphExecDestroy(exec);
   cudaGraphDestroy(graph);
+  k_cgd_finish<<<kCgBlocks, kCgThreads, 0, st>>>(n, x2, r2, x, r);
+  ctx->launches++;
+  NALU_CUDA(ctx, cudaGetLastError());
   *iters_out = it;
   if (bad) return set_error(ctx, NALU_ERR_NONFINITE, "CG breakdown (non-finite residual)");
   return conv ? NALU_OK : NALU_ERR_NOT_CONVERGED;

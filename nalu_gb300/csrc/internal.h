@@ -91,6 +91,7 @@ struct SolverWork {
   DBuf<double> scal;     // device scalars
   DBuf<double> partial;  // block partial sums
   DBuf<float2> p2;       // search direction as FP32 pairs (df64 SpMV)
+  DBuf<float2> x2, r2, q2;  // Jacobi-CG iterate, residual and A p as FP32 pairs
   DBuf<double> cscal;    // CG scalars written by the last block of each kernel
   DBuf<unsigned> ccount; // arrival counter of the single-block reductions
   int64_t n = 0;

@@ -87,20 +87,30 @@ __device__ __forceinline__ void acc_sq_df(float& sh, float& sl, float2 x, float 
   sl = __fadd_rn(sl, __fadd_rn(er, lo));
 }
 
-// one SELL-32 row: sum_k val[base + 32 k] * p[col[base + 32 k]]
-__device__ __forceinline__ double sell_row_df(int64_t base, int len, const int32_t* __restrict__ scol,
-                                              const float2* __restrict__ sval, const float2* __restrict__ p) {
+// s += a * b for FP32 pairs a, b: TwoProd of the high parts, the cross terms,
+// TwoSum into (sh, sl)
+__device__ __forceinline__ void acc_mul_df(float& sh, float& sl, float2 a, float2 b) {
+  const float ph = __fmul_rn(a.x, b.x);
+  const float pe = __fmaf_rn(a.x, b.x, -ph);                   // exact product error
+  const float cr = __fmaf_rn(a.x, b.y, __fmul_rn(a.y, b.x));   // cross terms
+  const float t = __fadd_rn(sh, ph);                           // TwoSum(sh, ph)
+  const float bp = __fsub_rn(t, sh);
+  const float er = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, bp)), __fsub_rn(ph, bp));
+  sh = t;
+  sl = __fadd_rn(sl, __fadd_rn(er, __fadd_rn(pe, cr)));
+}
+
+// (sh, sl) renormalised to an FP32 pair (FastTwoSum; |sl| is small against |sh|)
+__device__ __forceinline__ float2 norm_df(float sh, float sl) {
+  const float hi = __fadd_rn(sh, sl);
+  return make_float2(hi, __fsub_rn(sl, __fsub_rn(hi, sh)));
+}
+
+// one SELL-32 row: sum_k val[base + 32 k] * p[col[base + 32 k]], as an FP32 pair
+__device__ __forceinline__ float2 sell_row_df2(int64_t base, int len, const int32_t* __restrict__ scol,
+                                               const float2* __restrict__ sval, const float2* __restrict__ p) {
   float sh = 0.0f, sl = 0.0f;
-  auto add = [&](float2 a, float2 b) {
-    const float ph = __fmul_rn(a.x, b.x);
-    const float pe = __fmaf_rn(a.x, b.x, -ph);                   // exact product error
-    const float cr = __fmaf_rn(a.x, b.y, __fmul_rn(a.y, b.x));   // cross terms
-    const float t = __fadd_rn(sh, ph);                           // TwoSum(sh, ph)
-    const float bp = __fsub_rn(t, sh);
-    const float er = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, bp)), __fsub_rn(ph, bp));
-    sh = t;
-    sl = __fadd_rn(sl, __fadd_rn(er, __fadd_rn(pe, cr)));
-  };
+  auto add = [&](float2 a, float2 b) { acc_mul_df(sh, sl, a, b); };
   // groups of 8 (predicated past the row length): all index and value loads
   // of a group are issued before the dependent gathers, so each thread keeps
   // many DRAM requests in flight
@@ -119,7 +129,13 @@ __device__ __forceinline__ double sell_row_df(int64_t base, int len, const int32
     for (int u = 0; u < 8; ++u)
       if (c[u] >= 0) add(a[u], b[u]);
   }
-  return widen_f(sh) + widen_f(sl);
+  return norm_df(sh, sl);
+}
+
+// the same row as an FP64 value
+__device__ __forceinline__ double sell_row_df(int64_t base, int len, const int32_t* __restrict__ scol,
+                                              const float2* __restrict__ sval, const float2* __restrict__ p) {
+  return join_df(sell_row_df2(base, len, scol, sval, p));
 }
 
 }  // namespace nalu_gb300
