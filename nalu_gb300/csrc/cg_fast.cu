@@ -7,6 +7,10 @@
 // The copy is made once per solve from the assembled CRS values (FP64 or
 // FP32 for the mixed-precision inner solve).
 //
+// pcg_df (the FP64 solve) keeps x, r, p and q = A p as FP32 pairs (about 48
+// significant bits) so that no iteration kernel issues an FP64 instruction per
+// row; x and r are split on entry and joined back to FP64 on exit.
+//
 // Iteration k (rz_k = r_k . z_k, z_k = D^-1 r_k):
 //   K0  beta = rz_k / rz_{k-1};  p = z + beta p
 //   K1  q = A p (one multiply-add per stored entry);  partial sums of p . q
