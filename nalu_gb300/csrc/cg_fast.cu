@@ -86,6 +86,33 @@ __global__ void k_sell_fill(int64_t n, const int64_t* __restrict__ rp, const int
   }
 }
 
+// 16-bit column offsets: one warp per slice; for entry k the base is the
+// smallest column of the slice's 32 rows, and a slice whose columns at some k
+// spread over more than 65535 is marked wide (it keeps the 32-bit indices)
+__global__ void k_sell_c16(int64_t nslices, const int64_t* __restrict__ sptr, const int32_t* __restrict__ slen,
+                           const int32_t* __restrict__ scol, uint16_t* __restrict__ col16,
+                           int32_t* __restrict__ cbase, uint8_t* __restrict__ wide) {
+  const int64_t s = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
+  const int lane = threadIdx.x & 31;
+  if (s >= nslices) return;
+  const int64_t b0 = sptr[s];
+  const int len = slen[s];
+  bool too_wide = false;
+  for (int k = 0; k < len; ++k) {
+    const int32_t c = scol[b0 + (int64_t)k * 32 + lane];
+    int32_t lo = c, hi = c;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+      hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    if ((int64_t)hi - lo > 65535) too_wide = true;
+    col16[b0 + (int64_t)k * 32 + lane] = (uint16_t)(c - lo);
+    if (lane == 0) cbase[b0 / 32 + k] = lo;
+  }
+  if (lane == 0) wide[s] = too_wide ? 1 : 0;
+}
+
 // z = D^-1 r ; partials of r.z and r.r
 template <class T>
 __global__ void __launch_bounds__(kCgThreads) k_cg_init(int64_t n, const T* __restrict__ r, const T* __restrict__ dinv,
@@ -229,6 +256,9 @@ __global__ void __launch_bounds__(kCgThreads) k_cgd_pupdate(int64_t n, const flo
 __global__ void __launch_bounds__(kCgThreads) k_cgd_spmv(int64_t n, int64_t npad, const int64_t* __restrict__ sptr,
                                                          const int32_t* __restrict__ slen,
                                                          const int32_t* __restrict__ scol,
+                                                         const uint16_t* __restrict__ col16,
+                                                         const int32_t* __restrict__ cbase,
+                                                         const uint8_t* __restrict__ wide,
                                                          const float2* __restrict__ sval,
                                                          const float2* __restrict__ p, float2* __restrict__ q2,
                                                          double* __restrict__ part, unsigned* __restrict__ cnt,
@@ -239,7 +269,10 @@ __global__ void __launch_bounds__(kCgThreads) k_cgd_spmv(int64_t n, int64_t npad
        row += (int64_t)gridDim.x * blockDim.x) {
     if (row >= n) continue;
     const int64_t s = row / kSlice;
-    const float2 qi = sell_row_df2(__ldg(sptr + s) + (row % kSlice), __ldg(slen + s), scol, sval, p);
+    const int64_t b0 = __ldg(sptr + s);
+    const float2 qi = __ldg(wide + s) ? sell_row_df2(b0 + (row % kSlice), __ldg(slen + s), scol, sval, p)
+                                      : sell_row_df2_c16(b0 + (row % kSlice), __ldg(slen + s), col16,
+                                                         cbase + b0 / kSlice, sval, p);
     q2[row] = qi;
     acc_mul_df(dh, dl, p[row], qi);
   }
@@ -324,6 +357,7 @@ int sell_build(nalu_ctx* ctx, SellMatrix& S, const VT** vals_out) {
   ctx->launches++;
   S.nslices = ns;
   S.stored = total;
+  S.c16_valid = false;
   *vals_out = vals;
   NALU_CUDA(ctx, cudaMemcpyAsync(S.ptr.p, hp.data(), sizeof(int64_t) * (ns + 1), cudaMemcpyHostToDevice, ctx->stream));
   NALU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -427,6 +461,17 @@ int pcg_df(nalu_ctx* ctx, const SellMatrix& S, double* x, double* r, double* z, 
   NALU_CUDA(ctx, cudaMemsetAsync(cnt, 0, sizeof(unsigned), st));
   NALU_CUDA(ctx, cudaMemsetAsync(cs, 0, sizeof(double) * 8, st));
   if (w.fdinv.n < n) NALU_CUDA(ctx, w.fdinv.alloc(n));
+  if (!S.c16_valid) {
+    SellMatrix& Sm = const_cast<SellMatrix&>(S);
+    if (Sm.col16.n < S.stored) NALU_CUDA(ctx, Sm.col16.alloc(S.stored));
+    if (Sm.cbase.n < S.stored / kSlice) NALU_CUDA(ctx, Sm.cbase.alloc(S.stored / kSlice + 1));
+    if (Sm.wide.n < S.nslices) NALU_CUDA(ctx, Sm.wide.alloc(S.nslices));
+    k_sell_c16<<<(unsigned)((S.nslices * 32 + 255) / 256), 256, 0, st>>>(S.nslices, S.ptr.p, S.len.p, S.col.p,
+                                                                         Sm.col16.p, Sm.cbase.p, Sm.wide.p);
+    ctx->launches++;
+    NALU_CUDA(ctx, cudaGetLastError());
+    Sm.c16_valid = true;
+  }
   float* dinvf = w.fdinv.p;
   k_convert_f<<<kCgBlocks, kCgThreads, 0, st>>>(n, dinv, dinvf);
   k_cgd_init<<<kCgBlocks, kCgThreads, 0, st>>>(n, r, dinvf, r2, x2, part, cnt, cs);
@@ -437,7 +482,8 @@ int pcg_df(nalu_ctx* ctx, const SellMatrix& S, double* x, double* r, double* z, 
   const unsigned g_ax = wave_grid(ctx, (const void*)k_cgd_axpy, kCgThreads);
   auto iteration = [&](int first) {
     k_cgd_pupdate<<<g_pu, kCgThreads, 0, st>>>(n, r2, dinvf, p, cs, first);
-    k_cgd_spmv<<<g_sp, kCgThreads, 0, st>>>(n, npad, S.ptr.p, S.len.p, S.col.p, S.val2.p, p, q2, part, cnt, cs);
+    k_cgd_spmv<<<g_sp, kCgThreads, 0, st>>>(n, npad, S.ptr.p, S.len.p, S.col.p, S.col16.p, S.cbase.p, S.wide.p,
+                                            S.val2.p, p, q2, part, cnt, cs);
     k_cgd_axpy<<<g_ax, kCgThreads, 0, st>>>(n, x2, p, r2, q2, dinvf, part, cnt, cs);
     ctx->launches += 3;
   };

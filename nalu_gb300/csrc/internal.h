@@ -67,6 +67,12 @@ struct SellMatrix {
   DBuf<float> valf;
   DBuf<float2> val2;   // FP32 pairs (hi, lo) for the df64 SpMV
   int64_t nslices = 0, stored = 0;
+  // compressed column indices: col = cbase[ptr[s] / 32 + k] + col16[entry] for
+  // the k-th entry of slice s, unless wide[s] (then col holds them)
+  DBuf<uint16_t> col16;
+  DBuf<int32_t> cbase;
+  DBuf<uint8_t> wide;
+  bool c16_valid = false;
 };
 
 // Learned preconditioner state (learned.cu).  The MLP parameters are FP32

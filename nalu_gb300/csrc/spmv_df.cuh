@@ -132,6 +132,30 @@ __device__ __forceinline__ float2 sell_row_df2(int64_t base, int len, const int3
   return norm_df(sh, sl);
 }
 
+// one SELL-32 row with 16-bit column offsets from a per-(slice, entry) base:
+// col = cbase[k] + col16[base + 32 k]
+__device__ __forceinline__ float2 sell_row_df2_c16(int64_t base, int len, const uint16_t* __restrict__ col16,
+                                                   const int32_t* __restrict__ cbase,
+                                                   const float2* __restrict__ sval, const float2* __restrict__ p) {
+  float sh = 0.0f, sl = 0.0f;
+  for (int k = 0; k < len; k += 8) {
+    int32_t c[8];
+    float2 a[8], b[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const bool in = k + u < len;
+      c[u] = in ? __ldg(cbase + k + u) + (int32_t)__ldg(col16 + base + (int64_t)(k + u) * 32) : -1;
+      a[u] = in ? __ldg(sval + base + (int64_t)(k + u) * 32) : make_float2(0.0f, 0.0f);
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) b[u] = c[u] >= 0 ? __ldg(p + c[u]) : make_float2(0.0f, 0.0f);
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+      if (c[u] >= 0) acc_mul_df(sh, sl, a[u], b[u]);
+  }
+  return norm_df(sh, sl);
+}
+
 // the same row as an FP64 value
 __device__ __forceinline__ double sell_row_df(int64_t base, int len, const int32_t* __restrict__ scol,
                                               const float2* __restrict__ sval, const float2* __restrict__ p) {
