@@ -364,6 +364,19 @@ int sell_build(nalu_ctx* ctx, SellMatrix& S, const VT** vals_out) {
   return cuda_check(ctx, cudaGetLastError(), "sell build");
 }
 
+int sell_c16_ensure(nalu_ctx* ctx, SellMatrix& S) {
+  if (S.c16_valid) return NALU_OK;
+  if (S.col16.n < S.stored) NALU_CUDA(ctx, S.col16.alloc(S.stored));
+  if (S.cbase.n < S.stored / kSlice + 1) NALU_CUDA(ctx, S.cbase.alloc(S.stored / kSlice + 1));
+  if (S.wide.n < S.nslices) NALU_CUDA(ctx, S.wide.alloc(S.nslices));
+  k_sell_c16<<<(unsigned)((S.nslices * 32 + 255) / 256), 256, 0, ctx->stream>>>(S.nslices, S.ptr.p, S.len.p, S.col.p,
+                                                                                S.col16.p, S.cbase.p, S.wide.p);
+  ctx->launches++;
+  const int rc = cuda_check(ctx, cudaGetLastError(), "sell c16");
+  if (rc == NALU_OK) S.c16_valid = true;
+  return rc;
+}
+
 // Jacobi-CG on A x = r (x from 0), vectors of type T, matrix values VT.
 // r holds the initial residual; on return x holds the solution increment.
 template <class T, class VT>
@@ -461,17 +474,8 @@ int pcg_df(nalu_ctx* ctx, const SellMatrix& S, double* x, double* r, double* z, 
   NALU_CUDA(ctx, cudaMemsetAsync(cnt, 0, sizeof(unsigned), st));
   NALU_CUDA(ctx, cudaMemsetAsync(cs, 0, sizeof(double) * 8, st));
   if (w.fdinv.n < n) NALU_CUDA(ctx, w.fdinv.alloc(n));
-  if (!S.c16_valid) {
-    SellMatrix& Sm = const_cast<SellMatrix&>(S);
-    if (Sm.col16.n < S.stored) NALU_CUDA(ctx, Sm.col16.alloc(S.stored));
-    if (Sm.cbase.n < S.stored / kSlice) NALU_CUDA(ctx, Sm.cbase.alloc(S.stored / kSlice + 1));
-    if (Sm.wide.n < S.nslices) NALU_CUDA(ctx, Sm.wide.alloc(S.nslices));
-    k_sell_c16<<<(unsigned)((S.nslices * 32 + 255) / 256), 256, 0, st>>>(S.nslices, S.ptr.p, S.len.p, S.col.p,
-                                                                         Sm.col16.p, Sm.cbase.p, Sm.wide.p);
-    ctx->launches++;
-    NALU_CUDA(ctx, cudaGetLastError());
-    Sm.c16_valid = true;
-  }
+  int rc = sell_c16_ensure(ctx, const_cast<SellMatrix&>(S));
+  if (rc) return rc;
   float* dinvf = w.fdinv.p;
   k_convert_f<<<kCgBlocks, kCgThreads, 0, st>>>(n, dinv, dinvf);
   k_cgd_init<<<kCgBlocks, kCgThreads, 0, st>>>(n, r, dinvf, r2, x2, part, cnt, cs);

@@ -73,6 +73,16 @@ struct SellMatrix {
   DBuf<int32_t> cbase;
   DBuf<uint8_t> wide;
   bool c16_valid = false;
+  // device pointers of the pattern, passed to kernels by value
+  struct View {
+    const int64_t* ptr;
+    const int32_t* len;
+    const int32_t* col;
+    const uint16_t* col16;
+    const int32_t* cbase;
+    const uint8_t* wide;
+  };
+  View view() const { return View{ptr.p, len.p, col.p, col16.p, cbase.p, wide.p}; }
 };
 
 // Learned preconditioner state (learned.cu).  The MLP parameters are FP32
@@ -98,6 +108,7 @@ struct SolverWork {
   DBuf<double> partial;  // block partial sums
   DBuf<float2> p2;       // search direction as FP32 pairs (df64 SpMV)
   DBuf<float2> x2, r2, q2;  // Jacobi-CG iterate, residual and A p as FP32 pairs
+  DBuf<float> zf;           // learned-FCG preconditioned residual (FP32 stencil output)
   DBuf<double> cscal;    // CG scalars written by the last block of each kernel
   DBuf<unsigned> ccount; // arrival counter of the single-block reductions
   int64_t n = 0;
@@ -235,6 +246,8 @@ int learned_prepare(nalu_ctx* ctx);  // slot map, stencil and SELL preconditione
 // for `stall_window` iterations
 int fcg_learned(nalu_ctx* ctx, double* x, double* r, double rtol, double r0norm, int max_it, int check_every,
                 int stall_window, int* iters_out, int* stalled, float* iter_ms = nullptr);
+// 16-bit column offsets of the SELL copy (built once per SELL build)
+int sell_c16_ensure(nalu_ctx* ctx, SellMatrix& S);  // cg_fast.cu
 unsigned wave_grid(nalu_ctx* ctx, const void* kernel, int threads);  // cg_fast.cu
 // *iter_ms (optional): device time of the iterations alone (set-up excluded)
 int pcg_df(nalu_ctx* ctx, const SellMatrix& S, double* x, double* r, double* z, double* q, const double* dinv,

@@ -441,80 +441,98 @@ __global__ void k_precond_apply_scale(int64_t n, const int64_t* __restrict__ spt
 //   z = M r;  beta = -(z . q_old) / (p_old . q_old);  p = z + beta p
 //   q = A p;  alpha = (p . r) / (p . q);  x += alpha p;  r -= alpha q
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kFcgThreads) k_fcg_prec(int64_t n, int64_t npad, const int64_t* __restrict__ sptr,
-                                                          const int32_t* __restrict__ slen,
-                                                          const int32_t* __restrict__ scol,
-                                                          const float* __restrict__ w, const double* __restrict__ r,
-                                                          const double* __restrict__ q, double* __restrict__ z,
+// Column of entry k of a SELL row: 16-bit offset from the (slice, entry) base,
+// or the 32-bit index in a wide slice (warp-uniform choice).
+struct SellCols {
+  const int32_t* __restrict__ col;
+  const uint16_t* __restrict__ col16;
+  const int32_t* __restrict__ cbase;  // of this slice
+  bool wide;
+  __device__ __forceinline__ int32_t at(int64_t base, int k) const {
+    return wide ? __ldg(col + base + (int64_t)k * kSlice)
+                : __ldg(cbase + k) + (int32_t)__ldg(col16 + base + (int64_t)k * kSlice);
+  }
+};
+
+__device__ __forceinline__ SellCols sell_cols(const SellMatrix::View& v, int64_t s) {
+  const int64_t b0 = __ldg(v.ptr + s);
+  return SellCols{v.col, v.col16, v.cbase + b0 / kSlice, __ldg(v.wide + s) != 0};
+}
+
+// z = M r (FP32 stencil values, FP32 residual); beta = -(z . q_old) / (p . q)_old by the last block
+__global__ void __launch_bounds__(kFcgThreads) k_fcg_prec(int64_t n, int64_t npad, SellMatrix::View S,
+                                                          const float* __restrict__ w, const float2* __restrict__ r2,
+                                                          const float2* __restrict__ q2, float* __restrict__ zf,
                                                           double* __restrict__ part, unsigned* __restrict__ cnt,
                                                           double* __restrict__ fs, int first) {
   __shared__ double sh[33];
-  double dot = 0.0;
+  float dh = 0.0f, dl = 0.0f;
   for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < npad;
        row += (int64_t)gridDim.x * blockDim.x) {
     if (row >= n) continue;
     const int64_t s = row / kSlice;
-    const int len = __ldg(slen + s);
-    const int64_t base = __ldg(sptr + s) + (row % kSlice);
+    const int len = __ldg(S.len + s);
+    const SellCols cols = sell_cols(S, s);
+    const int64_t base = __ldg(S.ptr + s) + (row % kSlice);
     float acc = 0.0f;
     for (int k = 0; k < len; k += 8) {  // loads of a group issued before the gathers
       int32_t c[8];
-      float a[8];
-      double b[8];
+      float a[8], b[8];
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
         const bool in = k + u < len;
-        c[u] = in ? __ldg(scol + base + (int64_t)(k + u) * kSlice) : -1;
+        c[u] = in ? cols.at(base, k + u) : -1;
         a[u] = in ? __ldg(w + base + (int64_t)(k + u) * kSlice) : 0.0f;
       }
 #pragma unroll
-      for (int u = 0; u < 8; ++u) b[u] = c[u] >= 0 ? __ldg(r + c[u]) : 0.0;
+      for (int u = 0; u < 8; ++u) b[u] = c[u] >= 0 ? __ldg(r2 + c[u]).x : 0.0f;
 #pragma unroll
-      for (int u = 0; u < 8; ++u) acc = fmaf(a[u], narrow_f(b[u]), acc);
+      for (int u = 0; u < 8; ++u) acc = fmaf(a[u], b[u], acc);
     }
-    const double zi = widen_f(acc);
-    z[row] = zi;
-    dot += zi * q[row];
+    zf[row] = acc;
+    acc_mul_df(dh, dl, make_float2(acc, 0.0f), q2[row]);
   }
-  const double v[1] = {dot};
+  const double v[1] = {join_df(make_float2(dh, dl))};
   double t[1];
   if (red::grid_reduce<1>(v, part, kFcgBlocks, cnt, t, sh) && threadIdx.x == 0)
     fs[FS_BETA] = first ? 0.0 : -t[0] / fs[FS_PQ];
 }
 
-__global__ void __launch_bounds__(kFcgThreads) k_fcg_pupdate(int64_t n, const double* __restrict__ z,
+__global__ void __launch_bounds__(kFcgThreads) k_fcg_pupdate(int64_t n, const float* __restrict__ zf,
                                                              float2* __restrict__ p, const double* __restrict__ fs,
                                                              int first) {
   const float2 beta = split_df(first ? 0.0 : fs[FS_BETA]);  // FP32-pair update, no FP64 instruction
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const float2 zi = split_df(z[i]);
+    const float2 zi = make_float2(zf[i], 0.0f);
     p[i] = first ? zi : fma_df(beta, p[i], zi);
   }
 }
 
 // q = A p (df64); alpha = (p . r) / (p . q) by the last block, which also
 // counts non-positive steps (the preconditioner is then not positive definite)
-__global__ void __launch_bounds__(kFcgThreads) k_fcg_spmv(int64_t n, int64_t npad, const int64_t* __restrict__ sptr,
-                                                          const int32_t* __restrict__ slen,
-                                                          const int32_t* __restrict__ scol,
+__global__ void __launch_bounds__(kFcgThreads) k_fcg_spmv(int64_t n, int64_t npad, SellMatrix::View S,
                                                           const float2* __restrict__ sval,
-                                                          const float2* __restrict__ p, const double* __restrict__ r,
-                                                          double* __restrict__ q, double* __restrict__ part,
+                                                          const float2* __restrict__ p, const float2* __restrict__ r2,
+                                                          float2* __restrict__ q2, double* __restrict__ part,
                                                           unsigned* __restrict__ cnt, double* __restrict__ fs,
                                                           int* __restrict__ nonpos) {
   __shared__ double sh[33];
-  double pq = 0.0, pr = 0.0;
+  float qh = 0.0f, ql = 0.0f, rh = 0.0f, rl = 0.0f;
   for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < npad;
        row += (int64_t)gridDim.x * blockDim.x) {
     if (row >= n) continue;
     const int64_t s = row / kSlice;
-    const double qi = sell_row_df(__ldg(sptr + s) + (row % kSlice), __ldg(slen + s), scol, sval, p);
-    q[row] = qi;
-    const double pi = join_df(p[row]);
-    pq += pi * qi;
-    pr += pi * r[row];
+    const int64_t b0 = __ldg(S.ptr + s);
+    const int len = __ldg(S.len + s);
+    const float2 qi = __ldg(S.wide + s)
+                          ? sell_row_df2(b0 + (row % kSlice), len, S.col, sval, p)
+                          : sell_row_df2_c16(b0 + (row % kSlice), len, S.col16, S.cbase + b0 / kSlice, sval, p);
+    q2[row] = qi;
+    const float2 pi = p[row];
+    acc_mul_df(qh, ql, pi, qi);
+    acc_mul_df(rh, rl, pi, r2[row]);
   }
-  const double v[2] = {pq, pr};
+  const double v[2] = {join_df(make_float2(qh, ql)), join_df(make_float2(rh, rl))};
   double t[2];
   if (red::grid_reduce<2>(v, part, kFcgBlocks, cnt, t, sh) && threadIdx.x == 0) {
     const double alpha = t[1] / t[0];
@@ -524,22 +542,41 @@ __global__ void __launch_bounds__(kFcgThreads) k_fcg_spmv(int64_t n, int64_t npa
   }
 }
 
-__global__ void __launch_bounds__(kFcgThreads) k_fcg_axpy(int64_t n, double* __restrict__ x,
-                                                          const float2* __restrict__ p, double* __restrict__ r,
-                                                          const double* __restrict__ q, double* __restrict__ part,
+// x += alpha p; r -= alpha q; r.r -- all as FP32 pairs
+__global__ void __launch_bounds__(kFcgThreads) k_fcg_axpy(int64_t n, float2* __restrict__ x2,
+                                                          const float2* __restrict__ p, float2* __restrict__ r2,
+                                                          const float2* __restrict__ q2, double* __restrict__ part,
                                                           unsigned* __restrict__ cnt, double* __restrict__ fs) {
   __shared__ double sh[33];
-  const double alpha = fs[FS_ALPHA];
+  const float2 alpha = split_df(fs[FS_ALPHA]);
+  const float2 nalpha = make_float2(-alpha.x, -alpha.y);
   float rh = 0.0f, rl = 0.0f;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    x[i] += alpha * join_df(p[i]);
-    const double ri = r[i] - alpha * q[i];
-    r[i] = ri;
-    acc_sq_df(rh, rl, split_df(ri), 1.0f);
+    x2[i] = fma_df(alpha, p[i], x2[i]);
+    const float2 ri = fma_df(nalpha, q2[i], r2[i]);
+    r2[i] = ri;
+    acc_sq_df(rh, rl, ri, 1.0f);
   }
   const double v[1] = {join_df(make_float2(rh, rl))};
   double t[1];
   if (red::grid_reduce<1>(v, part, kFcgBlocks, cnt, t, sh) && threadIdx.x == 0) fs[FS_RR] = t[0];
+}
+
+// FP64 <-> FP32-pair vectors at the ends of the solve
+__global__ void k_fcg_split(int64_t n, const double* __restrict__ r, float2* __restrict__ r2,
+                            float2* __restrict__ x2, float2* __restrict__ q2) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    r2[i] = split_df(r[i]);
+    x2[i] = make_float2(0.0f, 0.0f);
+    q2[i] = make_float2(0.0f, 0.0f);
+  }
+}
+__global__ void k_fcg_join(int64_t n, const float2* __restrict__ x2, const float2* __restrict__ r2,
+                           double* __restrict__ x, double* __restrict__ r) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    x[i] = join_df(x2[i]);
+    r[i] = join_df(r2[i]);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -876,30 +913,36 @@ int fcg_learned(nalu_ctx* ctx, double* x, double* r, double rtol, double r0norm,
   if (s.p2.n < n) NALU_CUDA(ctx, s.p2.alloc(n));
   if (s.cscal.n < 8) NALU_CUDA(ctx, s.cscal.alloc(8));
   if (s.ccount.n < 1) NALU_CUDA(ctx, s.ccount.alloc(1));
+  if (s.x2.n < n) NALU_CUDA(ctx, s.x2.alloc(n));
+  if (s.r2.n < n) NALU_CUDA(ctx, s.r2.alloc(n));
+  if (s.q2.n < n) NALU_CUDA(ctx, s.q2.alloc(n));
+  if (s.zf.n < n) NALU_CUDA(ctx, s.zf.alloc(n));
+  int rc = sell_c16_ensure(ctx, s.sell);
+  if (rc) return rc;
+  const SellMatrix::View SV = S.view();
   double* part = s.partial.p;
   unsigned* cnt = s.ccount.p;
   double* fs = s.cscal.p;
-  double *z = s.z.p, *q = s.q.p;
-  float2* p = s.p2.p;
+  float* zf = s.zf.p;
+  float2 *p = s.p2.p, *x2 = s.x2.p, *r2 = s.r2.p, *q2 = s.q2.p;
   DBuf<int> nonpos;
   NALU_CUDA(ctx, nonpos.alloc(1));
   cudaStream_t st = ctx->stream;
   NALU_CUDA(ctx, cudaMemsetAsync(nonpos.p, 0, sizeof(int), st));
   NALU_CUDA(ctx, cudaMemsetAsync(cnt, 0, sizeof(unsigned), st));
   NALU_CUDA(ctx, cudaMemsetAsync(fs, 0, sizeof(double) * 8, st));
-  NALU_CUDA(ctx, cudaMemsetAsync(x, 0, sizeof(double) * n, st));
-  NALU_CUDA(ctx, cudaMemsetAsync(q, 0, sizeof(double) * n, st));
+  k_fcg_split<<<kFcgBlocks, kFcgThreads, 0, st>>>(n, r, r2, x2, q2);
+  ctx->launches++;
   const float* w = ctx->learned.wsell.p;
   const unsigned g_pc = wave_grid(ctx, (const void*)k_fcg_prec, kFcgThreads);
   const unsigned g_pu = wave_grid(ctx, (const void*)k_fcg_pupdate, kFcgThreads);
   const unsigned g_sp = wave_grid(ctx, (const void*)k_fcg_spmv, kFcgThreads);
   const unsigned g_ax = wave_grid(ctx, (const void*)k_fcg_axpy, kFcgThreads);
   auto iteration = [&](int first) {
-    k_fcg_prec<<<g_pc, kFcgThreads, 0, st>>>(n, npad, S.ptr.p, S.len.p, S.col.p, w, r, q, z, part, cnt, fs, first);
-    k_fcg_pupdate<<<g_pu, kFcgThreads, 0, st>>>(n, z, p, fs, first);
-    k_fcg_spmv<<<g_sp, kFcgThreads, 0, st>>>(n, npad, S.ptr.p, S.len.p, S.col.p, S.val2.p, p, r, q, part, cnt, fs,
-                                             nonpos.p);
-    k_fcg_axpy<<<g_ax, kFcgThreads, 0, st>>>(n, x, p, r, q, part, cnt, fs);
+    k_fcg_prec<<<g_pc, kFcgThreads, 0, st>>>(n, npad, SV, w, r2, q2, zf, part, cnt, fs, first);
+    k_fcg_pupdate<<<g_pu, kFcgThreads, 0, st>>>(n, zf, p, fs, first);
+    k_fcg_spmv<<<g_sp, kFcgThreads, 0, st>>>(n, npad, SV, S.val2.p, p, r2, q2, part, cnt, fs, nonpos.p);
+    k_fcg_axpy<<<g_ax, kFcgThreads, 0, st>>>(n, x2, p, r2, q2, part, cnt, fs);
     ctx->launches += 4;
   };
   iteration(1);
@@ -964,6 +1007,9 @@ int fcg_learned(nalu_ctx* ctx, double* x, double* r, double rtol, double r0norm,
   }
   cudaGraphExecDestroy(exec);
   cudaGraphDestroy(graph);
+  k_fcg_join<<<kFcgBlocks, kFcgThreads, 0, st>>>(n, x2, r2, x, r);
+  ctx->launches++;
+  NALU_CUDA(ctx, cudaGetLastError());
   *iters_out = it;
   if (bad) *stalled = 1;  // a breakdown is handed to the fallback like a stall
   if (*stalled && !(last < r0norm)) {
