@@ -441,22 +441,29 @@ __global__ void k_precond_apply_scale(int64_t n, const int64_t* __restrict__ spt
 //   z = M r;  beta = -(z . q_old) / (p_old . q_old);  p = z + beta p
 //   q = A p;  alpha = (p . r) / (p . q);  x += alpha p;  r -= alpha q
 // ---------------------------------------------------------------------------
-// Column of entry k of a SELL row: 16-bit offset from the (slice, entry) base,
-// or the 32-bit index in a wide slice (warp-uniform choice).
-struct SellCols {
-  const int32_t* __restrict__ col;
-  const uint16_t* __restrict__ col16;
-  const int32_t* __restrict__ cbase;  // of this slice
-  bool wide;
-  __device__ __forceinline__ int32_t at(int64_t base, int k) const {
-    return wide ? __ldg(col + base + (int64_t)k * kSlice)
-                : __ldg(cbase + k) + (int32_t)__ldg(col16 + base + (int64_t)k * kSlice);
+// z_row = sum_k w[base + 32 k] r[col_k] in FP32, col_k from the 32-bit
+// indices (WIDE) or the 16-bit offsets from the slice's entry bases
+template <bool WIDE>
+__device__ __forceinline__ float prec_row(int64_t base, int len, const SellMatrix::View& S,
+                                          const int32_t* __restrict__ cbase, const float* __restrict__ w,
+                                          const float2* __restrict__ r2) {
+  float acc = 0.0f;
+  for (int k = 0; k < len; k += 8) {  // loads of a group issued before the gathers
+    int32_t c[8];
+    float a[8], b[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const bool in = k + u < len;
+      const int64_t e = base + (int64_t)(k + u) * kSlice;
+      c[u] = in ? (WIDE ? __ldg(S.col + e) : __ldg(cbase + k + u) + (int32_t)__ldg(S.col16 + e)) : -1;
+      a[u] = in ? __ldg(w + e) : 0.0f;
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) b[u] = c[u] >= 0 ? __ldg(r2 + c[u]).x : 0.0f;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) acc = fmaf(a[u], b[u], acc);
   }
-};
-
-__device__ __forceinline__ SellCols sell_cols(const SellMatrix::View& v, int64_t s) {
-  const int64_t b0 = __ldg(v.ptr + s);
-  return SellCols{v.col, v.col16, v.cbase + b0 / kSlice, __ldg(v.wide + s) != 0};
+  return acc;
 }
 
 // z = M r (FP32 stencil values, FP32 residual); beta = -(z . q_old) / (p . q)_old by the last block
@@ -472,23 +479,10 @@ __global__ void __launch_bounds__(kFcgThreads) k_fcg_prec(int64_t n, int64_t npa
     if (row >= n) continue;
     const int64_t s = row / kSlice;
     const int len = __ldg(S.len + s);
-    const SellCols cols = sell_cols(S, s);
-    const int64_t base = __ldg(S.ptr + s) + (row % kSlice);
-    float acc = 0.0f;
-    for (int k = 0; k < len; k += 8) {  // loads of a group issued before the gathers
-      int32_t c[8];
-      float a[8], b[8];
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const bool in = k + u < len;
-        c[u] = in ? cols.at(base, k + u) : -1;
-        a[u] = in ? __ldg(w + base + (int64_t)(k + u) * kSlice) : 0.0f;
-      }
-#pragma unroll
-      for (int u = 0; u < 8; ++u) b[u] = c[u] >= 0 ? __ldg(r2 + c[u]).x : 0.0f;
-#pragma unroll
-      for (int u = 0; u < 8; ++u) acc = fmaf(a[u], b[u], acc);
-    }
+    const int64_t b0 = __ldg(S.ptr + s);
+    const int64_t base = b0 + (row % kSlice);
+    const float acc = __ldg(S.wide + s) ? prec_row<true>(base, len, S, nullptr, w, r2)
+                                        : prec_row<false>(base, len, S, S.cbase + b0 / kSlice, w, r2);
     zf[row] = acc;
     acc_mul_df(dh, dl, make_float2(acc, 0.0f), q2[row]);
   }
