@@ -252,8 +252,13 @@ __global__ void __launch_bounds__(kCgThreads) k_cgd_pupdate(int64_t n, const flo
   }
 }
 
+// resident blocks per SM the SpMV's register allocation must allow
+#ifndef NALU_CG_SPMV_MINB
+#define NALU_CG_SPMV_MINB 4  // 64 registers: 4 blocks of 256 (measured best: 5 spills, 1 takes 72)
+#endif
+
 // q = A p (FP32 pairs); alpha = r.z / p.q by the last block
-__global__ void __launch_bounds__(kCgThreads) k_cgd_spmv(int64_t n, int64_t npad, const int64_t* __restrict__ sptr,
+__global__ void __launch_bounds__(kCgThreads, NALU_CG_SPMV_MINB) k_cgd_spmv(int64_t n, int64_t npad, const int64_t* __restrict__ sptr,
                                                          const int32_t* __restrict__ slen,
                                                          const int32_t* __restrict__ scol,
                                                          const uint16_t* __restrict__ col16,

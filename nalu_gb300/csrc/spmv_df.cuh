@@ -12,6 +12,12 @@
 
 #include "df64.h"
 
+// gathers issued per group in the SELL row loops (all index and value loads of
+// a group before its dependent gathers)
+#ifndef NALU_SPMV_GROUP
+#define NALU_SPMV_GROUP 8
+#endif
+
 namespace nalu_gb300 {
 
 // FP32 pair of a double (hi nearest, lo the next 24 bits) with integer ops.
@@ -138,19 +144,20 @@ __device__ __forceinline__ float2 sell_row_df2_c16(int64_t base, int len, const 
                                                    const int32_t* __restrict__ cbase,
                                                    const float2* __restrict__ sval, const float2* __restrict__ p) {
   float sh = 0.0f, sl = 0.0f;
-  for (int k = 0; k < len; k += 8) {
-    int32_t c[8];
-    float2 a[8], b[8];
+  constexpr int G = NALU_SPMV_GROUP;
+  for (int k = 0; k < len; k += G) {
+    int32_t c[G];
+    float2 a[G], b[G];
 #pragma unroll
-    for (int u = 0; u < 8; ++u) {
+    for (int u = 0; u < G; ++u) {
       const bool in = k + u < len;
       c[u] = in ? __ldg(cbase + k + u) + (int32_t)__ldg(col16 + base + (int64_t)(k + u) * 32) : -1;
       a[u] = in ? __ldg(sval + base + (int64_t)(k + u) * 32) : make_float2(0.0f, 0.0f);
     }
 #pragma unroll
-    for (int u = 0; u < 8; ++u) b[u] = c[u] >= 0 ? __ldg(p + c[u]) : make_float2(0.0f, 0.0f);
+    for (int u = 0; u < G; ++u) b[u] = c[u] >= 0 ? __ldg(p + c[u]) : make_float2(0.0f, 0.0f);
 #pragma unroll
-    for (int u = 0; u < 8; ++u)
+    for (int u = 0; u < G; ++u)
       if (c[u] >= 0) acc_mul_df(sh, sl, a[u], b[u]);
   }
   return norm_df(sh, sl);
