@@ -54,6 +54,9 @@ struct TileArgs {
   const int64_t* __restrict__ sptr;
   const int32_t* __restrict__ slen;
   const int32_t* __restrict__ scol;
+  const uint16_t* __restrict__ col16;  // 16-bit column offsets (see cg_fast.cu)
+  const int32_t* __restrict__ cbase;
+  const uint8_t* __restrict__ wide;
   const float2* __restrict__ sval;
   const float* __restrict__ dinvf;
   double* x;
@@ -116,12 +119,21 @@ __global__ void __launch_bounds__(kBT) k_bt_prec(TileArgs a) {
   if (i < a.tile_rows[t]) {
     const int64_t row = a.tile_row0[t] + i;
     const int64_t sl = row / kSliceB;
-    const int64_t base = __ldg(a.sptr + sl) + (row % kSliceB);
+    const int64_t b0 = __ldg(a.sptr + sl);
+    const int64_t base = b0 + (row % kSliceB);
     const int len = __ldg(a.slen + sl);
     float acc = 0.0f;
-    for (int k = 0; k < len; ++k) {
-      const int64_t e = base + (int64_t)k * kSliceB;
-      acc = fmaf(__ldg(a.wsell + e), narrow_f(__ldg(a.r + __ldg(a.scol + e))), acc);
+    if (__ldg(a.wide + sl)) {
+      for (int k = 0; k < len; ++k) {
+        const int64_t e = base + (int64_t)k * kSliceB;
+        acc = fmaf(__ldg(a.wsell + e), narrow_f(__ldg(a.r + __ldg(a.scol + e))), acc);
+      }
+    } else {
+      const int32_t* cb = a.cbase + b0 / kSliceB;
+      for (int k = 0; k < len; ++k) {
+        const int64_t e = base + (int64_t)k * kSliceB;
+        acc = fmaf(__ldg(a.wsell + e), narrow_f(__ldg(a.r + __ldg(cb + k) + (int32_t)__ldg(a.col16 + e))), acc);
+      }
     }
     const double zi = widen_f(acc);
     a.z[row] = zi;
@@ -157,7 +169,11 @@ __global__ void __launch_bounds__(kBT) k_bt_spmv(TileArgs a) {
   if (i < a.tile_rows[t]) {
     const int64_t row = a.tile_row0[t] + i;
     const int64_t s = row / kSliceB;
-    const double qi = sell_row_df(__ldg(a.sptr + s) + (row % kSliceB), __ldg(a.slen + s), a.scol, a.sval, a.p);
+    const int64_t b0 = __ldg(a.sptr + s);
+    const int len = __ldg(a.slen + s);
+    const double qi = __ldg(a.wide + s) ? sell_row_df(b0 + (row % kSliceB), len, a.scol, a.sval, a.p)
+                                        : join_df(sell_row_df2_c16(b0 + (row % kSliceB), len, a.col16,
+                                                                   a.cbase + b0 / kSliceB, a.sval, a.p));
     a.q[row] = qi;
     const double pi = join_df(a.p[row]);
     dot = pi * qi;
@@ -371,6 +387,10 @@ int solve_batched(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* inf
   a.sptr = s.sell.ptr.p;
   a.slen = s.sell.len.p;
   a.scol = s.sell.col.p;
+  if ((rc = sell_c16_ensure(ctx, s.sell))) return rc;
+  a.col16 = s.sell.col16.p;
+  a.cbase = s.sell.cbase.p;
+  a.wide = s.sell.wide.p;
   a.sval = s.sell.val2.p;
   a.dinvf = dinvf.p;
   a.x = ctx->d_x.p;
