@@ -411,6 +411,8 @@ def bench_aux(ng, ctx, c, conn, rho):
     out = {"workload": "continuity_adv_hex8_128^3_zstretch1.05 mesh of the headline"}
     ctx.field_set("velocity_rtm", ctx.field_get("velocity", (n, 3)))
     out["mdot_ms"] = timed_ms(ctx, ctx.compute_mdot)
+    o_df = ng.default_assemble_opts(arith=ng.ARITH_DF64)
+    out["mdot_df64_ms"] = timed_ms(ctx, lambda: ctx.compute_mdot(o_df))
     out["dual_volume_ms"] = timed_ms(ctx, ctx.compute_dual_volume)
     out["nodal_gradient_pressure_ms"] = timed_ms(ctx, lambda: ctx.compute_nodal_gradient("pressure", "dpdx"))
     out["nodal_gradient_velocity_ms"] = timed_ms(ctx, lambda: ctx.compute_nodal_gradient("velocity", "dudx"))

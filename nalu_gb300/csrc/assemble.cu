@@ -414,6 +414,7 @@ int launch_capture(nalu_ctx* ctx, int kernel, const nalu_assemble_opts& o, int64
 }
 
 int launch_mdot(nalu_ctx* ctx, const nalu_assemble_opts& o) {
+  if (o.arith == NALU_ARITH_DF64) return launch_mdot_df(ctx, o);
   AsmArgs a = base_args(ctx, NALU_KERNEL_CONTINUITY_ADV, o);
   a.f_u = ctx->fields[NALU_FIELD_VELOCITY_RTM].d.p;
   a.count = ctx->n_elems;

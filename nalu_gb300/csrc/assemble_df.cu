@@ -31,6 +31,60 @@ __global__ void k_prepass_w_df(const double* __restrict__ u, const double* __res
   for (int d = 0; d < 3; ++d) out[3 * i + d] = df_from_double(r * __ldg(u + 3 * i + d) + tau * __ldg(gp + 3 * i + d));
 }
 
+// ComputeMdot in df64: one thread per element, the twelve SCS mass flow rates
+template <bool SMDOT, bool SPOIS>
+__global__ void __launch_bounds__(kAsmBlockDF, NALU_DF_MINB) k_mdot_df(int64_t n_elems, const int32_t* __restrict__ conn,
+                                                                    const double* __restrict__ x,
+                                                                    const df64* __restrict__ w,
+                                                                    const double* __restrict__ p, df64 tau,
+                                                                    double* __restrict__ mdot, int32_t* flags) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n_elems) return;
+  int nd[8];
+  {
+    const int4* c4 = reinterpret_cast<const int4*>(conn + 8 * e);
+    const int4 p0 = __ldg(c4), p1 = __ldg(c4 + 1);
+    nd[0] = p0.x; nd[1] = p0.y; nd[2] = p0.z; nd[3] = p0.w;
+    nd[4] = p1.x; nd[5] = p1.y; nd[6] = p1.z; nd[7] = p1.w;
+  }
+  double xe[8][3];
+  df64 we[8][3], pe[8];
+#pragma unroll
+  for (int n = 0; n < 8; ++n) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      xe[n][d] = __ldg(x + 3 * (int64_t)nd[n] + d);
+      we[n][d] = w[3 * (int64_t)nd[n] + d];
+    }
+    pe[n] = df_split_bits(__ldg(p + nd[n]));
+  }
+  const double mindet = mdot_elem_df<SMDOT, SPOIS>(xe, we, pe, tau, mdot + 12 * e);
+  if (!(mindet > 1.0e-50)) atomicAdd(flags + FLAG_NEG_JAC, 1);
+}
+
+int launch_mdot_df(nalu_ctx* ctx, const nalu_assemble_opts& o) {
+  const int64_t n = ctx->n_nodes, E = ctx->n_elems;
+  if (ctx->d_node_df.n < 3 * n) NALU_CUDA(ctx, ctx->d_node_df.alloc(3 * n));
+  df64* w = reinterpret_cast<df64*>(ctx->d_node_df.p);
+  k_prepass_w_df<<<nblk_df(n, 256), 256, 0, ctx->stream>>>(ctx->fields[NALU_FIELD_VELOCITY_RTM].d.p,
+                                                        ctx->fields[NALU_FIELD_DPDX].d.p,
+                                                        ctx->fields[NALU_FIELD_DENSITY].d.p, o.proj_time_scale, w, n);
+  const unsigned grid = nblk_df(E, kAsmBlockDF);
+  const double* x = ctx->fields[NALU_FIELD_COORDINATES].d.p;
+  const double* p = ctx->fields[NALU_FIELD_PRESSURE].d.p;
+  double* out = ctx->fields[NALU_FIELD_MDOT_SCS].d.p;
+  const df64 tau = df_from_double(o.proj_time_scale);
+  if (o.shift_mdot) {
+    if (o.shift_poisson) k_mdot_df<true, true><<<grid, kAsmBlockDF, 0, ctx->stream>>>(E, ctx->d_conn.p, x, w, p, tau, out, ctx->d_flags.p);
+    else k_mdot_df<true, false><<<grid, kAsmBlockDF, 0, ctx->stream>>>(E, ctx->d_conn.p, x, w, p, tau, out, ctx->d_flags.p);
+  } else {
+    if (o.shift_poisson) k_mdot_df<false, true><<<grid, kAsmBlockDF, 0, ctx->stream>>>(E, ctx->d_conn.p, x, w, p, tau, out, ctx->d_flags.p);
+    else k_mdot_df<false, false><<<grid, kAsmBlockDF, 0, ctx->stream>>>(E, ctx->d_conn.p, x, w, p, tau, out, ctx->d_flags.p);
+  }
+  ctx->launches += 2;
+  return cuda_check(ctx, cudaGetLastError(), "df64 mdot launch");
+}
+
 namespace {
 
 void launch_df(nalu_ctx* ctx, int kernel, const nalu_assemble_opts& o, const AsmArgsDF& a, int out) {

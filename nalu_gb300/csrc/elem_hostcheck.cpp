@@ -105,6 +105,24 @@ void hc_scalar_diff_df(const double* xin, const double* q, const double* k, int 
   }
 }
 
+void hc_mdot_df(const double* xin, const double* rho, const double* u, const double* p, const double* gp,
+                double tau, int smdot, int spois, double* mdot) {
+  df64 w[8][3], pd[8];
+  for (int n = 0; n < 8; ++n)
+    for (int d = 0; d < 3; ++d) w[n][d] = df_from_double(rho[n] * u[n * 3 + d] + tau * gp[n * 3 + d]);
+  for (int n = 0; n < 8; ++n) pd[n] = df_split_bits(p[n]);
+  const df64 t = df_from_double(tau);
+  with_x(xin, [&](double (&x)[8][3]) {
+    if (smdot) {
+      if (spois) mdot_elem_df<true, true>(x, w, pd, t, mdot);
+      else mdot_elem_df<true, false>(x, w, pd, t, mdot);
+    } else {
+      if (spois) mdot_elem_df<false, true>(x, w, pd, t, mdot);
+      else mdot_elem_df<false, false>(x, w, pd, t, mdot);
+    }
+  });
+}
+
 void hc_continuity_df(const double* xin, const double* u, const double* rho, const double* p,
                       const double* gp, double tau, int smdot, int spois, int reduced, double* lhs,
                       double* rhs) {

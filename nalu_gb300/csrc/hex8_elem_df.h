@@ -315,6 +315,59 @@ NALU_HD double continuity_elem_df(const double x[8][3], const df64 w[8][3], df64
   return f2d_bits(mindet);
 }
 
+// ---------------------------------------------------------------------------
+// Mass flow rate at the SCS in df64 (ComputeMdotElemAlgorithm.C:200-245):
+//   mdot_ip = (rho u + tau Gp)_ip . A - tau (dN/dx . A) . p
+// SMDOT: shifted shape functions for the interpolation; SPOIS: shifted grad
+// op for the pressure gradient.  Writes out[ip] (12 values) as FP64.
+// ---------------------------------------------------------------------------
+template <bool SMDOT, bool SPOIS>
+NALU_HD double mdot_elem_df(const double x[8][3], const df64 w[8][3], const df64 p[8], df64 tau, double* out) {
+  EdgeFormDF f;
+  {
+    df64 d[8][3];
+    rel_coords_df(x, d);
+    edge_form_df(d, f);
+  }
+  df64 wc[3][8];
+#pragma unroll
+  for (int comp = 0; comp < 3; ++comp) {
+    df64 v[8];
+#pragma unroll
+    for (int n = 0; n < 8; ++n) v[n] = w[n][comp];
+    trilinear_coeffs_df(v, wc[comp]);
+  }
+  float mindet = 3.0e38f;
+#pragma unroll 1
+  for (int ip = 0; ip < 12; ++ip) {
+    IpGeomDF g;
+    ip_geometry_df(f, ip, g);
+    mindet = fminf(mindet, g.det.hi);
+    float s_std[3], s_sh[3];
+    ip_location(ip, 0.25f, s_std);
+    ip_location(ip, 0.5f, s_sh);
+    const float* sm = SMDOT ? s_sh : s_std;
+    const df64 wx = trilinear_eval_df(wc[0], sm);
+    const df64 wy = trilinear_eval_df(wc[1], sm);
+    const df64 wz = trilinear_eval_df(wc[2], sm);
+    const df64 m0 = df_fma(wz, g.area[2], df_fma(wy, g.area[1], df_mul(wx, g.area[0])));
+    df64 fs[8];
+    if (SPOIS) {
+      df64 Gs[3], dets;
+      ip_shifted_G_df(f, ip, g.area, Gs, dets);
+      mindet = fminf(mindet, dets.hi);
+      lhs_factors_df(Gs, df_rcp(dets), s_sh, fs);  // = dN_c/dx . A
+    } else {
+      lhs_factors_df(g.G, df_rcp(g.det), s_std, fs);
+    }
+    df64 dpa = df_zero();
+#pragma unroll
+    for (int c = 0; c < 8; ++c) dpa = df_fma(fs[c], p[c], dpa);
+    out[ip] = df_to_double_bits(df_sub(m0, df_mul(tau, dpa)));
+  }
+  return f2d_bits(mindet);
+}
+
 // plain array accumulator (host check)
 struct ArrayAccDF {
   df64* m;

@@ -212,6 +212,7 @@ int launch_capture(nalu_ctx* ctx, int kernel, const nalu_assemble_opts& o, int64
 int launch_mdot(nalu_ctx* ctx, const nalu_assemble_opts& o);
 // assemble_df.cu (double-float element math for the scalar kernels)
 int launch_assemble_df(nalu_ctx* ctx, int kernel, const nalu_assemble_opts& o, int scatter);
+int launch_mdot_df(nalu_ctx* ctx, const nalu_assemble_opts& o);  // ComputeMdot, df64 element math
 int launch_capture_df(nalu_ctx* ctx, int kernel, const nalu_assemble_opts& o, int64_t elem, double* d_lhs,
                       double* d_rhs);
 int launch_slot_table(nalu_ctx* ctx);

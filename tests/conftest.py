@@ -52,6 +52,7 @@ def elemcheck():
     L.hc_scalar_diff_df.argtypes = [P, P, P, ctypes.c_int, P, P]
     L.hc_continuity_df.argtypes = [P] * 5 + [ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P]
     L.hc_mdot.argtypes = [P] * 5 + [ctypes.c_double, ctypes.c_int, ctypes.c_int, P]
+    L.hc_mdot_df.argtypes = [P] * 5 + [ctypes.c_double, ctypes.c_int, ctypes.c_int, P]
     return L
 
 

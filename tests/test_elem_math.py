@@ -79,6 +79,22 @@ def test_mdot_random_elements(elemcheck, oracle, sm, sp):
         check_dense(m2[None], m1[None], what="mdot")
 
 
+@pytest.mark.parametrize("sm,sp", [(0, 0), (1, 0), (0, 1), (1, 1)])
+def test_mdot_df_random_elements(elemcheck, oracle, sm, sp):
+    """df64 mdot (the ARITH_DF64 ComputeMdot kernel's element math) against the
+    FP64 oracle: |a - b| <= 1e-12 (max |b|) + ..., helpers.check_dense"""
+    rng = np.random.default_rng(31)
+    for t in range(200):
+        h = rng.uniform(1 / 128, 1 / 8)
+        c = np.ascontiguousarray((BASE + 0.2 * rng.uniform(-1, 1, (8, 3))) * h + rng.uniform(0, 1, 3))
+        u, gp = np.ascontiguousarray(rng.normal(size=(8, 3))), np.ascontiguousarray(rng.normal(size=(8, 3)))
+        rho, p, tau = rng.uniform(0.5, 2, 8), rng.normal(size=8), rng.uniform(0.1, 2)
+        m1 = oracle.mdot_elem(c, rho, u, p, gp, tau, sm, sp)
+        m2 = np.zeros(12)
+        elemcheck.hc_mdot_df(P(c), P(rho), P(u), P(p), P(gp), float(tau), sm, sp, P(m2))
+        check_dense(m2[None], m1[None], what="mdot df64")
+
+
 # ---- double-float (df64) element math of the ARITH_DF64 kernels -------------
 def _hc_scalar_df(L, c, q, k, sh):
     lhs, rhs = np.zeros(64), np.zeros(8)

@@ -190,14 +190,16 @@ def test_continuity_128_properties(gpu_ctx_factory, oracle):
     ctx.close()
 
 
-def test_mdot_matches_oracle(gpu_ctx_factory, oracle):
+@pytest.mark.parametrize("arith", [ng.ARITH_FP64, ng.ARITH_DF64])
+def test_mdot_matches_oracle(gpu_ctx_factory, oracle, arith):
     c, conn, gid = block_mesh(7, 6, 5, jitter=0.1, seed=8)
     u, rho, p, gp = continuity_fields(c, seed=9)
     ctx = _ctx(gpu_ctx_factory, c, conn, gid)
     for n, v in (("velocity_rtm", u), ("density", rho), ("pressure", p), ("dpdx", gp)):
         ctx.field_set(n, v)
     for sm, sp in [(0, 0), (1, 0), (0, 1), (1, 1)]:
-        ctx.compute_mdot(ng.default_assemble_opts(shift_mdot=sm, shift_poisson=sp, proj_time_scale=0.5))
+        ctx.compute_mdot(ng.default_assemble_opts(shift_mdot=sm, shift_poisson=sp, proj_time_scale=0.5,
+                                                  arith=arith))
         m = ctx.field_get("mass_flow_rate_scs", (conn.shape[0], 12))
         om = np.stack([oracle.mdot_elem(c[e], rho[e], u[e], p[e], gp[e], 0.5, sm, sp) for e in conn])
         check_dense(m, om, what="mdot")
