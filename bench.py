@@ -416,6 +416,10 @@ def bench_aux(ng, ctx, c, conn, rho):
     out["dual_volume_ms"] = timed_ms(ctx, ctx.compute_dual_volume)
     out["nodal_gradient_pressure_ms"] = timed_ms(ctx, lambda: ctx.compute_nodal_gradient("pressure", "dpdx"))
     out["nodal_gradient_velocity_ms"] = timed_ms(ctx, lambda: ctx.compute_nodal_gradient("velocity", "dudx"))
+    out["nodal_gradient_pressure_df64_ms"] = timed_ms(
+        ctx, lambda: ctx.compute_nodal_gradient("pressure", "dpdx", arith=ng.ARITH_DF64))
+    out["nodal_gradient_velocity_df64_ms"] = timed_ms(
+        ctx, lambda: ctx.compute_nodal_gradient("velocity", "dudx", arith=ng.ARITH_DF64))
     t0 = time.perf_counter()
     nf = ctx.faceset_skin(0)
     out["skin_faces"] = nf

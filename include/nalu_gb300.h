@@ -207,8 +207,9 @@ int nalu_capture_scv_volumes(nalu_ctx* ctx, int64_t elem, double* vol);
  * (dst 9 components, d src_i / dx_j at 3 i + j, e.g. VELOCITY -> DUDX).
  * Needs NALU_FIELD_DUAL_VOLUME.  The boundary-face closure
  * (AssembleNodalGradBoundaryAlgorithm) is not part of this call.
- * shifted: shifted_shape_fcn at the ips. */
-int nalu_compute_nodal_gradient(nalu_ctx* ctx, int src_field, int dst_field, int shifted);
+ * shifted: shifted_shape_fcn at the ips.  arith: NALU_ARITH_FP64, or
+ * NALU_ARITH_DF64 (areas and sums as FP32 pairs, about 48 bits). */
+int nalu_compute_nodal_gradient(nalu_ctx* ctx, int src_field, int dst_field, int shifted, int arith);
 
 /* ---- boundary faces ------------------------------------------------------
  * A side set is a list of element sides, as the mesh's boundary parts hold

@@ -123,7 +123,7 @@ def lib():
             "nalu_compute_mdot": (I, [P, P]),
             "nalu_compute_dual_volume": (I, [P]),
             "nalu_capture_scv_volumes": (I, [P, I64, P]),
-            "nalu_compute_nodal_gradient": (I, [P, I, I, I]),
+            "nalu_compute_nodal_gradient": (I, [P, I, I, I, I]),
             "nalu_linsys_write_system": (I, [P, ctypes.c_char_p]),
             "nalu_linsys_write_solution": (I, [P, ctypes.c_char_p]),
             "nalu_faceset_define": (I, [P, I, I64, P, P]),
@@ -316,9 +316,9 @@ class Context:
         self._check(lib().nalu_capture_scv_volumes(self._h, int(elem), _ptr(v)), "capture_scv_volumes")
         return v
 
-    def compute_nodal_gradient(self, src, dst, shifted=False):
-        self._check(lib().nalu_compute_nodal_gradient(self._h, FIELD[src], FIELD[dst], int(bool(shifted))),
-                    "compute_nodal_gradient")
+    def compute_nodal_gradient(self, src, dst, shifted=False, arith=ARITH_FP64):
+        self._check(lib().nalu_compute_nodal_gradient(self._h, FIELD[src], FIELD[dst], int(bool(shifted)),
+                                                      int(arith)), "compute_nodal_gradient")
 
     # MatrixMarket dumps
     def write_system(self, base):

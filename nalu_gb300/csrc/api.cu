@@ -868,7 +868,7 @@ int nalu_capture_scv_volumes(nalu_ctx* ctx, int64_t elem, double* vol) {
   return NALU_OK;
 }
 
-int nalu_compute_nodal_gradient(nalu_ctx* ctx, int src_field, int dst_field, int shifted) {
+int nalu_compute_nodal_gradient(nalu_ctx* ctx, int src_field, int dst_field, int shifted, int arith) {
   if (!ctx || src_field < 0 || src_field >= NALU_FIELD_COUNT || dst_field < 0 || dst_field >= NALU_FIELD_COUNT ||
       src_field == NALU_FIELD_MDOT_SCS || dst_field == NALU_FIELD_MDOT_SCS || src_field == dst_field)
     return set_error(ctx, NALU_ERR_ARG, "gradient fields");
@@ -882,8 +882,9 @@ int nalu_compute_nodal_gradient(nalu_ctx* ctx, int src_field, int dst_field, int
   Field& g = ctx->fields[dst_field];
   if (g.d.n != ctx->n_nodes * dc) NALU_CUDA(ctx, g.d.alloc(ctx->n_nodes * dc));
   g.comps = dc;
+  if (arith != NALU_ARITH_FP64 && arith != NALU_ARITH_DF64) return set_error(ctx, NALU_ERR_ARG, "arith");
   int rc = launch_nodal_grad(ctx, ctx->fields[src_field].d.p, sc, ctx->fields[NALU_FIELD_DUAL_VOLUME].d.p, g.d.p,
-                             shifted != 0);
+                             shifted != 0, arith);
   if (rc) return rc;
   g.set = true;
   return NALU_OK;

@@ -22,6 +22,7 @@
 #include <cstdint>
 
 #include "hex8_elem.h"
+#include "hex8_elem_df.h"
 #include "internal.h"
 #include "scv.cuh"
 
@@ -140,6 +141,75 @@ __global__ void __launch_bounds__(128) k_nodal_grad(int64_t n_elems, const int32
   }
 }
 
+// the three SCS ips of each node (lrscv: node left (+) or right (-) of the ip)
+__constant__ int8_t c_node_ip[8][3] = {{0, 3, 8}, {0, 1, 9}, {1, 2, 10}, {2, 3, 11},
+                                       {4, 7, 8}, {4, 5, 9}, {5, 6, 10}, {6, 7, 11}};
+
+// Element part of the projected nodal gradient in df64: node by node (a
+// warp-uniform loop), the node's three SCS contributions +-q_ip A summed as
+// FP32 pairs in registers, then NC x 3 FP64 atomics scaled by 1/V.  Areas
+// are formed per (node, ip), i.e. twice per ip, on the FP32 pipes.
+template <int NC, bool SHIFT>
+__global__ void __launch_bounds__(128) k_nodal_grad_df(int64_t n_elems, const int32_t* __restrict__ conn,
+                                                       const double* __restrict__ x, const double* __restrict__ q,
+                                                       const double* __restrict__ dvol, double* grad) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n_elems) return;
+  int nd[8];
+  double xc[8][3];
+#pragma unroll
+  for (int n = 0; n < 8; ++n) {
+    nd[n] = __ldg(conn + 8 * e + n);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) xc[n][d] = __ldg(x + 3 * (int64_t)nd[n] + d);
+  }
+  EdgeFormDF f;
+  {
+    df64 dd[8][3];
+    rel_coords_df(xc, dd);
+    edge_form_df(dd, f);
+  }
+  df64 qn[8][NC];
+#pragma unroll
+  for (int n = 0; n < 8; ++n)
+#pragma unroll
+    for (int k = 0; k < NC; ++k) qn[n][k] = df_split_bits(__ldg(q + (int64_t)nd[n] * NC + k));
+#pragma unroll 1
+  for (int r = 0; r < 8; ++r) {
+    df64 acc[NC][3];
+#pragma unroll
+    for (int k = 0; k < NC; ++k) acc[k][0] = acc[k][1] = acc[k][2] = df_zero();
+#pragma unroll 1
+    for (int t = 0; t < 3; ++t) {
+      const int ip = c_node_ip[r][t];
+      IpGeomDF g;
+      ip_geometry_df(f, ip, g);
+      float s[3];
+      ip_location(ip, SHIFT ? 0.5f : 0.25f, s);
+      const float sg = ip_left(ip) == r ? 1.0f : -1.0f;
+#pragma unroll
+      for (int k = 0; k < NC; ++k) {
+        df64 qi = df_zero();
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+          const float w = (0.5f + corner_sign(c, 0) * s[0]) * (0.5f + corner_sign(c, 1) * s[1]) *
+                          (0.5f + corner_sign(c, 2) * s[2]);  // exact
+          qi = df_add(qi, df_mul_f(qn[c][k], w));
+        }
+        qi = df_mul_f(qi, sg);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) acc[k][j] = df_fma(qi, g.area[j], acc[k][j]);
+      }
+    }
+    const double inv = 1.0 / __ldg(dvol + nd[r]);
+#pragma unroll
+    for (int k = 0; k < NC; ++k)
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+        atomicAdd(grad + ((int64_t)nd[r] * NC + k) * 3 + j, df_to_double_bits(acc[k][j]) * inv);
+  }
+}
+
 __global__ void k_zero(int64_t n, double* p) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) p[i] = 0.0;
@@ -174,14 +244,23 @@ int ensure_scv_cache(nalu_ctx* ctx) {
   return launch_dual_volume(ctx, nullptr, -1, nullptr);
 }
 
-int launch_nodal_grad(nalu_ctx* ctx, const double* q, int ncomp, const double* dvol, double* grad, bool shifted) {
+int launch_nodal_grad(nalu_ctx* ctx, const double* q, int ncomp, const double* dvol, double* grad, bool shifted,
+                      int arith) {
   const int64_t E = ctx->n_elems;
   const int64_t total = ctx->n_nodes * 3 * ncomp;
   if (E <= 0 || total <= 0) return NALU_OK;
   k_zero<<<(unsigned)((total + 255) / 256), 256, 0, ctx->stream>>>(total, grad);
   const unsigned grid = (unsigned)((E + 127) / 128);
   const double* x = ctx->fields[NALU_FIELD_COORDINATES].d.p;
-  if (ncomp == 1) {
+  if (arith == NALU_ARITH_DF64) {
+    if (ncomp == 1) {
+      if (shifted) k_nodal_grad_df<1, true><<<grid, 128, 0, ctx->stream>>>(E, ctx->d_conn.p, x, q, dvol, grad);
+      else k_nodal_grad_df<1, false><<<grid, 128, 0, ctx->stream>>>(E, ctx->d_conn.p, x, q, dvol, grad);
+    } else {
+      if (shifted) k_nodal_grad_df<3, true><<<grid, 128, 0, ctx->stream>>>(E, ctx->d_conn.p, x, q, dvol, grad);
+      else k_nodal_grad_df<3, false><<<grid, 128, 0, ctx->stream>>>(E, ctx->d_conn.p, x, q, dvol, grad);
+    }
+  } else if (ncomp == 1) {
     if (shifted) k_nodal_grad<1, true><<<grid, 128, 0, ctx->stream>>>(E, ctx->d_conn.p, x, q, dvol, grad);
     else k_nodal_grad<1, false><<<grid, 128, 0, ctx->stream>>>(E, ctx->d_conn.p, x, q, dvol, grad);
   } else {

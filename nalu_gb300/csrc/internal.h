@@ -222,7 +222,8 @@ int launch_mass(nalu_ctx* ctx, int kernel, const nalu_assemble_opts& o, int scat
 int launch_dual_volume(nalu_ctx* ctx, double* vol, int64_t cap_elem, double* cap);
 // make d_scv hold the current coordinates' SCV volumes
 int ensure_scv_cache(nalu_ctx* ctx);
-int launch_nodal_grad(nalu_ctx* ctx, const double* q, int ncomp, const double* dvol, double* grad, bool shifted);
+int launch_nodal_grad(nalu_ctx* ctx, const double* q, int ncomp, const double* dvol, double* grad, bool shifted,
+                      int arith);
 int launch_expand_graph(nalu_ctx* ctx);
 int launch_sum_into(nalu_ctx* ctx, int64_t n, const int64_t* d_elems, const double* d_lhs,
                     const double* d_rhs);

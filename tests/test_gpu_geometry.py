@@ -3,7 +3,7 @@ dual_nodal_volume (HexSCV::determinant scattered to the nodes) and the element
 part of the projected nodal gradient (AssembleNodalGradElemAlgorithm and its
 velocity form).  The device sums element contributions with atomics, so the
 order of the (at most 8 per node) additions varies: tolerance
-|a - b| <= 1e-13 max|b| for the gradient.  Volumes: 1e-13 relative.  The
+|a - b| <= 1e-13 max|b| for the gradient (FP64 and df64 arithmetic).  Volumes: 1e-13 relative.  The
 device evaluates Grandy's volume in its face form about the element centroid;
 the reference's corner-coordinate form (which the oracle reproduces bit for
 bit) carries up to ~1e-14 relative rounding of its own on small elements away
@@ -45,8 +45,9 @@ def test_dual_volume(gpu_ctx_factory, oracle, case):
     ctx.close()
 
 
+@pytest.mark.parametrize("arith", [ng.ARITH_FP64, ng.ARITH_DF64])
 @pytest.mark.parametrize("shifted", [False, True])
-def test_nodal_gradient(gpu_ctx_factory, oracle, shifted):
+def test_nodal_gradient(gpu_ctx_factory, oracle, shifted, arith):
     c, conn, _ = block_mesh(19, 14, 9, jitter=0.3, seed=8)
     n = c.shape[0]
     rng = np.random.default_rng(11)
@@ -56,17 +57,17 @@ def test_nodal_gradient(gpu_ctx_factory, oracle, shifted):
     ctx.compute_dual_volume()
     vol = oracle.dual_volume(c, conn)
     ctx.field_set("pressure", p)
-    ctx.compute_nodal_gradient("pressure", "dpdx", shifted)
+    ctx.compute_nodal_gradient("pressure", "dpdx", shifted, arith)
     got = ctx.field_get("dpdx", (n, 3))
     ref = oracle.nodal_grad_elem(c, conn, p, vol, shifted)
     assert np.max(np.abs(got - ref)) <= 1e-13 * np.max(np.abs(ref))
     ctx.field_set("velocity", u)
-    ctx.compute_nodal_gradient("velocity", "dudx", shifted)
+    ctx.compute_nodal_gradient("velocity", "dudx", shifted, arith)
     got = ctx.field_get("dudx", (n, 9)).reshape(n, 3, 3)
     ref = oracle.nodal_grad_elem(c, conn, u, vol, shifted)
     assert np.max(np.abs(got - ref)) <= 1e-13 * np.max(np.abs(ref))
     # a second call overwrites (zeroes first) rather than accumulates
-    ctx.compute_nodal_gradient("velocity", "dudx", shifted)
+    ctx.compute_nodal_gradient("velocity", "dudx", shifted, arith)
     again = ctx.field_get("dudx", (n, 9)).reshape(n, 3, 3)
     assert np.max(np.abs(again - ref)) <= 1e-13 * np.max(np.abs(ref))
     ctx.close()
