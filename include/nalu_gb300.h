@@ -211,6 +211,33 @@ int nalu_capture_scv_volumes(nalu_ctx* ctx, int64_t elem, double* vol);
  * NALU_ARITH_DF64 (areas and sums as FP32 pairs, about 48 bits). */
 int nalu_compute_nodal_gradient(nalu_ctx* ctx, int src_field, int dst_field, int shifted, int arith);
 
+/* ---- Hex8 master element, batched (src/master_element/Hex8CVFEM.C) --------
+ * MasterElement calls for nelem elements at once, evaluated on the device:
+ * coords [nelem][8][3] in the element's node order; outputs per element in
+ * the reference's layouts.  on_device: the arrays are device pointers (else
+ * host arrays, copied).  The grad ops return NALU_ERR_NEG_JACOBIAN when some
+ * element has det(J) <= 0 at one of its points (outputs still written). */
+/* HexSCS::determinant (:547-580): areav [nelem][12][3] */
+int nalu_hex_scs_determinant(nalu_ctx* ctx, int64_t nelem, const double* coords, double* areav, int on_device);
+/* HexSCS::grad_op / shifted_grad_op (:523-541, generic_grad_op):
+ * gradop, deriv [nelem][12][8][3] (deriv may be NULL) */
+int nalu_hex_scs_grad_op(nalu_ctx* ctx, int64_t nelem, const double* coords, int shifted, double* gradop,
+                         double* deriv, int on_device);
+/* HexSCV::grad_op / shifted_grad_op (:185-232): [nelem][8][8][3] */
+int nalu_hex_scv_grad_op(nalu_ctx* ctx, int64_t nelem, const double* coords, int shifted, double* gradop,
+                         double* deriv, int on_device);
+/* HexSCV::determinant (:149-180): vol [nelem][8] */
+int nalu_hex_scv_determinant(nalu_ctx* ctx, int64_t nelem, const double* coords, double* vol, int on_device);
+/* HexSCS::face_grad_op / shifted_face_grad_op (:668-684) at the exposed-face
+ * ips of side side[e] of each element: gradop [nelem][4][8][3] */
+int nalu_hex_face_grad_op(nalu_ctx* ctx, int64_t nelem, const int32_t* side, const double* coords, int shifted,
+                          double* gradop, int on_device);
+/* constant tables: HexSCS::adjacentNodes (lrscv_, int[24]), HexSCS::shape_fcn /
+ * shifted_shape_fcn ([12][8]), HexSCS::side_node_ordinals (int[4]) */
+void nalu_hex_scs_adjacent_nodes(int32_t* lrscv);
+void nalu_hex_scs_shape_fcn(int shifted, double* shp);
+void nalu_hex_side_node_ordinals(int side, int32_t* nodes4);
+
 /* ---- boundary faces ------------------------------------------------------
  * A side set is a list of element sides, as the mesh's boundary parts hold
  * them: face k is side side[k] of element elem[k], with the Hex8 side

@@ -126,6 +126,14 @@ def lib():
             "nalu_compute_nodal_gradient": (I, [P, I, I, I, I]),
             "nalu_linsys_write_system": (I, [P, ctypes.c_char_p]),
             "nalu_linsys_write_solution": (I, [P, ctypes.c_char_p]),
+            "nalu_hex_scs_determinant": (I, [P, I64, P, P, I]),
+            "nalu_hex_scs_grad_op": (I, [P, I64, P, I, P, P, I]),
+            "nalu_hex_scv_grad_op": (I, [P, I64, P, I, P, P, I]),
+            "nalu_hex_scv_determinant": (I, [P, I64, P, P, I]),
+            "nalu_hex_face_grad_op": (I, [P, I64, P, P, I, P, I]),
+            "nalu_hex_scs_adjacent_nodes": (None, [P]),
+            "nalu_hex_scs_shape_fcn": (None, [I, P]),
+            "nalu_hex_side_node_ordinals": (None, [I, P]),
             "nalu_faceset_define": (I, [P, I, I64, P, P]),
             "nalu_faceset_skin": (I, [P, I, ctypes.POINTER(I64)]),
             "nalu_faceset_size": (I, [P, I, ctypes.POINTER(I64)]),
@@ -326,6 +334,41 @@ class Context:
 
     def write_solution(self, base):
         self._check(lib().nalu_linsys_write_solution(self._h, os.fsencode(base)), "write_solution")
+
+    # Hex8 master element, batched over elements (coords [nelem, 8, 3])
+    def hex_scs_determinant(self, coords):
+        c = np.ascontiguousarray(coords, np.float64).reshape(-1, 8, 3)
+        a = np.zeros((c.shape[0], 12, 3))
+        self._check(lib().nalu_hex_scs_determinant(self._h, c.shape[0], _ptr(c), _ptr(a), 0), "hex_scs_determinant")
+        return a
+
+    def hex_scs_grad_op(self, coords, shifted=False):
+        c = np.ascontiguousarray(coords, np.float64).reshape(-1, 8, 3)
+        g, d = np.zeros((c.shape[0], 12, 8, 3)), np.zeros((c.shape[0], 12, 8, 3))
+        self._check(lib().nalu_hex_scs_grad_op(self._h, c.shape[0], _ptr(c), int(bool(shifted)), _ptr(g), _ptr(d), 0),
+                    "hex_scs_grad_op")
+        return g, d
+
+    def hex_scv_grad_op(self, coords, shifted=False):
+        c = np.ascontiguousarray(coords, np.float64).reshape(-1, 8, 3)
+        g, d = np.zeros((c.shape[0], 8, 8, 3)), np.zeros((c.shape[0], 8, 8, 3))
+        self._check(lib().nalu_hex_scv_grad_op(self._h, c.shape[0], _ptr(c), int(bool(shifted)), _ptr(g), _ptr(d), 0),
+                    "hex_scv_grad_op")
+        return g, d
+
+    def hex_scv_determinant(self, coords):
+        c = np.ascontiguousarray(coords, np.float64).reshape(-1, 8, 3)
+        v = np.zeros((c.shape[0], 8))
+        self._check(lib().nalu_hex_scv_determinant(self._h, c.shape[0], _ptr(c), _ptr(v), 0), "hex_scv_determinant")
+        return v
+
+    def hex_face_grad_op(self, coords, side, shifted=False):
+        c = np.ascontiguousarray(coords, np.float64).reshape(-1, 8, 3)
+        sd = np.ascontiguousarray(side, np.int32)
+        g = np.zeros((c.shape[0], 4, 8, 3))
+        self._check(lib().nalu_hex_face_grad_op(self._h, c.shape[0], _ptr(sd), _ptr(c), int(bool(shifted)), _ptr(g),
+                                                0), "hex_face_grad_op")
+        return g
 
     # boundary faces (side sets)
     def faceset_define(self, set_id, elem, side):

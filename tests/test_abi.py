@@ -49,3 +49,24 @@ def test_null_arguments_are_rejected(cudalib):
     assert L.nalu_create(0, None) == -1
     assert L.nalu_destroy(None) == -1
     assert L.nalu_mesh_create(None, 8, 1, None, None, None) == -1
+
+
+def test_master_element_tables(cudalib, oracle):
+    """HexSCS::adjacentNodes, shape_fcn / shifted_shape_fcn and the side node
+    ordinals from the library's host tables equal the oracle's (pinned to the
+    compiled reference)"""
+    import ctypes
+    import numpy as np
+    P = lambda a: ctypes.c_void_p(a.ctypes.data)
+    lr = np.zeros(24, np.int32)
+    cudalib.nalu_hex_scs_adjacent_nodes(P(lr))
+    olr, loc, locs = oracle.scs_tables()
+    assert np.array_equal(lr, olr)
+    for sh, iso in ((0, loc), (1, locs)):
+        shp = np.zeros(96)
+        cudalib.nalu_hex_scs_shape_fcn(sh, P(shp))
+        assert np.array_equal(shp.reshape(12, 8), oracle.shape_fcn(iso.reshape(12, 3)))
+    for s in range(6):
+        nd = np.zeros(4, np.int32)
+        cudalib.nalu_hex_side_node_ordinals(s, P(nd))
+        assert np.array_equal(nd, oracle.side_nodes(s))
