@@ -13,6 +13,7 @@ from helpers import block_mesh
 pytestmark = pytest.mark.gpu
 
 
+@pytest.mark.filterwarnings("ignore::DeprecationWarning")  # scipy's mmread return-type notice
 @pytest.mark.parametrize("num_dof", [1, 3])
 def test_write_system_and_solution(gpu_ctx_factory, tmp_path, num_dof):
     sio = pytest.importorskip("scipy.io")
