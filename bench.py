@@ -114,6 +114,21 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
+# FP64 work of the continuity element math, FLOP per element: SASS counters
+# (DADD + DMUL + 2 DFMA) of the FP64 variant of the same kernel over one
+# 128^3 launch (profiles/continuity_assembly_128_fp64_flops.md)
+FP64_FLOP_PER_ELEM = 2458
+
+
+def compute_roof(n_elems, kernel_ms, fp64_tflops):
+    """the assembly measured against the FP64 compute roof: FP64-equivalent
+    FLOP/s of the timed kernel over the measured FP64 rate"""
+    flops = FP64_FLOP_PER_ELEM * n_elems
+    achieved = flops / (kernel_ms * 1e-3) / 1e12
+    return {"fp64_flop_per_element": FP64_FLOP_PER_ELEM, "fp64_equivalent_tflops": achieved,
+            "fp64_peak_tflops": fp64_tflops, "frac_of_fp64_peak": achieved / fp64_tflops if fp64_tflops else None}
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -373,7 +388,8 @@ def bench_gpu(args):
                            parallelism="replicas" if ws > 1 else "single"),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "peak_kind": peak_kind, "algorithmic_bytes_per_launch": alg,
-                         "kernel_ms": avg_ms, "fp64_probe_tflops": fp64_peak},
+                         "kernel_ms": avg_ms, "fp64_probe_tflops": fp64_peak,
+                         "compute": compute_roof(n_elems, avg_ms, fp64_peak)},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches, "clocks": clk.summary(), "cpu_baseline": cpu, "solve": solve,
             "batch": batch, "momentum_c3": momentum, "heat_c1": heat, "geometry_boundary_time": aux}
