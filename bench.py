@@ -129,6 +129,18 @@ def compute_roof(n_elems, kernel_ms, fp64_tflops):
             "fp64_peak_tflops": fp64_tflops, "frac_of_fp64_peak": achieved / fp64_tflops if fp64_tflops else None}
 
 
+def solve_iteration_roof(ms, iterations, nnz, n):
+    """a Jacobi-PCG iteration against HBM: the compulsory bytes of an FP64 CSR
+    iteration (SpMV 12 nnz + 8 (n + 1) + 16 n, vector phase 64 n), per
+    iteration time"""
+    bytes_it = 12 * nnz + 8 * (n + 1) + 16 * n + 64 * n
+    us = 1e3 * ms / max(1, iterations)
+    gbs = bytes_it / (us * 1e-6) / 1e9
+    peak, kind = peaks()
+    return {"us": us, "algorithmic_bytes": bytes_it, "achieved_gbs": gbs, "frac_of_hbm": gbs / peak,
+            "peak_kind": kind, "bytes_definition": "FP64 CSR (12 B per entry) + vectors, counted once"}
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -334,6 +346,8 @@ def bench_gpu(args):
                            "outer_iterations": info.outer_iterations, "true_rel_res": info.true_rel_res,
                            "status": info.status}
         solve["system"] = "continuity Laplacian of the same mesh, pressure pinned at node 0 (resetRows + diag 1)"
+        solve["jacobi_pcg_fp64"]["per_iteration"] = solve_iteration_roof(
+            solve["jacobi_pcg_fp64"]["ms"], solve["jacobi_pcg_fp64"]["iterations"], nnz, n_rows)
         # learned preconditioner: 20K pairs from PCG's first direction for 4 seeded random rhs of this
         # 128^3 system, Adam on the GPU, then flexible CG with the learned stencil
         t0 = time.perf_counter()
