@@ -308,10 +308,12 @@ def bench_gpu(args):
     d2h = out_v.array.nbytes + out_r.array.nbytes
 
     def e2e_step():
-        # upload this step's inputs, assemble, start the download of the result;
-        # the download overlaps the next step's upload and assembly
+        # stage this step's inputs (upload stream, second field buffers), assemble
+        # (waits for them in stream order), start the download of the result
+        # (copy stream): the upload of step k+1 overlaps the assembly of step k,
+        # the download of step k the assembly of step k+1
         for nm, a in pin_in.items():
-            ctx.field_set_ptr(nm, a.ptr, a.array.size)
+            ctx.field_set_async_ptr(nm, a.ptr, a.array.size)
         ctx.zero()
         ctx.assemble(ng.KERNEL_CONTINUITY_ADV, opts)
         ctx.system_to_ptr_async(out_v.ptr, out_r.ptr)

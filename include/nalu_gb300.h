@@ -84,6 +84,15 @@ enum nalu_field {
 /* copy a field in (host or device source, caller node order) */
 int nalu_field_set(nalu_ctx* ctx, int field, const double* src, int64_t count, int src_is_device);
 int nalu_field_get(nalu_ctx* ctx, int field, double* dst, int64_t count, int dst_is_device);
+/* The same upload without joining the compute stream: the copy (from host
+ * memory, pinned with nalu_host_alloc for it to be asynchronous) runs on an
+ * upload stream into a second buffer of the field, and the next call that
+ * reads fields (assembly, mdot, gradients, face kernels, field_get, ...) waits
+ * for it in stream order and swaps it in.  The upload of step k+1 so overlaps
+ * the assembly of step k.  The host buffer must stay unchanged until then
+ * (nalu_synchronize waits for every stream).  No reference counterpart (STK
+ * fields live on the host). */
+int nalu_field_set_async(nalu_ctx* ctx, int field, const double* src, int64_t count);
 
 /* ---- linear system (LinearSystem, include/LinearSystem.h:39-167) -------- */
 /* buildElemToNodeGraph + finalizeLinearSystem (src/TpetraLinearSystem.C:430-435,

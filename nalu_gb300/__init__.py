@@ -104,6 +104,7 @@ def lib():
             "nalu_mesh_create": (I, [P, I64, I64, P, P, P]),
             "nalu_field_set": (I, [P, I, P, I64, I]),
             "nalu_field_get": (I, [P, I, P, I64, I]),
+            "nalu_field_set_async": (I, [P, I, P, I64]),
             "nalu_linsys_build_elem_graph": (I, [P, I]),
             "nalu_linsys_sizes": (I, [P, P, P, P]),
             "nalu_linsys_graph": (I, [P, P, P]),
@@ -534,6 +535,10 @@ class Context:
         self._check(lib().nalu_flush_l2(self._h, nbytes), "flush_l2")
 
     # raw pointer variants (pinned host buffers)
+    def field_set_async_ptr(self, name, ptr, count):
+        """staged upload from (pinned) host memory; swapped in by the next call that reads fields"""
+        self._check(lib().nalu_field_set_async(self._h, FIELD[name], ptr, count), "field_set_async(%s)" % name)
+
     def field_set_ptr(self, name, ptr, count):
         self._check(lib().nalu_field_set(self._h, FIELD[name], ptr, count, 0), "field_set(%s)" % name)
 

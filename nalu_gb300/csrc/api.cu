@@ -67,6 +67,26 @@ int field_comps(int f) {
   }
 }
 
+int resolve_uploads(nalu_ctx* ctx) {
+  if (!ctx->any_pending) return NALU_OK;
+  cudaSetDevice(ctx->device);
+  NALU_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->ev_uploaded, 0));
+  for (int fi = 0; fi < NALU_FIELD_COUNT; ++fi) {
+    Field& f = ctx->fields[fi];
+    if (!f.pending) continue;
+    f.swap_back();
+    f.pending = false;
+    f.set = true;
+    if (fi == NALU_FIELD_COORDINATES) ++ctx->coords_version;
+  }
+  // the retired buffers were read by the work queued so far; the next upload
+  // into them waits for this point
+  NALU_CUDA(ctx, cudaEventRecord(ctx->ev_released, ctx->stream));
+  ctx->released_recorded = true;
+  ctx->any_pending = false;
+  return NALU_OK;
+}
+
 }  // namespace nalu_gb300
 
 namespace {
@@ -178,6 +198,12 @@ int nalu_destroy(nalu_ctx* ctx) {
   s.sell.vald.free();
   s.sell.valf.free();
   if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
+  if (ctx->upload_stream) {
+    cudaStreamSynchronize(ctx->upload_stream);
+    cudaEventDestroy(ctx->ev_uploaded);
+    cudaEventDestroy(ctx->ev_released);
+    cudaStreamDestroy(ctx->upload_stream);
+  }
   if (ctx->ev_snap) cudaEventDestroy(ctx->ev_snap);
   if (ctx->ev_copied) cudaEventDestroy(ctx->ev_copied);
   if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
@@ -200,6 +226,7 @@ int nalu_synchronize(nalu_ctx* ctx) {
   if (!ctx) return NALU_ERR_ARG;
   NALU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   if (ctx->copy_stream) NALU_CUDA(ctx, cudaStreamSynchronize(ctx->copy_stream));
+  if (ctx->upload_stream) NALU_CUDA(ctx, cudaStreamSynchronize(ctx->upload_stream));
   ctx->copy_pending = false;
   return NALU_OK;
 }
@@ -263,6 +290,7 @@ int nalu_flush_l2(nalu_ctx* ctx, size_t bytes) {
 // ---- mesh -------------------------------------------------------------------
 int nalu_mesh_create(nalu_ctx* ctx, int64_t n_nodes, int64_t n_elems, const int32_t* conn, const int64_t* gid,
                      const double* coords) {
+  if (ctx) NALU_RESOLVE_UPLOADS(ctx);
   if (!ctx || n_nodes <= 0 || n_elems <= 0 || !conn || !coords) return set_error(ctx, NALU_ERR_ARG, "mesh args");
   if (n_nodes >= (int64_t)INT32_MAX / 3) return set_error(ctx, NALU_ERR_CAPACITY, "too many nodes for int32 LIDs");
   cudaSetDevice(ctx->device);
@@ -316,6 +344,8 @@ int nalu_field_set(nalu_ctx* ctx, int field, const double* src, int64_t count, i
   if (!ctx || field < 0 || field >= NALU_FIELD_COUNT || !src) return set_error(ctx, NALU_ERR_ARG, "field args");
   if (ctx->n_nodes == 0) return set_error(ctx, NALU_ERR_STATE, "no mesh");
   cudaSetDevice(ctx->device);
+  int rc0 = resolve_uploads(ctx);  // an earlier staged upload must not land after this one
+  if (rc0) return rc0;
   const int comps = field_comps(field);
   const bool elem = field == NALU_FIELD_MDOT_SCS;
   const int64_t n = elem ? ctx->n_elems : ctx->n_nodes;
@@ -340,8 +370,45 @@ int nalu_field_set(nalu_ctx* ctx, int field, const double* src, int64_t count, i
   return NALU_OK;
 }
 
+int nalu_field_set_async(nalu_ctx* ctx, int field, const double* src, int64_t count) {
+  if (!ctx || field < 0 || field >= NALU_FIELD_COUNT || !src) return set_error(ctx, NALU_ERR_ARG, "field args");
+  if (ctx->n_nodes == 0) return set_error(ctx, NALU_ERR_STATE, "no mesh");
+  const int comps = field_comps(field);
+  const bool elem = field == NALU_FIELD_MDOT_SCS;
+  const int64_t n = elem ? ctx->n_elems : ctx->n_nodes;
+  if (count != n * comps) return set_error(ctx, NALU_ERR_ARG, "field size mismatch");
+  cudaSetDevice(ctx->device);
+  if (!ctx->upload_stream) {
+    NALU_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->upload_stream, cudaStreamNonBlocking));
+    NALU_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_uploaded, cudaEventDisableTiming));
+    NALU_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_released, cudaEventDisableTiming));
+  }
+  Field& f = ctx->fields[field];
+  // buffers are (re)sized only when the field is new or changes size
+  if (f.d.n != count) NALU_CUDA(ctx, f.d.alloc(count));
+  if (f.back.n != count) NALU_CUDA(ctx, f.back.alloc(count));
+  if (ctx->released_recorded) NALU_CUDA(ctx, cudaStreamWaitEvent(ctx->upload_stream, ctx->ev_released, 0));
+  if (elem || ctx->identity_order) {
+    NALU_CUDA(ctx, cudaMemcpyAsync(f.back.p, src, sizeof(double) * count, cudaMemcpyHostToDevice, ctx->upload_stream));
+  } else {
+    if (f.stage.n != count) NALU_CUDA(ctx, f.stage.alloc(count));
+    NALU_CUDA(ctx, cudaMemcpyAsync(f.stage.p, src, sizeof(double) * count, cudaMemcpyHostToDevice, ctx->upload_stream));
+    int rc = launch_permute_in_on(ctx, ctx->upload_stream, f.stage.p, f.back.p, comps, n);
+    if (rc) return rc;
+  }
+  NALU_CUDA(ctx, cudaEventRecord(ctx->ev_uploaded, ctx->upload_stream));
+  f.comps = comps;
+  f.pending = true;
+  ctx->any_pending = true;
+  return NALU_OK;
+}
+
 int nalu_field_get(nalu_ctx* ctx, int field, double* dst, int64_t count, int dst_is_device) {
   if (!ctx || field < 0 || field >= NALU_FIELD_COUNT || !dst) return set_error(ctx, NALU_ERR_ARG, "field args");
+  {
+    const int rc0 = resolve_uploads(ctx);
+    if (rc0) return rc0;
+  }
   Field& f = ctx->fields[field];
   if (!f.set) return set_error(ctx, NALU_ERR_STATE, "field not set");
   if (count != f.d.n) return set_error(ctx, NALU_ERR_ARG, "field size mismatch");
@@ -753,6 +820,7 @@ double time_assemble(nalu_ctx* ctx, int kernel, const nalu_assemble_opts& o, int
 }  // namespace
 
 int nalu_assemble(nalu_ctx* ctx, int kernel, const nalu_assemble_opts* opts) {
+  if (ctx) NALU_RESOLVE_UPLOADS(ctx);
   if (!ctx || !opts || kernel < 0 || kernel > NALU_KERNEL_MOMENTUM_MASS)
     return set_error(ctx, NALU_ERR_ARG, "assemble args");
   if (ctx->num_dof == 0) return set_error(ctx, NALU_ERR_STATE, "no graph");
@@ -802,6 +870,7 @@ int nalu_assemble(nalu_ctx* ctx, int kernel, const nalu_assemble_opts* opts) {
 
 int nalu_capture_element(nalu_ctx* ctx, int kernel, const nalu_assemble_opts* opts, int64_t elem, double* lhs,
                          double* rhs) {
+  if (ctx) NALU_RESOLVE_UPLOADS(ctx);
   if (!ctx || !opts || !lhs || !rhs || kernel < 0 || kernel > NALU_KERNEL_MOMENTUM_MASS)
     return set_error(ctx, NALU_ERR_ARG, "capture args");
   if (elem < 0 || elem >= ctx->n_elems) return set_error(ctx, NALU_ERR_ARG, "element out of range");
@@ -828,6 +897,7 @@ int nalu_capture_element(nalu_ctx* ctx, int kernel, const nalu_assemble_opts* op
 }
 
 int nalu_compute_mdot(nalu_ctx* ctx, const nalu_assemble_opts* opts) {
+  if (ctx) NALU_RESOLVE_UPLOADS(ctx);
   if (!ctx || !opts) return NALU_ERR_ARG;
   for (int f : {NALU_FIELD_COORDINATES, NALU_FIELD_DENSITY, NALU_FIELD_VELOCITY_RTM, NALU_FIELD_PRESSURE, NALU_FIELD_DPDX})
     if (!ctx->fields[f].set) return set_error(ctx, NALU_ERR_STATE, "mdot input field not set");
@@ -843,6 +913,7 @@ int nalu_compute_mdot(nalu_ctx* ctx, const nalu_assemble_opts* opts) {
 
 // ---- nodal geometry and gradients -------------------------------------------------
 int nalu_compute_dual_volume(nalu_ctx* ctx) {
+  if (ctx) NALU_RESOLVE_UPLOADS(ctx);
   if (!ctx) return NALU_ERR_ARG;
   if (!ctx->fields[NALU_FIELD_COORDINATES].set) return set_error(ctx, NALU_ERR_STATE, "no mesh");
   cudaSetDevice(ctx->device);
@@ -856,6 +927,7 @@ int nalu_compute_dual_volume(nalu_ctx* ctx) {
 }
 
 int nalu_capture_scv_volumes(nalu_ctx* ctx, int64_t elem, double* vol) {
+  if (ctx) NALU_RESOLVE_UPLOADS(ctx);
   if (!ctx || !vol || elem < 0 || elem >= ctx->n_elems) return NALU_ERR_ARG;
   if (!ctx->fields[NALU_FIELD_COORDINATES].set) return set_error(ctx, NALU_ERR_STATE, "no mesh");
   cudaSetDevice(ctx->device);
@@ -869,6 +941,7 @@ int nalu_capture_scv_volumes(nalu_ctx* ctx, int64_t elem, double* vol) {
 }
 
 int nalu_compute_nodal_gradient(nalu_ctx* ctx, int src_field, int dst_field, int shifted, int arith) {
+  if (ctx) NALU_RESOLVE_UPLOADS(ctx);
   if (!ctx || src_field < 0 || src_field >= NALU_FIELD_COUNT || dst_field < 0 || dst_field >= NALU_FIELD_COUNT ||
       src_field == NALU_FIELD_MDOT_SCS || dst_field == NALU_FIELD_MDOT_SCS || src_field == dst_field)
     return set_error(ctx, NALU_ERR_ARG, "gradient fields");

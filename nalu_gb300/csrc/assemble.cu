@@ -472,6 +472,11 @@ int launch_permute_in(nalu_ctx* ctx, const double* src, double* dst, int comps, 
   ctx->launches++;
   return cuda_check(ctx, cudaGetLastError(), "permute launch");
 }
+int launch_permute_in_on(nalu_ctx* ctx, cudaStream_t st, const double* src, double* dst, int comps, int64_t n) {
+  k_permute<<<(unsigned)blocks_for(n, 256), 256, 0, st>>>(src, dst, ctx->d_lid.p, comps, n, 1);
+  ctx->launches++;
+  return cuda_check(ctx, cudaGetLastError(), "permute launch");
+}
 int launch_permute_out(nalu_ctx* ctx, const double* src, double* dst, int comps, int64_t n) {
   k_permute<<<(unsigned)blocks_for(n, 256), 256, 0, ctx->stream>>>(src, dst, ctx->d_lid.p, comps, n, 0);
   ctx->launches++;

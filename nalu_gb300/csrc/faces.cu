@@ -427,6 +427,7 @@ using namespace nalu_gb300;
 extern "C" {
 
 int nalu_faceset_define(nalu_ctx* ctx, int set, int64_t n, const int64_t* elem, const int32_t* side) {
+  if (ctx) NALU_RESOLVE_UPLOADS(ctx);
   if (!ctx || set < 0 || set >= NALU_MAX_FACE_SETS || n < 0 || (n > 0 && (!elem || !side)))
     return set_error(ctx, NALU_ERR_ARG, "face set args");
   if (!ctx->fields[NALU_FIELD_COORDINATES].set) return set_error(ctx, NALU_ERR_STATE, "no mesh");
@@ -456,6 +457,7 @@ int nalu_faceset_define(nalu_ctx* ctx, int set, int64_t n, const int64_t* elem, 
 }
 
 int nalu_faceset_skin(nalu_ctx* ctx, int set, int64_t* n_faces) {
+  if (ctx) NALU_RESOLVE_UPLOADS(ctx);
   if (!ctx || set < 0 || set >= NALU_MAX_FACE_SETS) return set_error(ctx, NALU_ERR_ARG, "face set args");
   if (!ctx->fields[NALU_FIELD_COORDINATES].set) return set_error(ctx, NALU_ERR_STATE, "no mesh");
   cudaSetDevice(ctx->device);
@@ -531,6 +533,7 @@ int nalu_faceset_dynamic_pressure(nalu_ctx* ctx, int set, const double* dynp) {
 }
 
 int nalu_faceset_exposed_area(nalu_ctx* ctx, int set, double* area) {
+  if (ctx) NALU_RESOLVE_UPLOADS(ctx);
   if (!ctx || !area) return NALU_ERR_ARG;
   int rc = check_set(ctx, set);
   if (rc) return rc;
@@ -550,6 +553,7 @@ int nalu_faceset_exposed_area(nalu_ctx* ctx, int set, double* area) {
 }
 
 int nalu_nodal_gradient_boundary(nalu_ctx* ctx, int set, int src_field, int dst_field, int shifted) {
+  if (ctx) NALU_RESOLVE_UPLOADS(ctx);
   if (!ctx) return NALU_ERR_ARG;
   int rc = check_set(ctx, set);
   if (rc) return rc;
@@ -578,6 +582,7 @@ int nalu_nodal_gradient_boundary(nalu_ctx* ctx, int set, int src_field, int dst_
 }
 
 static int face_kernel_setup(nalu_ctx* ctx, int set, int kernel, const nalu_assemble_opts* o, FaceArgs& a) {
+  if (ctx) NALU_RESOLVE_UPLOADS(ctx);
   if (!ctx || !o) return NALU_ERR_ARG;
   int rc = check_set(ctx, set);
   if (rc) return rc;

@@ -6,6 +6,7 @@
 
 #include <cstdint>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/nalu_gb300.h"
@@ -56,6 +57,14 @@ struct Field {
   DBuf<double> d;
   int comps = 0;
   bool set = false;
+  // nalu_field_set_async: the next contents, uploaded on the upload stream,
+  // swapped into d by the next call that reads fields (stream order)
+  DBuf<double> back, stage;
+  bool pending = false;
+  void swap_back() {
+    std::swap(d.p, back.p);
+    std::swap(d.n, back.n);
+  }
 };
 
 // SELL-32 copy of the CRS matrix for the fast CG (cg_fast.cu)
@@ -186,6 +195,12 @@ struct nalu_ctx {
   // boundary side sets (nalu_faceset_define / nalu_faceset_skin)
   nalu_gb300::FaceSet face_sets[NALU_MAX_FACE_SETS];
 
+  // staged field uploads (nalu_field_set_async): a third stream, the event of
+  // the latest upload, and the event after which the retired buffers are free
+  cudaStream_t upload_stream = nullptr;
+  cudaEvent_t ev_uploaded = nullptr, ev_released = nullptr;
+  bool any_pending = false, released_recorded = false;
+
   // HexSCV volumes [E][8], kept while the coordinates do not change
   // (coords_version counts coordinate uploads)
   nalu_gb300::DBuf<double> d_scv;
@@ -198,6 +213,15 @@ enum FlagSlot { FLAG_NEG_JAC = 0, FLAG_GRAPH_MISS = 1, FLAG_CAPACITY = 2, FLAG_N
 
 int set_error(nalu_ctx* ctx, int status, const std::string& msg);
 int field_comps(int field);
+// swap in the fields staged by nalu_field_set_async (the main stream waits
+// for their upload); every call that reads fields starts with it
+int resolve_uploads(nalu_ctx* ctx);
+#define NALU_RESOLVE_UPLOADS(ctx)                  \
+  do {                                             \
+    const int rc_res_ = resolve_uploads(ctx);      \
+    if (rc_res_ != NALU_OK) return rc_res_;        \
+  } while (0)
+int launch_permute_in_on(nalu_ctx* ctx, cudaStream_t st, const double* src, double* dst, int comps, int64_t n);
 int cuda_check(nalu_ctx* ctx, cudaError_t e, const char* what);
 #define NALU_CUDA(ctx, call)                                      \
   do {                                                            \
