@@ -70,3 +70,15 @@ def test_master_element_tables(cudalib, oracle):
         nd = np.zeros(4, np.int32)
         cudalib.nalu_hex_side_node_ordinals(s, P(nd))
         assert np.array_equal(nd, oracle.side_nodes(s))
+    # interpolation at the ips reproduces a linear field on a distorted element
+    # (unit_tests/UnitTestMasterElements.C:64-102)
+    rng = np.random.default_rng(0)
+    x = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0], [0, 0, 1], [1, 0, 1], [1, 1, 1], [0, 1, 1]], float)
+    x = x + 0.2 * rng.uniform(-1, 1, (8, 3))
+    a, b = rng.standard_normal(3), rng.standard_normal()
+    for sh in (0, 1):
+        shp = np.zeros(96)
+        cudalib.nalu_hex_scs_shape_fcn(sh, P(shp))
+        shp = shp.reshape(12, 8)
+        assert np.allclose(shp @ (x @ a + b), (shp @ x) @ a + b, atol=1e-14)
+        assert np.allclose(shp.sum(axis=1), 1.0, atol=1e-15)

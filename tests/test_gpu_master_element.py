@@ -64,3 +64,28 @@ def test_master_element_golds_and_errors(gpu_ctx_factory, golds):
         ctx.hex_face_grad_op(BASE[None], [6])
     assert e.value.status == -1
     ctx.close()
+
+
+def test_master_element_properties(gpu_ctx_factory):
+    """the reference's master-element property tests
+    (unit_tests/UnitTestMasterElements.C:104-159, 185-228): the grad ops of
+    every point set reproduce the gradient of a random linear field exactly on
+    distorted elements; SCV volumes scale with det(QR) under a linear map"""
+    ctx = gpu_ctx_factory()
+    rng = np.random.default_rng(0)
+    c = _elements(200, 7)
+    a, b = rng.standard_normal(3), rng.standard_normal()
+    f = c @ a + b                                           # [200, 8]
+    for sh in (False, True):
+        for g in (ctx.hex_scs_grad_op(c, sh)[0], ctx.hex_scv_grad_op(c, sh)[0],
+                  ctx.hex_face_grad_op(c, np.arange(200) % 6, sh)):
+            grad = np.einsum("eknd,en->ekd", g, f)
+            assert np.max(np.abs(grad - a)) <= 1e-10 * np.max(np.abs(a))
+    q, _ = np.linalg.qr(rng.standard_normal((3, 3)))
+    m = q @ np.diag(rng.uniform(0.5, 1.5, 3))
+    if np.linalg.det(m) < 0:
+        m[:, 0] *= -1.0
+    v0 = ctx.hex_scv_determinant(c)
+    v1 = ctx.hex_scv_determinant(c @ m.T)
+    assert np.max(np.abs(v1 - np.linalg.det(m) * v0) / np.abs(v1)) <= 1e-12
+    ctx.close()
