@@ -441,11 +441,22 @@ __global__ void k_precond_apply_scale(int64_t n, const int64_t* __restrict__ spt
 //   z = M r;  beta = -(z . q_old) / (p_old . q_old);  p = z + beta p
 //   q = A p;  alpha = (p . r) / (p . q);  x += alpha p;  r -= alpha q
 // ---------------------------------------------------------------------------
-// z_row = sum_k w[base + 32 k] r[col_k] in FP32, col_k from the 32-bit
+// FP32 -> BF16, round to nearest even (finite values; the SPD scaling keeps
+// the stencil finite)
+__global__ void k_to_bf16(int64_t n, const float* __restrict__ w, uint16_t* __restrict__ w16) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t u = __float_as_uint(w[i]);
+  w16[i] = (uint16_t)((u + 0x7fffu + ((u >> 16) & 1u)) >> 16);
+}
+
+__device__ __forceinline__ float bf16_f(uint16_t h) { return __uint_as_float((uint32_t)h << 16); }
+
+// z_row = sum_k w[base + 32 k] r[col_k] in FP32 (w as BF16), col_k from the 32-bit
 // indices (WIDE) or the 16-bit offsets from the slice's entry bases
 template <bool WIDE>
 __device__ __forceinline__ float prec_row(int64_t base, int len, const SellMatrix::View& S,
-                                          const int32_t* __restrict__ cbase, const float* __restrict__ w,
+                                          const int32_t* __restrict__ cbase, const uint16_t* __restrict__ w,
                                           const float2* __restrict__ r2) {
   float acc = 0.0f;
   for (int k = 0; k < len; k += 8) {  // loads of a group issued before the gathers
@@ -456,7 +467,7 @@ __device__ __forceinline__ float prec_row(int64_t base, int len, const SellMatri
       const bool in = k + u < len;
       const int64_t e = base + (int64_t)(k + u) * kSlice;
       c[u] = in ? (WIDE ? __ldg(S.col + e) : __ldg(cbase + k + u) + (int32_t)__ldg(S.col16 + e)) : -1;
-      a[u] = in ? __ldg(w + e) : 0.0f;
+      a[u] = in ? bf16_f(__ldg(w + e)) : 0.0f;
     }
 #pragma unroll
     for (int u = 0; u < 8; ++u) b[u] = c[u] >= 0 ? __ldg(r2 + c[u]).x : 0.0f;
@@ -468,7 +479,7 @@ __device__ __forceinline__ float prec_row(int64_t base, int len, const SellMatri
 
 // z = M r (FP32 stencil values, FP32 residual); beta = -(z . q_old) / (p . q)_old by the last block
 __global__ void __launch_bounds__(kFcgThreads) k_fcg_prec(int64_t n, int64_t npad, SellMatrix::View S,
-                                                          const float* __restrict__ w, const float2* __restrict__ r2,
+                                                          const uint16_t* __restrict__ w, const float2* __restrict__ r2,
                                                           const float2* __restrict__ q2, float* __restrict__ zf,
                                                           double* __restrict__ part, unsigned* __restrict__ cnt,
                                                           double* __restrict__ fs, int first) {
@@ -891,7 +902,9 @@ int learned_prepare(nalu_ctx* ctx) {
   NALU_CUDA(ctx, srow.alloc(n));
   k_precond_rowscale<<<g, 256, 0, ctx->stream>>>(n, S.ptr.p, S.len.p, S.col.p, L.wsell.p, ctx->sw.dinv.p, srow.p);
   k_precond_apply_scale<<<g, 256, 0, ctx->stream>>>(n, S.ptr.p, S.len.p, S.col.p, L.wsell.p, srow.p);
-  ctx->launches += 3;
+  if (L.wsell16.n < S.stored) NALU_CUDA(ctx, L.wsell16.alloc(S.stored));
+  k_to_bf16<<<(unsigned)((S.stored + 255) / 256), 256, 0, ctx->stream>>>(S.stored, L.wsell.p, L.wsell16.p);
+  ctx->launches += 4;
   NALU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return cuda_check(ctx, cudaGetLastError(), "learned preconditioner values");
 }
@@ -927,7 +940,7 @@ int fcg_learned(nalu_ctx* ctx, double* x, double* r, double rtol, double r0norm,
   NALU_CUDA(ctx, cudaMemsetAsync(fs, 0, sizeof(double) * 8, st));
   k_fcg_split<<<kFcgBlocks, kFcgThreads, 0, st>>>(n, r, r2, x2, q2);
   ctx->launches++;
-  const float* w = ctx->learned.wsell.p;
+  const uint16_t* w = ctx->learned.wsell16.p;
   const unsigned g_pc = wave_grid(ctx, (const void*)k_fcg_prec, kFcgThreads);
   const unsigned g_pu = wave_grid(ctx, (const void*)k_fcg_pupdate, kFcgThreads);
   const unsigned g_sp = wave_grid(ctx, (const void*)k_fcg_spmv, kFcgThreads);
