@@ -102,7 +102,8 @@ struct LearnedState {
   DBuf<int32_t> nbr;                          // [n][27] neighbour LID per topological slot, -1 if none
   DBuf<float> stencil;                        // [n][27] MLP output per slot
   DBuf<float> wsell;                          // preconditioner values on the SELL pattern of A
-  DBuf<uint16_t> wsell16;                     // the same as BF16 (the flexible CG's stencil apply)
+  DBuf<uint16_t> wsell16;                     // the same as BF16 (wide slices of the stencil apply)
+  DBuf<uint32_t> wpack;                       // BF16 value << 16 | 16-bit column offset, per SELL entry
   int64_t nbr_nodes = 0;                      // mesh size the slot map was built for
   bool has_weights = false;
 };

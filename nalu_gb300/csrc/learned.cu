@@ -452,6 +452,43 @@ __global__ void k_to_bf16(int64_t n, const float* __restrict__ w, uint16_t* __re
 
 __device__ __forceinline__ float bf16_f(uint16_t h) { return __uint_as_float((uint32_t)h << 16); }
 
+// one word per SELL entry for the stencil apply: BF16 value (high half) and
+// the 16-bit column offset (low half)
+__global__ void k_pack_prec(int64_t n, const uint16_t* __restrict__ w16, const uint16_t* __restrict__ col16,
+                            uint32_t* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = ((uint32_t)w16[i] << 16) | (uint32_t)col16[i];
+}
+
+// gathers in flight per group in the packed stencil apply
+#ifndef NALU_PREC_GROUP
+#define NALU_PREC_GROUP 16
+#endif
+
+// z_row from the packed words (non-wide slices)
+__device__ __forceinline__ float prec_row_packed(int64_t base, int len, const uint32_t* __restrict__ wp,
+                                                 const int32_t* __restrict__ cbase,
+                                                 const float2* __restrict__ r2) {
+  constexpr int G = NALU_PREC_GROUP;
+  float acc = 0.0f;
+  for (int k = 0; k < len; k += G) {
+    uint32_t v[G];
+    int32_t c[G];
+#pragma unroll
+    for (int u = 0; u < G; ++u) {
+      const bool in = k + u < len;
+      v[u] = in ? __ldg(wp + base + (int64_t)(k + u) * kSlice) : 0u;
+      c[u] = in ? __ldg(cbase + k + u) + (int32_t)(v[u] & 0xffffu) : -1;
+    }
+    float b[G];
+#pragma unroll
+    for (int u = 0; u < G; ++u) b[u] = c[u] >= 0 ? __ldg(r2 + c[u]).x : 0.0f;
+#pragma unroll
+    for (int u = 0; u < G; ++u) acc = fmaf(__uint_as_float(v[u] & 0xffff0000u), b[u], acc);
+  }
+  return acc;
+}
+
 // z_row = sum_k w[base + 32 k] r[col_k] in FP32 (w as BF16), col_k from the 32-bit
 // indices (WIDE) or the 16-bit offsets from the slice's entry bases
 template <bool WIDE>
@@ -479,7 +516,8 @@ __device__ __forceinline__ float prec_row(int64_t base, int len, const SellMatri
 
 // z = M r (FP32 stencil values, FP32 residual); beta = -(z . q_old) / (p . q)_old by the last block
 __global__ void __launch_bounds__(kFcgThreads) k_fcg_prec(int64_t n, int64_t npad, SellMatrix::View S,
-                                                          const uint16_t* __restrict__ w, const float2* __restrict__ r2,
+                                                          const uint16_t* __restrict__ w,
+                                                          const uint32_t* __restrict__ wp, const float2* __restrict__ r2,
                                                           const float2* __restrict__ q2, float* __restrict__ zf,
                                                           double* __restrict__ part, unsigned* __restrict__ cnt,
                                                           double* __restrict__ fs, int first) {
@@ -493,7 +531,7 @@ __global__ void __launch_bounds__(kFcgThreads) k_fcg_prec(int64_t n, int64_t npa
     const int64_t b0 = __ldg(S.ptr + s);
     const int64_t base = b0 + (row % kSlice);
     const float acc = __ldg(S.wide + s) ? prec_row<true>(base, len, S, nullptr, w, r2)
-                                        : prec_row<false>(base, len, S, S.cbase + b0 / kSlice, w, r2);
+                                        : prec_row_packed(base, len, wp, S.cbase + b0 / kSlice, r2);
     zf[row] = acc;
     acc_mul_df(dh, dl, make_float2(acc, 0.0f), q2[row]);
   }
@@ -941,12 +979,17 @@ int fcg_learned(nalu_ctx* ctx, double* x, double* r, double rtol, double r0norm,
   k_fcg_split<<<kFcgBlocks, kFcgThreads, 0, st>>>(n, r, r2, x2, q2);
   ctx->launches++;
   const uint16_t* w = ctx->learned.wsell16.p;
+  LearnedState& L = ctx->learned;
+  if (L.wpack.n < S.stored) NALU_CUDA(ctx, L.wpack.alloc(S.stored));
+  k_pack_prec<<<(unsigned)((S.stored + 255) / 256), 256, 0, st>>>(S.stored, L.wsell16.p, S.col16.p, L.wpack.p);
+  ctx->launches++;
+  const uint32_t* wp = L.wpack.p;
   const unsigned g_pc = wave_grid(ctx, (const void*)k_fcg_prec, kFcgThreads);
   const unsigned g_pu = wave_grid(ctx, (const void*)k_fcg_pupdate, kFcgThreads);
   const unsigned g_sp = wave_grid(ctx, (const void*)k_fcg_spmv, kFcgThreads);
   const unsigned g_ax = wave_grid(ctx, (const void*)k_fcg_axpy, kFcgThreads);
   auto iteration = [&](int first) {
-    k_fcg_prec<<<g_pc, kFcgThreads, 0, st>>>(n, npad, SV, w, r2, q2, zf, part, cnt, fs, first);
+    k_fcg_prec<<<g_pc, kFcgThreads, 0, st>>>(n, npad, SV, w, wp, r2, q2, zf, part, cnt, fs, first);
     k_fcg_pupdate<<<g_pu, kFcgThreads, 0, st>>>(n, zf, p, fs, first);
     k_fcg_spmv<<<g_sp, kFcgThreads, 0, st>>>(n, npad, SV, S.val2.p, p, r2, q2, part, cnt, fs, nonpos.p);
     k_fcg_axpy<<<g_ax, kFcgThreads, 0, st>>>(n, x2, p, r2, q2, part, cnt, fs);
