@@ -462,7 +462,7 @@ __global__ void k_pack_prec(int64_t n, const uint16_t* __restrict__ w16, const u
 
 // gathers in flight per group in the packed stencil apply
 #ifndef NALU_PREC_GROUP
-#define NALU_PREC_GROUP 16
+#define NALU_PREC_GROUP 8  // measured at 128^3: 8 -> 1012 ms, 16 -> 1036, 24 -> 1229
 #endif
 
 // z_row from the packed words (non-wide slices)
