@@ -59,9 +59,11 @@ struct TileArgs {
   const uint8_t* __restrict__ wide;
   const float2* __restrict__ sval;
   const float* __restrict__ dinvf;
-  double* x;
-  double* r;
-  double* q;
+  double* x;    // FP64 solution, accumulated over rounds
+  double* r;    // FP64 residual at the start of a round
+  float2* x2;   // this round's increment, FP32 pairs (folded into x after the round)
+  float2* r2;   // residual, FP32 pairs
+  float2* q2;   // A p, FP32 pairs
   float2* p;
   double* tpart;        // [2][ntiles]
   unsigned* pcnt;       // [P] arrival tickets
@@ -126,18 +128,18 @@ __global__ void __launch_bounds__(kBT) k_bt_prec(TileArgs a) {
     if (__ldg(a.wide + sl)) {
       for (int k = 0; k < len; ++k) {
         const int64_t e = base + (int64_t)k * kSliceB;
-        acc = fmaf(__ldg(a.wsell + e), narrow_f(__ldg(a.r + __ldg(a.scol + e))), acc);
+        acc = fmaf(__ldg(a.wsell + e), __ldg(a.r2 + __ldg(a.scol + e)).x, acc);
       }
     } else {
       const int32_t* cb = a.cbase + b0 / kSliceB;
       for (int k = 0; k < len; ++k) {
         const int64_t e = base + (int64_t)k * kSliceB;
-        acc = fmaf(__ldg(a.wsell + e), narrow_f(__ldg(a.r + __ldg(cb + k) + (int32_t)__ldg(a.col16 + e))), acc);
+        acc = fmaf(__ldg(a.wsell + e), __ldg(a.r2 + __ldg(cb + k) + (int32_t)__ldg(a.col16 + e)).x, acc);
       }
     }
     const double zi = widen_f(acc);
     a.z[row] = zi;
-    dot = zi * a.q[row];
+    dot = zi * join_df(a.q2[row]);
   }
   const double v[1] = {dot};
   double tot[1];
@@ -154,8 +156,7 @@ __global__ void __launch_bounds__(kBT) k_bt_pupdate(TileArgs a) {
   const int64_t row = a.tile_row0[t] + i;
   const float2 beta = split_df(a.beta[pr]);
   const float2 z = a.mode[pr] == 1 ? split_df(a.z[row])
-                                   : fma_df(split_df(a.r[row]), make_float2(a.dinvf[row], 0.0f),
-                                            make_float2(0.0f, 0.0f));
+                                   : fma_df(a.r2[row], make_float2(a.dinvf[row], 0.0f), make_float2(0.0f, 0.0f));
   a.p[row] = fma_df(beta, a.p[row], z);
 }
 
@@ -165,21 +166,21 @@ __global__ void __launch_bounds__(kBT) k_bt_spmv(TileArgs a) {
   const int pr = a.tile_prob[t];
   if (a.done[pr]) return;
   const int i = threadIdx.x;
-  double dot = 0.0, dpr = 0.0;
+  float dh = 0.0f, dl = 0.0f, rh = 0.0f, rl = 0.0f;
   if (i < a.tile_rows[t]) {
     const int64_t row = a.tile_row0[t] + i;
     const int64_t s = row / kSliceB;
     const int64_t b0 = __ldg(a.sptr + s);
     const int len = __ldg(a.slen + s);
-    const double qi = __ldg(a.wide + s) ? sell_row_df(b0 + (row % kSliceB), len, a.scol, a.sval, a.p)
-                                        : join_df(sell_row_df2_c16(b0 + (row % kSliceB), len, a.col16,
-                                                                   a.cbase + b0 / kSliceB, a.sval, a.p));
-    a.q[row] = qi;
-    const double pi = join_df(a.p[row]);
-    dot = pi * qi;
-    dpr = pi * a.r[row];
+    const float2 qi = __ldg(a.wide + s) ? sell_row_df2(b0 + (row % kSliceB), len, a.scol, a.sval, a.p)
+                                        : sell_row_df2_c16(b0 + (row % kSliceB), len, a.col16,
+                                                           a.cbase + b0 / kSliceB, a.sval, a.p);
+    a.q2[row] = qi;
+    const float2 pi = a.p[row];
+    acc_mul_df(dh, dl, pi, qi);
+    acc_mul_df(rh, rl, pi, a.r2[row]);
   }
-  const double v[2] = {dot, dpr};
+  const double v[2] = {join_df(make_float2(dh, dl)), join_df(make_float2(rh, rl))};
   double tot[2];
   if (problem_reduce<2>(a, t, pr, v, tot, sh) && threadIdx.x == 0) {
     if (a.mode[pr] == 1) {  // flexible CG: alpha = (p . r) / (p . A p)
@@ -205,11 +206,10 @@ __global__ void __launch_bounds__(kBT) k_bt_axpy(TileArgs a) {
   float zh = 0.0f, zl = 0.0f, rh = 0.0f, rl = 0.0f;
   if (i < a.tile_rows[t]) {
     const int64_t row = a.tile_row0[t] + i;
-    const double al = a.alpha[pr];
-    a.x[row] += al * join_df(a.p[row]);
-    const double ri = a.r[row] - al * a.q[row];
-    a.r[row] = ri;
-    const float2 rs = split_df(ri);
+    const float2 al = split_df(a.alpha[pr]);
+    a.x2[row] = fma_df(al, a.p[row], a.x2[row]);
+    const float2 rs = fma_df(make_float2(-al.x, -al.y), a.q2[row], a.r2[row]);
+    a.r2[row] = rs;
     acc_sq_df(zh, zl, rs, a.dinvf[row]);
     acc_sq_df(rh, rl, rs, 1.0f);
   }
@@ -241,6 +241,14 @@ __global__ void k_batch_prep(int64_t n, const uint8_t* __restrict__ idmask, cons
   x[i] = xi;
 }
 
+// x += this round's FP32-pair increment; the increment restarts from 0
+__global__ void k_batch_fold(int64_t n, float2* __restrict__ x2, double* __restrict__ x) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  x[i] += join_df(x2[i]);
+  x2[i] = make_float2(0.0f, 0.0f);
+}
+
 // r = b - A x (FP64 CRS), p = 0; per-tile r.D^-1 r, r.r, b.b
 __global__ void __launch_bounds__(kBT) k_batch_resid(TileArgs a, const int64_t* __restrict__ rp,
                                                      const int32_t* __restrict__ ci, const double* __restrict__ v,
@@ -255,8 +263,10 @@ __global__ void __launch_bounds__(kBT) k_batch_resid(TileArgs a, const int64_t* 
     for (int64_t j = rp[row]; j < rp[row + 1]; ++j) s += v[j] * a.x[ci[j]];
     const double ri = b[row] - s;
     a.r[row] = ri;
+    a.r2[row] = split_df(ri);
+    a.x2[row] = make_float2(0.0f, 0.0f);
     a.p[row] = make_float2(0.0f, 0.0f);
-    a.q[row] = 0.0;
+    a.q2[row] = make_float2(0.0f, 0.0f);
     rz += ri * (widen_f(a.dinvf[row]) * ri);
     rr += ri * ri;
     bb += b[row] * b[row];
@@ -395,7 +405,12 @@ int solve_batched(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* inf
   a.dinvf = dinvf.p;
   a.x = ctx->d_x.p;
   a.r = s.r.p;
-  a.q = s.q.p;
+  if (s.x2.n < n) NALU_CUDA(ctx, s.x2.alloc(n));
+  if (s.r2.n < n) NALU_CUDA(ctx, s.r2.alloc(n));
+  if (s.q2.n < n) NALU_CUDA(ctx, s.q2.alloc(n));
+  a.x2 = s.x2.p;
+  a.r2 = s.r2.p;
+  a.q2 = s.q2.p;
   a.p = p2.p;
   a.tpart = tpart;
   a.pcnt = d_cnt.p;
@@ -504,7 +519,10 @@ int solve_batched(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* inf
       NALU_CUDA(ctx, cudaStreamSynchronize(st));
       if (std::all_of(done.begin(), done.end(), [](int d) { return d != 0; })) break;
     }
-    return NALU_OK;
+    // the round's increment into the FP64 solution
+    k_batch_fold<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, a.x2, a.x);
+    ctx->launches++;
+    return cuda_check(ctx, cudaGetLastError(), "batch fold");
   };
 
   if (learned && o.learned_probe) {
