@@ -51,6 +51,11 @@ __device__ __forceinline__ double block_sum(double v, double* sh) {
   return r;
 }
 
+// accumulator of a row: FP32 when matrix and vector are FP32 (the inner
+// solve of the FP32-inner / FP64-refinement scheme), FP64 otherwise
+template <class VT, class XT> struct RowAcc { using type = double; };
+template <> struct RowAcc<float, float> { using type = float; };
+
 // y = A x, TPR threads per row; optional partial of dot(x_own, y)
 template <class VT, class XT, int TPR, bool DOT>
 __global__ void __launch_bounds__(256) k_spmv(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
@@ -61,19 +66,20 @@ __global__ void __launch_bounds__(256) k_spmv(int64_t n, const int64_t* __restri
   const int64_t rows_per_block = blockDim.x / TPR;
   double dot = 0.0;
   // the loop bound is uniform across the warp (all lanes reach the shuffles)
+  using Acc = typename RowAcc<VT, XT>::type;
   for (int64_t base = (int64_t)blockIdx.x * rows_per_block; base < n; base += (int64_t)gridDim.x * rows_per_block) {
     const int64_t row = base + threadIdx.x / TPR;
     const bool valid = row < n;
-    double s = 0.0;
+    Acc s = 0;
     if (valid) {
       const int64_t b = __ldg(rp + row), e = __ldg(rp + row + 1);
-      for (int64_t j = b + sub; j < e; j += TPR) s += (double)__ldg(v + j) * (double)__ldg(x + __ldg(ci + j));
+      for (int64_t j = b + sub; j < e; j += TPR) s += (Acc)__ldg(v + j) * (Acc)__ldg(x + __ldg(ci + j));
     }
 #pragma unroll
     for (int o = TPR / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, TPR);
     if (valid && sub == 0) {
       y[row] = (XT)s;
-      if (DOT) dot += s * (double)x[row];
+      if (DOT) dot += (double)s * (double)x[row];
     }
   }
   if (DOT) {
@@ -113,13 +119,15 @@ __global__ void __launch_bounds__(256) k_residual(int64_t n, const int64_t* __re
 }
 
 // finish a reduction of `nparts` partial arrays into scal[dst..]
+// (one warp per part, lanes over the blocks in a fixed order)
 __global__ void k_finish(const double* __restrict__ partial, int nblocks, int nparts, double* scal, int dst) {
-  __shared__ double sh[32];
-  for (int p = 0; p < nparts; ++p) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int p = wid; p < nparts; p += nw) {
     double s = 0.0;
-    for (int i = threadIdx.x; i < nblocks; i += blockDim.x) s += partial[p * nblocks + i];
-    s = block_sum<double>(s, sh);
-    if (threadIdx.x == 0) scal[dst + p] = s;
+    for (int i = lane; i < nblocks; i += 32) s += partial[p * nblocks + i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) scal[dst + p] = s;
   }
 }
 
@@ -224,33 +232,48 @@ __global__ void k_add_to(int64_t n, double* __restrict__ x, const T* __restrict_
 // ---------------------------------------------------------------------------
 // GMRES helpers: dots of w against k+1 basis vectors, axpys, normalisation
 // ---------------------------------------------------------------------------
+// (eight dots per pass over w; per-thread sums in T, block sums in FP64)
 template <class T>
 __global__ void __launch_bounds__(kRedThreads) k_multi_dot(int64_t n, int k, const T* __restrict__ V, const T* __restrict__ w,
                                                            double* __restrict__ partial) {
   __shared__ double sh[32];
-  for (int j = 0; j < k; ++j) {
-    double s = 0.0;
-    const T* vj = V + (int64_t)j * n;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-      s += (double)vj[i] * (double)w[i];
-    s = block_sum<double>(s, sh);
-    if (threadIdx.x == 0) partial[j * gridDim.x + blockIdx.x] = s;
+  constexpr int C = 8;
+  for (int j0 = 0; j0 < k; j0 += C) {
+    T s[C];
+#pragma unroll
+    for (int u = 0; u < C; ++u) s[u] = 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+      const T wi = w[i];
+#pragma unroll
+      for (int u = 0; u < C; ++u)
+        if (j0 + u < k) s[u] += V[(int64_t)(j0 + u) * n + i] * wi;
+    }
+#pragma unroll
+    for (int u = 0; u < C; ++u) {
+      if (j0 + u >= k) break;  // uniform over the block
+      const double t = block_sum<double>((double)s[u], sh);
+      if (threadIdx.x == 0) partial[(j0 + u) * gridDim.x + blockIdx.x] = t;
+    }
   }
 }
 // w -= sum_j h[j] V_j ; partial of w.w
+// (arithmetic in T, coefficients staged in shared memory; k <= 64)
 template <class T>
 __global__ void __launch_bounds__(kRedThreads) k_multi_axpy(int64_t n, int k, const T* __restrict__ V, T* __restrict__ w,
                                                             const double* __restrict__ h, double* __restrict__ partial) {
   __shared__ double sh[32];
-  double ww = 0.0;
+  __shared__ T hs[64];
+  for (int j = threadIdx.x; j < k; j += blockDim.x) hs[j] = (T)h[j];
+  __syncthreads();
+  T ww = 0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    double s = (double)w[i];
-    for (int j = 0; j < k; ++j) s -= h[j] * (double)V[(int64_t)j * n + i];
-    w[i] = (T)s;
+    T s = w[i];
+    for (int j = 0; j < k; ++j) s -= hs[j] * V[(int64_t)j * n + i];
+    w[i] = s;
     ww += s * s;
   }
-  ww = block_sum<double>(ww, sh);
-  if (threadIdx.x == 0) partial[blockIdx.x] = ww;
+  const double wt = block_sum<double>((double)ww, sh);
+  if (threadIdx.x == 0) partial[blockIdx.x] = wt;
 }
 template <class T>
 __global__ void k_scale_into(int64_t n, const T* __restrict__ w, T* __restrict__ out, const double* __restrict__ s,
@@ -519,9 +542,12 @@ int gmres(nalu_ctx* ctx, const Mat<VT>& A, Work<T>& w, double rtol, int max_it, 
   double* scal = ctx->sw.scal.p;
   double* partial = ctx->sw.partial.p;
   // r (T) holds the initial residual; x (T) accumulates the solution
-  std::vector<double> H((size_t)(m + 1) * m, 0.0), cs(m), sn(m), gv(m + 1), y(m), hcol(m + 2);
+  // dh: pass-1 and pass-2 Gram-Schmidt coefficients side by side, each
+  // [h_0..h_k, .., |w|^2 at m+1], read back together once per iteration
+  const int hs = m + 2;
+  std::vector<double> H((size_t)(m + 1) * m, 0.0), cs(m), sn(m), gv(m + 1), y(m), hcol(2 * hs);
   DBuf<double> dh;
-  NALU_CUDA(ctx, dh.alloc(m + 2));
+  NALU_CUDA(ctx, dh.alloc(2 * hs));
   cudaMemsetAsync(w.x, 0, sizeof(T) * n, ctx->stream);
   int it = 0;
   const double stop = rtol * r0norm;
@@ -554,16 +580,17 @@ int gmres(nalu_ctx* ctx, const Mat<VT>& A, Work<T>& w, double rtol, int max_it, 
       }
       // classical Gram-Schmidt, twice (CGS2)
       for (int pass = 0; pass < 2; ++pass) {
+        double* hp = dh.p + pass * hs;
         k_multi_dot<T><<<g, kRedThreads, 0, ctx->stream>>>(n, k + 1, V, wv, partial);
-        k_finish<<<1, 256, 0, ctx->stream>>>(partial, g, k + 1, dh.p, 0);
-        k_multi_axpy<T><<<g, kRedThreads, 0, ctx->stream>>>(n, k + 1, V, wv, dh.p, partial + (size_t)(m + 1) * g);
-        k_finish<<<1, 256, 0, ctx->stream>>>(partial + (size_t)(m + 1) * g, g, 1, dh.p, m + 1);
+        k_finish<<<1, 256, 0, ctx->stream>>>(partial, g, k + 1, hp, 0);
+        k_multi_axpy<T><<<g, kRedThreads, 0, ctx->stream>>>(n, k + 1, V, wv, hp, partial + (size_t)(m + 1) * g);
+        k_finish<<<1, 256, 0, ctx->stream>>>(partial + (size_t)(m + 1) * g, g, 1, hp, m + 1);
         ctx->launches += 4;
-        cudaMemcpyAsync(hcol.data(), dh.p, sizeof(double) * (m + 2), cudaMemcpyDeviceToHost, ctx->stream);
-        cudaStreamSynchronize(ctx->stream);
-        for (int j = 0; j <= k; ++j) H[(size_t)j * m + k] += hcol[j];
       }
-      const double hn = std::sqrt(hcol[m + 1]);
+      cudaMemcpyAsync(hcol.data(), dh.p, sizeof(double) * 2 * hs, cudaMemcpyDeviceToHost, ctx->stream);
+      cudaStreamSynchronize(ctx->stream);
+      for (int j = 0; j <= k; ++j) H[(size_t)j * m + k] += hcol[j] + hcol[hs + j];
+      const double hn = std::sqrt(hcol[hs + m + 1]);
       H[(size_t)(k + 1) * m + k] = hn;
       double ih = hn > 0 ? 1.0 / hn : 0.0;
       cudaMemcpyAsync(scal + S_TMP, &ih, sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
