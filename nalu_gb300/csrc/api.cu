@@ -197,6 +197,9 @@ int nalu_destroy(nalu_ctx* ctx) {
   s.sell.col.free();
   s.sell.vald.free();
   s.sell.valf.free();
+  s.b3rp.free();
+  s.b3col.free();
+  s.b3val.free();
   if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
   if (ctx->upload_stream) {
     cudaStreamSynchronize(ctx->upload_stream);

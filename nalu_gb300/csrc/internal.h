@@ -122,6 +122,13 @@ struct SolverWork {
   DBuf<float> zf;           // learned-FCG preconditioned residual (FP32 stencil output)
   DBuf<double> cscal;    // CG scalars written by the last block of each kernel
   DBuf<unsigned> ccount; // arrival counter of the single-block reductions
+  // FP32 3x3-block copy of a 3-dof matrix (node rows, node columns, nine
+  // value planes of b3_nblk floats), rebuilt by each mixed-precision solve
+  DBuf<int64_t> b3rp;
+  DBuf<int32_t> b3col;
+  DBuf<float> b3val;
+  DBuf<int> b3flag;
+  int64_t b3_nblk = 0;
   int64_t n = 0;
 };
 

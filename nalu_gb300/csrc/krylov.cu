@@ -18,6 +18,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstdint>
 #include <mutex>
 #include <vector>
@@ -28,6 +29,7 @@ namespace nalu_gb300 {
 
 constexpr int kRedBlocks = 1024;   // fixed grid for deterministic reductions
 constexpr int kRedThreads = 256;
+constexpr int kMaxRestart = 1000;  // Krylov basis size bound of GMRES(m)
 
 template <class T>
 __device__ __forceinline__ T warp_sum(T v) {
@@ -88,6 +90,103 @@ __global__ void __launch_bounds__(256) k_spmv(int64_t n, const int64_t* __restri
   }
 }
 
+// y = A x on the FP32 3x3-block copy: TPB threads per node row, each
+// summing the 3x3 products of its blocks (value k = 3 r + c of block b at
+// bv[k * nblk + b]); 4.4 bytes per nonzero against 8 for FP32 CRS.
+template <class XT, int TPB, bool DOT>
+__global__ void __launch_bounds__(256) k_spmv_b3(int64_t nb, int64_t nblk, const int64_t* __restrict__ brp,
+                                                 const int32_t* __restrict__ bcol, const float* __restrict__ bv,
+                                                 const XT* __restrict__ x, XT* __restrict__ y,
+                                                 double* __restrict__ partial) {
+  __shared__ double sh[32];
+  using Acc = typename RowAcc<float, XT>::type;
+  const int sub = threadIdx.x % TPB;
+  const int64_t nodes_per_block = blockDim.x / TPB;
+  double dot = 0.0;
+  // the loop bound is uniform across the warp (all lanes reach the shuffles)
+  for (int64_t base = (int64_t)blockIdx.x * nodes_per_block; base < nb; base += (int64_t)gridDim.x * nodes_per_block) {
+    const int64_t node = base + threadIdx.x / TPB;
+    const bool valid = node < nb;
+    Acc s0 = 0, s1 = 0, s2 = 0;
+    if (valid) {
+      const int64_t e = __ldg(brp + node + 1);
+      for (int64_t b = __ldg(brp + node) + sub; b < e; b += TPB) {
+        const int64_t c3 = 3 * (int64_t)__ldg(bcol + b);
+        const Acc x0 = (Acc)__ldg(x + c3), x1 = (Acc)__ldg(x + c3 + 1), x2 = (Acc)__ldg(x + c3 + 2);
+        float a[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) a[k] = __ldg(bv + k * nblk + b);
+        s0 += (Acc)a[0] * x0 + (Acc)a[1] * x1 + (Acc)a[2] * x2;
+        s1 += (Acc)a[3] * x0 + (Acc)a[4] * x1 + (Acc)a[5] * x2;
+        s2 += (Acc)a[6] * x0 + (Acc)a[7] * x1 + (Acc)a[8] * x2;
+      }
+    }
+#pragma unroll
+    for (int o = TPB / 2; o > 0; o >>= 1) {
+      s0 += __shfl_xor_sync(0xffffffffu, s0, o, TPB);
+      s1 += __shfl_xor_sync(0xffffffffu, s1, o, TPB);
+      s2 += __shfl_xor_sync(0xffffffffu, s2, o, TPB);
+    }
+    if (valid && sub == 0) {
+      y[3 * node] = (XT)s0;
+      y[3 * node + 1] = (XT)s1;
+      y[3 * node + 2] = (XT)s2;
+      if (DOT) dot += (double)s0 * (double)x[3 * node] + (double)s1 * (double)x[3 * node + 1] +
+                      (double)s2 * (double)x[3 * node + 2];
+    }
+  }
+  if (DOT) {
+    const double t = block_sum<double>(dot, sh);
+    if (threadIdx.x == 0) partial[blockIdx.x] = t;
+  }
+}
+
+// Structure of the 3x3-block copy, one thread per node.  The CRS graph must
+// have the 3-dof Tpetra form: the three rows of a node share one column
+// pattern made of whole column triples (3 c, 3 c + 1, 3 c + 2).  A node
+// that breaks it sets *bad; otherwise brp[node] = rp[3 node] / 9 and the
+// block columns follow the first row's triples.
+__global__ void k_b3_struct(int64_t nb, const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                            int64_t* __restrict__ brp, int32_t* __restrict__ bcol, int* __restrict__ bad) {
+  const int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (node > nb) return;
+  if (node == nb) {
+    const int64_t nnz = rp[3 * nb];
+    if (nnz % 9) atomicOr(bad, 1);
+    brp[nb] = nnz / 9;
+    return;
+  }
+  const int64_t r0 = rp[3 * node], len = rp[3 * node + 1] - r0;
+  bool ok = len % 3 == 0 && r0 % 9 == 0 && rp[3 * node + 2] - rp[3 * node + 1] == len &&
+            rp[3 * node + 3] - rp[3 * node + 2] == len;
+  if (ok) {
+    const int64_t b0 = r0 / 9;
+    brp[node] = b0;
+    for (int64_t e = 0; e < len && ok; e += 3) {
+      const int32_t c = ci[r0 + e];
+      ok = c % 3 == 0 && ci[r0 + e + 1] == c + 1 && ci[r0 + e + 2] == c + 2;
+      for (int r = 1; r < 3 && ok; ++r) {
+        const int64_t rr = rp[3 * node + r] + e;
+        ok = ci[rr] == c && ci[rr + 1] == c + 1 && ci[rr + 2] == c + 2;
+      }
+      bcol[b0 + e / 3] = c / 3;
+    }
+  }
+  if (!ok) atomicOr(bad, 1);
+}
+
+// FP32 block values from the FP64 CRS values, one warp per row (coalesced
+// reads; each lane's entry goes to plane 3 (row % 3) + entry % 3).
+__global__ void k_b3_values(int64_t n, int64_t nblk, const int64_t* __restrict__ rp, const double* __restrict__ v,
+                            float* __restrict__ bv) {
+  const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (row >= n) return;
+  const int64_t r0 = rp[row], len = rp[row + 1] - r0, b0 = rp[row - row % 3] / 9;
+  const int plane0 = 3 * (int)(row % 3);
+  for (int64_t e = lane; e < len; e += 32) bv[(int64_t)(plane0 + (int)(e % 3)) * nblk + b0 + e / 3] = (float)v[r0 + e];
+}
+
 // r = b - A x (FP64), with partial of r.r
 __global__ void __launch_bounds__(256) k_residual(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
                                                   const double* __restrict__ v, const double* __restrict__ x,
@@ -132,15 +231,31 @@ __global__ void k_finish(const double* __restrict__ partial, int nblocks, int np
 }
 
 // scalar slots
-enum { S_RZ = 0, S_PQ = 1, S_RZNEW = 2, S_RR = 3, S_ALPHA = 4, S_BETA = 5, S_BB = 6, S_TMP = 7, S_BAD = 8 };
+enum { S_RZ = 0, S_PQ = 1, S_RZNEW = 2, S_RR = 3, S_ALPHA = 4, S_BETA = 5, S_BB = 6, S_TMP = 7, S_BAD = 8, S_STOP = 9 };
+
+// True once r.r has reached the stop threshold scal[S_STOP] (0: none set).
+// CG iterations run in chunks captured as one graph, so a chunk can overrun
+// convergence; past the threshold alpha = beta = 0 freezes the iterate
+// instead of driving an FP32 recurrence residual to zero (and 0/0).
+__device__ __forceinline__ bool cg_frozen(const double* scal) {
+  return scal[S_STOP] > 0.0 && scal[S_RR] <= scal[S_STOP];
+}
 
 __global__ void k_alpha(double* scal) {
+  if (cg_frozen(scal)) {
+    scal[S_ALPHA] = 0.0;
+    return;
+  }
   const double pq = scal[S_PQ];
   const double a = scal[S_RZ] / pq;
   scal[S_ALPHA] = isfinite(a) ? a : 0.0;
   if (!isfinite(a)) scal[S_BAD] = 1.0;
 }
 __global__ void k_beta(double* scal) {
+  if (cg_frozen(scal)) {
+    scal[S_BETA] = 0.0;
+    return;
+  }
   const double b = scal[S_RZNEW] / scal[S_RZ];
   scal[S_BETA] = isfinite(b) ? b : 0.0;
   if (!isfinite(b)) scal[S_BAD] = 1.0;
@@ -232,55 +347,108 @@ __global__ void k_add_to(int64_t n, double* __restrict__ x, const T* __restrict_
 // ---------------------------------------------------------------------------
 // GMRES helpers: dots of w against k+1 basis vectors, axpys, normalisation
 // ---------------------------------------------------------------------------
-// (eight dots per pass over w; per-thread sums in T, block sums in FP64)
+// Finish of `nparts` per-block partial arrays (part p of block column b at
+// partial[p * gridDim.x + b], stored by thread 0 of the block that owns it)
+// into dst[p]: the block that arrives last (of gridDim.x * gridDim.y) sums
+// every part, one warp per part, in a fixed order, and resets the counter.
+__device__ __forceinline__ void last_block_finish(const double* partial, int nparts, unsigned* counter,
+                                                  double* __restrict__ dst) {
+  __shared__ unsigned ticket;
+  if (counter == nullptr) return;  // the caller finishes with k_finish
+  if (threadIdx.x == 0) {
+    __threadfence();
+    ticket = atomicAdd(counter, 1u);
+  }
+  __syncthreads();
+  if (ticket != gridDim.x * gridDim.y - 1) return;
+  __threadfence();
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int p = wid; p < nparts; p += nw) {
+    double s = 0.0;
+#pragma unroll 8
+    for (int i = lane; i < (int)gridDim.x; i += 32) s += __ldcg(partial + (size_t)p * gridDim.x + i);
+    s = warp_sum(s);
+    if (lane == 0) dst[p] = s;
+  }
+  if (threadIdx.x == 0) *counter = 0u;
+}
+
+// dst[j] = V_j . w for j < k (V column-major, n per column).  Eight dots per
+// block row (blockIdx.y = j / 8, so the column groups run side by side);
+// the column index is clamped so that all eight loads issue unconditionally
+// (the duplicates past k hit the cache and are not summed).  Per-thread sums
+// in T, block and grid sums in FP64.  A 1-D grid loops over the groups.
 template <class T>
-__global__ void __launch_bounds__(kRedThreads) k_multi_dot(int64_t n, int k, const T* __restrict__ V, const T* __restrict__ w,
-                                                           double* __restrict__ partial) {
+__global__ void __launch_bounds__(kRedThreads) k_multi_dot(int64_t n, int k, const T* __restrict__ V,
+                                                           const T* __restrict__ w, double* __restrict__ partial,
+                                                           unsigned* __restrict__ counter, double* __restrict__ dst) {
   __shared__ double sh[32];
   constexpr int C = 8;
-  for (int j0 = 0; j0 < k; j0 += C) {
+  for (int j0 = (int)blockIdx.y * C; j0 < k; j0 += (int)gridDim.y * C) {
+    const T* vp[C];
+#pragma unroll
+    for (int u = 0; u < C; ++u) vp[u] = V + (int64_t)min(j0 + u, k - 1) * n;
     T s[C];
 #pragma unroll
     for (int u = 0; u < C; ++u) s[u] = 0;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
       const T wi = w[i];
+      T a[C];
 #pragma unroll
-      for (int u = 0; u < C; ++u)
-        if (j0 + u < k) s[u] += V[(int64_t)(j0 + u) * n + i] * wi;
+      for (int u = 0; u < C; ++u) a[u] = vp[u][i];
+#pragma unroll
+      for (int u = 0; u < C; ++u) s[u] += a[u] * wi;
     }
 #pragma unroll
     for (int u = 0; u < C; ++u) {
       if (j0 + u >= k) break;  // uniform over the block
       const double t = block_sum<double>((double)s[u], sh);
-      if (threadIdx.x == 0) partial[(j0 + u) * gridDim.x + blockIdx.x] = t;
+      if (threadIdx.x == 0) partial[(size_t)(j0 + u) * gridDim.x + blockIdx.x] = t;
     }
   }
+  last_block_finish(partial, k, counter, dst);
 }
-// w -= sum_j h[j] V_j ; partial of w.w
-// (arithmetic in T, coefficients staged in shared memory; k <= 64)
+
+// w -= sum_j h_j V_j (j < k), then dst[0] = |w|^2.  Arithmetic in T; the
+// coefficients are staged in dynamic shared memory, zero-padded to a
+// multiple of eight so that eight clamped loads issue per step.
 template <class T>
 __global__ void __launch_bounds__(kRedThreads) k_multi_axpy(int64_t n, int k, const T* __restrict__ V, T* __restrict__ w,
-                                                            const double* __restrict__ h, double* __restrict__ partial) {
+                                                            const double* __restrict__ h, double* __restrict__ partial,
+                                                            unsigned* __restrict__ counter, double* __restrict__ dst) {
   __shared__ double sh[32];
-  __shared__ T hs[64];
-  for (int j = threadIdx.x; j < k; j += blockDim.x) hs[j] = (T)h[j];
+  extern __shared__ unsigned char dyn[];
+  T* hs = reinterpret_cast<T*>(dyn);
+  constexpr int C = 8;
+  const int kp = (k + C - 1) / C * C;
+  for (int j = threadIdx.x; j < kp; j += blockDim.x) hs[j] = j < k ? (T)h[j] : (T)0;
   __syncthreads();
   T ww = 0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     T s = w[i];
-    for (int j = 0; j < k; ++j) s -= hs[j] * V[(int64_t)j * n + i];
+    for (int j0 = 0; j0 < k; j0 += C) {
+      T a[C];
+#pragma unroll
+      for (int u = 0; u < C; ++u) a[u] = V[(int64_t)min(j0 + u, k - 1) * n + i];
+#pragma unroll
+      for (int u = 0; u < C; ++u) s -= hs[j0 + u] * a[u];
+    }
     w[i] = s;
     ww += s * s;
   }
   const double wt = block_sum<double>((double)ww, sh);
   if (threadIdx.x == 0) partial[blockIdx.x] = wt;
+  last_block_finish(partial, 1, counter, dst);
 }
+
+template <class T>
+inline size_t multi_axpy_smem(int k) { return sizeof(T) * (size_t)((k + 7) / 8 * 8); }
 template <class T>
 __global__ void k_scale_into(int64_t n, const T* __restrict__ w, T* __restrict__ out, const double* __restrict__ s,
                              int inv_sqrt) {
-  const double f = inv_sqrt ? (s[0] > 0 ? 1.0 / sqrt(s[0]) : 0.0) : s[0];
+  const T f = (T)(inv_sqrt ? (s[0] > 0 ? 1.0 / sqrt(s[0]) : 0.0) : s[0]);
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    out[i] = (T)(f * (double)w[i]);
+    out[i] = f * w[i];
 }
 // z = sum_j y_j V_j (combination), into T
 template <class T>
@@ -307,11 +475,23 @@ struct Mat {
   const int32_t* ci;
   const VT* v;
   int tpr;
+  // optional FP32 3x3-block copy (3-dof systems): used by spmv_launch when set
+  const int64_t* brp = nullptr;
+  const int32_t* bcol = nullptr;
+  const float* bv = nullptr;
+  int64_t nblk = 0;
 };
 
 template <class VT, class XT, bool DOT>
 void spmv_launch(nalu_ctx* ctx, const Mat<VT>& A, const XT* x, XT* y, double* partial) {
   const int threads = 256;
+  if (A.bv) {
+    constexpr int TPB = 8;
+    const int64_t nb = A.n / 3, npb = threads / TPB;
+    k_spmv_b3<XT, TPB, DOT><<<DOT ? kRedBlocks : (unsigned)((nb + npb - 1) / npb), threads, 0, ctx->stream>>>(
+        nb, A.nblk, A.brp, A.bcol, A.bv, x, y, partial);
+    return;
+  }
   if (A.tpr == 16) {
     const int64_t rpb = threads / 16;
     k_spmv<VT, XT, 16, DOT><<<DOT ? kRedBlocks : (unsigned)((A.n + rpb - 1) / rpb), threads, 0, ctx->stream>>>(
@@ -409,7 +589,7 @@ void cg_chunk(nalu_ctx* ctx, const Mat<VT>& A, Work<T>& w, double* scal, double*
     if (!jac) {
       // z = cheb(r); r.z recomputed with the Chebyshev z
       cheb_apply<VT, T>(ctx, A, w.dinv, w.r, w.z, ctmp1, ctmp2, cheb);
-      k_multi_dot<T><<<g, kRedThreads, 0, ctx->stream>>>(n, 1, w.r, w.z, partial);
+      k_multi_dot<T><<<g, kRedThreads, 0, ctx->stream>>>(n, 1, w.r, w.z, partial, nullptr, nullptr);
       k_finish<<<1, 256, 0, ctx->stream>>>(partial, g, 1, scal, S_RZNEW);
       ctx->launches += 2;
     }
@@ -435,7 +615,7 @@ double estimate_lmax(nalu_ctx* ctx, const Mat<VT>& A, const T* dinv, T* a, T* b,
   for (int it = 0; it < 30; ++it) {
     spmv_launch<VT, T, false>(ctx, A, a, b, nullptr);
     k_copy_scale<T><<<g, 256, 0, ctx->stream>>>(n, b, b, nullptr, dinv);
-    k_multi_dot<T><<<g, kRedThreads, 0, ctx->stream>>>(n, 1, b, b, partial);
+    k_multi_dot<T><<<g, kRedThreads, 0, ctx->stream>>>(n, 1, b, b, partial, nullptr, nullptr);
     k_finish<<<1, 256, 0, ctx->stream>>>(partial, g, 1, scal, S_TMP);
     k_scale_into<T><<<g, 256, 0, ctx->stream>>>(n, b, a, scal + S_TMP, 1);
     ctx->launches += 4;
@@ -458,7 +638,8 @@ double read_scalar(nalu_ctx* ctx, double* d) {
 // ||v|| (FP64, fixed-order reduction)
 double vec_norm(nalu_ctx* ctx, const double* v) {
   const int64_t n = ctx->n_rows;
-  k_multi_dot<double><<<grid_for(n, kRedThreads), kRedThreads, 0, ctx->stream>>>(n, 1, v, v, ctx->sw.partial.p);
+  k_multi_dot<double><<<grid_for(n, kRedThreads), kRedThreads, 0, ctx->stream>>>(n, 1, v, v, ctx->sw.partial.p,
+                                                                                  nullptr, nullptr);
   k_finish<<<1, 256, 0, ctx->stream>>>(ctx->sw.partial.p, grid_for(n, kRedThreads), 1, ctx->sw.scal.p, S_TMP);
   ctx->launches += 2;
   return std::sqrt(read_scalar(ctx, ctx->sw.scal.p + S_TMP));
@@ -490,7 +671,7 @@ int pcg(nalu_ctx* ctx, const Mat<VT>& A, Work<T>& w, double rtol, int max_it, in
     ctx->launches++;
   }
   cudaMemcpyAsync(w.p, w.z, sizeof(T) * n, cudaMemcpyDeviceToDevice, ctx->stream);
-  k_multi_dot<T><<<g, kRedThreads, 0, ctx->stream>>>(n, 1, w.r, w.z, partial);
+  k_multi_dot<T><<<g, kRedThreads, 0, ctx->stream>>>(n, 1, w.r, w.z, partial, nullptr, nullptr);
   k_finish<<<1, 256, 0, ctx->stream>>>(partial, g, 1, scal, S_RZ);
   ctx->launches += 2;
   // capture a chunk into a graph
@@ -509,6 +690,9 @@ int pcg(nalu_ctx* ctx, const Mat<VT>& A, Work<T>& w, double rtol, int max_it, in
   int it = 0;
   int rc = NALU_OK;
   const double stop = rtol * r0norm;
+  const double rr0 = r0norm * r0norm, stop2 = stop * stop;
+  cudaMemcpyAsync(scal + S_RR, &rr0, sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
+  cudaMemcpyAsync(scal + S_STOP, &stop2, sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
   while (it < max_it) {
     cudaGraphLaunch(exec, ctx->stream);
     it += chunk;
@@ -539,6 +723,9 @@ int gmres(nalu_ctx* ctx, const Mat<VT>& A, Work<T>& w, double rtol, int max_it, 
           int* iters_out, double r0norm) {
   const int64_t n = A.n;
   const unsigned g = grid_for(n, kRedThreads);
+  // Gram-Schmidt kernels: one resident wave (k_multi_dot holds 16 sums and
+  // 8 column pointers per thread, so fewer blocks fit than kRedBlocks)
+  const unsigned gw = std::min(g, wave_grid(ctx, (const void*)k_multi_dot<T>, kRedThreads));
   double* scal = ctx->sw.scal.p;
   double* partial = ctx->sw.partial.p;
   // r (T) holds the initial residual; x (T) accumulates the solution
@@ -548,6 +735,9 @@ int gmres(nalu_ctx* ctx, const Mat<VT>& A, Work<T>& w, double rtol, int max_it, 
   std::vector<double> H((size_t)(m + 1) * m, 0.0), cs(m), sn(m), gv(m + 1), y(m), hcol(2 * hs);
   DBuf<double> dh;
   NALU_CUDA(ctx, dh.alloc(2 * hs));
+  if (ctx->sw.ccount.n < 1) NALU_CUDA(ctx, ctx->sw.ccount.alloc(1));
+  unsigned* cnt = ctx->sw.ccount.p;
+  NALU_CUDA(ctx, cudaMemsetAsync(cnt, 0, sizeof(unsigned), ctx->stream));
   cudaMemsetAsync(w.x, 0, sizeof(T) * n, ctx->stream);
   int it = 0;
   const double stop = rtol * r0norm;
@@ -581,11 +771,12 @@ int gmres(nalu_ctx* ctx, const Mat<VT>& A, Work<T>& w, double rtol, int max_it, 
       // classical Gram-Schmidt, twice (CGS2)
       for (int pass = 0; pass < 2; ++pass) {
         double* hp = dh.p + pass * hs;
-        k_multi_dot<T><<<g, kRedThreads, 0, ctx->stream>>>(n, k + 1, V, wv, partial);
-        k_finish<<<1, 256, 0, ctx->stream>>>(partial, g, k + 1, hp, 0);
-        k_multi_axpy<T><<<g, kRedThreads, 0, ctx->stream>>>(n, k + 1, V, wv, hp, partial + (size_t)(m + 1) * g);
-        k_finish<<<1, 256, 0, ctx->stream>>>(partial + (size_t)(m + 1) * g, g, 1, hp, m + 1);
-        ctx->launches += 4;
+        // one resident wave in all: the 8-column groups side by side
+        const unsigned gy = (unsigned)(k + 1 + 7) / 8, gx = std::max(1u, gw / gy);
+        k_multi_dot<T><<<dim3(gx, gy), kRedThreads, 0, ctx->stream>>>(n, k + 1, V, wv, partial, cnt, hp);
+        k_multi_axpy<T><<<g, kRedThreads, multi_axpy_smem<T>(k + 1), ctx->stream>>>(
+            n, k + 1, V, wv, hp, partial + (size_t)(m + 1) * gx, cnt, hp + m + 1);
+        ctx->launches += 2;
       }
       cudaMemcpyAsync(hcol.data(), dh.p, sizeof(double) * 2 * hs, cudaMemcpyDeviceToHost, ctx->stream);
       cudaStreamSynchronize(ctx->stream);
@@ -643,7 +834,8 @@ int gmres(nalu_ctx* ctx, const Mat<VT>& A, Work<T>& w, double rtol, int max_it, 
     spmv_launch<VT, T, false>(ctx, A, w.x, w.q, nullptr);
     cudaMemcpyAsync(rcur, w.r, sizeof(T) * n, cudaMemcpyDeviceToDevice, ctx->stream);
     cudaMemcpyAsync(dh.p, &one, sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
-    k_multi_axpy<T><<<g, kRedThreads, 0, ctx->stream>>>(n, 1, w.q, rcur, dh.p, partial);
+    k_multi_axpy<T><<<g, kRedThreads, multi_axpy_smem<T>(1), ctx->stream>>>(n, 1, w.q, rcur, dh.p, partial, nullptr,
+                                                                           nullptr);
     k_finish<<<1, 256, 0, ctx->stream>>>(partial, g, 1, scal, S_TMP);
     ctx->launches += 2;
     beta = std::sqrt(read_scalar(ctx, scal + S_TMP));
@@ -677,13 +869,49 @@ int spmv_fp64(nalu_ctx* ctx, const double* x, double* y) {
 
 namespace {
 
+// FP32 3x3-block copy of the current FP64 matrix for the mixed-precision
+// inner solve of a 3-dof system.  *ok stays false (and nothing is an error)
+// when the graph is not of the 3-dof form or NALU_B3=0.
+int b3_build(nalu_ctx* ctx, bool* ok) {
+  *ok = false;
+  SolverWork& s = ctx->sw;
+  const int64_t n = ctx->n_rows;
+  const char* env = std::getenv("NALU_B3");
+  if (ctx->num_dof != 3 || n % 3 || ctx->nnz % 9 || (env && env[0] == '0')) return NALU_OK;
+  const int64_t nb = n / 3, nblk = ctx->nnz / 9;
+  if (s.b3rp.n < nb + 1) NALU_CUDA(ctx, s.b3rp.alloc(nb + 1));
+  if (s.b3col.n < nblk) NALU_CUDA(ctx, s.b3col.alloc(nblk));
+  if (s.b3val.n < 9 * nblk) NALU_CUDA(ctx, s.b3val.alloc(9 * nblk));
+  if (s.b3flag.n < 1) NALU_CUDA(ctx, s.b3flag.alloc(1));
+  NALU_CUDA(ctx, cudaMemsetAsync(s.b3flag.p, 0, sizeof(int), ctx->stream));
+  k_b3_struct<<<(unsigned)((nb + 1 + 255) / 256), 256, 0, ctx->stream>>>(nb, ctx->d_rowptr.p, ctx->d_colind.p,
+                                                                          s.b3rp.p, s.b3col.p, s.b3flag.p);
+  ctx->launches++;
+  int bad = 0;
+  NALU_CUDA(ctx, cudaMemcpyAsync(&bad, s.b3flag.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  NALU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (bad) return NALU_OK;
+  k_b3_values<<<(unsigned)((n * 32 + 255) / 256), 256, 0, ctx->stream>>>(n, nblk, ctx->d_rowptr.p, ctx->d_values.p,
+                                                                          s.b3val.p);
+  ctx->launches++;
+  s.b3_nblk = nblk;
+  *ok = true;
+  return cuda_check(ctx, cudaGetLastError(), "3x3-block copy");
+}
+
 template <class T>
 int run_inner(nalu_ctx* ctx, const nalu_solver_opts& o, T* r, T* x, T* z, T* p, T* q, T* dinv, T* V, T* ct1, T* ct2,
-              const void* vals, bool fp32vals, double rtol, double r0norm, int max_it, int* iters) {
+              const void* vals, bool fp32vals, double rtol, double r0norm, int max_it, int* iters, bool b3 = false) {
   Work<T> w{r, z, p, q, dinv, x, V};
   const int tpr = ctx->num_dof >= 3 ? 16 : 8;
   if (fp32vals) {
     Mat<float> A{ctx->n_rows, ctx->d_rowptr.p, ctx->d_colind.p, (const float*)vals, tpr};
+    if (b3) {
+      A.brp = ctx->sw.b3rp.p;
+      A.bcol = ctx->sw.b3col.p;
+      A.bv = ctx->sw.b3val.p;
+      A.nblk = ctx->sw.b3_nblk;
+    }
     Cheb<float, T> ch;
     if (o.precond == NALU_PRECOND_CHEBYSHEV) {
       ch.degree = o.cheb_degree > 1 ? o.cheb_degree : 4;
@@ -715,6 +943,8 @@ int solve(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* info) {
   const int64_t n = ctx->n_rows;
   SolverWork& s = ctx->sw;
   const int m = o.restart > 0 ? o.restart : 50;
+  if (o.method == NALU_SOLVER_GMRES && m > kMaxRestart)
+    return set_error(ctx, NALU_ERR_ARG, "GMRES restart (Krylov space size) above 1000");
   int rc = NALU_OK;
   if ((rc = ensure(ctx, s.scal, 16))) return rc;
   if ((rc = ensure(ctx, s.partial, (int64_t)kRedBlocks * (m + 3)))) return rc;
@@ -732,7 +962,7 @@ int solve(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* info) {
   // ||b||
   const double bnorm = [&]() {
     k_multi_dot<double><<<grid_for(n, kRedThreads), kRedThreads, 0, ctx->stream>>>(n, 1, ctx->d_rhs.p, ctx->d_rhs.p,
-                                                                                    s.partial.p);
+                                                                                    s.partial.p, nullptr, nullptr);
     k_finish<<<1, 256, 0, ctx->stream>>>(s.partial.p, grid_for(n, kRedThreads), 1, s.scal.p, S_BB);
     ctx->launches += 2;
     return std::sqrt(read_scalar(ctx, s.scal.p + S_BB));
@@ -747,6 +977,7 @@ int solve(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* info) {
   nalu_solver_opts fb = o;  // Chebyshev-Jacobi PCG after a stall of the learned FCG
   fb.precond = NALU_PRECOND_CHEBYSHEV;
   int total_it = 0, outer = 0;
+  bool b3 = false;  // the mixed-precision inner solve runs on the 3x3-block copy
   double res = true_residual(ctx, ctx->d_x.p, s.tmp.p) / bref;
   const int max_outer = mixed ? 60 : 8;
   while (res > o.tol && outer < max_outer && total_it < o.max_iters) {
@@ -833,7 +1064,9 @@ int solve(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* info) {
       }
       k_add_to<double><<<grid_for(n, 256), 256, 0, ctx->stream>>>(n, ctx->d_x.p, s.w.p);
     } else {
-      if ((rc = ensuref(ctx, s.fvals, ctx->nnz)) || (rc = ensuref(ctx, s.fr, n)) || (rc = ensuref(ctx, s.fz, n)) ||
+      const bool fast_cg = o.method == NALU_SOLVER_CG && o.precond == NALU_PRECOND_JACOBI;
+      if (outer == 1 && !fast_cg && (rc = b3_build(ctx, &b3))) return rc;
+      if ((!b3 && (rc = ensuref(ctx, s.fvals, ctx->nnz))) || (rc = ensuref(ctx, s.fr, n)) || (rc = ensuref(ctx, s.fz, n)) ||
           (rc = ensuref(ctx, s.fp, n)) || (rc = ensuref(ctx, s.fq, n)) || (rc = ensuref(ctx, s.fdinv, n)) ||
           (rc = ensuref(ctx, s.fx, n)) || (rc = ensure(ctx, s.ap, n)))
         return rc;
@@ -842,9 +1075,9 @@ int solve(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* info) {
       NALU_CUDA(ctx, ft1.alloc(n));
       NALU_CUDA(ctx, ft2.alloc(n));
       if (outer == 1) {
-        k_convert<double, float><<<kRedBlocks, 256, 0, ctx->stream>>>(ctx->nnz, ctx->d_values.p, s.fvals.p);
+        if (!b3) k_convert<double, float><<<kRedBlocks, 256, 0, ctx->stream>>>(ctx->nnz, ctx->d_values.p, s.fvals.p);
         k_convert<double, float><<<kRedBlocks, 256, 0, ctx->stream>>>(n, s.dinv.p, s.fdinv.p);
-        ctx->launches += 2;
+        ctx->launches += b3 ? 1 : 2;
       }
       k_convert<double, float><<<kRedBlocks, 256, 0, ctx->stream>>>(n, s.tmp.p, s.fr.p);
       ctx->launches++;
@@ -856,7 +1089,7 @@ int solve(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* info) {
                                     r0, o.max_iters - total_it, o.check_every, &its);
       } else {
         rc = run_inner<float>(ctx, o, s.fr.p, s.fx.p, s.fz.p, s.fp.p, s.fq.p, s.fdinv.p, s.fV.p, ft1.p, ft2.p,
-                              s.fvals.p, true, rtol, r0, o.max_iters - total_it, &its);
+                              s.fvals.p, true, rtol, r0, o.max_iters - total_it, &its, b3);
       }
       k_add_to<float><<<grid_for(n, 256), 256, 0, ctx->stream>>>(n, ctx->d_x.p, s.fx.p);
       cudaStreamSynchronize(ctx->stream);
@@ -977,7 +1210,7 @@ extern "C" int nalu_pcg_jacobi_noalloc(int64_t n, const int64_t* rowptr, const i
   const unsigned g = grid_for(n, kRedThreads);
   k_dinv<double, double><<<g256, 256, 0, s>>>(n, rowptr, colind, values, dinv, mask);
   k_init_x<<<g256, 256, 0, s>>>(n, x, rhs, mask, 1);
-  k_multi_dot<double><<<g, kRedThreads, 0, s>>>(n, 1, rhs, rhs, partial);
+  k_multi_dot<double><<<g, kRedThreads, 0, s>>>(n, 1, rhs, rhs, partial, nullptr, nullptr);
   k_finish<<<1, 256, 0, s>>>(partial, g, 1, scal, S_BB);
   int64_t nnz = 0;
   err = cudaMemcpyAsync(&nnz, rowptr + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
@@ -998,7 +1231,7 @@ extern "C" int nalu_pcg_jacobi_noalloc(int64_t n, const int64_t* rowptr, const i
     const double stop = std::max(tol * bref * 0.5, 1e-15 * r0);
     k_copy_scale<double><<<g256, 256, 0, s>>>(n, r, z, nullptr, dinv);
     cudaMemcpyAsync(p, z, sizeof(double) * n, cudaMemcpyDeviceToDevice, s);
-    k_multi_dot<double><<<g, kRedThreads, 0, s>>>(n, 1, r, z, partial);
+    k_multi_dot<double><<<g, kRedThreads, 0, s>>>(n, 1, r, z, partial, nullptr, nullptr);
     k_finish<<<1, 256, 0, s>>>(partial, g, 1, scal, S_RZ);
     while (total < max_iters) {
       const int chunk = std::min(25, max_iters - total);

@@ -42,6 +42,7 @@ def _true_res(oracle, ctx, x):
     (ng.SOLVER_CG, ng.PRECOND_JACOBI, ng.PRECISION_FP64),
     (ng.SOLVER_CG, ng.PRECOND_CHEBYSHEV, ng.PRECISION_FP64),
     (ng.SOLVER_CG, ng.PRECOND_JACOBI, ng.PRECISION_FP32_INNER_IR),
+    (ng.SOLVER_CG, ng.PRECOND_CHEBYSHEV, ng.PRECISION_FP32_INNER_IR),
     (ng.SOLVER_GMRES, ng.PRECOND_JACOBI, ng.PRECISION_FP64),
     (ng.SOLVER_GMRES, ng.PRECOND_JACOBI, ng.PRECISION_FP32_INNER_IR),
 ])
@@ -80,10 +81,15 @@ def test_continuity_pinned_cg(gpu_ctx_factory, oracle):
     ctx.close()
 
 
-def test_momentum_gmres_mixed(gpu_ctx_factory, oracle):
+def _momentum_system(gpu_ctx_factory, advect=True):
+    """MomentumUpwAdvDiff (alpha_upw 0.5) on a jittered 10^3 mesh with a
+    random-Fourier velocity and a lumped time term on the diagonal, so the
+    3-dof system is non-singular.  Without advection (zero velocity, a
+    near-symmetric diffusion system) the right-hand side, zero from the
+    kernel, gets a seeded random source."""
     c, conn, gid = block_mesh(10, jitter=0.05, seed=4)
     n = c.shape[0]
-    u = ng.meshgen.fourier_velocity(c, n_modes=16, seed=5)
+    u = ng.meshgen.fourier_velocity(c, n_modes=16, seed=5) if advect else np.zeros((n, 3))
     ctx = gpu_ctx_factory()
     ctx.mesh_create(c, conn, gid)
     for nm, val in (("velocity", u), ("velocity_rtm", u), ("density", np.ones(n)), ("viscosity", np.full(n, 1e-3)),
@@ -98,13 +104,44 @@ def test_momentum_gmres_mixed(gpu_ctx_factory, oracle):
     ctx.load_complete()
     v, b = ctx.system()
     diag = np.array([v[rp[i] + np.where(ci[rp[i]:rp[i + 1]] == i)[0][0]] for i in range(rp.size - 1)])
+    src = np.zeros((n, 3)) if advect else np.random.default_rng(6).standard_normal((n, 3))
     for node in range(n):
         for d in range(3):
-            ctx.sum_into_diag(node, d, 0.01 + abs(diag[3 * node + d]), 0.0)
+            ctx.sum_into_diag(node, d, 0.01 + abs(diag[3 * node + d]), src[node, d])
+    return ctx
+
+
+def test_momentum_gmres_mixed(gpu_ctx_factory, oracle):
+    ctx = _momentum_system(gpu_ctx_factory)
     info = ctx.solve(ng.default_solver_opts(method=ng.SOLVER_GMRES, precision=ng.PRECISION_FP32_INNER_IR,
                                             tol=1e-8, restart=50, max_iters=5000))
     res, _ = _true_res(oracle, ctx, ctx.solution())
     assert info.true_rel_res <= 1e-8 and res <= 1.05e-8
+    ctx.close()
+
+
+@pytest.mark.parametrize("method,precond,advect", [
+    (ng.SOLVER_GMRES, ng.PRECOND_JACOBI, True),
+    (ng.SOLVER_CG, ng.PRECOND_CHEBYSHEV, False),
+])
+def test_momentum_mixed_block_copy(gpu_ctx_factory, oracle, monkeypatch, method, precond, advect):
+    """The mixed-precision inner solve of a 3-dof system runs its SpMV on an
+    FP32 3x3-block copy of the matrix (NALU_B3=0: on FP32 CRS instead). Both
+    reach the tolerance, checked with the oracle's FP64 SpMV, and agree to the
+    accuracy that tolerance allows."""
+    ctx = _momentum_system(gpu_ctx_factory, advect)
+    opts = ng.default_solver_opts(method=method, precond=precond, precision=ng.PRECISION_FP32_INNER_IR, tol=1e-10,
+                                  restart=50, max_iters=5000)
+    monkeypatch.delenv("NALU_B3", raising=False)
+    info_b = ctx.solve(opts)
+    x_b = ctx.solution()
+    monkeypatch.setenv("NALU_B3", "0")
+    info_c = ctx.solve(opts)
+    x_c = ctx.solution()
+    for info, x in ((info_b, x_b), (info_c, x_c)):
+        res, _ = _true_res(oracle, ctx, x)
+        assert info.status == 0 and info.true_rel_res <= 1e-10 and res <= 1.05e-10
+    assert np.max(np.abs(x_b - x_c)) <= 1e-7 * np.max(np.abs(x_c))
     ctx.close()
 
 
