@@ -730,14 +730,31 @@ int gmres(nalu_ctx* ctx, const Mat<VT>& A, Work<T>& w, double rtol, int max_it, 
   double* partial = ctx->sw.partial.p;
   // r (T) holds the initial residual; x (T) accumulates the solution
   // dh: pass-1 and pass-2 Gram-Schmidt coefficients side by side, each
-  // [h_0..h_k, .., |w|^2 at m+1], read back together once per iteration
+  // [h_0..h_k, .., |w|^2 at m+1]; both come back to the host together, once
+  // per column, into one of two pinned slots, while the device already
+  // works on the next column (the host's Givens step overlaps it)
   const int hs = m + 2;
-  std::vector<double> H((size_t)(m + 1) * m, 0.0), cs(m), sn(m), gv(m + 1), y(m), hcol(2 * hs);
+  std::vector<double> H((size_t)(m + 1) * m, 0.0), cs(m), sn(m), gv(m + 1), y(m);
   DBuf<double> dh;
   NALU_CUDA(ctx, dh.alloc(2 * hs));
   if (ctx->sw.ccount.n < 1) NALU_CUDA(ctx, ctx->sw.ccount.alloc(1));
   unsigned* cnt = ctx->sw.ccount.p;
   NALU_CUDA(ctx, cudaMemsetAsync(cnt, 0, sizeof(unsigned), ctx->stream));
+  double* hpin = nullptr;
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  cudaError_t he = cudaMallocHost(&hpin, sizeof(double) * 4 * hs);
+  if (he == cudaSuccess) he = cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming);
+  if (he == cudaSuccess) he = cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming);
+  auto release = [&]() {
+    for (cudaEvent_t e : ev)
+      if (e) cudaEventDestroy(e);
+    if (hpin) cudaFreeHost(hpin);
+    dh.free();
+  };
+  if (he != cudaSuccess) {
+    release();
+    return cuda_check(ctx, he, "GMRES host buffers");
+  }
   cudaMemsetAsync(w.x, 0, sizeof(T) * n, ctx->stream);
   int it = 0;
   const double stop = rtol * r0norm;
@@ -746,8 +763,65 @@ int gmres(nalu_ctx* ctx, const Mat<VT>& A, Work<T>& w, double rtol, int max_it, 
   cudaMemcpyAsync(rcur, w.r, sizeof(T) * n, cudaMemcpyDeviceToDevice, ctx->stream);
   double beta = r0norm;
   int rc = NALU_OK;
+  T* V = w.V;
+  // column k: w = A M^-1 v_k, CGS2 against v_0..v_k, v_k+1 = w / |w| (the
+  // norm read on the device), coefficients to pinned slot k % 2 + event
+  auto enqueue_column = [&](int k) {
+    T* vk = V + (int64_t)k * n;
+    T* wv = V + (int64_t)(k + 1) * n;
+    if (precond == NALU_PRECOND_JACOBI) {
+      k_copy_scale<T><<<g, 256, 0, ctx->stream>>>(n, vk, w.q, nullptr, w.dinv);
+      spmv_launch<VT, T, false>(ctx, A, w.q, wv, nullptr);
+      ctx->launches++;
+    } else {
+      spmv_launch<VT, T, false>(ctx, A, vk, wv, nullptr);
+    }
+    // classical Gram-Schmidt, twice (CGS2)
+    for (int pass = 0; pass < 2; ++pass) {
+      double* hp = dh.p + pass * hs;
+      // one resident wave in all: the 8-column groups side by side
+      const unsigned gy = (unsigned)(k + 1 + 7) / 8, gx = std::max(1u, gw / gy);
+      k_multi_dot<T><<<dim3(gx, gy), kRedThreads, 0, ctx->stream>>>(n, k + 1, V, wv, partial, cnt, hp);
+      k_multi_axpy<T><<<g, kRedThreads, multi_axpy_smem<T>(k + 1), ctx->stream>>>(
+          n, k + 1, V, wv, hp, partial + (size_t)(m + 1) * gx, cnt, hp + m + 1);
+      ctx->launches += 2;
+    }
+    k_scale_into<T><<<g, 256, 0, ctx->stream>>>(n, wv, wv, dh.p + hs + m + 1, 1);
+    cudaMemcpyAsync(hpin + (k & 1) * 2 * hs, dh.p, sizeof(double) * 2 * hs, cudaMemcpyDeviceToHost, ctx->stream);
+    cudaEventRecord(ev[k & 1], ctx->stream);
+    ctx->launches++;
+  };
+  // Givens step for column k once its coefficients are in; true when the
+  // cycle ends with it (converged, or a non-finite rotation)
+  auto process_column = [&](int k) -> bool {
+    const cudaError_t e = cudaEventSynchronize(ev[k & 1]);
+    if (e != cudaSuccess) {
+      rc = cuda_check(ctx, e, "GMRES column");
+      return true;
+    }
+    const double* hc = hpin + (k & 1) * 2 * hs;
+    for (int j = 0; j <= k; ++j) H[(size_t)j * m + k] = hc[j] + hc[hs + j];
+    H[(size_t)(k + 1) * m + k] = std::sqrt(hc[hs + m + 1]);
+    for (int j = 0; j < k; ++j) {
+      const double t = cs[j] * H[(size_t)j * m + k] + sn[j] * H[(size_t)(j + 1) * m + k];
+      H[(size_t)(j + 1) * m + k] = -sn[j] * H[(size_t)j * m + k] + cs[j] * H[(size_t)(j + 1) * m + k];
+      H[(size_t)j * m + k] = t;
+    }
+    const double a = H[(size_t)k * m + k], b = H[(size_t)(k + 1) * m + k];
+    const double den = std::sqrt(a * a + b * b);
+    cs[k] = den > 0 ? a / den : 1.0;
+    sn[k] = den > 0 ? b / den : 0.0;
+    H[(size_t)k * m + k] = den;
+    H[(size_t)(k + 1) * m + k] = 0.0;
+    gv[k + 1] = -sn[k] * gv[k];
+    gv[k] = cs[k] * gv[k];
+    if (!std::isfinite(gv[k + 1])) {
+      rc = set_error(ctx, NALU_ERR_NONFINITE, "GMRES breakdown");
+      return true;
+    }
+    return std::fabs(gv[k + 1]) <= stop;
+  };
   while (it < max_it) {
-    T* V = w.V;
     // V_0 = r / beta
     const double inv = 1.0 / beta;
     cudaMemcpyAsync(scal + S_TMP, &inv, sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
@@ -755,64 +829,18 @@ int gmres(nalu_ctx* ctx, const Mat<VT>& A, Work<T>& w, double rtol, int max_it, 
     ctx->launches++;
     std::fill(gv.begin(), gv.end(), 0.0);
     gv[0] = beta;
-    int k = 0;
+    int k = 0;  // columns processed in this cycle
     bool done = false;
-    for (; k < m && it < max_it; ++k, ++it) {
-      T* vk = V + (int64_t)k * n;
-      T* wv = V + (int64_t)(k + 1) * n;
-      // wv = A M^-1 vk
-      if (precond == NALU_PRECOND_JACOBI) {
-        k_copy_scale<T><<<g, 256, 0, ctx->stream>>>(n, vk, w.q, nullptr, w.dinv);
-        spmv_launch<VT, T, false>(ctx, A, w.q, wv, nullptr);
-        ctx->launches++;
-      } else {
-        spmv_launch<VT, T, false>(ctx, A, vk, wv, nullptr);
-      }
-      // classical Gram-Schmidt, twice (CGS2)
-      for (int pass = 0; pass < 2; ++pass) {
-        double* hp = dh.p + pass * hs;
-        // one resident wave in all: the 8-column groups side by side
-        const unsigned gy = (unsigned)(k + 1 + 7) / 8, gx = std::max(1u, gw / gy);
-        k_multi_dot<T><<<dim3(gx, gy), kRedThreads, 0, ctx->stream>>>(n, k + 1, V, wv, partial, cnt, hp);
-        k_multi_axpy<T><<<g, kRedThreads, multi_axpy_smem<T>(k + 1), ctx->stream>>>(
-            n, k + 1, V, wv, hp, partial + (size_t)(m + 1) * gx, cnt, hp + m + 1);
-        ctx->launches += 2;
-      }
-      cudaMemcpyAsync(hcol.data(), dh.p, sizeof(double) * 2 * hs, cudaMemcpyDeviceToHost, ctx->stream);
-      cudaStreamSynchronize(ctx->stream);
-      for (int j = 0; j <= k; ++j) H[(size_t)j * m + k] += hcol[j] + hcol[hs + j];
-      const double hn = std::sqrt(hcol[hs + m + 1]);
-      H[(size_t)(k + 1) * m + k] = hn;
-      double ih = hn > 0 ? 1.0 / hn : 0.0;
-      cudaMemcpyAsync(scal + S_TMP, &ih, sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
-      k_scale_into<T><<<g, 256, 0, ctx->stream>>>(n, wv, wv, scal + S_TMP, 0);
-      ctx->launches++;
-      for (int j = 0; j < k; ++j) {
-        const double t = cs[j] * H[(size_t)j * m + k] + sn[j] * H[(size_t)(j + 1) * m + k];
-        H[(size_t)(j + 1) * m + k] = -sn[j] * H[(size_t)j * m + k] + cs[j] * H[(size_t)(j + 1) * m + k];
-        H[(size_t)j * m + k] = t;
-      }
-      const double a = H[(size_t)k * m + k], b = H[(size_t)(k + 1) * m + k];
-      const double den = std::sqrt(a * a + b * b);
-      cs[k] = den > 0 ? a / den : 1.0;
-      sn[k] = den > 0 ? b / den : 0.0;
-      H[(size_t)k * m + k] = den;
-      H[(size_t)(k + 1) * m + k] = 0.0;
-      gv[k + 1] = -sn[k] * gv[k];
-      gv[k] = cs[k] * gv[k];
-      if (!std::isfinite(gv[k + 1])) {
-        rc = set_error(ctx, NALU_ERR_NONFINITE, "GMRES breakdown");
-        done = true;
-        ++k;
-        ++it;
-        break;
-      }
-      if (std::fabs(gv[k + 1]) <= stop) {
-        done = true;
-        ++k;
-        ++it;
-        break;
-      }
+    enqueue_column(0);
+    int next = 1;  // next column to enqueue
+    while (true) {
+      // one column ahead (discarded if column k ends the cycle)
+      if (next < m && it + (next - k) < max_it) enqueue_column(next++);
+      done = process_column(k);
+      ++k;
+      ++it;
+      if (done || k >= m || it >= max_it) break;
+      if (next == k) enqueue_column(next++);
     }
     for (int j = k - 1; j >= 0; --j) {
       double s = gv[j];
@@ -841,7 +869,8 @@ int gmres(nalu_ctx* ctx, const Mat<VT>& A, Work<T>& w, double rtol, int max_it, 
     beta = std::sqrt(read_scalar(ctx, scal + S_TMP));
     if (beta <= stop) break;
   }
-  dh.free();
+  cudaStreamSynchronize(ctx->stream);
+  release();
   *iters_out = it;
   if (rc == NALU_OK && it >= max_it) rc = NALU_ERR_NOT_CONVERGED;
   return rc;
