@@ -129,9 +129,11 @@ int nalu_linsys_copy(nalu_ctx* ctx, double* values, double* rhs, int dst_is_devi
  * on a second stream, so the transfer overlaps whatever is queued next
  * (field uploads, zeroSystem, assembly).  values / rhs are host buffers,
  * pinned (nalu_host_alloc) for the transfer to be asynchronous; they hold the
- * result after nalu_linsys_copy_wait or nalu_synchronize.  A second call
- * waits on the device for the first download before reusing the snapshot.
- * No reference counterpart (Tpetra's matrix lives on the host). */
+ * result after nalu_linsys_copy_wait or nalu_synchronize.  Two snapshots
+ * are used in turn: a call waits on the device only for the download two
+ * calls back, so consecutive downloads run back to back.  Downloads complete
+ * in call order; calls that share host buffers leave the last call's result
+ * there.  No reference counterpart (Tpetra's matrix lives on the host). */
 int nalu_linsys_copy_async(nalu_ctx* ctx, double* values, double* rhs);
 int nalu_linsys_copy_wait(nalu_ctx* ctx);
 

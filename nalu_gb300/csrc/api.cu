@@ -208,7 +208,8 @@ int nalu_destroy(nalu_ctx* ctx) {
     cudaStreamDestroy(ctx->upload_stream);
   }
   if (ctx->ev_snap) cudaEventDestroy(ctx->ev_snap);
-  if (ctx->ev_copied) cudaEventDestroy(ctx->ev_copied);
+  for (cudaEvent_t e : ctx->ev_copied)
+    if (e) cudaEventDestroy(e);
   if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
@@ -230,7 +231,7 @@ int nalu_synchronize(nalu_ctx* ctx) {
   NALU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   if (ctx->copy_stream) NALU_CUDA(ctx, cudaStreamSynchronize(ctx->copy_stream));
   if (ctx->upload_stream) NALU_CUDA(ctx, cudaStreamSynchronize(ctx->upload_stream));
-  ctx->copy_pending = false;
+  ctx->copy_pending[0] = ctx->copy_pending[1] = false;
   return NALU_OK;
 }
 
@@ -695,37 +696,42 @@ int nalu_linsys_copy_async(nalu_ctx* ctx, double* values, double* rhs) {
   if (!ctx->copy_stream) {
     NALU_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
     NALU_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_snap, cudaEventDisableTiming));
-    NALU_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_copied, cudaEventDisableTiming));
+    NALU_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_copied[0], cudaEventDisableTiming));
+    NALU_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_copied[1], cudaEventDisableTiming));
   }
-  if (ctx->stage_values.n < ctx->nnz) NALU_CUDA(ctx, ctx->stage_values.alloc(ctx->nnz));
-  if (ctx->stage_rhs.n < ctx->n_rows) NALU_CUDA(ctx, ctx->stage_rhs.alloc(ctx->n_rows));
-  // the staging copy may be overwritten only after the previous download ended
-  if (ctx->copy_pending) NALU_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->ev_copied, 0));
+  const int k = ctx->copy_slot;
+  nalu_gb300::DBuf<double>& sv = ctx->stage_values[k];
+  nalu_gb300::DBuf<double>& sr = ctx->stage_rhs[k];
+  if (sv.n < ctx->nnz) NALU_CUDA(ctx, sv.alloc(ctx->nnz));
+  if (sr.n < ctx->n_rows) NALU_CUDA(ctx, sr.alloc(ctx->n_rows));
+  // this staging copy may be overwritten only after its previous download ended
+  if (ctx->copy_pending[k]) NALU_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->ev_copied[k], 0));
   if (values)
-    NALU_CUDA(ctx, cudaMemcpyAsync(ctx->stage_values.p, ctx->d_values.p, sizeof(double) * ctx->nnz,
-                                   cudaMemcpyDeviceToDevice, ctx->stream));
+    NALU_CUDA(ctx, cudaMemcpyAsync(sv.p, ctx->d_values.p, sizeof(double) * ctx->nnz, cudaMemcpyDeviceToDevice,
+                                   ctx->stream));
   if (rhs)
-    NALU_CUDA(ctx, cudaMemcpyAsync(ctx->stage_rhs.p, ctx->d_rhs.p, sizeof(double) * ctx->n_rows,
-                                   cudaMemcpyDeviceToDevice, ctx->stream));
+    NALU_CUDA(ctx, cudaMemcpyAsync(sr.p, ctx->d_rhs.p, sizeof(double) * ctx->n_rows, cudaMemcpyDeviceToDevice,
+                                   ctx->stream));
   NALU_CUDA(ctx, cudaEventRecord(ctx->ev_snap, ctx->stream));
   NALU_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_snap, 0));
   if (values)
-    NALU_CUDA(ctx, cudaMemcpyAsync(values, ctx->stage_values.p, sizeof(double) * ctx->nnz, cudaMemcpyDeviceToHost,
-                                   ctx->copy_stream));
+    NALU_CUDA(ctx, cudaMemcpyAsync(values, sv.p, sizeof(double) * ctx->nnz, cudaMemcpyDeviceToHost, ctx->copy_stream));
   if (rhs)
-    NALU_CUDA(ctx, cudaMemcpyAsync(rhs, ctx->stage_rhs.p, sizeof(double) * ctx->n_rows, cudaMemcpyDeviceToHost,
-                                   ctx->copy_stream));
-  NALU_CUDA(ctx, cudaEventRecord(ctx->ev_copied, ctx->copy_stream));
-  ctx->copy_pending = true;
+    NALU_CUDA(ctx, cudaMemcpyAsync(rhs, sr.p, sizeof(double) * ctx->n_rows, cudaMemcpyDeviceToHost, ctx->copy_stream));
+  NALU_CUDA(ctx, cudaEventRecord(ctx->ev_copied[k], ctx->copy_stream));
+  ctx->copy_pending[k] = true;
+  ctx->copy_slot = k ^ 1;
   return NALU_OK;
 }
 
 int nalu_linsys_copy_wait(nalu_ctx* ctx) {
   if (!ctx) return NALU_ERR_ARG;
-  if (!ctx->copy_pending) return NALU_OK;
   cudaSetDevice(ctx->device);
-  NALU_CUDA(ctx, cudaEventSynchronize(ctx->ev_copied));
-  ctx->copy_pending = false;
+  for (int k = 0; k < 2; ++k) {
+    if (!ctx->copy_pending[k]) continue;
+    NALU_CUDA(ctx, cudaEventSynchronize(ctx->ev_copied[k]));
+    ctx->copy_pending[k] = false;
+  }
   return NALU_OK;
 }
 

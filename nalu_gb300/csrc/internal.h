@@ -185,12 +185,15 @@ struct nalu_ctx {
   // errors raised by kernels (negative Jacobian count, graph misses, ...)
   nalu_gb300::DBuf<int32_t> d_flags;     // [4]
 
-  // asynchronous result download (nalu_linsys_copy_async): staging copy of
-  // values/rhs, a second stream for the device-to-host transfer, events
+  // asynchronous result download (nalu_linsys_copy_async): two staging
+  // copies of values/rhs used in turn (a snapshot waits only for the
+  // download two calls back, so downloads run back to back), a second
+  // stream for the device-to-host transfers, events
   cudaStream_t copy_stream = nullptr;
-  cudaEvent_t ev_snap = nullptr, ev_copied = nullptr;
-  bool copy_pending = false;
-  nalu_gb300::DBuf<double> stage_values, stage_rhs;
+  cudaEvent_t ev_snap = nullptr, ev_copied[2] = {nullptr, nullptr};
+  bool copy_pending[2] = {false, false};
+  int copy_slot = 0;
+  nalu_gb300::DBuf<double> stage_values[2], stage_rhs[2];
 
   // timing
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;

@@ -141,19 +141,23 @@ __global__ void __launch_bounds__(256) k_spmv_b3(int64_t nb, int64_t nblk, const
   }
 }
 
-// Structure of the 3x3-block copy, one thread per node.  The CRS graph must
-// have the 3-dof Tpetra form: the three rows of a node share one column
-// pattern made of whole column triples (3 c, 3 c + 1, 3 c + 2).  A node
-// that breaks it sets *bad; otherwise brp[node] = rp[3 node] / 9 and the
-// block columns follow the first row's triples.
+// Structure of the 3x3-block copy, one warp per node (lanes over the
+// node's column triples).  The CRS graph must have the 3-dof Tpetra form:
+// the three rows of a node share one column pattern made of whole column
+// triples (3 c, 3 c + 1, 3 c + 2).  A node that breaks it sets *bad;
+// otherwise brp[node] = rp[3 node] / 9 and the block columns follow the
+// first row's triples.
 __global__ void k_b3_struct(int64_t nb, const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
                             int64_t* __restrict__ brp, int32_t* __restrict__ bcol, int* __restrict__ bad) {
-  const int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t node = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
   if (node > nb) return;
   if (node == nb) {
-    const int64_t nnz = rp[3 * nb];
-    if (nnz % 9) atomicOr(bad, 1);
-    brp[nb] = nnz / 9;
+    if (lane == 0) {
+      const int64_t nnz = rp[3 * nb];
+      if (nnz % 9) atomicOr(bad, 1);
+      brp[nb] = nnz / 9;
+    }
     return;
   }
   const int64_t r0 = rp[3 * node], len = rp[3 * node + 1] - r0;
@@ -161,15 +165,17 @@ __global__ void k_b3_struct(int64_t nb, const int64_t* __restrict__ rp, const in
             rp[3 * node + 3] - rp[3 * node + 2] == len;
   if (ok) {
     const int64_t b0 = r0 / 9;
-    brp[node] = b0;
-    for (int64_t e = 0; e < len && ok; e += 3) {
+    if (lane == 0) brp[node] = b0;
+    for (int64_t t = lane; t < len / 3; t += 32) {
+      const int64_t e = 3 * t;
       const int32_t c = ci[r0 + e];
-      ok = c % 3 == 0 && ci[r0 + e + 1] == c + 1 && ci[r0 + e + 2] == c + 2;
-      for (int r = 1; r < 3 && ok; ++r) {
+      bool tok = c % 3 == 0 && ci[r0 + e + 1] == c + 1 && ci[r0 + e + 2] == c + 2;
+      for (int r = 1; r < 3; ++r) {
         const int64_t rr = rp[3 * node + r] + e;
-        ok = ci[rr] == c && ci[rr + 1] == c + 1 && ci[rr + 2] == c + 2;
+        tok = tok && ci[rr] == c && ci[rr + 1] == c + 1 && ci[rr + 2] == c + 2;
       }
-      bcol[b0 + e / 3] = c / 3;
+      bcol[b0 + t] = c / 3;
+      ok = ok && tok;
     }
   }
   if (!ok) atomicOr(bad, 1);
@@ -913,8 +919,8 @@ int b3_build(nalu_ctx* ctx, bool* ok) {
   if (s.b3val.n < 9 * nblk) NALU_CUDA(ctx, s.b3val.alloc(9 * nblk));
   if (s.b3flag.n < 1) NALU_CUDA(ctx, s.b3flag.alloc(1));
   NALU_CUDA(ctx, cudaMemsetAsync(s.b3flag.p, 0, sizeof(int), ctx->stream));
-  k_b3_struct<<<(unsigned)((nb + 1 + 255) / 256), 256, 0, ctx->stream>>>(nb, ctx->d_rowptr.p, ctx->d_colind.p,
-                                                                          s.b3rp.p, s.b3col.p, s.b3flag.p);
+  k_b3_struct<<<(unsigned)(((nb + 1) * 32 + 255) / 256), 256, 0, ctx->stream>>>(nb, ctx->d_rowptr.p, ctx->d_colind.p,
+                                                                                 s.b3rp.p, s.b3col.p, s.b3flag.p);
   ctx->launches++;
   int bad = 0;
   NALU_CUDA(ctx, cudaMemcpyAsync(&bad, s.b3flag.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));

@@ -366,8 +366,9 @@ def test_df64_golds_capture(gpu_ctx_factory, golds):
 
 def test_async_download_matches_blocking_copy(gpu_ctx_factory):
     """nalu_linsys_copy_async: the pinned host copy equals the blocking copy,
-    also for two downloads in a row with a different assembly in between
-    (the second snapshot waits for the first transfer)."""
+    also for three downloads in a row with a different assembly in between
+    (two snapshots in turn: the third reuses the first's once its transfer
+    has ended)."""
     c, conn, gid = block_mesh(20, jitter=0.1, seed=31)
     n = c.shape[0]
     u, rho, p, gp = continuity_fields(c, seed=32)
@@ -377,7 +378,7 @@ def test_async_download_matches_blocking_copy(gpu_ctx_factory):
         ctx.field_set(nm, val)
     ctx.build_elem_graph(1)
     nr, nnz, _ = ctx.sizes()
-    outs = [(ng.PinnedArray((nnz,)), ng.PinnedArray((nr,))) for _ in range(2)]
+    outs = [(ng.PinnedArray((nnz,)), ng.PinnedArray((nr,))) for _ in range(3)]
     refs = []
     for k, (ov, orr) in enumerate(outs):
         ctx.field_set("density", rho * (1.0 + k))
@@ -390,6 +391,7 @@ def test_async_download_matches_blocking_copy(gpu_ctx_factory):
         np.testing.assert_array_equal(ov.array, rv)
         np.testing.assert_array_equal(orr.array, rr)
     assert not np.array_equal(outs[0][1].array, outs[1][1].array)
+    assert not np.array_equal(outs[0][1].array, outs[2][1].array)
     for ov, orr in outs:
         ov.free()
         orr.free()
