@@ -119,16 +119,16 @@ __global__ void __launch_bounds__(kCgThreads) k_cg_init(int64_t n, const T* __re
                                                         T* __restrict__ z, double* __restrict__ rz_part,
                                                         double* __restrict__ rr_part) {
   __shared__ double sh[33];
-  double rz = 0.0, rr = 0.0;
+  T rz = 0, rr = 0;  // arithmetic in T (FP32 for the FP32-inner solve), block sums in FP64
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const double ri = (double)r[i];
-    const double zi = (double)dinv[i] * ri;
-    z[i] = (T)zi;
+    const T ri = r[i];
+    const T zi = dinv[i] * ri;
+    z[i] = zi;
     rz += ri * zi;
     rr += ri * ri;
   }
-  block_store(rz, rz_part + blockIdx.x, sh);
-  block_store(rr, rr_part + blockIdx.x, sh);
+  block_store((double)rz, rz_part + blockIdx.x, sh);
+  block_store((double)rr, rr_part + blockIdx.x, sh);
 }
 
 // p = z + beta p with beta = rz_cur / rz_prev (beta = 0 on the first iteration)
@@ -143,18 +143,22 @@ __global__ void __launch_bounds__(kCgThreads) k_cg_pupdate(int64_t n, const T* _
     const double b = block_total(rz_prev, kCgBlocks, sh);
     beta = a / b;
   }
+  const T b = (T)beta;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    p[i] = first ? z[i] : (T)((double)z[i] + beta * (double)p[i]);
+    p[i] = first ? z[i] : z[i] + b * p[i];
 }
 
-// q = A p on the SELL-32 copy (one multiply-add per stored entry); partials of p.q
+// q = A p on the SELL-32 copy (one multiply-add per stored entry, in stored
+// order); partials of p.q.  Column and value loads go out in predicated
+// groups of eight ahead of their gathers (past the row's length: column of
+// the group's first entry, value 0).
 template <class T, class VT>
 __global__ void __launch_bounds__(kCgThreads) k_cg_spmv(int64_t n, int64_t nrows_padded, const int64_t* __restrict__ sptr,
                                                         const int32_t* __restrict__ slen, const int32_t* __restrict__ scol,
                                                         const VT* __restrict__ sval, const T* __restrict__ p,
                                                         T* __restrict__ q, double* __restrict__ pq_part) {
   __shared__ double sh[33];
-  double dot = 0.0;
+  T dot = 0;
   for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < nrows_padded;
        row += (int64_t)gridDim.x * blockDim.x) {
     if (row >= n) continue;
@@ -162,14 +166,23 @@ __global__ void __launch_bounds__(kCgThreads) k_cg_spmv(int64_t n, int64_t nrows
     const int len = __ldg(slen + s);
     const int64_t base = __ldg(sptr + s) + (row % kSlice);
     T acc = 0;
-    for (int k = 0; k < len; ++k) {
-      const int32_t c = __ldg(scol + base + (int64_t)k * kSlice);
-      acc += (T)__ldg(sval + base + (int64_t)k * kSlice) * __ldg(p + c);
+    for (int k = 0; k < len; k += 8) {
+      int32_t c[8];
+      VT v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const bool in = k + u < len;
+        const int64_t off = base + (int64_t)(in ? k + u : k) * kSlice;
+        c[u] = __ldg(scol + off);
+        v[u] = in ? __ldg(sval + off) : (VT)0;
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) acc += (T)v[u] * __ldg(p + c[u]);
     }
     q[row] = acc;
-    dot += (double)p[row] * (double)acc;
+    dot += p[row] * acc;
   }
-  block_store(dot, pq_part + blockIdx.x, sh);
+  block_store((double)dot, pq_part + blockIdx.x, sh);
 }
 
 template <class T>
@@ -182,19 +195,19 @@ __global__ void __launch_bounds__(kCgThreads) k_cg_axpy(int64_t n, T* __restrict
   __shared__ double sh[33];
   const double rz = block_total(rz_cur, kCgBlocks, sh);
   const double pq = block_total(pq_part, kCgBlocks, sh);
-  const double alpha = rz / pq;
-  double rzn = 0.0, rr = 0.0;
+  const T alpha = (T)(rz / pq);
+  T rzn = 0, rr = 0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    x[i] = (T)((double)x[i] + alpha * (double)p[i]);
-    const double ri = (double)r[i] - alpha * (double)q[i];
-    r[i] = (T)ri;
-    const double zi = (double)dinv[i] * ri;
-    z[i] = (T)zi;
+    x[i] = x[i] + alpha * p[i];
+    const T ri = r[i] - alpha * q[i];
+    r[i] = ri;
+    const T zi = dinv[i] * ri;
+    z[i] = zi;
     rzn += ri * zi;
     rr += ri * ri;
   }
-  block_store(rzn, rz_next + blockIdx.x, sh);
-  block_store(rr, rr_part + blockIdx.x, sh);
+  block_store((double)rzn, rz_next + blockIdx.x, sh);
+  block_store((double)rr, rr_part + blockIdx.x, sh);
 }
 
 template <class T, class VT>
