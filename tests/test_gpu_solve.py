@@ -81,6 +81,28 @@ def test_continuity_pinned_cg(gpu_ctx_factory, oracle):
     ctx.close()
 
 
+@pytest.mark.parametrize("precision", [ng.PRECISION_FP64, ng.PRECISION_FP32_INNER_IR])
+def test_gmres_restart_cycles_match_oracle(gpu_ctx_factory, oracle, precision):
+    """Restarted GMRES(10) over many restart cycles needs about as many
+    iterations as the oracle's GMRES(10) on the same system (61 on this 16^3
+    heat system).  Every cycle must build its Hessenberg matrix afresh: a
+    cycle that adds to the previous cycle's rotated columns stalls (in a CPU
+    replay of that mistake, still 1.4e-6 after 20,000 iterations).  The
+    device aims at half the tolerance and starts identity rows from x = b,
+    hence the margin; the FP32-inner solve restarts at every refinement."""
+    ctx = _heat_system(gpu_ctx_factory, N=16)
+    info = ctx.solve(ng.default_solver_opts(method=ng.SOLVER_GMRES, precond=ng.PRECOND_JACOBI, precision=precision,
+                                            tol=1e-8, restart=10, max_iters=5000))
+    res, (rp, ci, v, b) = _true_res(oracle, ctx, ctx.solution())
+    _, it_o, res_o = oracle.gmres_jacobi(rp, ci, v, b, restart=10, tol=1e-8, max_it=5000)
+    assert res_o <= 1e-8
+    assert info.status == 0 and res <= 1.05e-8
+    # FP32-inner: restarts at each FP64 refinement (inner tolerance 1e-4)
+    slack = 1.3 if precision == ng.PRECISION_FP64 else 2.0
+    assert info.iterations <= slack * it_o + 10, (info.iterations, it_o)
+    ctx.close()
+
+
 def _momentum_system(gpu_ctx_factory, advect=True):
     """MomentumUpwAdvDiff (alpha_upw 0.5) on a jittered 10^3 mesh with a
     random-Fourier velocity and a lumped time term on the diagonal, so the
