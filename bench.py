@@ -364,7 +364,8 @@ def bench_gpu(args):
                                                     learned_probe=probe), raise_on_error=False)
             solve[key] = {"ms": 1e3 * info.seconds, "setup_ms": 1e3 * info.setup_seconds,
                           "iterations": info.iterations, "learned_iterations": info.learned_iterations,
-                          "fallback": info.fallback, "true_rel_res": info.true_rel_res, "status": info.status}
+                          "fallback": info.fallback, "true_rel_res": info.true_rel_res, "status": info.status,
+                          "probe_rates": [info.probe_rate_jacobi, info.probe_rate_learned]}
         solve["learned_fallback_codes"] = ("0 learned FCG finished, 1 it stalled -> Chebyshev-Jacobi PCG, "
                                            "2 Jacobi-CG finished (opening probe or pace bound); learned_fcg runs "
                                            "the flexible CG itself, learned_fcg_probe the default with the probe")
@@ -608,7 +609,7 @@ def bench_c4(ng, weights, dev=0, N=192):
                      "status": info.status}
         if kw:
             out[name].update(setup_ms=1e3 * info.setup_seconds, learned_iterations=info.learned_iterations,
-                             fallback=info.fallback)
+                             fallback=info.fallback, probe_rates=[info.probe_rate_jacobi, info.probe_rate_learned])
     out["learned_vs_plain_time"] = out["jacobi_pcg_fp64"]["ms"] / out["learned_fcg"]["ms"]
     out["learned_probe_vs_plain_time"] = out["jacobi_pcg_fp64"]["ms"] / out["learned_fcg_probe"]["ms"]
     ctx.close()

@@ -348,6 +348,8 @@ typedef struct nalu_solve_info {
   int learned_iterations;/* iterations spent in the learned FCG (probe included);
                             iterations counts the probe runs too */
   double setup_seconds;  /* learned preconditioner set-up (MLP stencil + SELL values) */
+  double probe_rate_jacobi;  /* opening probe, ln(residual reduction) per ms of */
+  double probe_rate_learned; /* iterations (negative; 0 when no probe ran) */
 } nalu_solve_info;
 void nalu_solver_opts_default(nalu_solver_opts* opts);
 /* solve A x = rhs into the context's solution vector */

@@ -75,7 +75,8 @@ class SolverOpts(ctypes.Structure):
 class SolveInfo(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int), ("outer_iterations", ctypes.c_int), ("status", ctypes.c_int),
                 ("true_rel_res", ctypes.c_double), ("seconds", ctypes.c_double), ("fallback", ctypes.c_int),
-                ("learned_iterations", ctypes.c_int), ("setup_seconds", ctypes.c_double)]
+                ("learned_iterations", ctypes.c_int), ("setup_seconds", ctypes.c_double),
+                ("probe_rate_jacobi", ctypes.c_double), ("probe_rate_learned", ctypes.c_double)]
 
 
 class TrainOpts(ctypes.Structure):

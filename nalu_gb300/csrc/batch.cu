@@ -583,6 +583,7 @@ int solve_batched(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* inf
   const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   bool all_ok = true;
   for (int pr = 0; pr < P; ++pr) {
+    infos[pr] = nalu_solve_info{};
     infos[pr].iterations = iters[pr];
     infos[pr].outer_iterations = 1;
     infos[pr].true_rel_res = true_res[pr];

@@ -1008,6 +1008,7 @@ int solve(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* info) {
     return set_error(ctx, NALU_ERR_ARG, "the learned preconditioner runs in FP64 flexible CG only");
   bool fallback = false, probe_chose_jacobi = false;
   int learned_its = 0, probe_its = 0, pace_its = 0;
+  double probe_rj = 0.0, probe_rl = 0.0;
   double setup_s = 0.0;
   nalu_solver_opts fb = o;  // Chebyshev-Jacobi PCG after a stall of the learned FCG
   fb.precond = NALU_PRECOND_CHEBYSHEV;
@@ -1055,6 +1056,8 @@ int solve(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* info) {
           const double ratej = std::log(std::max(resj, 1e-300) / r0) / std::max(tj, 1e-3);
           const double ratel = std::log(std::max(resl, 1e-300) / r0) / std::max(tl, 1e-3);
           use_jacobi = stl || (rcl != NALU_OK && rcl != NALU_ERR_NOT_CONVERGED) || !(ratel < ratej);
+          probe_rj = ratej;
+          probe_rl = ratel;
           // pace: Jacobi-CG's probe rate, extrapolated, gives the iterations it
           // would need; the learned FCG gets at most twice as many
           if (resj < r0 && resj > 0.0) {
@@ -1146,6 +1149,8 @@ int solve(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* info) {
   info->fallback = probe_chose_jacobi ? 2 : (fallback ? 1 : 0);
   info->learned_iterations = learned_its;
   info->setup_seconds = setup_s;
+  info->probe_rate_jacobi = probe_rj;
+  info->probe_rate_learned = probe_rl;
   info->true_rel_res = res;
   info->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   if (rc == NALU_OK && res > o.tol) rc = set_error(ctx, NALU_ERR_NOT_CONVERGED, "tolerance not reached");
