@@ -82,3 +82,29 @@ def test_master_element_tables(cudalib, oracle):
         shp = shp.reshape(12, 8)
         assert np.allclose(shp @ (x @ a + b), (shp @ x) @ a + b, atol=1e-14)
         assert np.allclose(shp.sum(axis=1), 1.0, atol=1e-15)
+
+
+def test_struct_layouts_match_header(tmp_path):
+    """The ctypes mirrors of the option and info structs have the size and
+    field offsets that a C compiler gives the header's structs."""
+    import shutil
+    if shutil.which("gcc") is None:
+        pytest.skip("no C compiler")
+    import nalu_gb300 as ng
+    structs = {"nalu_assemble_opts": ng.AssembleOpts, "nalu_solver_opts": ng.SolverOpts,
+               "nalu_solve_info": ng.SolveInfo, "nalu_train_opts": ng.TrainOpts}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "nalu_gb300.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append('printf("%s %%zu\\n", sizeof(%s));' % (cname, cname))
+        for field in py._fields_:
+            lines.append('printf("%s.%s %%zu\\n", offsetof(%s, %s));' % (cname, field[0], cname, field[0]))
+    lines += ["return 0;", "}"]
+    src, exe = tmp_path / "layout.c", tmp_path / "layout"
+    src.write_text("\n".join(lines) + "\n")
+    subprocess.run(["gcc", "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = dict(line.split() for line in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                        check=True).stdout.splitlines())
+    for cname, py in structs.items():
+        assert int(got[cname]) == ctypes.sizeof(py), cname
+        for field in py._fields_:
+            assert int(got["%s.%s" % (cname, field[0])]) == getattr(py, field[0]).offset, (cname, field[0])
