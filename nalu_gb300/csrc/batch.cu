@@ -7,8 +7,8 @@
 // df64 SELL-32 SpMV, search direction as FP32 pairs, dot products as FP32
 // pairs, x and r in FP64.
 //
-// Rows are cut into tiles of at most 256 rows that never cross a problem
-// boundary; one block owns one tile and one thread one row.  An iteration is
+// Rows are cut into tiles of at most 1024 rows that never cross a problem
+// boundary; one block owns one tile and one thread four of its rows.  An iteration is
 // three kernels over the tiles:
 //   pupdate  p = D^-1 r + beta_p p
 //   spmv     q = A p, tile sums of p.q; the last tile of a problem to finish
@@ -38,8 +38,9 @@
 namespace nalu_gb300 {
 namespace {
 
-constexpr int kBT = 256;  // threads per block = rows per tile
-constexpr int kTileRows = kBT;
+constexpr int kBT = 256;                  // threads per block (one block per tile)
+constexpr int kRowsPerThread = 4;         // a tile's fixed costs (block sums, ticket) over 4 rows a thread
+constexpr int kTileRows = kRowsPerThread * kBT;
 constexpr int kSliceB = 32;
 
 struct TileArgs {
@@ -116,9 +117,8 @@ __global__ void __launch_bounds__(kBT) k_bt_prec(TileArgs a) {
   const int t = blockIdx.x;
   const int pr = a.tile_prob[t];
   if (a.done[pr] || a.mode[pr] != 1) return;
-  const int i = threadIdx.x;
   double dot = 0.0;
-  if (i < a.tile_rows[t]) {
+  for (int i = threadIdx.x; i < a.tile_rows[t]; i += kBT) {
     const int64_t row = a.tile_row0[t] + i;
     const int64_t sl = row / kSliceB;
     const int64_t b0 = __ldg(a.sptr + sl);
@@ -139,7 +139,7 @@ __global__ void __launch_bounds__(kBT) k_bt_prec(TileArgs a) {
     }
     const double zi = widen_f(acc);
     a.z[row] = zi;
-    dot = zi * join_df(a.q2[row]);
+    dot += zi * join_df(a.q2[row]);
   }
   const double v[1] = {dot};
   double tot[1];
@@ -151,13 +151,14 @@ __global__ void __launch_bounds__(kBT) k_bt_pupdate(TileArgs a) {
   const int t = blockIdx.x;
   const int pr = a.tile_prob[t];
   if (a.done[pr]) return;
-  const int i = threadIdx.x;
-  if (i >= a.tile_rows[t]) return;
-  const int64_t row = a.tile_row0[t] + i;
   const float2 beta = split_df(a.beta[pr]);
-  const float2 z = a.mode[pr] == 1 ? split_df(a.z[row])
-                                   : fma_df(a.r2[row], make_float2(a.dinvf[row], 0.0f), make_float2(0.0f, 0.0f));
-  a.p[row] = fma_df(beta, a.p[row], z);
+  const bool learned = a.mode[pr] == 1;
+  for (int i = threadIdx.x; i < a.tile_rows[t]; i += kBT) {
+    const int64_t row = a.tile_row0[t] + i;
+    const float2 z = learned ? split_df(a.z[row])
+                             : fma_df(a.r2[row], make_float2(a.dinvf[row], 0.0f), make_float2(0.0f, 0.0f));
+    a.p[row] = fma_df(beta, a.p[row], z);
+  }
 }
 
 __global__ void __launch_bounds__(kBT) k_bt_spmv(TileArgs a) {
@@ -165,9 +166,8 @@ __global__ void __launch_bounds__(kBT) k_bt_spmv(TileArgs a) {
   const int t = blockIdx.x;
   const int pr = a.tile_prob[t];
   if (a.done[pr]) return;
-  const int i = threadIdx.x;
   float dh = 0.0f, dl = 0.0f, rh = 0.0f, rl = 0.0f;
-  if (i < a.tile_rows[t]) {
+  for (int i = threadIdx.x; i < a.tile_rows[t]; i += kBT) {
     const int64_t row = a.tile_row0[t] + i;
     const int64_t s = row / kSliceB;
     const int64_t b0 = __ldg(a.sptr + s);
@@ -202,11 +202,10 @@ __global__ void __launch_bounds__(kBT) k_bt_axpy(TileArgs a) {
   const int t = blockIdx.x;
   const int pr = a.tile_prob[t];
   if (a.done[pr]) return;
-  const int i = threadIdx.x;
   float zh = 0.0f, zl = 0.0f, rh = 0.0f, rl = 0.0f;
-  if (i < a.tile_rows[t]) {
+  const float2 al = split_df(a.alpha[pr]);
+  for (int i = threadIdx.x; i < a.tile_rows[t]; i += kBT) {
     const int64_t row = a.tile_row0[t] + i;
-    const float2 al = split_df(a.alpha[pr]);
     a.x2[row] = fma_df(al, a.p[row], a.x2[row]);
     const float2 rs = fma_df(make_float2(-al.x, -al.y), a.q2[row], a.r2[row]);
     a.r2[row] = rs;
@@ -255,9 +254,8 @@ __global__ void __launch_bounds__(kBT) k_batch_resid(TileArgs a, const int64_t* 
                                                      const double* __restrict__ b, double* __restrict__ tb) {
   __shared__ double sh[33];
   const int t = blockIdx.x;
-  const int i = threadIdx.x;
   double rz = 0.0, rr = 0.0, bb = 0.0;
-  if (i < a.tile_rows[t]) {
+  for (int i = threadIdx.x; i < a.tile_rows[t]; i += kBT) {
     const int64_t row = a.tile_row0[t] + i;
     double s = 0.0;
     for (int64_t j = rp[row]; j < rp[row + 1]; ++j) s += v[j] * a.x[ci[j]];
@@ -308,7 +306,7 @@ int solve_batched(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* inf
   if (P < 1) return set_error(ctx, NALU_ERR_STATE, "no problem partition (nalu_set_problems)");
   const int64_t n = ctx->n_rows;
   const int nd = ctx->num_dof;
-  // tiles of <= 256 rows inside each problem
+  // tiles of <= kTileRows rows inside each problem
   std::vector<int64_t> trow0;
   std::vector<int32_t> trows, tprob, pt0(P), pt1(P);
   for (int pr = 0; pr < P; ++pr) {
