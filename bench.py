@@ -193,6 +193,67 @@ def run_cpu_sample(O, c, conn, graph, u, rho, p, gp, n_elems_sample, n_threads):
     return n_elems_sample / dt, dt
 
 
+def err_over_tol(actual, expected, rowptr=None):
+    """largest |a - b| / (1e-12 max(|a|,|b|) + 1e-12 scale) -- the parity
+    tolerance of the tests; scale is the row's largest |entry| for CRS values
+    (rowptr given), the vector's largest |entry| otherwise.  <= 1 passes."""
+    if rowptr is not None:
+        n = rowptr.size - 1
+        rowid = np.repeat(np.arange(n), np.diff(rowptr))
+        rm = np.zeros(n)
+        np.maximum.at(rm, rowid, np.abs(expected))
+        floor = rm[rowid]
+        del rowid
+    else:
+        floor = np.max(np.abs(expected))
+    allowed = 1e-12 * np.maximum(np.abs(actual), np.abs(expected)) + 1e-12 * floor
+    return float(np.max(np.abs(actual - expected) / allowed))
+
+
+class OracleChecker:
+    """The oracle as the checker of the GPU results, run after every timed
+    region: the FP64 CPU restatement assembles the same system, and the
+    worst error ratio against the test tolerance is reported per result."""
+
+    def __init__(self, threads):
+        from oracle import oracle as O
+        if not os.path.exists(os.path.join(ROOT, "oracle", "liboracle.so")):
+            subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "liboracle.so"], check=True)
+        self.O = O
+        self.threads = threads
+
+    def continuity(self, ctx, c, conn, gid, u, rho, p, gp):
+        O = self.O
+        rp, ci = ctx.graph()
+        orp, oci, lid = O.graph(c.shape[0], conn, 1, gid)
+        vals, rhs = ctx.system()
+        t0 = time.perf_counter()
+        ov, orhs = O.assemble(O.KERNEL_CONTINUITY_ADV, c, conn, rp, ci, lid, scalar=p, coeff=rho, vec=u, vec2=gp,
+                              n_threads=self.threads)
+        t_asm = time.perf_counter() - t0
+        return {"values": err_over_tol(vals, ov, rp), "rhs": err_over_tol(rhs, orhs),
+                "graph_bit_exact": bool(np.array_equal(rp, orp) and np.array_equal(ci, oci)),
+                "oracle_assembly_s": t_asm, "oracle_threads": self.threads}
+
+    def momentum(self, ctx, kernel_oracle, c, conn, gid, u, mu, rho, gju, mdot, opts):
+        O = self.O
+        rp, ci = ctx.graph()
+        _, _, lid = O.graph(c.shape[0], conn, 3, gid)
+        vals, rhs = ctx.system()
+        ov, orhs = O.assemble(kernel_oracle, c, conn, rp, ci, lid, coeff=mu, vec=u, vec2=u, rho=rho, gju=gju,
+                              mdot=mdot, opts=O.opts_block(**opts), n_threads=self.threads)
+        return {"values": err_over_tol(vals, ov, rp), "rhs": err_over_tol(rhs, orhs)}
+
+    def residual(self, ctx):
+        """true relative residual ||b - A x|| / ||b|| of the solution, by the
+        oracle's FP64 SpMV on the host copy of the system"""
+        rp, ci = ctx.graph()
+        vals, b = ctx.system()
+        x = ctx.solution()
+        r = b - self.O.spmv(rp, ci, vals, x, n_threads=self.threads)
+        return float(np.linalg.norm(r) / np.linalg.norm(b))
+
+
 def bench_reference(args):
     ws, rank, local, dist = dist_init()
     if rank != 0:
@@ -267,6 +328,9 @@ def bench_gpu(args):
         for sc in (ng.SCATTER_ATOMIC, ng.SCATTER_COLOURED):
             modes["%s_%s_ms" % (arith_names[ar], {1: "atomic", 2: "coloured"}[sc])] = time_mode(ctx, ar, sc)
     best = min(modes, key=modes.get)
+    # both arithmetics' rates, best scatter each (device time of one assembly, best of 3)
+    arith_rates = {"%s_elements_per_s" % an: n_elems / (1e-3 * min(v for k, v in modes.items() if k.startswith(an)))
+                   for an in arith_names.values() if any(k.startswith(an) for k in modes)}
     arith = ng.ARITH_DF64 if best.startswith("df64") else ng.ARITH_FP64
     scatter = ng.SCATTER_COLOURED if "coloured" in best else ng.SCATTER_ATOMIC
     opts = ng.default_assemble_opts(scatter=scatter, arith=arith)
@@ -375,9 +439,22 @@ def bench_gpu(args):
         solve["learned_probe_vs_plain_time"] = solve["jacobi_pcg_fp64"]["ms"] / solve["learned_fcg_probe"]["ms"]
         if not args.no_c4:
             solve["c4_192"] = bench_c4(ng, learned_w, local)
+    # the oracle checks every reported result after its timed region (rank 0, single GPU)
+    checker = OracleChecker(cpu_threads()) if rank == 0 and ws == 1 and not args.no_cpu else None
+    precision = None
+    if checker is not None:
+        # the headline system in both arithmetics against one FP64 oracle assembly
+        for nm, v in (("velocity", u), ("density", rho), ("pressure", p), ("dpdx", gp)):
+            ctx.field_set(nm, v)
+        precision = {"tolerance": "|a-b| <= 1e-12 max(|a|,|b|) + 1e-12 (row max |b|); ratio <= 1 passes"}
+        for an, ar in (("df64", ng.ARITH_DF64), ("fp64", ng.ARITH_FP64)):
+            ctx.zero()
+            ctx.assemble(ng.KERNEL_CONTINUITY_ADV, ng.default_assemble_opts(scatter=scatter, arith=ar))
+            ctx.load_complete()
+            precision["assembly_128_%s" % an] = checker.continuity(ctx, c, conn, gid, u, rho, p, gp)
     aux = bench_aux(ng, ctx, c, conn, rho) if extras and not args.no_aux else None
     batch = bench_batch(ng, local) if extras and not args.no_batch else None
-    momentum = bench_c3(ng, local) if extras and not args.no_c3 else None
+    momentum = bench_c3(ng, local, checker=checker) if extras and not args.no_c3 else None
     heat = bench_c1(ng, local) if extras and not args.no_c1 else None
     # ---- CPU baseline on rank 0 (oracle, bounded sample) ----
     cpu = None
@@ -399,6 +476,12 @@ def bench_gpu(args):
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
             "dtype": "f64" if arith == ng.ARITH_FP64 else "f64 in/out, df64 (FP32-pair) element math",
+            "fp64_elements_per_s": arith_rates.get("fp64_elements_per_s"),
+            "df64_elements_per_s": arith_rates.get("df64_elements_per_s"),
+            "max_err_over_tol": (None if precision is None else
+                                 max(precision["assembly_128_%s" % arith_names[arith]]["values"],
+                                     precision["assembly_128_%s" % arith_names[arith]]["rhs"])),
+            "precision": precision,
             "data": "synthetic",
             "config": dict(workload_config(), scatter={1: "atomic", 2: "coloured"}.get(scatter, str(scatter)),
                            arith=arith_names[arith], mode_ms=modes,
@@ -517,7 +600,7 @@ def bench_c1(ng, dev=0, N=32, reps=5):
     return out
 
 
-def bench_c3(ng, dev=0, N=96, reps=5):
+def bench_c3(ng, dev=0, N=96, reps=5, checker=None):
     """Momentum (24x24 element matrices, 3 dofs/node) on a 96^3 unit cube with
     the Fourier64 velocity, viscosity 1e-3, mdot from the velocity
     (ComputeMdotElemAlgorithm): assembly time of the central
@@ -563,6 +646,20 @@ def bench_c3(ng, dev=0, N=96, reps=5):
         ms = timed_ms(ctx, lambda: ctx.assemble(ng.KERNEL_MOMENTUM_MASS, o), reps)
         out["mass"]["lumped" if lumped else "consistent"] = {"assemble_ms": ms,
                                                              "elements_per_s": conn.shape[0] / (ms * 1e-3)}
+    if checker is not None:
+        # df64 momentum values against the FP64 oracle (both kernels)
+        mdot = ctx.field_get("mass_flow_rate_scs", (conn.shape[0], 12))
+        O = checker.O
+        out["precision"] = {}
+        for name, kern, okern, kw in (
+                ("central_df64", ng.KERNEL_MOMENTUM_ADV_DIFF, O.KERNEL_MOMENTUM_ADV_DIFF, {}),
+                ("upwind_0.5_df64", ng.KERNEL_MOMENTUM_UPW_ADV_DIFF, O.KERNEL_MOMENTUM_UPW_ADV_DIFF,
+                 dict(alpha_upw=0.5, hybrid_factor=1.0))):
+            ctx.zero()
+            ctx.assemble(kern, ng.default_assemble_opts(arith=ng.ARITH_DF64, **kw))
+            out["precision"][name] = checker.momentum(ctx, okern, c, conn, gid, u, np.full(n, 1e-3), np.ones(n),
+                                                      np.zeros((n, 9)), mdot, kw)
+        del mdot
     ctx.zero()
     ctx.assemble(ng.KERNEL_MOMENTUM_UPW_ADV_DIFF,
                  ng.default_assemble_opts(arith=ng.ARITH_DF64, alpha_upw=0.5, hybrid_factor=1.0))
@@ -576,6 +673,9 @@ def bench_c3(ng, dev=0, N=96, reps=5):
     out["solve_gmres50_fp32_ir"] = {"ms": 1e3 * info.seconds, "iterations": info.iterations,
                                     "outer_iterations": info.outer_iterations, "true_rel_res": info.true_rel_res,
                                     "status": info.status}
+    if checker is not None:
+        # the mixed-precision solution's residual by the oracle's FP64 SpMV
+        out["solve_gmres50_fp32_ir"]["oracle_true_rel_res"] = checker.residual(ctx)
     ctx.close()
     return out
 
@@ -594,6 +694,20 @@ def bench_c4(ng, weights, dev=0, N=192):
     ctx.field_set("pressure", np.zeros(n))
     ctx.field_set("dpdx", np.zeros((n, 3)))
     ctx.build_elem_graph(1)
+    n_rows, nnz, _ = ctx.sizes()
+    E = conn.shape[0]
+    # the assembly at this size (the benchmark spec's 192^3 target): both
+    # arithmetics, best scatter each, device time per launch
+    asm = {}
+    peak, peak_kind = peaks()
+    alg = algorithmic_bytes(n, E, nnz, n_rows)
+    fp64_tf = ctx.probe_fp64_tflops()
+    for an, ar in (("df64", ng.ARITH_DF64), ("fp64", ng.ARITH_FP64)):
+        ms = min(time_mode(ctx, ar, sc) for sc in (ng.SCATTER_ATOMIC, ng.SCATTER_COLOURED))
+        gbs = alg / (ms * 1e-3) / 1e9
+        asm[an] = {"ms": ms, "elements_per_s": E / (ms * 1e-3), "achieved_gbs": gbs, "frac_of_hbm": gbs / peak,
+                   "peak_kind": peak_kind, "compute": compute_roof(E, ms, fp64_tf)}
+    asm["algorithmic_bytes_per_launch"] = alg
     ctx.zero()
     ctx.assemble(ng.KERNEL_CONTINUITY_ADV)
     ctx.reset_rows([0])
@@ -601,7 +715,7 @@ def bench_c4(ng, weights, dev=0, N=192):
     ctx.load_complete()
     ctx.learned_set_weights(weights)
     out = {"workload": "continuity_adv_hex8_192^3_zstretch1.05_fourier64, pinned node 0", "nodes": int(n),
-           "nnz": int(ctx.sizes()[1])}
+           "nnz": int(nnz), "assembly": asm}
     for name, kw in (("jacobi_pcg_fp64", {}), ("learned_fcg", {"precond": ng.PRECOND_LEARNED, "learned_probe": 0}),
                      ("learned_fcg_probe", {"precond": ng.PRECOND_LEARNED})):
         info = ctx.solve(ng.default_solver_opts(tol=1e-8, max_iters=60000, check_every=50, **kw), raise_on_error=False)

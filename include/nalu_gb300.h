@@ -443,7 +443,10 @@ int nalu_learned_stencil(nalu_ctx* ctx, float* stencil);
  * device looks up that array's device address and must therefore come before
  * any stream capture on that device.  All calls on a device share the array:
  * calls that overlap on the GPU race on it.  stream may be NULL (the legacy
- * default stream); the call returns after the solve has finished. */
+ * default stream); the call returns after the solve has finished.
+ * *iterations is the number of CG steps that moved the iterate, counted on
+ * the device (steps issued past convergence inside a 25-step chunk are
+ * frozen and not counted). */
 int nalu_pcg_jacobi_noalloc(int64_t n, const int64_t* rowptr, const int32_t* colind,
                             const double* values, const double* rhs, double* x, double tol,
                             int max_iters, int* iterations, double* true_rel_res, void* stream);

@@ -79,11 +79,12 @@ __global__ void __launch_bounds__(kAsmBlockDF, NALU_DF_MINB) k_assemble_scalar_d
   for (int n = 0; n < 8; ++n) pv[n] = __ldg(a.f_a + nd[n]);
   df64 rhs_df[8];
   double mindet;
+  int kexp;  // normalisation: lhs entries x 2^kexp, rhs (flux) entries x 2^(2 kexp)
   if constexpr (KIND == 0) {
     df64 k[8];
 #pragma unroll
     for (int n = 0; n < 8; ++n) k[n] = a.nodal[nd[n]];
-    mindet = scalar_diff_lhs_df<SHIFT>(x, k, acc);
+    mindet = scalar_diff_lhs_df<SHIFT>(x, k, acc, kexp);
 #pragma unroll
     for (int r = 0; r < 8; ++r) rhs_df[r] = df_zero();
   } else {
@@ -95,7 +96,7 @@ __global__ void __launch_bounds__(kAsmBlockDF, NALU_DF_MINB) k_assemble_scalar_d
     df64 pd[8];
 #pragma unroll
     for (int n = 0; n < 8; ++n) pd[n] = df_split_bits(pv[n]);
-    mindet = continuity_elem_df<MODE, SMDOT>(x, w, a.inv_tau, pd, acc, rhs_df);
+    mindet = continuity_elem_df<MODE, SMDOT>(x, w, a.inv_tau, pd, acc, rhs_df, kexp);
   }
   if (!(mindet > 1.0e-50)) atomicAdd(a.flags + FLAG_NEG_JAC, 1);
   const bool rhs_from_lhs = (KIND == 0) || (MODE != 1);
@@ -103,10 +104,10 @@ __global__ void __launch_bounds__(kAsmBlockDF, NALU_DF_MINB) k_assemble_scalar_d
   if (OUT == 2) {
 #pragma unroll
     for (int r = 0; r < 8; ++r) {
-      double s = df_to_double_bits(rhs_df[r]);
+      double s = df_to_double_bits(rhs_df[r], 2 * kexp);
 #pragma unroll
       for (int c = 0; c < 8; ++c) {
-        const double v = df_to_double_bits(acc.get(r, c));
+        const double v = df_to_double_bits(acc.get(r, c), kexp);
         a.cap_lhs[r * 8 + c] = v;
         if (rhs_from_lhs) s -= v * pv[c];
       }
@@ -119,12 +120,12 @@ __global__ void __launch_bounds__(kAsmBlockDF, NALU_DF_MINB) k_assemble_scalar_d
   for (int r = 0; r < 8; ++r) {
     const int64_t base = __ldg(a.rowptr + nd[r]);
     const uint2 o2 = __ldg(reinterpret_cast<const uint2*>(sl + 8 * r));
-    double s = df_to_double_bits(rhs_df[r]);
+    double s = df_to_double_bits(rhs_df[r], 2 * kexp);
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
       const uint32_t word = c < 4 ? o2.x : o2.y;
       const int off = (word >> (8 * (c & 3))) & 0xff;
-      const double v = df_to_double_bits(acc.get(r, c));
+      const double v = df_to_double_bits(acc.get(r, c), kexp);
       if (rhs_from_lhs) s -= v * pv[c];
       double* dst = a.values + base + off;
       if (OUT == 0) atomicAdd(dst, v);

@@ -71,29 +71,40 @@ DF_HD float u2f(uint32_t u) { float f; std::memcpy(&f, &u, 4); return f; }
 DF_HD int clz32(uint32_t v) { return v ? __builtin_clz(v) : 32; }
 #endif
 
-// Exact widening of a float to a double (normal floats; zero and float
-// subnormals, |f| < 2^-126, map to zero).
-DF_HD double f2d_bits(float f) {
+// Exact widening of f * 2^k to a double (normal floats; zero and float
+// subnormals, |f| < 2^-126, map to zero; results beyond the FP64 exponent
+// range saturate to 0 / inf).  k = 0 is the plain widening.
+DF_HD double f2d_bits(float f, int k = 0) {
   const uint32_t u = f2u(f);
   const uint32_t e = (u >> 23) & 0xff;
   if (e == 0) return 0.0;
   const uint64_t sign = (uint64_t)(u >> 31) << 63;
-  const uint64_t exp = (uint64_t)(e - 127 + 1023) << 52;
-  return u2d(sign | exp | ((uint64_t)(u & 0x7fffff) << 29));
+  const int ee = (int)e - 127 + 1023 + k;
+  if (ee <= 0) return u2d(sign);
+  if (ee >= 2047) return u2d(sign | (0x7ffull << 52));
+  return u2d(sign | ((uint64_t)ee << 52) | ((uint64_t)(u & 0x7fffff) << 29));
 }
 
-// hi + lo as a double: both widen exactly and their sum (<= 48 significant
-// bits) is exact in FP64, so one FP64 add is the only FP64 instruction.
-DF_HD double df_to_double_bits(df64 a) { return f2d_bits(a.hi) + f2d_bits(a.lo); }
+// (hi + lo) * 2^k as a double: both widen exactly and their sum (<= 48
+// significant bits) is exact in FP64, so one FP64 add is the only FP64
+// instruction.  The power-of-two factor undoes an exact scaling of the
+// inputs (per-element coordinate normalisation) at no cost.
+DF_HD double df_to_double_bits(df64 a, int k = 0) { return f2d_bits(a.hi, k) + f2d_bits(a.lo, k); }
 
-// Split a double into hi (nearest float) + lo (the remaining significand
-// bits, truncated to 24) with integer instructions only.  |d| must lie in
-// [2^-100, 2^127); smaller magnitudes return 0 (below anything the
-// element math sees relative to its inputs), which keeps lo a normal float.
-DF_HD df64 df_split_bits(double d) {
+// 2^k as a float, k in [-126, 127]
+DF_HD float pow2f(int k) { return u2f((uint32_t)(k + 127) << 23); }
+// unbiased binary exponent of a double (-1023 for zero and subnormals)
+DF_HD int dexp(double d) { return (int)((d2u(d) >> 52) & 0x7ff) - 1023; }
+
+// Split d * 2^-k into hi (nearest float) + lo (the remaining significand
+// bits, truncated to 24) with integer instructions only (the scaling is an
+// exponent shift, exact).  |d| 2^-k must lie in [2^-100, 2^127); smaller
+// magnitudes return 0 (below anything the element math sees relative to its
+// inputs), which keeps lo a normal float.
+DF_HD df64 df_split_bits(double d, int k = 0) {
   const uint64_t b = d2u(d);
   const int e = (int)((b >> 52) & 0x7ff);
-  const int E = e - 1023;
+  const int E = e - 1023 - k;
   if (e == 0 || E < -100) return {0.0f, 0.0f};
   const uint32_t sgn = (uint32_t)(b >> 32) & 0x80000000u;
   const uint64_t sig = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);  // 53 bits

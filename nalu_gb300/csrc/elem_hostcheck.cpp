@@ -90,14 +90,15 @@ extern "C" {
 void hc_scalar_diff_df(const double* xin, const double* q, const double* k, int shift, double* lhs,
                        double* rhs) {
   df64 kd[8], m[64];
+  int kexp = 0;
   for (int n = 0; n < 8; ++n) kd[n] = df_from_double(k[n]);
   with_x(xin, [&](double (&x)[8][3]) {
     df64 rr_acc[8];
     ArrayAccDF acc{m, rr_acc};
-    if (shift) scalar_diff_lhs_df<true>(x, kd, acc);
-    else scalar_diff_lhs_df<false>(x, kd, acc);
+    if (shift) scalar_diff_lhs_df<true>(x, kd, acc, kexp);
+    else scalar_diff_lhs_df<false>(x, kd, acc, kexp);
   });
-  for (int i = 0; i < 64; ++i) lhs[i] = df_to_double_bits(m[i]);
+  for (int i = 0; i < 64; ++i) lhs[i] = df_to_double_bits(m[i], kexp);
   for (int r = 0; r < 8; ++r) {
     double s = 0.0;
     for (int c = 0; c < 8; ++c) s += lhs[r * 8 + c] * q[c];
@@ -132,23 +133,24 @@ void hc_continuity_df(const double* xin, const double* u, const double* rho, con
   for (int n = 0; n < 8; ++n) pd[n] = df_split_bits(p[n]);
   const int mode = spois ? 2 : (reduced ? 1 : 0);
   const df64 it = df_from_double(1.0 / tau);
+  int kexp = 0;
   with_x(xin, [&](double (&x)[8][3]) {
     df64 rr_acc[8];
     ArrayAccDF acc{m, rr_acc};
     if (mode == 0) {
-      if (smdot) continuity_elem_df<0, true>(x, w, it, pd, acc, r8);
-      else continuity_elem_df<0, false>(x, w, it, pd, acc, r8);
+      if (smdot) continuity_elem_df<0, true>(x, w, it, pd, acc, r8, kexp);
+      else continuity_elem_df<0, false>(x, w, it, pd, acc, r8, kexp);
     } else if (mode == 1) {
-      if (smdot) continuity_elem_df<1, true>(x, w, it, pd, acc, r8);
-      else continuity_elem_df<1, false>(x, w, it, pd, acc, r8);
+      if (smdot) continuity_elem_df<1, true>(x, w, it, pd, acc, r8, kexp);
+      else continuity_elem_df<1, false>(x, w, it, pd, acc, r8, kexp);
     } else {
-      if (smdot) continuity_elem_df<2, true>(x, w, it, pd, acc, r8);
-      else continuity_elem_df<2, false>(x, w, it, pd, acc, r8);
+      if (smdot) continuity_elem_df<2, true>(x, w, it, pd, acc, r8, kexp);
+      else continuity_elem_df<2, false>(x, w, it, pd, acc, r8, kexp);
     }
   });
-  for (int i = 0; i < 64; ++i) lhs[i] = df_to_double_bits(m[i]);
+  for (int i = 0; i < 64; ++i) lhs[i] = df_to_double_bits(m[i], kexp);
   for (int r = 0; r < 8; ++r) {
-    double s = df_to_double_bits(r8[r]);
+    double s = df_to_double_bits(r8[r], 2 * kexp);
     if (mode != 1)
       for (int c = 0; c < 8; ++c) s -= lhs[r * 8 + c] * p[c];
     rhs[r] = s;

@@ -164,9 +164,10 @@ __global__ void __launch_bounds__(128) k_nodal_grad_df(int64_t n_elems, const in
     for (int d = 0; d < 3; ++d) xc[n][d] = __ldg(x + 3 * (int64_t)nd[n] + d);
   }
   EdgeFormDF f;
+  int kexp;  // normalised areas: x 2^(2 kexp)
   {
     df64 dd[8][3];
-    rel_coords_df(xc, dd);
+    kexp = rel_coords_df(xc, dd);
     edge_form_df(dd, f);
   }
   df64 qn[8][NC];
@@ -206,7 +207,7 @@ __global__ void __launch_bounds__(128) k_nodal_grad_df(int64_t n_elems, const in
     for (int k = 0; k < NC; ++k)
 #pragma unroll
       for (int j = 0; j < 3; ++j)
-        atomicAdd(grad + ((int64_t)nd[r] * NC + k) * 3 + j, df_to_double_bits(acc[k][j]) * inv);
+        atomicAdd(grad + ((int64_t)nd[r] * NC + k) * 3 + j, df_to_double_bits(acc[k][j], 2 * kexp) * inv);
   }
 }
 

@@ -25,14 +25,36 @@ struct EdgeFormDF {
   df64 A[3][3], B[3][3], C[3][3], D[3][3];  // [k][component]
 };
 
-// x relative to node 0 (FP64 differences), split into df64
-NALU_HD void rel_coords_df(const double x[8][3], df64 d[8][3]) {
+// Bound of the per-element normalisation exponent: 2^(2k) and 2^(-k) stay
+// normal floats, so kernels can move area- and length-scaled quantities
+// back to physical units in df64 as well as in FP64.
+constexpr int kNormExpMax = 62;
+
+// x relative to node 0 (FP64 differences), scaled by 2^-k and split into
+// df64, where 2^k bounds the largest difference: the element math then runs
+// on O(1) numbers whatever the mesh's units.  Products of three or four
+// lengths (det J, adj(J)^T A) would otherwise leave the FP32 exponent range
+// for element sizes below about 1e-9 or above 1e9.  Lengths in the results
+// carry the factor 2^k exactly (a power of two): the caller rescales them.
+NALU_HD int rel_coords_df(const double x[8][3], df64 d[8][3]) {
+  double dx[8][3];
+  int emax = -1023;
+#pragma unroll
+  for (int n = 1; n < 8; ++n)
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      dx[n][i] = x[n][i] - x[0][i];
+      const int e = dexp(dx[n][i]);
+      emax = e > emax ? e : emax;
+    }
+  const int k = emax < -kNormExpMax ? -kNormExpMax : (emax > kNormExpMax ? kNormExpMax : emax);
 #pragma unroll
   for (int i = 0; i < 3; ++i) d[0][i] = df_zero();
 #pragma unroll
   for (int n = 1; n < 8; ++n)
 #pragma unroll
-    for (int i = 0; i < 3; ++i) d[n][i] = df_split_bits(x[n][i] - x[0][i]);
+    for (int i = 0; i < 3; ++i) d[n][i] = df_split_bits(dx[n][i], k);
+  return k;
 }
 
 NALU_HD void edge_form_df(const df64 d[8][3], EdgeFormDF& f) {
@@ -219,12 +241,14 @@ NALU_HD void accumulate_ip_df(Acc& acc, int ip, const df64 fac[8]) {
 // ---------------------------------------------------------------------------
 // ScalarDiffElemKernel in df64 (k given per node as df64)
 // ---------------------------------------------------------------------------
+// The element matrix comes out in normalised units: entries times 2^kexp
+// are the physical ones (a diffusion matrix scales like a length).
 template <bool SHIFT, class Acc>
-NALU_HD double scalar_diff_lhs_df(const double x[8][3], const df64 k[8], Acc& acc) {
+NALU_HD double scalar_diff_lhs_df(const double x[8][3], const df64 k[8], Acc& acc, int& kexp) {
   EdgeFormDF f;
   {
     df64 d[8][3];
-    rel_coords_df(x, d);
+    kexp = rel_coords_df(x, d);
     edge_form_df(d, f);
   }
   df64 kc[8];
@@ -252,17 +276,20 @@ NALU_HD double scalar_diff_lhs_df(const double x[8][3], const df64 k[8], Acc& ac
 
 // ---------------------------------------------------------------------------
 // ContinuityAdvElemKernel in df64 (MODE as in hex8_elem.h).  The caller adds
-// -lhs . p in FP64 for MODE 0/2.
+// -lhs . p in FP64 for MODE 0/2.  Normalised units: lhs entries times
+// 2^kexp and rhs entries (mass flow rates, area-scaled) times 2^(2 kexp) are
+// the physical ones.
 // ---------------------------------------------------------------------------
 template <int MODE, bool SMDOT, class Acc>
 NALU_HD double continuity_elem_df(const double x[8][3], const df64 w[8][3], df64 inv_tau, const df64 p[8],
-                                  Acc& acc, df64 rhs[8]) {
+                                  Acc& acc, df64 rhs[8], int& kexp) {
   EdgeFormDF f;
   {
     df64 d[8][3];
-    rel_coords_df(x, d);
+    kexp = rel_coords_df(x, d);
     edge_form_df(d, f);
   }
+  const float inv_len = pow2f(-kexp);  // the length-scaled pressure term joins an area-scaled flux
   df64 wc[3][8];
 #pragma unroll
   for (int comp = 0; comp < 3; ++comp) {
@@ -303,7 +330,7 @@ NALU_HD double continuity_elem_df(const double x[8][3], const df64 w[8][3], df64
       df64 dpa = df_zero();
 #pragma unroll
       for (int c = 0; c < 8; ++c) dpa = df_fma(fs[c], p[c], dpa);
-      m = df_add(m, dpa);
+      m = df_add(m, df_scale2(dpa, inv_len));
     }
     // rhs[il] -= m ; rhs[ir] += m, accumulated beside the element matrix
     // (runtime row index; registers cannot be indexed at run time)
@@ -324,11 +351,13 @@ NALU_HD double continuity_elem_df(const double x[8][3], const df64 w[8][3], df64
 template <bool SMDOT, bool SPOIS>
 NALU_HD double mdot_elem_df(const double x[8][3], const df64 w[8][3], const df64 p[8], df64 tau, double* out) {
   EdgeFormDF f;
+  int kexp;
   {
     df64 d[8][3];
-    rel_coords_df(x, d);
+    kexp = rel_coords_df(x, d);
     edge_form_df(d, f);
   }
+  const float inv_len = pow2f(-kexp);
   df64 wc[3][8];
 #pragma unroll
   for (int comp = 0; comp < 3; ++comp) {
@@ -363,7 +392,7 @@ NALU_HD double mdot_elem_df(const double x[8][3], const df64 w[8][3], const df64
     df64 dpa = df_zero();
 #pragma unroll
     for (int c = 0; c < 8; ++c) dpa = df_fma(fs[c], p[c], dpa);
-    out[ip] = df_to_double_bits(df_sub(m0, df_mul(tau, dpa)));
+    out[ip] = df_to_double_bits(df_sub(m0, df_scale2(df_mul(tau, dpa), inv_len)), 2 * kexp);
   }
   return f2d_bits(mindet);
 }

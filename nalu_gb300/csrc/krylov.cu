@@ -247,7 +247,7 @@ __device__ __forceinline__ bool cg_frozen(const double* scal) {
   return scal[S_STOP] > 0.0 && scal[S_RR] <= scal[S_STOP];
 }
 
-__global__ void k_alpha(double* scal) {
+__device__ __forceinline__ void k_alpha_body(double* scal) {
   if (cg_frozen(scal)) {
     scal[S_ALPHA] = 0.0;
     return;
@@ -257,6 +257,7 @@ __global__ void k_alpha(double* scal) {
   scal[S_ALPHA] = isfinite(a) ? a : 0.0;
   if (!isfinite(a)) scal[S_BAD] = 1.0;
 }
+__global__ void k_alpha(double* scal) { k_alpha_body(scal); }
 __global__ void k_beta(double* scal) {
   if (cg_frozen(scal)) {
     scal[S_BETA] = 0.0;
@@ -1209,6 +1210,15 @@ double read_scalar_on(cudaStream_t s, const double* d, cudaError_t* err) {
   return h;
 }
 
+// scalar slot counting the iterations that moved the iterate (alpha taken
+// while the recurrence residual was still above the stop threshold)
+constexpr int S_NA_ITS = 10;
+
+__global__ void k_alpha_counted(double* scal) {
+  if (!cg_frozen(scal)) scal[S_NA_ITS] += 1.0;
+  k_alpha_body(scal);
+}
+
 template <int TPR>
 void noalloc_cg_chunk(cudaStream_t s, int64_t n, const int64_t* rp, const int32_t* ci, const double* v, double* x,
                       double* r, double* z, double* p, double* q, const double* dinv, double* partial, double* scal,
@@ -1217,7 +1227,7 @@ void noalloc_cg_chunk(cudaStream_t s, int64_t n, const int64_t* rp, const int32_
   for (int it = 0; it < iters; ++it) {
     k_spmv<double, double, TPR, true><<<kRedBlocks, 256, 0, s>>>(n, rp, ci, v, p, q, partial);
     k_finish<<<1, 256, 0, s>>>(partial, kRedBlocks, 1, scal, S_PQ);
-    k_alpha<<<1, 1, 0, s>>>(scal);
+    k_alpha_counted<<<1, 1, 0, s>>>(scal);
     k_cg_update<double><<<g, kRedThreads, 0, s>>>(n, scal, x, p, r, q, z, dinv, partial, 1);
     k_finish<<<1, 256, 0, s>>>(partial, g, 2, scal, S_RZNEW);
     k_beta<<<1, 1, 0, s>>>(scal);
@@ -1252,33 +1262,48 @@ extern "C" int nalu_pcg_jacobi_noalloc(int64_t n, const int64_t* rowptr, const i
   k_init_x<<<g256, 256, 0, s>>>(n, x, rhs, mask, 1);
   k_multi_dot<double><<<g, kRedThreads, 0, s>>>(n, 1, rhs, rhs, partial, nullptr, nullptr);
   k_finish<<<1, 256, 0, s>>>(partial, g, 1, scal, S_BB);
+  if ((err = cudaGetLastError()) != cudaSuccess) return NALU_ERR_CUDA;
   int64_t nnz = 0;
-  err = cudaMemcpyAsync(&nnz, rowptr + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
+  if ((err = cudaMemcpyAsync(&nnz, rowptr + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+    return NALU_ERR_CUDA;
   const double bnorm = std::sqrt(read_scalar_on(s, scal + S_BB, &err));
   if (err != cudaSuccess) return NALU_ERR_CUDA;
   const bool wide = nnz > 40 * n;  // 3-dof rows (81 entries) use 16 threads per row
   const double bref = bnorm > 0 ? bnorm : 1.0;
-  int total = 0;
+  int total = 0;  // iterations issued (whole chunks); the reported count comes from the device
   double res = 0.0;
   int status = NALU_OK;
   for (int outer = 0; outer < 8; ++outer) {
     k_residual<<<kRedBlocks, 256, 0, s>>>(n, rowptr, colind, values, x, rhs, r, partial);
     k_finish<<<1, 256, 0, s>>>(partial, kRedBlocks, 1, scal, S_TMP);
-    const double r0 = std::sqrt(read_scalar_on(s, scal + S_TMP, &err));
+    if ((err = cudaGetLastError()) != cudaSuccess) return NALU_ERR_CUDA;
+    const double r0sq = read_scalar_on(s, scal + S_TMP, &err);
     if (err != cudaSuccess) return NALU_ERR_CUDA;
+    const double r0 = std::sqrt(r0sq);
     res = r0 / bref;
     if (res <= tol || total >= max_iters) break;
     const double stop = std::max(tol * bref * 0.5, 1e-15 * r0);
+    // seed the recurrence residual and the stop threshold: once r.r falls to
+    // stop^2 inside a chunk, alpha = beta = 0 freeze the iterate (an exactly
+    // converged residual would otherwise give p.Ap = 0 and 0/0)
+    const double seed[2] = {r0sq, stop * stop};
     k_copy_scale<double><<<g256, 256, 0, s>>>(n, r, z, nullptr, dinv);
-    cudaMemcpyAsync(p, z, sizeof(double) * n, cudaMemcpyDeviceToDevice, s);
+    if ((err = cudaMemcpyAsync(p, z, sizeof(double) * n, cudaMemcpyDeviceToDevice, s)) != cudaSuccess)
+      return NALU_ERR_CUDA;
+    if ((err = cudaMemcpyAsync(scal + S_RR, &seed[0], sizeof(double), cudaMemcpyHostToDevice, s)) != cudaSuccess)
+      return NALU_ERR_CUDA;
+    if ((err = cudaMemcpyAsync(scal + S_STOP, &seed[1], sizeof(double), cudaMemcpyHostToDevice, s)) != cudaSuccess)
+      return NALU_ERR_CUDA;
     k_multi_dot<double><<<g, kRedThreads, 0, s>>>(n, 1, r, z, partial, nullptr, nullptr);
     k_finish<<<1, 256, 0, s>>>(partial, g, 1, scal, S_RZ);
     while (total < max_iters) {
       const int chunk = std::min(25, max_iters - total);
       if (wide) noalloc_cg_chunk<16>(s, n, rowptr, colind, values, x, r, z, p, q, dinv, partial, scal, chunk);
       else noalloc_cg_chunk<8>(s, n, rowptr, colind, values, x, r, z, p, q, dinv, partial, scal, chunk);
+      if ((err = cudaGetLastError()) != cudaSuccess) return NALU_ERR_CUDA;
       total += chunk;
       const double rr = read_scalar_on(s, scal + S_RR, &err);
+      if (err != cudaSuccess) return NALU_ERR_CUDA;
       const double bad = read_scalar_on(s, scal + S_BAD, &err);
       if (err != cudaSuccess) return NALU_ERR_CUDA;
       if (bad != 0.0 || !std::isfinite(rr)) {
@@ -1291,9 +1316,12 @@ extern "C" int nalu_pcg_jacobi_noalloc(int64_t n, const int64_t* rowptr, const i
   }
   k_residual<<<kRedBlocks, 256, 0, s>>>(n, rowptr, colind, values, x, rhs, r, partial);
   k_finish<<<1, 256, 0, s>>>(partial, kRedBlocks, 1, scal, S_TMP);
+  if ((err = cudaGetLastError()) != cudaSuccess) return NALU_ERR_CUDA;
   res = std::sqrt(read_scalar_on(s, scal + S_TMP, &err)) / bref;
   if (err != cudaSuccess) return NALU_ERR_CUDA;
-  if (iterations) *iterations = total;
+  const double its = read_scalar_on(s, scal + S_NA_ITS, &err);
+  if (err != cudaSuccess) return NALU_ERR_CUDA;
+  if (iterations) *iterations = (int)its;
   if (true_rel_res) *true_rel_res = res;
   if (status != NALU_OK) return status;
   return res <= tol ? NALU_OK : NALU_ERR_NOT_CONVERGED;

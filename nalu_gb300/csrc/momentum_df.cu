@@ -103,6 +103,7 @@ __global__ void __launch_bounds__(kMomThreads) k_assemble_momentum_df(MomArgs a)
   extern __shared__ df64 smd[];
   __shared__ int s_nodes[kMomElems][8];
   __shared__ int64_t s_elem[kMomElems];
+  __shared__ int s_kexp[kMomElems][8];  // per node: exponent of its largest coordinate difference
   const int t = threadIdx.x;
   const int el = t / 12, sub = t % 12;
   const int64_t gi = (int64_t)blockIdx.x * kMomElems + el;
@@ -110,6 +111,11 @@ __global__ void __launch_bounds__(kMomThreads) k_assemble_momentum_df(MomArgs a)
   df64* S = smd + el * MomLayoutDF::SIZE;
 
   // ---- phase 0: gather ----
+  // Coordinates relative to node 0 are normalised by 2^-k, 2^k bounding the
+  // element's largest difference (as rel_coords_df): the geometry then runs on
+  // O(1) numbers, and areas (x 2^2k), grad ops (x 2^-k) and lengths (x 2^k)
+  // return to physical units right after it.
+  double dxv[3] = {0.0, 0.0, 0.0};
   if (valid) {
     const int64_t e = (OUT == 2) ? a.cap_elem : (a.elems ? (int64_t)a.elems[gi] : gi);
     if (sub == 0) s_elem[el] = e;
@@ -117,11 +123,13 @@ __global__ void __launch_bounds__(kMomThreads) k_assemble_momentum_df(MomArgs a)
       const int n = __ldg(a.conn + 8 * e + sub);
       const int n0 = __ldg(a.conn + 8 * e);
       s_nodes[el][sub] = n;
+      int emax = -1023;
       for (int d = 0; d < 3; ++d) {
-        S[MomLayout::X + 3 * sub + d] =
-            sub == 0 ? df_zero() : spl(__ldg(a.x + 3 * (int64_t)n + d) - __ldg(a.x + 3 * (int64_t)n0 + d));
+        dxv[d] = sub == 0 ? 0.0 : __ldg(a.x + 3 * (int64_t)n + d) - __ldg(a.x + 3 * (int64_t)n0 + d);
+        emax = max(emax, dexp(dxv[d]));
         S[MomLayout::U + 3 * sub + d] = spl(__ldg(a.u + 3 * (int64_t)n + d));
       }
+      s_kexp[el][sub] = emax;
       S[MomLayout::MU + sub] = spl(__ldg(a.mu + n));
       if (UPW) {
         for (int d = 0; d < 3; ++d) S[MomLayout::VR + 3 * sub + d] = spl(__ldg(a.vrtm + 3 * (int64_t)n + d));
@@ -130,6 +138,16 @@ __global__ void __launch_bounds__(kMomThreads) k_assemble_momentum_df(MomArgs a)
       }
     }
     S[MomLayout::MD + sub] = spl(__ldg(a.mdot + 12 * e + sub));
+  }
+  __syncthreads();
+  int kexp = 0;
+  if (valid) {
+    int emax = s_kexp[el][0];
+#pragma unroll
+    for (int q = 1; q < 8; ++q) emax = max(emax, s_kexp[el][q]);
+    kexp = min(max(emax, -kNormExpMax), kNormExpMax);
+    if (sub < 8)
+      for (int d = 0; d < 3; ++d) S[MomLayout::X + 3 * sub + d] = df_split_bits(dxv[d], kexp);
   }
   __syncthreads();
   if (valid && sub < 9) edge_entry_df(S + MomLayout::X, sub / 3, sub % 3, S + MomLayoutDF::EF + 4 * sub);
@@ -147,9 +165,10 @@ __global__ void __launch_bounds__(kMomThreads) k_assemble_momentum_df(MomArgs a)
     cofactor_df(j, adj, det);
     const int dd = ip_dir(ip);
     const float sg4 = (ip < 8 && (ip & 3) == 2) ? -0.25f : 0.25f;
-    df64 A[3];
+    df64 A[3];  // physical area vector: normalised cofactor column x 2^2k
+    const float sgA = sg4 * pow2f(2 * kexp);
 #pragma unroll
-    for (int i = 0; i < 3; ++i) A[i] = df_scale2(dd == 0 ? adj[i][0] : (dd == 1 ? adj[i][1] : adj[i][2]), sg4);
+    for (int i = 0; i < 3; ++i) A[i] = df_scale2(dd == 0 ? adj[i][0] : (dd == 1 ? adj[i][1] : adj[i][2]), sgA);
     float mindet = det.hi;
 #pragma unroll
     for (int k = 0; k < 3; ++k) g[k] = s[k];
@@ -160,7 +179,7 @@ __global__ void __launch_bounds__(kMomThreads) k_assemble_momentum_df(MomArgs a)
       mindet = fminf(mindet, det.hi);
     }
     if (!(mindet > 1.0e-37f)) atomicAdd(a.flags + FLAG_NEG_JAC, 1);  // det <= 0 (or below FP32 range)
-    const df64 inv = df_rcp(det);
+    const df64 inv = df_scale2(df_rcp(det), pow2f(-kexp));  // adj / det in physical units (x 2^-k)
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -229,6 +248,13 @@ __global__ void __launch_bounds__(kMomThreads) k_assemble_momentum_df(MomArgs a)
           duL[i] = df_fma(df_sub(cIp[jj], X[3 * il + jj]), GJ[9 * il + 3 * i + jj], duL[i]);
           duR[i] = df_fma(df_sub(X[3 * ir + jj], cIp[jj]), GJ[9 * ir + 3 * i + jj], duR[i]);
         }
+      }
+      const float len = pow2f(kexp);  // normalised lengths back to physical units
+      udotx = df_scale2(udotx, len);
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        duL[i] = df_scale2(duL[i], len);
+        duR[i] = df_scale2(duR[i], len);
       }
       const df64 diffIp = df_scale2(df_add(df_div(MUn[il], RHO[il]), df_div(MUn[ir], RHO[ir])), 0.5f);
       const df64 pe = df_div(df_abs(udotx), df_add(diffIp, small_));

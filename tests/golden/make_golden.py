@@ -2,7 +2,7 @@
 
 Run once where the NaluCFD/Nalu source tree is available:
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <reference checkout>
 
 It reads the test sources as text (no reference code is executed) and writes
 ``tests/golden/nalu_unit_golds.json``.  The fixture records, per gold, the
@@ -131,4 +131,6 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <reference checkout>")
+    main(sys.argv[1])

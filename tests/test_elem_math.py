@@ -144,3 +144,37 @@ def test_df64_random_elements(elemcheck, oracle, translate):
             l2, r2 = _hc_cont_df(elemcheck, c, u, rho, p, gp, tau, *opts)
             check_dense(l2, l1, what="df64 continuity lhs %s" % (opts,))
             check_dense(r2[None], r1[None], what="df64 continuity rhs %s" % (opts,))
+
+
+@pytest.mark.parametrize("scale", [1e-9, 1e-15, 1e9, 1e15])
+def test_df64_scale_invariance(elemcheck, oracle, scale):
+    """Coordinates in units from 1e-15 to 1e15 (element sizes 1e-18 .. 1e14):
+    the df64 math normalises every element by a power of two, so products of
+    three or four lengths (det J, adj(J)^T A) never leave the FP32 exponent
+    range.  Same 1e-12 rule as at unit scale, aspect ratios up to 80."""
+    rng = np.random.default_rng(50)
+    for t in range(120):
+        h = rng.uniform(1 / 256, 1 / 16)
+        c = (BASE + 0.2 * rng.uniform(-1, 1, (8, 3))) * h
+        c[:, 2] *= rng.choice([1.0, 1 / 80.0])  # thin cells of the stretched meshes
+        c = (c + h * rng.uniform(0, 2, 3)) * scale  # near the origin: FP64 coordinates resolve thin cells
+        q, k = rng.uniform(0, 1, 8), rng.uniform(0.5, 2, 8)
+        for sh in (0, 1):
+            l1, r1 = oracle.scalar_diff_elem(c, q, k, sh)
+            l2, r2 = _hc_scalar_df(elemcheck, c, q, k, sh)
+            check_dense(l2, l1, what="df64 lhs x%g" % scale)
+            check_dense(r2[None], r1[None], what="df64 rhs x%g" % scale)
+        u, gp = rng.normal(size=(8, 3)), rng.normal(size=(8, 3)) / scale
+        rho, p, tau = rng.uniform(0.5, 2, 8), rng.normal(size=8), rng.uniform(0.1, 2)
+        for opts in [(0, 0, 0), (0, 0, 1), (0, 1, 1), (1, 0, 0)]:
+            l1, r1 = oracle.continuity_adv_elem(c, u, rho, p, gp, tau, *opts)
+            l2, r2 = _hc_cont_df(elemcheck, c, u, rho, p, gp, tau, *opts)
+            check_dense(l2, l1, what="df64 continuity lhs x%g %s" % (scale, opts))
+            check_dense(r2[None], r1[None], what="df64 continuity rhs x%g %s" % (scale, opts))
+        cc = np.ascontiguousarray(c)
+        for sm, sp in [(0, 0), (1, 1)]:
+            m1 = oracle.mdot_elem(cc, rho, u, p, gp, tau, sm, sp)
+            m2 = np.zeros(12)
+            elemcheck.hc_mdot_df(P(cc), P(rho), P(np.ascontiguousarray(u)), P(p), P(np.ascontiguousarray(gp)),
+                                 float(tau), sm, sp, P(m2))
+            check_dense(m2[None], m1[None], what="mdot df64 x%g" % scale)
