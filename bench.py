@@ -334,6 +334,12 @@ def bench_gpu(args):
     arith = ng.ARITH_DF64 if best.startswith("df64") else ng.ARITH_FP64
     scatter = ng.SCATTER_COLOURED if "coloured" in best else ng.SCATTER_ATOMIC
     opts = ng.default_assemble_opts(scatter=scatter, arith=arith)
+    # the df64 kernel's schedule (elements to threads) was autotuned by the library on its first call
+    tuning = None
+    if ng.ARITH_DF64 in want:
+        sch, sc, table = ctx.assemble_tuning(ng.KERNEL_CONTINUITY_ADV)
+        tuning = {"schedule": ng.SCHEDULE_NAMES[sch], "scatter": {1: "atomic", 2: "coloured"}[sc],
+                  "candidates_ms": {"%s/%s" % k: v for k, v in table.items()}}
     for _ in range(max(args.warmup, 3)):
         ctx.zero()
         ctx.assemble(ng.KERNEL_CONTINUITY_ADV, opts)
@@ -484,7 +490,7 @@ def bench_gpu(args):
             "precision": precision,
             "data": "synthetic",
             "config": dict(workload_config(), scatter={1: "atomic", 2: "coloured"}.get(scatter, str(scatter)),
-                           arith=arith_names[arith], mode_ms=modes,
+                           arith=arith_names[arith], mode_ms=modes, df64_autotune=tuning,
                            parallelism="replicas" if ws > 1 else "single"),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "peak_kind": peak_kind, "algorithmic_bytes_per_launch": alg,

@@ -184,13 +184,24 @@ typedef struct nalu_assemble_opts {
   double gamma1;            /* TimeIntegrator::get_gamma1 (default 1, BDF1) */
   double gamma2;            /* get_gamma2 (default -1) */
   double gamma3;            /* get_gamma3 (default 0) */
-  int reserved[4];
+  int schedule;             /* enum nalu_schedule (double-float scalar kernels) */
+  int reserved[3];
 } nalu_assemble_opts;
 /* arithmetic of the element math; inputs, outputs, the CRS scatter and the
  * residual's -lhs.q term stay FP64 in both modes */
 enum nalu_arith {
   NALU_ARITH_FP64 = 0,  /* FP64 throughout */
   NALU_ARITH_DF64 = 1   /* double-float (hi+lo FP32 pair, ~48-bit) on the FP32 pipes */
+};
+/* how the double-float scalar kernels (ARITH_DF64, ScalarDiff / ContinuityAdv)
+ * map elements to threads; AUTO times every schedule x scatter pair on the
+ * first call of a context and kernel and keeps the fastest
+ * (nalu_assemble_tuning reports the table) */
+enum nalu_schedule {
+  NALU_SCHEDULE_AUTO = 0,
+  NALU_SCHEDULE_ELEMENT = 1, /* one thread per element, 64-thread blocks */
+  NALU_SCHEDULE_IP8 = 2,     /* one thread per (element, SCS ip), 8 elements per block */
+  NALU_SCHEDULE_IP16 = 3     /* the same, 16 elements per block, tighter register budget */
 };
 void nalu_assemble_opts_default(nalu_assemble_opts* opts);
 /* run one element kernel over all elements and sum into the system */
@@ -450,6 +461,13 @@ int nalu_learned_stencil(nalu_ctx* ctx, float* stencil);
 int nalu_pcg_jacobi_noalloc(int64_t n, const int64_t* rowptr, const int32_t* colind,
                             const double* values, const double* rhs, double* x, double tol,
                             int max_iters, int* iterations, double* true_rel_res, void* stream);
+
+/* the autotuned choice of the double-float scalar kernel `kernel` in this
+ * context: schedule, scatter and the measured device time (ms) of every
+ * candidate, ms[(schedule - 1) * 2 + (scatter - 1)] (-1 where not timed);
+ * NALU_ERR_STATE before the first tuned call.  No counterpart in the
+ * reference (its element loop has one fixed schedule per execution space). */
+int nalu_assemble_tuning(const nalu_ctx* ctx, int kernel, int* schedule, int* scatter, double* ms);
 
 /* ---- measurement helpers ------------------------------------------------ */
 /* number of this library's kernel launches since the context was created */

@@ -41,6 +41,8 @@ FACE_CONTINUITY_INFLOW, FACE_CONTINUITY_OPEN = 0, 1
 MAX_FACE_SETS = 16
 SCATTER_AUTO, SCATTER_ATOMIC, SCATTER_COLOURED = 0, 1, 2
 ARITH_FP64, ARITH_DF64 = 0, 1
+SCHEDULE_AUTO, SCHEDULE_ELEMENT, SCHEDULE_IP8, SCHEDULE_IP16 = 0, 1, 2, 3
+SCHEDULE_NAMES = {SCHEDULE_ELEMENT: "element", SCHEDULE_IP8: "ip8", SCHEDULE_IP16: "ip16"}
 SOLVER_CG, SOLVER_GMRES = 0, 1
 PRECOND_NONE, PRECOND_JACOBI, PRECOND_CHEBYSHEV, PRECOND_LEARNED = 0, 1, 2, 3
 LEARNED_PARAMS = 15361
@@ -61,7 +63,7 @@ class AssembleOpts(ctypes.Structure):
                 ("hybrid_factor", ctypes.c_double), ("scatter", ctypes.c_int), ("arith", ctypes.c_int),
                 ("lumped_mass", ctypes.c_int), ("balanced_force", ctypes.c_int), ("dt", ctypes.c_double),
                 ("gamma1", ctypes.c_double), ("gamma2", ctypes.c_double), ("gamma3", ctypes.c_double),
-                ("reserved", ctypes.c_int * 4)]
+                ("schedule", ctypes.c_int), ("reserved", ctypes.c_int * 3)]
 
 
 class SolverOpts(ctypes.Structure):
@@ -160,6 +162,7 @@ def lib():
             "nalu_learned_gradient": (I, [P, P, P, P, I64, P, ctypes.POINTER(D)]),
             "nalu_learned_stencil": (I, [P, P]),
             "nalu_solve_batched": (I, [P, P, P]),
+            "nalu_assemble_tuning": (I, [P, I, ctypes.POINTER(I), ctypes.POINTER(I), P]),
             "nalu_kernel_launch_count": (I64, [P]),
             "nalu_last_assemble_ms": (D, [P]),
             "nalu_probe_fp64_tflops": (I, [P, ctypes.POINTER(D)]),
@@ -303,6 +306,17 @@ class Context:
     def assemble(self, kernel, opts=None):
         opts = default_assemble_opts() if opts is None else opts
         self._check(lib().nalu_assemble(self._h, kernel, ctypes.byref(opts)), "assemble")
+
+    def assemble_tuning(self, kernel):
+        """the autotuned (schedule, scatter) of a double-float scalar kernel and
+        the device time (ms) of every candidate {(schedule, scatter): ms}"""
+        sch, sc = ctypes.c_int(), ctypes.c_int()
+        ms = np.zeros(6)
+        self._check(lib().nalu_assemble_tuning(self._h, kernel, ctypes.byref(sch), ctypes.byref(sc), _ptr(ms)),
+                    "assemble_tuning")
+        table = {(SCHEDULE_NAMES[1 + k // 2], {0: "atomic", 1: "coloured"}[k % 2]): float(ms[k])
+                 for k in range(6) if ms[k] >= 0}
+        return sch.value, sc.value, table
 
     def capture_element(self, kernel, elem, opts=None):
         opts = default_assemble_opts() if opts is None else opts

@@ -543,6 +543,7 @@ int nalu_linsys_build_elem_graph(nalu_ctx* ctx, int num_dof) {
   NALU_CUDA(ctx, cudaMemsetAsync(ctx->d_rhs.p, 0, sizeof(double) * ctx->n_rows, ctx->stream));
   NALU_CUDA(ctx, cudaMemsetAsync(ctx->d_x.p, 0, sizeof(double) * ctx->n_rows, ctx->stream));
   for (int& s : ctx->scatter_choice) s = 0;
+  for (int k = 0; k < 2; ++k) ctx->df_schedule[k] = ctx->df_scatter[k] = 0;
   // the host build (sorting, colouring) is synchronous; the uploads finish here
   NALU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return check_flags(ctx);
@@ -826,7 +827,63 @@ double time_assemble(nalu_ctx* ctx, int kernel, const nalu_assemble_opts& o, int
   cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
   return ms;
 }
+
+// Autotuner of the double-float scalar kernels: on the first call of a
+// context and kernel whose schedule or scatter is AUTO, time every schedule
+// (element per thread, ip per thread with 8 or 16 elements per block) with
+// both scatters on scratch copies of the system (two rounds, the second
+// counts), keep the fastest pair and its table.  Resolves o.schedule and
+// scatter for this call.
+int tune_df(nalu_ctx* ctx, int kernel, nalu_assemble_opts& o, int& scatter) {
+  const int k = kernel == NALU_KERNEL_SCALAR_DIFF ? 0 : 1;
+  const bool auto_sched = !(o.schedule >= NALU_SCHEDULE_ELEMENT && o.schedule <= NALU_SCHEDULE_IP16);
+  const bool auto_scatter = scatter == NALU_SCATTER_AUTO;
+  int rc = NALU_OK;
+  if ((auto_sched || auto_scatter) && ctx->df_schedule[k] == 0) {
+    DBuf<double> sv, sr;
+    NALU_CUDA(ctx, sv.alloc(ctx->nnz));
+    NALU_CUDA(ctx, sr.alloc(ctx->n_rows));
+    NALU_CUDA(ctx, cudaMemcpyAsync(sv.p, ctx->d_values.p, sizeof(double) * ctx->nnz, cudaMemcpyDeviceToDevice, ctx->stream));
+    NALU_CUDA(ctx, cudaMemcpyAsync(sr.p, ctx->d_rhs.p, sizeof(double) * ctx->n_rows, cudaMemcpyDeviceToDevice, ctx->stream));
+    double best = 1e30;
+    int best_sched = NALU_SCHEDULE_IP8, best_sc = NALU_SCATTER_ATOMIC;
+    for (int rep = 0; rep < 2; ++rep)
+      for (int sch = NALU_SCHEDULE_ELEMENT; sch <= NALU_SCHEDULE_IP16; ++sch)
+        for (int sc : {NALU_SCATTER_ATOMIC, NALU_SCATTER_COLOURED}) {
+          nalu_assemble_opts t = o;
+          t.schedule = sch;
+          const double ms = time_assemble(ctx, kernel, t, sc, &rc);
+          if (rc) return rc;
+          if (rep == 1) {
+            ctx->df_tune_ms[k][sch - 1][sc - 1] = ms;
+            if (ms < best) best = ms, best_sched = sch, best_sc = sc;
+          }
+        }
+    NALU_CUDA(ctx, cudaMemcpyAsync(ctx->d_values.p, sv.p, sizeof(double) * ctx->nnz, cudaMemcpyDeviceToDevice, ctx->stream));
+    NALU_CUDA(ctx, cudaMemcpyAsync(ctx->d_rhs.p, sr.p, sizeof(double) * ctx->n_rows, cudaMemcpyDeviceToDevice, ctx->stream));
+    NALU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->df_schedule[k] = best_sched;
+    ctx->df_scatter[k] = best_sc;
+    rc = check_flags(ctx);
+    if (rc) return rc;
+  }
+  if (auto_sched) o.schedule = ctx->df_schedule[k] ? ctx->df_schedule[k] : NALU_SCHEDULE_IP8;
+  if (auto_scatter) scatter = ctx->df_scatter[k] ? ctx->df_scatter[k] : NALU_SCATTER_ATOMIC;
+  return NALU_OK;
+}
 }  // namespace
+
+int nalu_assemble_tuning(const nalu_ctx* ctx, int kernel, int* schedule, int* scatter, double* ms) {
+  if (!ctx || kernel < NALU_KERNEL_SCALAR_DIFF || kernel > NALU_KERNEL_CONTINUITY_ADV) return NALU_ERR_ARG;
+  const int k = kernel == NALU_KERNEL_SCALAR_DIFF ? 0 : 1;
+  if (ctx->df_schedule[k] == 0) return NALU_ERR_STATE;
+  if (schedule) *schedule = ctx->df_schedule[k];
+  if (scatter) *scatter = ctx->df_scatter[k];
+  if (ms)
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 2; ++j) ms[2 * i + j] = ctx->df_tune_ms[k][i][j] > 0 ? ctx->df_tune_ms[k][i][j] : -1.0;
+  return NALU_OK;
+}
 
 int nalu_assemble(nalu_ctx* ctx, int kernel, const nalu_assemble_opts* opts) {
   if (ctx) NALU_RESOLVE_UPLOADS(ctx);
@@ -843,6 +900,16 @@ int nalu_assemble(nalu_ctx* ctx, int kernel, const nalu_assemble_opts* opts) {
   int scatter = opts->scatter;
   // the mass kernels scatter a few entries per row: atomics, no autotuning
   if (scatter == NALU_SCATTER_AUTO && kernel >= NALU_KERNEL_CONTINUITY_MASS) scatter = NALU_SCATTER_ATOMIC;
+  if (opts->arith == NALU_ARITH_DF64 && kernel <= NALU_KERNEL_CONTINUITY_ADV) {
+    // double-float scalar kernels: schedule x scatter, tuned together
+    nalu_assemble_opts o = *opts;
+    rc = tune_df(ctx, kernel, o, scatter);
+    if (rc) return rc;
+    cudaEventRecord(ctx->ev0, ctx->stream);
+    rc = launch_assemble(ctx, kernel, o, scatter);
+    cudaEventRecord(ctx->ev1, ctx->stream);
+    return rc;
+  }
   if (scatter == NALU_SCATTER_AUTO) {
     scatter = ctx->scatter_choice[kernel];
     if (scatter == 0) {

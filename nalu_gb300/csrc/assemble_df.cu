@@ -12,10 +12,13 @@
 #include <cstdint>
 
 #include "assemble_df.cuh"
+#include "assemble_ip.cuh"
 
 namespace nalu_gb300 {
 
 NALU_DF_VARIANTS(NALU_DF_EXTERN)
+NALU_IP_VARIANTS(NALU_IP_EXTERN, 8)
+NALU_IP_VARIANTS(NALU_IP_EXTERN, 16)
 
 __global__ void k_prepass_k_df(const double* __restrict__ k, df64* __restrict__ out, int64_t n) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -87,7 +90,29 @@ int launch_mdot_df(nalu_ctx* ctx, const nalu_assemble_opts& o) {
 
 namespace {
 
-void launch_df(nalu_ctx* ctx, int kernel, const nalu_assemble_opts& o, const AsmArgsDF& a, int out) {
+template <int EPB>
+void launch_ip(nalu_ctx* ctx, int kernel, const nalu_assemble_opts& o, const AsmArgsDF& a, int out) {
+  if (kernel == NALU_KERNEL_SCALAR_DIFF) {
+    if (o.shifted_grad_op) launch_ip_variant<EPB, 0, 0, true, false>(ctx, a, out);
+    else launch_ip_variant<EPB, 0, 0, false, false>(ctx, a, out);
+    return;
+  }
+  const int mode = o.shift_poisson ? 2 : (o.reduced_sens ? 1 : 0);
+  if (o.shift_mdot) {
+    if (mode == 0) launch_ip_variant<EPB, 1, 0, false, true>(ctx, a, out);
+    else if (mode == 1) launch_ip_variant<EPB, 1, 1, false, true>(ctx, a, out);
+    else launch_ip_variant<EPB, 1, 2, false, true>(ctx, a, out);
+  } else {
+    if (mode == 0) launch_ip_variant<EPB, 1, 0, false, false>(ctx, a, out);
+    else if (mode == 1) launch_ip_variant<EPB, 1, 1, false, false>(ctx, a, out);
+    else launch_ip_variant<EPB, 1, 2, false, false>(ctx, a, out);
+  }
+}
+
+// schedule: NALU_SCHEDULE_ELEMENT, _IP8 or _IP16 (resolved by the caller)
+void launch_df(nalu_ctx* ctx, int kernel, const nalu_assemble_opts& o, const AsmArgsDF& a, int out, int schedule) {
+  if (schedule == NALU_SCHEDULE_IP8) return launch_ip<8>(ctx, kernel, o, a, out);
+  if (schedule == NALU_SCHEDULE_IP16) return launch_ip<16>(ctx, kernel, o, a, out);
   if (kernel == NALU_KERNEL_SCALAR_DIFF) {
     if (o.shifted_grad_op) launch_df_variant<0, 0, true, false>(ctx, a, out);
     else launch_df_variant<0, 0, false, false>(ctx, a, out);
@@ -103,6 +128,14 @@ void launch_df(nalu_ctx* ctx, int kernel, const nalu_assemble_opts& o, const Asm
     else if (mode == 1) launch_df_variant<1, 1, false, false>(ctx, a, out);
     else launch_df_variant<1, 2, false, false>(ctx, a, out);
   }
+}
+
+// the schedule a call runs: the option if set, else the context's tuned
+// choice for the kernel, else one thread per SCS ip with 8 elements per block
+int resolve_schedule(const nalu_ctx* ctx, int kernel, const nalu_assemble_opts& o) {
+  if (o.schedule >= NALU_SCHEDULE_ELEMENT && o.schedule <= NALU_SCHEDULE_IP16) return o.schedule;
+  const int k = kernel == NALU_KERNEL_SCALAR_DIFF ? 0 : 1;
+  return ctx->df_schedule[k] ? ctx->df_schedule[k] : NALU_SCHEDULE_IP8;
 }
 
 // split the nodal inputs into df64 (scratch owned by the context)
@@ -144,17 +177,18 @@ int launch_assemble_df(nalu_ctx* ctx, int kernel, const nalu_assemble_opts& o, i
   AsmArgsDF a = base_args_df(ctx, kernel, o);
   int rc = prepass(ctx, kernel, o, a);
   if (rc) return rc;
+  const int schedule = resolve_schedule(ctx, kernel, o);
   if (scatter == NALU_SCATTER_COLOURED) {
     const int nc = (int)ctx->colour_offsets.size() - 1;
     for (int c = 0; c < nc; ++c) {
       AsmArgsDF ac = a;
       ac.elems = ctx->d_colour_elems.p + ctx->colour_offsets[c];
       ac.count = ctx->colour_offsets[c + 1] - ctx->colour_offsets[c];
-      launch_df(ctx, kernel, o, ac, 1);
+      launch_df(ctx, kernel, o, ac, 1, schedule);
     }
   } else {
     a.count = ctx->n_elems;
-    launch_df(ctx, kernel, o, a, 0);
+    launch_df(ctx, kernel, o, a, 0, schedule);
   }
   return cuda_check(ctx, cudaGetLastError(), "df64 assemble launch");
 }
@@ -168,7 +202,7 @@ int launch_capture_df(nalu_ctx* ctx, int kernel, const nalu_assemble_opts& o, in
   a.cap_elem = elem;
   a.cap_lhs = d_lhs;
   a.cap_rhs = d_rhs;
-  launch_df(ctx, kernel, o, a, 2);
+  launch_df(ctx, kernel, o, a, 2, resolve_schedule(ctx, kernel, o));
   return cuda_check(ctx, cudaGetLastError(), "df64 capture launch");
 }
 

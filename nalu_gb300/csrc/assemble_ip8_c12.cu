@@ -1,0 +1,10 @@
+// Explicit instantiations of the ip-per-thread double-float assembly kernel
+// (assemble_ip.cuh), 8 elements per block; split so nvcc compiles in parallel.
+#include "assemble_ip.cuh"
+
+namespace nalu_gb300 {
+template void launch_ip_variant<8, 1, 1, false, false>(nalu_ctx*, AsmArgsDF, int);
+template void launch_ip_variant<8, 1, 1, false, true>(nalu_ctx*, AsmArgsDF, int);
+template void launch_ip_variant<8, 1, 2, false, false>(nalu_ctx*, AsmArgsDF, int);
+template void launch_ip_variant<8, 1, 2, false, true>(nalu_ctx*, AsmArgsDF, int);
+}  // namespace nalu_gb300

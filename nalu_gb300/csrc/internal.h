@@ -178,6 +178,10 @@ struct nalu_ctx {
   nalu_gb300::DBuf<double> d_node_df;    // df64 split of nodal kernel inputs (8 B each)
   std::vector<int64_t> colour_offsets;   // [n_colours+1]
   int scatter_choice[6] = {0, 0, 0, 0, 0, 0};  // autotuned scatter per kernel (0 = not tuned)
+  // autotuned schedule x scatter of the double-float scalar kernels, per kernel,
+  // with the device time of every candidate [schedule - 1][scatter - 1]
+  int df_schedule[2] = {0, 0}, df_scatter[2] = {0, 0};
+  double df_tune_ms[2][3][2] = {};
 
   // independent problems in one context (node offsets in LID order)
   std::vector<int64_t> problem_offsets;

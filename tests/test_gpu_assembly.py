@@ -296,8 +296,12 @@ def test_negative_jacobian_reported(gpu_ctx_factory):
 # ---------------------------------------------------------------------------
 # double-float element math (ARITH_DF64) against the FP64 oracle
 # ---------------------------------------------------------------------------
+SCHEDULES = [ng.SCHEDULE_ELEMENT, ng.SCHEDULE_IP8, ng.SCHEDULE_IP16]
+
+
+@pytest.mark.parametrize("schedule", SCHEDULES)
 @pytest.mark.parametrize("scatter", [ng.SCATTER_ATOMIC, ng.SCATTER_COLOURED])
-def test_df64_scalar_diff_32cube(gpu_ctx_factory, oracle, scatter):
+def test_df64_scalar_diff_32cube(gpu_ctx_factory, oracle, scatter, schedule):
     c, conn, gid = block_mesh(32, jitter=0.1, seed=11)
     rng = np.random.default_rng(12)
     T, k = rng.uniform(0, 1, c.shape[0]), rng.uniform(0.5, 2.0, c.shape[0])
@@ -310,7 +314,7 @@ def test_df64_scalar_diff_32cube(gpu_ctx_factory, oracle, scatter):
     for shifted in (0, 1):
         ctx.zero()
         ctx.assemble(ng.KERNEL_SCALAR_DIFF, ng.default_assemble_opts(scatter=scatter, shifted_grad_op=shifted,
-                                                                     arith=ng.ARITH_DF64))
+                                                                     arith=ng.ARITH_DF64, schedule=schedule))
         ctx.load_complete()
         vals, rhs = ctx.system()
         ov, orhs = oracle.assemble(oracle.KERNEL_SCALAR_DIFF, c, conn, rp, ci, lid, scalar=T, coeff=k,
@@ -320,9 +324,11 @@ def test_df64_scalar_diff_32cube(gpu_ctx_factory, oracle, scatter):
     ctx.close()
 
 
+@pytest.mark.parametrize("schedule", SCHEDULES)
 @pytest.mark.parametrize("kw", [{}, {"reduced_sens": 1}, {"reduced_sens": 1, "shift_poisson": 1},
-                                {"shift_mdot": 1}, {"proj_time_scale": 0.37}])
-def test_df64_continuity(gpu_ctx_factory, oracle, kw):
+                                {"shift_mdot": 1}, {"proj_time_scale": 0.37},
+                                {"reduced_sens": 1, "shift_mdot": 1, "proj_time_scale": 0.37}])
+def test_df64_continuity(gpu_ctx_factory, oracle, kw, schedule):
     c, conn, gid = block_mesh(12, 10, 9, jitter=0.1, seed=3, z_ratio=1.05)
     u, rho, p, gp = continuity_fields(c, seed=4)
     ctx = _ctx(gpu_ctx_factory, c, conn, gid)
@@ -330,7 +336,7 @@ def test_df64_continuity(gpu_ctx_factory, oracle, kw):
         ctx.field_set(n, v)
     ctx.build_elem_graph(1)
     ctx.zero()
-    ctx.assemble(ng.KERNEL_CONTINUITY_ADV, ng.default_assemble_opts(arith=ng.ARITH_DF64, **kw))
+    ctx.assemble(ng.KERNEL_CONTINUITY_ADV, ng.default_assemble_opts(arith=ng.ARITH_DF64, schedule=schedule, **kw))
     ctx.load_complete()
     vals, rhs = ctx.system()
     rp, ci = ctx.graph()
@@ -344,12 +350,14 @@ def test_df64_continuity(gpu_ctx_factory, oracle, kw):
     ctx.close()
 
 
-def test_df64_golds_capture(gpu_ctx_factory, golds):
+@pytest.mark.parametrize("schedule", SCHEDULES)
+def test_df64_golds_capture(gpu_ctx_factory, golds, schedule):
     c, conn, gid = block_mesh(1, 1, 1)
     ctx = _ctx(gpu_ctx_factory, c, conn)
     ctx.field_set("scalar_q", TrigFields.temperature(c))
     ctx.field_set("diff_coeff", np.ones(8))
-    lhs, rhs = ctx.capture_element(ng.KERNEL_SCALAR_DIFF, 0, ng.default_assemble_opts(arith=ng.ARITH_DF64))
+    lhs, rhs = ctx.capture_element(ng.KERNEL_SCALAR_DIFF, 0,
+                                   ng.default_assemble_opts(arith=ng.ARITH_DF64, schedule=schedule))
     assert np.max(np.abs(lhs.ravel() - golds["scalar_diff"]["lhs"])) <= 1e-15
     ctx.field_set("velocity", TrigFields.velocity(c))
     ctx.field_set("density", np.ones(8))
@@ -358,7 +366,7 @@ def test_df64_golds_capture(gpu_ctx_factory, golds):
     for key, kw in [("continuity_default", {}), ("continuity_reduced_sens", {"reduced_sens": 1}),
                     ("continuity_reduced_shift", {"reduced_sens": 1, "shift_poisson": 1})]:
         lhs, rhs = ctx.capture_element(ng.KERNEL_CONTINUITY_ADV, 0,
-                                       ng.default_assemble_opts(arith=ng.ARITH_DF64, **kw))
+                                       ng.default_assemble_opts(arith=ng.ARITH_DF64, schedule=schedule, **kw))
         assert np.max(np.abs(lhs.ravel() - golds[key]["lhs"])) <= 1e-15, key
         assert np.max(np.abs(rhs - golds[key]["rhs"])) <= 1e-15, key
     ctx.close()
@@ -452,4 +460,37 @@ def test_df64_momentum_golds(gpu_ctx_factory, golds):
     g = golds["momentum_adv_diff"]
     assert np.max(np.abs(lhs.ravel() - g["lhs"])) <= 1e-14
     assert np.max(np.abs(rhs - g["rhs"])) <= 1e-14
+    ctx.close()
+
+
+def test_df64_autotuner_table(gpu_ctx_factory):
+    """The first AUTO df64 assembly times every schedule x scatter pair and
+    keeps the fastest; the table and the choice are reported, and the result
+    is the same system as an explicit run of the chosen pair."""
+    c, conn, gid = block_mesh(16, 14, 12, jitter=0.1, seed=9, z_ratio=1.05)
+    u, rho, p, gp = continuity_fields(c, seed=10)
+    ctx = _ctx(gpu_ctx_factory, c, conn, gid)
+    for n, v in (("velocity", u), ("density", rho), ("pressure", p), ("dpdx", gp)):
+        ctx.field_set(n, v)
+    ctx.build_elem_graph(1)
+    with pytest.raises(ng.NaluError):
+        ctx.assemble_tuning(ng.KERNEL_CONTINUITY_ADV)
+    ctx.zero()
+    ctx.assemble(ng.KERNEL_CONTINUITY_ADV, ng.default_assemble_opts(arith=ng.ARITH_DF64))
+    v_auto, r_auto = ctx.system()
+    sch, sc, table = ctx.assemble_tuning(ng.KERNEL_CONTINUITY_ADV)
+    assert len(table) == 6 and all(ms > 0 for ms in table.values())
+    best = min(table, key=table.get)
+    assert best == (ng.SCHEDULE_NAMES[sch], {1: "atomic", 2: "coloured"}[sc])
+    ctx.zero()
+    ctx.assemble(ng.KERNEL_CONTINUITY_ADV, ng.default_assemble_opts(arith=ng.ARITH_DF64, schedule=sch, scatter=sc))
+    v_exp, r_exp = ctx.system()
+    rp, _ = ctx.graph()
+    check_csr_values(v_auto, v_exp, rp, what="auto vs explicit")
+    check_vec(r_auto, r_exp, what="auto vs explicit rhs")
+    # the tuning did not leave its trial assemblies in the system
+    ctx.zero()
+    ctx.assemble(ng.KERNEL_CONTINUITY_ADV, ng.default_assemble_opts(arith=ng.ARITH_DF64, schedule=sch, scatter=sc))
+    v2, _ = ctx.system()
+    check_csr_values(v2, v_exp, rp, what="repeat")
     ctx.close()

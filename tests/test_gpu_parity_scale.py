@@ -50,7 +50,8 @@ def _continuity_ctx(c, conn, gid, u, rho, p, gp):
     return ctx
 
 
-def _check_continuity(ctx, oracle, c, conn, gid, u, rho, p, gp, scatters, opts=None, what=""):
+def _check_continuity(ctx, oracle, c, conn, gid, u, rho, p, gp, scatters, opts=None, what="",
+                      schedules=(ng.SCHEDULE_AUTO,)):
     rp, ci = ctx.graph()
     orp, oci, lid = oracle.graph(c.shape[0], conn, 1, gid)
     assert np.array_equal(rp, orp) and np.array_equal(ci, oci), "graph differs from the restated Tpetra graph"
@@ -60,15 +61,18 @@ def _check_continuity(ctx, oracle, c, conn, gid, u, rho, p, gp, scatters, opts=N
     ov, orhs = oracle.assemble(oracle.KERNEL_CONTINUITY_ADV, c, conn, rp, ci, lid, scalar=p, coeff=rho, vec=u,
                                vec2=gp, opts=o, n_threads=THREADS)
     ratios = {}
-    for sc in scatters:
-        ctx.zero()
-        ctx.assemble(ng.KERNEL_CONTINUITY_ADV, ng.default_assemble_opts(scatter=sc, arith=ng.ARITH_DF64, **kw))
-        ctx.load_complete()
-        vals, rhs = ctx.system()
-        check_csr_values(vals, ov, rp, what="%s df64 values (scatter %d)" % (what, sc))
-        check_vec(rhs, orhs, what="%s df64 rhs (scatter %d)" % (what, sc))
-        ratios[sc] = (err_ratio_csr(vals, ov, rp), err_ratio_vec(rhs, orhs))
-        print("%s scatter %d: max err/tol values %.3g rhs %.3g" % (what, sc, *ratios[sc]))
+    for sch in schedules:
+        for sc in scatters:
+            ctx.zero()
+            ctx.assemble(ng.KERNEL_CONTINUITY_ADV,
+                         ng.default_assemble_opts(scatter=sc, arith=ng.ARITH_DF64, schedule=sch, **kw))
+            ctx.load_complete()
+            vals, rhs = ctx.system()
+            tag = "%s df64 schedule %d scatter %d" % (what, sch, sc)
+            check_csr_values(vals, ov, rp, what=tag + " values")
+            check_vec(rhs, orhs, what=tag + " rhs")
+            ratios[sch, sc] = (err_ratio_csr(vals, ov, rp), err_ratio_vec(rhs, orhs))
+            print("%s: max err/tol values %.3g rhs %.3g" % (tag, *ratios[sch, sc]))
     return ratios
 
 
@@ -79,7 +83,7 @@ def test_df64_continuity_bench_workload(oracle):
     ctx = _continuity_ctx(c, conn, gid, u, rho, p, gp)
     assert ctx.sizes()[1] == 57066625
     _check_continuity(ctx, oracle, c, conn, gid, u, rho, p, gp, (ng.SCATTER_ATOMIC, ng.SCATTER_COLOURED),
-                      what="128^3 bench")
+                      what="128^3 bench", schedules=(ng.SCHEDULE_ELEMENT, ng.SCHEDULE_IP8, ng.SCHEDULE_IP16))
     ctx.close()
 
 
@@ -95,7 +99,7 @@ def test_df64_continuity_128_pressure_and_options(oracle):
     ctx = _continuity_ctx(c, conn, gid, u, rho, p, gp)
     for kw in ({"proj_time_scale": 0.37}, {"reduced_sens": 1, "shift_poisson": 1, "shift_mdot": 1}):
         _check_continuity(ctx, oracle, c, conn, gid, u, rho, p, gp, (ng.SCATTER_ATOMIC,), opts=kw,
-                          what="128^3 %s" % kw)
+                          what="128^3 %s" % kw, schedules=(ng.SCHEDULE_ELEMENT, ng.SCHEDULE_IP8, ng.SCHEDULE_IP16))
     ctx.close()
 
 
@@ -177,7 +181,8 @@ def test_df64_scaled_coordinates(oracle, scale):
     ctx = _continuity_ctx(c, conn, gid, u, rho, p, gp)
     for kw in ({}, {"reduced_sens": 1}, {"reduced_sens": 1, "shift_poisson": 1}, {"shift_mdot": 1}):
         _check_continuity(ctx, oracle, c, conn, gid, u, rho, p, gp, (ng.SCATTER_ATOMIC, ng.SCATTER_COLOURED),
-                          opts=kw, what="x%g %s" % (scale, kw))
+                          opts=kw, what="x%g %s" % (scale, kw),
+                          schedules=(ng.SCHEDULE_ELEMENT, ng.SCHEDULE_IP8, ng.SCHEDULE_IP16))
     # heat conduction
     rng = np.random.default_rng(7)
     T, k = rng.uniform(0, 1, c.shape[0]), rng.uniform(0.5, 2.0, c.shape[0])
@@ -186,14 +191,16 @@ def test_df64_scaled_coordinates(oracle, scale):
     rp, ci = ctx.graph()
     _, _, lid = oracle.graph(c.shape[0], conn, 1, gid)
     for sh in (0, 1):
-        ctx.zero()
-        ctx.assemble(ng.KERNEL_SCALAR_DIFF, ng.default_assemble_opts(shifted_grad_op=sh, arith=ng.ARITH_DF64))
-        ctx.load_complete()
-        vals, rhs = ctx.system()
         ov, orhs = oracle.assemble(oracle.KERNEL_SCALAR_DIFF, c, conn, rp, ci, lid, scalar=T, coeff=k,
                                    opts=oracle.opts_block(shifted_grad_op=sh), n_threads=THREADS)
-        check_csr_values(vals, ov, rp, what="x%g df64 heat values" % scale)
-        check_vec(rhs, orhs, what="x%g df64 heat rhs" % scale)
+        for sch in (ng.SCHEDULE_ELEMENT, ng.SCHEDULE_IP8, ng.SCHEDULE_IP16):
+            ctx.zero()
+            ctx.assemble(ng.KERNEL_SCALAR_DIFF, ng.default_assemble_opts(shifted_grad_op=sh, arith=ng.ARITH_DF64,
+                                                                         schedule=sch))
+            ctx.load_complete()
+            vals, rhs = ctx.system()
+            check_csr_values(vals, ov, rp, what="x%g df64 heat values (schedule %d)" % (scale, sch))
+            check_vec(rhs, orhs, what="x%g df64 heat rhs (schedule %d)" % (scale, sch))
     # mass flow rates
     for nm, v in (("velocity_rtm", u),):
         ctx.field_set(nm, v)
