@@ -324,19 +324,23 @@ def bench_gpu(args):
     arith_names = {ng.ARITH_FP64: "fp64", ng.ARITH_DF64: "df64"}
     want = {"auto": (ng.ARITH_FP64, ng.ARITH_DF64), "fp64": (ng.ARITH_FP64,), "df64": (ng.ARITH_DF64,)}[args.arith]
     modes = {}
+    sched = {"auto": ng.SCHEDULE_AUTO, "element": ng.SCHEDULE_ELEMENT, "ip8": ng.SCHEDULE_IP8,
+             "ip16": ng.SCHEDULE_IP16}[args.schedule]
+    scatters = {"auto": (ng.SCATTER_ATOMIC, ng.SCATTER_COLOURED), "atomic": (ng.SCATTER_ATOMIC,),
+                "coloured": (ng.SCATTER_COLOURED,)}[args.scatter]
     for ar in want:
-        for sc in (ng.SCATTER_ATOMIC, ng.SCATTER_COLOURED):
-            modes["%s_%s_ms" % (arith_names[ar], {1: "atomic", 2: "coloured"}[sc])] = time_mode(ctx, ar, sc)
+        for sc in scatters:
+            modes["%s_%s_ms" % (arith_names[ar], {1: "atomic", 2: "coloured"}[sc])] = time_mode(ctx, ar, sc, sched=sched)
     best = min(modes, key=modes.get)
     # both arithmetics' rates, best scatter each (device time of one assembly, best of 3)
     arith_rates = {"%s_elements_per_s" % an: n_elems / (1e-3 * min(v for k, v in modes.items() if k.startswith(an)))
                    for an in arith_names.values() if any(k.startswith(an) for k in modes)}
     arith = ng.ARITH_DF64 if best.startswith("df64") else ng.ARITH_FP64
     scatter = ng.SCATTER_COLOURED if "coloured" in best else ng.SCATTER_ATOMIC
-    opts = ng.default_assemble_opts(scatter=scatter, arith=arith)
+    opts = ng.default_assemble_opts(scatter=scatter, arith=arith, schedule=sched)
     # the df64 kernel's schedule (elements to threads) was autotuned by the library on its first call
     tuning = None
-    if ng.ARITH_DF64 in want:
+    if ng.ARITH_DF64 in want and sched == ng.SCHEDULE_AUTO:
         sch, sc, table = ctx.assemble_tuning(ng.KERNEL_CONTINUITY_ADV)
         tuning = {"schedule": ng.SCHEDULE_NAMES[sch], "scatter": {1: "atomic", 2: "coloured"}[sc],
                   "candidates_ms": {"%s/%s" % k: v for k, v in table.items()}}
@@ -808,10 +812,10 @@ def bench_batch(ng, dev=0, n_problems=64, seed=2025, reps=2):
     return out
 
 
-def time_mode(ctx, arith, scatter, reps=3):
+def time_mode(ctx, arith, scatter, reps=3, sched=0):
     """Device time (ms, best of reps after one warm-up) of one continuity assembly."""
     import nalu_gb300 as ng
-    o = ng.default_assemble_opts(scatter=scatter, arith=arith)
+    o = ng.default_assemble_opts(scatter=scatter, arith=arith, schedule=sched)
     best = None
     for r in range(reps + 1):
         ctx.zero()
@@ -842,6 +846,10 @@ def main():
     ap.add_argument("--size", type=int, default=128, help="elements per edge (default: the 128^3 workload)")
     ap.add_argument("--arith", default="auto", choices=["auto", "fp64", "df64"],
                     help="element-math arithmetic (auto: the faster; both pass the parity tests)")
+    ap.add_argument("--schedule", default="auto", choices=["auto", "element", "ip8", "ip16"],
+                    help="df64 kernel schedule (auto: the library's autotuner)")
+    ap.add_argument("--scatter", default="auto", choices=["auto", "atomic", "coloured"],
+                    help="scatter of the headline assembly (auto: the faster)")
     args = ap.parse_args()
     global N_EDGE
     N_EDGE = args.size
