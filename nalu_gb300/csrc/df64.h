@@ -71,18 +71,22 @@ DF_HD float u2f(uint32_t u) { float f; std::memcpy(&f, &u, 4); return f; }
 DF_HD int clz32(uint32_t v) { return v ? __builtin_clz(v) : 32; }
 #endif
 
-// Exact widening of f * 2^k to a double (normal floats; zero and float
-// subnormals, |f| < 2^-126, map to zero; results beyond the FP64 exponent
-// range saturate to 0 / inf).  k = 0 is the plain widening.
+#ifdef __CUDA_ARCH__
+DF_HD double hilo2d(uint32_t hi, uint32_t lo) { return __hiloint2double((int)hi, (int)lo); }
+#else
+DF_HD double hilo2d(uint32_t hi, uint32_t lo) { return u2d(((uint64_t)hi << 32) | lo); }
+#endif
+
+// Exact widening of f * 2^k to a double, built in the two 32-bit halves of
+// the result: sign, exponent rebased by 1023 - 127 + k, the 23 significand
+// bits shifted into place.  Normal floats; zero and float subnormals
+// (|f| < 2^-126) map to zero.  |k| <= 800 keeps every normal float's
+// exponent inside the FP64 range (the element math uses |k| <= 124).
 DF_HD double f2d_bits(float f, int k = 0) {
   const uint32_t u = f2u(f);
-  const uint32_t e = (u >> 23) & 0xff;
-  if (e == 0) return 0.0;
-  const uint64_t sign = (uint64_t)(u >> 31) << 63;
-  const int ee = (int)e - 127 + 1023 + k;
-  if (ee <= 0) return u2d(sign);
-  if (ee >= 2047) return u2d(sign | (0x7ffull << 52));
-  return u2d(sign | ((uint64_t)ee << 52) | ((uint64_t)(u & 0x7fffff) << 29));
+  const uint32_t e = (u >> 23) & 0xffu;
+  const uint32_t hi = (u & 0x80000000u) | ((e + (uint32_t)(896 + k)) << 20) | ((u >> 3) & 0xfffffu);
+  return e == 0 ? 0.0 : hilo2d(hi, u << 29);
 }
 
 // (hi + lo) * 2^k as a double: both widen exactly and their sum (<= 48

@@ -40,8 +40,8 @@ def elemcheck():
     import ctypes
     out = os.path.join(ROOT, "nalu_gb300", "_lib", "libnalu_elemcheck.so")
     src = os.path.join(ROOT, "nalu_gb300", "csrc", "elem_hostcheck.cpp")
-    hdr = os.path.join(ROOT, "nalu_gb300", "csrc", "hex8_elem.h")
-    if not os.path.exists(out) or os.path.getmtime(out) < max(os.path.getmtime(src), os.path.getmtime(hdr)):
+    hdrs = [os.path.join(ROOT, "nalu_gb300", "csrc", h) for h in ("hex8_elem.h", "hex8_elem_df.h", "df64.h")]
+    if not os.path.exists(out) or os.path.getmtime(out) < max(os.path.getmtime(f) for f in [src] + hdrs):
         os.makedirs(os.path.dirname(out), exist_ok=True)
         subprocess.run(["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-shared", "-o", out, src],
                        check=True)
