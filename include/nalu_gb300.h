@@ -315,8 +315,16 @@ enum nalu_precond {
   NALU_PRECOND_NONE = 0,
   NALU_PRECOND_JACOBI = 1,    /* Ifpack2 RELAXATION Jacobi, one sweep */
   NALU_PRECOND_CHEBYSHEV = 2, /* Chebyshev polynomial in D^-1 A */
-  NALU_PRECOND_LEARNED = 3    /* learned 27-point stencil (below) in flexible CG;
+  NALU_PRECOND_LEARNED = 3,   /* learned 27-point stencil (below) in flexible CG;
                                  scalar systems, FP64, needs weights */
+  /* aggregation multigrid in flexible CG, the GPU counterpart of the MueLu
+   * choice (src/LinearSolverConfig.C:92-96): pairwise aggregation on the
+   * strong couplings, Galerkin coarse operators, K-cycle, FP32 cycle inside
+   * FP64 flexible CG; scalar systems, FP64 precision.  MULTILEVEL smooths with
+   * damped Jacobi on every level; LEARNED_MULTILEVEL with the learned
+   * 27-point stencil on the fine level (needs weights) */
+  NALU_PRECOND_MULTILEVEL = 4,
+  NALU_PRECOND_LEARNED_MULTILEVEL = 5
 };
 enum nalu_precision {
   NALU_PRECISION_FP64 = 0,          /* everything FP64 */
@@ -342,7 +350,10 @@ typedef struct nalu_solver_opts {
                         unit of device time, and bounds the learned FCG by twice
                         the iterations the probe predicts for Jacobi-CG; 0 runs
                         the learned FCG with the stall fallback only */
-  int reserved[4];
+  int ml_kcycle_levels; /* multilevel preconditioners: coarse levels 1..k solve
+                           their coarse problem by K-cycle (two flexible CG steps),
+                           deeper ones by V-cycle; 0 (default) all, -1 none */
+  int reserved[3];
 } nalu_solver_opts;
 typedef struct nalu_solve_info {
   int iterations;        /* inner iterations in total */
@@ -468,6 +479,11 @@ int nalu_pcg_jacobi_noalloc(int64_t n, const int64_t* rowptr, const int32_t* col
  * NALU_ERR_STATE before the first tuned call.  No counterpart in the
  * reference (its element loop has one fixed schedule per execution space). */
 int nalu_assemble_tuning(const nalu_ctx* ctx, int kernel, int* schedule, int* scatter, double* ms);
+
+/* the level sizes of the last multilevel solve's hierarchy: returns the
+ * number of levels (0 when none was built) and fills rows[l], nnz[l] for
+ * l < max_levels (either may be NULL).  No counterpart in the reference. */
+int nalu_multilevel_levels(const nalu_ctx* ctx, int max_levels, int64_t* rows, int64_t* nnz);
 
 /* ---- measurement helpers ------------------------------------------------ */
 /* number of this library's kernel launches since the context was created */

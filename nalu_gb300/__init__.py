@@ -45,6 +45,7 @@ SCHEDULE_AUTO, SCHEDULE_ELEMENT, SCHEDULE_IP8, SCHEDULE_IP16 = 0, 1, 2, 3
 SCHEDULE_NAMES = {SCHEDULE_ELEMENT: "element", SCHEDULE_IP8: "ip8", SCHEDULE_IP16: "ip16"}
 SOLVER_CG, SOLVER_GMRES = 0, 1
 PRECOND_NONE, PRECOND_JACOBI, PRECOND_CHEBYSHEV, PRECOND_LEARNED = 0, 1, 2, 3
+PRECOND_MULTILEVEL, PRECOND_LEARNED_MULTILEVEL = 4, 5
 LEARNED_PARAMS = 15361
 PRECISION_FP64, PRECISION_FP32_INNER_IR = 0, 1
 
@@ -71,7 +72,7 @@ class SolverOpts(ctypes.Structure):
                 ("max_iters", ctypes.c_int), ("restart", ctypes.c_int), ("cheb_degree", ctypes.c_int),
                 ("check_every", ctypes.c_int), ("x0_zero", ctypes.c_int), ("tol", ctypes.c_double),
                 ("inner_tol", ctypes.c_double), ("stall_window", ctypes.c_int), ("learned_probe", ctypes.c_int),
-                ("reserved", ctypes.c_int * 4)]
+                ("ml_kcycle_levels", ctypes.c_int), ("reserved", ctypes.c_int * 3)]
 
 
 class SolveInfo(ctypes.Structure):
@@ -163,6 +164,7 @@ def lib():
             "nalu_learned_stencil": (I, [P, P]),
             "nalu_solve_batched": (I, [P, P, P]),
             "nalu_assemble_tuning": (I, [P, I, ctypes.POINTER(I), ctypes.POINTER(I), P]),
+            "nalu_multilevel_levels": (I, [P, I, P, P]),
             "nalu_kernel_launch_count": (I64, [P]),
             "nalu_last_assemble_ms": (D, [P]),
             "nalu_probe_fp64_tflops": (I, [P, ctypes.POINTER(D)]),
@@ -317,6 +319,12 @@ class Context:
         table = {(SCHEDULE_NAMES[1 + k // 2], {0: "atomic", 1: "coloured"}[k % 2]): float(ms[k])
                  for k in range(6) if ms[k] >= 0}
         return sch.value, sc.value, table
+
+    def multilevel_levels(self):
+        """(rows, nnz) per level of the last multilevel solve's hierarchy"""
+        rows, nnz = np.zeros(16, np.int64), np.zeros(16, np.int64)
+        nl = lib().nalu_multilevel_levels(self._h, 16, _ptr(rows), _ptr(nnz))
+        return rows[:nl].tolist(), nnz[:nl].tolist()
 
     def capture_element(self, kernel, elem, opts=None):
         opts = default_assemble_opts() if opts is None else opts

@@ -171,6 +171,7 @@ int nalu_destroy(nalu_ctx* ctx) {
   if (!ctx) return NALU_ERR_ARG;
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
+  nalu_gb300::ml_free(ctx);
   ctx->d_conn.free();
   ctx->d_lid.free();
   for (auto& f : ctx->fields) f.d.free();
@@ -1105,3 +1106,8 @@ int nalu_spmv(nalu_ctx* ctx, const double* x, double* y, int is_device) {
 }
 
 }  // extern "C"
+
+int nalu_multilevel_levels(const nalu_ctx* ctx, int max_levels, int64_t* rows, int64_t* nnz) {
+  if (!ctx || max_levels < 0) return NALU_ERR_ARG;
+  return nalu_gb300::ml_levels(ctx, max_levels, rows, nnz);
+}

@@ -146,6 +146,10 @@ struct FaceSet {
 
 }  // namespace nalu_gb300
 
+namespace nalu_gb300 {
+struct MlState;  // multilevel preconditioner hierarchy (multilevel.cu)
+}
+
 struct nalu_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -207,6 +211,7 @@ struct nalu_ctx {
 
   nalu_gb300::SolverWork sw;
   nalu_gb300::LearnedState learned;
+  nalu_gb300::MlState* ml = nullptr;  // aggregation multigrid of the last multilevel solve
 
   // boundary side sets (nalu_faceset_define / nalu_faceset_skin)
   nalu_gb300::FaceSet face_sets[NALU_MAX_FACE_SETS];
@@ -282,7 +287,15 @@ int compute_dinv(nalu_ctx* ctx);  // sw.dinv and d_bcmask for the current matrix
 template <class VT>
 int sell_build(nalu_ctx* ctx, SellMatrix& S, const VT** vals_out);
 // learned.cu
-int learned_prepare(nalu_ctx* ctx);  // slot map, stencil and SELL preconditioner for the current matrix
+int learned_prepare(nalu_ctx* ctx);
+// aggregation multigrid (multilevel.cu): the hierarchy for the current scalar
+// matrix; flexible CG with it on the residual r (in place) for the correction
+// x; the hierarchy's level sizes; its release
+int ml_setup(nalu_ctx* ctx, bool learned_smoother);
+int fcg_multilevel(nalu_ctx* ctx, double* x, double* r, double rtol, double r0norm, int max_it, int check_every,
+                   int klevels, int* iters_out);
+int ml_levels(const nalu_ctx* ctx, int max_levels, int64_t* rows, int64_t* nnz);
+void ml_free(nalu_ctx* ctx);  // slot map, stencil and SELL preconditioner for the current matrix
 // flexible CG with the learned preconditioner on A x = r (x from 0); returns
 // NALU_ERR_NOT_CONVERGED with *stalled = 1 when the residual made no progress
 // for `stall_window` iterations

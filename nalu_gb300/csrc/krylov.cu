@@ -1007,6 +1007,9 @@ int solve(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* info) {
   const bool learned = o.precond == NALU_PRECOND_LEARNED;
   if (learned && (o.method != NALU_SOLVER_CG || mixed))
     return set_error(ctx, NALU_ERR_ARG, "the learned preconditioner runs in FP64 flexible CG only");
+  const bool multilevel = o.precond == NALU_PRECOND_MULTILEVEL || o.precond == NALU_PRECOND_LEARNED_MULTILEVEL;
+  if (multilevel && (o.method != NALU_SOLVER_CG || mixed || ctx->num_dof != 1))
+    return set_error(ctx, NALU_ERR_ARG, "the multilevel preconditioner runs in FP64 flexible CG on scalar systems");
   bool fallback = false, probe_chose_jacobi = false;
   int learned_its = 0, probe_its = 0, pace_its = 0;
   double probe_rj = 0.0, probe_rl = 0.0;
@@ -1090,6 +1093,21 @@ int solve(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* info) {
             rc = NALU_OK;
           }
         }
+      } else if (multilevel) {
+        // aggregation multigrid in flexible CG (multilevel.cu), the hierarchy
+        // built for this matrix once per call
+        if (outer == 1) {
+          const auto ts = std::chrono::steady_clock::now();
+          if (o.precond == NALU_PRECOND_LEARNED_MULTILEVEL) {
+            const float2* sv2 = nullptr;
+            if ((rc = sell_build<float2>(ctx, s.sell, &sv2)) || (rc = learned_prepare(ctx))) return rc;
+          }
+          if ((rc = ml_setup(ctx, o.precond == NALU_PRECOND_LEARNED_MULTILEVEL))) return rc;
+          NALU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+          setup_s += std::chrono::duration<double>(std::chrono::steady_clock::now() - ts).count();
+        }
+        rc = fcg_multilevel(ctx, s.w.p, s.r.p, rtol, r0, o.max_iters - total_it, o.check_every, o.ml_kcycle_levels,
+                            &its);
       } else if (o.method == NALU_SOLVER_CG && (o.precond == NALU_PRECOND_JACOBI || probe_chose_jacobi)) {
         // two-kernel Jacobi-CG on the SELL-32 copy (cg_fast.cu)
         const double* sv = nullptr;

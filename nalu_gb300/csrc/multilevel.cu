@@ -1,0 +1,1201 @@
+// multilevel.cu -- aggregation multigrid preconditioner for the scalar
+// (continuity / heat) systems, in flexible CG, with either damped Jacobi or
+// the learned 27-point stencil (learned.cu) as the fine-level smoother.
+//
+// The reference solves the continuity system with Belos CG and either an
+// Ifpack2 Jacobi sweep or MueLu (src/LinearSolverConfig.C:81-96); this is the
+// GPU counterpart of the second choice, built around the learned smoother:
+//
+// Set-up, all on the device:
+//   * aggregation: three passes of pairwise handshake matching per level on
+//     the strong negative couplings (-a_ij >= 0.25 max_k -a_ik).  A row
+//     proposes to the unmatched strong neighbour of highest priority: the
+//     edge's symmetric strength -a_ij / sqrt(a_ii a_jj) in half-octave bins,
+//     ties within a bin broken by a per-round hash of the edge.  Mutual
+//     proposals pair up.  Unmatched rows then join the pair of their strongest
+//     matched strong neighbour, else stay singletons (identity rows always do);
+//   * coarse operators: Galerkin A_c = P^T A P for the piecewise-constant P of
+//     each pass, one warp per coarse row: the member rows' entries are
+//     gathered into shared memory, their distinct coarse columns found with a
+//     shared hash set, ranked (ascending column order) and summed in the
+//     gathered order, so the coarse matrix is deterministic;
+//   * FP32 copies, inverse diagonals, and smoothing weights 4 / (3 lambda_max)
+//     from power iteration (of D^-1 A, or of M A for the learned smoother);
+//   * the coarsest level (at most 512 rows, 1024 if coarsening stalls) is
+//     inverted densely: FP32 Gauss-Jordan with partial pivoting in one block.
+// Cycle (FP32 vectors and values): one pre- and one post-smoothing step per
+// level; the coarse problem of each level solved by a K-cycle (two flexible
+// CG steps preconditioned by the next level's cycle, Notay & Vassilevski 2008)
+// on the first `ml_kcycle_levels` coarse levels and by a V-cycle below.  The
+// outer flexible CG (FP64 vectors and values) judges convergence on the true
+// FP64 residual, as every other solve here.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <vector>
+
+#include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
+
+#include "internal.h"
+
+namespace nalu_gb300 {
+namespace {
+
+constexpr int kMlThreads = 256;
+constexpr int kMlBlocks = 1216;       // 8 blocks per SM: grid of the streaming kernels
+constexpr float kStrong = 0.25f;      // strong coupling: -a_ij >= kStrong * max_k -a_ik
+constexpr int kMatchRounds = 6;       // handshake rounds per pairwise pass
+constexpr int kPassesPerLevel = 3;    // pairwise passes per level
+constexpr int kMaxLevels = 12;
+constexpr int64_t kCoarsest = 512;    // coarsen until at most this many rows
+constexpr int64_t kDenseMax = 1024;   // largest coarsest level inverted densely
+constexpr int kGalWarps = 4;          // warps per block of the Galerkin kernels
+constexpr int kGalList = 1024;        // gathered entries per coarse row (at most)
+constexpr int kGalHash = 512;         // hash slots per warp
+constexpr int kGalUnique = 256;       // distinct coarse columns per row (at most)
+constexpr int kTpr = 4;               // threads per row of the CRS kernels
+
+__device__ __forceinline__ uint64_t d2u_bits(double d) { return (uint64_t)__double_as_longlong(d); }
+__device__ __forceinline__ int64_t gtid() { return (int64_t)blockIdx.x * blockDim.x + threadIdx.x; }
+__device__ __forceinline__ int64_t gstride() { return (int64_t)gridDim.x * blockDim.x; }
+
+// ---------------------------------------------------------------------------
+// aggregation
+// ---------------------------------------------------------------------------
+// smax[i] = max_{j != i} -a_ij (0 if none), diag[i] = |a_ii|
+__global__ void k_ml_smax(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                          const double* __restrict__ v, double* __restrict__ smax, double* __restrict__ diag) {
+  for (int64_t i = gtid(); i < n; i += gstride()) {
+    double m = 0.0, d = 0.0;
+    for (int64_t k = rp[i]; k < rp[i + 1]; ++k) {
+      if (ci[k] != i) m = fmax(m, -v[k]);
+      else d = fabs(v[k]);
+    }
+    smax[i] = m;
+    diag[i] = d;
+  }
+}
+
+// floor(2 log2 x) for x > 0, from the exponent and the significand
+__device__ __forceinline__ int strength_bin(double x) {
+  const uint64_t b = d2u_bits(x);
+  const int e = (int)((b >> 52) & 0x7ff) - 1023;
+  const double m = __longlong_as_double((long long)((b & 0x000FFFFFFFFFFFFFull) | (1023ull << 52)));
+  return 2 * e + (m >= 1.4142135623730951 ? 1 : 0);
+}
+// symmetric per-round hash of the edge (i, j)
+__device__ __forceinline__ uint64_t edge_hash(int32_t i, int32_t j, int round) {
+  uint64_t h = (uint64_t)min(i, j) * 0x9E3779B97F4A7C15ull + (uint64_t)max(i, j) * 0xBF58476D1CE4E5B9ull +
+               (uint64_t)(round + 1) * 0x94D049BB133111EBull;
+  h ^= h >> 31;
+  h *= 0xD6E8FEB86659FD93ull;
+  h ^= h >> 32;
+  return h;
+}
+
+// choice[i]: the unmatched strong neighbour of highest priority (-1: none).
+// Binning the strength is what lets handshakes succeed along chains whose
+// couplings change monotonically (the z lines of stretched meshes): with exact
+// strengths every row there proposes to the same side and few proposals are
+// mutual.
+__global__ void k_ml_choose(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                            const double* __restrict__ v, const double* __restrict__ smax,
+                            const double* __restrict__ diag, const int32_t* __restrict__ partner, int round,
+                            int32_t* __restrict__ choice) {
+  for (int64_t i = gtid(); i < n; i += gstride()) {
+    int32_t best = -1;
+    if (partner[i] < 0 && smax[i] > 0.0) {
+      const double thr = kStrong * smax[i];
+      int best_bin = -(1 << 30);
+      uint64_t best_h = 0;
+      for (int64_t k = rp[i]; k < rp[i + 1]; ++k) {
+        const int32_t j = ci[k];
+        const double w = -v[k];
+        if (j == i || partner[j] >= 0 || !(w >= thr)) continue;
+        const double dd = diag[i] * diag[j];
+        const int bin = dd > 0.0 ? strength_bin(w / sqrt(dd)) : -(1 << 29);
+        const uint64_t h = edge_hash((int32_t)i, j, round);
+        if (bin > best_bin || (bin == best_bin && (h > best_h || (h == best_h && j < best)))) {
+          best_bin = bin;
+          best_h = h;
+          best = j;
+        }
+      }
+    }
+    choice[i] = best;
+  }
+}
+
+// mutual choices become pairs
+__global__ void k_ml_match(int64_t n, const int32_t* __restrict__ choice, int32_t* __restrict__ partner) {
+  for (int64_t i = gtid(); i < n; i += gstride()) {
+    const int32_t j = choice[i];
+    if (partner[i] < 0 && j >= 0 && choice[j] == (int32_t)i) partner[i] = j;
+  }
+}
+
+// leader of each row: the smaller row of its pair; unmatched rows join the
+// pair of the strongest matched strong neighbour, else lead themselves
+__global__ void k_ml_attach(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                            const double* __restrict__ v, const double* __restrict__ smax,
+                            const int32_t* __restrict__ partner, int32_t* __restrict__ leader) {
+  for (int64_t i = gtid(); i < n; i += gstride()) {
+    const int32_t p = partner[i];
+    if (p >= 0) {
+      leader[i] = min((int32_t)i, p);
+      continue;
+    }
+    int32_t best = -1;
+    if (smax[i] > 0.0) {
+      const double thr = kStrong * smax[i];
+      double bw = 0.0;
+      for (int64_t k = rp[i]; k < rp[i + 1]; ++k) {
+        const int32_t j = ci[k];
+        const double w = -v[k];
+        if (j == i || partner[j] < 0 || !(w >= thr)) continue;
+        if (w > bw || (w == bw && j < best)) bw = w, best = j;
+      }
+    }
+    leader[i] = best >= 0 ? min(best, partner[best]) : (int32_t)i;
+  }
+}
+
+__global__ void k_ml_flag_leaders(int64_t n, const int32_t* __restrict__ leader, int32_t* __restrict__ flag) {
+  for (int64_t i = gtid(); i < n; i += gstride()) flag[i] = leader[i] == (int32_t)i ? 1 : 0;
+}
+__global__ void k_ml_assign(int64_t n, const int32_t* __restrict__ leader, const int32_t* __restrict__ id,
+                            int32_t* __restrict__ agg) {
+  for (int64_t i = gtid(); i < n; i += gstride()) agg[i] = id[leader[i]];
+}
+// map[i] <- agg[map[i]]: compose the passes of one level
+__global__ void k_ml_compose(int64_t n, int32_t* __restrict__ map, const int32_t* __restrict__ agg) {
+  for (int64_t i = gtid(); i < n; i += gstride()) map[i] = agg[map[i]];
+}
+__global__ void k_ml_iota(int64_t n, int32_t* __restrict__ a) {
+  for (int64_t i = gtid(); i < n; i += gstride()) a[i] = (int32_t)i;
+}
+__global__ void k_ml_fill_i32(int64_t n, int32_t* __restrict__ a, int32_t v) {
+  for (int64_t i = gtid(); i < n; i += gstride()) a[i] = v;
+}
+// member offsets of each aggregate from the sorted aggregate ids (every id in
+// [0, nc) has at least one member, its leader)
+__global__ void k_ml_member_ptr(int64_t n, int64_t nc, const int32_t* __restrict__ sorted_agg,
+                                int64_t* __restrict__ mptr) {
+  for (int64_t i = gtid(); i < n; i += gstride()) {
+    const int32_t a = sorted_agg[i];
+    if (i == 0)
+      for (int32_t c = 0; c <= a; ++c) mptr[c] = 0;
+    const int32_t next = i + 1 < n ? sorted_agg[i + 1] : (int32_t)nc;
+    for (int32_t c = a + 1; c <= next; ++c) mptr[c] = i + 1;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Galerkin coarse matrix, one warp per coarse row.  COUNT: the number of
+// distinct columns per row into cnt; else the row (ascending columns) at crp[I].
+// ---------------------------------------------------------------------------
+struct GalSmem {
+  int key[kGalList];
+  double val[kGalList];
+  int hash[kGalHash];
+  int uniq[kGalUnique];
+};
+
+template <bool COUNT>
+__global__ void __launch_bounds__(32 * kGalWarps) k_ml_galerkin(
+    int64_t nc, const int64_t* __restrict__ mptr, const int32_t* __restrict__ mem, const int64_t* __restrict__ rp,
+    const int32_t* __restrict__ ci, const double* __restrict__ v, const int32_t* __restrict__ agg,
+    const int64_t* __restrict__ crp, int64_t* __restrict__ cnt, int32_t* __restrict__ cci, double* __restrict__ cv,
+    int* __restrict__ overflow) {
+  extern __shared__ unsigned char smraw[];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  GalSmem& S = reinterpret_cast<GalSmem*>(smraw)[w];
+  const int64_t warps = (int64_t)gridDim.x * kGalWarps;
+  for (int64_t I = (int64_t)blockIdx.x * kGalWarps + w; I < nc; I += warps) {
+    // the member rows' entries, as coarse columns, in member then entry order
+    int L = 0;
+    bool over = false;
+    for (int64_t m = mptr[I]; m < mptr[I + 1]; ++m) {
+      const int32_t i = mem[m];
+      const int64_t b = rp[i];
+      const int len = (int)(rp[i + 1] - b);
+      if (L + len > kGalList) {
+        over = true;
+        break;
+      }
+      for (int k = lane; k < len; k += 32) {
+        S.key[L + k] = agg[ci[b + k]];
+        S.val[L + k] = v[b + k];
+      }
+      L += len;
+    }
+    for (int h = lane; h < kGalHash; h += 32) S.hash[h] = -1;
+    __syncwarp();
+    // distinct keys into the hash set (bounded linear probing)
+    for (int p = lane; p < L; p += 32) {
+      const int key = S.key[p];
+      int h = (int)(((unsigned)key * 2654435761u) >> 23) & (kGalHash - 1);
+      for (int probe = 0; probe < kGalHash; ++probe) {
+        const int prev = atomicCAS(&S.hash[h], -1, key);
+        if (prev == -1 || prev == key) break;
+        h = (h + 1) & (kGalHash - 1);
+      }
+    }
+    __syncwarp();
+    int U = 0;
+    for (int h0 = 0; h0 < kGalHash; h0 += 32) {
+      const int key = S.hash[h0 + lane];
+      const unsigned has = __ballot_sync(0xffffffffu, key >= 0);
+      const int pos = U + __popc(has & ((1u << lane) - 1u));
+      if (key >= 0 && pos < kGalUnique) S.uniq[pos] = key;
+      U += __popc(has);
+    }
+    __syncwarp();
+    if (U > kGalUnique) over = true;
+    if (over) {
+      if (lane == 0) {
+        atomicAdd(overflow, 1);
+        if (COUNT) cnt[I] = 0;
+      }
+      __syncwarp();
+      continue;
+    }
+    if (COUNT) {
+      if (lane == 0) cnt[I] = U;
+    } else {
+      const int64_t base = crp[I];
+      for (int u = lane; u < U; u += 32) {
+        const int key = S.uniq[u];
+        int rank = 0;
+        for (int q = 0; q < U; ++q) rank += S.uniq[q] < key ? 1 : 0;
+        double sum = 0.0;
+        for (int p = 0; p < L; ++p)
+          if (S.key[p] == key) sum += S.val[p];
+        cci[base + rank] = key;
+        cv[base + rank] = sum;
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// FP32 values and inverse diagonal of a level
+__global__ void k_ml_prep(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                          const double* __restrict__ vd, float* __restrict__ vf, float* __restrict__ dinv) {
+  for (int64_t i = gtid(); i < n; i += gstride()) {
+    double d = 0.0;
+    for (int64_t k = rp[i]; k < rp[i + 1]; ++k) {
+      vf[k] = (float)vd[k];
+      if (ci[k] == i) d = vd[k];
+    }
+    dinv[i] = d != 0.0 ? (float)(1.0 / d) : 0.0f;
+  }
+}
+
+// learned smoother values from A's SELL-32 layout (entry k of row i at
+// sptr[i / 32] + 32 k + i % 32, in the row's CRS order) to CRS order
+__global__ void k_ml_sell_to_crs(int64_t n, const int64_t* __restrict__ rp, const int64_t* __restrict__ sptr,
+                                 const float* __restrict__ ws, float* __restrict__ m) {
+  for (int64_t i = gtid(); i < n; i += gstride()) {
+    const int64_t base = sptr[i / 32] + (i % 32);
+    const int64_t b = rp[i], len = rp[i + 1] - b;
+    for (int64_t k = 0; k < len; ++k) m[b + k] = ws[base + 32 * k];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// cycle kernels (FP32), kTpr threads per row.  The row loop runs the same
+// number of times in every lane (rows past n repeat row n-1 and write
+// nothing), so the width-kTpr shuffles always see their whole group.
+// ---------------------------------------------------------------------------
+#define ML_ROW_LOOP(n)                                                                    \
+  const int sub = threadIdx.x % kTpr;                                                     \
+  const int64_t rstride = (int64_t)gridDim.x * (blockDim.x / kTpr);                       \
+  const int64_t rend = (n) + (rstride - (n) % rstride) % rstride;                         \
+  for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / kTpr; i < rend; i += rstride)
+
+__device__ __forceinline__ float row_dot(const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                                         const float* __restrict__ v, const float* __restrict__ x, int64_t i,
+                                         int sub) {
+  float s = 0.0f;
+  for (int64_t k = rp[i] + sub; k < rp[i + 1]; k += kTpr) s = fmaf(__ldg(v + k), __ldg(x + ci[k]), s);
+#pragma unroll
+  for (int o = kTpr / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, kTpr);
+  return s;
+}
+
+// t = b - A x
+__global__ void __launch_bounds__(kMlThreads) k_ml_residual(int64_t n, const int64_t* __restrict__ rp,
+                                                            const int32_t* __restrict__ ci,
+                                                            const float* __restrict__ v, const float* __restrict__ x,
+                                                            const float* __restrict__ b, float* __restrict__ t) {
+  ML_ROW_LOOP(n) {
+    const int64_t r = i < n ? i : n - 1;
+    const float ax = row_dot(rp, ci, v, x, r, sub);
+    if (i < n && sub == 0) t[i] = b[i] - ax;
+  }
+}
+
+// damped Jacobi from zero fused with the residual: z = w D^-1 b; t = b - A z
+__global__ void __launch_bounds__(kMlThreads) k_ml_jac0_residual(int64_t n, const int64_t* __restrict__ rp,
+                                                                 const int32_t* __restrict__ ci,
+                                                                 const float* __restrict__ v,
+                                                                 const float* __restrict__ dinv, float omega,
+                                                                 const float* __restrict__ b, float* __restrict__ z,
+                                                                 float* __restrict__ t) {
+  ML_ROW_LOOP(n) {
+    const int64_t r = i < n ? i : n - 1;
+    float s = 0.0f;
+    for (int64_t k = rp[r] + sub; k < rp[r + 1]; k += kTpr) {
+      const int32_t j = ci[k];
+      s = fmaf(__ldg(v + k), omega * __ldg(dinv + j) * __ldg(b + j), s);
+    }
+#pragma unroll
+    for (int o = kTpr / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, kTpr);
+    if (i < n && sub == 0) {
+      z[i] = omega * dinv[i] * b[i];
+      t[i] = b[i] - s;
+    }
+  }
+}
+
+// damped Jacobi step fused with the residual: zo = z + w D^-1 (b - A z)
+__global__ void __launch_bounds__(kMlThreads) k_ml_jac_step(int64_t n, const int64_t* __restrict__ rp,
+                                                            const int32_t* __restrict__ ci,
+                                                            const float* __restrict__ v,
+                                                            const float* __restrict__ dinv, float omega,
+                                                            const float* __restrict__ b, const float* __restrict__ z,
+                                                            float* __restrict__ zo) {
+  ML_ROW_LOOP(n) {
+    const int64_t r = i < n ? i : n - 1;
+    const float ax = row_dot(rp, ci, v, z, r, sub);
+    if (i < n && sub == 0) zo[i] = z[i] + omega * dinv[i] * (b[i] - ax);
+  }
+}
+
+// learned smoother step: zo = (z or 0) + w M t
+__global__ void __launch_bounds__(kMlThreads) k_ml_mstep(int64_t n, const int64_t* __restrict__ rp,
+                                                         const int32_t* __restrict__ ci, const float* __restrict__ m,
+                                                         float omega, const float* __restrict__ t,
+                                                         const float* __restrict__ z, float* __restrict__ zo) {
+  ML_ROW_LOOP(n) {
+    const int64_t r = i < n ? i : n - 1;
+    const float mt = row_dot(rp, ci, m, t, r, sub);
+    if (i < n && sub == 0) zo[i] = (z ? z[i] : 0.0f) + omega * mt;
+  }
+}
+
+// restriction rc[I] = sum of t over the members of I (member order)
+__global__ void k_ml_restrict(int64_t nc, const int64_t* __restrict__ mptr, const int32_t* __restrict__ mem,
+                              const float* __restrict__ t, float* __restrict__ rc) {
+  for (int64_t I = gtid(); I < nc; I += gstride()) {
+    float s = 0.0f;
+    for (int64_t m = mptr[I]; m < mptr[I + 1]; ++m) s += t[mem[m]];
+    rc[I] = s;
+  }
+}
+
+// prolongation z[i] += e[agg[i]]
+__global__ void k_ml_prolong(int64_t n, const int32_t* __restrict__ agg, const float* __restrict__ e,
+                             float* __restrict__ z) {
+  for (int64_t i = gtid(); i < n; i += gstride()) z[i] += e[agg[i]];
+}
+
+// ---- deterministic dot products: block partials, the last block finishes ---
+__device__ __forceinline__ double ml_warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+// NP block sums of vals[] into partial[p * gridDim + block]; the last block to
+// arrive (ticket after a fence) sums every column in block order into out[p]
+// and resets the ticket
+template <int NP>
+__device__ __forceinline__ void ml_reduce(double (&vals)[NP], double* __restrict__ partial,
+                                          unsigned* __restrict__ counter, double* __restrict__ out) {
+  __shared__ double sh[NP][32];
+  __shared__ bool last;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int p = 0; p < NP; ++p) {
+    const double s = ml_warp_sum(vals[p]);
+    if (lane == 0) sh[p][w] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+      const double s = ml_warp_sum(lane < nw ? sh[p][lane] : 0.0);
+      if (lane == 0) partial[p * gridDim.x + blockIdx.x] = s;
+    }
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+#pragma unroll
+  for (int p = 0; p < NP; ++p) {
+    double s = 0.0;
+    for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) s += partial[p * gridDim.x + b];
+    s = ml_warp_sum(s);
+    if (lane == 0) sh[p][w] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+      const double s = ml_warp_sum(lane < nw ? sh[p][lane] : 0.0);
+      if (lane == 0) out[p] = s;
+    }
+  }
+  if (threadIdx.x == 0) *counter = 0u;
+}
+
+// ---- K-cycle at one coarse level (device scalars ks[0..4]) ------------------
+// y = A x; out[0] = x . y, out[1] = x . r (and out[2] = x . w1 when W1)
+template <bool W1>
+__global__ void __launch_bounds__(kMlThreads) k_ml_kspmv(int64_t n, const int64_t* __restrict__ rp,
+                                                         const int32_t* __restrict__ ci, const float* __restrict__ a,
+                                                         const float* __restrict__ x, float* __restrict__ y,
+                                                         const float* __restrict__ r, const float* __restrict__ w1,
+                                                         double* __restrict__ partial, unsigned* __restrict__ counter,
+                                                         double* __restrict__ out) {
+  constexpr int NP = W1 ? 3 : 2;
+  double acc[NP] = {};
+  ML_ROW_LOOP(n) {
+    const int64_t rr = i < n ? i : n - 1;
+    const float ax = row_dot(rp, ci, a, x, rr, sub);
+    if (i < n && sub == 0) {
+      y[i] = ax;
+      const double xi = x[i];
+      acc[0] += xi * ax;
+      acc[1] += xi * r[i];
+      if (W1) acc[NP - 1] += xi * w1[i];
+    }
+  }
+  ml_reduce<NP>(acc, partial, counter, out);
+}
+
+// rt = r - (alpha1 / rho1) w1 (no step when rho1 is not positive)
+__global__ void k_ml_kstep1(int64_t n, const double* __restrict__ ks, const float* __restrict__ r,
+                            const float* __restrict__ w1, float* __restrict__ rt) {
+  const double rho1 = ks[0];
+  const float a = rho1 > 0.0 && isfinite(rho1) ? (float)(ks[1] / rho1) : 0.0f;
+  for (int64_t i = gtid(); i < n; i += gstride()) rt[i] = r[i] - a * w1[i];
+}
+// e = c1 v1 + c2 v2: rho1 = ks[0], alpha1 = ks[1], beta = ks[2] (v2.w2),
+// alpha2 = ks[3] (v2.rt), gamma = ks[4] (v2.w1)
+__global__ void k_ml_kcombine(int64_t n, const double* __restrict__ ks, const float* __restrict__ v1,
+                              const float* __restrict__ v2, float* __restrict__ e) {
+  const double rho1 = ks[0], a1 = ks[1], beta = ks[2], a2 = ks[3], gam = ks[4];
+  double c1 = 0.0, c2 = 0.0;
+  if (rho1 > 0.0 && isfinite(rho1)) {
+    c1 = a1 / rho1;
+    const double rho2 = beta - gam * gam / rho1;
+    if (rho2 > 1e-12 * beta && isfinite(rho2)) {
+      c2 = a2 / rho2;
+      c1 -= gam * a2 / (rho1 * rho2);
+    }
+  }
+  const float f1 = (float)c1, f2 = (float)c2;
+  for (int64_t i = gtid(); i < n; i += gstride()) e[i] = f1 * v1[i] + f2 * v2[i];
+}
+
+// ---- coarsest level: dense inverse (FP32 Gauss-Jordan, one block) -----------
+// D [n][2n] row-major: the matrix and the identity beside it
+__global__ void k_ml_dense_fill(int n, float* __restrict__ D) {
+  for (int64_t t = gtid(); t < (int64_t)n * 2 * n; t += gstride()) {
+    const int i = (int)(t / (2 * n)), j = (int)(t % (2 * n));
+    D[t] = j >= n ? (j - n == i ? 1.0f : 0.0f) : 0.0f;
+  }
+}
+__global__ void k_ml_dense_scatter(int n, const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                                   const double* __restrict__ v, float* __restrict__ D) {
+  for (int64_t i = gtid(); i < n; i += gstride())
+    for (int64_t k = rp[i]; k < rp[i + 1]; ++k) D[i * 2 * n + ci[k]] += (float)v[k];
+}
+// [A | I] -> [I | A^-1] with partial pivoting; a zero pivot sets *bad
+__global__ void __launch_bounds__(1024) k_ml_gauss_jordan(int n, float* __restrict__ D, int* __restrict__ bad) {
+  __shared__ float bv[32];
+  __shared__ int bi[32];
+  __shared__ int piv;
+  __shared__ float pinv;
+  const int m = 2 * n;
+  for (int k = 0; k < n; ++k) {
+    float best = -1.0f;
+    int bidx = k;
+    for (int i = k + threadIdx.x; i < n; i += blockDim.x) {
+      const float a = fabsf(D[(int64_t)i * m + k]);
+      if (a > best) best = a, bidx = i;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const float ob = __shfl_xor_sync(0xffffffffu, best, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bidx, o);
+      if (ob > best || (ob == best && oi < bidx)) best = ob, bidx = oi;
+    }
+    if ((threadIdx.x & 31) == 0) bv[threadIdx.x >> 5] = best, bi[threadIdx.x >> 5] = bidx;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      best = threadIdx.x < (blockDim.x >> 5) ? bv[threadIdx.x] : -1.0f;
+      bidx = threadIdx.x < (blockDim.x >> 5) ? bi[threadIdx.x] : k;
+      for (int o = 16; o > 0; o >>= 1) {
+        const float ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bidx, o);
+        if (ob > best || (ob == best && oi < bidx)) best = ob, bidx = oi;
+      }
+      if (threadIdx.x == 0) {
+        piv = bidx;
+        if (!(best > 0.0f)) *bad = 1;
+      }
+    }
+    __syncthreads();
+    const int p = piv;
+    if (p != k)
+      for (int j = threadIdx.x; j < m; j += blockDim.x) {
+        const float a = D[(int64_t)k * m + j];
+        D[(int64_t)k * m + j] = D[(int64_t)p * m + j];
+        D[(int64_t)p * m + j] = a;
+      }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const float d = D[(int64_t)k * m + k];
+      pinv = d != 0.0f ? 1.0f / d : 0.0f;
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < m; j += blockDim.x) D[(int64_t)k * m + j] *= pinv;
+    __syncthreads();
+    // eliminate column k from every other row (columns left of k are done)
+    for (int64_t t = threadIdx.x; t < (int64_t)n * m; t += blockDim.x) {
+      const int i = (int)(t / m), j = (int)(t % m);
+      if (i == k || j <= k) continue;
+      D[t] -= D[(int64_t)i * m + k] * D[(int64_t)k * m + j];
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+      if (i != k) D[(int64_t)i * m + k] = 0.0f;
+    __syncthreads();
+  }
+}
+// Inv [n][n] <- right half of D
+__global__ void k_ml_dense_extract(int n, const float* __restrict__ D, float* __restrict__ Inv) {
+  for (int64_t t = gtid(); t < (int64_t)n * n; t += gstride()) {
+    const int i = (int)(t / n), j = (int)(t % n);
+    Inv[t] = D[(int64_t)i * 2 * n + n + j];
+  }
+}
+// e = Inv r, one warp per row
+__global__ void k_ml_dense_apply(int n, const float* __restrict__ Inv, const float* __restrict__ r,
+                                 float* __restrict__ e) {
+  const int64_t row = gtid() >> 5;
+  const int lane = threadIdx.x & 31;
+  if (row >= n) return;
+  float s = 0.0f;
+  for (int j = lane; j < n; j += 32) s = fmaf(Inv[row * n + j], r[j], s);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) e[row] = s;
+}
+
+// ---- power iteration for the smoothing weight -------------------------------
+__global__ void __launch_bounds__(kMlThreads) k_ml_power_ax(int64_t n, const int64_t* __restrict__ rp,
+                                                            const int32_t* __restrict__ ci,
+                                                            const float* __restrict__ a, const float* __restrict__ x,
+                                                            float* __restrict__ t) {
+  ML_ROW_LOOP(n) {
+    const int64_t r = i < n ? i : n - 1;
+    const float ax = row_dot(rp, ci, a, x, r, sub);
+    if (i < n && sub == 0) t[i] = ax;
+  }
+}
+// y = S t (S = M, or D^-1 when m is null); out[0] = y . y
+__global__ void __launch_bounds__(kMlThreads) k_ml_power_s(int64_t n, const int64_t* __restrict__ rp,
+                                                           const int32_t* __restrict__ ci, const float* __restrict__ m,
+                                                           const float* __restrict__ dinv, const float* __restrict__ t,
+                                                           float* __restrict__ y, double* __restrict__ partial,
+                                                           unsigned* __restrict__ counter, double* __restrict__ out) {
+  double acc[1] = {0.0};
+  ML_ROW_LOOP(n) {
+    const int64_t r = i < n ? i : n - 1;
+    const float st = m ? row_dot(rp, ci, m, t, r, sub) : dinv[r] * t[r];
+    if (i < n && sub == 0) {
+      y[i] = st;
+      acc[0] += (double)st * st;
+    }
+  }
+  ml_reduce<1>(acc, partial, counter, out);
+}
+__global__ void k_ml_scale(int64_t n, const double* __restrict__ ks, const float* __restrict__ y,
+                           float* __restrict__ x) {
+  const double nrm = sqrt(ks[0]);
+  const float s = nrm > 0.0 ? (float)(1.0 / nrm) : 0.0f;
+  for (int64_t i = gtid(); i < n; i += gstride()) x[i] = s * y[i];
+}
+// a positive, unit-norm-ish start vector
+__global__ void k_ml_seed(int64_t n, float* __restrict__ x) {
+  const float s = (float)(1.0 / sqrt((double)n));
+  for (int64_t i = gtid(); i < n; i += gstride()) {
+    uint32_t h = (uint32_t)i * 2654435761u + 12345u;
+    h ^= h >> 16;
+    h *= 0x7feb352du;
+    h ^= h >> 15;
+    x[i] = s * (0.5f + (float)(h & 0xffffu) / 65536.0f);
+  }
+}
+
+// ---- outer flexible CG (FP64) ----------------------------------------------
+// scalars os[]: [0] r.r, [1] p.q of the previous step, [2] beta, [3] alpha,
+// [4] first-step flag, [5] stop threshold on r.r, [6] breakdown count,
+// [7] steps taken before convergence;
+// dots[]: [0] p.q, [1] p.r, [2] z.q_old
+__global__ void k_mlo_tof(int64_t n, const double* __restrict__ r, float* __restrict__ rf) {
+  for (int64_t i = gtid(); i < n; i += gstride()) rf[i] = (float)r[i];
+}
+__global__ void __launch_bounds__(kMlThreads) k_mlo_zq(int64_t n, const float* __restrict__ z,
+                                                       const double* __restrict__ q, double* __restrict__ partial,
+                                                       unsigned* __restrict__ counter, double* __restrict__ out) {
+  double acc[1] = {0.0};
+  for (int64_t i = gtid(); i < n; i += gstride()) acc[0] += (double)z[i] * q[i];
+  ml_reduce<1>(acc, partial, counter, out);
+}
+// beta = -(z . q_old) / (p . q)_old; 0 on the first step and once converged
+__global__ void k_mlo_beta(double* __restrict__ os, const double* __restrict__ zq) {
+  const bool frozen = os[5] > 0.0 && os[0] <= os[5];
+  if (os[4] != 0.0 || frozen) {
+    os[2] = 0.0;
+  } else {
+    const double b = -zq[0] / os[1];
+    os[2] = isfinite(b) ? b : 0.0;
+  }
+}
+__global__ void k_mlo_pupdate(int64_t n, const float* __restrict__ z, double* __restrict__ p,
+                              const double* __restrict__ os) {
+  const double b = os[2];
+  const bool first = os[4] != 0.0;
+  for (int64_t i = gtid(); i < n; i += gstride()) p[i] = (double)z[i] + (first ? 0.0 : b * p[i]);
+}
+// q = A p; dots[0] = p . q, dots[1] = p . r
+__global__ void __launch_bounds__(kMlThreads) k_mlo_spmv(int64_t n, const int64_t* __restrict__ rp,
+                                                         const int32_t* __restrict__ ci, const double* __restrict__ v,
+                                                         const double* __restrict__ p, double* __restrict__ q,
+                                                         const double* __restrict__ r, double* __restrict__ partial,
+                                                         unsigned* __restrict__ counter, double* __restrict__ dots) {
+  double acc[2] = {};
+  ML_ROW_LOOP(n) {
+    const int64_t rr = i < n ? i : n - 1;
+    double s = 0.0;
+    for (int64_t k = rp[rr] + sub; k < rp[rr + 1]; k += kTpr) s = fma(v[k], p[ci[k]], s);
+#pragma unroll
+    for (int o = kTpr / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, kTpr);
+    if (i < n && sub == 0) {
+      q[i] = s;
+      acc[0] += p[i] * s;
+      acc[1] += p[i] * r[i];
+    }
+  }
+  ml_reduce<2>(acc, partial, counter, dots);
+}
+// alpha = (p . r) / (p . q); zero once converged; a non-positive p . q before
+// convergence counts as a breakdown
+__global__ void k_mlo_alpha(double* __restrict__ os, const double* __restrict__ dots) {
+  const bool frozen = os[5] > 0.0 && os[0] <= os[5];
+  const double pq = dots[0];
+  double a = pq > 0.0 ? dots[1] / pq : 0.0;
+  if (!(pq > 0.0) || !isfinite(a)) {
+    if (!frozen) os[6] += 1.0;
+    a = 0.0;
+  }
+  os[3] = frozen ? 0.0 : a;
+  if (!frozen && pq > 0.0) os[1] = pq;
+  if (!frozen) os[7] += 1.0;  // steps that moved the iterate
+  os[4] = 0.0;
+}
+// x += alpha p; r -= alpha q; os[0] = r . r
+__global__ void __launch_bounds__(kMlThreads) k_mlo_axpy(int64_t n, double* __restrict__ x, const double* __restrict__ p,
+                                                         double* __restrict__ r, const double* __restrict__ q,
+                                                         double* __restrict__ partial, unsigned* __restrict__ counter,
+                                                         double* __restrict__ os) {
+  const double a = os[3];
+  double acc[1] = {0.0};
+  for (int64_t i = gtid(); i < n; i += gstride()) {
+    x[i] += a * p[i];
+    const double ri = r[i] - a * q[i];
+    r[i] = ri;
+    acc[0] += ri * ri;
+  }
+  ml_reduce<1>(acc, partial, counter, os);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+struct MlLevel {
+  int64_t n = 0, nnz = 0;
+  const int64_t* rp = nullptr;
+  const int32_t* ci = nullptr;
+  const double* vd = nullptr;
+  DBuf<int64_t> own_rp;
+  DBuf<int32_t> own_ci;
+  DBuf<double> own_vd;
+  DBuf<float> vf, dinv, msm;  // FP32 values, inverse diagonal, learned smoother (level 0)
+  DBuf<int32_t> agg;          // row -> next level's row
+  DBuf<int64_t> mptr;         // members of the next level's rows
+  DBuf<int32_t> mem;
+  DBuf<float> z, t, z2, b;    // cycle vectors
+  DBuf<float> v1, v2, w1, w2, rt, e;  // K-cycle vectors (as a coarse level)
+  DBuf<float> inv;            // dense inverse (coarsest level)
+  float omega = 0.6f;
+};
+
+struct MlState {
+  std::vector<MlLevel> lv;
+  DBuf<double> partial, ks;   // reduction partials; device scalars (8 per level, then the outer FCG's)
+  DBuf<unsigned> counter;     // reduction tickets
+  bool learned = false;
+  bool ready = false;
+  int klevels = 1 << 20;      // coarse levels 1..klevels solved by K-cycle, deeper ones by V-cycle
+};
+
+namespace {
+
+constexpr int kCounters = 64;
+
+unsigned grid_n(int64_t n) {
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + kMlThreads - 1) / kMlThreads, kMlBlocks));
+}
+unsigned grid_rows(int64_t n) {
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>((n * kTpr + kMlThreads - 1) / kMlThreads, 4 * kMlBlocks));
+}
+
+template <class T>
+int exclusive_scan(nalu_ctx* ctx, const T* in, T* out, int64_t n) {
+  size_t tmp = 0;
+  NALU_CUDA(ctx, cub::DeviceScan::ExclusiveSum(nullptr, tmp, in, out, (int)n, ctx->stream));
+  DBuf<unsigned char> t;
+  NALU_CUDA(ctx, t.alloc((int64_t)tmp + 1));
+  NALU_CUDA(ctx, cub::DeviceScan::ExclusiveSum(t.p, tmp, in, out, (int)n, ctx->stream));
+  NALU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));  // t is freed on return
+  return NALU_OK;
+}
+template <class T>
+T read_one(nalu_ctx* ctx, const T* d) {
+  T h{};
+  cudaMemcpyAsync(&h, d, sizeof(T), cudaMemcpyDeviceToHost, ctx->stream);
+  cudaStreamSynchronize(ctx->stream);
+  return h;
+}
+
+// one pairwise pass on (n, rp, ci, v): agg [n] -> [0, *nc)
+int pairwise_pass(nalu_ctx* ctx, int64_t n, const int64_t* rp, const int32_t* ci, const double* v, int32_t* agg,
+                  int64_t* nc_out) {
+  cudaStream_t s = ctx->stream;
+  DBuf<double> smax, diag;
+  DBuf<int32_t> partner, choice, leader, flag, id;
+  NALU_CUDA(ctx, smax.alloc(n));
+  NALU_CUDA(ctx, diag.alloc(n));
+  NALU_CUDA(ctx, partner.alloc(n));
+  NALU_CUDA(ctx, choice.alloc(n));
+  NALU_CUDA(ctx, leader.alloc(n));
+  NALU_CUDA(ctx, flag.alloc(n + 1));
+  NALU_CUDA(ctx, id.alloc(n + 1));
+  const unsigned g = grid_n(n);
+  k_ml_smax<<<g, kMlThreads, 0, s>>>(n, rp, ci, v, smax.p, diag.p);
+  k_ml_fill_i32<<<g, kMlThreads, 0, s>>>(n, partner.p, -1);
+  for (int r = 0; r < kMatchRounds; ++r) {
+    k_ml_choose<<<g, kMlThreads, 0, s>>>(n, rp, ci, v, smax.p, diag.p, partner.p, r, choice.p);
+    k_ml_match<<<g, kMlThreads, 0, s>>>(n, choice.p, partner.p);
+  }
+  k_ml_attach<<<g, kMlThreads, 0, s>>>(n, rp, ci, v, smax.p, partner.p, leader.p);
+  k_ml_flag_leaders<<<g, kMlThreads, 0, s>>>(n, leader.p, flag.p);
+  NALU_CUDA(ctx, cudaMemsetAsync(flag.p + n, 0, sizeof(int32_t), s));
+  int rc = exclusive_scan<int32_t>(ctx, flag.p, id.p, n + 1);
+  if (rc) return rc;
+  k_ml_assign<<<g, kMlThreads, 0, s>>>(n, leader.p, id.p, agg);
+  ctx->launches += 6 + 2 * kMatchRounds;
+  *nc_out = read_one(ctx, id.p + n);
+  return cuda_check(ctx, cudaGetLastError(), "pairwise aggregation");
+}
+
+// members of each aggregate, in row order: mptr [nc+1], mem [n]
+int build_members(nalu_ctx* ctx, int64_t n, int64_t nc, const int32_t* agg, DBuf<int64_t>& mptr, DBuf<int32_t>& mem) {
+  cudaStream_t s = ctx->stream;
+  DBuf<int32_t> keys_out, iota;
+  NALU_CUDA(ctx, keys_out.alloc(n));
+  NALU_CUDA(ctx, iota.alloc(n));
+  NALU_CUDA(ctx, mem.alloc(n));
+  NALU_CUDA(ctx, mptr.alloc(nc + 1));
+  k_ml_iota<<<grid_n(n), kMlThreads, 0, s>>>(n, iota.p);
+  size_t tmp = 0;
+  NALU_CUDA(ctx, cub::DeviceRadixSort::SortPairs(nullptr, tmp, agg, keys_out.p, iota.p, mem.p, (int)n, 0, 32, s));
+  DBuf<unsigned char> t;
+  NALU_CUDA(ctx, t.alloc((int64_t)tmp + 1));
+  NALU_CUDA(ctx, cub::DeviceRadixSort::SortPairs(t.p, tmp, agg, keys_out.p, iota.p, mem.p, (int)n, 0, 32, s));
+  k_ml_member_ptr<<<grid_n(n), kMlThreads, 0, s>>>(n, nc, keys_out.p, mptr.p);
+  ctx->launches += 2;
+  NALU_CUDA(ctx, cudaStreamSynchronize(s));  // temporaries are freed on return
+  return cuda_check(ctx, cudaGetLastError(), "aggregate members");
+}
+
+// Galerkin product of (n, rp, ci, v) for the aggregation agg -> coarse CRS
+int galerkin(nalu_ctx* ctx, const int64_t* rp, const int32_t* ci, const double* v, const int32_t* agg, int64_t nc,
+             const int64_t* mptr, const int32_t* mem, DBuf<int64_t>& crp, DBuf<int32_t>& cci, DBuf<double>& cv,
+             int64_t* cnnz) {
+  cudaStream_t s = ctx->stream;
+  DBuf<int64_t> cnt;
+  DBuf<int> over;
+  NALU_CUDA(ctx, cnt.alloc(nc + 1));
+  NALU_CUDA(ctx, crp.alloc(nc + 1));
+  NALU_CUDA(ctx, over.alloc(1));
+  NALU_CUDA(ctx, cudaMemsetAsync(over.p, 0, sizeof(int), s));
+  NALU_CUDA(ctx, cudaMemsetAsync(cnt.p + nc, 0, sizeof(int64_t), s));
+  const size_t smem = sizeof(GalSmem) * kGalWarps;
+  NALU_CUDA(ctx, cudaFuncSetAttribute(k_ml_galerkin<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  NALU_CUDA(ctx, cudaFuncSetAttribute(k_ml_galerkin<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>((nc + kGalWarps - 1) / kGalWarps, 4 * kMlBlocks));
+  k_ml_galerkin<true><<<g, 32 * kGalWarps, smem, s>>>(nc, mptr, mem, rp, ci, v, agg, nullptr, cnt.p, nullptr, nullptr,
+                                                      over.p);
+  int rc = exclusive_scan<int64_t>(ctx, cnt.p, crp.p, nc + 1);
+  if (rc) return rc;
+  if (read_one(ctx, over.p) != 0) return set_error(ctx, NALU_ERR_CAPACITY, "multilevel: coarse row too long");
+  *cnnz = read_one(ctx, crp.p + nc);
+  NALU_CUDA(ctx, cci.alloc(std::max<int64_t>(*cnnz, 1)));
+  NALU_CUDA(ctx, cv.alloc(std::max<int64_t>(*cnnz, 1)));
+  k_ml_galerkin<false><<<g, 32 * kGalWarps, smem, s>>>(nc, mptr, mem, rp, ci, v, agg, crp.p, nullptr, cci.p, cv.p,
+                                                       over.p);
+  ctx->launches += 2;
+  NALU_CUDA(ctx, cudaStreamSynchronize(s));
+  return cuda_check(ctx, cudaGetLastError(), "Galerkin product");
+}
+
+// lambda_max of S A (S = D^-1, or the learned M) by power iteration
+float power_lambda(nalu_ctx* ctx, MlState& M, MlLevel& L, const float* m, int iters) {
+  cudaStream_t s = ctx->stream;
+  const int64_t n = L.n;
+  float *x = L.z.p, *t = L.t.p, *y = L.z2.p;
+  k_ml_seed<<<grid_n(n), kMlThreads, 0, s>>>(n, x);
+  for (int it = 0; it < iters; ++it) {
+    k_ml_power_ax<<<grid_rows(n), kMlThreads, 0, s>>>(n, L.rp, L.ci, L.vf.p, x, t);
+    k_ml_power_s<<<grid_rows(n), kMlThreads, 0, s>>>(n, L.rp, L.ci, m, L.dinv.p, t, y, M.partial.p, M.counter.p,
+                                                      M.ks.p);
+    k_ml_scale<<<grid_n(n), kMlThreads, 0, s>>>(n, M.ks.p, y, x);
+    ctx->launches += 3;
+  }
+  // x was unit before the last product: lambda ~ ||S A x||
+  const double yy = read_one(ctx, M.ks.p);
+  return (float)std::sqrt(std::max(yy, 0.0));
+}
+
+int alloc_level_vectors(nalu_ctx* ctx, MlLevel& L, bool kcycle) {
+  const int64_t n = std::max<int64_t>(L.n, 1);
+  for (DBuf<float>* b : {&L.z, &L.t, &L.z2, &L.b}) NALU_CUDA(ctx, b->alloc(n));
+  if (kcycle)
+    for (DBuf<float>* b : {&L.v1, &L.v2, &L.w1, &L.w2, &L.rt, &L.e}) NALU_CUDA(ctx, b->alloc(n));
+  return NALU_OK;
+}
+
+}  // namespace
+
+// Build the hierarchy for the current scalar matrix (for the learned smoother,
+// learned_prepare has run on it).
+int ml_setup(nalu_ctx* ctx, bool learned) {
+  if (!ctx->ml) ctx->ml = new MlState();
+  MlState& M = *ctx->ml;
+  M.lv.clear();
+  M.ready = false;
+  M.learned = learned;
+  cudaStream_t s = ctx->stream;
+  NALU_CUDA(ctx, M.partial.alloc(3 * 4 * kMlBlocks + 64));
+  NALU_CUDA(ctx, M.ks.alloc(8 * (kMaxLevels + 2)));
+  NALU_CUDA(ctx, M.counter.alloc(kCounters));
+  NALU_CUDA(ctx, cudaMemsetAsync(M.counter.p, 0, sizeof(unsigned) * kCounters, s));
+  NALU_CUDA(ctx, cudaMemsetAsync(M.ks.p, 0, sizeof(double) * 8 * (kMaxLevels + 2), s));
+  M.lv.reserve(kMaxLevels + 1);
+  M.lv.emplace_back();
+  {
+    MlLevel& L0 = M.lv[0];
+    L0.n = ctx->n_rows;
+    L0.nnz = ctx->nnz;
+    L0.rp = ctx->d_rowptr.p;
+    L0.ci = ctx->d_colind.p;
+    L0.vd = ctx->d_values.p;
+  }
+  int rc = NALU_OK;
+  // levels of up to three pairwise passes each, down to kCoarsest rows
+  while ((int)M.lv.size() < kMaxLevels && M.lv.back().n > kCoarsest) {
+    MlLevel& F = M.lv.back();
+    NALU_CUDA(ctx, F.agg.alloc(F.n));
+    k_ml_iota<<<grid_n(F.n), kMlThreads, 0, s>>>(F.n, F.agg.p);
+    ctx->launches++;
+    int64_t n = F.n, nnz = F.nnz;
+    const int64_t* rp = F.rp;
+    const int32_t* ci = F.ci;
+    const double* v = F.vd;
+    DBuf<int64_t> crp;
+    DBuf<int32_t> cci;
+    DBuf<double> cv;
+    for (int pass = 0; pass < kPassesPerLevel; ++pass) {
+      DBuf<int32_t> agg;
+      NALU_CUDA(ctx, agg.alloc(n));
+      int64_t nc = 0;
+      if ((rc = pairwise_pass(ctx, n, rp, ci, v, agg.p, &nc))) return rc;
+      if (nc >= n) break;  // nothing left to pair
+      DBuf<int64_t> mptr;
+      DBuf<int32_t> mem;
+      if ((rc = build_members(ctx, n, nc, agg.p, mptr, mem))) return rc;
+      DBuf<int64_t> nrp;
+      DBuf<int32_t> nci;
+      DBuf<double> nv;
+      int64_t cnnz = 0;
+      if ((rc = galerkin(ctx, rp, ci, v, agg.p, nc, mptr.p, mem.p, nrp, nci, nv, &cnnz))) return rc;
+      k_ml_compose<<<grid_n(F.n), kMlThreads, 0, s>>>(F.n, F.agg.p, agg.p);
+      ctx->launches++;
+      NALU_CUDA(ctx, cudaStreamSynchronize(s));
+      crp = std::move(nrp);
+      cci = std::move(nci);
+      cv = std::move(nv);
+      rp = crp.p;
+      ci = cci.p;
+      v = cv.p;
+      n = nc;
+      nnz = cnnz;
+      if (n <= kCoarsest) break;
+    }
+    if (n >= F.n) break;  // no coarsening: F is the coarsest level
+    if ((rc = build_members(ctx, F.n, n, F.agg.p, F.mptr, F.mem))) return rc;
+    M.lv.emplace_back();
+    MlLevel& C = M.lv.back();
+    C.n = n;
+    C.nnz = nnz;
+    C.own_rp = std::move(crp);
+    C.own_ci = std::move(cci);
+    C.own_vd = std::move(cv);
+    C.rp = C.own_rp.p;
+    C.ci = C.own_ci.p;
+    C.vd = C.own_vd.p;
+  }
+  const int nl = (int)M.lv.size();
+  if (M.lv.back().n > kDenseMax)
+    return set_error(ctx, NALU_ERR_CAPACITY, "multilevel: coarsest level above 1024 rows (too few strong couplings)");
+  // FP32 copies, vectors
+  for (int l = 0; l < nl; ++l) {
+    MlLevel& L = M.lv[l];
+    NALU_CUDA(ctx, L.vf.alloc(std::max<int64_t>(L.nnz, 1)));
+    NALU_CUDA(ctx, L.dinv.alloc(std::max<int64_t>(L.n, 1)));
+    k_ml_prep<<<grid_n(L.n), kMlThreads, 0, s>>>(L.n, L.rp, L.ci, L.vd, L.vf.p, L.dinv.p);
+    ctx->launches++;
+    if ((rc = alloc_level_vectors(ctx, L, l > 0 && l < nl - 1))) return rc;
+  }
+  if (learned) {
+    MlLevel& L0 = M.lv[0];
+    NALU_CUDA(ctx, L0.msm.alloc(std::max<int64_t>(L0.nnz, 1)));
+    k_ml_sell_to_crs<<<grid_n(L0.n), kMlThreads, 0, s>>>(L0.n, L0.rp, ctx->sw.sell.ptr.p, ctx->learned.wsell.p,
+                                                         L0.msm.p);
+    ctx->launches++;
+  }
+  // smoothing weights
+  for (int l = 0; l < nl - 1; ++l) {
+    MlLevel& L = M.lv[l];
+    const float lam = power_lambda(ctx, M, L, (l == 0 && learned) ? L.msm.p : nullptr, 12);
+    L.omega = lam > 0.0f && std::isfinite(lam) ? 4.0f / (3.0f * lam) : 0.6f;
+  }
+  {
+    // coarsest level: dense inverse
+    MlLevel& C = M.lv.back();
+    const int nc = (int)C.n;
+    DBuf<float> D;
+    DBuf<int> bad;
+    NALU_CUDA(ctx, D.alloc((int64_t)nc * 2 * nc));
+    NALU_CUDA(ctx, C.inv.alloc((int64_t)nc * nc));
+    NALU_CUDA(ctx, bad.alloc(1));
+    NALU_CUDA(ctx, cudaMemsetAsync(bad.p, 0, sizeof(int), s));
+    k_ml_dense_fill<<<grid_n((int64_t)nc * 2 * nc), kMlThreads, 0, s>>>(nc, D.p);
+    k_ml_dense_scatter<<<grid_n(nc), kMlThreads, 0, s>>>(nc, C.rp, C.ci, C.vd, D.p);
+    k_ml_gauss_jordan<<<1, 1024, 0, s>>>(nc, D.p, bad.p);
+    k_ml_dense_extract<<<grid_n((int64_t)nc * nc), kMlThreads, 0, s>>>(nc, D.p, C.inv.p);
+    ctx->launches += 4;
+    if (read_one(ctx, bad.p)) return set_error(ctx, NALU_ERR_NONFINITE, "multilevel: singular coarsest matrix");
+  }
+  NALU_CUDA(ctx, cudaStreamSynchronize(s));
+  M.ready = true;
+  return cuda_check(ctx, cudaGetLastError(), "multilevel set-up");
+}
+
+namespace {
+
+void cycle(nalu_ctx* ctx, MlState& M, int l, const float* b, float* z, int* site);
+
+// e ~ A_l^-1 r at a coarse level l: the dense inverse at the coarsest level,
+// else a K-cycle (two flexible CG steps preconditioned by the cycle of level
+// l) or, below the K-cycle levels, one cycle
+void coarse_solve(nalu_ctx* ctx, MlState& M, int l, const float* r, float* e, int* site) {
+  cudaStream_t s = ctx->stream;
+  MlLevel& L = M.lv[l];
+  const int nl = (int)M.lv.size();
+  if (l == nl - 1) {
+    k_ml_dense_apply<<<(unsigned)((L.n * 32 + kMlThreads - 1) / kMlThreads), kMlThreads, 0, s>>>((int)L.n, L.inv.p, r,
+                                                                                                  e);
+    ctx->launches++;
+    return;
+  }
+  if (l > M.klevels) {
+    cycle(ctx, M, l, r, e, site);
+    return;
+  }
+  double* ks = M.ks.p + 8 * l;
+  const unsigned gr = grid_rows(L.n), gn = grid_n(L.n);
+  cycle(ctx, M, l, r, L.v1.p, site);
+  const int c1 = (*site)++ % kCounters;
+  k_ml_kspmv<false><<<gr, kMlThreads, 0, s>>>(L.n, L.rp, L.ci, L.vf.p, L.v1.p, L.w1.p, r, nullptr, M.partial.p,
+                                               M.counter.p + c1, ks);  // ks[0] rho1, ks[1] alpha1
+  k_ml_kstep1<<<gn, kMlThreads, 0, s>>>(L.n, ks, r, L.w1.p, L.rt.p);
+  cycle(ctx, M, l, L.rt.p, L.v2.p, site);
+  const int c2 = (*site)++ % kCounters;
+  k_ml_kspmv<true><<<gr, kMlThreads, 0, s>>>(L.n, L.rp, L.ci, L.vf.p, L.v2.p, L.w2.p, L.rt.p, L.w1.p, M.partial.p,
+                                              M.counter.p + c2, ks + 2);  // ks[2] beta, ks[3] alpha2, ks[4] gamma
+  k_ml_kcombine<<<gn, kMlThreads, 0, s>>>(L.n, ks, L.v1.p, L.v2.p, e);
+  ctx->launches += 4;
+}
+
+// z = B_l b: the cycle at level l from a zero guess (l below the coarsest)
+void cycle(nalu_ctx* ctx, MlState& M, int l, const float* b, float* z, int* site) {
+  cudaStream_t s = ctx->stream;
+  MlLevel& L = M.lv[l];
+  MlLevel& C = M.lv[l + 1];
+  const unsigned gr = grid_rows(L.n), gn = grid_n(L.n), gc = grid_n(C.n);
+  const bool learned = l == 0 && M.learned;
+  // pre-smoothing from zero, then the residual
+  if (learned) {
+    k_ml_mstep<<<gr, kMlThreads, 0, s>>>(L.n, L.rp, L.ci, L.msm.p, L.omega, b, nullptr, z);
+    k_ml_residual<<<gr, kMlThreads, 0, s>>>(L.n, L.rp, L.ci, L.vf.p, z, b, L.t.p);
+    ctx->launches += 2;
+  } else {
+    k_ml_jac0_residual<<<gr, kMlThreads, 0, s>>>(L.n, L.rp, L.ci, L.vf.p, L.dinv.p, L.omega, b, z, L.t.p);
+    ctx->launches++;
+  }
+  // coarse correction
+  float* ec = (l + 1 == (int)M.lv.size() - 1) ? C.z.p : C.e.p;
+  k_ml_restrict<<<gc, kMlThreads, 0, s>>>(C.n, L.mptr.p, L.mem.p, L.t.p, C.b.p);
+  coarse_solve(ctx, M, l + 1, C.b.p, ec, site);
+  k_ml_prolong<<<gn, kMlThreads, 0, s>>>(L.n, L.agg.p, ec, z);
+  ctx->launches += 2;
+  // post-smoothing
+  if (learned) {
+    k_ml_residual<<<gr, kMlThreads, 0, s>>>(L.n, L.rp, L.ci, L.vf.p, z, b, L.t.p);
+    k_ml_mstep<<<gr, kMlThreads, 0, s>>>(L.n, L.rp, L.ci, L.msm.p, L.omega, L.t.p, z, L.z2.p);
+  } else {
+    k_ml_jac_step<<<gr, kMlThreads, 0, s>>>(L.n, L.rp, L.ci, L.vf.p, L.dinv.p, L.omega, b, z, L.z2.p);
+  }
+  cudaMemcpyAsync(z, L.z2.p, sizeof(float) * L.n, cudaMemcpyDeviceToDevice, s);
+  ctx->launches += learned ? 2 : 1;
+}
+
+}  // namespace
+
+// Flexible CG preconditioned by the multilevel cycle, on the residual r (FP64,
+// updated in place) for the correction x (FP64, from zero), to
+// ||r|| <= rtol r0norm.  One step is captured as a CUDA graph and replayed;
+// convergence is read every check_every steps (at most 10).
+int fcg_multilevel(nalu_ctx* ctx, double* x, double* r, double rtol, double r0norm, int max_it, int check_every,
+                   int klevels, int* iters_out) {
+  *iters_out = 0;
+  if (!ctx->ml || !ctx->ml->ready || ctx->ml->lv.empty())
+    return set_error(ctx, NALU_ERR_STATE, "multilevel hierarchy not built");
+  MlState& M = *ctx->ml;
+  M.klevels = klevels == 0 ? (1 << 20) : (klevels < 0 ? 0 : klevels);
+  const int64_t n = ctx->n_rows;
+  cudaStream_t s = ctx->stream;
+  DBuf<double> p, q;
+  DBuf<float> rf;
+  NALU_CUDA(ctx, p.alloc(n));
+  NALU_CUDA(ctx, q.alloc(n));
+  NALU_CUDA(ctx, rf.alloc(n));
+  NALU_CUDA(ctx, cudaMemsetAsync(x, 0, sizeof(double) * n, s));
+  NALU_CUDA(ctx, cudaMemsetAsync(p.p, 0, sizeof(double) * n, s));
+  NALU_CUDA(ctx, cudaMemsetAsync(q.p, 0, sizeof(double) * n, s));
+  double* os = M.ks.p + 8 * kMaxLevels;  // outer scalars
+  double* dots = os + 8;
+  const double stop = rtol * r0norm;
+  {
+    const double init[8] = {r0norm * r0norm, 1.0, 0.0, 0.0, 1.0, stop * stop, 0.0, 0.0};
+    NALU_CUDA(ctx, cudaMemcpyAsync(os, init, sizeof(init), cudaMemcpyHostToDevice, s));
+    NALU_CUDA(ctx, cudaStreamSynchronize(s));
+  }
+  MlLevel& L0 = M.lv[0];
+  auto step = [&]() {
+    int site = 0;
+    k_mlo_tof<<<grid_n(n), kMlThreads, 0, s>>>(n, r, rf.p);
+    if (M.lv.size() == 1) coarse_solve(ctx, M, 0, rf.p, L0.z.p, &site);  // one level: the dense inverse
+    else cycle(ctx, M, 0, rf.p, L0.z.p, &site);
+    const int c0 = site++ % kCounters, c1 = site++ % kCounters, c2 = site++ % kCounters;
+    k_mlo_zq<<<grid_n(n), kMlThreads, 0, s>>>(n, L0.z.p, q.p, M.partial.p, M.counter.p + c0, dots + 2);
+    k_mlo_beta<<<1, 1, 0, s>>>(os, dots + 2);
+    k_mlo_pupdate<<<grid_n(n), kMlThreads, 0, s>>>(n, L0.z.p, p.p, os);
+    k_mlo_spmv<<<grid_rows(n), kMlThreads, 0, s>>>(n, L0.rp, L0.ci, L0.vd, p.p, q.p, r, M.partial.p,
+                                                   M.counter.p + c1, dots);
+    k_mlo_alpha<<<1, 1, 0, s>>>(os, dots);
+    k_mlo_axpy<<<grid_n(n), kMlThreads, 0, s>>>(n, x, p.p, r, q.p, M.partial.p, M.counter.p + c2, os);
+    ctx->launches += 7;
+  };
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  NALU_CUDA(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  step();
+  cudaError_t ce = cudaStreamEndCapture(s, &graph);
+  if (ce != cudaSuccess) return cuda_check(ctx, ce, "capture multilevel FCG step");
+  ce = cudaGraphInstantiate(&exec, graph, 0);
+  if (ce != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    return cuda_check(ctx, ce, "instantiate multilevel FCG step");
+  }
+  const int every = std::max(1, check_every > 0 ? std::min(check_every, 10) : 5);
+  int it = 0, rc = NALU_OK;
+  bool converged = false;
+  while (it < max_it) {
+    const int chunk = std::min(every, max_it - it);
+    for (int k = 0; k < chunk; ++k) cudaGraphLaunch(exec, s);
+    it += chunk;
+    double h[8];
+    cudaMemcpyAsync(h, os, sizeof(h), cudaMemcpyDeviceToHost, s);
+    const cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+      rc = cuda_check(ctx, e, "multilevel FCG");
+      break;
+    }
+    if (h[6] != 0.0 || !std::isfinite(h[0])) {
+      rc = set_error(ctx, NALU_ERR_NONFINITE, "multilevel FCG breakdown (non-positive or non-finite step)");
+      break;
+    }
+    if (std::sqrt(h[0]) <= stop) {
+      converged = true;
+      break;
+    }
+  }
+  cudaGraphExecDestroy(exec);
+  cudaGraphDestroy(graph);
+  if (rc == NALU_OK && !converged) rc = NALU_ERR_NOT_CONVERGED;
+  *iters_out = (int)read_one(ctx, os + 7);
+  return rc;
+}
+
+void ml_free(nalu_ctx* ctx) {
+  delete ctx->ml;
+  ctx->ml = nullptr;
+}
+
+int ml_levels(const nalu_ctx* ctx, int max_levels, int64_t* rows, int64_t* nnz) {
+  if (!ctx->ml || !ctx->ml->ready) return 0;
+  const int nl = (int)ctx->ml->lv.size();
+  for (int l = 0; l < nl && l < max_levels; ++l) {
+    if (rows) rows[l] = ctx->ml->lv[l].n;
+    if (nnz) nnz[l] = ctx->ml->lv[l].nnz;
+  }
+  return nl;
+}
+
+}  // namespace nalu_gb300
