@@ -13,7 +13,8 @@
 //     edge's symmetric strength -a_ij / sqrt(a_ii a_jj) in half-octave bins,
 //     ties within a bin broken by a per-round hash of the edge.  Mutual
 //     proposals pair up.  Unmatched rows then join the pair of their strongest
-//     matched strong neighbour, else stay singletons (identity rows always do);
+//     matched strong neighbour (at most two per matched row), else stay
+//     singletons (identity rows always do);
 //   * coarse operators: Galerkin A_c = P^T A P for the piecewise-constant P of
 //     each pass, one warp per coarse row: the member rows' entries are
 //     gathered into shared memory, their distinct coarse columns found with a
@@ -53,9 +54,10 @@ constexpr int kMaxLevels = 12;
 constexpr int64_t kCoarsest = 512;    // coarsen until at most this many rows
 constexpr int64_t kDenseMax = 1024;   // largest coarsest level inverted densely
 constexpr int kGalWarps = 4;          // warps per block of the Galerkin kernels
-constexpr int kGalList = 1024;        // gathered entries per coarse row (at most)
-constexpr int kGalHash = 512;         // hash slots per warp
-constexpr int kGalUnique = 256;       // distinct coarse columns per row (at most)
+constexpr int kGalList = 2048;        // gathered entries per coarse row (at most)
+constexpr int kGalHash = 1024;        // hash slots per warp (a power of two, 2^10)
+constexpr int kGalUnique = 512;       // distinct coarse columns per row (at most)
+constexpr int kMaxAttach = 2;         // unmatched rows a matched row takes into its pair (at most)
 constexpr int kTpr = 4;               // threads per row of the CRS kernels
 
 __device__ __forceinline__ uint64_t d2u_bits(double d) { return (uint64_t)__double_as_longlong(d); }
@@ -137,19 +139,14 @@ __global__ void k_ml_match(int64_t n, const int32_t* __restrict__ choice, int32_
   }
 }
 
-// leader of each row: the smaller row of its pair; unmatched rows join the
-// pair of the strongest matched strong neighbour, else lead themselves
-__global__ void k_ml_attach(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
+// target[i]: for an unmatched row, its strongest matched strong neighbour
+// (-1: none); -1 for matched rows
+__global__ void k_ml_target(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
                             const double* __restrict__ v, const double* __restrict__ smax,
-                            const int32_t* __restrict__ partner, int32_t* __restrict__ leader) {
+                            const int32_t* __restrict__ partner, int32_t* __restrict__ target) {
   for (int64_t i = gtid(); i < n; i += gstride()) {
-    const int32_t p = partner[i];
-    if (p >= 0) {
-      leader[i] = min((int32_t)i, p);
-      continue;
-    }
     int32_t best = -1;
-    if (smax[i] > 0.0) {
+    if (partner[i] < 0 && smax[i] > 0.0) {
       const double thr = kStrong * smax[i];
       double bw = 0.0;
       for (int64_t k = rp[i]; k < rp[i + 1]; ++k) {
@@ -159,7 +156,32 @@ __global__ void k_ml_attach(int64_t n, const int64_t* __restrict__ rp, const int
         if (w > bw || (w == bw && j < best)) bw = w, best = j;
       }
     }
-    leader[i] = best >= 0 ? min(best, partner[best]) : (int32_t)i;
+    target[i] = best;
+  }
+}
+
+// leader of each row: the smaller row of its pair.  An unmatched row joins
+// its target's pair if it is among the first kMaxAttach rows (by index) that
+// chose that target -- a deterministic bound on aggregate size (the rows that
+// chose j are all in row j's pattern, which is structurally symmetric); else
+// it leads itself
+__global__ void k_ml_attach(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                            const int32_t* __restrict__ partner, const int32_t* __restrict__ target,
+                            int32_t* __restrict__ leader) {
+  for (int64_t i = gtid(); i < n; i += gstride()) {
+    const int32_t p = partner[i];
+    if (p >= 0) {
+      leader[i] = min((int32_t)i, p);
+      continue;
+    }
+    const int32_t j = target[i];
+    int rank = 0;
+    if (j >= 0)
+      for (int64_t k = rp[j]; k < rp[j + 1]; ++k) {
+        const int32_t c = ci[k];
+        rank += (c < (int32_t)i && target[c] == j) ? 1 : 0;
+      }
+    leader[i] = (j >= 0 && rank < kMaxAttach) ? min(j, partner[j]) : (int32_t)i;
   }
 }
 
@@ -237,7 +259,7 @@ __global__ void __launch_bounds__(32 * kGalWarps) k_ml_galerkin(
     // distinct keys into the hash set (bounded linear probing)
     for (int p = lane; p < L; p += 32) {
       const int key = S.key[p];
-      int h = (int)(((unsigned)key * 2654435761u) >> 23) & (kGalHash - 1);
+      int h = (int)(((unsigned)key * 2654435761u) >> 22) & (kGalHash - 1);  // top 10 bits
       for (int probe = 0; probe < kGalHash; ++probe) {
         const int prev = atomicCAS(&S.hash[h], -1, key);
         if (prev == -1 || prev == key) break;
@@ -796,12 +818,13 @@ int pairwise_pass(nalu_ctx* ctx, int64_t n, const int64_t* rp, const int32_t* ci
                   int64_t* nc_out) {
   cudaStream_t s = ctx->stream;
   DBuf<double> smax, diag;
-  DBuf<int32_t> partner, choice, leader, flag, id;
+  DBuf<int32_t> partner, choice, leader, flag, id, target;
   NALU_CUDA(ctx, smax.alloc(n));
   NALU_CUDA(ctx, diag.alloc(n));
   NALU_CUDA(ctx, partner.alloc(n));
   NALU_CUDA(ctx, choice.alloc(n));
   NALU_CUDA(ctx, leader.alloc(n));
+  NALU_CUDA(ctx, target.alloc(n));
   NALU_CUDA(ctx, flag.alloc(n + 1));
   NALU_CUDA(ctx, id.alloc(n + 1));
   const unsigned g = grid_n(n);
@@ -811,13 +834,14 @@ int pairwise_pass(nalu_ctx* ctx, int64_t n, const int64_t* rp, const int32_t* ci
     k_ml_choose<<<g, kMlThreads, 0, s>>>(n, rp, ci, v, smax.p, diag.p, partner.p, r, choice.p);
     k_ml_match<<<g, kMlThreads, 0, s>>>(n, choice.p, partner.p);
   }
-  k_ml_attach<<<g, kMlThreads, 0, s>>>(n, rp, ci, v, smax.p, partner.p, leader.p);
+  k_ml_target<<<g, kMlThreads, 0, s>>>(n, rp, ci, v, smax.p, partner.p, target.p);
+  k_ml_attach<<<g, kMlThreads, 0, s>>>(n, rp, ci, partner.p, target.p, leader.p);
   k_ml_flag_leaders<<<g, kMlThreads, 0, s>>>(n, leader.p, flag.p);
   NALU_CUDA(ctx, cudaMemsetAsync(flag.p + n, 0, sizeof(int32_t), s));
   int rc = exclusive_scan<int32_t>(ctx, flag.p, id.p, n + 1);
   if (rc) return rc;
   k_ml_assign<<<g, kMlThreads, 0, s>>>(n, leader.p, id.p, agg);
-  ctx->launches += 6 + 2 * kMatchRounds;
+  ctx->launches += 7 + 2 * kMatchRounds;
   *nc_out = read_one(ctx, id.p + n);
   return cuda_check(ctx, cudaGetLastError(), "pairwise aggregation");
 }
