@@ -14,7 +14,9 @@
 //     ties within a bin broken by a per-round hash of the edge.  Mutual
 //     proposals pair up.  Unmatched rows then join the pair of their strongest
 //     matched strong neighbour (at most two per matched row), else stay
-//     singletons (identity rows always do);
+//     singletons.  Rows without off-diagonal entries (Dirichlet and pinned
+//     rows) are on no coarse level: their rows of P are zero and the
+//     smoother alone treats them;
 //   * coarse operators: Galerkin A_c = P^T A P for the piecewise-constant P of
 //     each pass, one warp per coarse row: the member rows' entries are
 //     gathered into shared memory, their distinct coarse columns found with a
@@ -67,16 +69,22 @@ __device__ __forceinline__ int64_t gstride() { return (int64_t)gridDim.x * block
 // ---------------------------------------------------------------------------
 // aggregation
 // ---------------------------------------------------------------------------
-// smax[i] = max_{j != i} -a_ij (0 if none), diag[i] = |a_ii|
+// smax[i] = max_{j != i} -a_ij (0 if none; -1 for an isolated row, one
+// without off-diagonal entries), diag[i] = |a_ii|
 __global__ void k_ml_smax(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
                           const double* __restrict__ v, double* __restrict__ smax, double* __restrict__ diag) {
   for (int64_t i = gtid(); i < n; i += gstride()) {
     double m = 0.0, d = 0.0;
+    bool off = false;
     for (int64_t k = rp[i]; k < rp[i + 1]; ++k) {
-      if (ci[k] != i) m = fmax(m, -v[k]);
-      else d = fabs(v[k]);
+      if (ci[k] != i) {
+        m = fmax(m, -v[k]);
+        off = off || v[k] != 0.0;
+      } else {
+        d = fabs(v[k]);
+      }
     }
-    smax[i] = m;
+    smax[i] = off ? m : -1.0;
     diag[i] = d;
   }
 }
@@ -166,12 +174,16 @@ __global__ void k_ml_target(int64_t n, const int64_t* __restrict__ rp, const int
 // chose j are all in row j's pattern, which is structurally symmetric); else
 // it leads itself
 __global__ void k_ml_attach(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
-                            const int32_t* __restrict__ partner, const int32_t* __restrict__ target,
-                            int32_t* __restrict__ leader) {
+                            const double* __restrict__ smax, const int32_t* __restrict__ partner,
+                            const int32_t* __restrict__ target, int32_t* __restrict__ leader) {
   for (int64_t i = gtid(); i < n; i += gstride()) {
     const int32_t p = partner[i];
     if (p >= 0) {
       leader[i] = min((int32_t)i, p);
+      continue;
+    }
+    if (smax[i] < 0.0) {  // isolated row: on no coarse level
+      leader[i] = -1;
       continue;
     }
     const int32_t j = target[i];
@@ -188,13 +200,14 @@ __global__ void k_ml_attach(int64_t n, const int64_t* __restrict__ rp, const int
 __global__ void k_ml_flag_leaders(int64_t n, const int32_t* __restrict__ leader, int32_t* __restrict__ flag) {
   for (int64_t i = gtid(); i < n; i += gstride()) flag[i] = leader[i] == (int32_t)i ? 1 : 0;
 }
+// agg[i] = compact id of i's leader, -1 for rows on no coarse level
 __global__ void k_ml_assign(int64_t n, const int32_t* __restrict__ leader, const int32_t* __restrict__ id,
                             int32_t* __restrict__ agg) {
-  for (int64_t i = gtid(); i < n; i += gstride()) agg[i] = id[leader[i]];
+  for (int64_t i = gtid(); i < n; i += gstride()) agg[i] = leader[i] >= 0 ? id[leader[i]] : -1;
 }
 // map[i] <- agg[map[i]]: compose the passes of one level
 __global__ void k_ml_compose(int64_t n, int32_t* __restrict__ map, const int32_t* __restrict__ agg) {
-  for (int64_t i = gtid(); i < n; i += gstride()) map[i] = agg[map[i]];
+  for (int64_t i = gtid(); i < n; i += gstride()) map[i] = map[i] >= 0 ? agg[map[i]] : -1;
 }
 __global__ void k_ml_iota(int64_t n, int32_t* __restrict__ a) {
   for (int64_t i = gtid(); i < n; i += gstride()) a[i] = (int32_t)i;
@@ -202,16 +215,16 @@ __global__ void k_ml_iota(int64_t n, int32_t* __restrict__ a) {
 __global__ void k_ml_fill_i32(int64_t n, int32_t* __restrict__ a, int32_t v) {
   for (int64_t i = gtid(); i < n; i += gstride()) a[i] = v;
 }
-// member offsets of each aggregate from the sorted aggregate ids (every id in
-// [0, nc) has at least one member, its leader)
-__global__ void k_ml_member_ptr(int64_t n, int64_t nc, const int32_t* __restrict__ sorted_agg,
+// member offsets of each aggregate from the aggregate ids sorted as unsigned
+// (every id in [0, nc) has a member, its leader; excluded rows, id -1, sort last)
+__global__ void k_ml_member_ptr(int64_t n, int64_t nc, const uint32_t* __restrict__ sorted_agg,
                                 int64_t* __restrict__ mptr) {
   for (int64_t i = gtid(); i < n; i += gstride()) {
-    const int32_t a = sorted_agg[i];
+    const int64_t a = min((int64_t)sorted_agg[i], nc);
     if (i == 0)
-      for (int32_t c = 0; c <= a; ++c) mptr[c] = 0;
-    const int32_t next = i + 1 < n ? sorted_agg[i + 1] : (int32_t)nc;
-    for (int32_t c = a + 1; c <= next; ++c) mptr[c] = i + 1;
+      for (int64_t c = 0; c <= a; ++c) mptr[c] = 0;
+    const int64_t next = i + 1 < n ? min((int64_t)sorted_agg[i + 1], nc) : nc;
+    for (int64_t c = a + 1; c <= next; ++c) mptr[c] = i + 1;
   }
 }
 
@@ -249,7 +262,7 @@ __global__ void __launch_bounds__(32 * kGalWarps) k_ml_galerkin(
         break;
       }
       for (int k = lane; k < len; k += 32) {
-        S.key[L + k] = agg[ci[b + k]];
+        S.key[L + k] = agg[ci[b + k]];  // -1: a column on no coarse level (dropped)
         S.val[L + k] = v[b + k];
       }
       L += len;
@@ -259,6 +272,7 @@ __global__ void __launch_bounds__(32 * kGalWarps) k_ml_galerkin(
     // distinct keys into the hash set (bounded linear probing)
     for (int p = lane; p < L; p += 32) {
       const int key = S.key[p];
+      if (key < 0) continue;
       int h = (int)(((unsigned)key * 2654435761u) >> 22) & (kGalHash - 1);  // top 10 bits
       for (int probe = 0; probe < kGalHash; ++probe) {
         const int prev = atomicCAS(&S.hash[h], -1, key);
@@ -423,7 +437,10 @@ __global__ void k_ml_restrict(int64_t nc, const int64_t* __restrict__ mptr, cons
 // prolongation z[i] += e[agg[i]]
 __global__ void k_ml_prolong(int64_t n, const int32_t* __restrict__ agg, const float* __restrict__ e,
                              float* __restrict__ z) {
-  for (int64_t i = gtid(); i < n; i += gstride()) z[i] += e[agg[i]];
+  for (int64_t i = gtid(); i < n; i += gstride()) {
+    const int32_t a = agg[i];
+    if (a >= 0) z[i] += e[a];
+  }
 }
 
 // ---- deterministic dot products: block partials, the last block finishes ---
@@ -835,7 +852,7 @@ int pairwise_pass(nalu_ctx* ctx, int64_t n, const int64_t* rp, const int32_t* ci
     k_ml_match<<<g, kMlThreads, 0, s>>>(n, choice.p, partner.p);
   }
   k_ml_target<<<g, kMlThreads, 0, s>>>(n, rp, ci, v, smax.p, partner.p, target.p);
-  k_ml_attach<<<g, kMlThreads, 0, s>>>(n, rp, ci, partner.p, target.p, leader.p);
+  k_ml_attach<<<g, kMlThreads, 0, s>>>(n, rp, ci, smax.p, partner.p, target.p, leader.p);
   k_ml_flag_leaders<<<g, kMlThreads, 0, s>>>(n, leader.p, flag.p);
   NALU_CUDA(ctx, cudaMemsetAsync(flag.p + n, 0, sizeof(int32_t), s));
   int rc = exclusive_scan<int32_t>(ctx, flag.p, id.p, n + 1);
@@ -849,17 +866,19 @@ int pairwise_pass(nalu_ctx* ctx, int64_t n, const int64_t* rp, const int32_t* ci
 // members of each aggregate, in row order: mptr [nc+1], mem [n]
 int build_members(nalu_ctx* ctx, int64_t n, int64_t nc, const int32_t* agg, DBuf<int64_t>& mptr, DBuf<int32_t>& mem) {
   cudaStream_t s = ctx->stream;
-  DBuf<int32_t> keys_out, iota;
+  DBuf<uint32_t> keys_out;
+  DBuf<int32_t> iota;
   NALU_CUDA(ctx, keys_out.alloc(n));
   NALU_CUDA(ctx, iota.alloc(n));
   NALU_CUDA(ctx, mem.alloc(n));
   NALU_CUDA(ctx, mptr.alloc(nc + 1));
   k_ml_iota<<<grid_n(n), kMlThreads, 0, s>>>(n, iota.p);
   size_t tmp = 0;
-  NALU_CUDA(ctx, cub::DeviceRadixSort::SortPairs(nullptr, tmp, agg, keys_out.p, iota.p, mem.p, (int)n, 0, 32, s));
+  const uint32_t* ukeys = reinterpret_cast<const uint32_t*>(agg);  // -1 sorts after every id
+  NALU_CUDA(ctx, cub::DeviceRadixSort::SortPairs(nullptr, tmp, ukeys, keys_out.p, iota.p, mem.p, (int)n, 0, 32, s));
   DBuf<unsigned char> t;
   NALU_CUDA(ctx, t.alloc((int64_t)tmp + 1));
-  NALU_CUDA(ctx, cub::DeviceRadixSort::SortPairs(t.p, tmp, agg, keys_out.p, iota.p, mem.p, (int)n, 0, 32, s));
+  NALU_CUDA(ctx, cub::DeviceRadixSort::SortPairs(t.p, tmp, ukeys, keys_out.p, iota.p, mem.p, (int)n, 0, 32, s));
   k_ml_member_ptr<<<grid_n(n), kMlThreads, 0, s>>>(n, nc, keys_out.p, mptr.p);
   ctx->launches += 2;
   NALU_CUDA(ctx, cudaStreamSynchronize(s));  // temporaries are freed on return
