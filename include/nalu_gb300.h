@@ -319,7 +319,7 @@ enum nalu_precond {
                                  scalar systems, FP64, needs weights */
   /* aggregation multigrid in flexible CG, the GPU counterpart of the MueLu
    * choice (src/LinearSolverConfig.C:92-96): pairwise aggregation on the
-   * strong couplings, Galerkin coarse operators, K-cycle, FP32 cycle inside
+   * strong couplings, Galerkin coarse operators, V- or K-cycle, FP32 cycle inside
    * FP64 flexible CG; scalar systems, FP64 precision.  MULTILEVEL smooths with
    * damped Jacobi on every level; LEARNED_MULTILEVEL with the learned
    * 27-point stencil on the fine level (needs weights) */
@@ -352,7 +352,8 @@ typedef struct nalu_solver_opts {
                         the learned FCG with the stall fallback only */
   int ml_kcycle_levels; /* multilevel preconditioners: coarse levels 1..k solve
                            their coarse problem by K-cycle (two flexible CG steps),
-                           deeper ones by V-cycle; 0 (default) all, -1 none */
+                           deeper ones by V-cycle; 0 (default): V-cycle throughout
+                           (the fastest on the continuity systems measured) */
   int reserved[3];
 } nalu_solver_opts;
 typedef struct nalu_solve_info {

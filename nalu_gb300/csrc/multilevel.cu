@@ -27,9 +27,9 @@
 //   * the coarsest level (at most 512 rows, 1024 if coarsening stalls) is
 //     inverted densely: FP32 Gauss-Jordan with partial pivoting in one block.
 // Cycle (FP32 vectors and values): one pre- and one post-smoothing step per
-// level; the coarse problem of each level solved by a K-cycle (two flexible
-// CG steps preconditioned by the next level's cycle, Notay & Vassilevski 2008)
-// on the first `ml_kcycle_levels` coarse levels and by a V-cycle below.  The
+// level; the coarse problem of each level solved by a V-cycle, or, on the
+// first `ml_kcycle_levels` coarse levels, by a K-cycle (two flexible CG steps
+// preconditioned by the next level's cycle, Notay & Vassilevski 2008).  The
 // outer flexible CG (FP64 vectors and values) judges convergence on the true
 // FP64 residual, as every other solve here.
 #include <cuda_runtime.h>
@@ -792,13 +792,29 @@ struct MlLevel {
   float omega = 0.6f;
 };
 
+// set-up temporaries, grown to the largest level and kept between solves
+struct MlScratch {
+  DBuf<double> smax, diag;
+  DBuf<int32_t> partner, choice, leader, target, flag, id, agg, iota, mem;
+  DBuf<uint32_t> keys;
+  DBuf<int64_t> cnt, mptr;
+  DBuf<int> flagd;
+  DBuf<unsigned char> cub;
+  DBuf<int64_t> rp[2];  // ping-pong coarse matrices of the passes within a level
+  DBuf<int32_t> ci[2];
+  DBuf<double> v[2];
+};
+
 struct MlState {
   std::vector<MlLevel> lv;
+  MlScratch sc;
   DBuf<double> partial, ks;   // reduction partials; device scalars (8 per level, then the outer FCG's)
+  DBuf<double> p, q;          // outer flexible CG vectors
+  DBuf<float> rf;             // the residual in FP32 (the cycle's input)
   DBuf<unsigned> counter;     // reduction tickets
   bool learned = false;
   bool ready = false;
-  int klevels = 1 << 20;      // coarse levels 1..klevels solved by K-cycle, deeper ones by V-cycle
+  int klevels = 0;            // coarse levels 1..klevels solved by K-cycle, deeper ones by V-cycle
 };
 
 namespace {
@@ -813,13 +829,16 @@ unsigned grid_rows(int64_t n) {
 }
 
 template <class T>
-int exclusive_scan(nalu_ctx* ctx, const T* in, T* out, int64_t n) {
+cudaError_t grow(DBuf<T>& b, int64_t n) {
+  return b.n >= n ? cudaSuccess : b.alloc(n);
+}
+
+template <class T>
+int exclusive_scan(nalu_ctx* ctx, MlScratch& S, const T* in, T* out, int64_t n) {
   size_t tmp = 0;
   NALU_CUDA(ctx, cub::DeviceScan::ExclusiveSum(nullptr, tmp, in, out, (int)n, ctx->stream));
-  DBuf<unsigned char> t;
-  NALU_CUDA(ctx, t.alloc((int64_t)tmp + 1));
-  NALU_CUDA(ctx, cub::DeviceScan::ExclusiveSum(t.p, tmp, in, out, (int)n, ctx->stream));
-  NALU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));  // t is freed on return
+  NALU_CUDA(ctx, grow(S.cub, (int64_t)tmp + 1));
+  NALU_CUDA(ctx, cub::DeviceScan::ExclusiveSum(S.cub.p, tmp, in, out, (int)n, ctx->stream));
   return NALU_OK;
 }
 template <class T>
@@ -830,89 +849,76 @@ T read_one(nalu_ctx* ctx, const T* d) {
   return h;
 }
 
-// one pairwise pass on (n, rp, ci, v): agg [n] -> [0, *nc)
-int pairwise_pass(nalu_ctx* ctx, int64_t n, const int64_t* rp, const int32_t* ci, const double* v, int32_t* agg,
+// one pairwise pass on (n, rp, ci, v): S.agg [n] -> [0, *nc) or -1
+int pairwise_pass(nalu_ctx* ctx, MlScratch& S, int64_t n, const int64_t* rp, const int32_t* ci, const double* v,
                   int64_t* nc_out) {
   cudaStream_t s = ctx->stream;
-  DBuf<double> smax, diag;
-  DBuf<int32_t> partner, choice, leader, flag, id, target;
-  NALU_CUDA(ctx, smax.alloc(n));
-  NALU_CUDA(ctx, diag.alloc(n));
-  NALU_CUDA(ctx, partner.alloc(n));
-  NALU_CUDA(ctx, choice.alloc(n));
-  NALU_CUDA(ctx, leader.alloc(n));
-  NALU_CUDA(ctx, target.alloc(n));
-  NALU_CUDA(ctx, flag.alloc(n + 1));
-  NALU_CUDA(ctx, id.alloc(n + 1));
+  NALU_CUDA(ctx, grow(S.smax, n));
+  NALU_CUDA(ctx, grow(S.diag, n));
+  for (DBuf<int32_t>* b : {&S.partner, &S.choice, &S.leader, &S.target, &S.agg}) NALU_CUDA(ctx, grow(*b, n));
+  NALU_CUDA(ctx, grow(S.flag, n + 1));
+  NALU_CUDA(ctx, grow(S.id, n + 1));
   const unsigned g = grid_n(n);
-  k_ml_smax<<<g, kMlThreads, 0, s>>>(n, rp, ci, v, smax.p, diag.p);
-  k_ml_fill_i32<<<g, kMlThreads, 0, s>>>(n, partner.p, -1);
+  k_ml_smax<<<g, kMlThreads, 0, s>>>(n, rp, ci, v, S.smax.p, S.diag.p);
+  k_ml_fill_i32<<<g, kMlThreads, 0, s>>>(n, S.partner.p, -1);
   for (int r = 0; r < kMatchRounds; ++r) {
-    k_ml_choose<<<g, kMlThreads, 0, s>>>(n, rp, ci, v, smax.p, diag.p, partner.p, r, choice.p);
-    k_ml_match<<<g, kMlThreads, 0, s>>>(n, choice.p, partner.p);
+    k_ml_choose<<<g, kMlThreads, 0, s>>>(n, rp, ci, v, S.smax.p, S.diag.p, S.partner.p, r, S.choice.p);
+    k_ml_match<<<g, kMlThreads, 0, s>>>(n, S.choice.p, S.partner.p);
   }
-  k_ml_target<<<g, kMlThreads, 0, s>>>(n, rp, ci, v, smax.p, partner.p, target.p);
-  k_ml_attach<<<g, kMlThreads, 0, s>>>(n, rp, ci, smax.p, partner.p, target.p, leader.p);
-  k_ml_flag_leaders<<<g, kMlThreads, 0, s>>>(n, leader.p, flag.p);
-  NALU_CUDA(ctx, cudaMemsetAsync(flag.p + n, 0, sizeof(int32_t), s));
-  int rc = exclusive_scan<int32_t>(ctx, flag.p, id.p, n + 1);
+  k_ml_target<<<g, kMlThreads, 0, s>>>(n, rp, ci, v, S.smax.p, S.partner.p, S.target.p);
+  k_ml_attach<<<g, kMlThreads, 0, s>>>(n, rp, ci, S.smax.p, S.partner.p, S.target.p, S.leader.p);
+  k_ml_flag_leaders<<<g, kMlThreads, 0, s>>>(n, S.leader.p, S.flag.p);
+  NALU_CUDA(ctx, cudaMemsetAsync(S.flag.p + n, 0, sizeof(int32_t), s));
+  int rc = exclusive_scan<int32_t>(ctx, S, S.flag.p, S.id.p, n + 1);
   if (rc) return rc;
-  k_ml_assign<<<g, kMlThreads, 0, s>>>(n, leader.p, id.p, agg);
+  k_ml_assign<<<g, kMlThreads, 0, s>>>(n, S.leader.p, S.id.p, S.agg.p);
   ctx->launches += 7 + 2 * kMatchRounds;
-  *nc_out = read_one(ctx, id.p + n);
+  *nc_out = read_one(ctx, S.id.p + n);
   return cuda_check(ctx, cudaGetLastError(), "pairwise aggregation");
 }
 
-// members of each aggregate, in row order: mptr [nc+1], mem [n]
-int build_members(nalu_ctx* ctx, int64_t n, int64_t nc, const int32_t* agg, DBuf<int64_t>& mptr, DBuf<int32_t>& mem) {
+// members of each aggregate, in row order: mptr [nc+1], mem [n] (excluded rows last, not counted)
+int build_members(nalu_ctx* ctx, MlScratch& S, int64_t n, int64_t nc, const int32_t* agg, int64_t* mptr,
+                  int32_t* mem) {
   cudaStream_t s = ctx->stream;
-  DBuf<uint32_t> keys_out;
-  DBuf<int32_t> iota;
-  NALU_CUDA(ctx, keys_out.alloc(n));
-  NALU_CUDA(ctx, iota.alloc(n));
-  NALU_CUDA(ctx, mem.alloc(n));
-  NALU_CUDA(ctx, mptr.alloc(nc + 1));
-  k_ml_iota<<<grid_n(n), kMlThreads, 0, s>>>(n, iota.p);
-  size_t tmp = 0;
+  NALU_CUDA(ctx, grow(S.keys, n));
+  NALU_CUDA(ctx, grow(S.iota, n));
+  k_ml_iota<<<grid_n(n), kMlThreads, 0, s>>>(n, S.iota.p);
   const uint32_t* ukeys = reinterpret_cast<const uint32_t*>(agg);  // -1 sorts after every id
-  NALU_CUDA(ctx, cub::DeviceRadixSort::SortPairs(nullptr, tmp, ukeys, keys_out.p, iota.p, mem.p, (int)n, 0, 32, s));
-  DBuf<unsigned char> t;
-  NALU_CUDA(ctx, t.alloc((int64_t)tmp + 1));
-  NALU_CUDA(ctx, cub::DeviceRadixSort::SortPairs(t.p, tmp, ukeys, keys_out.p, iota.p, mem.p, (int)n, 0, 32, s));
-  k_ml_member_ptr<<<grid_n(n), kMlThreads, 0, s>>>(n, nc, keys_out.p, mptr.p);
+  size_t tmp = 0;
+  NALU_CUDA(ctx, cub::DeviceRadixSort::SortPairs(nullptr, tmp, ukeys, S.keys.p, S.iota.p, mem, (int)n, 0, 32, s));
+  NALU_CUDA(ctx, grow(S.cub, (int64_t)tmp + 1));
+  NALU_CUDA(ctx, cub::DeviceRadixSort::SortPairs(S.cub.p, tmp, ukeys, S.keys.p, S.iota.p, mem, (int)n, 0, 32, s));
+  k_ml_member_ptr<<<grid_n(n), kMlThreads, 0, s>>>(n, nc, S.keys.p, mptr);
   ctx->launches += 2;
-  NALU_CUDA(ctx, cudaStreamSynchronize(s));  // temporaries are freed on return
   return cuda_check(ctx, cudaGetLastError(), "aggregate members");
 }
 
-// Galerkin product of (n, rp, ci, v) for the aggregation agg -> coarse CRS
-int galerkin(nalu_ctx* ctx, const int64_t* rp, const int32_t* ci, const double* v, const int32_t* agg, int64_t nc,
-             const int64_t* mptr, const int32_t* mem, DBuf<int64_t>& crp, DBuf<int32_t>& cci, DBuf<double>& cv,
-             int64_t* cnnz) {
+// Galerkin product of (rp, ci, v) for the aggregation agg -> coarse CRS in
+// the scratch matrix `slot`
+int galerkin(nalu_ctx* ctx, MlScratch& S, const int64_t* rp, const int32_t* ci, const double* v, const int32_t* agg,
+             int64_t nc, const int64_t* mptr, const int32_t* mem, int slot, int64_t* cnnz) {
   cudaStream_t s = ctx->stream;
-  DBuf<int64_t> cnt;
-  DBuf<int> over;
-  NALU_CUDA(ctx, cnt.alloc(nc + 1));
-  NALU_CUDA(ctx, crp.alloc(nc + 1));
-  NALU_CUDA(ctx, over.alloc(1));
-  NALU_CUDA(ctx, cudaMemsetAsync(over.p, 0, sizeof(int), s));
-  NALU_CUDA(ctx, cudaMemsetAsync(cnt.p + nc, 0, sizeof(int64_t), s));
+  NALU_CUDA(ctx, grow(S.cnt, nc + 1));
+  NALU_CUDA(ctx, grow(S.rp[slot], nc + 1));
+  NALU_CUDA(ctx, grow(S.flagd, 1));
+  NALU_CUDA(ctx, cudaMemsetAsync(S.flagd.p, 0, sizeof(int), s));
+  NALU_CUDA(ctx, cudaMemsetAsync(S.cnt.p + nc, 0, sizeof(int64_t), s));
   const size_t smem = sizeof(GalSmem) * kGalWarps;
   NALU_CUDA(ctx, cudaFuncSetAttribute(k_ml_galerkin<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   NALU_CUDA(ctx, cudaFuncSetAttribute(k_ml_galerkin<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>((nc + kGalWarps - 1) / kGalWarps, 4 * kMlBlocks));
-  k_ml_galerkin<true><<<g, 32 * kGalWarps, smem, s>>>(nc, mptr, mem, rp, ci, v, agg, nullptr, cnt.p, nullptr, nullptr,
-                                                      over.p);
-  int rc = exclusive_scan<int64_t>(ctx, cnt.p, crp.p, nc + 1);
+  k_ml_galerkin<true><<<g, 32 * kGalWarps, smem, s>>>(nc, mptr, mem, rp, ci, v, agg, nullptr, S.cnt.p, nullptr,
+                                                      nullptr, S.flagd.p);
+  int rc = exclusive_scan<int64_t>(ctx, S, S.cnt.p, S.rp[slot].p, nc + 1);
   if (rc) return rc;
-  if (read_one(ctx, over.p) != 0) return set_error(ctx, NALU_ERR_CAPACITY, "multilevel: coarse row too long");
-  *cnnz = read_one(ctx, crp.p + nc);
-  NALU_CUDA(ctx, cci.alloc(std::max<int64_t>(*cnnz, 1)));
-  NALU_CUDA(ctx, cv.alloc(std::max<int64_t>(*cnnz, 1)));
-  k_ml_galerkin<false><<<g, 32 * kGalWarps, smem, s>>>(nc, mptr, mem, rp, ci, v, agg, crp.p, nullptr, cci.p, cv.p,
-                                                       over.p);
+  if (read_one(ctx, S.flagd.p) != 0) return set_error(ctx, NALU_ERR_CAPACITY, "multilevel: coarse row too long");
+  *cnnz = read_one(ctx, S.rp[slot].p + nc);
+  NALU_CUDA(ctx, grow(S.ci[slot], std::max<int64_t>(*cnnz, 1)));
+  NALU_CUDA(ctx, grow(S.v[slot], std::max<int64_t>(*cnnz, 1)));
+  k_ml_galerkin<false><<<g, 32 * kGalWarps, smem, s>>>(nc, mptr, mem, rp, ci, v, agg, S.rp[slot].p, nullptr,
+                                                       S.ci[slot].p, S.v[slot].p, S.flagd.p);
   ctx->launches += 2;
-  NALU_CUDA(ctx, cudaStreamSynchronize(s));
   return cuda_check(ctx, cudaGetLastError(), "Galerkin product");
 }
 
@@ -936,9 +942,9 @@ float power_lambda(nalu_ctx* ctx, MlState& M, MlLevel& L, const float* m, int it
 
 int alloc_level_vectors(nalu_ctx* ctx, MlLevel& L, bool kcycle) {
   const int64_t n = std::max<int64_t>(L.n, 1);
-  for (DBuf<float>* b : {&L.z, &L.t, &L.z2, &L.b}) NALU_CUDA(ctx, b->alloc(n));
+  for (DBuf<float>* b : {&L.z, &L.t, &L.z2, &L.b}) NALU_CUDA(ctx, grow(*b, n));
   if (kcycle)
-    for (DBuf<float>* b : {&L.v1, &L.v2, &L.w1, &L.w2, &L.rt, &L.e}) NALU_CUDA(ctx, b->alloc(n));
+    for (DBuf<float>* b : {&L.v1, &L.v2, &L.w1, &L.w2, &L.rt, &L.e}) NALU_CUDA(ctx, grow(*b, n));
   return NALU_OK;
 }
 
@@ -949,17 +955,18 @@ int alloc_level_vectors(nalu_ctx* ctx, MlLevel& L, bool kcycle) {
 int ml_setup(nalu_ctx* ctx, bool learned) {
   if (!ctx->ml) ctx->ml = new MlState();
   MlState& M = *ctx->ml;
-  M.lv.clear();
   M.ready = false;
   M.learned = learned;
   cudaStream_t s = ctx->stream;
-  NALU_CUDA(ctx, M.partial.alloc(3 * 4 * kMlBlocks + 64));
-  NALU_CUDA(ctx, M.ks.alloc(8 * (kMaxLevels + 2)));
-  NALU_CUDA(ctx, M.counter.alloc(kCounters));
+  NALU_CUDA(ctx, grow(M.partial, 3 * 4 * kMlBlocks + 64));
+  NALU_CUDA(ctx, grow(M.ks, 8 * (kMaxLevels + 2)));
+  NALU_CUDA(ctx, grow(M.counter, kCounters));
   NALU_CUDA(ctx, cudaMemsetAsync(M.counter.p, 0, sizeof(unsigned) * kCounters, s));
   NALU_CUDA(ctx, cudaMemsetAsync(M.ks.p, 0, sizeof(double) * 8 * (kMaxLevels + 2), s));
+  // levels are rebuilt in place: their buffers are kept between solves and
+  // grow only when a level needs more
   M.lv.reserve(kMaxLevels + 1);
-  M.lv.emplace_back();
+  if (M.lv.empty()) M.lv.emplace_back();
   {
     MlLevel& L0 = M.lv[0];
     L0.n = ctx->n_rows;
@@ -969,74 +976,73 @@ int ml_setup(nalu_ctx* ctx, bool learned) {
     L0.vd = ctx->d_values.p;
   }
   int rc = NALU_OK;
+  MlScratch& S = M.sc;
   // levels of up to three pairwise passes each, down to kCoarsest rows
-  while ((int)M.lv.size() < kMaxLevels && M.lv.back().n > kCoarsest) {
-    MlLevel& F = M.lv.back();
-    NALU_CUDA(ctx, F.agg.alloc(F.n));
+  int top = 0;  // the level being coarsened
+  while (top + 1 < kMaxLevels && M.lv[top].n > kCoarsest) {
+    MlLevel& F = M.lv[top];
+    NALU_CUDA(ctx, grow(F.agg, F.n));
     k_ml_iota<<<grid_n(F.n), kMlThreads, 0, s>>>(F.n, F.agg.p);
     ctx->launches++;
     int64_t n = F.n, nnz = F.nnz;
     const int64_t* rp = F.rp;
     const int32_t* ci = F.ci;
     const double* v = F.vd;
-    DBuf<int64_t> crp;
-    DBuf<int32_t> cci;
-    DBuf<double> cv;
+    int slot = -1;
     for (int pass = 0; pass < kPassesPerLevel; ++pass) {
-      DBuf<int32_t> agg;
-      NALU_CUDA(ctx, agg.alloc(n));
       int64_t nc = 0;
-      if ((rc = pairwise_pass(ctx, n, rp, ci, v, agg.p, &nc))) return rc;
+      if ((rc = pairwise_pass(ctx, S, n, rp, ci, v, &nc))) return rc;
       if (nc >= n) break;  // nothing left to pair
-      DBuf<int64_t> mptr;
-      DBuf<int32_t> mem;
-      if ((rc = build_members(ctx, n, nc, agg.p, mptr, mem))) return rc;
-      DBuf<int64_t> nrp;
-      DBuf<int32_t> nci;
-      DBuf<double> nv;
+      NALU_CUDA(ctx, grow(S.mptr, nc + 1));
+      NALU_CUDA(ctx, grow(S.mem, n));
+      if ((rc = build_members(ctx, S, n, nc, S.agg.p, S.mptr.p, S.mem.p))) return rc;
+      slot = (slot + 1) & 1;
       int64_t cnnz = 0;
-      if ((rc = galerkin(ctx, rp, ci, v, agg.p, nc, mptr.p, mem.p, nrp, nci, nv, &cnnz))) return rc;
-      k_ml_compose<<<grid_n(F.n), kMlThreads, 0, s>>>(F.n, F.agg.p, agg.p);
+      if ((rc = galerkin(ctx, S, rp, ci, v, S.agg.p, nc, S.mptr.p, S.mem.p, slot, &cnnz))) return rc;
+      k_ml_compose<<<grid_n(F.n), kMlThreads, 0, s>>>(F.n, F.agg.p, S.agg.p);
       ctx->launches++;
-      NALU_CUDA(ctx, cudaStreamSynchronize(s));
-      crp = std::move(nrp);
-      cci = std::move(nci);
-      cv = std::move(nv);
-      rp = crp.p;
-      ci = cci.p;
-      v = cv.p;
+      rp = S.rp[slot].p;
+      ci = S.ci[slot].p;
+      v = S.v[slot].p;
       n = nc;
       nnz = cnnz;
       if (n <= kCoarsest) break;
     }
     if (n >= F.n) break;  // no coarsening: F is the coarsest level
-    if ((rc = build_members(ctx, F.n, n, F.agg.p, F.mptr, F.mem))) return rc;
-    M.lv.emplace_back();
-    MlLevel& C = M.lv.back();
+    NALU_CUDA(ctx, grow(F.mptr, n + 1));
+    NALU_CUDA(ctx, grow(F.mem, F.n));
+    if ((rc = build_members(ctx, S, F.n, n, F.agg.p, F.mptr.p, F.mem.p))) return rc;
+    if ((int)M.lv.size() < top + 2) M.lv.emplace_back();  // capacity reserved: F stays valid
+    MlLevel& C = M.lv[top + 1];
     C.n = n;
     C.nnz = nnz;
-    C.own_rp = std::move(crp);
-    C.own_ci = std::move(cci);
-    C.own_vd = std::move(cv);
+    NALU_CUDA(ctx, grow(C.own_rp, n + 1));
+    NALU_CUDA(ctx, grow(C.own_ci, std::max<int64_t>(nnz, 1)));
+    NALU_CUDA(ctx, grow(C.own_vd, std::max<int64_t>(nnz, 1)));
+    NALU_CUDA(ctx, cudaMemcpyAsync(C.own_rp.p, rp, sizeof(int64_t) * (n + 1), cudaMemcpyDeviceToDevice, s));
+    NALU_CUDA(ctx, cudaMemcpyAsync(C.own_ci.p, ci, sizeof(int32_t) * nnz, cudaMemcpyDeviceToDevice, s));
+    NALU_CUDA(ctx, cudaMemcpyAsync(C.own_vd.p, v, sizeof(double) * nnz, cudaMemcpyDeviceToDevice, s));
     C.rp = C.own_rp.p;
     C.ci = C.own_ci.p;
     C.vd = C.own_vd.p;
+    ++top;
   }
+  M.lv.resize(top + 1);
   const int nl = (int)M.lv.size();
   if (M.lv.back().n > kDenseMax)
     return set_error(ctx, NALU_ERR_CAPACITY, "multilevel: coarsest level above 1024 rows (too few strong couplings)");
   // FP32 copies, vectors
   for (int l = 0; l < nl; ++l) {
     MlLevel& L = M.lv[l];
-    NALU_CUDA(ctx, L.vf.alloc(std::max<int64_t>(L.nnz, 1)));
-    NALU_CUDA(ctx, L.dinv.alloc(std::max<int64_t>(L.n, 1)));
+    NALU_CUDA(ctx, grow(L.vf, std::max<int64_t>(L.nnz, 1)));
+    NALU_CUDA(ctx, grow(L.dinv, std::max<int64_t>(L.n, 1)));
     k_ml_prep<<<grid_n(L.n), kMlThreads, 0, s>>>(L.n, L.rp, L.ci, L.vd, L.vf.p, L.dinv.p);
     ctx->launches++;
     if ((rc = alloc_level_vectors(ctx, L, l > 0 && l < nl - 1))) return rc;
   }
   if (learned) {
     MlLevel& L0 = M.lv[0];
-    NALU_CUDA(ctx, L0.msm.alloc(std::max<int64_t>(L0.nnz, 1)));
+    NALU_CUDA(ctx, grow(L0.msm, std::max<int64_t>(L0.nnz, 1)));
     k_ml_sell_to_crs<<<grid_n(L0.n), kMlThreads, 0, s>>>(L0.n, L0.rp, ctx->sw.sell.ptr.p, ctx->learned.wsell.p,
                                                          L0.msm.p);
     ctx->launches++;
@@ -1054,7 +1060,7 @@ int ml_setup(nalu_ctx* ctx, bool learned) {
     DBuf<float> D;
     DBuf<int> bad;
     NALU_CUDA(ctx, D.alloc((int64_t)nc * 2 * nc));
-    NALU_CUDA(ctx, C.inv.alloc((int64_t)nc * nc));
+    NALU_CUDA(ctx, grow(C.inv, (int64_t)nc * nc));
     NALU_CUDA(ctx, bad.alloc(1));
     NALU_CUDA(ctx, cudaMemsetAsync(bad.p, 0, sizeof(int), s));
     k_ml_dense_fill<<<grid_n((int64_t)nc * 2 * nc), kMlThreads, 0, s>>>(nc, D.p);
@@ -1150,14 +1156,15 @@ int fcg_multilevel(nalu_ctx* ctx, double* x, double* r, double rtol, double r0no
   if (!ctx->ml || !ctx->ml->ready || ctx->ml->lv.empty())
     return set_error(ctx, NALU_ERR_STATE, "multilevel hierarchy not built");
   MlState& M = *ctx->ml;
-  M.klevels = klevels == 0 ? (1 << 20) : (klevels < 0 ? 0 : klevels);
+  M.klevels = std::max(klevels, 0);
   const int64_t n = ctx->n_rows;
   cudaStream_t s = ctx->stream;
-  DBuf<double> p, q;
-  DBuf<float> rf;
-  NALU_CUDA(ctx, p.alloc(n));
-  NALU_CUDA(ctx, q.alloc(n));
-  NALU_CUDA(ctx, rf.alloc(n));
+  NALU_CUDA(ctx, grow(M.p, n));
+  NALU_CUDA(ctx, grow(M.q, n));
+  NALU_CUDA(ctx, grow(M.rf, n));
+  DBuf<double>& p = M.p;
+  DBuf<double>& q = M.q;
+  DBuf<float>& rf = M.rf;
   NALU_CUDA(ctx, cudaMemsetAsync(x, 0, sizeof(double) * n, s));
   NALU_CUDA(ctx, cudaMemsetAsync(p.p, 0, sizeof(double) * n, s));
   NALU_CUDA(ctx, cudaMemsetAsync(q.p, 0, sizeof(double) * n, s));
