@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <functional>
 #include <string>
 #include <utility>
 #include <vector>
@@ -292,6 +293,10 @@ int learned_prepare(nalu_ctx* ctx);
 // matrix; flexible CG with it on the residual r (in place) for the correction
 // x; the hierarchy's level sizes; its release
 int ml_setup(nalu_ctx* ctx, bool learned_smoother);
+// flexible CG on FP32-pair vectors (learned.cu) preconditioned by prec(rf, zf),
+// which launches kernels computing zf ~ A^-1 rf on the context stream
+int fcg_df_external(nalu_ctx* ctx, double* x, double* r, double rtol, double r0norm, int max_it, int check_every,
+                    const std::function<void(const float*, float*)>& prec, int* iters_out);
 int fcg_multilevel(nalu_ctx* ctx, double* x, double* r, double rtol, double r0norm, int max_it, int check_every,
                    int klevels, int* iters_out);
 int ml_levels(const nalu_ctx* ctx, int max_levels, int64_t* rows, int64_t* nnz);

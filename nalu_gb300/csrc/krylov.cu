@@ -1098,10 +1098,9 @@ int solve(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* info) {
         // built for this matrix once per call
         if (outer == 1) {
           const auto ts = std::chrono::steady_clock::now();
-          if (o.precond == NALU_PRECOND_LEARNED_MULTILEVEL) {
-            const float2* sv2 = nullptr;
-            if ((rc = sell_build<float2>(ctx, s.sell, &sv2)) || (rc = learned_prepare(ctx))) return rc;
-          }
+          const float2* sv2 = nullptr;  // the outer flexible CG's df64 SpMV runs on the SELL-32 copy
+          if ((rc = sell_build<float2>(ctx, s.sell, &sv2))) return rc;
+          if (o.precond == NALU_PRECOND_LEARNED_MULTILEVEL && (rc = learned_prepare(ctx))) return rc;
           if ((rc = ml_setup(ctx, o.precond == NALU_PRECOND_LEARNED_MULTILEVEL))) return rc;
           NALU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
           setup_s += std::chrono::duration<double>(std::chrono::steady_clock::now() - ts).count();

@@ -37,6 +37,7 @@
 #include <climits>
 #include <cmath>
 #include <cstring>
+#include <functional>
 #include <numeric>
 #include <utility>
 #include <vector>
@@ -622,6 +623,35 @@ __global__ void k_fcg_join(int64_t n, const float2* __restrict__ x2, const float
   }
 }
 
+// flexible CG with an external preconditioner: beta = -(z . q_old) / (p . q)_old
+// from the preconditioned residual z (FP32) by the last block
+__global__ void __launch_bounds__(kFcgThreads) k_fcg_beta(int64_t n, const float* __restrict__ zf,
+                                                          const float2* __restrict__ q2, double* __restrict__ part,
+                                                          unsigned* __restrict__ cnt, double* __restrict__ fs,
+                                                          int first) {
+  __shared__ double sh[33];
+  float dh = 0.0f, dl = 0.0f;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    acc_mul_df(dh, dl, make_float2(zf[i], 0.0f), q2[i]);
+  const double v[1] = {join_df(make_float2(dh, dl))};
+  double t[1];
+  if (red::grid_reduce<1>(v, part, kFcgBlocks, cnt, t, sh) && threadIdx.x == 0)
+    fs[FS_BETA] = first ? 0.0 : -t[0] / fs[FS_PQ];
+}
+// the high words of the FP32-pair residual: the preconditioner's FP32 input
+__global__ void k_fcg_hi(int64_t n, const float2* __restrict__ r2, float* __restrict__ rf) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    rf[i] = r2[i].x;
+}
+// steps that moved the iterate: counted while r.r is above the stop threshold
+// (fs[4] threshold, fs[5] count, fs[6] 1 while counting)
+__global__ void k_fcg_count(double* __restrict__ fs) {
+  if (fs[6] != 0.0) {
+    fs[5] += 1.0;
+    if (fs[FS_RR] <= fs[4]) fs[6] = 0.0;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // training (FP32)
 // ---------------------------------------------------------------------------
@@ -1067,6 +1097,113 @@ int fcg_learned(nalu_ctx* ctx, double* x, double* r, double rtol, double r0norm,
     NALU_CUDA(ctx, cudaMemsetAsync(x, 0, sizeof(double) * n, st));
   }
   if (bad) return NALU_ERR_NOT_CONVERGED;
+  return conv ? NALU_OK : NALU_ERR_NOT_CONVERGED;
+}
+
+// Flexible CG (FCG(1)) on FP32-pair vectors with the df64 SELL-32 SpMV, as the
+// learned FCG, preconditioned by prec(rf, zf): kernels on the context stream
+// that compute zf ~ A^-1 rf from the FP32 residual rf (captured into the
+// iteration's CUDA graph).  x (FP64) receives the correction from zero, r (FP64)
+// the updated residual; the stop rule is ||r|| <= rtol r0norm, checked every
+// check_every (at most 10) steps; *iters_out counts the steps taken before it
+// was met, exactly (counted on the device).
+int fcg_df_external(nalu_ctx* ctx, double* x, double* r, double rtol, double r0norm, int max_it, int check_every,
+                    const std::function<void(const float*, float*)>& prec, int* iters_out) {
+  const int64_t n = ctx->n_rows;
+  SolverWork& s = ctx->sw;
+  const SellMatrix& S = s.sell;
+  const int64_t npad = S.nslices * kSlice;
+  *iters_out = 0;
+  if (s.partial.n < 2 * kFcgBlocks) NALU_CUDA(ctx, s.partial.alloc(2 * kFcgBlocks));
+  if (s.p2.n < n) NALU_CUDA(ctx, s.p2.alloc(n));
+  if (s.cscal.n < 8) NALU_CUDA(ctx, s.cscal.alloc(8));
+  if (s.ccount.n < 1) NALU_CUDA(ctx, s.ccount.alloc(1));
+  if (s.x2.n < n) NALU_CUDA(ctx, s.x2.alloc(n));
+  if (s.r2.n < n) NALU_CUDA(ctx, s.r2.alloc(n));
+  if (s.q2.n < n) NALU_CUDA(ctx, s.q2.alloc(n));
+  if (s.zf.n < n) NALU_CUDA(ctx, s.zf.alloc(n));
+  if (s.fr.n < n) NALU_CUDA(ctx, s.fr.alloc(n));
+  int rc = sell_c16_ensure(ctx, s.sell);
+  if (rc) return rc;
+  const SellMatrix::View SV = S.view();
+  double* part = s.partial.p;
+  unsigned* cnt = s.ccount.p;
+  double* fs = s.cscal.p;
+  float* zf = s.zf.p;
+  float* rf = s.fr.p;
+  float2 *p = s.p2.p, *x2 = s.x2.p, *r2 = s.r2.p, *q2 = s.q2.p;
+  DBuf<int> nonpos;
+  NALU_CUDA(ctx, nonpos.alloc(1));
+  cudaStream_t st = ctx->stream;
+  const double stop = rtol * r0norm;
+  {
+    const double init[8] = {0.0, 0.0, 0.0, r0norm * r0norm, stop * stop, 0.0, 1.0, 0.0};
+    NALU_CUDA(ctx, cudaMemsetAsync(nonpos.p, 0, sizeof(int), st));
+    NALU_CUDA(ctx, cudaMemsetAsync(cnt, 0, sizeof(unsigned), st));
+    NALU_CUDA(ctx, cudaMemcpyAsync(fs, init, sizeof(init), cudaMemcpyHostToDevice, st));
+    NALU_CUDA(ctx, cudaStreamSynchronize(st));
+  }
+  k_fcg_split<<<kFcgBlocks, kFcgThreads, 0, st>>>(n, r, r2, x2, q2);
+  ctx->launches++;
+  const unsigned g_b = wave_grid(ctx, (const void*)k_fcg_beta, kFcgThreads);
+  const unsigned g_pu = wave_grid(ctx, (const void*)k_fcg_pupdate, kFcgThreads);
+  const unsigned g_sp = wave_grid(ctx, (const void*)k_fcg_spmv, kFcgThreads);
+  const unsigned g_ax = wave_grid(ctx, (const void*)k_fcg_axpy, kFcgThreads);
+  auto iteration = [&](int first) {
+    k_fcg_hi<<<kFcgBlocks, kFcgThreads, 0, st>>>(n, r2, rf);
+    prec(rf, zf);
+    k_fcg_beta<<<g_b, kFcgThreads, 0, st>>>(n, zf, q2, part, cnt, fs, first);
+    k_fcg_pupdate<<<g_pu, kFcgThreads, 0, st>>>(n, zf, p, fs, first);
+    k_fcg_spmv<<<g_sp, kFcgThreads, 0, st>>>(n, npad, SV, S.val2.p, p, r2, q2, part, cnt, fs, nonpos.p);
+    k_fcg_axpy<<<g_ax, kFcgThreads, 0, st>>>(n, x2, p, r2, q2, part, cnt, fs);
+    k_fcg_count<<<1, 1, 0, st>>>(fs);
+    ctx->launches += 6;
+  };
+  iteration(1);
+  const int chunk = std::max(1, check_every > 0 ? std::min(check_every, 10) : 10);
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaError_t ce = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+  if (ce != cudaSuccess) return cuda_check(ctx, ce, "begin capture");
+  for (int k = 0; k < chunk; ++k) iteration(0);
+  ce = cudaStreamEndCapture(st, &graph);
+  if (ce != cudaSuccess) return cuda_check(ctx, ce, "end capture");
+  ce = cudaGraphInstantiate(&exec, graph, 0);
+  if (ce != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    return cuda_check(ctx, ce, "instantiate");
+  }
+  int it = 1, hnonpos = 0;
+  bool conv = false;
+  for (;;) {
+    double h[8] = {};
+    cudaMemcpyAsync(h, fs, sizeof(h), cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(&hnonpos, nonpos.p, sizeof(int), cudaMemcpyDeviceToHost, st);
+    const cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+      rc = cuda_check(ctx, e, "flexible CG");
+      break;
+    }
+    const double res = std::sqrt(h[FS_RR]);
+    *iters_out = (int)h[5];
+    if (!std::isfinite(res) || hnonpos > 0) {
+      rc = set_error(ctx, NALU_ERR_NONFINITE, "flexible CG breakdown (non-finite or non-positive step)");
+      break;
+    }
+    if (res <= stop) {
+      conv = true;
+      break;
+    }
+    if (it >= max_it) break;
+    cudaGraphLaunch(exec, st);
+    it += chunk;
+  }
+  cudaGraphExecDestroy(exec);
+  cudaGraphDestroy(graph);
+  k_fcg_join<<<kFcgBlocks, kFcgThreads, 0, st>>>(n, x2, r2, x, r);
+  ctx->launches++;
+  NALU_CUDA(ctx, cudaGetLastError());
+  if (rc) return rc;
   return conv ? NALU_OK : NALU_ERR_NOT_CONVERGED;
 }
 

@@ -24,14 +24,14 @@
 //     gathered order, so the coarse matrix is deterministic;
 //   * FP32 copies, inverse diagonals, and smoothing weights 4 / (3 lambda_max)
 //     from power iteration (of D^-1 A, or of M A for the learned smoother);
-//   * the coarsest level (at most 512 rows, 1024 if coarsening stalls) is
+//   * the coarsest level (at most 256 rows, 1024 if coarsening stalls) is
 //     inverted densely: FP32 Gauss-Jordan with partial pivoting in one block.
 // Cycle (FP32 vectors and values): one pre- and one post-smoothing step per
 // level; the coarse problem of each level solved by a V-cycle, or, on the
 // first `ml_kcycle_levels` coarse levels, by a K-cycle (two flexible CG steps
 // preconditioned by the next level's cycle, Notay & Vassilevski 2008).  The
-// outer flexible CG (FP64 vectors and values) judges convergence on the true
-// FP64 residual, as every other solve here.
+// outer flexible CG runs on FP32-pair vectors with the df64 SpMV (learned.cu);
+// the solve judges convergence on the true FP64 residual, as every other here.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -53,7 +53,7 @@ constexpr float kStrong = 0.25f;      // strong coupling: -a_ij >= kStrong * max
 constexpr int kMatchRounds = 6;       // handshake rounds per pairwise pass
 constexpr int kPassesPerLevel = 3;    // pairwise passes per level
 constexpr int kMaxLevels = 12;
-constexpr int64_t kCoarsest = 512;    // coarsen until at most this many rows
+constexpr int64_t kCoarsest = 256;    // coarsen until at most this many rows
 constexpr int64_t kDenseMax = 1024;   // largest coarsest level inverted densely
 constexpr int kGalWarps = 4;          // warps per block of the Galerkin kernels
 constexpr int kGalList = 2048;        // gathered entries per coarse row (at most)
@@ -70,7 +70,7 @@ __device__ __forceinline__ int64_t gstride() { return (int64_t)gridDim.x * block
 // aggregation
 // ---------------------------------------------------------------------------
 // smax[i] = max_{j != i} -a_ij (0 if none; -1 for an isolated row, one
-// without off-diagonal entries), diag[i] = |a_ii|
+// without off-diagonal entries), diag[i] = 1 / sqrt|a_ii| (0 for a zero diagonal)
 __global__ void k_ml_smax(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
                           const double* __restrict__ v, double* __restrict__ smax, double* __restrict__ diag) {
   for (int64_t i = gtid(); i < n; i += gstride()) {
@@ -85,7 +85,7 @@ __global__ void k_ml_smax(int64_t n, const int64_t* __restrict__ rp, const int32
       }
     }
     smax[i] = off ? m : -1.0;
-    diag[i] = d;
+    diag[i] = d > 0.0 ? rsqrt(d) : 0.0;
   }
 }
 
@@ -96,13 +96,15 @@ __device__ __forceinline__ int strength_bin(double x) {
   const double m = __longlong_as_double((long long)((b & 0x000FFFFFFFFFFFFFull) | (1023ull << 52)));
   return 2 * e + (m >= 1.4142135623730951 ? 1 : 0);
 }
-// symmetric per-round hash of the edge (i, j)
-__device__ __forceinline__ uint64_t edge_hash(int32_t i, int32_t j, int round) {
-  uint64_t h = (uint64_t)min(i, j) * 0x9E3779B97F4A7C15ull + (uint64_t)max(i, j) * 0xBF58476D1CE4E5B9ull +
-               (uint64_t)(round + 1) * 0x94D049BB133111EBull;
-  h ^= h >> 31;
-  h *= 0xD6E8FEB86659FD93ull;
-  h ^= h >> 32;
+// symmetric per-round hash of the edge (i, j) (32-bit mix, murmur3 finaliser)
+__device__ __forceinline__ uint32_t edge_hash(int32_t i, int32_t j, int round) {
+  uint32_t h = (uint32_t)min(i, j) * 0x9E3779B1u ^ ((uint32_t)max(i, j) + 0x7F4A7C15u) * 0x85EBCA77u;
+  h ^= (uint32_t)(round + 1) * 0xC2B2AE3Du;
+  h ^= h >> 16;
+  h *= 0x85EBCA6Bu;
+  h ^= h >> 13;
+  h *= 0xC2B2AE35u;
+  h ^= h >> 16;
   return h;
 }
 
@@ -120,14 +122,15 @@ __global__ void k_ml_choose(int64_t n, const int64_t* __restrict__ rp, const int
     if (partner[i] < 0 && smax[i] > 0.0) {
       const double thr = kStrong * smax[i];
       int best_bin = -(1 << 30);
-      uint64_t best_h = 0;
+      uint32_t best_h = 0;
+      const double isd = diag[i];
       for (int64_t k = rp[i]; k < rp[i + 1]; ++k) {
         const int32_t j = ci[k];
         const double w = -v[k];
         if (j == i || partner[j] >= 0 || !(w >= thr)) continue;
-        const double dd = diag[i] * diag[j];
-        const int bin = dd > 0.0 ? strength_bin(w / sqrt(dd)) : -(1 << 29);
-        const uint64_t h = edge_hash((int32_t)i, j, round);
+        const double dd = isd * diag[j];
+        const int bin = dd > 0.0 ? strength_bin(w * dd) : -(1 << 29);
+        const uint32_t h = edge_hash((int32_t)i, j, round);
         if (bin > best_bin || (bin == best_bin && (h > best_h || (h == best_h && j < best)))) {
           best_bin = bin;
           best_h = h;
@@ -267,22 +270,27 @@ __global__ void __launch_bounds__(32 * kGalWarps) k_ml_galerkin(
       }
       L += len;
     }
-    for (int h = lane; h < kGalHash; h += 32) S.hash[h] = -1;
+    // hash set of the row's size: a power of two >= 2 L (at least 64 slots),
+    // so short rows clear and scan few slots
+    const int hbits = max(6, 32 - __clz(max(2 * L - 1, 1)));
+    const int hsize = min(1 << hbits, kGalHash);
+    const int hshift = 32 - __ffs(hsize) + 1;  // top log2(hsize) bits of the product
+    for (int h = lane; h < hsize; h += 32) S.hash[h] = -1;
     __syncwarp();
     // distinct keys into the hash set (bounded linear probing)
     for (int p = lane; p < L; p += 32) {
       const int key = S.key[p];
       if (key < 0) continue;
-      int h = (int)(((unsigned)key * 2654435761u) >> 22) & (kGalHash - 1);  // top 10 bits
-      for (int probe = 0; probe < kGalHash; ++probe) {
+      int h = (int)(((unsigned)key * 2654435761u) >> hshift) & (hsize - 1);
+      for (int probe = 0; probe < hsize; ++probe) {
         const int prev = atomicCAS(&S.hash[h], -1, key);
         if (prev == -1 || prev == key) break;
-        h = (h + 1) & (kGalHash - 1);
+        h = (h + 1) & (hsize - 1);
       }
     }
     __syncwarp();
     int U = 0;
-    for (int h0 = 0; h0 < kGalHash; h0 += 32) {
+    for (int h0 = 0; h0 < hsize; h0 += 32) {
       const int key = S.hash[h0 + lane];
       const unsigned has = __ballot_sync(0xffffffffu, key >= 0);
       const int pos = U + __popc(has & ((1u << lane) - 1u));
@@ -608,11 +616,18 @@ __global__ void __launch_bounds__(1024) k_ml_gauss_jordan(int n, float* __restri
     __syncthreads();
     for (int j = threadIdx.x; j < m; j += blockDim.x) D[(int64_t)k * m + j] *= pinv;
     __syncthreads();
-    // eliminate column k from every other row (columns left of k are done)
-    for (int64_t t = threadIdx.x; t < (int64_t)n * m; t += blockDim.x) {
-      const int i = (int)(t / m), j = (int)(t % m);
-      if (i == k || j <= k) continue;
-      D[t] -= D[(int64_t)i * m + k] * D[(int64_t)k * m + j];
+    // eliminate column k from every other row (columns left of k are done):
+    // one warp per row, lanes along the columns (coalesced, no index division)
+    {
+      const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+      const float* pk = D + (int64_t)k * m;
+      for (int i = warp; i < n; i += nw) {
+        if (i == k) continue;
+        float* pi = D + (int64_t)i * m;
+        const float f = pi[k];
+        if (f == 0.0f) continue;
+        for (int j = k + 1 + lane; j < m; j += 32) pi[j] -= f * pk[j];
+      }
     }
     __syncthreads();
     for (int i = threadIdx.x; i < n; i += blockDim.x)
@@ -686,89 +701,6 @@ __global__ void k_ml_seed(int64_t n, float* __restrict__ x) {
   }
 }
 
-// ---- outer flexible CG (FP64) ----------------------------------------------
-// scalars os[]: [0] r.r, [1] p.q of the previous step, [2] beta, [3] alpha,
-// [4] first-step flag, [5] stop threshold on r.r, [6] breakdown count,
-// [7] steps taken before convergence;
-// dots[]: [0] p.q, [1] p.r, [2] z.q_old
-__global__ void k_mlo_tof(int64_t n, const double* __restrict__ r, float* __restrict__ rf) {
-  for (int64_t i = gtid(); i < n; i += gstride()) rf[i] = (float)r[i];
-}
-__global__ void __launch_bounds__(kMlThreads) k_mlo_zq(int64_t n, const float* __restrict__ z,
-                                                       const double* __restrict__ q, double* __restrict__ partial,
-                                                       unsigned* __restrict__ counter, double* __restrict__ out) {
-  double acc[1] = {0.0};
-  for (int64_t i = gtid(); i < n; i += gstride()) acc[0] += (double)z[i] * q[i];
-  ml_reduce<1>(acc, partial, counter, out);
-}
-// beta = -(z . q_old) / (p . q)_old; 0 on the first step and once converged
-__global__ void k_mlo_beta(double* __restrict__ os, const double* __restrict__ zq) {
-  const bool frozen = os[5] > 0.0 && os[0] <= os[5];
-  if (os[4] != 0.0 || frozen) {
-    os[2] = 0.0;
-  } else {
-    const double b = -zq[0] / os[1];
-    os[2] = isfinite(b) ? b : 0.0;
-  }
-}
-__global__ void k_mlo_pupdate(int64_t n, const float* __restrict__ z, double* __restrict__ p,
-                              const double* __restrict__ os) {
-  const double b = os[2];
-  const bool first = os[4] != 0.0;
-  for (int64_t i = gtid(); i < n; i += gstride()) p[i] = (double)z[i] + (first ? 0.0 : b * p[i]);
-}
-// q = A p; dots[0] = p . q, dots[1] = p . r
-__global__ void __launch_bounds__(kMlThreads) k_mlo_spmv(int64_t n, const int64_t* __restrict__ rp,
-                                                         const int32_t* __restrict__ ci, const double* __restrict__ v,
-                                                         const double* __restrict__ p, double* __restrict__ q,
-                                                         const double* __restrict__ r, double* __restrict__ partial,
-                                                         unsigned* __restrict__ counter, double* __restrict__ dots) {
-  double acc[2] = {};
-  ML_ROW_LOOP(n) {
-    const int64_t rr = i < n ? i : n - 1;
-    double s = 0.0;
-    for (int64_t k = rp[rr] + sub; k < rp[rr + 1]; k += kTpr) s = fma(v[k], p[ci[k]], s);
-#pragma unroll
-    for (int o = kTpr / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, kTpr);
-    if (i < n && sub == 0) {
-      q[i] = s;
-      acc[0] += p[i] * s;
-      acc[1] += p[i] * r[i];
-    }
-  }
-  ml_reduce<2>(acc, partial, counter, dots);
-}
-// alpha = (p . r) / (p . q); zero once converged; a non-positive p . q before
-// convergence counts as a breakdown
-__global__ void k_mlo_alpha(double* __restrict__ os, const double* __restrict__ dots) {
-  const bool frozen = os[5] > 0.0 && os[0] <= os[5];
-  const double pq = dots[0];
-  double a = pq > 0.0 ? dots[1] / pq : 0.0;
-  if (!(pq > 0.0) || !isfinite(a)) {
-    if (!frozen) os[6] += 1.0;
-    a = 0.0;
-  }
-  os[3] = frozen ? 0.0 : a;
-  if (!frozen && pq > 0.0) os[1] = pq;
-  if (!frozen) os[7] += 1.0;  // steps that moved the iterate
-  os[4] = 0.0;
-}
-// x += alpha p; r -= alpha q; os[0] = r . r
-__global__ void __launch_bounds__(kMlThreads) k_mlo_axpy(int64_t n, double* __restrict__ x, const double* __restrict__ p,
-                                                         double* __restrict__ r, const double* __restrict__ q,
-                                                         double* __restrict__ partial, unsigned* __restrict__ counter,
-                                                         double* __restrict__ os) {
-  const double a = os[3];
-  double acc[1] = {0.0};
-  for (int64_t i = gtid(); i < n; i += gstride()) {
-    x[i] += a * p[i];
-    const double ri = r[i] - a * q[i];
-    r[i] = ri;
-    acc[0] += ri * ri;
-  }
-  ml_reduce<1>(acc, partial, counter, os);
-}
-
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -808,9 +740,7 @@ struct MlScratch {
 struct MlState {
   std::vector<MlLevel> lv;
   MlScratch sc;
-  DBuf<double> partial, ks;   // reduction partials; device scalars (8 per level, then the outer FCG's)
-  DBuf<double> p, q;          // outer flexible CG vectors
-  DBuf<float> rf;             // the residual in FP32 (the cycle's input)
+  DBuf<double> partial, ks;   // reduction partials; device scalars (8 per level)
   DBuf<unsigned> counter;     // reduction tickets
   bool learned = false;
   bool ready = false;
@@ -1146,10 +1076,10 @@ void cycle(nalu_ctx* ctx, MlState& M, int l, const float* b, float* z, int* site
 
 }  // namespace
 
-// Flexible CG preconditioned by the multilevel cycle, on the residual r (FP64,
-// updated in place) for the correction x (FP64, from zero), to
-// ||r|| <= rtol r0norm.  One step is captured as a CUDA graph and replayed;
-// convergence is read every check_every steps (at most 10).
+// Flexible CG preconditioned by the multilevel cycle (the FP32-pair flexible
+// CG of learned.cu with the df64 SELL-32 SpMV; the cycle runs on the FP32
+// residual), on the residual r (FP64, updated in place) for the correction x
+// (FP64, from zero), to ||r|| <= rtol r0norm.
 int fcg_multilevel(nalu_ctx* ctx, double* x, double* r, double rtol, double r0norm, int max_it, int check_every,
                    int klevels, int* iters_out) {
   *iters_out = 0;
@@ -1157,80 +1087,12 @@ int fcg_multilevel(nalu_ctx* ctx, double* x, double* r, double rtol, double r0no
     return set_error(ctx, NALU_ERR_STATE, "multilevel hierarchy not built");
   MlState& M = *ctx->ml;
   M.klevels = std::max(klevels, 0);
-  const int64_t n = ctx->n_rows;
-  cudaStream_t s = ctx->stream;
-  NALU_CUDA(ctx, grow(M.p, n));
-  NALU_CUDA(ctx, grow(M.q, n));
-  NALU_CUDA(ctx, grow(M.rf, n));
-  DBuf<double>& p = M.p;
-  DBuf<double>& q = M.q;
-  DBuf<float>& rf = M.rf;
-  NALU_CUDA(ctx, cudaMemsetAsync(x, 0, sizeof(double) * n, s));
-  NALU_CUDA(ctx, cudaMemsetAsync(p.p, 0, sizeof(double) * n, s));
-  NALU_CUDA(ctx, cudaMemsetAsync(q.p, 0, sizeof(double) * n, s));
-  double* os = M.ks.p + 8 * kMaxLevels;  // outer scalars
-  double* dots = os + 8;
-  const double stop = rtol * r0norm;
-  {
-    const double init[8] = {r0norm * r0norm, 1.0, 0.0, 0.0, 1.0, stop * stop, 0.0, 0.0};
-    NALU_CUDA(ctx, cudaMemcpyAsync(os, init, sizeof(init), cudaMemcpyHostToDevice, s));
-    NALU_CUDA(ctx, cudaStreamSynchronize(s));
-  }
-  MlLevel& L0 = M.lv[0];
-  auto step = [&]() {
+  auto prec = [&](const float* rf, float* zf) {
     int site = 0;
-    k_mlo_tof<<<grid_n(n), kMlThreads, 0, s>>>(n, r, rf.p);
-    if (M.lv.size() == 1) coarse_solve(ctx, M, 0, rf.p, L0.z.p, &site);  // one level: the dense inverse
-    else cycle(ctx, M, 0, rf.p, L0.z.p, &site);
-    const int c0 = site++ % kCounters, c1 = site++ % kCounters, c2 = site++ % kCounters;
-    k_mlo_zq<<<grid_n(n), kMlThreads, 0, s>>>(n, L0.z.p, q.p, M.partial.p, M.counter.p + c0, dots + 2);
-    k_mlo_beta<<<1, 1, 0, s>>>(os, dots + 2);
-    k_mlo_pupdate<<<grid_n(n), kMlThreads, 0, s>>>(n, L0.z.p, p.p, os);
-    k_mlo_spmv<<<grid_rows(n), kMlThreads, 0, s>>>(n, L0.rp, L0.ci, L0.vd, p.p, q.p, r, M.partial.p,
-                                                   M.counter.p + c1, dots);
-    k_mlo_alpha<<<1, 1, 0, s>>>(os, dots);
-    k_mlo_axpy<<<grid_n(n), kMlThreads, 0, s>>>(n, x, p.p, r, q.p, M.partial.p, M.counter.p + c2, os);
-    ctx->launches += 7;
+    if (M.lv.size() == 1) coarse_solve(ctx, M, 0, rf, zf, &site);  // one level: the dense inverse
+    else cycle(ctx, M, 0, rf, zf, &site);
   };
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
-  NALU_CUDA(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-  step();
-  cudaError_t ce = cudaStreamEndCapture(s, &graph);
-  if (ce != cudaSuccess) return cuda_check(ctx, ce, "capture multilevel FCG step");
-  ce = cudaGraphInstantiate(&exec, graph, 0);
-  if (ce != cudaSuccess) {
-    cudaGraphDestroy(graph);
-    return cuda_check(ctx, ce, "instantiate multilevel FCG step");
-  }
-  const int every = std::max(1, check_every > 0 ? std::min(check_every, 10) : 5);
-  int it = 0, rc = NALU_OK;
-  bool converged = false;
-  while (it < max_it) {
-    const int chunk = std::min(every, max_it - it);
-    for (int k = 0; k < chunk; ++k) cudaGraphLaunch(exec, s);
-    it += chunk;
-    double h[8];
-    cudaMemcpyAsync(h, os, sizeof(h), cudaMemcpyDeviceToHost, s);
-    const cudaError_t e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) {
-      rc = cuda_check(ctx, e, "multilevel FCG");
-      break;
-    }
-    if (h[6] != 0.0 || !std::isfinite(h[0])) {
-      rc = set_error(ctx, NALU_ERR_NONFINITE, "multilevel FCG breakdown (non-positive or non-finite step)");
-      break;
-    }
-    if (std::sqrt(h[0]) <= stop) {
-      converged = true;
-      break;
-    }
-  }
-  cudaGraphExecDestroy(exec);
-  cudaGraphDestroy(graph);
-  if (rc == NALU_OK && !converged) rc = NALU_ERR_NOT_CONVERGED;
-  *iters_out = (int)read_one(ctx, os + 7);
-  return rc;
+  return fcg_df_external(ctx, x, r, rtol, r0norm, max_it, check_every, prec, iters_out);
 }
 
 void ml_free(nalu_ctx* ctx) {

@@ -58,7 +58,7 @@ def test_multilevel_jacobi_solves(oracle, N, z_ratio, jitter):
               % (N, z_ratio, jitter, kl, rows, info.iterations, plain.iterations, res))
         assert len(rows) >= 2 and rows[0] == ctx.sizes()[0]
         # three pairwise passes per level coarsen by 3 or more; the coarsest
-        # level may come from fewer passes (it stops at 512 rows)
+        # level may come from fewer passes (it stops at 256 rows)
         assert all(rows[k + 1] * 3 <= rows[k] for k in range(len(rows) - 2)), rows
         assert rows[-1] < rows[-2]
         assert rows[-1] <= 1024
@@ -109,13 +109,13 @@ def test_multilevel_heat_dirichlet(oracle):
 
 
 def test_multilevel_small_system_single_level(oracle):
-    """A system below the coarsest size (8^3 nodes) is one dense level: the
+    """A system below the coarsest size (6^3 nodes) is one dense level: the
     preconditioner is its inverse and flexible CG converges at once."""
-    ctx = _continuity_system(7, 1.05)
+    ctx = _continuity_system(5, 1.05)
     info = ctx.solve(ng.default_solver_opts(tol=1e-8, max_iters=200, precond=ng.PRECOND_MULTILEVEL))
     _check_solution(ctx, oracle, info)
     rows, _ = ctx.multilevel_levels()
-    assert rows == [512] and info.iterations <= 5
+    assert rows == [216] and info.iterations <= 5
     ctx.close()
 
 
