@@ -579,10 +579,13 @@ __global__ void __launch_bounds__(kFcgThreads) k_fcg_spmv(int64_t n, int64_t npa
   const double v[2] = {join_df(make_float2(qh, ql)), join_df(make_float2(rh, rl))};
   double t[2];
   if (red::grid_reduce<2>(v, part, kFcgBlocks, cnt, t, sh) && threadIdx.x == 0) {
-    const double alpha = t[1] / t[0];
-    fs[FS_PQ] = t[0];
+    // fs[4] > 0: a stop threshold on r.r past which the iterate is frozen
+    // (chunks of steps run between convergence checks); 0 in the learned FCG
+    const bool frozen = fs[4] > 0.0 && fs[FS_RR] <= fs[4];
+    const double alpha = frozen ? 0.0 : t[1] / t[0];
+    if (!frozen) fs[FS_PQ] = t[0];
     fs[FS_ALPHA] = alpha;
-    if (!(alpha > 0.0)) *nonpos += 1;
+    if (!frozen && !(alpha > 0.0)) *nonpos += 1;
   }
 }
 
@@ -1186,12 +1189,12 @@ int fcg_df_external(nalu_ctx* ctx, double* x, double* r, double rtol, double r0n
     }
     const double res = std::sqrt(h[FS_RR]);
     *iters_out = (int)h[5];
-    if (!std::isfinite(res) || hnonpos > 0) {
-      rc = set_error(ctx, NALU_ERR_NONFINITE, "flexible CG breakdown (non-finite or non-positive step)");
+    if (std::isfinite(res) && res <= stop) {
+      conv = true;
       break;
     }
-    if (res <= stop) {
-      conv = true;
+    if (!std::isfinite(res) || hnonpos > 0) {
+      rc = set_error(ctx, NALU_ERR_NONFINITE, "flexible CG breakdown (non-finite or non-positive step)");
       break;
     }
     if (it >= max_it) break;
