@@ -1098,8 +1098,8 @@ int solve(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* info) {
         // built for this matrix once per call
         if (outer == 1) {
           const auto ts = std::chrono::steady_clock::now();
-          const float2* sv2 = nullptr;  // the outer flexible CG's df64 SpMV runs on the SELL-32 copy
-          if ((rc = sell_build<float2>(ctx, s.sell, &sv2))) return rc;
+          const float2* sv2 = nullptr;  // the outer flexible CG's df64 SpMV and the fine-level cycle run
+          if ((rc = sell_build<float2>(ctx, s.sell, &sv2)) || (rc = sell_c16_ensure(ctx, s.sell))) return rc;
           if (o.precond == NALU_PRECOND_LEARNED_MULTILEVEL && (rc = learned_prepare(ctx))) return rc;
           if ((rc = ml_setup(ctx, o.precond == NALU_PRECOND_LEARNED_MULTILEVEL))) return rc;
           NALU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));

@@ -55,10 +55,6 @@ constexpr int kPassesPerLevel = 3;    // pairwise passes per level
 constexpr int kMaxLevels = 12;
 constexpr int64_t kCoarsest = 256;    // coarsen until at most this many rows
 constexpr int64_t kDenseMax = 1024;   // largest coarsest level inverted densely
-constexpr int kGalWarps = 4;          // warps per block of the Galerkin kernels
-constexpr int kGalList = 2048;        // gathered entries per coarse row (at most)
-constexpr int kGalHash = 1024;        // hash slots per warp (a power of two, 2^10)
-constexpr int kGalUnique = 512;       // distinct coarse columns per row (at most)
 constexpr int kMaxAttach = 2;         // unmatched rows a matched row takes into its pair (at most)
 constexpr int kTpr = 4;               // threads per row of the CRS kernels
 
@@ -235,22 +231,34 @@ __global__ void k_ml_member_ptr(int64_t n, int64_t nc, const uint32_t* __restric
 // Galerkin coarse matrix, one warp per coarse row.  COUNT: the number of
 // distinct columns per row into cnt; else the row (ascending columns) at crp[I].
 // ---------------------------------------------------------------------------
+// Two capacities: rows of up to 256 gathered entries / 128 distinct columns
+// (8 warps per block, 45 KB: the usual case), and a large one (2048 / 512,
+// 4 warps per block, 120 KB) run only for a pass whose rows overflow the first.
+template <int LIST, int HASH, int UNIQ>
 struct GalSmem {
-  int key[kGalList];
-  double val[kGalList];
-  int hash[kGalHash];
-  int uniq[kGalUnique];
+  int key[LIST];
+  double val[LIST];
+  int hash[HASH];
+  int uniq[UNIQ];
 };
+template <int LIST, int HASH, int UNIQ, int WARPS>
+struct GalCfg {
+  static constexpr int kList = LIST, kHash = HASH, kUnique = UNIQ, kWarps = WARPS;
+  using Smem = GalSmem<LIST, HASH, UNIQ>;
+};
+using GalSmall = GalCfg<256, 512, 128, 8>;
+using GalLarge = GalCfg<2048, 1024, 512, 4>;
 
-template <bool COUNT>
-__global__ void __launch_bounds__(32 * kGalWarps) k_ml_galerkin(
+template <bool COUNT, class CFG>
+__global__ void __launch_bounds__(32 * CFG::kWarps) k_ml_galerkin(
     int64_t nc, const int64_t* __restrict__ mptr, const int32_t* __restrict__ mem, const int64_t* __restrict__ rp,
     const int32_t* __restrict__ ci, const double* __restrict__ v, const int32_t* __restrict__ agg,
     const int64_t* __restrict__ crp, int64_t* __restrict__ cnt, int32_t* __restrict__ cci, double* __restrict__ cv,
     int* __restrict__ overflow) {
+  constexpr int kGalWarps = CFG::kWarps, kGalList = CFG::kList, kGalHash = CFG::kHash, kGalUnique = CFG::kUnique;
   extern __shared__ unsigned char smraw[];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  GalSmem& S = reinterpret_cast<GalSmem*>(smraw)[w];
+  typename CFG::Smem& S = reinterpret_cast<typename CFG::Smem*>(smraw)[w];
   const int64_t warps = (int64_t)gridDim.x * kGalWarps;
   for (int64_t I = (int64_t)blockIdx.x * kGalWarps + w; I < nc; I += warps) {
     // the member rows' entries, as coarse columns, in member then entry order
@@ -430,6 +438,81 @@ __global__ void __launch_bounds__(kMlThreads) k_ml_mstep(int64_t n, const int64_
     const float mt = row_dot(rp, ci, m, t, r, sub);
     if (i < n && sub == 0) zo[i] = (z ? z[i] : 0.0f) + omega * mt;
   }
+}
+
+// ---- fine-level cycle kernels on A's SELL-32 copy (one thread per row;
+// entry k of row i at ptr[i / 32] + 32 k + i % 32; padding entries carry a zero
+// value; 16-bit column offsets from per-slice bases unless the slice is wide) --
+template <class XGet>
+__device__ __forceinline__ float sell_row_f(const SellMatrix::View& S, const float* __restrict__ val, int64_t row,
+                                            XGet x) {
+  const int64_t s = row >> 5;
+  const int64_t b0 = __ldg(S.ptr + s);
+  const int len = __ldg(S.len + s);
+  const int64_t base = b0 + (row & 31);
+  const bool wide = __ldg(S.wide + s) != 0;
+  const int32_t* cb = S.cbase + (b0 >> 5);
+  float acc = 0.0f;
+  for (int k = 0; k < len; k += 8) {  // loads of a group issued before the gathers
+    int32_t c[8];
+    float a[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const bool in = k + u < len;
+      const int64_t e = base + (int64_t)(k + u) * 32;
+      c[u] = in ? (wide ? __ldg(S.col + e) : __ldg(cb + k + u) + (int32_t)__ldg(S.col16 + e)) : -1;
+      a[u] = in ? __ldg(val + e) : 0.0f;
+    }
+    float b[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) b[u] = c[u] >= 0 ? x(c[u]) : 0.0f;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) acc = fmaf(a[u], b[u], acc);
+  }
+  return acc;
+}
+// z = w D^-1 b; t = b - A z
+__global__ void __launch_bounds__(kMlThreads) k_ml0_jac0_residual(int64_t n, SellMatrix::View S,
+                                                                  const float* __restrict__ val,
+                                                                  const float* __restrict__ dinv, float omega,
+                                                                  const float* __restrict__ b, float* __restrict__ z,
+                                                                  float* __restrict__ t) {
+  for (int64_t i = gtid(); i < n; i += gstride()) {
+    const float az = sell_row_f(S, val, i, [&](int32_t c) { return omega * __ldg(dinv + c) * __ldg(b + c); });
+    z[i] = omega * dinv[i] * b[i];
+    t[i] = b[i] - az;
+  }
+}
+// zo = z + w D^-1 (b - A z)
+__global__ void __launch_bounds__(kMlThreads) k_ml0_jac_step(int64_t n, SellMatrix::View S,
+                                                             const float* __restrict__ val,
+                                                             const float* __restrict__ dinv, float omega,
+                                                             const float* __restrict__ b, const float* __restrict__ z,
+                                                             float* __restrict__ zo) {
+  for (int64_t i = gtid(); i < n; i += gstride()) {
+    const float az = sell_row_f(S, val, i, [&](int32_t c) { return __ldg(z + c); });
+    zo[i] = z[i] + omega * dinv[i] * (b[i] - az);
+  }
+}
+// t = b - A x
+__global__ void __launch_bounds__(kMlThreads) k_ml0_residual(int64_t n, SellMatrix::View S,
+                                                             const float* __restrict__ val, const float* __restrict__ x,
+                                                             const float* __restrict__ b, float* __restrict__ t) {
+  for (int64_t i = gtid(); i < n; i += gstride())
+    t[i] = b[i] - sell_row_f(S, val, i, [&](int32_t c) { return __ldg(x + c); });
+}
+// zo = (z or 0) + w M t, M on the same SELL pattern
+__global__ void __launch_bounds__(kMlThreads) k_ml0_mstep(int64_t n, SellMatrix::View S, const float* __restrict__ m,
+                                                          float omega, const float* __restrict__ t,
+                                                          const float* __restrict__ z, float* __restrict__ zo) {
+  for (int64_t i = gtid(); i < n; i += gstride()) {
+    const float mt = sell_row_f(S, m, i, [&](int32_t c) { return __ldg(t + c); });
+    zo[i] = (z ? z[i] : 0.0f) + omega * mt;
+  }
+}
+// FP32 SELL values: the high words of the FP32-pair copy
+__global__ void k_ml0_sell_f32(int64_t stored, const float2* __restrict__ v2, float* __restrict__ vf) {
+  for (int64_t e = gtid(); e < stored; e += gstride()) vf[e] = v2[e].x;
 }
 
 // restriction rc[I] = sum of t over the members of I (member order)
@@ -722,6 +805,12 @@ struct MlLevel {
   DBuf<float> v1, v2, w1, w2, rt, e;  // K-cycle vectors (as a coarse level)
   DBuf<float> inv;            // dense inverse (coarsest level)
   float omega = 0.6f;
+  // level 0: the cycle's SpMVs on A's SELL-32 copy (FP32 values; the learned
+  // smoother's values are on the same pattern)
+  bool sell = false;
+  SellMatrix::View sv{};
+  DBuf<float> sellv;
+  const float* sellm = nullptr;
 };
 
 // set-up temporaries, grown to the largest level and kept between solves
@@ -824,32 +913,62 @@ int build_members(nalu_ctx* ctx, MlScratch& S, int64_t n, int64_t nc, const int3
   return cuda_check(ctx, cudaGetLastError(), "aggregate members");
 }
 
+// count pass of the Galerkin product with capacity CFG; *ok: no row overflowed
+template <class CFG>
+int galerkin_count(nalu_ctx* ctx, MlScratch& S, const int64_t* rp, const int32_t* ci, const double* v,
+                   const int32_t* agg, int64_t nc, const int64_t* mptr, const int32_t* mem, bool* ok) {
+  cudaStream_t s = ctx->stream;
+  const size_t smem = sizeof(typename CFG::Smem) * CFG::kWarps;
+  NALU_CUDA(ctx, cudaFuncSetAttribute(k_ml_galerkin<true, CFG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+  NALU_CUDA(ctx, cudaMemsetAsync(S.flagd.p, 0, sizeof(int), s));
+  const unsigned g =
+      (unsigned)std::max<int64_t>(1, std::min<int64_t>((nc + CFG::kWarps - 1) / CFG::kWarps, 8 * kMlBlocks));
+  k_ml_galerkin<true, CFG><<<g, 32 * CFG::kWarps, smem, s>>>(nc, mptr, mem, rp, ci, v, agg, nullptr, S.cnt.p,
+                                                              nullptr, nullptr, S.flagd.p);
+  ctx->launches++;
+  *ok = read_one(ctx, S.flagd.p) == 0;
+  return cuda_check(ctx, cudaGetLastError(), "Galerkin count");
+}
+template <class CFG>
+int galerkin_fill(nalu_ctx* ctx, MlScratch& S, const int64_t* rp, const int32_t* ci, const double* v,
+                  const int32_t* agg, int64_t nc, const int64_t* mptr, const int32_t* mem, int slot) {
+  cudaStream_t s = ctx->stream;
+  const size_t smem = sizeof(typename CFG::Smem) * CFG::kWarps;
+  NALU_CUDA(ctx, cudaFuncSetAttribute(k_ml_galerkin<false, CFG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+  const unsigned g =
+      (unsigned)std::max<int64_t>(1, std::min<int64_t>((nc + CFG::kWarps - 1) / CFG::kWarps, 8 * kMlBlocks));
+  k_ml_galerkin<false, CFG><<<g, 32 * CFG::kWarps, smem, s>>>(nc, mptr, mem, rp, ci, v, agg, S.rp[slot].p, nullptr,
+                                                               S.ci[slot].p, S.v[slot].p, S.flagd.p);
+  ctx->launches++;
+  return cuda_check(ctx, cudaGetLastError(), "Galerkin fill");
+}
+
 // Galerkin product of (rp, ci, v) for the aggregation agg -> coarse CRS in
-// the scratch matrix `slot`
+// the scratch matrix `slot` (the small capacity, the large one if a row
+// overflows it; NALU_ERR_CAPACITY beyond that)
 int galerkin(nalu_ctx* ctx, MlScratch& S, const int64_t* rp, const int32_t* ci, const double* v, const int32_t* agg,
              int64_t nc, const int64_t* mptr, const int32_t* mem, int slot, int64_t* cnnz) {
   cudaStream_t s = ctx->stream;
   NALU_CUDA(ctx, grow(S.cnt, nc + 1));
   NALU_CUDA(ctx, grow(S.rp[slot], nc + 1));
   NALU_CUDA(ctx, grow(S.flagd, 1));
-  NALU_CUDA(ctx, cudaMemsetAsync(S.flagd.p, 0, sizeof(int), s));
   NALU_CUDA(ctx, cudaMemsetAsync(S.cnt.p + nc, 0, sizeof(int64_t), s));
-  const size_t smem = sizeof(GalSmem) * kGalWarps;
-  NALU_CUDA(ctx, cudaFuncSetAttribute(k_ml_galerkin<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  NALU_CUDA(ctx, cudaFuncSetAttribute(k_ml_galerkin<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>((nc + kGalWarps - 1) / kGalWarps, 4 * kMlBlocks));
-  k_ml_galerkin<true><<<g, 32 * kGalWarps, smem, s>>>(nc, mptr, mem, rp, ci, v, agg, nullptr, S.cnt.p, nullptr,
-                                                      nullptr, S.flagd.p);
-  int rc = exclusive_scan<int64_t>(ctx, S, S.cnt.p, S.rp[slot].p, nc + 1);
+  bool ok = false, large = false;
+  int rc = galerkin_count<GalSmall>(ctx, S, rp, ci, v, agg, nc, mptr, mem, &ok);
   if (rc) return rc;
-  if (read_one(ctx, S.flagd.p) != 0) return set_error(ctx, NALU_ERR_CAPACITY, "multilevel: coarse row too long");
+  if (!ok) {
+    large = true;
+    if ((rc = galerkin_count<GalLarge>(ctx, S, rp, ci, v, agg, nc, mptr, mem, &ok))) return rc;
+    if (!ok) return set_error(ctx, NALU_ERR_CAPACITY, "multilevel: coarse row too long");
+  }
+  if ((rc = exclusive_scan<int64_t>(ctx, S, S.cnt.p, S.rp[slot].p, nc + 1))) return rc;
   *cnnz = read_one(ctx, S.rp[slot].p + nc);
   NALU_CUDA(ctx, grow(S.ci[slot], std::max<int64_t>(*cnnz, 1)));
   NALU_CUDA(ctx, grow(S.v[slot], std::max<int64_t>(*cnnz, 1)));
-  k_ml_galerkin<false><<<g, 32 * kGalWarps, smem, s>>>(nc, mptr, mem, rp, ci, v, agg, S.rp[slot].p, nullptr,
-                                                       S.ci[slot].p, S.v[slot].p, S.flagd.p);
-  ctx->launches += 2;
-  return cuda_check(ctx, cudaGetLastError(), "Galerkin product");
+  return large ? galerkin_fill<GalLarge>(ctx, S, rp, ci, v, agg, nc, mptr, mem, slot)
+               : galerkin_fill<GalSmall>(ctx, S, rp, ci, v, agg, nc, mptr, mem, slot);
 }
 
 // lambda_max of S A (S = D^-1, or the learned M) by power iteration
@@ -977,6 +1096,20 @@ int ml_setup(nalu_ctx* ctx, bool learned) {
                                                          L0.msm.p);
     ctx->launches++;
   }
+  {
+    // level 0 on the SELL-32 copy (built by the solve for the outer CG)
+    MlLevel& L0 = M.lv[0];
+    const SellMatrix& SM = ctx->sw.sell;
+    L0.sell = false;
+    if (SM.c16_valid && SM.val2.p && SM.nslices * 32 >= L0.n) {
+      NALU_CUDA(ctx, grow(L0.sellv, std::max<int64_t>(SM.stored, 1)));
+      k_ml0_sell_f32<<<grid_n(SM.stored), kMlThreads, 0, s>>>(SM.stored, SM.val2.p, L0.sellv.p);
+      ctx->launches++;
+      L0.sv = SM.view();
+      L0.sellm = learned ? ctx->learned.wsell.p : nullptr;
+      L0.sell = true;
+    }
+  }
   // smoothing weights
   for (int l = 0; l < nl - 1; ++l) {
     MlLevel& L = M.lv[l];
@@ -1048,6 +1181,32 @@ void cycle(nalu_ctx* ctx, MlState& M, int l, const float* b, float* z, int* site
   MlLevel& C = M.lv[l + 1];
   const unsigned gr = grid_rows(L.n), gn = grid_n(L.n), gc = grid_n(C.n);
   const bool learned = l == 0 && M.learned;
+  if (L.sell) {
+    // level 0 on the SELL-32 copy
+    const unsigned gs = grid_n(L.n);
+    if (learned) {
+      k_ml0_mstep<<<gs, kMlThreads, 0, s>>>(L.n, L.sv, L.sellm, L.omega, b, nullptr, z);
+      k_ml0_residual<<<gs, kMlThreads, 0, s>>>(L.n, L.sv, L.sellv.p, z, b, L.t.p);
+      ctx->launches += 2;
+    } else {
+      k_ml0_jac0_residual<<<gs, kMlThreads, 0, s>>>(L.n, L.sv, L.sellv.p, L.dinv.p, L.omega, b, z, L.t.p);
+      ctx->launches++;
+    }
+    float* ec = (l + 1 == (int)M.lv.size() - 1) ? C.z.p : C.e.p;
+    k_ml_restrict<<<gc, kMlThreads, 0, s>>>(C.n, L.mptr.p, L.mem.p, L.t.p, C.b.p);
+    coarse_solve(ctx, M, l + 1, C.b.p, ec, site);
+    k_ml_prolong<<<gn, kMlThreads, 0, s>>>(L.n, L.agg.p, ec, z);
+    ctx->launches += 2;
+    if (learned) {
+      k_ml0_residual<<<gs, kMlThreads, 0, s>>>(L.n, L.sv, L.sellv.p, z, b, L.t.p);
+      k_ml0_mstep<<<gs, kMlThreads, 0, s>>>(L.n, L.sv, L.sellm, L.omega, L.t.p, z, L.z2.p);
+    } else {
+      k_ml0_jac_step<<<gs, kMlThreads, 0, s>>>(L.n, L.sv, L.sellv.p, L.dinv.p, L.omega, b, z, L.z2.p);
+    }
+    cudaMemcpyAsync(z, L.z2.p, sizeof(float) * L.n, cudaMemcpyDeviceToDevice, s);
+    ctx->launches += learned ? 2 : 1;
+    return;
+  }
   // pre-smoothing from zero, then the residual
   if (learned) {
     k_ml_mstep<<<gr, kMlThreads, 0, s>>>(L.n, L.rp, L.ci, L.msm.p, L.omega, b, nullptr, z);
