@@ -443,15 +443,9 @@ __global__ void __launch_bounds__(kMlThreads) k_ml_mstep(int64_t n, const int64_
 // ---- fine-level cycle kernels on A's SELL-32 copy (one thread per row;
 // entry k of row i at ptr[i / 32] + 32 k + i % 32; padding entries carry a zero
 // value; 16-bit column offsets from per-slice bases unless the slice is wide) --
-template <class XGet>
-__device__ __forceinline__ float sell_row_f(const SellMatrix::View& S, const float* __restrict__ val, int64_t row,
-                                            XGet x) {
-  const int64_t s = row >> 5;
-  const int64_t b0 = __ldg(S.ptr + s);
-  const int len = __ldg(S.len + s);
-  const int64_t base = b0 + (row & 31);
-  const bool wide = __ldg(S.wide + s) != 0;
-  const int32_t* cb = S.cbase + (b0 >> 5);
+template <bool WIDE, class XGet>
+__device__ __forceinline__ float sell_row_f_impl(const SellMatrix::View& S, const float* __restrict__ val,
+                                                 int64_t base, int len, const int32_t* __restrict__ cb, XGet x) {
   float acc = 0.0f;
   for (int k = 0; k < len; k += 8) {  // loads of a group issued before the gathers
     int32_t c[8];
@@ -460,7 +454,7 @@ __device__ __forceinline__ float sell_row_f(const SellMatrix::View& S, const flo
     for (int u = 0; u < 8; ++u) {
       const bool in = k + u < len;
       const int64_t e = base + (int64_t)(k + u) * 32;
-      c[u] = in ? (wide ? __ldg(S.col + e) : __ldg(cb + k + u) + (int32_t)__ldg(S.col16 + e)) : -1;
+      c[u] = in ? (WIDE ? __ldg(S.col + e) : __ldg(cb + k + u) + (int32_t)__ldg(S.col16 + e)) : -1;
       a[u] = in ? __ldg(val + e) : 0.0f;
     }
     float b[8];
@@ -470,6 +464,19 @@ __device__ __forceinline__ float sell_row_f(const SellMatrix::View& S, const flo
     for (int u = 0; u < 8; ++u) acc = fmaf(a[u], b[u], acc);
   }
   return acc;
+}
+// the wide / 16-bit column choice is made once per row, so each path keeps
+// its group of loads ahead of the gathers
+template <class XGet>
+__device__ __forceinline__ float sell_row_f(const SellMatrix::View& S, const float* __restrict__ val, int64_t row,
+                                            XGet x) {
+  const int64_t s = row >> 5;
+  const int64_t b0 = __ldg(S.ptr + s);
+  const int len = __ldg(S.len + s);
+  const int64_t base = b0 + (row & 31);
+  const int32_t* cb = S.cbase + (b0 >> 5);
+  return __ldg(S.wide + s) ? sell_row_f_impl<true>(S, val, base, len, cb, x)
+                           : sell_row_f_impl<false>(S, val, base, len, cb, x);
 }
 // z = w D^-1 b; t = b - A z
 __global__ void __launch_bounds__(kMlThreads) k_ml0_jac0_residual(int64_t n, SellMatrix::View S,
