@@ -120,13 +120,35 @@ class ClockSampler:
 FP64_FLOP_PER_ELEM = 2458
 
 
-def compute_roof(n_elems, kernel_ms, fp64_tflops):
-    """the assembly measured against the FP64 compute roof: FP64-equivalent
-    FLOP/s of the timed kernel over the measured FP64 rate"""
+SM_COUNT, SMSP_PER_SM, WARP = 152, 4, 32
+
+
+def compute_roof(n_elems, kernel_ms, fp64_tflops, arith="fp64", sm_mhz=None):
+    """the assembly against its compute roofs.  FP64 kernel: FP64 FLOP/s over
+    the measured FP64 rate.  df64 kernel: the same operations run as FP32-pair
+    sequences on the FP32 pipes, so the FP64 rate is not its roof (its
+    FP64-equivalent rate exceeds it by design); its roof is instruction issue,
+    one warp instruction per cycle per SM sub-partition: the instructions per
+    element of the committed profile of the same kernel and workload, times
+    the elements, over the kernel time, against that issue rate at the
+    sampled SM clock."""
     flops = FP64_FLOP_PER_ELEM * n_elems
     achieved = flops / (kernel_ms * 1e-3) / 1e12
-    return {"fp64_flop_per_element": FP64_FLOP_PER_ELEM, "fp64_equivalent_tflops": achieved,
-            "fp64_peak_tflops": fp64_tflops, "frac_of_fp64_peak": achieved / fp64_tflops if fp64_tflops else None}
+    out = {"fp64_flop_per_element": FP64_FLOP_PER_ELEM, "fp64_equivalent_tflops": achieved,
+           "fp64_peak_tflops": fp64_tflops}
+    if arith == "fp64":
+        out["frac_of_fp64_peak"] = achieved / fp64_tflops if fp64_tflops else None
+        return out
+    _, prof = profile_traffic("df64")
+    ipe = prof.get("thread_instructions_per_element") if prof else None
+    if ipe:
+        mhz = sm_mhz or 2070.0
+        peak = SM_COUNT * SMSP_PER_SM * WARP * mhz * 1e6  # thread instructions per second
+        rate = ipe * n_elems / (kernel_ms * 1e-3)
+        out["issue"] = {"thread_instructions_per_element": ipe, "achieved_per_s": rate, "peak_per_s": peak,
+                        "frac": rate / peak, "sm_mhz": mhz,
+                        "source": "instructions per element from profiles/continuity_assembly_128_df64.json"}
+    return out
 
 
 def solve_iteration_roof(ms, iterations, nnz, n):
@@ -408,7 +430,15 @@ def bench_gpu(args):
     # the other configurations are reported by a single-GPU run only: with N > 1
     # every rank runs the replicated headline measurement and nothing else
     extras = ws == 1
-    if extras and not args.no_solve:
+    if extras and not args.no_solve and args.solve_set == "multilevel":
+        # profiling runs: the Jacobi-smoothed multigrid solve alone
+        ctx.zero()
+        ctx.assemble(ng.KERNEL_CONTINUITY_ADV, opts)
+        ctx.reset_rows([0])
+        ctx.sum_into_diag(0, 0, 1.0, 0.0)
+        ctx.load_complete()
+        solve = multilevel_solves(ng, ctx, learned=False)
+    elif extras and not args.no_solve:
         ctx.zero()
         ctx.assemble(ng.KERNEL_CONTINUITY_ADV, opts)
         ctx.reset_rows([0])
@@ -504,7 +534,8 @@ def bench_gpu(args):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "peak_kind": peak_kind, "algorithmic_bytes_per_launch": alg,
                          "kernel_ms": avg_ms, "fp64_probe_tflops": fp64_peak,
-                         "compute": compute_roof(n_elems, avg_ms, fp64_peak)},
+                         "compute": compute_roof(n_elems, avg_ms, fp64_peak, arith_names[arith],
+                                                 clk.summary().get("sm_mhz"))},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches, "clocks": clk.summary(), "cpu_baseline": cpu, "solve": solve,
             "batch": batch, "momentum_c3": momentum, "heat_c1": heat, "geometry_boundary_time": aux}
@@ -721,7 +752,7 @@ def bench_c4(ng, weights, dev=0, N=192):
         ms = min(time_mode(ctx, ar, sc) for sc in (ng.SCATTER_ATOMIC, ng.SCATTER_COLOURED))
         gbs = alg / (ms * 1e-3) / 1e9
         asm[an] = {"ms": ms, "elements_per_s": E / (ms * 1e-3), "achieved_gbs": gbs, "frac_of_hbm": gbs / peak,
-                   "peak_kind": peak_kind, "compute": compute_roof(E, ms, fp64_tf)}
+                   "peak_kind": peak_kind, "compute": compute_roof(E, ms, fp64_tf, an)}
     asm["algorithmic_bytes_per_launch"] = alg
     ctx.zero()
     ctx.assemble(ng.KERNEL_CONTINUITY_ADV)
@@ -742,13 +773,14 @@ def bench_c4(ng, weights, dev=0, N=192):
     return out
 
 
-def multilevel_solves(ng, ctx, reps=2):
+def multilevel_solves(ng, ctx, reps=2, learned=True):
     """The continuity system of ctx through the aggregation multigrid in
     flexible CG: learned fine-level smoother (the learned preconditioner) and
     damped-Jacobi smoothing (the same method without the network); best of
     reps calls, each building its hierarchy (set-up included in ms)."""
     out = {}
-    for key, pc in (("learned_multilevel", ng.PRECOND_LEARNED_MULTILEVEL), ("multilevel_jacobi", ng.PRECOND_MULTILEVEL)):
+    variants = (("learned_multilevel", ng.PRECOND_LEARNED_MULTILEVEL),) if learned else ()
+    for key, pc in variants + (("multilevel_jacobi", ng.PRECOND_MULTILEVEL),):
         best = None
         for _ in range(reps):
             info = ctx.solve(ng.default_solver_opts(tol=1e-8, max_iters=5000, check_every=10, precond=pc),
@@ -759,8 +791,9 @@ def multilevel_solves(ng, ctx, reps=2):
         out[key] = {"ms": 1e3 * best.seconds, "setup_ms": 1e3 * best.setup_seconds, "iterations": best.iterations,
                     "true_rel_res": best.true_rel_res, "status": best.status, "level_rows": rows,
                     "operator_complexity": sum(nnz) / nnz[0] if nnz else None}
-    out["learned_smoother_iteration_gain"] = out["multilevel_jacobi"]["iterations"] / max(
-        1, out["learned_multilevel"]["iterations"])
+    if learned:
+        out["learned_smoother_iteration_gain"] = out["multilevel_jacobi"]["iterations"] / max(
+            1, out["learned_multilevel"]["iterations"])
     return out
 
 
@@ -832,7 +865,41 @@ def bench_batch(ng, dev=0, n_problems=64, seed=2025, reps=2):
                           "max_true_rel_res": max(i.true_rel_res for i in linfos),
                           "all_converged": all(i.status == 0 for i in linfos), "training_s": train_s}
     out["learned_vs_plain_time"] = infos[0].seconds / lsolve
+    out.update(batch_multilevel(ng, ctx, off, asm_ms))
     ctx.close()
+    return out
+
+
+def batch_multilevel(ng, ctx, off, asm_ms):
+    """The whole batch as one block-diagonal system through the multilevel
+    flexible CG (aggregation never crosses problems: they share no
+    couplings).  The union tolerance is tightened to 0.9e-8 min_k ||b_k|| / ||b||
+    so that every problem meets 1e-8; each problem's true residual is checked
+    after the solve (FP64 SpMV on the device, norms per problem on the host)."""
+    import ctypes
+    n_rows = ctx.sizes()[0]
+    b = np.zeros(n_rows)
+    if ng.lib().nalu_linsys_copy(ctx.handle, None, b.ctypes.data_as(ctypes.c_void_p), 0) != 0:
+        raise RuntimeError("rhs copy failed")
+    seg = np.add.reduceat(b * b, off[:-1])
+    bk = np.sqrt(seg)
+    tol_u = 0.9e-8 * float(np.min(bk[bk > 0])) / float(np.linalg.norm(b))
+    out = {}
+    for key, pc in (("multilevel_jacobi_union", ng.PRECOND_MULTILEVEL),
+                    ("learned_multilevel_union", ng.PRECOND_LEARNED_MULTILEVEL)):
+        best = None
+        for _ in range(2):
+            info = ctx.solve(ng.default_solver_opts(tol=tol_u, max_iters=5000, check_every=10, precond=pc),
+                             raise_on_error=False)
+            if best is None or info.seconds < best.seconds:
+                best = info
+        x = ctx.solution()
+        r = b - ctx.spmv(x)
+        rk = np.sqrt(np.add.reduceat(r * r, off[:-1])) / np.where(bk > 0, bk, 1.0)
+        out[key] = {"solve_ms": 1e3 * best.seconds, "setup_ms": 1e3 * best.setup_seconds,
+                    "iterations": best.iterations, "union_tol": tol_u, "status": best.status,
+                    "max_problem_true_rel_res": float(np.max(rk)), "all_problems_converged": bool(np.all(rk <= 1e-8)),
+                    "problems_per_s": len(bk) / (asm_ms * 1e-3 + best.seconds)}
     return out
 
 
@@ -860,6 +927,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-solve", action="store_true")
+    ap.add_argument("--solve-set", default="all", choices=["all", "multilevel"],
+                    help="solves on the headline system: all, or the Jacobi-smoothed multigrid alone (profiling)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-problem batched workload")
     ap.add_argument("--no-c4", action="store_true", help="skip the 192^3 learned-vs-plain continuity solve")
