@@ -846,20 +846,26 @@ def bench_batch(ng, dev=0, n_problems=64, seed=2025, reps=2):
            "all_converged": all(i.status == 0 for i in infos), "preconditioner": "jacobi (plain PCG)"}
     # learned flexible CG on the same batch: weights trained on this union system
     # (20K PCG first-direction pairs, 4 seeded rhs, 40 epochs); the solve time
-    # includes the stencil set-up, the training is reported beside it
+    # includes the stencil set-up of the problems that try it, the training is
+    # reported beside it
     t0 = time.perf_counter()
     ctx.learned_init(7)
     st, rf, tg = ctx.learned_harvest(n_samples=20000, n_rhs=4, seed=2026)
     ctx.learned_train(st, rf, tg, epochs=40)
     train_s = time.perf_counter() - t0
-    linfos = ctx.solve_batched(ng.default_solver_opts(tol=1e-8, max_iters=40000, precond=ng.PRECOND_LEARNED),
+    linfos = None
+    for _ in range(reps):  # the same repetitions as the plain solve, fastest kept
+        li = ctx.solve_batched(ng.default_solver_opts(tol=1e-8, max_iters=40000, precond=ng.PRECOND_LEARNED),
                                raise_on_error=False)
+        if linfos is None or li[0].seconds < linfos[0].seconds:
+            linfos = li
     lits = sorted(i.iterations for i in linfos)
     lsolve = linfos[0].seconds
     out["learned_fcg"] = {"solve_ms": 1e3 * lsolve, "setup_ms": 1e3 * linfos[0].setup_seconds,
                           "problems_per_s": n_problems / (asm_ms * 1e-3 + lsolve),
                           "iterations_min_median_max": [lits[0], lits[len(lits) // 2], lits[-1]],
                           "problems_on_learned": int(sum(i.fallback == 0 for i in linfos)),
+                          "problems_with_learned_iterations": int(sum(i.learned_iterations > 0 for i in linfos)),
                           "problems_probe_chose_jacobi": int(sum(i.fallback == 2 for i in linfos)),
                           "problems_fell_back_after_stall": int(sum(i.fallback == 1 for i in linfos)),
                           "max_true_rel_res": max(i.true_rel_res for i in linfos),

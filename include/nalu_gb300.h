@@ -363,11 +363,13 @@ typedef struct nalu_solve_info {
   double true_rel_res;   /* FP64 ||b - A x|| / ||b|| */
   double seconds;        /* wall time of the whole call, set-up included */
   int fallback;          /* learned FCG: 0 it finished the solve; 1 it stalled or broke
-                            down and Chebyshev-Jacobi PCG finished; 2 Jacobi-CG
-                            finished, chosen by the opening probe (a short run of
-                            each method from the same start, compared per unit of
-                            device time) or because the learned FCG used twice the
-                            iterations the probe predicts for Jacobi-CG */
+                            down and Chebyshev-Jacobi PCG (batched: Jacobi-CG)
+                            finished; 2 Jacobi-CG finished, chosen by the opening
+                            probe (compared per unit of device time; batched: also
+                            a problem with too few iterations left to try the
+                            learned one, or whose batch's first trial lost) or
+                            because the learned FCG used twice the iterations the
+                            probe predicts for Jacobi-CG */
   int learned_iterations;/* iterations spent in the learned FCG (probe included);
                             iterations counts the probe runs too */
   double setup_seconds;  /* learned preconditioner set-up (MLP stencil + SELL values) */
@@ -391,9 +393,15 @@ int nalu_spmv(nalu_ctx* ctx, const double* x, double* y, int is_device);
  * batched solve below keeps separate scalars and a separate stop test per
  * problem.  No reference counterpart: Nalu solves one system per rank. */
 int nalu_set_problems(nalu_ctx* ctx, int n, const int64_t* node_offsets);
-/* Jacobi-preconditioned CG on every problem at once in one persistent
- * cooperative kernel (per-problem alpha/beta and convergence); infos[k]
- * receives problem k's iterations and true FP64 relative residual. */
+/* Jacobi-preconditioned CG on every problem at once (per-problem alpha/beta
+ * and convergence; CUDA-graph chunks of tile kernels over the union matrix);
+ * infos[k] receives problem k's iterations and true FP64 relative residual.
+ * With NALU_PRECOND_LEARNED a problem changes method in place between chunks,
+ * without a restart of the others or a discarded iteration: with the probe on,
+ * every problem opens with Jacobi-CG; only problems with many predicted
+ * iterations left are candidates, and the learned preconditioner is set up
+ * (rows of that problem only) and tried on the largest one first; the others
+ * follow only if it beats its own Jacobi-CG rate per unit of device time. */
 int nalu_solve_batched(nalu_ctx* ctx, const nalu_solver_opts* opts, nalu_solve_info* infos);
 
 /* ---- learned preconditioner -------------------------------------------- */

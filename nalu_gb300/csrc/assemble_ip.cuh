@@ -78,13 +78,19 @@ constexpr int kFacRow = 9;             // factors of one ip: 8 (+1 pad)
 constexpr int kFacStride = 12 * kFacRow + 1;
 
 // registers the launch bounds allow per thread: 65536 / (12 EPB * blocks per
-// SM): 8 elements per block at 8 blocks (85 registers, 24 warps per SM), 16 at
-// 5 blocks (68 registers, 30 warps): two register budgets for the autotuner
-template <int EPB>
+// SM).  The standard kernels (LIGHT) run at 40 registers and 48 warps per SM
+// (continuity: an 8-byte spill; measured fastest at 128^3, 5% ahead of 64
+// registers); the continuity variants with the pressure-stabilisation
+// difference or shifted gradients (MODE 1, 2) and the shifted diffusion hold
+// more live state and keep 85 (8 elements per block) or 64 registers (16),
+// which they fill without spilling more than a word.
+template <int EPB, bool LIGHT>
 struct IpSched {
   static constexpr int kThreads = 12 * EPB;
-  static constexpr int kMinBlocks = EPB == 8 ? 8 : 5;
+  static constexpr int kMinBlocks = EPB == 8 ? (LIGHT ? 16 : 8) : (LIGHT ? 7 : 5);
 };
+template <int KIND, int MODE, bool SHIFT>
+constexpr bool ip_light() { return MODE == 0 && !(KIND == 0 && SHIFT); }
 
 // J' columns at the ip (rotated frame: column 0 = normal axis dd, 1 = t1,
 // 2 = t2), from the edge form in shared memory.  s1, s2: ip coordinates along
@@ -146,7 +152,8 @@ __device__ __forceinline__ df64 trilinear_rot_df(const df64* c, int t1, int t2, 
 }
 
 template <int EPB, int KIND, int MODE, bool SHIFT, bool SMDOT>
-__global__ void __launch_bounds__(IpSched<EPB>::kThreads, IpSched<EPB>::kMinBlocks)
+__global__ void __launch_bounds__(IpSched<EPB, ip_light<KIND, MODE, SHIFT>()>::kThreads,
+                                 IpSched<EPB, ip_light<KIND, MODE, SHIFT>()>::kMinBlocks)
     k_assemble_ip_df(AsmArgsDF a) {
   constexpr int NCOMP = KIND == 0 ? 1 : 3;
   __shared__ df64 s_ef[EPB][kEfStride];
@@ -373,7 +380,7 @@ void launch_ip_variant(nalu_ctx* ctx, AsmArgsDF a, int out) {
   if (a.count <= 0) return;
   a.out = out;
   const unsigned grid = (unsigned)((a.count + EPB - 1) / EPB);
-  k_assemble_ip_df<EPB, KIND, MODE, SHIFT, SMDOT><<<grid, IpSched<EPB>::kThreads, 0, ctx->stream>>>(a);
+  k_assemble_ip_df<EPB, KIND, MODE, SHIFT, SMDOT><<<grid, 12 * EPB, 0, ctx->stream>>>(a);
   ctx->launches++;
 }
 

@@ -43,6 +43,14 @@ constexpr int kRowsPerThread = 4;         // a tile's fixed costs (block sums, t
 constexpr int kTileRows = kRowsPerThread * kBT;
 constexpr int kSliceB = 32;
 
+struct GraphExecs {
+  cudaGraphExec_t e[2] = {nullptr, nullptr};
+  ~GraphExecs() {
+    for (auto x : e)
+      if (x) cudaGraphExecDestroy(x);
+  }
+};
+
 struct TileArgs {
   int64_t n;
   int P, ntiles;
@@ -217,10 +225,8 @@ __global__ void __launch_bounds__(kBT) k_bt_axpy(TileArgs a) {
   if (problem_reduce<2>(a, t, pr, v, tot, sh) && threadIdx.x == 0) {
     const bool learned = a.mode[pr] == 1;
     const double be = learned ? 0.0 : tot[0] / a.rz[pr];
-    if (!learned) {
-      a.beta[pr] = be;
-      a.rz[pr] = tot[0];
-    }
+    if (!learned) a.beta[pr] = be;
+    a.rz[pr] = tot[0];  // kept in learned mode too: a problem may change to Jacobi-CG in place
     a.rr[pr] = tot[1];
     a.iters[pr] += 1;
     a.kiter[pr] += 1;
@@ -331,9 +337,9 @@ int solve_batched(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* inf
     return set_error(ctx, NALU_ERR_ARG, "the learned preconditioner runs in FP64 flexible CG only");
   double setup_s = 0.0;
   if (learned) {
-    const auto ts = std::chrono::steady_clock::now();
-    if ((rc = learned_prepare(ctx))) return rc;
-    setup_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - ts).count();
+    LearnedState& L = ctx->learned;
+    if (!L.has_weights) return set_error(ctx, NALU_ERR_STATE, "learned preconditioner has no weights");
+    if (L.wsell.n < s.sell.stored) NALU_CUDA(ctx, L.wsell.alloc(s.sell.stored));
   }
   DBuf<int32_t> d_ints;  // trows | tprob | pt0 | pt1 | done | iters | mode | kiter | liters
   DBuf<double> d_dbl;    // tpart[2 ntiles] | tb[ntiles] | alpha beta rz rr stop2 [P] | sums [3P]
@@ -376,7 +382,7 @@ int solve_batched(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* inf
   NALU_CUDA(ctx, cudaMemcpyAsync(pt1_d, pt1.data(), sizeof(int32_t) * P, cudaMemcpyHostToDevice, st));
   NALU_CUDA(ctx, cudaMemsetAsync(iters_d, 0, sizeof(int32_t) * P, st));
   NALU_CUDA(ctx, cudaMemsetAsync(liters_d, 0, sizeof(int32_t) * P, st));
-  std::vector<int32_t> mode(P, learned ? 1 : 0), fallback(P, 0);
+  std::vector<int32_t> mode(P, 0), fallback(P, learned ? 2 : 0);
   NALU_CUDA(ctx, cudaMemsetAsync(d_cnt.p, 0, sizeof(unsigned) * P, st));
   k_to_float<<<1024, 256, 0, st>>>(n, s.dinv.p, dinvf.p);
   k_batch_prep<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, ctx->d_bcmask.p, ctx->d_rhs.p, ctx->d_x.p,
@@ -419,7 +425,7 @@ int solve_batched(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* inf
   a.stop2 = stop2_d;
   a.done = done_d;
   a.iters = iters_d;
-  a.wsell = learned ? ctx->learned.wsell.p : nullptr;
+  a.wsell = learned ? ctx->learned.wsell.p : nullptr;  // rows set up problem by problem
   a.z = zbuf.p;
   a.mode = mode_d;
   a.pq = pq_d;
@@ -427,32 +433,37 @@ int solve_batched(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* inf
   a.liters = liters_d;
 
   const int chunk = o.check_every > 0 ? o.check_every : 25;
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
-  cudaError_t ce = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
-  if (ce != cudaSuccess) return cuda_check(ctx, ce, "begin capture");
-  for (int k = 0; k < chunk; ++k) {
-    if (learned) k_bt_prec<<<ntiles, kBT, 0, st>>>(a);
-    k_bt_pupdate<<<ntiles, kBT, 0, st>>>(a);
-    k_bt_spmv<<<ntiles, kBT, 0, st>>>(a);
-    k_bt_axpy<<<ntiles, kBT, 0, st>>>(a);
-  }
-  ce = cudaStreamEndCapture(st, &graph);
-  if (ce != cudaSuccess) return cuda_check(ctx, ce, "end capture");
-  ce = cudaGraphInstantiate(&exec, graph, 0);
-  if (ce != cudaSuccess) {
+  // two graphs of `chunk` iterations: Jacobi-CG only (three kernels an
+  // iteration) and with the learned stencil apply (four); the second runs only
+  // while some unfinished problem is in learned mode
+  GraphExecs gx;
+  auto capture = [&](bool with_prec, cudaGraphExec_t* out) -> int {
+    cudaGraph_t graph = nullptr;
+    cudaError_t ce = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+    if (ce != cudaSuccess) return cuda_check(ctx, ce, "begin capture");
+    for (int k = 0; k < chunk; ++k) {
+      if (with_prec) k_bt_prec<<<ntiles, kBT, 0, st>>>(a);
+      k_bt_pupdate<<<ntiles, kBT, 0, st>>>(a);
+      k_bt_spmv<<<ntiles, kBT, 0, st>>>(a);
+      k_bt_axpy<<<ntiles, kBT, 0, st>>>(a);
+    }
+    ce = cudaStreamEndCapture(st, &graph);
+    if (ce != cudaSuccess) return cuda_check(ctx, ce, "end capture");
+    ce = cudaGraphInstantiate(out, graph, 0);
     cudaGraphDestroy(graph);
-    return cuda_check(ctx, ce, "instantiate");
-  }
+    return ce == cudaSuccess ? NALU_OK : cuda_check(ctx, ce, "instantiate");
+  };
+  if ((rc = capture(false, &gx.e[0]))) return rc;
+  if (learned && (rc = capture(true, &gx.e[1]))) return rc;
 
   std::vector<double> sums(3 * P);
   std::vector<int32_t> done(P), iters(P);
   std::vector<double> true_res(P, 0.0), r0(P, 0.0);
   const int window = o.stall_window > 0 ? o.stall_window : 20;
   // one round: true residual r = b - A x (FP64), Jacobi r.z and ||b|| per
-  // problem, then the per-problem start of CG; returns true when every
-  // problem already meets the tolerance
-  auto start_round = [&](bool apply_breakdowns) -> int {
+  // problem, then the per-problem start of CG (or flexible CG, per mode);
+  // returns 1 when every problem already meets the tolerance
+  auto start_round = [&]() -> int {
     k_batch_resid<<<ntiles, kBT, 0, st>>>(a, ctx->d_rowptr.p, ctx->d_colind.p, ctx->d_values.p, ctx->d_rhs.p, tb);
     k_batch_sums<<<std::min(P, 1024), kBT, 0, st>>>(tpart, tpart + ntiles, tb, pt0_d, pt1_d, P, sums_d);
     ctx->launches += 2;
@@ -465,10 +476,6 @@ int solve_batched(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* inf
       const double bref = bnorm > 0 ? bnorm : 1.0;
       r0[pr] = std::sqrt(sums[P + pr]);
       true_res[pr] = r0[pr] / bref;
-      if (apply_breakdowns && done[pr] == 3) {  // learned FCG stopped: Jacobi-CG from here
-        mode[pr] = 0;
-        fallback[pr] = 2;
-      }
       done[pr] = true_res[pr] <= o.tol ? 1 : 0;
       all = all && done[pr];
       stop2[pr] = std::pow(0.5 * o.tol * bref, 2);
@@ -483,39 +490,189 @@ int solve_batched(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* inf
     NALU_CUDA(ctx, cudaMemcpyAsync(mode_d, mode.data(), sizeof(int32_t) * P, cudaMemcpyHostToDevice, st));
     return 0;
   };
-  // CG on the current residual for at most max_its iterations; x is updated in
-  // place.  A learned problem whose residual norm has no new minimum for
-  // max(stall_window, 4 x the age of its minimum) iterations stops and
-  // continues with Jacobi-CG after the restart (the single-system rule).
-  std::vector<double> rrh(P);
-  std::vector<int> pace(P, 0);  // learned problems: iteration budget from the Jacobi probe (0: none)
-  auto run_chunks = [&](int max_its, bool stall_test) -> int {
-    std::vector<double> best(P, INFINITY);
-    std::vector<int> best_it(P, 0);
+
+  // ---- the learned preconditioner, problem by problem --------------------
+  // A problem changes method in place between chunks (no restart of the
+  // others, no iteration discarded): to learned FCG with kiter = 0 (its next
+  // step is p = M r), to Jacobi-CG with beta = 0 (p = D^-1 r; r.D^-1 r is kept
+  // by every iteration).  With the probe on, the round opens with `probe`
+  // iterations of Jacobi-CG for all problems; their rates predict each
+  // problem's remaining Jacobi-CG iterations.  Only problems with at least
+  // kLearnedMinRemaining x probe of them left are candidates (the learned
+  // set-up and probe cannot pay off on the rest), and the candidate with the
+  // most remaining row-iterations alone is set up and run `probe` iterations
+  // in learned mode while the others continue Jacobi-CG.  From the two phases'
+  // device times, the cost of a learned row-iteration over a Jacobi one
+  // (kappa) follows; the learned FCG wins when its residual reduction per
+  // unit of time beats the problem's own Jacobi-CG rate.  If it loses, the
+  // problem changes back and no other problem is set up.  If it wins, every
+  // other candidate is set up and changes; each is judged the same way after
+  // its own `probe` learned iterations.  A learned problem also changes back
+  // when its residual stalls (no new minimum for max(window, 10 x the
+  // iterations taken to reach it)), when its learned iterations pass twice the
+  // predicted Jacobi-CG count, or when its step breaks down.
+  constexpr int kLearnedMinRemaining = 4;
+  const int probe = chunk * std::max(1, (std::max(40, 2 * window) + chunk - 1) / chunk);
+  std::vector<int64_t> prow0(P), prow1(P);
+  for (int pr = 0; pr < P; ++pr) {
+    prow0[pr] = ctx->problem_offsets[pr] * nd;
+    prow1[pr] = ctx->problem_offsets[pr + 1] * nd;
+  }
+  std::vector<double> rrh(P), lres0(P, 0.0), best(P, INFINITY), rate_j(P, 0.0), rate_l(P, 0.0), remain_j(P, 0.0);
+  std::vector<int> lit(P, 0), best_it(P, 0), pace(P, 0);
+  std::vector<char> prepared(P, 0), judged(P, 0), candidate(P, 0);
+  double kappa = 1.0, u_j = 0.0;  // learned / Jacobi cost per row-iteration; ms per Jacobi row-iteration
+  auto set_mode = [&](int pr, int m) -> int {
+    mode[pr] = m;
+    const int32_t zi = 0;
+    const double zd = 0.0;
+    NALU_CUDA(ctx, cudaMemcpyAsync(mode_d + pr, &mode[pr], sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    NALU_CUDA(ctx, cudaMemcpyAsync(kiter_d + pr, &zi, sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    NALU_CUDA(ctx, cudaMemcpyAsync(beta_d + pr, &zd, sizeof(double), cudaMemcpyHostToDevice, st));
+    if (done[pr] == 3) {
+      done[pr] = 0;
+      NALU_CUDA(ctx, cudaMemcpyAsync(done_d + pr, &done[pr], sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    }
+    return NALU_OK;
+  };
+  auto to_learned = [&](int pr) -> int {
+    if (!prepared[pr]) {
+      const auto ts = std::chrono::steady_clock::now();
+      int r = learned_prepare_rows(ctx, prow0[pr], prow1[pr]);
+      if (r) return r;
+      NALU_CUDA(ctx, cudaStreamSynchronize(st));
+      setup_s += std::chrono::duration<double>(std::chrono::steady_clock::now() - ts).count();
+      prepared[pr] = 1;
+    }
+    lit[pr] = 0;
+    lres0[pr] = std::sqrt(std::max(rrh[pr], 0.0));
+    best[pr] = lres0[pr];
+    best_it[pr] = 0;
+    fallback[pr] = 0;
+    return set_mode(pr, 1);
+  };
+  auto to_jacobi = [&](int pr, int why) -> int {
+    fallback[pr] = why;
+    return set_mode(pr, 0);
+  };
+  // learned rate (ln residual reduction per iteration) since the change
+  auto learned_rate = [&](int pr) {
+    return std::log(std::max(std::sqrt(std::max(rrh[pr], 0.0)), 1e-300) / std::max(lres0[pr], 1e-300)) /
+           std::max(lit[pr], 1);
+  };
+  auto learned_wins = [&](int pr) { return done[pr] != 3 && rate_l[pr] < kappa * rate_j[pr]; };
+  auto rows_active = [&](int m) {
+    int64_t s0 = 0;
+    for (int pr = 0; pr < P; ++pr)
+      if (!done[pr] && (m < 0 || mode[pr] == m)) s0 += prow1[pr] - prow0[pr];
+    return s0;
+  };
+  cudaEvent_t pe[2];
+  for (auto& e : pe) NALU_CUDA(ctx, cudaEventCreate(&e));
+  struct EvFree {
+    cudaEvent_t* e;
+    ~EvFree() { cudaEventDestroy(e[0]); cudaEventDestroy(e[1]); }
+  } evfree{pe};
+  enum Phase { kJacobiProbe, kLearnedProbe, kDecided };
+  Phase phase = (learned && o.learned_probe) ? kJacobiProbe : kDecided;
+  int rep = -1;
+  double rows_a = 0.0, rows_bj = 0.0, rows_bl = 0.0;  // row-iterations of the two timed phases
+
+  // one round of at most max_its iterations; x is updated in place
+  auto run_round = [&](int max_its) -> int {
+    int phase_it = 0;
+    if (phase != kDecided) NALU_CUDA(ctx, cudaEventRecord(pe[0], st));
     for (int it = 0; it < max_its; it += chunk) {
-      cudaGraphLaunch(exec, st);
-      ctx->launches += (learned ? 4 : 3) * chunk;
+      const bool any_learned = learned && rows_active(1) > 0;
+      if (phase == kJacobiProbe) rows_a += (double)rows_active(-1) * chunk;
+      if (phase == kLearnedProbe) {
+        rows_bj += (double)rows_active(0) * chunk;
+        rows_bl += (double)rows_active(1) * chunk;
+      }
+      cudaGraphLaunch(gx.e[any_learned ? 1 : 0], st);
+      ctx->launches += (any_learned ? 4 : 3) * chunk;
       NALU_CUDA(ctx, cudaMemcpyAsync(done.data(), done_d, sizeof(int32_t) * P, cudaMemcpyDeviceToHost, st));
       NALU_CUDA(ctx, cudaMemcpyAsync(rrh.data(), rr_d, sizeof(double) * P, cudaMemcpyDeviceToHost, st));
+      if (phase != kDecided) NALU_CUDA(ctx, cudaEventRecord(pe[1], st));
       NALU_CUDA(ctx, cudaStreamSynchronize(st));
-      const int now = it + chunk;
-      for (int pr = 0; pr < P && stall_test; ++pr) {
-        if (done[pr] != 0 || mode[pr] != 1) continue;
-        const double res = std::sqrt(rrh[pr]);
-        bool stop = pace[pr] > 0 && now > pace[pr];  // behind Jacobi-CG's pace
-        if (res < 0.999 * best[pr]) {
-          best[pr] = res;
-          best_it[pr] = now;
-        } else if (now - best_it[pr] > std::max(window, 10 * best_it[pr])) {
-          stop = true;
+      phase_it += chunk;
+      for (int pr = 0; pr < P; ++pr)
+        if (mode[pr] == 1 && (done[pr] == 0 || done[pr] == 3)) lit[pr] += chunk;
+      const bool all_done = std::all_of(done.begin(), done.end(), [](int d) { return d == 1 || d == 2; });
+      if (phase == kJacobiProbe && (phase_it >= probe || all_done)) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, pe[0], pe[1]);
+        u_j = rows_a > 0 ? ms / rows_a : 0.0;
+        double best_work = -1.0;
+        for (int pr = 0; pr < P; ++pr) {
+          if (done[pr]) continue;
+          const double res = std::sqrt(std::max(rrh[pr], 0.0));
+          const double stop = 0.5 * o.tol * std::sqrt(std::max(sums[2 * P + pr], 0.0));
+          rate_j[pr] = std::log(std::max(res, 1e-300) / std::max(r0[pr], 1e-300)) / phase_it;
+          remain_j[pr] = rate_j[pr] < 0.0 ? std::log(std::max(stop, 1e-300) / std::max(res, 1e-300)) / rate_j[pr]
+                                          : INFINITY;
+          if (remain_j[pr] < (double)kLearnedMinRemaining * probe) continue;
+          candidate[pr] = 1;
+          pace[pr] = (int)std::min(2.0 * remain_j[pr], 2.0e9);
+          const double work = std::min(remain_j[pr], 1e12) * (double)(prow1[pr] - prow0[pr]);
+          if (work > best_work) {
+            best_work = work;
+            rep = pr;
+          }
         }
-        if (stop) {
-          done[pr] = 3;
-          NALU_CUDA(ctx, cudaMemcpyAsync(done_d + pr, &done[pr], sizeof(int32_t), cudaMemcpyHostToDevice, st));
+        phase = kDecided;
+        if (rep >= 0) {
+          if ((rc = to_learned(rep))) return rc;
+          phase = kLearnedProbe;
+          phase_it = 0;
+          NALU_CUDA(ctx, cudaEventRecord(pe[0], st));
+        }
+      } else if (phase == kLearnedProbe && (phase_it >= probe || done[rep] != 0 || all_done)) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, pe[0], pe[1]);
+        if (rows_bl > 0 && u_j > 0)
+          kappa = std::min(10.0, std::max(1.0, 1.0 + (ms - u_j * (rows_bj + rows_bl)) / (u_j * rows_bl)));
+        rate_l[rep] = learned_rate(rep);
+        judged[rep] = 1;
+        phase = kDecided;
+        if (!learned_wins(rep)) {
+          if (done[rep] == 0 || done[rep] == 3) {
+            if ((rc = to_jacobi(rep, 2))) return rc;
+          } else {
+            fallback[rep] = 2;
+          }
+        } else {
+          for (int pr = 0; pr < P; ++pr)
+            if (candidate[pr] && pr != rep && !done[pr] && (rc = to_learned(pr))) return rc;
+        }
+      } else if (phase == kDecided && learned) {
+        for (int pr = 0; pr < P; ++pr) {
+          if (mode[pr] != 1 || done[pr] == 1 || done[pr] == 2) continue;
+          if (done[pr] == 3) {  // the learned step was not positive: Jacobi-CG from here
+            if ((rc = to_jacobi(pr, 1))) return rc;
+            continue;
+          }
+          const double res = std::sqrt(std::max(rrh[pr], 0.0));
+          if (o.learned_probe && !judged[pr] && lit[pr] >= probe) {
+            rate_l[pr] = learned_rate(pr);
+            judged[pr] = 1;
+            if (!learned_wins(pr)) {
+              if ((rc = to_jacobi(pr, 2))) return rc;
+              continue;
+            }
+          }
+          const bool behind = pace[pr] > 0 && lit[pr] > pace[pr];  // behind Jacobi-CG's pace
+          bool stalled = false;
+          if (res < 0.999 * best[pr]) {
+            best[pr] = res;
+            best_it[pr] = lit[pr];
+          } else if (lit[pr] - best_it[pr] > std::max(window, 10 * best_it[pr])) {
+            stalled = true;
+          }
+          if ((behind || stalled) && (rc = to_jacobi(pr, behind ? 2 : 1))) return rc;
         }
       }
-      NALU_CUDA(ctx, cudaStreamSynchronize(st));
-      if (std::all_of(done.begin(), done.end(), [](int d) { return d != 0; })) break;
+      if (all_done) break;
     }
     // the round's increment into the FP64 solution
     k_batch_fold<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, a.x2, a.x);
@@ -523,59 +680,22 @@ int solve_batched(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* inf
     return cuda_check(ctx, cudaGetLastError(), "batch fold");
   };
 
-  if (learned && o.learned_probe) {
-    // probe: a short run of Jacobi-CG and of the learned FCG from the same
-    // start; each problem keeps the method that reduced its residual faster
-    // per unit of device time (the batch's time per iteration of each method)
-    DBuf<double> x0;
-    NALU_CUDA(ctx, x0.alloc(n));
-    NALU_CUDA(ctx, cudaMemcpyAsync(x0.p, ctx->d_x.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
-    const int probe = chunk * std::max(1, (std::max(40, 2 * window) + chunk - 1) / chunk);
-    std::vector<double> res[2];
-    float ms[2] = {0.f, 0.f};
-    cudaEvent_t pe[2];
-    for (auto& e : pe) NALU_CUDA(ctx, cudaEventCreate(&e));
-    bool trivial = false;
-    for (int m = 0; m < 2 && !trivial; ++m) {
-      std::fill(mode.begin(), mode.end(), m);
-      NALU_CUDA(ctx, cudaMemcpyAsync(ctx->d_x.p, x0.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
-      if (start_round(false)) {
-        trivial = true;
-        break;
-      }
-      NALU_CUDA(ctx, cudaEventRecord(pe[0], st));
-      int rcp = run_chunks(probe, false);
-      if (rcp) return rcp;
-      NALU_CUDA(ctx, cudaEventRecord(pe[1], st));
-      NALU_CUDA(ctx, cudaEventSynchronize(pe[1]));
-      cudaEventElapsedTime(&ms[m], pe[0], pe[1]);
-      res[m].resize(P);
-      for (int pr = 0; pr < P; ++pr)
-        res[m][pr] = done[pr] == 3 ? INFINITY : std::sqrt(std::max(rrh[pr], 0.0));
-    }
-    for (auto& e : pe) cudaEventDestroy(e);
-    for (int pr = 0; pr < P && !trivial; ++pr) {
-      const double lj = std::log(std::max(res[0][pr], 1e-300) / std::max(r0[pr], 1e-300));
-      const double rj = lj / std::max(ms[0], 1e-3f);
-      const double rl = std::log(std::max(res[1][pr], 1e-300) / std::max(r0[pr], 1e-300)) / std::max(ms[1], 1e-3f);
-      mode[pr] = rl < rj ? 1 : 0;
-      if (!mode[pr]) fallback[pr] = 2;
-      // iterations Jacobi-CG would need (probe rate extrapolated); the learned
-      // FCG gets at most twice as many before the problem changes to Jacobi-CG
-      if (lj < 0.0) pace[pr] = (int)std::min(2.0 * probe * std::log(0.5 * o.tol) / lj + probe, 2.0e9);
-    }
-    NALU_CUDA(ctx, cudaMemcpyAsync(ctx->d_x.p, x0.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+  if (learned && !o.learned_probe) {  // every problem in learned mode from the start
+    if ((rc = learned_prepare_rows(ctx, 0, n))) return rc;
+    std::fill(prepared.begin(), prepared.end(), 1);
+    std::fill(mode.begin(), mode.end(), 1);
+    std::fill(fallback.begin(), fallback.end(), 0);
   }
   for (int outer = 0; outer < 6; ++outer) {
-    if (start_round(outer > 0)) break;
-    int rcr = run_chunks(o.max_iters, learned);
+    if (start_round()) break;
+    if (outer == 0 && learned && !o.learned_probe)
+      for (int pr = 0; pr < P; ++pr) lres0[pr] = best[pr] = r0[pr];
+    int rcr = run_round(o.max_iters);
     if (rcr) return rcr;
     if (std::any_of(done.begin(), done.end(), [](int d) { return d == 2; })) break;
   }
   std::vector<int32_t> liters(P, 0);
   NALU_CUDA(ctx, cudaMemcpyAsync(liters.data(), liters_d, sizeof(int32_t) * P, cudaMemcpyDeviceToHost, st));
-  cudaGraphExecDestroy(exec);
-  cudaGraphDestroy(graph);
   NALU_CUDA(ctx, cudaMemcpyAsync(iters.data(), iters_d, sizeof(int32_t) * P, cudaMemcpyDeviceToHost, st));
   NALU_CUDA(ctx, cudaStreamSynchronize(st));
   const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -589,6 +709,10 @@ int solve_batched(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* inf
     infos[pr].fallback = fallback[pr];
     infos[pr].learned_iterations = liters[pr];
     infos[pr].setup_seconds = setup_s;
+    // probe rates as ln(residual reduction) per ms of this problem's iterations
+    const double ms_it = u_j * (double)(prow1[pr] - prow0[pr]);
+    if (ms_it > 0.0 && rate_j[pr] != 0.0) infos[pr].probe_rate_jacobi = rate_j[pr] / ms_it;
+    if (ms_it > 0.0 && judged[pr]) infos[pr].probe_rate_learned = rate_l[pr] / (kappa * ms_it);
     infos[pr].status = true_res[pr] <= o.tol ? NALU_OK : (done[pr] == 2 ? NALU_ERR_NONFINITE : NALU_ERR_NOT_CONVERGED);
     all_ok = all_ok && infos[pr].status == NALU_OK;
   }

@@ -103,6 +103,7 @@ struct LearnedState {
   DBuf<int32_t> nbr;                          // [n][27] neighbour LID per topological slot, -1 if none
   DBuf<float> stencil;                        // [n][27] MLP output per slot
   DBuf<float> wsell;                          // preconditioner values on the SELL pattern of A
+  DBuf<float> srow;                           // [n] row factors of the SPD safeguard (set-up scratch)
   DBuf<uint16_t> wsell16;                     // the same as BF16 (wide slices of the stencil apply)
   DBuf<uint32_t> wpack;                       // BF16 value << 16 | 16-bit column offset, per SELL entry
   int64_t nbr_nodes = 0;                      // mesh size the slot map was built for
@@ -289,6 +290,9 @@ template <class VT>
 int sell_build(nalu_ctx* ctx, SellMatrix& S, const VT** vals_out);
 // learned.cu
 int learned_prepare(nalu_ctx* ctx);
+// the learned preconditioner's FP32 values (wsell) of rows [row0, row1) only;
+// the rows' neighbours in A must lie in the same range (a problem of a batch)
+int learned_prepare_rows(nalu_ctx* ctx, int64_t row0, int64_t row1);
 // aggregation multigrid (multilevel.cu): the hierarchy for the current scalar
 // matrix; flexible CG with it on the residual r (in place) for the correction
 // x; the hierarchy's level sizes; its release

@@ -222,7 +222,7 @@ constexpr int kStWarpFloats = 148;  // 81 static features (+3 pad) + 64 layer-1 
 constexpr size_t kStSmem = sizeof(float) * (81 * 64 + 27 * 64 + 4 * 64 + 8) + sizeof(uint16_t) * 2 * 64 * kWStride +
                            sizeof(float) * kStWarps * kStWarpFloats;
 
-__global__ void __launch_bounds__(kStThreads) k_mlp_stencil(int64_t n, const float* __restrict__ P,
+__global__ void __launch_bounds__(kStThreads) k_mlp_stencil(int64_t row0, int64_t row1, const float* __restrict__ P,
                                                             const uint16_t* __restrict__ wbf,
                                                             const int32_t* __restrict__ nbr,
                                                             const int64_t* __restrict__ rp,
@@ -262,7 +262,7 @@ __global__ void __launch_bounds__(kStThreads) k_mlp_stencil(int64_t n, const flo
   float* st = wsp + warp * kStWarpFloats;
   float* hs = st + 84;
   const float b4 = bb[256];
-  for (int64_t i = (int64_t)blockIdx.x * kStWarps + warp; i < n; i += (int64_t)gridDim.x * kStWarps) {
+  for (int64_t i = row0 + (int64_t)blockIdx.x * kStWarps + warp; i < row1; i += (int64_t)gridDim.x * kStWarps) {
     if (idmask[i]) {  // warp-uniform
       if (lane < 27) out[i * 27 + lane] = 0.0f;
       continue;
@@ -337,13 +337,13 @@ __global__ void k_prep_wbf(const float* __restrict__ P, uint16_t* __restrict__ w
 // Preconditioner values on A's SELL-32 pattern: the symmetric part of
 // D^-1 (I + C).  Identity rows keep 1 on the diagonal and nothing else;
 // columns of identity rows are dropped.
-__global__ void k_precond_sell(int64_t n, const int64_t* __restrict__ rp, const int64_t* __restrict__ sptr,
+__global__ void k_precond_sell(int64_t row0, int64_t row1, const int64_t* __restrict__ rp, const int64_t* __restrict__ sptr,
                                const int32_t* __restrict__ slen, const int32_t* __restrict__ scol,
                                const int32_t* __restrict__ nbr, const float* __restrict__ c,
                                const double* __restrict__ dinv, const uint8_t* __restrict__ idmask,
                                float* __restrict__ w) {
-  const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (row >= n) return;
+  const int64_t row = row0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= row1) return;
   const int64_t s = row / kSlice;
   const int64_t base = sptr[s] + row % kSlice;
   const int len = slen[s];
@@ -382,11 +382,11 @@ __global__ void k_precond_sell(int64_t n, const int64_t* __restrict__ rp, const 
 constexpr float kSpdTheta = 0.95f;
 constexpr float kSpdDiagFloor = 0.25f;
 
-__global__ void k_precond_rowscale(int64_t n, const int64_t* __restrict__ sptr, const int32_t* __restrict__ slen,
+__global__ void k_precond_rowscale(int64_t row0, int64_t row1, const int64_t* __restrict__ sptr, const int32_t* __restrict__ slen,
                                    const int32_t* __restrict__ scol, float* __restrict__ w,
                                    const double* __restrict__ dinv, float* __restrict__ srow) {
-  const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (row >= n) return;
+  const int64_t row = row0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= row1) return;
   const int64_t base = sptr[row / kSlice] + row % kSlice;
   const int len = slen[row / kSlice];
   const float di = (float)dinv[row];
@@ -422,11 +422,11 @@ __global__ void k_precond_rowscale(int64_t n, const int64_t* __restrict__ sptr, 
   srow[row] = sc;
 }
 
-__global__ void k_precond_apply_scale(int64_t n, const int64_t* __restrict__ sptr, const int32_t* __restrict__ slen,
+__global__ void k_precond_apply_scale(int64_t row0, int64_t row1, const int64_t* __restrict__ sptr, const int32_t* __restrict__ slen,
                                       const int32_t* __restrict__ scol, float* __restrict__ w,
                                       const float* __restrict__ srow) {
-  const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (row >= n) return;
+  const int64_t row = row0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= row1) return;
   const int64_t base = sptr[row / kSlice] + row % kSlice;
   const int len = slen[row / kSlice];
   const float si = srow[row];
@@ -872,17 +872,19 @@ int build_slot_map(nalu_ctx* ctx) {
   return cuda_check(ctx, cudaGetLastError(), "slot map");
 }
 
-int launch_stencil(nalu_ctx* ctx) {
+// the stencil of rows [row0, row1) (all rows by default)
+int launch_stencil(nalu_ctx* ctx, int64_t row0 = 0, int64_t row1 = -1) {
   LearnedState& L = ctx->learned;
   const int64_t n = ctx->n_rows;
+  if (row1 < 0) row1 = n;
   if (L.stencil.n < n * 27) NALU_CUDA(ctx, L.stencil.alloc(n * 27));
   k_prep_wbf<<<(2 * 64 * kWStride + 255) / 256, 256, 0, ctx->stream>>>(L.params.p, L.wbf.p);
   NALU_CUDA(ctx, cudaFuncSetAttribute(k_mlp_stencil, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStSmem));
   int per_sm = 0;
   NALU_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mlp_stencil, kStThreads, kStSmem));
-  const int64_t need = (n + kStWarps - 1) / kStWarps;
+  const int64_t need = (row1 - row0 + kStWarps - 1) / kStWarps;
   const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)std::max(1, per_sm) * ctx->sm_count));
-  k_mlp_stencil<<<grid, kStThreads, kStSmem, ctx->stream>>>(n, L.params.p, L.wbf.p, L.nbr.p, ctx->d_rowptr.p,
+  k_mlp_stencil<<<grid, kStThreads, kStSmem, ctx->stream>>>(row0, row1, L.params.p, L.wbf.p, L.nbr.p, ctx->d_rowptr.p,
                                                            ctx->d_colind.p, ctx->d_values.p, ctx->sw.dinv.p,
                                                            ctx->d_bcmask.p, L.stencil.p);
   ctx->launches += 2;
@@ -956,26 +958,37 @@ void backward(nalu_ctx* ctx, TrainWork& w, const float* P, float* G) {
 
 }  // namespace
 
-int learned_prepare(nalu_ctx* ctx) {
+int learned_prepare_rows(nalu_ctx* ctx, int64_t row0, int64_t row1) {
   int rc = check_scalar(ctx);
   if (rc) return rc;
   LearnedState& L = ctx->learned;
   if (!L.has_weights) return set_error(ctx, NALU_ERR_STATE, "learned preconditioner has no weights");
-  if ((rc = build_slot_map(ctx))) return rc;
-  if ((rc = launch_stencil(ctx))) return rc;
-  const SellMatrix& S = ctx->sw.sell;
   const int64_t n = ctx->n_rows;
+  if (row0 < 0 || row1 > n || row0 >= row1) return set_error(ctx, NALU_ERR_ARG, "learned set-up: bad row range");
+  if ((rc = build_slot_map(ctx))) return rc;
+  if ((rc = launch_stencil(ctx, row0, row1))) return rc;
+  const SellMatrix& S = ctx->sw.sell;
   if (L.wsell.n < S.stored) NALU_CUDA(ctx, L.wsell.alloc(S.stored));
-  const unsigned g = (unsigned)((n + 255) / 256);
-  k_precond_sell<<<g, 256, 0, ctx->stream>>>(n, ctx->d_rowptr.p, S.ptr.p, S.len.p, S.col.p, L.nbr.p, L.stencil.p,
-                                             ctx->sw.dinv.p, ctx->d_bcmask.p, L.wsell.p);
-  DBuf<float> srow;
-  NALU_CUDA(ctx, srow.alloc(n));
-  k_precond_rowscale<<<g, 256, 0, ctx->stream>>>(n, S.ptr.p, S.len.p, S.col.p, L.wsell.p, ctx->sw.dinv.p, srow.p);
-  k_precond_apply_scale<<<g, 256, 0, ctx->stream>>>(n, S.ptr.p, S.len.p, S.col.p, L.wsell.p, srow.p);
+  if (L.srow.n < n) NALU_CUDA(ctx, L.srow.alloc(n));
+  const unsigned g = (unsigned)((row1 - row0 + 255) / 256);
+  k_precond_sell<<<g, 256, 0, ctx->stream>>>(row0, row1, ctx->d_rowptr.p, S.ptr.p, S.len.p, S.col.p, L.nbr.p,
+                                             L.stencil.p, ctx->sw.dinv.p, ctx->d_bcmask.p, L.wsell.p);
+  k_precond_rowscale<<<g, 256, 0, ctx->stream>>>(row0, row1, S.ptr.p, S.len.p, S.col.p, L.wsell.p, ctx->sw.dinv.p,
+                                                 L.srow.p);
+  k_precond_apply_scale<<<g, 256, 0, ctx->stream>>>(row0, row1, S.ptr.p, S.len.p, S.col.p, L.wsell.p, L.srow.p);
+  ctx->launches += 3;
+  return cuda_check(ctx, cudaGetLastError(), "learned preconditioner values");
+}
+
+int learned_prepare(nalu_ctx* ctx) {
+  const int64_t n = ctx->n_rows;
+  int rc = learned_prepare_rows(ctx, 0, n);
+  if (rc) return rc;
+  LearnedState& L = ctx->learned;
+  const SellMatrix& S = ctx->sw.sell;
   if (L.wsell16.n < S.stored) NALU_CUDA(ctx, L.wsell16.alloc(S.stored));
   k_to_bf16<<<(unsigned)((S.stored + 255) / 256), 256, 0, ctx->stream>>>(S.stored, L.wsell.p, L.wsell16.p);
-  ctx->launches += 4;
+  ctx->launches++;
   NALU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return cuda_check(ctx, cudaGetLastError(), "learned preconditioner values");
 }
