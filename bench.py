@@ -477,8 +477,15 @@ def bench_gpu(args):
                                            "same with the opening probe; learned_multilevel uses the stencil as "
                                            "the fine-level smoother of the aggregation multigrid, "
                                            "multilevel_jacobi is that multigrid with damped-Jacobi smoothing")
+        # model FLOPs of one trained sample (27 slot rows): layers 2-3 forward, dH2 and dH1, dW3 and dW2
+        # (6 x 2 x 27 x 64 x 64) plus the static part of layer 1 forward and backward (2 x 2 x 64 x 81)
+        flops_sample = 6 * 2 * 27 * 64 * 64 + 2 * 2 * 64 * 81
+        trained = (int(0.9 * tg.size) // 256) * 256 * 40  # samples of the 40 epochs (batch 256, 10% held out)
         solve["learned_training"] = {"pairs": int(tg.size), "harvest_s": t1 - t0, "train_s": t2 - t1,
-                                     "epochs": 40, "val_mse_first_last": [float(hist[0, 1]), float(hist[-1, 1])]}
+                                     "epochs": 40, "precision": "bf16 tensor cores (mma.sync m16n8k16), "
+                                     "fp32 accumulation, fp32 master weights and Adam; two launches per step",
+                                     "model_tflops": trained * flops_sample / (t2 - t1) * 1e-12,
+                                     "val_mse_first_last": [float(hist[0, 1]), float(hist[-1, 1])]}
         solve["learned_vs_plain_time"] = solve["jacobi_pcg_fp64"]["ms"] / solve["learned_multilevel"]["ms"]
         solve["learned_stencil_fcg_vs_plain_time"] = solve["jacobi_pcg_fp64"]["ms"] / solve["learned_fcg"]["ms"]
         solve["learned_probe_vs_plain_time"] = solve["jacobi_pcg_fp64"]["ms"] / solve["learned_fcg_probe"]["ms"]
@@ -851,8 +858,10 @@ def bench_batch(ng, dev=0, n_problems=64, seed=2025, reps=2):
     t0 = time.perf_counter()
     ctx.learned_init(7)
     st, rf, tg = ctx.learned_harvest(n_samples=20000, n_rhs=4, seed=2026)
+    t1 = time.perf_counter()
     ctx.learned_train(st, rf, tg, epochs=40)
     train_s = time.perf_counter() - t0
+    train_only_s = time.perf_counter() - t1
     linfos = None
     for _ in range(reps):  # the same repetitions as the plain solve, fastest kept
         li = ctx.solve_batched(ng.default_solver_opts(tol=1e-8, max_iters=40000, precond=ng.PRECOND_LEARNED),
@@ -869,7 +878,8 @@ def bench_batch(ng, dev=0, n_problems=64, seed=2025, reps=2):
                           "problems_probe_chose_jacobi": int(sum(i.fallback == 2 for i in linfos)),
                           "problems_fell_back_after_stall": int(sum(i.fallback == 1 for i in linfos)),
                           "max_true_rel_res": max(i.true_rel_res for i in linfos),
-                          "all_converged": all(i.status == 0 for i in linfos), "training_s": train_s}
+                          "all_converged": all(i.status == 0 for i in linfos), "training_s": train_s,
+                          "train_only_s": train_only_s}
     out["learned_vs_plain_time"] = infos[0].seconds / lsolve
     out.update(batch_multilevel(ng, ctx, off, asm_ms))
     ctx.close()

@@ -440,19 +440,29 @@ typedef struct nalu_train_opts {
   double lr;           /* Adam step size, default 1e-3 (beta 0.9/0.999, eps 1e-8) */
   double val_fraction; /* held-out share of the samples, default 0.1 */
   uint64_t seed;       /* sample order */
-  int reserved[4];
+  int precision;       /* enum nalu_train_precision, default NALU_TRAIN_BF16 */
+  int reserved[3];
 } nalu_train_opts;
+enum nalu_train_precision {
+  NALU_TRAIN_BF16 = 0, /* fused step on the tensor cores: BF16 weights and
+                          activations, FP32 accumulation, FP32 master weights
+                          and Adam; two launches per step, one graph per epoch */
+  NALU_TRAIN_FP32 = 1  /* FP32 CUDA-core GEMMs (the exact path) */
+};
 void nalu_train_opts_default(nalu_train_opts* opts);
 /* Adam on the mean squared error of the stencil form
  * pred = rf_13 + sum_s mask_s mlp(impulse_s, st) / sqrt(27) * rf_s against
- * the targets, on the GPU (FP32).  history [epochs][2]: train and held-out
- * MSE after each epoch (may be NULL). */
+ * the targets, on the GPU (opts->precision).  history [epochs][2]: train and
+ * held-out MSE after each epoch (may be NULL). */
 int nalu_learned_train(nalu_ctx* ctx, const float* static_feats, const float* resid_feats, const float* targets,
                        int64_t n, const nalu_train_opts* opts, float* history);
 /* loss and gradient of that loss at the current weights over n <= 1024
  * samples (one batch); grad [NALU_LEARNED_PARAMS], host arrays */
 int nalu_learned_gradient(nalu_ctx* ctx, const float* static_feats, const float* resid_feats, const float* targets,
                           int64_t n, float* grad, double* loss);
+/* the same from the fused BF16 tensor-core training step (any n >= 1) */
+int nalu_learned_gradient_bf16(nalu_ctx* ctx, const float* static_feats, const float* resid_feats,
+                               const float* targets, int64_t n, float* grad, double* loss);
 /* the stencil of the current scalar system: stencil [n_rows][27] (host),
  * mlp(impulse_s) / sqrt(27) per slot, 0 for missing neighbours and for
  * identity rows */

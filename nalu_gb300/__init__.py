@@ -46,6 +46,7 @@ SCHEDULE_NAMES = {SCHEDULE_ELEMENT: "element", SCHEDULE_IP8: "ip8", SCHEDULE_IP1
 SOLVER_CG, SOLVER_GMRES = 0, 1
 PRECOND_NONE, PRECOND_JACOBI, PRECOND_CHEBYSHEV, PRECOND_LEARNED = 0, 1, 2, 3
 PRECOND_MULTILEVEL, PRECOND_LEARNED_MULTILEVEL = 4, 5
+TRAIN_BF16, TRAIN_FP32 = 0, 1
 LEARNED_PARAMS = 15361
 PRECISION_FP64, PRECISION_FP32_INNER_IR = 0, 1
 
@@ -84,7 +85,8 @@ class SolveInfo(ctypes.Structure):
 
 class TrainOpts(ctypes.Structure):
     _fields_ = [("epochs", ctypes.c_int), ("batch", ctypes.c_int), ("lr", ctypes.c_double),
-                ("val_fraction", ctypes.c_double), ("seed", ctypes.c_uint64), ("reserved", ctypes.c_int * 4)]
+                ("val_fraction", ctypes.c_double), ("seed", ctypes.c_uint64), ("precision", ctypes.c_int),
+                ("reserved", ctypes.c_int * 3)]
 
 
 _lib = None
@@ -161,6 +163,7 @@ def lib():
             "nalu_train_opts_default": (None, [P]),
             "nalu_learned_train": (I, [P, P, P, P, I64, P, P]),
             "nalu_learned_gradient": (I, [P, P, P, P, I64, P, ctypes.POINTER(D)]),
+            "nalu_learned_gradient_bf16": (I, [P, P, P, P, I64, P, ctypes.POINTER(D)]),
             "nalu_learned_stencil": (I, [P, P]),
             "nalu_solve_batched": (I, [P, P, P]),
             "nalu_assemble_tuning": (I, [P, I, ctypes.POINTER(I), ctypes.POINTER(I), P]),
@@ -506,12 +509,15 @@ class Context:
                                              _ptr(hist)), "learned_train")
         return hist
 
-    def learned_gradient(self, st, rf, tg):
+    def learned_gradient(self, st, rf, tg, precision=None):
+        """loss and gradient at the current weights: the FP32 path (default)
+        or the fused BF16 tensor-core step (precision=TRAIN_BF16)"""
         st, rf, tg = (np.ascontiguousarray(a, np.float32) for a in (st, rf, tg))
         g = np.zeros(LEARNED_PARAMS, np.float32)
         loss = ctypes.c_double()
-        self._check(lib().nalu_learned_gradient(self._h, _ptr(st), _ptr(rf), _ptr(tg), tg.size, _ptr(g),
-                                                ctypes.byref(loss)), "learned_gradient")
+        fn = lib().nalu_learned_gradient_bf16 if precision == TRAIN_BF16 else lib().nalu_learned_gradient
+        self._check(fn(self._h, _ptr(st), _ptr(rf), _ptr(tg), tg.size, _ptr(g), ctypes.byref(loss)),
+                    "learned_gradient")
         return loss.value, g
 
     def learned_stencil(self):

@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 SOURCES = ["api.cu", "assemble.cu", "assemble_df.cu", "assemble_df_sd.cu", "assemble_df_c0.cu", "assemble_df_c1.cu",
            "assemble_df_c2.cu", "assemble_ip8_c0.cu", "assemble_ip8_c12.cu", "assemble_ip8_sd.cu", "assemble_ip16_c0.cu",
-           "assemble_ip16_c12.cu", "assemble_ip16_sd.cu", "momentum.cu", "momentum_df.cu", "krylov.cu", "cg_fast.cu", "batch.cu", "learned.cu", "multilevel.cu", "geometry.cu", "mass.cu", "faces.cu", "dump.cu", "master_element.cu"]
+           "assemble_ip16_c12.cu", "assemble_ip16_sd.cu", "momentum.cu", "momentum_df.cu", "krylov.cu", "cg_fast.cu", "batch.cu", "learned.cu", "train_tc.cu", "multilevel.cu", "geometry.cu", "mass.cu", "faces.cu", "dump.cu", "master_element.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

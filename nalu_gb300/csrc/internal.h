@@ -290,6 +290,22 @@ template <class VT>
 int sell_build(nalu_ctx* ctx, SellMatrix& S, const VT** vals_out);
 // learned.cu
 int learned_prepare(nalu_ctx* ctx);
+// train_tc.cu: the fused BF16 tensor-core training step (device arrays)
+struct TrainData {
+  const float* st;      // [n][81] static features
+  const float* rf;      // [n][27] residual features
+  const float* tg;      // [n] targets
+  const int32_t* idx;   // [epochs * steps_per_epoch][B] training order
+  const int32_t* vidx;  // [n_val] held-out samples
+  int B, steps_per_epoch, epochs;
+  int64_t n_val;
+  float lr;
+};
+int train_tc(nalu_ctx* ctx, const TrainData& d, float* history);
+// gradient (into grad_dev, [NALU_LEARNED_PARAMS]) and mean squared error
+// (loss_dev[0]) of the samples idx[0..n) at the current weights
+int gradient_tc(nalu_ctx* ctx, const float* st, const float* rf, const float* tg, const int32_t* idx, int n,
+                float* grad_dev, float* loss_dev);
 // the learned preconditioner's FP32 values (wsell) of rows [row0, row1) only;
 // the rows' neighbours in A must lie in the same range (a problem of a batch)
 int learned_prepare_rows(nalu_ctx* ctx, int64_t row0, int64_t row1);

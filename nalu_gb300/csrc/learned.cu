@@ -27,8 +27,9 @@
 //   SELL values     one thread per row, symmetrised
 //   FCG             four kernels per iteration, partial sums re-reduced in a
 //                   fixed order by every block (deterministic)
-//   training        FP32 tiled SGEMM with bias/GELU epilogues, reductions in
-//                   fixed order, Adam; one step is one CUDA graph
+//   training        by default the fused BF16 tensor-core step of train_tc.cu;
+//                   here the FP32 path: tiled SGEMM with bias/GELU epilogues,
+//                   reductions in fixed order, Adam; one step is one CUDA graph
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -44,23 +45,12 @@
 
 #include "df64.h"
 #include "internal.h"
+#include "learned_mlp.cuh"
 #include "reduce.cuh"
 #include "spmv_df.cuh"
 
 namespace nalu_gb300 {
 
-constexpr int kNP = NALU_LEARNED_PARAMS;
-constexpr int OFF_W1 = 0;      // [64][108]
-constexpr int OFF_B1 = 6912;   // [64]
-constexpr int OFF_W2 = 6976;   // [64][64]
-constexpr int OFF_B2 = 11072;  // [64]
-constexpr int OFF_W3 = 11136;  // [64][64]
-constexpr int OFF_B3 = 15232;  // [64]
-constexpr int OFF_W4 = 15296;  // [64]
-constexpr int OFF_B4 = 15360;  // [1]
-static_assert(OFF_B4 + 1 == kNP, "parameter layout");
-constexpr int kWStride = 72;   // padded BF16 row stride of W2/W3 in the stencil kernel (conflict-free B loads)
-constexpr float kSqrt27 = 5.196152422706632f;
 
 constexpr int kFcgBlocks = 1024;
 constexpr int kFcgThreads = 256;
@@ -153,69 +143,6 @@ __global__ void k_harvest(int64_t count, const int64_t* __restrict__ rows, const
 // ---------------------------------------------------------------------------
 // stencil kernel (inference, BF16 tensor cores)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ float tanh_fast(float x) {
-  float y;
-  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
-  return y;
-}
-__device__ __forceinline__ float gelu_fast(float x) {
-  const float u = 0.7978845608028654f * fmaf(0.044715f * x, x * x, x);
-  return 0.5f * x * (1.0f + tanh_fast(u));
-}
-__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
-  const __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
-  return *reinterpret_cast<const uint32_t*>(&h);
-}
-__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-      "{%0,%1,%2,%3};"
-      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
-}
-
-// acc[mt][j] = bias + A[mt] (16 x 64) . W^T  for the 8 n-tiles of 64 outputs;
-// W: BF16 [64][kWStride] viewed as u32 (row stride kWStride/2)
-__device__ __forceinline__ void mlp_layer(float (&acc)[2][8][4], const uint32_t (&a)[2][4][4],
-                                          const uint32_t* __restrict__ W, const float* __restrict__ bias, int g,
-                                          int t) {
-#pragma unroll
-  for (int j = 0; j < 8; ++j) {
-    const float b0 = bias[8 * j + 2 * t], b1 = bias[8 * j + 2 * t + 1];
-#pragma unroll
-    for (int mt = 0; mt < 2; ++mt) {
-      acc[mt][j][0] = b0;
-      acc[mt][j][1] = b1;
-      acc[mt][j][2] = b0;
-      acc[mt][j][3] = b1;
-    }
-  }
-#pragma unroll
-  for (int kk = 0; kk < 4; ++kk) {
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      const uint32_t* row = W + (8 * j + g) * (kWStride / 2);
-      const uint32_t b0 = row[8 * kk + t], b1 = row[8 * kk + 4 + t];
-      mma_bf16(acc[0][j], a[0][kk], b0, b1);
-      mma_bf16(acc[1][j], a[1][kk], b0, b1);
-    }
-  }
-}
-
-__device__ __forceinline__ void gelu_pack(const float (&acc)[2][8][4], uint32_t (&a)[2][4][4]) {
-#pragma unroll
-  for (int mt = 0; mt < 2; ++mt)
-#pragma unroll
-    for (int kk = 0; kk < 4; ++kk) {
-      const float* c0 = acc[mt][2 * kk];
-      const float* c1 = acc[mt][2 * kk + 1];
-      a[mt][kk][0] = pack_bf16(gelu_fast(c0[0]), gelu_fast(c0[1]));
-      a[mt][kk][1] = pack_bf16(gelu_fast(c0[2]), gelu_fast(c0[3]));
-      a[mt][kk][2] = pack_bf16(gelu_fast(c1[0]), gelu_fast(c1[1]));
-      a[mt][kk][3] = pack_bf16(gelu_fast(c1[2]), gelu_fast(c1[3]));
-    }
-}
-
 constexpr int kStThreads = 128;
 constexpr int kStWarps = kStThreads / 32;
 constexpr int kStWarpFloats = 148;  // 81 static features (+3 pad) + 64 layer-1 values
@@ -1388,6 +1315,36 @@ int nalu_learned_gradient(nalu_ctx* ctx, const float* static_feats, const float*
   return cuda_check(ctx, cudaGetLastError(), "gradient");
 }
 
+int nalu_learned_gradient_bf16(nalu_ctx* ctx, const float* static_feats, const float* resid_feats,
+                               const float* targets, int64_t n, float* grad, double* loss) {
+  if (!ctx || !static_feats || !resid_feats || !targets || !grad || n < 1 || n > INT_MAX / 81) return NALU_ERR_ARG;
+  if (!ctx->learned.has_weights) return set_error(ctx, NALU_ERR_STATE, "no weights");
+  cudaSetDevice(ctx->device);
+  DBuf<int32_t> idx;
+  DBuf<float> st, rf, tg, g, l;
+  NALU_CUDA(ctx, idx.alloc(n));
+  NALU_CUDA(ctx, st.alloc(n * 81));
+  NALU_CUDA(ctx, rf.alloc(n * 27));
+  NALU_CUDA(ctx, tg.alloc(n));
+  NALU_CUDA(ctx, g.alloc(kNP));
+  NALU_CUDA(ctx, l.alloc(1));
+  std::vector<int32_t> hidx(n);
+  std::iota(hidx.begin(), hidx.end(), 0);
+  cudaStream_t s0 = ctx->stream;
+  NALU_CUDA(ctx, cudaMemcpyAsync(idx.p, hidx.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, s0));
+  NALU_CUDA(ctx, cudaMemcpyAsync(st.p, static_feats, sizeof(float) * n * 81, cudaMemcpyHostToDevice, s0));
+  NALU_CUDA(ctx, cudaMemcpyAsync(rf.p, resid_feats, sizeof(float) * n * 27, cudaMemcpyHostToDevice, s0));
+  NALU_CUDA(ctx, cudaMemcpyAsync(tg.p, targets, sizeof(float) * n, cudaMemcpyHostToDevice, s0));
+  int rc = gradient_tc(ctx, st.p, rf.p, tg.p, idx.p, (int)n, g.p, l.p);
+  if (rc) return rc;
+  float lv = 0.0f;
+  NALU_CUDA(ctx, cudaMemcpyAsync(grad, g.p, sizeof(float) * kNP, cudaMemcpyDeviceToHost, s0));
+  NALU_CUDA(ctx, cudaMemcpyAsync(&lv, l.p, sizeof(float), cudaMemcpyDeviceToHost, s0));
+  NALU_CUDA(ctx, cudaStreamSynchronize(s0));
+  if (loss) *loss = lv;
+  return NALU_OK;
+}
+
 int nalu_learned_train(nalu_ctx* ctx, const float* static_feats, const float* resid_feats, const float* targets,
                        int64_t n, const nalu_train_opts* opts, float* history) {
   if (!ctx || !static_feats || !resid_feats || !targets || !opts || n < 2) return NALU_ERR_ARG;
@@ -1416,6 +1373,8 @@ int nalu_learned_train(nalu_ctx* ctx, const float* static_feats, const float* re
   const int val_batches = (int)((n_val + B - 1) / B);
   std::vector<int32_t> vidx((size_t)std::max(1, val_batches) * B, order.empty() ? 0 : order[0]);
   for (int64_t i = 0; i < n_val; ++i) vidx[i] = order[i];
+  const bool tc = opts->precision == NALU_TRAIN_BF16;
+  if (!tc && opts->precision != NALU_TRAIN_FP32) return set_error(ctx, NALU_ERR_ARG, "train opts: precision");
   DBuf<float> st, rf, tg;
   DBuf<int32_t> d_idx, d_vidx, d_step;
   NALU_CUDA(ctx, st.alloc(n * 81));
@@ -1434,6 +1393,10 @@ int nalu_learned_train(nalu_ctx* ctx, const float* static_feats, const float* re
   LearnedState& L = ctx->learned;
   NALU_CUDA(ctx, cudaMemsetAsync(L.adam_m.p, 0, sizeof(float) * kNP, st0));
   NALU_CUDA(ctx, cudaMemsetAsync(L.adam_v.p, 0, sizeof(float) * kNP, st0));
+  if (tc) {
+    TrainData d{st.p, rf.p, tg.p, d_idx.p, d_vidx.p, B, steps_per_epoch, opts->epochs, n_val, (float)opts->lr};
+    return train_tc(ctx, d, history);
+  }
   TrainWork w;
   if ((rc = w.alloc(ctx, B, total_steps))) return rc;
   TrainWork wv;
