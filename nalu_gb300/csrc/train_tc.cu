@@ -3,7 +3,10 @@
 // with FP32 master weights and Adam.
 //
 //   k_train_step   one warp per sample, four samples per block (128 rows: the
-//                  27 impulse slots of each sample and 5 zero rows).  Forward:
+//                  27 impulse slots of each sample and 5 zero rows).  The FP32
+//                  weights arrive in shared memory by 16-byte async copies
+//                  (cp.async, all in flight at once) and are converted there.
+//                  Forward:
 //                  the static part of layer 1 in FP32, layers 2 and 3 on the
 //                  tensor cores with the activations in registers (the
 //                  accumulators of one layer are the A fragments of the next),
@@ -15,8 +18,8 @@
 //                  activations staged transposed in shared memory, each warp
 //                  16 output rows); layer 1, the output layer and the biases in
 //                  FP32.  Each block writes its partial gradient (no atomics).
-//   k_train_adam   sums the block partials in block order (deterministic) and
-//                  takes the Adam step on the FP32 master weights.
+//   k_train_adam   sums the block partials in a fixed order (deterministic)
+//                  and takes the Adam step on the FP32 master weights.
 // An epoch is one CUDA graph of 2 x steps launches.  The FP32 CUDA-core path
 // of learned.cu (about twenty launches per step) stays as the exact one.
 #include <cuda_bf16.h>
@@ -43,14 +46,16 @@ constexpr int kPartStride = kNP + 1;        // block partial: gradient, then the
 constexpr int kSmW1s = 81 * kW1S;           // static part of W1, [k][o]
 constexpr int kSmW1r = 27 * kW1S;           // sqrt27 W1[o][s], [s][o]
 constexpr int kSmBB = 4 * 64 + 8;           // b1 | b2 | b3 | w4 | b4
-constexpr int kSmZ = kTrWarps * 2048;       // per warp: z2 in fragment order, later dZ1 [27][kW1S]
+constexpr int kSmZ = kTrWarps * 2048;       // per warp: gelu'(Z2) in fragment order, later dZ1 [27][kW1S]
 constexpr int kSmWarp = 84 + 32 + 64 + 4 * 64 + 8;  // per warp: features | rf | hs | 4 vectors | scalars
 constexpr int kSmW = 64 * kWStride / 2;     // one BF16 64x64 weight copy
 constexpr int kSmT = 64 * kTS / 2;          // one transposed BF16 activation [64][kTS]
 constexpr size_t kTrSmem =
-    4 * (size_t)(kSmW1s + kSmW1r + kSmBB + kSmZ + kTrWarps * kSmWarp + 4 * kSmW + 3 * kSmT);
+    4 * (size_t)(kSmW1s + kSmW1r + kSmBB + kTrWarps * kSmWarp + 4 * kSmW + kSmZ + 3 * kSmT);
+constexpr int kStageFloats = OFF_B4;  // P[0, OFF_B4) is staged by 16-byte async copies (b4 is read directly)
 static_assert(kTrSmem <= 227 * 1024, "training step shared memory");
-static_assert((kSmW1s + kSmW1r + kSmBB + kSmZ + kTrWarps * kSmWarp) % 4 == 0, "16-byte aligned BF16 area");
+static_assert((kSmW1s + kSmW1r + kSmBB + kTrWarps * kSmWarp) % 4 == 0, "16-byte aligned BF16 area");
+static_assert(kStageFloats % 4 == 0 && 4 * kStageFloats <= 4 * (kSmZ + 3 * kSmT), "staging area");
 
 __device__ __forceinline__ uint16_t bf16_bits(float x) {
   const __nv_bfloat16 h = __float2bfloat16_rn(x);
@@ -148,46 +153,25 @@ __global__ void __launch_bounds__(kTrThreads, 1)
   float* w1s = reinterpret_cast<float*>(smem);
   float* w1r = w1s + kSmW1s;
   float* bb = w1r + kSmW1r;
-  float* zs = bb + kSmBB;
-  float* wsm = zs + kSmZ;
+  float* wsm = bb + kSmBB;
   uint32_t* w2 = reinterpret_cast<uint32_t*>(wsm + kTrWarps * kSmWarp);
   uint32_t* w3 = w2 + kSmW;
   uint32_t* w2t = w3 + kSmW;
   uint32_t* w3t = w2t + kSmW;
-  uint32_t* h1t = w3t + kSmW;
+  float* zs = reinterpret_cast<float*>(w3t + kSmW);
+  uint32_t* h1t = reinterpret_cast<uint32_t*>(zs + kSmZ);
   uint32_t* h2t = h1t + kSmT;
   uint32_t* dzt = h2t + kSmT;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
 
-  // weights: FP32 layer-1 tables, BF16 W2, W3 ([o][k]) and their transposes
-  for (int i = tid; i < 64 * 108; i += kTrThreads) {
-    const int o = i / 108, c = i % 108;
-    const float w = P[OFF_W1 + i];
-    if (c < 27)
-      w1r[c * kW1S + o] = kSqrt27 * w;
-    else
-      w1s[(c - 27) * kW1S + o] = w;
-  }
-  for (int i = tid; i < 64; i += kTrThreads) {
-    bb[i] = P[OFF_B1 + i];
-    bb[64 + i] = P[OFF_B2 + i];
-    bb[128 + i] = P[OFF_B3 + i];
-    bb[192 + i] = P[OFF_W4 + i];
-  }
-  if (tid == 0) bb[256] = P[OFF_B4];
+  // the FP32 weights staged into shared memory (zs and the transposed
+  // activations, not yet in use) by 16-byte async copies, all in flight at once
+  float* stage = zs;
   {
-    uint16_t* w2h = reinterpret_cast<uint16_t*>(w2);
-    uint16_t* w3h = reinterpret_cast<uint16_t*>(w3);
-    uint16_t* w2th = reinterpret_cast<uint16_t*>(w2t);
-    uint16_t* w3th = reinterpret_cast<uint16_t*>(w3t);
-    for (int i = tid; i < 64 * 64; i += kTrThreads) {
-      const int o = i >> 6, k = i & 63;
-      const uint16_t v2 = bf16_bits(P[OFF_W2 + i]), v3 = bf16_bits(P[OFF_W3 + i]);
-      w2h[o * kWStride + k] = v2;
-      w3h[o * kWStride + k] = v3;
-      w2th[k * kWStride + o] = v2;
-      w3th[k * kWStride + o] = v3;
-    }
+    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(stage);
+    for (int c = tid; c < kStageFloats / 4; c += kTrThreads)
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sbase + 16u * c), "l"(P + 4 * c) : "memory");
+    asm volatile("cp.async.commit_group;" ::: "memory");
   }
   // this warp's sample
   float* my = wsm + warp * kSmWarp;
@@ -203,7 +187,38 @@ __global__ void __launch_bounds__(kTrThreads, 1)
   for (int k = lane; k < 84; k += 32) stw[k] = (have && k < 81) ? st[src * 81 + k] : 0.0f;
   rfw[lane] = (have && lane < 27) ? rf[src * 27 + lane] : 0.0f;
   const float target = have ? tg[src] : 0.0f;
+  asm volatile("cp.async.wait_all;" ::: "memory");
   __syncthreads();
+  // weights: FP32 layer-1 tables, BF16 W2, W3 ([o][k]) and their transposes
+  static_assert(kTrThreads >= 108, "one layer-1 column per thread");
+  if (tid < 108) {  // column c = tid of W1[o][c], row by row (no division)
+    float* dst = tid < 27 ? w1r + tid * kW1S : w1s + (tid - 27) * kW1S;
+    const float sc = tid < 27 ? kSqrt27 : 1.0f;
+#pragma unroll 8
+    for (int o = 0; o < 64; ++o) dst[o] = sc * stage[OFF_W1 + o * 108 + tid];
+  }
+  for (int i = tid; i < 64; i += kTrThreads) {
+    bb[i] = stage[OFF_B1 + i];
+    bb[64 + i] = stage[OFF_B2 + i];
+    bb[128 + i] = stage[OFF_B3 + i];
+    bb[192 + i] = stage[OFF_W4 + i];
+  }
+  if (tid == 0) bb[256] = P[OFF_B4];
+  {
+    uint16_t* w2h = reinterpret_cast<uint16_t*>(w2);
+    uint16_t* w3h = reinterpret_cast<uint16_t*>(w3);
+    uint16_t* w2th = reinterpret_cast<uint16_t*>(w2t);
+    uint16_t* w3th = reinterpret_cast<uint16_t*>(w3t);
+    for (int i = tid; i < 64 * 64; i += kTrThreads) {
+      const int o = i >> 6, k = i & 63;
+      const uint16_t v2 = bf16_bits(stage[OFF_W2 + i]), v3 = bf16_bits(stage[OFF_W3 + i]);
+      w2h[o * kWStride + k] = v2;
+      w3h[o * kWStride + k] = v3;
+      w2th[k * kWStride + o] = v2;
+      w3th[k * kWStride + o] = v3;
+    }
+  }
+  __syncthreads();  // the staging area is reused below
 
   // ---- forward ----
 #pragma unroll
@@ -245,20 +260,17 @@ __global__ void __launch_bounds__(kTrThreads, 1)
   float acc[2][8][4];
   mlp_layer(acc, a, w2, bb + 64, g, t);  // Z2
   float* z2w = zs + warp * 2048;
-  if (grad) {
-#pragma unroll
-    for (int mt = 0; mt < 2; ++mt)
-#pragma unroll
-      for (int j = 0; j < 8; ++j)
-#pragma unroll
-        for (int e = 0; e < 4; ++e) z2w[((mt * 8 + j) * 4 + e) * 32 + lane] = acc[mt][j][e];
-  }
 #pragma unroll
   for (int mt = 0; mt < 2; ++mt)
 #pragma unroll
     for (int j = 0; j < 8; ++j)
 #pragma unroll
-      for (int e = 0; e < 4; ++e) acc[mt][j][e] = gelu_fast(acc[mt][j][e]);
+      for (int e = 0; e < 4; ++e) {
+        float hv, dv;
+        gelu_both(acc[mt][j][e], hv, dv);
+        z2w[((mt * 8 + j) * 4 + e) * 32 + lane] = dv;  // gelu'(Z2), for dZ2 (unused in evaluation)
+        acc[mt][j][e] = hv;
+      }
   if (grad) store_t(acc, reinterpret_cast<uint16_t*>(h2t), warp, g, t);
   pack_a(acc, a);
   mlp_layer(acc, a, w3, bb + 128, g, t);  // Z3
@@ -356,7 +368,7 @@ __global__ void __launch_bounds__(kTrThreads, 1)
       for (int j = 0; j < 8; ++j)
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
-          const float dz = acc[mt][j][e] * gelu_grad_fast(z2w[((mt * 8 + j) * 4 + e) * 32 + lane]);  // dZ2
+          const float dz = acc[mt][j][e] * z2w[((mt * 8 + j) * 4 + e) * 32 + lane];  // dZ2
           acc[mt][j][e] = dz;
           v2[j][e & 1] += dz;
         }
@@ -399,18 +411,24 @@ __global__ void __launch_bounds__(kTrThreads, 1)
     __syncthreads();  // dZ2^T, dZ1 and the vectors of the four samples
     block_wgrad(dzt, h1t, out + OFF_W2, warp, g, t);
     // layer 1, output layer and biases: sums over the four samples in order
-    for (int i = tid; i < 64 * 108; i += kTrThreads) {
-      const int o = i / 108, c = i % 108;
-      float v = 0.0f;
-      if (c < 27) {
+    if (tid < 108) {  // column c = tid, row by row (coalesced rows of 108)
+      const int c = tid;
+      float sv[kTrWarps];
 #pragma unroll
-        for (int w = 0; w < kTrWarps; ++w) v += zs[w * 2048 + c * kW1S + o];
-        v *= kSqrt27;
-      } else {
+      for (int w = 0; w < kTrWarps; ++w) sv[w] = c < 27 ? 0.0f : wsm[w * kSmWarp + c - 27];
+#pragma unroll 4
+      for (int o = 0; o < 64; ++o) {
+        float v = 0.0f;
+        if (c < 27) {
 #pragma unroll
-        for (int w = 0; w < kTrWarps; ++w) v = fmaf(wsm[w * kSmWarp + 180 + 192 + o], wsm[w * kSmWarp + c - 27], v);
+          for (int w = 0; w < kTrWarps; ++w) v += zs[w * 2048 + c * kW1S + o];
+          v *= kSqrt27;
+        } else {
+#pragma unroll
+          for (int w = 0; w < kTrWarps; ++w) v = fmaf(wsm[w * kSmWarp + 180 + 192 + o], sv[w], v);
+        }
+        out[OFF_W1 + o * 108 + c] = v;
       }
-      out[OFF_W1 + i] = v;
     }
     for (int o = tid; o < 64; o += kTrThreads) {
       float s1 = 0.0f, s2 = 0.0f, s3 = 0.0f, s4 = 0.0f;
@@ -445,16 +463,29 @@ __global__ void __launch_bounds__(kTrThreads, 1)
   }
 }
 
-// gradient = sum of the block partials (block order); loss[step] = the mean
-// squared error; with apply, the Adam step (beta 0.9 / 0.999, eps 1e-8)
-__global__ void k_train_adam(const float* __restrict__ part, int nblk, float* __restrict__ P, float* __restrict__ m,
-                             float* __restrict__ v, float* __restrict__ grad_out, float* __restrict__ loss_out,
-                             const int* __restrict__ epoch, int k_in_epoch, int steps_per_epoch, int nvalid, float lr,
-                             int apply) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i > kNP) return;
+// gradient = sum of the block partials in a fixed order (partial c goes to
+// warp c % 8, each warp sums its partials in order, then the eight warp sums
+// in order); loss[step] = the mean squared error; with apply, the Adam step
+// (beta 0.9 / 0.999, eps 1e-8).  A block covers 32 parameters.
+constexpr int kAdamWarps = 8;
+__global__ void __launch_bounds__(32 * kAdamWarps)
+    k_train_adam(const float* __restrict__ part, int nblk, float* __restrict__ P, float* __restrict__ m,
+                 float* __restrict__ v, float* __restrict__ grad_out, float* __restrict__ loss_out,
+                 const int* __restrict__ epoch, int k_in_epoch, int steps_per_epoch, int nvalid, float lr, int apply) {
+  __shared__ float sh[kAdamWarps][32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int i = blockIdx.x * 32 + lane;
+  float s = 0.0f;
+  if (i <= kNP) {
+#pragma unroll 4
+    for (int c = warp; c < nblk; c += kAdamWarps) s += part[(int64_t)c * kPartStride + i];
+  }
+  sh[warp][lane] = s;
+  __syncthreads();
+  if (warp != 0 || i > kNP) return;
   float gsum = 0.0f;
-  for (int c = 0; c < nblk; ++c) gsum += part[(int64_t)c * kPartStride + i];
+#pragma unroll
+  for (int w = 0; w < kAdamWarps; ++w) gsum += sh[w][lane];
   const int step = (epoch ? *epoch : 0) * steps_per_epoch + k_in_epoch;
   if (i == kNP) {
     if (loss_out) loss_out[step] = gsum / (float)nvalid;
@@ -495,7 +526,7 @@ int train_tc(nalu_ctx* ctx, const TrainData& d, float* history) {
   NALU_CUDA(ctx, losses.alloc((int64_t)d.steps_per_epoch * d.epochs));
   NALU_CUDA(ctx, d_epoch.alloc(1));
   NALU_CUDA(ctx, cudaMemsetAsync(d_epoch.p, 0, sizeof(int), st0));
-  const unsigned agrid = (unsigned)((kNP + 1 + 255) / 256);
+  const unsigned agrid = (unsigned)((kNP + 1 + 31) / 32);
   // one epoch as a graph: (step, Adam) x steps_per_epoch, then epoch += 1
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -504,7 +535,7 @@ int train_tc(nalu_ctx* ctx, const TrainData& d, float* history) {
   for (int k = 0; k < d.steps_per_epoch; ++k) {
     k_train_step<<<nblk, kTrThreads, kTrSmem, st0>>>(L.params.p, d.st, d.rf, d.tg, d.idx, d_epoch.p, k,
                                                      d.steps_per_epoch, d.B, d.B, 1, part.p);
-    k_train_adam<<<agrid, 256, 0, st0>>>(part.p, nblk, L.params.p, L.adam_m.p, L.adam_v.p, nullptr, losses.p,
+    k_train_adam<<<agrid, 32 * kAdamWarps, 0, st0>>>(part.p, nblk, L.params.p, L.adam_m.p, L.adam_v.p, nullptr, losses.p,
                                          d_epoch.p, k, d.steps_per_epoch, d.B, d.lr, 1);
   }
   k_epoch_inc<<<1, 1, 0, st0>>>(d_epoch.p);
@@ -563,7 +594,7 @@ int gradient_tc(nalu_ctx* ctx, const float* st, const float* rf, const float* tg
   NALU_CUDA(ctx, part.alloc((int64_t)nblk * kPartStride));
   k_train_step<<<nblk, kTrThreads, kTrSmem, ctx->stream>>>(ctx->learned.params.p, st, rf, tg, idx, nullptr, 0, 0, n,
                                                            n, 1, part.p);
-  k_train_adam<<<(unsigned)((kNP + 1 + 255) / 256), 256, 0, ctx->stream>>>(
+  k_train_adam<<<(unsigned)((kNP + 1 + 31) / 32), 32 * kAdamWarps, 0, ctx->stream>>>(
       part.p, nblk, nullptr, nullptr, nullptr, grad_dev, loss_dev, nullptr, 0, 0, n, 0.0f, 0);
   ctx->launches += 2;
   NALU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
