@@ -158,10 +158,13 @@ __global__ void __launch_bounds__(IpSched<EPB, ip_light<KIND, MODE, SHIFT>()>::k
   constexpr int NCOMP = KIND == 0 ? 1 : 3;
   __shared__ df64 s_ef[EPB][kEfStride];
   __shared__ df64 s_wc[EPB][kWcStride];
-  __shared__ df64 s_x[EPB][kXStride];
   __shared__ df64 s_fac[EPB][kFacStride];
+  // the normalised coordinates live only in phases 0a-0b, the factors from
+  // phase 1 on: they share storage (smaller blocks, one more block per SM)
+  static_assert(kXStride <= kFacStride, "coordinates fit the factor rows");
+  df64(*s_x)[kXStride] = reinterpret_cast<df64(*)[kXStride]>(&s_fac[0][0]);
   __shared__ df64 s_m[EPB][13];
-  __shared__ df64 s_pd[EPB][9];
+  __shared__ df64 s_pd[EPB][MODE == 1 ? 9 : 1];
   __shared__ double s_p[EPB][9];
   __shared__ int s_nd[EPB][8];
   __shared__ int s_k[EPB];
