@@ -81,15 +81,18 @@ struct TileArgs {
   double* rz;           // [P]
   double* rr;           // [P]
   const double* stop2;  // [P]
-  int* done;            // [P] 0 active, 1 converged, 2 breakdown, 3 learned step not positive
+  int* done;            // [P] 0 active, 1 converged, 2 breakdown, 3 flexible-CG step not positive
   int* iters;           // [P] iterations in total
-  // learned flexible CG (mode 1): z = M r with the learned stencil values
+  // flexible CG: z = M r with the learned stencil values (mode 1) or from the
+  // multigrid V-cycle on the union system (mode 2, zf)
   const float* wsell;   // preconditioner values on the SELL pattern (or null)
   double* z;            // [n]
-  const int* mode;      // [P] 0 Jacobi-CG, 1 learned FCG
+  const int* mode;      // [P] 0 Jacobi-CG, 1 learned FCG, 2 multigrid FCG
+  float* rf;            // [n] FP32 residual, the V-cycle's input (mode 2)
+  const float* zf;      // [n] the V-cycle's output (mode 2)
   double* pq;           // [P] p.Ap of the previous iteration
   int* kiter;           // [P] iterations since the last restart
-  int* liters;          // [P] iterations in learned mode
+  int* liters;          // [P] iterations in flexible CG (learned or multigrid)
 };
 
 // The last tile of problem pr to arrive returns true (after a fence), with
@@ -119,15 +122,34 @@ __device__ bool problem_reduce(const TileArgs& a, int t, int pr, const double (&
   return true;
 }
 
-// learned problems: z = M r (FP32 stencil values); beta = -(z . q_old) / (p . q)_old
+// multigrid problems: the V-cycle's FP32 input, the high part of r
+__global__ void __launch_bounds__(kBT) k_bt_hi(TileArgs a) {
+  const int t = blockIdx.x;
+  const int pr = a.tile_prob[t];
+  if (a.done[pr] || a.mode[pr] != 2) return;
+  for (int i = threadIdx.x; i < a.tile_rows[t]; i += kBT) {
+    const int64_t row = a.tile_row0[t] + i;
+    a.rf[row] = a.r2[row].x;
+  }
+}
+
+// flexible-CG problems: z = M r (learned: FP32 stencil values; multigrid: the
+// V-cycle's output); beta = -(z . q_old) / (p . q)_old
 __global__ void __launch_bounds__(kBT) k_bt_prec(TileArgs a) {
   __shared__ double sh[33];
   const int t = blockIdx.x;
   const int pr = a.tile_prob[t];
-  if (a.done[pr] || a.mode[pr] != 1) return;
+  const int m = a.mode[pr];
+  if (a.done[pr] || m == 0) return;
   double dot = 0.0;
   for (int i = threadIdx.x; i < a.tile_rows[t]; i += kBT) {
     const int64_t row = a.tile_row0[t] + i;
+    if (m == 2) {
+      const double zi = widen_f(a.zf[row]);
+      a.z[row] = zi;
+      dot += zi * join_df(a.q2[row]);
+      continue;
+    }
     const int64_t sl = row / kSliceB;
     const int64_t b0 = __ldg(a.sptr + sl);
     const int64_t base = b0 + (row % kSliceB);
@@ -160,7 +182,7 @@ __global__ void __launch_bounds__(kBT) k_bt_pupdate(TileArgs a) {
   const int pr = a.tile_prob[t];
   if (a.done[pr]) return;
   const float2 beta = split_df(a.beta[pr]);
-  const bool learned = a.mode[pr] == 1;
+  const bool learned = a.mode[pr] != 0;  // flexible CG: p = z + beta p
   for (int i = threadIdx.x; i < a.tile_rows[t]; i += kBT) {
     const int64_t row = a.tile_row0[t] + i;
     const float2 z = learned ? split_df(a.z[row])
@@ -191,7 +213,7 @@ __global__ void __launch_bounds__(kBT) k_bt_spmv(TileArgs a) {
   const double v[2] = {join_df(make_float2(dh, dl)), join_df(make_float2(rh, rl))};
   double tot[2];
   if (problem_reduce<2>(a, t, pr, v, tot, sh) && threadIdx.x == 0) {
-    if (a.mode[pr] == 1) {  // flexible CG: alpha = (p . r) / (p . A p)
+    if (a.mode[pr] != 0) {  // flexible CG: alpha = (p . r) / (p . A p)
       const double al = tot[1] / tot[0];
       a.pq[pr] = tot[0];
       a.alpha[pr] = al;
@@ -223,10 +245,10 @@ __global__ void __launch_bounds__(kBT) k_bt_axpy(TileArgs a) {
   const double v[2] = {join_df(make_float2(zh, zl)), join_df(make_float2(rh, rl))};
   double tot[2];
   if (problem_reduce<2>(a, t, pr, v, tot, sh) && threadIdx.x == 0) {
-    const bool learned = a.mode[pr] == 1;
+    const bool learned = a.mode[pr] != 0;  // flexible CG: beta comes from k_bt_prec
     const double be = learned ? 0.0 : tot[0] / a.rz[pr];
     if (!learned) a.beta[pr] = be;
-    a.rz[pr] = tot[0];  // kept in learned mode too: a problem may change to Jacobi-CG in place
+    a.rz[pr] = tot[0];  // kept in flexible CG too: a problem may change to Jacobi-CG in place
     a.rr[pr] = tot[1];
     a.iters[pr] += 1;
     a.kiter[pr] += 1;
@@ -333,13 +355,31 @@ int solve_batched(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* inf
   if ((rc = sell_build<float2>(ctx, s.sell, &sv2))) return rc;
   DBuf<int64_t> d_trow0;
   const bool learned = o.precond == NALU_PRECOND_LEARNED;
-  if (learned && (o.method != NALU_SOLVER_CG || o.precision != NALU_PRECISION_FP64))
-    return set_error(ctx, NALU_ERR_ARG, "the learned preconditioner runs in FP64 flexible CG only");
+  const bool multilevel = o.precond == NALU_PRECOND_MULTILEVEL;
+  const bool flexible = learned || multilevel;
+  if (flexible && (o.method != NALU_SOLVER_CG || o.precision != NALU_PRECISION_FP64))
+    return set_error(ctx, NALU_ERR_ARG, "the learned and multigrid preconditioners run in FP64 flexible CG only");
+  if (!(o.precond == NALU_PRECOND_JACOBI || flexible))
+    return set_error(ctx, NALU_ERR_ARG, "batched solve: Jacobi, learned or multigrid preconditioner");
   double setup_s = 0.0;
   if (learned) {
     LearnedState& L = ctx->learned;
     if (!L.has_weights) return set_error(ctx, NALU_ERR_STATE, "learned preconditioner has no weights");
     if (L.wsell.n < s.sell.stored) NALU_CUDA(ctx, L.wsell.alloc(s.sell.stored));
+  }
+  DBuf<float> rfb, zfb;
+  if (multilevel) {
+    // one hierarchy for the union: aggregation follows couplings, so no
+    // aggregate spans two problems, every coarse operator is block diagonal and
+    // the V-cycle applies each problem's own preconditioner
+    if (nd != 1) return set_error(ctx, NALU_ERR_ARG, "the multigrid preconditioner needs a scalar system");
+    const auto ts = std::chrono::steady_clock::now();
+    if ((rc = sell_c16_ensure(ctx, s.sell)) || (rc = ml_setup(ctx, false))) return rc;
+    NALU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    setup_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - ts).count();
+    NALU_CUDA(ctx, rfb.alloc(n));
+    NALU_CUDA(ctx, zfb.alloc(n));
+    NALU_CUDA(ctx, cudaMemsetAsync(rfb.p, 0, sizeof(float) * n, ctx->stream));
   }
   DBuf<int32_t> d_ints;  // trows | tprob | pt0 | pt1 | done | iters | mode | kiter | liters
   DBuf<double> d_dbl;    // tpart[2 ntiles] | tb[ntiles] | alpha beta rz rr stop2 [P] | sums [3P]
@@ -350,7 +390,7 @@ int solve_batched(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* inf
   NALU_CUDA(ctx, d_ints.alloc(2 * (int64_t)ntiles + 7 * (int64_t)P));
   NALU_CUDA(ctx, d_dbl.alloc(3 * (int64_t)ntiles + 9 * (int64_t)P));
   DBuf<double> zbuf;
-  if (learned) NALU_CUDA(ctx, zbuf.alloc(n));
+  if (flexible) NALU_CUDA(ctx, zbuf.alloc(n));
   NALU_CUDA(ctx, d_cnt.alloc(P));
   NALU_CUDA(ctx, dinvf.alloc(n));
   NALU_CUDA(ctx, p2.alloc(n));
@@ -382,7 +422,7 @@ int solve_batched(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* inf
   NALU_CUDA(ctx, cudaMemcpyAsync(pt1_d, pt1.data(), sizeof(int32_t) * P, cudaMemcpyHostToDevice, st));
   NALU_CUDA(ctx, cudaMemsetAsync(iters_d, 0, sizeof(int32_t) * P, st));
   NALU_CUDA(ctx, cudaMemsetAsync(liters_d, 0, sizeof(int32_t) * P, st));
-  std::vector<int32_t> mode(P, 0), fallback(P, learned ? 2 : 0);
+  std::vector<int32_t> mode(P, multilevel ? 2 : 0), fallback(P, learned ? 2 : 0);
   NALU_CUDA(ctx, cudaMemsetAsync(d_cnt.p, 0, sizeof(unsigned) * P, st));
   k_to_float<<<1024, 256, 0, st>>>(n, s.dinv.p, dinvf.p);
   k_batch_prep<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, ctx->d_bcmask.p, ctx->d_rhs.p, ctx->d_x.p,
@@ -427,6 +467,8 @@ int solve_batched(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* inf
   a.iters = iters_d;
   a.wsell = learned ? ctx->learned.wsell.p : nullptr;  // rows set up problem by problem
   a.z = zbuf.p;
+  a.rf = rfb.p;
+  a.zf = zfb.p;
   a.mode = mode_d;
   a.pq = pq_d;
   a.kiter = kiter_d;
@@ -434,14 +476,19 @@ int solve_batched(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* inf
 
   const int chunk = o.check_every > 0 ? o.check_every : 25;
   // two graphs of `chunk` iterations: Jacobi-CG only (three kernels an
-  // iteration) and with the learned stencil apply (four); the second runs only
-  // while some unfinished problem is in learned mode
+  // iteration) and flexible CG (the learned stencil apply, or the union
+  // V-cycle, first); the second runs only while some unfinished problem is
+  // in flexible CG
   GraphExecs gx;
   auto capture = [&](bool with_prec, cudaGraphExec_t* out) -> int {
     cudaGraph_t graph = nullptr;
     cudaError_t ce = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
     if (ce != cudaSuccess) return cuda_check(ctx, ce, "begin capture");
     for (int k = 0; k < chunk; ++k) {
+      if (with_prec && multilevel) {
+        k_bt_hi<<<ntiles, kBT, 0, st>>>(a);
+        ml_apply(ctx, a.rf, zfb.p);
+      }
       if (with_prec) k_bt_prec<<<ntiles, kBT, 0, st>>>(a);
       k_bt_pupdate<<<ntiles, kBT, 0, st>>>(a);
       k_bt_spmv<<<ntiles, kBT, 0, st>>>(a);
@@ -454,7 +501,7 @@ int solve_batched(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* inf
     return ce == cudaSuccess ? NALU_OK : cuda_check(ctx, ce, "instantiate");
   };
   if ((rc = capture(false, &gx.e[0]))) return rc;
-  if (learned && (rc = capture(true, &gx.e[1]))) return rc;
+  if (flexible && (rc = capture(true, &gx.e[1]))) return rc;
 
   std::vector<double> sums(3 * P);
   std::vector<int32_t> done(P), iters(P);
@@ -561,10 +608,10 @@ int solve_batched(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* inf
            std::max(lit[pr], 1);
   };
   auto learned_wins = [&](int pr) { return done[pr] != 3 && rate_l[pr] < kappa * rate_j[pr]; };
-  auto rows_active = [&](int m) {
+  auto rows_active = [&](int m) {  // m < 0: every mode; m = 3: flexible CG (modes 1 and 2)
     int64_t s0 = 0;
     for (int pr = 0; pr < P; ++pr)
-      if (!done[pr] && (m < 0 || mode[pr] == m)) s0 += prow1[pr] - prow0[pr];
+      if (!done[pr] && (m < 0 || mode[pr] == m || (m == 3 && mode[pr] != 0))) s0 += prow1[pr] - prow0[pr];
     return s0;
   };
   cudaEvent_t pe[2];
@@ -583,7 +630,7 @@ int solve_batched(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* inf
     int phase_it = 0;
     if (phase != kDecided) NALU_CUDA(ctx, cudaEventRecord(pe[0], st));
     for (int it = 0; it < max_its; it += chunk) {
-      const bool any_learned = learned && rows_active(1) > 0;
+      const bool any_learned = flexible && rows_active(3) > 0;
       if (phase == kJacobiProbe) rows_a += (double)rows_active(-1) * chunk;
       if (phase == kLearnedProbe) {
         rows_bj += (double)rows_active(0) * chunk;
@@ -645,6 +692,9 @@ int solve_batched(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* inf
           for (int pr = 0; pr < P; ++pr)
             if (candidate[pr] && pr != rep && !done[pr] && (rc = to_learned(pr))) return rc;
         }
+      } else if (phase == kDecided && multilevel) {
+        for (int pr = 0; pr < P; ++pr)
+          if (mode[pr] == 2 && done[pr] == 3 && (rc = to_jacobi(pr, 1))) return rc;  // not positive: Jacobi-CG
       } else if (phase == kDecided && learned) {
         for (int pr = 0; pr < P; ++pr) {
           if (mode[pr] != 1 || done[pr] == 1 || done[pr] == 2) continue;

@@ -319,6 +319,8 @@ int fcg_df_external(nalu_ctx* ctx, double* x, double* r, double rtol, double r0n
                     const std::function<void(const float*, float*)>& prec, int* iters_out);
 int fcg_multilevel(nalu_ctx* ctx, double* x, double* r, double rtol, double r0norm, int max_it, int check_every,
                    int klevels, int* iters_out);
+// one multigrid cycle z = M r (FP32, on the context's stream; graph-capturable)
+int ml_apply(nalu_ctx* ctx, const float* rf, float* zf);
 int ml_levels(const nalu_ctx* ctx, int max_levels, int64_t* rows, int64_t* nnz);
 void ml_free(nalu_ctx* ctx);  // slot map, stencil and SELL preconditioner for the current matrix
 // flexible CG with the learned preconditioner on A x = r (x from 0); returns

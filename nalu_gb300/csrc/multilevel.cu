@@ -1013,6 +1013,7 @@ int ml_setup(nalu_ctx* ctx, bool learned) {
   MlState& M = *ctx->ml;
   M.ready = false;
   M.learned = learned;
+  M.klevels = 0;  // V-cycle unless the flexible CG that uses it asks otherwise
   cudaStream_t s = ctx->stream;
   NALU_CUDA(ctx, grow(M.partial, 3 * 4 * kMlBlocks + 64));
   NALU_CUDA(ctx, grow(M.ks, 8 * (kMaxLevels + 2)));
@@ -1259,6 +1260,16 @@ int fcg_multilevel(nalu_ctx* ctx, double* x, double* r, double rtol, double r0no
     else cycle(ctx, M, 0, rf, zf, &site);
   };
   return fcg_df_external(ctx, x, r, rtol, r0norm, max_it, check_every, prec, iters_out);
+}
+
+int ml_apply(nalu_ctx* ctx, const float* rf, float* zf) {
+  if (!ctx->ml || !ctx->ml->ready || ctx->ml->lv.empty())
+    return set_error(ctx, NALU_ERR_STATE, "multilevel hierarchy not built");
+  MlState& M = *ctx->ml;
+  int site = 0;
+  if (M.lv.size() == 1) coarse_solve(ctx, M, 0, rf, zf, &site);
+  else cycle(ctx, M, 0, rf, zf, &site);
+  return NALU_OK;
 }
 
 void ml_free(nalu_ctx* ctx) {
