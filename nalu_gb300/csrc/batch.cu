@@ -371,10 +371,14 @@ int solve_batched(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* inf
   if (multilevel) {
     // one hierarchy for the union: aggregation follows couplings, so no
     // aggregate spans two problems, every coarse operator is block diagonal and
-    // the V-cycle applies each problem's own preconditioner
+    // the V-cycle applies each problem's own preconditioner; each problem
+    // coarsens down to the coarsest size on its own and keeps a dense block
+    // of its own there
     if (nd != 1) return set_error(ctx, NALU_ERR_ARG, "the multigrid preconditioner needs a scalar system");
     const auto ts = std::chrono::steady_clock::now();
-    if ((rc = sell_c16_ensure(ctx, s.sell)) || (rc = ml_setup(ctx, false))) return rc;
+    std::vector<int64_t> roff(P + 1);
+    for (int pr = 0; pr <= P; ++pr) roff[pr] = ctx->problem_offsets[pr] * nd;
+    if ((rc = sell_c16_ensure(ctx, s.sell)) || (rc = ml_setup(ctx, false, &roff))) return rc;
     NALU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     setup_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - ts).count();
     NALU_CUDA(ctx, rfb.alloc(n));

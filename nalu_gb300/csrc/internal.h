@@ -312,7 +312,9 @@ int learned_prepare_rows(nalu_ctx* ctx, int64_t row0, int64_t row1);
 // aggregation multigrid (multilevel.cu): the hierarchy for the current scalar
 // matrix; flexible CG with it on the residual r (in place) for the correction
 // x; the hierarchy's level sizes; its release
-int ml_setup(nalu_ctx* ctx, bool learned_smoother);
+// row_off: row ranges of independent problems (a block-diagonal union), each
+// coarsened on its own down to the coarsest size (null: one problem)
+int ml_setup(nalu_ctx* ctx, bool learned_smoother, const std::vector<int64_t>* row_off = nullptr);
 // flexible CG on FP32-pair vectors (learned.cu) preconditioned by prec(rf, zf),
 // which launches kernels computing zf ~ A^-1 rf on the context stream
 int fcg_df_external(nalu_ctx* ctx, double* x, double* r, double rtol, double r0norm, int max_it, int check_every,

@@ -643,6 +643,30 @@ __global__ void k_ml_kcombine(int64_t n, const double* __restrict__ ks, const fl
   for (int64_t i = gtid(); i < n; i += gstride()) e[i] = f1 * v1[i] + f2 * v2[i];
 }
 
+// ---- independent problems (a batch's union system) --------------------------
+// Rows of a problem that is already at or below the coarsest size get no
+// strong neighbour: they stay singletons, and the problem keeps its size on
+// the next levels while larger ones coarsen on.  off [P+1]: the problems' row
+// ranges on this level.
+__global__ void k_ml_freeze(int64_t n, const int64_t* __restrict__ off, int P, int64_t target,
+                            double* __restrict__ smax) {
+  for (int64_t i = gtid(); i < n; i += gstride()) {
+    int lo = 0, hi = P;  // off[lo] <= i < off[hi]
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (off[mid] <= i) lo = mid;
+      else hi = mid;
+    }
+    if (off[lo + 1] - off[lo] <= target && smax[i] > 0.0) smax[i] = 0.0;
+  }
+}
+// the problems' row ranges on the next level: the leaders before each range
+// (coarse rows are numbered in the order of their leaders)
+__global__ void k_ml_next_offsets(int P, const int64_t* __restrict__ off, const int32_t* __restrict__ id,
+                                  int64_t* __restrict__ out) {
+  for (int64_t p = gtid(); p <= P; p += gstride()) out[p] = id[off[p]];
+}
+
 // ---- coarsest level: dense inverse (FP32 Gauss-Jordan, one block) -----------
 // D [n][2n] row-major: the matrix and the identity beside it
 __global__ void k_ml_dense_fill(int n, float* __restrict__ D) {
@@ -656,8 +680,9 @@ __global__ void k_ml_dense_scatter(int n, const int64_t* __restrict__ rp, const 
   for (int64_t i = gtid(); i < n; i += gstride())
     for (int64_t k = rp[i]; k < rp[i + 1]; ++k) D[i * 2 * n + ci[k]] += (float)v[k];
 }
-// [A | I] -> [I | A^-1] with partial pivoting; a zero pivot sets *bad
-__global__ void __launch_bounds__(1024) k_ml_gauss_jordan(int n, float* __restrict__ D, int* __restrict__ bad) {
+// [A | I] -> [I | A^-1] with partial pivoting, by the whole block; a zero
+// pivot sets *bad
+__device__ void gauss_jordan_block(int n, float* __restrict__ D, int* __restrict__ bad) {
   __shared__ float bv[32];
   __shared__ int bi[32];
   __shared__ int piv;
@@ -725,6 +750,29 @@ __global__ void __launch_bounds__(1024) k_ml_gauss_jordan(int n, float* __restri
     __syncthreads();
   }
 }
+__global__ void __launch_bounds__(1024) k_ml_gauss_jordan(int n, float* __restrict__ D, int* __restrict__ bad) {
+  gauss_jordan_block(n, D, bad);
+}
+// one block per diagonal block: block b's [A | I] at D + doff[b], of order
+// boff[b+1] - boff[b]
+__global__ void __launch_bounds__(1024) k_ml_gauss_jordan_blocks(const int64_t* __restrict__ boff,
+                                                                 const int64_t* __restrict__ doff,
+                                                                 float* __restrict__ D, int* __restrict__ bad) {
+  const int b = blockIdx.x;
+  const int n = (int)(boff[b + 1] - boff[b]);
+  if (n > 0) gauss_jordan_block(n, D + doff[b], bad);
+}
+// one diagonal block [b0, b0 + n) of a block-diagonal matrix (rp offset to
+// its first row); entries outside the block are not expected and are skipped
+__global__ void k_ml_dense_scatter_block(int n, int64_t b0, const int64_t* __restrict__ rp,
+                                         const int32_t* __restrict__ ci, const double* __restrict__ v,
+                                         float* __restrict__ D) {
+  for (int64_t i = gtid(); i < n; i += gstride())
+    for (int64_t k = rp[i]; k < rp[i + 1]; ++k) {
+      const int64_t c = (int64_t)ci[k] - b0;
+      if (c >= 0 && c < n) D[i * 2 * n + c] += (float)v[k];
+    }
+}
 // Inv [n][n] <- right half of D
 __global__ void k_ml_dense_extract(int n, const float* __restrict__ D, float* __restrict__ Inv) {
   for (int64_t t = gtid(); t < (int64_t)n * n; t += gstride()) {
@@ -740,6 +788,24 @@ __global__ void k_ml_dense_apply(int n, const float* __restrict__ Inv, const flo
   if (row >= n) return;
   float s = 0.0f;
   for (int j = lane; j < n; j += 32) s = fmaf(Inv[row * n + j], r[j], s);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) e[row] = s;
+}
+
+// e = Inv r for a block-diagonal inverse: row's block brow[row], blocks at
+// rows [boff[b], boff[b+1]), their inverses at inv + ioff[b]; one warp per row
+__global__ void k_ml_dense_apply_blocks(int64_t n, const int32_t* __restrict__ brow, const int64_t* __restrict__ boff,
+                                        const int64_t* __restrict__ ioff, const float* __restrict__ inv,
+                                        const float* __restrict__ r, float* __restrict__ e) {
+  const int64_t row = gtid() >> 5;
+  const int lane = threadIdx.x & 31;
+  if (row >= n) return;
+  const int b = brow[row];
+  const int64_t b0 = boff[b], nb = boff[b + 1] - b0;
+  const float* I = inv + ioff[b] + (row - b0) * nb;
+  float s = 0.0f;
+  for (int64_t j = lane; j < nb; j += 32) s = fmaf(I[j], r[b0 + j], s);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
   if (lane == 0) e[row] = s;
@@ -831,6 +897,7 @@ struct MlScratch {
   DBuf<int64_t> rp[2];  // ping-pong coarse matrices of the passes within a level
   DBuf<int32_t> ci[2];
   DBuf<double> v[2];
+  DBuf<int64_t> off, off2;  // problems' row ranges on the current level, and the next
 };
 
 struct MlState {
@@ -841,6 +908,10 @@ struct MlState {
   bool learned = false;
   bool ready = false;
   int klevels = 0;            // coarse levels 1..klevels solved by K-cycle, deeper ones by V-cycle
+  // independent problems: the coarsest level's diagonal blocks (one per problem)
+  std::vector<int64_t> boff;  // block row ranges [P+1] (one block without problems)
+  DBuf<int64_t> boff_d, ioff_d;
+  DBuf<int32_t> brow;         // block of each coarsest row
 };
 
 namespace {
@@ -877,7 +948,7 @@ T read_one(nalu_ctx* ctx, const T* d) {
 
 // one pairwise pass on (n, rp, ci, v): S.agg [n] -> [0, *nc) or -1
 int pairwise_pass(nalu_ctx* ctx, MlScratch& S, int64_t n, const int64_t* rp, const int32_t* ci, const double* v,
-                  int64_t* nc_out) {
+                  int P, int64_t* nc_out) {
   cudaStream_t s = ctx->stream;
   NALU_CUDA(ctx, grow(S.smax, n));
   NALU_CUDA(ctx, grow(S.diag, n));
@@ -886,6 +957,10 @@ int pairwise_pass(nalu_ctx* ctx, MlScratch& S, int64_t n, const int64_t* rp, con
   NALU_CUDA(ctx, grow(S.id, n + 1));
   const unsigned g = grid_n(n);
   k_ml_smax<<<g, kMlThreads, 0, s>>>(n, rp, ci, v, S.smax.p, S.diag.p);
+  if (P > 1) {
+    k_ml_freeze<<<g, kMlThreads, 0, s>>>(n, S.off.p, P, kCoarsest, S.smax.p);
+    ctx->launches++;
+  }
   k_ml_fill_i32<<<g, kMlThreads, 0, s>>>(n, S.partner.p, -1);
   for (int r = 0; r < kMatchRounds; ++r) {
     k_ml_choose<<<g, kMlThreads, 0, s>>>(n, rp, ci, v, S.smax.p, S.diag.p, S.partner.p, r, S.choice.p);
@@ -1008,7 +1083,7 @@ int alloc_level_vectors(nalu_ctx* ctx, MlLevel& L, bool kcycle) {
 
 // Build the hierarchy for the current scalar matrix (for the learned smoother,
 // learned_prepare has run on it).
-int ml_setup(nalu_ctx* ctx, bool learned) {
+int ml_setup(nalu_ctx* ctx, bool learned, const std::vector<int64_t>* row_off) {
   if (!ctx->ml) ctx->ml = new MlState();
   MlState& M = *ctx->ml;
   M.ready = false;
@@ -1034,9 +1109,24 @@ int ml_setup(nalu_ctx* ctx, bool learned) {
   }
   int rc = NALU_OK;
   MlScratch& S = M.sc;
+  // problems (row ranges of independent blocks): each coarsens down to
+  // kCoarsest rows on its own; without them the whole system is one
+  std::vector<int64_t> off = row_off ? *row_off : std::vector<int64_t>{0, ctx->n_rows};
+  const int P = (int)off.size() - 1;
+  if (P < 1 || off[0] != 0 || off[P] != ctx->n_rows) return set_error(ctx, NALU_ERR_ARG, "multilevel: row ranges");
+  auto max_block = [&]() {
+    int64_t m = 0;
+    for (int p = 0; p < P; ++p) m = std::max(m, off[p + 1] - off[p]);
+    return m;
+  };
+  if (P > 1) {
+    NALU_CUDA(ctx, grow(S.off, P + 1));
+    NALU_CUDA(ctx, grow(S.off2, P + 1));
+    NALU_CUDA(ctx, cudaMemcpyAsync(S.off.p, off.data(), sizeof(int64_t) * (P + 1), cudaMemcpyHostToDevice, s));
+  }
   // levels of up to three pairwise passes each, down to kCoarsest rows
   int top = 0;  // the level being coarsened
-  while (top + 1 < kMaxLevels && M.lv[top].n > kCoarsest) {
+  while (top + 1 < kMaxLevels && max_block() > kCoarsest) {
     MlLevel& F = M.lv[top];
     NALU_CUDA(ctx, grow(F.agg, F.n));
     k_ml_iota<<<grid_n(F.n), kMlThreads, 0, s>>>(F.n, F.agg.p);
@@ -1048,8 +1138,17 @@ int ml_setup(nalu_ctx* ctx, bool learned) {
     int slot = -1;
     for (int pass = 0; pass < kPassesPerLevel; ++pass) {
       int64_t nc = 0;
-      if ((rc = pairwise_pass(ctx, S, n, rp, ci, v, &nc))) return rc;
+      if ((rc = pairwise_pass(ctx, S, n, rp, ci, v, P, &nc))) return rc;
       if (nc >= n) break;  // nothing left to pair
+      if (P > 1) {
+        k_ml_next_offsets<<<1, 128, 0, s>>>(P, S.off.p, S.id.p, S.off2.p);
+        ctx->launches++;
+        NALU_CUDA(ctx, cudaMemcpyAsync(off.data(), S.off2.p, sizeof(int64_t) * (P + 1), cudaMemcpyDeviceToHost, s));
+        NALU_CUDA(ctx, cudaMemcpyAsync(S.off.p, S.off2.p, sizeof(int64_t) * (P + 1), cudaMemcpyDeviceToDevice, s));
+        NALU_CUDA(ctx, cudaStreamSynchronize(s));
+      } else {
+        off[1] = nc;
+      }
       NALU_CUDA(ctx, grow(S.mptr, nc + 1));
       NALU_CUDA(ctx, grow(S.mem, n));
       if ((rc = build_members(ctx, S, n, nc, S.agg.p, S.mptr.p, S.mem.p))) return rc;
@@ -1063,7 +1162,7 @@ int ml_setup(nalu_ctx* ctx, bool learned) {
       v = S.v[slot].p;
       n = nc;
       nnz = cnnz;
-      if (n <= kCoarsest) break;
+      if (max_block() <= kCoarsest) break;
     }
     if (n >= F.n) break;  // no coarsening: F is the coarsest level
     NALU_CUDA(ctx, grow(F.mptr, n + 1));
@@ -1086,8 +1185,9 @@ int ml_setup(nalu_ctx* ctx, bool learned) {
   }
   M.lv.resize(top + 1);
   const int nl = (int)M.lv.size();
-  if (M.lv.back().n > kDenseMax)
+  if (max_block() > kDenseMax)
     return set_error(ctx, NALU_ERR_CAPACITY, "multilevel: coarsest level above 1024 rows (too few strong couplings)");
+  M.boff = off;
   // FP32 copies, vectors
   for (int l = 0; l < nl; ++l) {
     MlLevel& L = M.lv[l];
@@ -1124,7 +1224,7 @@ int ml_setup(nalu_ctx* ctx, bool learned) {
     const float lam = power_lambda(ctx, M, L, (l == 0 && learned) ? L.msm.p : nullptr, 12);
     L.omega = lam > 0.0f && std::isfinite(lam) ? 4.0f / (3.0f * lam) : 0.6f;
   }
-  {
+  if (P == 1) {
     // coarsest level: dense inverse
     MlLevel& C = M.lv.back();
     const int nc = (int)C.n;
@@ -1140,6 +1240,54 @@ int ml_setup(nalu_ctx* ctx, bool learned) {
     k_ml_dense_extract<<<grid_n((int64_t)nc * nc), kMlThreads, 0, s>>>(nc, D.p, C.inv.p);
     ctx->launches += 4;
     if (read_one(ctx, bad.p)) return set_error(ctx, NALU_ERR_NONFINITE, "multilevel: singular coarsest matrix");
+  } else {
+    // coarsest level of independent problems: one dense inverse per problem
+    // (the coarsest matrix is block diagonal), applied by one launch
+    MlLevel& C = M.lv.back();
+    std::vector<int64_t> ioff(P + 1, 0);
+    std::vector<int32_t> brow((size_t)std::max<int64_t>(C.n, 1), 0);
+    int64_t nbmax = 0;
+    for (int p = 0; p < P; ++p) {
+      const int64_t nb = off[p + 1] - off[p];
+      ioff[p + 1] = ioff[p] + nb * nb;
+      nbmax = std::max(nbmax, nb);
+      for (int64_t r = off[p]; r < off[p + 1]; ++r) brow[r] = p;
+    }
+    (void)nbmax;
+    DBuf<float> D;  // every block's [A | I], side by side
+    DBuf<int64_t> doff_d;
+    DBuf<int> bad;
+    NALU_CUDA(ctx, D.alloc(std::max<int64_t>(2 * ioff[P], 1)));
+    NALU_CUDA(ctx, grow(C.inv, std::max<int64_t>(ioff[P], 1)));
+    NALU_CUDA(ctx, bad.alloc(1));
+    NALU_CUDA(ctx, doff_d.alloc(P + 1));
+    NALU_CUDA(ctx, cudaMemsetAsync(bad.p, 0, sizeof(int), s));
+    std::vector<int64_t> doff(P + 1);
+    for (int p = 0; p <= P; ++p) doff[p] = 2 * ioff[p];
+    NALU_CUDA(ctx, cudaMemcpyAsync(doff_d.p, doff.data(), sizeof(int64_t) * (P + 1), cudaMemcpyHostToDevice, s));
+    NALU_CUDA(ctx, grow(M.boff_d, P + 1));
+    NALU_CUDA(ctx, grow(M.ioff_d, P + 1));
+    NALU_CUDA(ctx, cudaMemcpyAsync(M.boff_d.p, off.data(), sizeof(int64_t) * (P + 1), cudaMemcpyHostToDevice, s));
+    NALU_CUDA(ctx, cudaMemcpyAsync(M.ioff_d.p, ioff.data(), sizeof(int64_t) * (P + 1), cudaMemcpyHostToDevice, s));
+    for (int p = 0; p < P; ++p) {
+      const int nb = (int)(off[p + 1] - off[p]);
+      if (nb == 0) continue;
+      k_ml_dense_fill<<<grid_n((int64_t)nb * 2 * nb), kMlThreads, 0, s>>>(nb, D.p + doff[p]);
+      k_ml_dense_scatter_block<<<grid_n(nb), kMlThreads, 0, s>>>(nb, off[p], C.rp + off[p], C.ci, C.vd,
+                                                                 D.p + doff[p]);
+      ctx->launches += 2;
+    }
+    k_ml_gauss_jordan_blocks<<<P, 1024, 0, s>>>(M.boff_d.p, doff_d.p, D.p, bad.p);
+    ctx->launches++;
+    for (int p = 0; p < P; ++p) {
+      const int nb = (int)(off[p + 1] - off[p]);
+      if (nb == 0) continue;
+      k_ml_dense_extract<<<grid_n((int64_t)nb * nb), kMlThreads, 0, s>>>(nb, D.p + doff[p], C.inv.p + ioff[p]);
+      ctx->launches++;
+    }
+    NALU_CUDA(ctx, grow(M.brow, (int64_t)brow.size()));
+    NALU_CUDA(ctx, cudaMemcpyAsync(M.brow.p, brow.data(), sizeof(int32_t) * brow.size(), cudaMemcpyHostToDevice, s));
+    if (read_one(ctx, bad.p)) return set_error(ctx, NALU_ERR_NONFINITE, "multilevel: singular coarsest block");
   }
   NALU_CUDA(ctx, cudaStreamSynchronize(s));
   M.ready = true;
@@ -1158,8 +1306,11 @@ void coarse_solve(nalu_ctx* ctx, MlState& M, int l, const float* r, float* e, in
   MlLevel& L = M.lv[l];
   const int nl = (int)M.lv.size();
   if (l == nl - 1) {
-    k_ml_dense_apply<<<(unsigned)((L.n * 32 + kMlThreads - 1) / kMlThreads), kMlThreads, 0, s>>>((int)L.n, L.inv.p, r,
-                                                                                                  e);
+    const unsigned g = (unsigned)((L.n * 32 + kMlThreads - 1) / kMlThreads);
+    if (M.boff.size() > 2)
+      k_ml_dense_apply_blocks<<<g, kMlThreads, 0, s>>>(L.n, M.brow.p, M.boff_d.p, M.ioff_d.p, L.inv.p, r, e);
+    else
+      k_ml_dense_apply<<<g, kMlThreads, 0, s>>>((int)L.n, L.inv.p, r, e);
     ctx->launches++;
     return;
   }
