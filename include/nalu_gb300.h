@@ -401,7 +401,10 @@ int nalu_set_problems(nalu_ctx* ctx, int n, const int64_t* node_offsets);
  * every problem opens with Jacobi-CG; only problems with many predicted
  * iterations left are candidates, and the learned preconditioner is set up
  * (rows of that problem only) and tried on the largest one first; the others
- * follow only if it beats its own Jacobi-CG rate per unit of device time. */
+ * follow only if it beats its own Jacobi-CG rate per unit of device time.
+ * With NALU_PRECOND_MULTILEVEL every problem runs flexible CG preconditioned by
+ * one aggregation-multigrid hierarchy of the union (block diagonal: each
+ * problem coarsens on its own and keeps its own dense coarsest block). */
 int nalu_solve_batched(nalu_ctx* ctx, const nalu_solver_opts* opts, nalu_solve_info* infos);
 
 /* ---- learned preconditioner -------------------------------------------- */
