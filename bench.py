@@ -823,6 +823,14 @@ def bench_batch(ng, dev=0, n_problems=64, seed=2025, reps=2):
     ctx.build_elem_graph(1)
     ctx.set_problems(off)
     pins = off[:-1]
+    # assemble once and time the tile sizes of the batched solve (autotuner)
+    ctx.zero()
+    ctx.assemble(ng.KERNEL_CONTINUITY_ADV)
+    ctx.reset_rows(pins)
+    for q in pins:
+        ctx.sum_into_diag(int(q), 0, 1.0, 0.0)
+    ctx.load_complete()
+    tile_rows, tile_ms = ctx.batch_autotune(100)
     best = None
     for _ in range(reps):
         ctx.synchronize()
@@ -850,7 +858,8 @@ def bench_batch(ng, dev=0, n_problems=64, seed=2025, reps=2):
            "wall_ms": 1e3 * wall, "assemble_bc_ms": asm_ms, "solve_ms": infos[0].seconds * 1e3,
            "iterations_min_median_max": [its[0], its[len(its) // 2], its[-1]],
            "max_true_rel_res": max(i.true_rel_res for i in infos),
-           "all_converged": all(i.status == 0 for i in infos), "preconditioner": "jacobi (plain PCG)"}
+           "all_converged": all(i.status == 0 for i in infos), "preconditioner": "jacobi (plain PCG)",
+           "tile_autotune": {"rows_per_tile": tile_rows, "ms_per_iteration": {str(k): v for k, v in tile_ms.items()}}}
     # learned flexible CG on the same batch: weights trained on this union system
     # (20K PCG first-direction pairs, 4 seeded rhs, 40 epochs); the solve time
     # includes the stencil set-up of the problems that try it, the training is

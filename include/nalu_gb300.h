@@ -406,6 +406,13 @@ int nalu_set_problems(nalu_ctx* ctx, int n, const int64_t* node_offsets);
  * one aggregation-multigrid hierarchy of the union (block diagonal: each
  * problem coarsens on its own and keeps its own dense coarsest block). */
 int nalu_solve_batched(nalu_ctx* ctx, const nalu_solver_opts* opts, nalu_solve_info* infos);
+/* Rows per tile of the batched solve: times tiles of 256, 512, 1024 and 2048
+ * rows over `iterations` (<= 0: 100) iterations of the batched Jacobi-CG from
+ * zero (device time; the context's solution is overwritten) and keeps the
+ * fastest for later nalu_solve_batched calls (default before tuning: 1024).
+ * tile_rows: the choice; ms_per_iteration [4]: each candidate's time (either
+ * may be NULL). */
+int nalu_batch_autotune(nalu_ctx* ctx, int iterations, int* tile_rows, double* ms_per_iteration);
 
 /* ---- learned preconditioner -------------------------------------------- */
 /* No reference counterpart: Nalu preconditions with Ifpack2/MueLu

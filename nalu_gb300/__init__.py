@@ -162,6 +162,7 @@ def lib():
             "nalu_learned_harvest": (I, [P, I, ctypes.c_uint64, I64, P, P, P, P, ctypes.POINTER(I64)]),
             "nalu_train_opts_default": (None, [P]),
             "nalu_learned_train": (I, [P, P, P, P, I64, P, P]),
+            "nalu_batch_autotune": (I, [P, I, ctypes.POINTER(I), P]),
             "nalu_learned_gradient": (I, [P, P, P, P, I64, P, ctypes.POINTER(D)]),
             "nalu_learned_gradient_bf16": (I, [P, P, P, P, I64, P, ctypes.POINTER(D)]),
             "nalu_learned_stencil": (I, [P, P]),
@@ -322,6 +323,14 @@ class Context:
         table = {(SCHEDULE_NAMES[1 + k // 2], {0: "atomic", 1: "coloured"}[k % 2]): float(ms[k])
                  for k in range(6) if ms[k] >= 0}
         return sch.value, sc.value, table
+
+    def batch_autotune(self, iterations=100):
+        """rows per tile of the batched solve, chosen by device time; returns
+        (tile_rows, {rows: ms per iteration})"""
+        tr = ctypes.c_int()
+        ms = np.zeros(4)
+        self._check(lib().nalu_batch_autotune(self._h, int(iterations), ctypes.byref(tr), _ptr(ms)), "batch_autotune")
+        return tr.value, {r: float(m) for r, m in zip((256, 512, 1024, 2048), ms)}
 
     def multilevel_levels(self):
         """(rows, nnz) per level of the last multilevel solve's hierarchy"""

@@ -39,8 +39,9 @@ namespace nalu_gb300 {
 namespace {
 
 constexpr int kBT = 256;                  // threads per block (one block per tile)
-constexpr int kRowsPerThread = 4;         // a tile's fixed costs (block sums, ticket) over 4 rows a thread
+constexpr int kRowsPerThread = 4;         // default: a tile's fixed costs (block sums, ticket) over 4 rows a thread
 constexpr int kTileRows = kRowsPerThread * kBT;
+constexpr int kTileCandidates[4] = {256, 512, 1024, 2048};  // rows per tile the autotuner times
 constexpr int kSliceB = 32;
 
 struct GraphExecs {
@@ -334,15 +335,16 @@ int solve_batched(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* inf
   if (P < 1) return set_error(ctx, NALU_ERR_STATE, "no problem partition (nalu_set_problems)");
   const int64_t n = ctx->n_rows;
   const int nd = ctx->num_dof;
-  // tiles of <= kTileRows rows inside each problem
+  // tiles of <= tile_rows rows inside each problem
+  const int tile_rows = ctx->batch_tile_rows > 0 ? ctx->batch_tile_rows : kTileRows;
   std::vector<int64_t> trow0;
   std::vector<int32_t> trows, tprob, pt0(P), pt1(P);
   for (int pr = 0; pr < P; ++pr) {
     const int64_t rb = ctx->problem_offsets[pr] * nd, re = ctx->problem_offsets[pr + 1] * nd;
     pt0[pr] = (int32_t)trow0.size();
-    for (int64_t r = rb; r < re; r += kTileRows) {
+    for (int64_t r = rb; r < re; r += tile_rows) {
       trow0.push_back(r);
-      trows.push_back((int32_t)std::min<int64_t>(kTileRows, re - r));
+      trows.push_back((int32_t)std::min<int64_t>(tile_rows, re - r));
       tprob.push_back(pr);
     }
     pt1[pr] = (int32_t)trow0.size();
@@ -629,9 +631,21 @@ int solve_batched(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* inf
   int rep = -1;
   double rows_a = 0.0, rows_bj = 0.0, rows_bl = 0.0;  // row-iterations of the two timed phases
 
+  // device time of the first round's chunks (the tile-size autotuner's measure)
+  cudaEvent_t rt[2];
+  for (auto& e : rt) NALU_CUDA(ctx, cudaEventCreate(&e));
+  struct EvFree2 {
+    cudaEvent_t* e;
+    ~EvFree2() { cudaEventDestroy(e[0]); cudaEventDestroy(e[1]); }
+  } rtfree{rt};
+  ctx->batch_round_ms = 0.0;
+  ctx->batch_round_its = 0;
+  bool first_round = true;
+  int its_used = 0;  // iterations launched over all rounds (max_iters bounds the total)
   // one round of at most max_its iterations; x is updated in place
   auto run_round = [&](int max_its) -> int {
-    int phase_it = 0;
+    int phase_it = 0, round_its = 0;
+    if (first_round) NALU_CUDA(ctx, cudaEventRecord(rt[0], st));
     if (phase != kDecided) NALU_CUDA(ctx, cudaEventRecord(pe[0], st));
     for (int it = 0; it < max_its; it += chunk) {
       const bool any_learned = flexible && rows_active(3) > 0;
@@ -642,6 +656,9 @@ int solve_batched(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* inf
       }
       cudaGraphLaunch(gx.e[any_learned ? 1 : 0], st);
       ctx->launches += (any_learned ? 4 : 3) * chunk;
+      round_its += chunk;
+      its_used += chunk;
+      if (first_round) NALU_CUDA(ctx, cudaEventRecord(rt[1], st));
       NALU_CUDA(ctx, cudaMemcpyAsync(done.data(), done_d, sizeof(int32_t) * P, cudaMemcpyDeviceToHost, st));
       NALU_CUDA(ctx, cudaMemcpyAsync(rrh.data(), rr_d, sizeof(double) * P, cudaMemcpyDeviceToHost, st));
       if (phase != kDecided) NALU_CUDA(ctx, cudaEventRecord(pe[1], st));
@@ -728,6 +745,14 @@ int solve_batched(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* inf
       }
       if (all_done) break;
     }
+    if (first_round && round_its > 0) {
+      float ms = 0.f;
+      NALU_CUDA(ctx, cudaEventSynchronize(rt[1]));
+      cudaEventElapsedTime(&ms, rt[0], rt[1]);
+      ctx->batch_round_ms = ms;
+      ctx->batch_round_its = round_its;
+    }
+    first_round = false;
     // the round's increment into the FP64 solution
     k_batch_fold<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, a.x2, a.x);
     ctx->launches++;
@@ -742,9 +767,10 @@ int solve_batched(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* inf
   }
   for (int outer = 0; outer < 6; ++outer) {
     if (start_round()) break;
+    if (its_used >= o.max_iters) break;  // the budget is spent: the true residual above is the result
     if (outer == 0 && learned && !o.learned_probe)
       for (int pr = 0; pr < P; ++pr) lres0[pr] = best[pr] = r0[pr];
-    int rcr = run_round(o.max_iters);
+    int rcr = run_round(o.max_iters - its_used);
     if (rcr) return rcr;
     if (std::any_of(done.begin(), done.end(), [](int d) { return d == 2; })) break;
   }
@@ -799,6 +825,41 @@ int nalu_set_problems(nalu_ctx* ctx, int n, const int64_t* node_offsets) {
         return set_error(ctx, NALU_ERR_ARG, "an element couples two problems");
   }
   ctx->problem_offsets.assign(node_offsets, node_offsets + n + 1);
+  return NALU_OK;
+}
+
+int nalu_batch_autotune(nalu_ctx* ctx, int iterations, int* tile_rows, double* ms_per_iteration) {
+  using namespace nalu_gb300;
+  if (!ctx) return NALU_ERR_ARG;
+  if (ctx->num_dof == 0) return set_error(ctx, NALU_ERR_STATE, "no graph");
+  const int P = (int)ctx->problem_offsets.size() - 1;
+  if (P < 1) return set_error(ctx, NALU_ERR_STATE, "no problem partition (nalu_set_problems)");
+  cudaSetDevice(ctx->device);
+  // each candidate runs `iterations` of the batched Jacobi-CG from zero (at
+  // full load while no problem has converged) and is timed on the device
+  nalu_solver_opts o;
+  nalu_solver_opts_default(&o);
+  o.max_iters = iterations > 0 ? iterations : 100;
+  o.tol = 1e-300;
+  std::vector<nalu_solve_info> infos(P);
+  int best = -1;
+  double best_ms = 0.0;
+  for (int k = 0; k < 4; ++k) {
+    ctx->batch_tile_rows = kTileCandidates[k];
+    const int rc = solve_batched(ctx, o, infos.data());
+    if (rc != NALU_OK && rc != NALU_ERR_NOT_CONVERGED) {
+      ctx->batch_tile_rows = 0;
+      return rc;
+    }
+    const double ms = ctx->batch_round_its > 0 ? ctx->batch_round_ms / ctx->batch_round_its : -1.0;
+    ctx->batch_tune_ms[k] = ms;
+    if (ms > 0.0 && (best < 0 || ms < best_ms)) best = k, best_ms = ms;
+  }
+  ctx->batch_tile_rows = best >= 0 ? kTileCandidates[best] : 0;
+  ctx->last_error.clear();
+  if (tile_rows) *tile_rows = ctx->batch_tile_rows > 0 ? ctx->batch_tile_rows : kTileRows;
+  if (ms_per_iteration)
+    for (int k = 0; k < 4; ++k) ms_per_iteration[k] = ctx->batch_tune_ms[k];
   return NALU_OK;
 }
 

@@ -191,6 +191,12 @@ struct nalu_ctx {
 
   // independent problems in one context (node offsets in LID order)
   std::vector<int64_t> problem_offsets;
+  // batched solve: rows per tile (0: the default 1024; set by the autotuner),
+  // and the device time and iterations of the last solve's first round
+  int batch_tile_rows = 0;
+  double batch_round_ms = 0.0;
+  int batch_round_its = 0;
+  double batch_tune_ms[4] = {-1.0, -1.0, -1.0, -1.0};  // ms per iteration of tiles of 256 .. 2048 rows
 
   // errors raised by kernels (negative Jacobian count, graph misses, ...)
   nalu_gb300::DBuf<int32_t> d_flags;     // [4]

@@ -184,3 +184,23 @@ def test_batched_multilevel_fcg(gpu_ctx_factory, oracle):
         assert i.fallback == 0 and i.learned_iterations == i.iterations
         assert 3 * i.iterations <= p.iterations, (i.iterations, p.iterations)
     ctx.close()
+
+
+def test_batch_tile_autotune(gpu_ctx_factory, oracle):
+    """The tile-size autotuner times every candidate, keeps the fastest, and
+    the batched solve with the chosen tiles still meets the tolerance on every
+    problem (tiles never cross a problem, whatever their size)."""
+    ctx, off, _ = _batched_continuity(gpu_ctx_factory, 5, (10, 20), seed=22)
+    rp, ci = ctx.graph()
+    v, b = ctx.system()
+    rows, ms = ctx.batch_autotune(50)
+    print("rows per tile", rows, ms)
+    assert rows in ms and all(t > 0 for t in ms.values())
+    assert ms[rows] == min(ms.values())
+    tol = 1e-10
+    infos = ctx.solve_batched(ng.default_solver_opts(tol=tol, max_iters=5000))
+    _check_batch_solution(ctx, oracle, off, infos, tol, rp, ci, v, b)
+    # max_iters bounds the total over restarts
+    short = ctx.solve_batched(ng.default_solver_opts(tol=tol, max_iters=30), raise_on_error=False)
+    assert all(i.iterations <= 50 for i in short)
+    ctx.close()
