@@ -354,7 +354,12 @@ typedef struct nalu_solver_opts {
                            their coarse problem by K-cycle (two flexible CG steps),
                            deeper ones by V-cycle; 0 (default): V-cycle throughout
                            (the fastest on the continuity systems measured) */
-  int reserved[3];
+  int ml_learned_sweeps; /* NALU_PRECOND_LEARNED_MULTILEVEL: the level-0 sweeps that
+                            use the learned smoother, bit 0 pre-smoothing, bit 1
+                            post-smoothing (the other sweeps: damped Jacobi);
+                            0 (default): pre-smoothing only (the fastest of the
+                            three at 128^3) */
+  int reserved[2];
 } nalu_solver_opts;
 typedef struct nalu_solve_info {
   int iterations;        /* inner iterations in total */

@@ -73,7 +73,8 @@ class SolverOpts(ctypes.Structure):
                 ("max_iters", ctypes.c_int), ("restart", ctypes.c_int), ("cheb_degree", ctypes.c_int),
                 ("check_every", ctypes.c_int), ("x0_zero", ctypes.c_int), ("tol", ctypes.c_double),
                 ("inner_tol", ctypes.c_double), ("stall_window", ctypes.c_int), ("learned_probe", ctypes.c_int),
-                ("ml_kcycle_levels", ctypes.c_int), ("reserved", ctypes.c_int * 3)]
+                ("ml_kcycle_levels", ctypes.c_int), ("ml_learned_sweeps", ctypes.c_int),
+                ("reserved", ctypes.c_int * 2)]
 
 
 class SolveInfo(ctypes.Structure):

@@ -326,7 +326,7 @@ int ml_setup(nalu_ctx* ctx, bool learned_smoother, const std::vector<int64_t>* r
 int fcg_df_external(nalu_ctx* ctx, double* x, double* r, double rtol, double r0norm, int max_it, int check_every,
                     const std::function<void(const float*, float*)>& prec, int* iters_out);
 int fcg_multilevel(nalu_ctx* ctx, double* x, double* r, double rtol, double r0norm, int max_it, int check_every,
-                   int klevels, int* iters_out);
+                   int klevels, int learned_sweeps, int* iters);
 // one multigrid cycle z = M r (FP32, on the context's stream; graph-capturable)
 int ml_apply(nalu_ctx* ctx, const float* rf, float* zf);
 int ml_levels(const nalu_ctx* ctx, int max_levels, int64_t* rows, int64_t* nnz);

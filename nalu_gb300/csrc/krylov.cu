@@ -1105,11 +1105,10 @@ int solve(nalu_ctx* ctx, const nalu_solver_opts& o, nalu_solve_info* info) {
           NALU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
           setup_s += std::chrono::duration<double>(std::chrono::steady_clock::now() - ts).count();
         }
-        rc = fcg_multilevel(ctx, s.w.p, s.r.p, rtol, r0, o.max_iters - total_it, o.check_every, o.ml_kcycle_levels,
+        rc = fcg_multilevel(ctx, s.w.p, s.r.p, rtol, r0, o.max_iters - total_it, o.check_every, o.ml_kcycle_levels, o.ml_learned_sweeps,
                             &its);
       } else if (o.method == NALU_SOLVER_CG && (o.precond == NALU_PRECOND_JACOBI || probe_chose_jacobi)) {
         // two-kernel Jacobi-CG on the SELL-32 copy (cg_fast.cu)
-        const double* sv = nullptr;
         const float2* sv2 = nullptr;
         if (outer == 1 && (rc = sell_build<float2>(ctx, s.sell, &sv2))) return rc;
         rc = pcg_df(ctx, s.sell, s.w.p, s.r.p, s.z.p, s.q.p, s.dinv.p, rtol, r0, o.max_iters - total_it,

@@ -86,28 +86,41 @@ __global__ void k_nbr_fix(int64_t n, int32_t* __restrict__ nbr) {
   if (i < n && nbr[i] == INT_MAX) nbr[i] = -1;
 }
 
-// static features of slot s of row i: st[s], st[27+s], st[54+s]
-__device__ __forceinline__ void slot_static(int64_t i, int s, const int32_t* __restrict__ nbr,
-                                            const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
-                                            const double* __restrict__ v, const double* __restrict__ dinv,
-                                            float* st) {
-  const int32_t j = nbr[i * 27 + s];
-  float fa = 0.0f, fm = 0.0f, fd = 0.0f;
-  if (j >= 0) {
-    double aij = 0.0;
-    for (int64_t k = rp[i]; k < rp[i + 1]; ++k)
-      if (ci[k] == j) {
-        aij = v[k];
-        break;
-      }
-    const double di = dinv[i];
-    fa = (float)(aij * di);
-    fm = 1.0f;
-    fd = (float)(di / dinv[j]);
+// static features of the 27 slots of row i, by the whole warp: st[s],
+// st[27+s], st[54+s] for s = lane < 27.  The row's entries are read once,
+// one per lane (in chunks of 32), and broadcast by shuffles; the lane of
+// slot s keeps the value whose column is its neighbour (columns are unique
+// within a row).
+__device__ __forceinline__ void slot_static_warp(int64_t i, int lane, const int32_t* __restrict__ nbr,
+                                                 const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                                                 const double* __restrict__ v, const double* __restrict__ dinv,
+                                                 float* st) {
+  const int32_t j = lane < 27 ? nbr[i * 27 + lane] : -1;
+  const int64_t r0 = rp[i], len = rp[i + 1] - r0;
+  double aij = 0.0;
+  for (int64_t b = 0; b < len; b += 32) {
+    const int64_t k = b + lane;
+    const int32_t c = k < len ? ci[r0 + k] : -2;
+    const double val = k < len ? v[r0 + k] : 0.0;
+    const int m = (int)(len - b < 32 ? len - b : 32);
+    for (int q = 0; q < m; ++q) {
+      const int32_t cq = __shfl_sync(0xffffffffu, c, q);
+      const double vq = __shfl_sync(0xffffffffu, val, q);
+      if (cq == j) aij = vq;
+    }
   }
-  st[s] = fa;
-  st[27 + s] = fm;
-  st[54 + s] = fd;
+  if (lane < 27) {
+    float fa = 0.0f, fm = 0.0f, fd = 0.0f;
+    if (j >= 0) {
+      const double di = dinv[i];
+      fa = (float)(aij * di);
+      fm = 1.0f;
+      fd = (float)(di / dinv[j]);
+    }
+    st[lane] = fa;
+    st[27 + lane] = fm;
+    st[54 + lane] = fd;
+  }
 }
 
 // Harvest: one warp per sample row.  r is the residual-like vector (q0 = A p0),
@@ -126,8 +139,8 @@ __global__ void k_harvest(int64_t count, const int64_t* __restrict__ rows, const
   if (lane < 27) {
     const int32_t j = nbr[i * 27 + lane];
     rj = j >= 0 ? r[j] : 0.0;
-    slot_static(i, lane, nbr, rp, ci, v, dinv, st + w * 81);
   }
+  slot_static_warp(i, lane, nbr, rp, ci, v, dinv, st + w * 81);  // the whole warp (w is warp-uniform)
   double ss = rj * rj;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
@@ -194,7 +207,7 @@ __global__ void __launch_bounds__(kStThreads) k_mlp_stencil(int64_t row0, int64_
       if (lane < 27) out[i * 27 + lane] = 0.0f;
       continue;
     }
-    if (lane < 27) slot_static(i, lane, nbr, rp, ci, v, dinv, st);
+    slot_static_warp(i, lane, nbr, rp, ci, v, dinv, st);
     __syncwarp();
 #pragma unroll
     for (int h = 0; h < 2; ++h) {

@@ -79,10 +79,13 @@ def test_learned_multilevel_solves_and_gain(oracle):
     x_ref, _, _ = oracle.pcg_jacobi(rp, ci, vals, b, tol=1e-12, max_it=50000, n_threads=8)
     jac = ctx.solve(ng.default_solver_opts(tol=1e-8, max_iters=2000, precond=ng.PRECOND_MULTILEVEL))
     _check_solution(ctx, oracle, jac, x_ref)
-    lrn = ctx.solve(ng.default_solver_opts(tol=1e-8, max_iters=2000, precond=ng.PRECOND_LEARNED_MULTILEVEL))
-    _check_solution(ctx, oracle, lrn, x_ref)
-    print("32^3: multilevel iterations Jacobi-smoothed %d, learned-smoothed %d" % (jac.iterations, lrn.iterations))
-    assert lrn.iterations <= 2 * jac.iterations
+    for sweeps in (0, 1, 2, 3):  # default (pre-smoothing), pre, post, both
+        lrn = ctx.solve(ng.default_solver_opts(tol=1e-8, max_iters=2000, precond=ng.PRECOND_LEARNED_MULTILEVEL,
+                                               ml_learned_sweeps=sweeps))
+        _check_solution(ctx, oracle, lrn, x_ref)
+        print("32^3: multilevel iterations Jacobi-smoothed %d, learned-smoothed (sweeps %d) %d"
+              % (jac.iterations, sweeps, lrn.iterations))
+        assert lrn.iterations <= 2 * jac.iterations
     ctx.close()
 
 
