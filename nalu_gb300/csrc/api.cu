@@ -543,7 +543,7 @@ int nalu_linsys_build_elem_graph(nalu_ctx* ctx, int num_dof) {
   NALU_CUDA(ctx, cudaMemsetAsync(ctx->d_values.p, 0, sizeof(double) * ctx->nnz, ctx->stream));
   NALU_CUDA(ctx, cudaMemsetAsync(ctx->d_rhs.p, 0, sizeof(double) * ctx->n_rows, ctx->stream));
   NALU_CUDA(ctx, cudaMemsetAsync(ctx->d_x.p, 0, sizeof(double) * ctx->n_rows, ctx->stream));
-  for (int& s : ctx->scatter_choice) s = 0;
+  for (auto& k : ctx->scatter_choice) k[0] = k[1] = 0;
   for (int k = 0; k < 2; ++k) ctx->df_schedule[k] = ctx->df_scatter[k] = 0;
   // the host build (sorting, colouring) is synchronous; the uploads finish here
   NALU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -912,7 +912,8 @@ int nalu_assemble(nalu_ctx* ctx, int kernel, const nalu_assemble_opts* opts) {
     return rc;
   }
   if (scatter == NALU_SCATTER_AUTO) {
-    scatter = ctx->scatter_choice[kernel];
+    const int ar = opts->arith == NALU_ARITH_DF64 ? 1 : 0;
+    scatter = ctx->scatter_choice[kernel][ar];
     if (scatter == 0) {
       // autotune: time both strategies on scratch copies of values/rhs
       DBuf<double> sv, sr;
@@ -933,7 +934,7 @@ int nalu_assemble(nalu_ctx* ctx, int kernel, const nalu_assemble_opts* opts) {
       NALU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
       sv.free();
       sr.free();
-      ctx->scatter_choice[kernel] = pick;
+      ctx->scatter_choice[kernel][ar] = pick;
       scatter = pick;
       rc = check_flags(ctx);
       if (rc) return rc;

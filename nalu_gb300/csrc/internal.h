@@ -183,7 +183,7 @@ struct nalu_ctx {
   nalu_gb300::DBuf<int32_t> d_colour_elems;  // element ids grouped by colour
   nalu_gb300::DBuf<double> d_node_df;    // df64 split of nodal kernel inputs (8 B each)
   std::vector<int64_t> colour_offsets;   // [n_colours+1]
-  int scatter_choice[6] = {0, 0, 0, 0, 0, 0};  // autotuned scatter per kernel (0 = not tuned)
+  int scatter_choice[6][2] = {};  // autotuned scatter per kernel and arithmetic (FP64, df64; 0 = not tuned)
   // autotuned schedule x scatter of the double-float scalar kernels, per kernel,
   // with the device time of every candidate [schedule - 1][scatter - 1]
   int df_schedule[2] = {0, 0}, df_scatter[2] = {0, 0};
