@@ -357,8 +357,10 @@ typedef struct nalu_solver_opts {
   int ml_learned_sweeps; /* NALU_PRECOND_LEARNED_MULTILEVEL: the level-0 sweeps that
                             use the learned smoother, bit 0 pre-smoothing, bit 1
                             post-smoothing (the other sweeps: damped Jacobi);
-                            0 (default): pre-smoothing only (the fastest of the
-                            three at 128^3) */
+                            0 (default): both, a symmetric cycle (one sweep is
+                            faster on some systems, 83.7 against 92.4 ms at
+                            128^3, but the cycle is then unsymmetric and
+                            converged far slower on others) */
   int reserved[2];
 } nalu_solver_opts;
 typedef struct nalu_solve_info {

@@ -909,7 +909,7 @@ struct MlState {
   bool learned = false;
   bool ready = false;
   int klevels = 0;            // coarse levels 1..klevels solved by K-cycle, deeper ones by V-cycle
-  int lsweeps = 1;            // learned smoother: pre-smoothing (bit 0), post-smoothing (bit 1); else Jacobi
+  int lsweeps = 3;            // learned smoother: pre-smoothing (bit 0), post-smoothing (bit 1); else Jacobi
   // independent problems: the coarsest level's diagonal blocks (one per problem)
   std::vector<int64_t> boff;  // block row ranges [P+1] (one block without problems)
   DBuf<int64_t> boff_d, ioff_d;
@@ -1414,9 +1414,11 @@ int fcg_multilevel(nalu_ctx* ctx, double* x, double* r, double rtol, double r0no
     return set_error(ctx, NALU_ERR_STATE, "multilevel hierarchy not built");
   MlState& M = *ctx->ml;
   M.klevels = std::max(klevels, 0);
-  // default: the learned smoother in pre-smoothing only (at 128^3: 89 steps,
-  // 83.7 ms; in both sweeps 83 steps but 92.4 ms; post only 89 steps, 83.9 ms)
-  M.lsweeps = learned_sweeps > 0 ? (learned_sweeps & 3) : 1;
+  // default: the learned smoother in both sweeps, which keeps the cycle
+  // symmetric (at 128^3: 83 steps, 92.4 ms; pre-smoothing only 89 steps,
+  // 83.7 ms, but that unsymmetric cycle took 1960 steps instead of 273 on the
+  // 64-mesh union system)
+  M.lsweeps = learned_sweeps > 0 ? (learned_sweeps & 3) : 3;
   auto prec = [&](const float* rf, float* zf) {
     int site = 0;
     if (M.lv.size() == 1) coarse_solve(ctx, M, 0, rf, zf, &site);  // one level: the dense inverse
