@@ -753,7 +753,7 @@ def bench_c4(ng, weights, dev=0, N=192):
     ctx.build_elem_graph(1)
     n_rows, nnz, _ = ctx.sizes()
     E = conn.shape[0]
-    # the assembly at this size (the benchmark spec's 192^3 target): both
+    # the assembly at this size (the 192^3 assembly target): both
     # arithmetics, best scatter each, device time per launch
     asm = {}
     peak, peak_kind = peaks()
