@@ -122,7 +122,7 @@ __device__ __forceinline__ void jacobian_rot_df(const df64* EF, int dd, int t1, 
 // G'_k = sum_i C'[i][k] area[i]
 __device__ __forceinline__ void g_of(const df64 c[3][3], const df64 area[3], df64 g[3]) {
 #pragma unroll
-  for (int k = 0; k < 3; ++k) g[k] = df_fma(c[2][k], area[2], df_fma(c[1][k], area[1], df_mul(c[0][k], area[0])));
+  for (int k = 0; k < 3; ++k) g[k] = df_dot3(c[0][k], area[0], c[1][k], area[1], c[2][k], area[2]);
 }
 
 // The eight lhs factors sum_k dN_c/ds_k g_k at an ip of the rotated frame
@@ -302,7 +302,7 @@ __global__ void __launch_bounds__(IpSched<EPB, ip_light<KIND, MODE, SHIFT>()>::k
         const df64 wx = trilinear_rot_df(s_wc[el], t1, t2, m1, m2);
         const df64 wy = trilinear_rot_df(s_wc[el] + 8, t1, t2, m1, m2);
         const df64 wz = trilinear_rot_df(s_wc[el] + 16, t1, t2, m1, m2);
-        df64 m = df_mul(df_fma(wz, area[2], df_fma(wy, area[1], df_mul(wx, area[0]))), a.inv_tau);
+        df64 m = df_mul(df_dot3(wx, area[0], wy, area[1], wz, area[2]), a.inv_tau);
         if (MODE == 1) {
           // reduced sensitivities: the standard-location pressure term joins mdot
           const df64 sstd = df_neg(df_rcp(det));
@@ -330,22 +330,20 @@ __global__ void __launch_bounds__(IpSched<EPB, ip_light<KIND, MODE, SHIFT>()>::k
   ips[1] = rb + (rq == 0 ? 3 : rq);
   ips[2] = 8 + rq;
   const int kexp = s_k[el];
+  // each entry sums its three ips' factors (ascending ip) as one unnormalised
+  // pair; the widening to FP64 below renormalises it
+  const bool l0 = ip_left(ips[0]) == r, l1 = ip_left(ips[1]) == r, l2 = ip_left(ips[2]) == r;
+  const df64* F0 = &s_fac[el][kFacRow * ips[0]];
+  const df64* F1 = &s_fac[el][kFacRow * ips[1]];
+  const df64* F2 = &s_fac[el][kFacRow * ips[2]];
   df64 v[8];
+#pragma unroll
+  for (int c = 0; c < 8; ++c)
+    v[c] = df_sum3_lazy(l0 ? F0[c] : df_neg(F0[c]), l1 ? F1[c] : df_neg(F1[c]), l2 ? F2[c] : df_neg(F2[c]));
   df64 rs = df_zero();
-#pragma unroll
-  for (int q = 0; q < 3; ++q) {
-    const int ip = ips[q];
-    const bool left = ip_left(ip) == r;
-    const df64* F = &s_fac[el][kFacRow * ip];
-#pragma unroll
-    for (int c = 0; c < 8; ++c) {
-      const df64 f = left ? F[c] : df_neg(F[c]);
-      v[c] = q == 0 ? f : df_add(v[c], f);
-    }
-    if (KIND == 1) {
-      const df64 m = s_m[el][ip];
-      rs = df_add(rs, left ? df_neg(m) : m);
-    }
+  if (KIND == 1) {
+    const df64 m0 = s_m[el][ips[0]], m1 = s_m[el][ips[1]], m2 = s_m[el][ips[2]];
+    rs = df_sum3_lazy(l0 ? df_neg(m0) : m0, l1 ? df_neg(m1) : m1, l2 ? df_neg(m2) : m2);
   }
   const bool rhs_from_lhs = (KIND == 0) || (MODE != 1);
   double s = KIND == 1 ? df_to_double_bits(rs, 2 * kexp) : 0.0;

@@ -130,7 +130,7 @@ NALU_HD void cofactor_df(const df64 j[3][3], df64 adj[3][3], df64& det) {
   adj[2][0] = df_cross(j[0][1], j[1][2], j[1][1], j[0][2]);
   adj[2][1] = df_cross(j[0][2], j[1][0], j[1][2], j[0][0]);
   adj[2][2] = df_cross(j[0][0], j[1][1], j[1][0], j[0][1]);
-  det = df_fma(j[2][0], adj[2][0], df_fma(j[1][0], adj[1][0], df_mul(j[0][0], adj[0][0])));
+  det = df_dot3(j[0][0], adj[0][0], j[1][0], adj[1][0], j[2][0], adj[2][0]);
 }
 
 struct IpGeomDF {
@@ -155,7 +155,7 @@ NALU_HD void ip_geometry_df(const EdgeFormDF& f, int ip, IpGeomDF& g) {
   }
 #pragma unroll
   for (int jj = 0; jj < 3; ++jj)
-    g.G[jj] = df_fma(adj[2][jj], g.area[2], df_fma(adj[1][jj], g.area[1], df_mul(adj[0][jj], g.area[0])));
+    g.G[jj] = df_dot3(adj[0][jj], g.area[0], adj[1][jj], g.area[1], adj[2][jj], g.area[2]);
   g.det = det;
 }
 
@@ -167,7 +167,7 @@ NALU_HD void ip_shifted_G_df(const EdgeFormDF& f, int ip, const df64 area[3], df
   cofactor_df(j, adj, det);
 #pragma unroll
   for (int jj = 0; jj < 3; ++jj)
-    G[jj] = df_fma(adj[2][jj], area[2], df_fma(adj[1][jj], area[1], df_mul(adj[0][jj], area[0])));
+    G[jj] = df_dot3(adj[0][jj], area[0], adj[1][jj], area[1], adj[2][jj], area[2]);
 }
 
 // fac[c] = sum_j dN_c/ds_j(s) * (G_j * scale)
@@ -323,7 +323,7 @@ NALU_HD double continuity_elem_df(const double x[8][3], const df64 w[8][3], df64
     const df64 wx = trilinear_eval_df(wc[0], sm);
     const df64 wy = trilinear_eval_df(wc[1], sm);
     const df64 wz = trilinear_eval_df(wc[2], sm);
-    df64 m = df_mul(df_fma(wz, g.area[2], df_fma(wy, g.area[1], df_mul(wx, g.area[0]))), inv_tau);
+    df64 m = df_mul(df_dot3(wx, g.area[0], wy, g.area[1], wz, g.area[2]), inv_tau);
     if (MODE == 1) {
       df64 fs[8];
       lhs_factors_df(g.G, df_neg(df_rcp(g.det)), s_std, fs);
@@ -379,7 +379,7 @@ NALU_HD double mdot_elem_df(const double x[8][3], const df64 w[8][3], const df64
     const df64 wx = trilinear_eval_df(wc[0], sm);
     const df64 wy = trilinear_eval_df(wc[1], sm);
     const df64 wz = trilinear_eval_df(wc[2], sm);
-    const df64 m0 = df_fma(wz, g.area[2], df_fma(wy, g.area[1], df_mul(wx, g.area[0])));
+    const df64 m0 = df_dot3(wx, g.area[0], wy, g.area[1], wz, g.area[2]);
     df64 fs[8];
     if (SPOIS) {
       df64 Gs[3], dets;

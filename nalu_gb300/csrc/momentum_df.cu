@@ -213,8 +213,8 @@ __global__ void __launch_bounds__(kMomThreads) k_assemble_momentum_df(MomArgs a)
         cIp[2] = df_add(cIp[2], df_mul_f(X[3 * c + 2], rAdv));
       }
       divU = df_fma(uc2, dn[2], df_fma(uc1, dn[1], df_fma(uc0, dn[0], divU)));
-      dA[c] = df_fma(dn[2], A[2], df_fma(dn[1], A[1], df_mul(dn[0], A[0])));
-      const df64 Au = df_fma(A[2], uc2, df_fma(A[1], uc1, df_mul(A[0], uc0)));
+      dA[c] = df_dot3(dn[0], A[0], dn[1], A[1], dn[2], A[2]);
+      const df64 Au = df_dot3(A[0], uc0, A[1], uc1, A[2], uc2);
       vr[0] = df_fma(dA[c], uc0, df_fma(dn[0], Au, vr[0]));
       vr[1] = df_fma(dA[c], uc1, df_fma(dn[1], Au, vr[1]));
       vr[2] = df_fma(dA[c], uc2, df_fma(dn[2], Au, vr[2]));
