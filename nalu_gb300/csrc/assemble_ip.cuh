@@ -109,9 +109,7 @@ __device__ __forceinline__ void jacobian_rot_df(const df64* EF, int dd, int t1, 
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
     const df64* c0 = EF + 4 * (3 * dd + i);
-    df64 r = df_add(c0[0], df_scale2(c0[1], su));
-    r = df_add(r, df_scale2(c0[2], sv));
-    j[i][0] = df_add(r, df_scale2(c0[3], suv));
+    j[i][0] = df_sum4(c0[0], df_scale2(c0[1], su), df_scale2(c0[2], sv), df_scale2(c0[3], suv));
     const df64* c1 = EF + 4 * (3 * t1 + i);
     j[i][1] = df_add(c1[0], df_scale2(c1[q1], s2));
     const df64* c2 = EF + 4 * (3 * t2 + i);
@@ -130,17 +128,29 @@ __device__ __forceinline__ void g_of(const df64 c[3][3], const df64 area[3], df6
 //   fac = c_dd h1 h2 g0 + (c1 h2 g1 + h1 c2 g2) / 2,   h = 1/2 + c s.
 // The corners of one normal edge (c_dd = +-1) share the bracket X and the
 // product Y: fac(+) = X + Y, fac(-) = X - Y.  f(node, value) receives them.
+// The factors are formed as unnormalised pairs: the three products k g with
+// exact float k (TwoProd error and low part folded into one FP32 term each),
+// X by one TwoSum, X +- Y by one TwoSum each, the low terms added in FP32
+// (33 FP32 operations per corner pair instead of 51).  Their consumers (the
+// row sums and the widening to FP64, or the products of the pressure term)
+// take unnormalised pairs.
 template <class F>
 __device__ __forceinline__ void factors_rot_df(const df64 g[3], float s1, float s2, uint32_t node_tab, F&& f) {
 #pragma unroll
   for (int pr = 0; pr < 4; ++pr) {
     const float c1 = (pr & 1) ? 1.0f : -1.0f, c2 = (pr & 2) ? 1.0f : -1.0f;
     const float h1 = 0.5f + c1 * s1, h2 = 0.5f + c2 * s2;  // exact
-    const df64 X = df_add(df_mul_f(g[1], 0.5f * c1 * h2), df_mul_f(g[2], 0.5f * c2 * h1));
-    const df64 Y = df_mul_f(g[0], h1 * h2);
+    const float k1 = 0.5f * c1 * h2, k2 = 0.5f * c2 * h1, k0 = h1 * h2;  // exact
+    const float p1 = f_mul(g[1].hi, k1), p2 = f_mul(g[2].hi, k2), p0 = f_mul(g[0].hi, k0);
+    const float e1 = f_fma(g[1].lo, k1, f_fma(g[1].hi, k1, -p1));
+    const float e2 = f_fma(g[2].lo, k2, f_fma(g[2].hi, k2, -p2));
+    const float e0 = f_fma(g[0].lo, k0, f_fma(g[0].hi, k0, -p0));
+    const df64 x = two_sum(p1, p2);                  // X = x.hi + xl
+    const float xl = f_add(x.lo, f_add(e1, e2));
+    const df64 sp = two_sum(x.hi, p0), sm = two_sum(x.hi, -p0);
     const int qm = 2 * pr, qp = 2 * pr + 1;  // rotated corner: bit 0 = sign along dd
-    f((int)((node_tab >> (3 * qp)) & 7u), df_add(X, Y));
-    f((int)((node_tab >> (3 * qm)) & 7u), df_sub(X, Y));
+    f((int)((node_tab >> (3 * qp)) & 7u), df64{sp.hi, f_add(sp.lo, f_add(xl, e0))});
+    f((int)((node_tab >> (3 * qm)) & 7u), df64{sm.hi, f_add(sm.lo, f_sub(xl, e0))});
   }
 }
 
