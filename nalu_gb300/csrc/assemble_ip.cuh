@@ -111,9 +111,9 @@ __device__ __forceinline__ void jacobian_rot_df(const df64* EF, int dd, int t1, 
     const df64* c0 = EF + 4 * (3 * dd + i);
     j[i][0] = df_sum4(c0[0], df_scale2(c0[1], su), df_scale2(c0[2], sv), df_scale2(c0[3], suv));
     const df64* c1 = EF + 4 * (3 * t1 + i);
-    j[i][1] = df_add(c1[0], df_scale2(c1[q1], s2));
+    j[i][1] = df_add_lazy(c1[0], df_scale2(c1[q1], s2));
     const df64* c2 = EF + 4 * (3 * t2 + i);
-    j[i][2] = df_add(c2[0], df_scale2(c2[q2], s1));
+    j[i][2] = df_add_lazy(c2[0], df_scale2(c2[q2], s1));
   }
 }
 
@@ -156,9 +156,8 @@ __device__ __forceinline__ void factors_rot_df(const df64 g[3], float s1, float 
 
 // trilinear coefficients at an ip (monomials with s_dd vanish)
 __device__ __forceinline__ df64 trilinear_rot_df(const df64* c, int t1, int t2, float s1, float s2) {
-  df64 r = df_add(c[0], df_scale2(c[1 << t1], s1));
-  r = df_add(r, df_scale2(c[1 << t2], s2));
-  return df_add(r, df_scale2(c[(1 << t1) | (1 << t2)], s1 * s2));
+  return df_sum4(c[0], df_scale2(c[1 << t1], s1), df_scale2(c[1 << t2], s2),
+                 df_scale2(c[(1 << t1) | (1 << t2)], s1 * s2));
 }
 
 template <int EPB, int KIND, int MODE, bool SHIFT, bool SMDOT>
