@@ -231,15 +231,17 @@ __global__ void __launch_bounds__(IpSched<EPB, ip_light<KIND, MODE, SHIFT>()>::k
       const int na = node_of(sg[0], sg[1], sg[2]);
       sg[k] = 1;
       const int nb = node_of(sg[0], sg[1], sg[2]);
-      ed[q] = df_sub(s_x[el][3 * nb + i], s_x[el][3 * na + i]);
+      ed[q] = df_add_lazy(s_x[el][3 * nb + i], df_neg(s_x[el][3 * na + i]));
     }
-    const df64 p01 = df_add(ed[0], ed[1]), m01 = df_sub(ed[1], ed[0]);
-    const df64 p23 = df_add(ed[2], ed[3]), m23 = df_sub(ed[3], ed[2]);
+    // unnormalised pairs throughout: the Jacobian sums (df_sum4,
+    // df_add_lazy) and the cofactor products take them
+    const df64 p01 = df_add_lazy(ed[0], ed[1]), m01 = df_add_lazy(ed[1], df_neg(ed[0]));
+    const df64 p23 = df_add_lazy(ed[2], ed[3]), m23 = df_add_lazy(ed[3], df_neg(ed[2]));
     df64* o = &s_ef[el][4 * ki];
-    o[0] = df_scale2(df_add(p01, p23), 0.25f);
-    o[1] = df_scale2(df_add(m01, m23), 0.5f);
-    o[2] = df_scale2(df_sub(p23, p01), 0.5f);
-    o[3] = df_sub(m23, m01);
+    o[0] = df_scale2(df_add_lazy(p01, p23), 0.25f);
+    o[1] = df_scale2(df_add_lazy(m01, m23), 0.5f);
+    o[2] = df_scale2(df_add_lazy(p23, df_neg(p01)), 0.5f);
+    o[3] = df_add_lazy(m23, df_neg(m01));
   } else if (t < (9 + NCOMP) * EPB) {
     const int tt = t - 9 * EPB;
     const int el = tt / NCOMP, comp = tt - NCOMP * (tt / NCOMP);
@@ -254,8 +256,8 @@ __global__ void __launch_bounds__(IpSched<EPB, ip_light<KIND, MODE, SHIFT>()>::k
       for (int m = 0; m < 8; ++m) {
         if (m & bit) continue;
         const df64 lo = v[m], hi = v[m | bit];
-        v[m] = df_scale2(df_add(lo, hi), 0.5f);
-        v[m | bit] = df_sub(hi, lo);
+        v[m] = df_scale2(df_add_lazy(lo, hi), 0.5f);
+        v[m | bit] = df_add_lazy(hi, df_neg(lo));
       }
     }
 #pragma unroll
