@@ -305,7 +305,7 @@ __global__ void __launch_bounds__(IpSched<EPB, ip_light<KIND, MODE, SHIFT>()>::k
       df64 scale = df_neg(df_rcp(detl));
       if (KIND == 0) scale = df_mul(trilinear_rot_df(s_wc[el], t1, t2, s1, s2), scale);  // -k_ip / det
 #pragma unroll
-      for (int k = 0; k < 3; ++k) gl[k] = df_mul(gl[k], scale);
+      for (int k = 0; k < 3; ++k) gl[k] = df_mul_lazy(gl[k], scale);
       const float l1 = SH ? 2.0f * s1 : s1, l2 = SH ? 2.0f * s2 : s2;
       factors_rot_df(gl, l1, l2, ntab, [&](int node, df64 v) { FAC[node] = v; });
       if (KIND == 1) {

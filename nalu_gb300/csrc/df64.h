@@ -239,6 +239,29 @@ DF_HD df64 df_cross(df64 a, df64 b, df64 c, df64 d) {
   return quick_two_sum(s.hi, s.lo);
 }
 
+// a * b - c * d as an unnormalised pair (df_cross without its final
+// renormalisation: 16 operations), for products that take unnormalised pairs
+DF_HD df64 df_cross_lazy(df64 a, df64 b, df64 c, df64 d) {
+  const float p = f_mul(a.hi, b.hi);
+  float e = f_fma(a.hi, b.hi, -p);
+  e = f_fma(a.hi, b.lo, e);
+  e = f_fma(a.lo, b.hi, e);
+  const float q = f_mul(c.hi, d.hi);
+  float g = f_fma(c.hi, d.hi, -q);
+  g = f_fma(c.hi, d.lo, g);
+  g = f_fma(c.lo, d.hi, g);
+  const df64 s = two_sum(p, -q);
+  return {s.hi, f_add(s.lo, f_sub(e, g))};
+}
+// a * b as an unnormalised pair (df_mul without its final renormalisation)
+DF_HD df64 df_mul_lazy(df64 a, df64 b) {
+  const float p = f_mul(a.hi, b.hi);
+  float e = f_fma(a.hi, b.hi, -p);
+  e = f_fma(a.hi, b.lo, e);
+  e = f_fma(a.lo, b.hi, e);
+  return {p, e};
+}
+
 // 1 / a: FP32 reciprocal refined by one Newton step in df64
 DF_HD df64 df_rcp(df64 a) {
   const float x0 = 1.0f / a.hi;

@@ -120,16 +120,18 @@ NALU_HD void jacobian_df(const EdgeFormDF& f, const float s[3], df64 j[3][3]) {
   }
 }
 
+// cofactors as unnormalised pairs (every consumer is a product or a dot
+// product, which take them); det renormalised
 NALU_HD void cofactor_df(const df64 j[3][3], df64 adj[3][3], df64& det) {
-  adj[0][0] = df_cross(j[1][1], j[2][2], j[2][1], j[1][2]);
-  adj[0][1] = df_cross(j[1][2], j[2][0], j[2][2], j[1][0]);
-  adj[0][2] = df_cross(j[1][0], j[2][1], j[2][0], j[1][1]);
-  adj[1][0] = df_cross(j[0][2], j[2][1], j[2][2], j[0][1]);
-  adj[1][1] = df_cross(j[0][0], j[2][2], j[2][0], j[0][2]);
-  adj[1][2] = df_cross(j[0][1], j[2][0], j[2][1], j[0][0]);
-  adj[2][0] = df_cross(j[0][1], j[1][2], j[1][1], j[0][2]);
-  adj[2][1] = df_cross(j[0][2], j[1][0], j[1][2], j[0][0]);
-  adj[2][2] = df_cross(j[0][0], j[1][1], j[1][0], j[0][1]);
+  adj[0][0] = df_cross_lazy(j[1][1], j[2][2], j[2][1], j[1][2]);
+  adj[0][1] = df_cross_lazy(j[1][2], j[2][0], j[2][2], j[1][0]);
+  adj[0][2] = df_cross_lazy(j[1][0], j[2][1], j[2][0], j[1][1]);
+  adj[1][0] = df_cross_lazy(j[0][2], j[2][1], j[2][2], j[0][1]);
+  adj[1][1] = df_cross_lazy(j[0][0], j[2][2], j[2][0], j[0][2]);
+  adj[1][2] = df_cross_lazy(j[0][1], j[2][0], j[2][1], j[0][0]);
+  adj[2][0] = df_cross_lazy(j[0][1], j[1][2], j[1][1], j[0][2]);
+  adj[2][1] = df_cross_lazy(j[0][2], j[1][0], j[1][2], j[0][0]);
+  adj[2][2] = df_cross_lazy(j[0][0], j[1][1], j[1][0], j[0][1]);
   det = df_dot3(j[0][0], adj[0][0], j[1][0], adj[1][0], j[2][0], adj[2][0]);
 }
 
