@@ -253,6 +253,17 @@ DF_HD df64 df_cross_lazy(df64 a, df64 b, df64 c, df64 d) {
   const df64 s = two_sum(p, -q);
   return {s.hi, f_add(s.lo, f_sub(e, g))};
 }
+// a * b + c as an unnormalised pair (df_fma without its final
+// renormalisation: 12 operations), for accumulations whose result is only
+// added to or widened to FP64
+DF_HD df64 df_fma_lazy(df64 a, df64 b, df64 c) {
+  const float p = f_mul(a.hi, b.hi);
+  float e = f_fma(a.hi, b.hi, -p);
+  e = f_fma(a.hi, b.lo, e);
+  e = f_fma(a.lo, b.hi, e);
+  const df64 s = two_sum(p, c.hi);
+  return {s.hi, f_add(s.lo, f_add(e, c.lo))};
+}
 // a * b as an unnormalised pair (df_mul without its final renormalisation)
 DF_HD df64 df_mul_lazy(df64 a, df64 b) {
   const float p = f_mul(a.hi, b.hi);

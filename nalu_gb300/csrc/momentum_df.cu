@@ -306,7 +306,9 @@ __global__ void __launch_bounds__(kMomThreads) k_assemble_momentum_df(MomArgs a)
   }
   __syncthreads();
 
-  // ---- phase 2: rows; each thread owns rows sub and sub+12 of its element ----
+  // ---- phase 2: rows; each thread owns rows sub and sub+12 of its element.
+  // The entries accumulate as unnormalised pairs (lazy products and sums);
+  // the widening to FP64 renormalises them ----
   if (!valid) return;
   for (int h = 0; h < 2; ++h) {
     const int row = sub + 12 * h;  // = 3 r + i
@@ -328,13 +330,13 @@ __global__ void __launch_bounds__(kMomThreads) k_assemble_momentum_df(MomArgs a)
 #pragma unroll
       for (int c = 0; c < 8; ++c) {
         const df64 di = DN[3 * c + i];
-        v[c][0] = df_fma(di, aa0, v[c][0]);
-        v[c][1] = df_fma(di, aa1, v[c][1]);
-        v[c][2] = df_fma(di, aa2, v[c][2]);
+        v[c][0] = df_fma_lazy(di, aa0, v[c][0]);
+        v[c][1] = df_fma_lazy(di, aa1, v[c][1]);
+        v[c][2] = df_fma_lazy(di, aa2, v[c][2]);
         const df64 dg = left ? DG[c] : df_neg(DG[c]);
-        if (i == 0) v[c][0] = df_add(v[c][0], dg);
-        else if (i == 1) v[c][1] = df_add(v[c][1], dg);
-        else v[c][2] = df_add(v[c][2], dg);
+        if (i == 0) v[c][0] = df_add_lazy(v[c][0], dg);
+        else if (i == 1) v[c][1] = df_add_lazy(v[c][1], dg);
+        else v[c][2] = df_add_lazy(v[c][2], dg);
       }
       if (UPW) {
         const df64 aL = S[MomLayout::ALHS + 2 * ip], aR = S[MomLayout::ALHS + 2 * ip + 1];
@@ -342,19 +344,19 @@ __global__ void __launch_bounds__(kMomThreads) k_assemble_momentum_df(MomArgs a)
 #pragma unroll
         for (int c = 0; c < 8; ++c) {
           if (c == il) {
-            if (i == 0) v[c][0] = df_add(v[c][0], sL);
-            else if (i == 1) v[c][1] = df_add(v[c][1], sL);
-            else v[c][2] = df_add(v[c][2], sL);
+            if (i == 0) v[c][0] = df_add_lazy(v[c][0], sL);
+            else if (i == 1) v[c][1] = df_add_lazy(v[c][1], sL);
+            else v[c][2] = df_add_lazy(v[c][2], sL);
           }
           if (c == ir) {
-            if (i == 0) v[c][0] = df_add(v[c][0], sR);
-            else if (i == 1) v[c][1] = df_add(v[c][1], sR);
-            else v[c][2] = df_add(v[c][2], sR);
+            if (i == 0) v[c][0] = df_add_lazy(v[c][0], sR);
+            else if (i == 1) v[c][1] = df_add_lazy(v[c][1], sR);
+            else v[c][2] = df_add_lazy(v[c][2], sR);
           }
         }
       }
       const df64 ri = S[MomLayout::RIP + 3 * ip + i];
-      rs = df_sub(rs, left ? ri : df_neg(ri));
+      rs = df_add_lazy(rs, left ? df_neg(ri) : ri);
     }
     if (OUT == 2) {
 #pragma unroll
