@@ -20,18 +20,20 @@ NALU_DF_VARIANTS(NALU_DF_EXTERN)
 NALU_IP_VARIANTS(NALU_IP_EXTERN, 8)
 NALU_IP_VARIANTS(NALU_IP_EXTERN, 16)
 
+// (the splits and the double-float arithmetic use the FP32 and integer pipes:
+// GB300's FP64 rate made the FP64 form of this pass FP64-bound, 74 us at 128^3)
 __global__ void k_prepass_k_df(const double* __restrict__ k, df64* __restrict__ out, int64_t n) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) out[i] = df_from_double(__ldg(k + i));
+  if (i < n) out[i] = df_split_bits(__ldg(k + i));
 }
 
 __global__ void k_prepass_w_df(const double* __restrict__ u, const double* __restrict__ gp,
-                               const double* __restrict__ rho, double tau, df64* __restrict__ out, int64_t n) {
+                               const double* __restrict__ rho, df64 tau, df64* __restrict__ out, int64_t n) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const double r = __ldg(rho + i);
+  const df64 r = df_split_bits(__ldg(rho + i));
 #pragma unroll
-  for (int d = 0; d < 3; ++d) out[3 * i + d] = df_from_double(r * __ldg(u + 3 * i + d) + tau * __ldg(gp + 3 * i + d));
+  for (int d = 0; d < 3; ++d) out[3 * i + d] = df_nodal_w(r, __ldg(u + 3 * i + d), tau, __ldg(gp + 3 * i + d));
 }
 
 // ComputeMdot in df64: one thread per element, the twelve SCS mass flow rates
@@ -71,7 +73,8 @@ int launch_mdot_df(nalu_ctx* ctx, const nalu_assemble_opts& o) {
   df64* w = reinterpret_cast<df64*>(ctx->d_node_df.p);
   k_prepass_w_df<<<nblk_df(n, 256), 256, 0, ctx->stream>>>(ctx->fields[NALU_FIELD_VELOCITY_RTM].d.p,
                                                         ctx->fields[NALU_FIELD_DPDX].d.p,
-                                                        ctx->fields[NALU_FIELD_DENSITY].d.p, o.proj_time_scale, w, n);
+                                                        ctx->fields[NALU_FIELD_DENSITY].d.p,
+                                                        df_split_bits(o.proj_time_scale), w, n);
   const unsigned grid = nblk_df(E, kAsmBlockDF);
   const double* x = ctx->fields[NALU_FIELD_COORDINATES].d.p;
   const double* p = ctx->fields[NALU_FIELD_PRESSURE].d.p;
@@ -149,8 +152,8 @@ int prepass(nalu_ctx* ctx, int kernel, const nalu_assemble_opts& o, AsmArgsDF& a
   } else {
     k_prepass_w_df<<<nblk_df(n, 256), 256, 0, ctx->stream>>>(ctx->fields[NALU_FIELD_VELOCITY].d.p,
                                                           ctx->fields[NALU_FIELD_DPDX].d.p,
-                                                          ctx->fields[NALU_FIELD_DENSITY].d.p, o.proj_time_scale,
-                                                          out, n);
+                                                          ctx->fields[NALU_FIELD_DENSITY].d.p,
+                                                          df_split_bits(o.proj_time_scale), out, n);
   }
   ctx->launches++;
   a.nodal = out;

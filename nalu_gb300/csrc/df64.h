@@ -193,6 +193,17 @@ DF_HD df64 df_fma(df64 a, df64 b, df64 c) {
   return quick_two_sum(s.hi, s.lo);
 }
 
+// The nodal input of the df64 continuity kernels, rho u + tau gp, as a
+// normalised pair with no FP64 instruction: the inputs split by integer
+// operations (df_split_bits, ~2^-48 relative), then two double-float products
+// and a sum.  Inputs must lie in [2^-100, 2^127) in magnitude or be zero (the
+// split drops smaller magnitudes).  An FP64 product, sum and conversion take
+// 6 FP64-pipe instructions per component, which made the per-node pass
+// FP64-bound on GB300.
+DF_HD df64 df_nodal_w(df64 rho, double u, df64 tau, double gp) {
+  return df_add(df_mul(rho, df_split_bits(u)), df_mul(tau, df_split_bits(gp)));
+}
+
 // a + b + c + d: three TwoSums of the leading parts, the low parts and the
 // TwoSum errors added in FP32, one renormalisation (27 operations instead of
 // three df_add, 33)
