@@ -2,8 +2,11 @@
 // mirroring the reference classes a Nalu caller uses on this path:
 //
 //   LinearSystem                 include/LinearSystem.h:39-167 (TpetraLinearSystem)
-//   Kernel + the four kernels    include/kernel/Kernel.h:95-125, src/kernel/*.C
+//   Kernel + the element kernels include/kernel/Kernel.h:95-125, src/kernel/*.C
 //   AssembleElemSolverAlgorithm  include/AssembleElemSolverAlgorithm.h:38-112
+//   HexSCS, HexSCV               include/master_element/Hex8CVFEM.h:67-234
+//   ComputeMdotElemAlgorithm, AssembleNodalGrad{Elem,Boundary}Algorithm,
+//   AssembleFaceElemSolverAlgorithm and the continuity face kernels
 //
 // Header only; every call forwards to the C ABI and turns a non-zero status
 // into nalu_gb300::Error.  Method names and argument meaning follow the
@@ -63,10 +66,93 @@ class Context {
     return n;
   }
   int64_t n_nodes() const { return n_nodes_; }
+  // a field back to the host (count values, in the caller's node order)
+  void fieldGet(nalu_field f, double* v, int64_t count) const {
+    check(nalu_field_get(ctx_, f, v, count, 0), "nalu_field_get");
+  }
+  // dual_nodal_volume from the coordinates (ComputeGeometryInteriorAlgorithm,
+  // src/ComputeGeometryInteriorAlgorithm.C): NALU_FIELD_DUAL_VOLUME
+  void computeDualNodalVolume() { check(nalu_compute_dual_volume(ctx_), "nalu_compute_dual_volume"); }
 
  private:
   nalu_ctx* ctx_ = nullptr;
   int64_t n_nodes_ = 0;
+};
+
+// Hex8 master elements (src/master_element/Hex8CVFEM.C), batched: the
+// MasterElement calls for nelem elements at once on the device.  coords
+// [nelem][8][3] in the element's node order (host arrays); outputs in the
+// reference's layouts.  The grad ops return false where some element has
+// det(J) <= 0 at one of its points (outputs still written), as the reference's
+// legacy grad_op reports through its error argument; other failures throw.
+class HexSCS {
+ public:
+  explicit HexSCS(Context& ctx) : ctx_(ctx) {}
+  // HexSCS::determinant (:547-580): areav [nelem][12][3]
+  void determinant(int64_t nelem, const double* coords, double* areav) const {
+    ctx_.check(nalu_hex_scs_determinant(ctx_.get(), nelem, coords, areav, 0), "HexSCS::determinant");
+  }
+  // HexSCS::grad_op (:523-529): gradop, deriv [nelem][12][8][3]; deriv may be null
+  bool grad_op(int64_t nelem, const double* coords, double* gradop, double* deriv = nullptr) const {
+    return jac_ok(nalu_hex_scs_grad_op(ctx_.get(), nelem, coords, 0, gradop, deriv, 0), "HexSCS::grad_op");
+  }
+  // HexSCS::shifted_grad_op (:535-541)
+  bool shifted_grad_op(int64_t nelem, const double* coords, double* gradop, double* deriv = nullptr) const {
+    return jac_ok(nalu_hex_scs_grad_op(ctx_.get(), nelem, coords, 1, gradop, deriv, 0), "HexSCS::shifted_grad_op");
+  }
+  // HexSCS::face_grad_op / shifted_face_grad_op (:668-684) at the exposed-face
+  // ips of side side[e] of each element: gradop [nelem][4][8][3]
+  bool face_grad_op(int64_t nelem, const int32_t* side, const double* coords, double* gradop,
+                    bool shifted = false) const {
+    return jac_ok(nalu_hex_face_grad_op(ctx_.get(), nelem, side, coords, shifted ? 1 : 0, gradop, 0),
+                  "HexSCS::face_grad_op");
+  }
+  // HexSCS::adjacentNodes (lrscv_): left/right node of each of the 12 ips
+  static std::vector<int32_t> adjacentNodes() {
+    std::vector<int32_t> v(24);
+    nalu_hex_scs_adjacent_nodes(v.data());
+    return v;
+  }
+  // HexSCS::shape_fcn / shifted_shape_fcn: [12][8]
+  static std::vector<double> shape_fcn(bool shifted = false) {
+    std::vector<double> v(96);
+    nalu_hex_scs_shape_fcn(shifted ? 1 : 0, v.data());
+    return v;
+  }
+  // HexSCS::side_node_ordinals: the 4 nodes of side `side`
+  static std::vector<int32_t> sideNodeOrdinals(int side) {
+    std::vector<int32_t> v(4);
+    nalu_hex_side_node_ordinals(side, v.data());
+    return v;
+  }
+
+ private:
+  bool jac_ok(int rc, const char* what) const {
+    if (rc == NALU_ERR_NEG_JACOBIAN) return false;
+    ctx_.check(rc, what);
+    return true;
+  }
+  Context& ctx_;
+};
+
+class HexSCV {
+ public:
+  explicit HexSCV(Context& ctx) : ctx_(ctx) {}
+  // HexSCV::determinant (:149-180): vol [nelem][8]
+  void determinant(int64_t nelem, const double* coords, double* vol) const {
+    ctx_.check(nalu_hex_scv_determinant(ctx_.get(), nelem, coords, vol, 0), "HexSCV::determinant");
+  }
+  // HexSCV::grad_op / shifted_grad_op (:185-232): gradop, deriv [nelem][8][8][3]
+  bool grad_op(int64_t nelem, const double* coords, double* gradop, double* deriv = nullptr,
+               bool shifted = false) const {
+    const int rc = nalu_hex_scv_grad_op(ctx_.get(), nelem, coords, shifted ? 1 : 0, gradop, deriv, 0);
+    if (rc == NALU_ERR_NEG_JACOBIAN) return false;
+    ctx_.check(rc, "HexSCV::grad_op");
+    return true;
+  }
+
+ private:
+  Context& ctx_;
 };
 
 // The TimeIntegrator values the kernels' setup() reads (BDF coefficients
@@ -199,6 +285,18 @@ class LinearSystem {
     ctx_.check(nalu_solution_get(ctx_.get(), x.data(), 0), "solution");
     return x;
   }
+  // the assembled values [nnz] and rhs [rows] (either may be null) and the
+  // CRS graph (rowptr [rows + 1], colind [nnz]), in Tpetra row order
+  void values(double* vals, double* rhs) const { ctx_.check(nalu_linsys_copy(ctx_.get(), vals, rhs, 0), "copy"); }
+  void graph(int64_t* rowptr, int32_t* colind) const {
+    ctx_.check(nalu_linsys_graph(ctx_.get(), rowptr, colind), "graph");
+  }
+  void sizes(int64_t* rows, int64_t* nnz) const { ctx_.check(nalu_linsys_sizes(ctx_.get(), rows, nnz, nullptr), "sizes"); }
+  // writeToFile / writeSolutionToFile (src/TpetraLinearSystem.C:1967-2117): MatrixMarket dumps
+  void writeToFile(const char* base) { ctx_.check(nalu_linsys_write_system(ctx_.get(), base), "writeToFile"); }
+  void writeSolutionToFile(const char* base) {
+    ctx_.check(nalu_linsys_write_solution(ctx_.get(), base), "writeSolutionToFile");
+  }
   int numDof() const { return numDof_; }
   int linearSolveIterations() const { return linearSolveIterations_; }
   double linearResidual() const { return linearResidual_; }
@@ -277,6 +375,54 @@ class AssembleFaceElemSolverAlgorithm {
  private:
   LinearSystem& linsys_;
   int set_;
+};
+
+// ComputeMdotElemAlgorithm (src/ComputeMdotElemAlgorithm.C:85-250): the SCS
+// mass flow rates (NALU_FIELD_MDOT_SCS) from density, velocity_rtm, pressure
+// and dpdx; tau = dt / gamma1.  arith: NALU_ARITH_FP64 or NALU_ARITH_DF64.
+class ComputeMdotElemAlgorithm {
+ public:
+  ComputeMdotElemAlgorithm(Context& ctx, bool shiftMdot = false, bool shiftPoisson = false, int arith = NALU_ARITH_FP64)
+      : ctx_(ctx) {
+    nalu_assemble_opts_default(&opts);
+    opts.shift_mdot = shiftMdot;
+    opts.shift_poisson = shiftPoisson;
+    opts.arith = arith;
+  }
+  void execute(const TimeIntegrator& ti = TimeIntegrator()) {
+    opts.proj_time_scale = ti.dt / ti.gamma1;
+    ctx_.check(nalu_compute_mdot(ctx_.get(), &opts), "ComputeMdotElemAlgorithm::execute");
+  }
+  nalu_assemble_opts opts;
+
+ private:
+  Context& ctx_;
+};
+
+// AssembleNodalGradElemAlgorithm / AssembleNodalGradUElemAlgorithm
+// (src/AssembleNodalGradElemAlgorithm.C): the element part of the projected
+// nodal gradient of src into dst (zeroed first; needs the dual nodal volume),
+// then, per boundary side set, AssembleNodalGradBoundaryAlgorithm
+// (src/AssembleNodalGradBoundaryAlgorithm.C:75-153) adds the face closure.
+class AssembleNodalGradElemAlgorithm {
+ public:
+  AssembleNodalGradElemAlgorithm(Context& ctx, nalu_field src, nalu_field dst, bool shifted = false,
+                                 int arith = NALU_ARITH_FP64)
+      : ctx_(ctx), src_(src), dst_(dst), shifted_(shifted), arith_(arith) {}
+  void execute() {
+    ctx_.check(nalu_compute_nodal_gradient(ctx_.get(), src_, dst_, shifted_ ? 1 : 0, arith_),
+               "AssembleNodalGradElemAlgorithm::execute");
+    for (int set : boundarySets_)
+      ctx_.check(nalu_nodal_gradient_boundary(ctx_.get(), set, src_, dst_, shifted_ ? 1 : 0),
+                 "AssembleNodalGradBoundaryAlgorithm::execute");
+  }
+  std::vector<int> boundarySets_;
+
+ private:
+  Context& ctx_;
+  nalu_field src_, dst_;
+  bool shifted_;
+  int arith_;
 };
 
 }  // namespace nalu_gb300

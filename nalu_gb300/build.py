@@ -64,10 +64,10 @@ def build(verbose=False, ptxas_info=False):
     # -ffp-contract=off: the double-float sequences must not be fused
     _run([cxx, "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-shared", "-o", check,
           os.path.join(CSRC, "elem_hostcheck.cpp")])
-    # C++ caller of the host interface (include/nalu_gb300.hpp)
-    _run([cxx, "-std=c++17", "-O2", "-o", os.path.join(OUT, "heat_conduction"),
-          os.path.join(HERE, "examples", "heat_conduction.cpp"), "-L" + OUT, "-lnalu_gb300",
-          "-Wl,-rpath," + OUT])
+    # C++ callers of the host interface (include/nalu_gb300.hpp)
+    for ex in ("heat_conduction", "continuity_step"):
+        _run([cxx, "-std=c++17", "-O2", "-o", os.path.join(OUT, ex), os.path.join(HERE, "examples", ex + ".cpp"),
+              "-L" + OUT, "-lnalu_gb300", "-Wl,-rpath," + OUT])
     for o in objs:
         os.remove(o)
     return lib

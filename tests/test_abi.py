@@ -108,3 +108,14 @@ def test_struct_layouts_match_header(tmp_path):
         assert int(got[cname]) == ctypes.sizeof(py), cname
         for field in py._fields_:
             assert int(got["%s.%s" % (cname, field[0])]) == getattr(py, field[0]).offset, (cname, field[0])
+
+
+@pytest.mark.parametrize("example", ["heat_conduction", "continuity_step"])
+def test_cpp_host_interface_compiles(example):
+    """The C++ mirror (include/nalu_gb300.hpp) and the C++ callers that drive
+    it compile cleanly against the header alone (no CUDA needed)."""
+    import shutil
+    if shutil.which("g++") is None:
+        pytest.skip("no C++ compiler")
+    src = os.path.join(ROOT, "nalu_gb300", "examples", example + ".cpp")
+    subprocess.run(["g++", "-std=c++17", "-Wall", "-Wextra", "-Werror", "-fsyntax-only", src], check=True)

@@ -182,6 +182,30 @@ def test_cpp_host_interface_heat_conduction():
     assert d["status"] == 0 and d["true_rel_res"] <= 1e-8
 
 
+def test_cpp_host_interface_continuity_step():
+    """The C++ caller nalu_gb300/examples/continuity_step.cpp drives HexSCS /
+    HexSCV, the dual nodal volume, the projected nodal gradient with its skin
+    closure, ComputeMdotElemAlgorithm and the pinned continuity solve through
+    the C++ mirror, on a 20^3 mesh of axis-aligned boxes (z ratio 1.05):
+    volumes sum to the unit cube, dN/dx sums to zero at every ip, the gradient
+    of a linear pressure is exact, mdot equals rho u_ip . A_ip (the pressure
+    terms cancel), and the solve reaches 1e-8."""
+    import json
+    import os
+    import subprocess
+    exe = os.path.join(os.path.dirname(ng.LIB_PATH), "continuity_step")
+    assert os.path.exists(exe), "build() did not produce the C++ example"
+    out = subprocess.run([exe, "20"], capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr
+    d = json.loads(out.stdout.strip().splitlines()[-1])
+    assert d["scv_volume_sum_err"] <= 1e-12 and d["dual_volume_sum_err"] <= 1e-12, d
+    assert d["grad_op_row_sum"] <= 1e-9 and d["jacobians_positive"], d
+    assert d["lrscv_0"] == [0, 1] and d["skin_faces"] == 6 * 20 * 20, d
+    assert d["linear_gradient_err"] <= 1e-10 and d["mdot_rel_err"] <= 1e-10, d
+    assert d["rows"] == 21 ** 3 and d["nnz"] == 61 ** 3, d
+    assert d["status"] == 0 and d["true_rel_res"] <= 1e-8, d
+
+
 def test_cg_wide_slices_permuted_ids(gpu_ctx_factory, oracle):
     """Random global ids scatter the columns of each SELL slice over the whole
     matrix, so most slices keep 32-bit column indices (the 16-bit offsets
