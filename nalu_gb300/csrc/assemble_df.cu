@@ -22,18 +22,32 @@ NALU_IP_VARIANTS(NALU_IP_EXTERN, 16)
 
 // (the splits and the double-float arithmetic use the FP32 and integer pipes:
 // GB300's FP64 rate made the FP64 form of this pass FP64-bound, 74 us at 128^3)
-__global__ void k_prepass_k_df(const double* __restrict__ k, df64* __restrict__ out, int64_t n) {
+// An input outside the pairs' range (inf, NaN, |x| >= 2^127) raises
+// FLAG_NONFINITE: the element kernels' widening back to FP64 would turn it
+// into a large finite value.
+__global__ void k_prepass_k_df(const double* __restrict__ k, df64* __restrict__ out, int64_t n, int32_t* flags) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) out[i] = df_split_bits(__ldg(k + i));
+  if (i >= n) return;
+  const double kv = __ldg(k + i);
+  out[i] = df_split_input(kv);
+  if (!df_split_in_range(kv)) atomicAdd(flags + FLAG_NONFINITE, 1);
 }
 
 __global__ void k_prepass_w_df(const double* __restrict__ u, const double* __restrict__ gp,
-                               const double* __restrict__ rho, df64 tau, df64* __restrict__ out, int64_t n) {
+                               const double* __restrict__ rho, df64 tau, df64* __restrict__ out, int64_t n,
+                               int32_t* flags) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const df64 r = df_split_bits(__ldg(rho + i));
+  const double rv = __ldg(rho + i);
+  const df64 r = df_split_input(rv);
+  bool ok = df_split_in_range(rv);
 #pragma unroll
-  for (int d = 0; d < 3; ++d) out[3 * i + d] = df_nodal_w(r, __ldg(u + 3 * i + d), tau, __ldg(gp + 3 * i + d));
+  for (int d = 0; d < 3; ++d) {
+    const double uv = __ldg(u + 3 * i + d), gv = __ldg(gp + 3 * i + d);
+    ok = ok && df_split_in_range(uv) && df_split_in_range(gv);
+    out[3 * i + d] = df_nodal_w(r, uv, tau, gv);
+  }
+  if (!ok) atomicAdd(flags + FLAG_NONFINITE, 1);
 }
 
 // ComputeMdot in df64: one thread per element, the twelve SCS mass flow rates
@@ -74,7 +88,7 @@ int launch_mdot_df(nalu_ctx* ctx, const nalu_assemble_opts& o) {
   k_prepass_w_df<<<nblk_df(n, 256), 256, 0, ctx->stream>>>(ctx->fields[NALU_FIELD_VELOCITY_RTM].d.p,
                                                         ctx->fields[NALU_FIELD_DPDX].d.p,
                                                         ctx->fields[NALU_FIELD_DENSITY].d.p,
-                                                        df_split_bits(o.proj_time_scale), w, n);
+                                                        df_split_input(o.proj_time_scale), w, n, ctx->d_flags.p);
   const unsigned grid = nblk_df(E, kAsmBlockDF);
   const double* x = ctx->fields[NALU_FIELD_COORDINATES].d.p;
   const double* p = ctx->fields[NALU_FIELD_PRESSURE].d.p;
@@ -148,12 +162,13 @@ int prepass(nalu_ctx* ctx, int kernel, const nalu_assemble_opts& o, AsmArgsDF& a
   if (ctx->d_node_df.n < need) NALU_CUDA(ctx, ctx->d_node_df.alloc(need));
   df64* out = reinterpret_cast<df64*>(ctx->d_node_df.p);
   if (kernel == NALU_KERNEL_SCALAR_DIFF) {
-    k_prepass_k_df<<<nblk_df(n, 256), 256, 0, ctx->stream>>>(ctx->fields[NALU_FIELD_DIFF_COEFF].d.p, out, n);
+    k_prepass_k_df<<<nblk_df(n, 256), 256, 0, ctx->stream>>>(ctx->fields[NALU_FIELD_DIFF_COEFF].d.p, out, n,
+                                                          ctx->d_flags.p);
   } else {
     k_prepass_w_df<<<nblk_df(n, 256), 256, 0, ctx->stream>>>(ctx->fields[NALU_FIELD_VELOCITY].d.p,
                                                           ctx->fields[NALU_FIELD_DPDX].d.p,
                                                           ctx->fields[NALU_FIELD_DENSITY].d.p,
-                                                          df_split_bits(o.proj_time_scale), out, n);
+                                                          df_split_input(o.proj_time_scale), out, n, ctx->d_flags.p);
   }
   ctx->launches++;
   a.nodal = out;

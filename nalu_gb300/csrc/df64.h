@@ -193,15 +193,26 @@ DF_HD df64 df_fma(df64 a, df64 b, df64 c) {
   return quick_two_sum(s.hi, s.lo);
 }
 
+// df_split_bits for an input field value.  Magnitudes of 2^127 and above,
+// infinities and NaN (df_split_in_range false) take the float conversion
+// instead (the nearest float, inf past FLT_MAX, or NaN) rather than a wrapped
+// exponent; the per-node passes that call it flag such inputs, since the
+// widening back to FP64 (f2d_bits) does not carry inf or NaN.  Magnitudes
+// below 2^-100 become zero, as in df_split_bits.
+DF_HD bool df_split_in_range(double d) { return (int)((d2u(d) >> 52) & 0x7ff) < 1023 + 127; }
+DF_HD df64 df_split_input(double d) {
+  if (!df_split_in_range(d)) return {(float)d, 0.0f};
+  return df_split_bits(d);
+}
+
 // The nodal input of the df64 continuity kernels, rho u + tau gp, as a
 // normalised pair with no FP64 instruction: the inputs split by integer
-// operations (df_split_bits, ~2^-48 relative), then two double-float products
-// and a sum.  Inputs must lie in [2^-100, 2^127) in magnitude or be zero (the
-// split drops smaller magnitudes).  An FP64 product, sum and conversion take
-// 6 FP64-pipe instructions per component, which made the per-node pass
-// FP64-bound on GB300.
+// operations (df_split_input, ~2^-48 relative), then two double-float
+// products and a sum.  An FP64 product, sum and conversion take 6 FP64-pipe
+// instructions per component, which made the per-node pass FP64-bound on
+// GB300.
 DF_HD df64 df_nodal_w(df64 rho, double u, df64 tau, double gp) {
-  return df_add(df_mul(rho, df_split_bits(u)), df_mul(tau, df_split_bits(gp)));
+  return df_add(df_mul(rho, df_split_input(u)), df_mul(tau, df_split_input(gp)));
 }
 
 // a + b + c + d: three TwoSums of the leading parts, the low parts and the

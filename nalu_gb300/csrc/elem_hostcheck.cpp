@@ -91,7 +91,7 @@ void hc_scalar_diff_df(const double* xin, const double* q, const double* k, int 
                        double* rhs) {
   df64 kd[8], m[64];
   int kexp = 0;
-  for (int n = 0; n < 8; ++n) kd[n] = df_split_bits(k[n]);
+  for (int n = 0; n < 8; ++n) kd[n] = df_split_input(k[n]);
   with_x(xin, [&](double (&x)[8][3]) {
     df64 rr_acc[8];
     ArrayAccDF acc{m, rr_acc};
@@ -110,7 +110,7 @@ void hc_mdot_df(const double* xin, const double* rho, const double* u, const dou
                 double tau, int smdot, int spois, double* mdot) {
   df64 w[8][3], pd[8];
   for (int n = 0; n < 8; ++n)
-    for (int d = 0; d < 3; ++d) w[n][d] = df_nodal_w(df_split_bits(rho[n]), u[n * 3 + d], df_split_bits(tau), gp[n * 3 + d]);
+    for (int d = 0; d < 3; ++d) w[n][d] = df_nodal_w(df_split_input(rho[n]), u[n * 3 + d], df_split_input(tau), gp[n * 3 + d]);
   for (int n = 0; n < 8; ++n) pd[n] = df_split_bits(p[n]);
   const df64 t = df_from_double(tau);
   with_x(xin, [&](double (&x)[8][3]) {
@@ -129,7 +129,7 @@ void hc_continuity_df(const double* xin, const double* u, const double* rho, con
                       double* rhs) {
   df64 w[8][3], m[64], r8[8], pd[8];
   for (int n = 0; n < 8; ++n)
-    for (int d = 0; d < 3; ++d) w[n][d] = df_nodal_w(df_split_bits(rho[n]), u[n * 3 + d], df_split_bits(tau), gp[n * 3 + d]);
+    for (int d = 0; d < 3; ++d) w[n][d] = df_nodal_w(df_split_input(rho[n]), u[n * 3 + d], df_split_input(tau), gp[n * 3 + d]);
   for (int n = 0; n < 8; ++n) pd[n] = df_split_bits(p[n]);
   const int mode = spois ? 2 : (reduced ? 1 : 0);
   const df64 it = df_from_double(1.0 / tau);

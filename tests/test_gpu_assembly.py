@@ -293,6 +293,43 @@ def test_negative_jacobian_reported(gpu_ctx_factory):
     ctx.close()
 
 
+@pytest.mark.parametrize("bad", [float("nan"), float("inf"), 1e300])
+def test_df64_out_of_range_input_reported(gpu_ctx_factory, bad):
+    """A nodal input the double-float pairs cannot hold (NaN, inf, |x| >=
+    2^127) in the velocity of a continuity assembly or the diffusion
+    coefficient of a heat assembly is reported as NALU_ERR_NONFINITE at the
+    next host synchronisation point, and the context stays usable."""
+    c, conn, gid = block_mesh(4, 3, 3)
+    n = c.shape[0]
+    u, rho, p, gp = continuity_fields(c, seed=3)
+    u[7, 1] = bad
+    ctx = _ctx(gpu_ctx_factory, c, conn, gid)
+    for nm, v in (("velocity", u), ("density", rho), ("pressure", p), ("dpdx", gp)):
+        ctx.field_set(nm, v)
+    ctx.build_elem_graph(1)
+    opts = ng.default_assemble_opts(scatter=ng.SCATTER_ATOMIC, arith=ng.ARITH_DF64, schedule=ng.SCHEDULE_IP16)
+    with pytest.raises(ng.NaluError) as ei:
+        ctx.zero()
+        ctx.assemble(ng.KERNEL_CONTINUITY_ADV, opts)
+        ctx.load_complete()
+    assert ei.value.status == -5
+    u[7, 1] = 0.5
+    ctx.field_set("velocity", u)
+    ctx.zero()
+    ctx.assemble(ng.KERNEL_CONTINUITY_ADV, opts)
+    ctx.load_complete()
+    k = np.ones(n)
+    k[5] = bad
+    ctx.field_set("scalar_q", np.zeros(n))
+    ctx.field_set("diff_coeff", k)
+    with pytest.raises(ng.NaluError) as ei:
+        ctx.zero()
+        ctx.assemble(ng.KERNEL_SCALAR_DIFF, ng.default_assemble_opts(scatter=ng.SCATTER_ATOMIC, arith=ng.ARITH_DF64))
+        ctx.load_complete()
+    assert ei.value.status == -5
+    ctx.close()
+
+
 # ---------------------------------------------------------------------------
 # double-float element math (ARITH_DF64) against the FP64 oracle
 # ---------------------------------------------------------------------------
