@@ -178,4 +178,3 @@ def test_df64_scale_invariance(elemcheck, oracle, scale):
             elemcheck.hc_mdot_df(P(cc), P(rho), P(np.ascontiguousarray(u)), P(p), P(np.ascontiguousarray(gp)),
                                  float(tau), sm, sp, P(m2))
             check_dense(m2[None], m1[None], what="mdot df64 x%g" % scale)
-
