@@ -208,7 +208,8 @@ DF_HD df64 df_split_input(double d) {
 // The nodal input of the df64 continuity kernels, rho u + tau gp, as a
 // normalised pair with no FP64 instruction: the inputs split by integer
 // operations (df_split_input, ~2^-48 relative), then two double-float
-// products and a sum.  An FP64 product, sum and conversion take 6 FP64-pipe
+// products and a sum (at most ~2^-45.9 of |rho u| + |tau gp| against FP64 on
+// random inputs).  An FP64 product, sum and conversion take 6 FP64-pipe
 // instructions per component, which made the per-node pass FP64-bound on
 // GB300.
 DF_HD df64 df_nodal_w(df64 rho, double u, df64 tau, double gp) {

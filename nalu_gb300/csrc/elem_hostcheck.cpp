@@ -124,6 +124,21 @@ void hc_mdot_df(const double* xin, const double* rho, const double* u, const dou
   });
 }
 
+// the per-node pass of the df64 continuity kernels on n values: w = rho u +
+// tau gp as a pair (hi, lo) per value, and whether every input was inside the
+// pairs' range (the condition the device pass flags)
+int hc_nodal_w(int64_t n, const double* rho, const double* u, double tau, const double* gp, float* hi, float* lo) {
+  int ok = 1;
+  const df64 t = df_split_input(tau);
+  for (int64_t i = 0; i < n; ++i) {
+    const df64 w = df_nodal_w(df_split_input(rho[i]), u[i], t, gp[i]);
+    hi[i] = w.hi;
+    lo[i] = w.lo;
+    ok &= df_split_in_range(rho[i]) && df_split_in_range(u[i]) && df_split_in_range(gp[i]) ? 1 : 0;
+  }
+  return ok && df_split_in_range(tau);
+}
+
 void hc_continuity_df(const double* xin, const double* u, const double* rho, const double* p,
                       const double* gp, double tau, int smdot, int spois, int reduced, double* lhs,
                       double* rhs) {

@@ -53,6 +53,8 @@ def elemcheck():
     L.hc_continuity_df.argtypes = [P] * 5 + [ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P]
     L.hc_mdot.argtypes = [P] * 5 + [ctypes.c_double, ctypes.c_int, ctypes.c_int, P]
     L.hc_mdot_df.argtypes = [P] * 5 + [ctypes.c_double, ctypes.c_int, ctypes.c_int, P]
+    L.hc_nodal_w.argtypes = [ctypes.c_int64, P, P, ctypes.c_double, P, P, P]
+    L.hc_nodal_w.restype = ctypes.c_int
     return L
 
 

@@ -178,3 +178,28 @@ def test_df64_scale_invariance(elemcheck, oracle, scale):
             elemcheck.hc_mdot_df(P(cc), P(rho), P(np.ascontiguousarray(u)), P(p), P(np.ascontiguousarray(gp)),
                                  float(tau), sm, sp, P(m2))
             check_dense(m2[None], m1[None], what="mdot df64 x%g" % scale)
+
+
+def test_df64_nodal_input_combination(elemcheck):
+    """The per-node pass of the df64 continuity kernels: rho u + tau gp formed
+    from exact-to-2^-48 FP32-pair splits of the inputs by double-float
+    products and a sum, against FP64 on 200 K random values of magnitude
+    1e-20..1e20: |hi + lo - w| <= 2^-45 (|rho u| + |tau gp|).  Inputs the pairs
+    cannot hold (NaN, inf, |x| >= 2^127) are reported (the device pass raises
+    NALU_ERR_NONFINITE for them) and come out non-finite or clamped."""
+    rng = np.random.default_rng(12)
+    n = 200000
+    sc = 10.0 ** rng.uniform(-20, 20, n)
+    rho = rng.uniform(0.5, 2.0, n)
+    u, gp = rng.normal(size=n) * sc, rng.normal(size=n) * sc
+    tau = 0.37
+    hi, lo = np.zeros(n, np.float32), np.zeros(n, np.float32)
+    assert elemcheck.hc_nodal_w(n, P(rho), P(u), tau, P(gp), P(hi), P(lo)) == 1
+    w = hi.astype(np.float64) + lo.astype(np.float64)
+    err = np.abs(w - (rho * u + tau * gp)) / (np.abs(rho * u) + np.abs(tau * gp))
+    assert err.max() <= 2.0 ** -45, err.max()
+    for bad in (float("nan"), float("inf"), 1e300, 2.0 ** 127):
+        u2 = u.copy()
+        u2[5] = bad
+        assert elemcheck.hc_nodal_w(n, P(rho), P(u2), tau, P(gp), P(hi), P(lo)) == 0
+    assert elemcheck.hc_nodal_w(1, P(rho), P(np.array([2.0 ** 126])), tau, P(gp), P(hi), P(lo)) == 1
